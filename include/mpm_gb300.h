@@ -1,0 +1,178 @@
+/*
+ * mpm_gb300 -- GB300-native (sm_103a) explicit USL step of mpm-2d behind a C
+ * ABI.  Plain pointers and sizes only; every entry point returns an int
+ * status (MPMG_OK on success) and never exits the process.
+ *
+ * This is the flat interface the libmpm-compatible entry points of
+ * mpm_libmpm.h are built on.  One mpmg_ctx holds one simulation resident in
+ * the GPU's memory: particle state in structure-of-arrays form in the
+ * caller's original particle order, the background grid, and the scratch the
+ * step needs (sort buffers, per-element partial sums, solver vectors).
+ *
+ * Reference interfaces each call replaces (paths inside neocpp89/mpm-2d):
+ *   mpmg_create      mpm_init (libmpm/process_usl.c:68-280) + material_init
+ *                    (materialsrc/*.c) + bc_validate (bcsrc/*.c), with the
+ *                    driver's dt (src/main.c:742)
+ *   mpmg_step        the driver loop body (src/main.c:946-977):
+ *                    explicit_mpm_step_usl_threaded (process_usl.c:465-592)
+ *                    followed by time_varying_loads (loading.c:34-54)
+ *   mpmg_get_field   reads of job->particles[] / job->nodes[] (process.h:116-213)
+ *   mpmg_destroy     mpm_cleanup (process_usl.c:974-1004)
+ */
+#ifndef MPM_GB300_H
+#define MPM_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define MPMG_API __attribute__((visibility("default")))
+#else
+#define MPMG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Values 1..3 match libmpm/exitcodes.h's CXSparse codes where
+   the meaning carries over (a failed fluidity solve is EXIT_ERROR_CS_SOL). */
+enum mpmg_status {
+    MPMG_OK = 0,
+    MPMG_ERR_SOLVER = 2,          /* fluidity solve did not converge (EXIT_ERROR_CS_SOL) */
+    MPMG_ERR_INVALID = 16,        /* bad argument or configuration */
+    MPMG_ERR_CUDA = 17,           /* CUDA runtime error (no GPU, launch failure, ...) */
+    MPMG_ERR_NOMEM = 18,          /* device allocation failed */
+    MPMG_ERR_UNKNOWN_FIELD = 19,
+    MPMG_ERR_UNSUPPORTED = 20,    /* material or boundary condition not implemented */
+    MPMG_ERR_DEVICE = 21,         /* a kernel reported an internal error (status word) */
+    MPMG_ERR_SCRATCH_LIMIT = 22   /* size exceeds a fixed scratch capacity */
+};
+
+/* Material kinds: the reference plugins with a device implementation. */
+enum mpmg_material {
+    MPMG_ISOLIN = 0,              /* materialsrc/isolin.c */
+    MPMG_G_LOCAL_MU2 = 1,         /* materialsrc/g_local_mu2.c */
+    MPMG_G_NONLOCAL_MU2 = 2,      /* materialsrc/g_nonlocal_mu2.c */
+    MPMG_G_NONLOCAL = 3           /* materialsrc/g_nonlocal.c */
+};
+
+/* Boundary-condition kinds: the reference plugins with a device implementation. */
+enum mpmg_bc {
+    MPMG_BOX = 0,                 /* bcsrc/box.c */
+    MPMG_SQUARE_SILO = 1          /* bcsrc/square_silo.c */
+};
+
+enum mpmg_gravity {
+    MPMG_GRAVITY_REFERENCE_RAMP = 0,  /* loading.c: 0 on step 1, then -9.8 t/0.1 up to -9.8 */
+    MPMG_GRAVITY_CONSTANT = 1         /* mpmg_config.gravity from step 1 on */
+};
+
+/* Material parameter slots (mpmg_config.mp).  mpmg_default_params fills the
+   reference's compile-time constants for a material kind. */
+enum mpmg_mparam {
+    MPMG_MP_E = 0, MPMG_MP_NU, MPMG_MP_MU_S, MPMG_MP_MU_2, MPMG_MP_I0,
+    MPMG_MP_GRAINS_RHO, MPMG_MP_GRAINS_D, MPMG_MP_A, MPMG_MP_RHO_CRITICAL,
+    MPMG_MP_B, MPMG_MP_COHESION,
+    MPMG_MP_COUNT = 16
+};
+
+typedef struct mpmg_config {
+    int Nx, Ny;              /* grid nodes per row and per column (reference: N, N) */
+    double h;                /* element edge (reference: len / (N - 1)) */
+    double xmax, ymax;       /* element-map inside bounds (reference: 1.0, 1.0) */
+    double dt;
+    int material;            /* enum mpmg_material */
+    double mp[MPMG_MP_COUNT];
+    int bc;                  /* enum mpmg_bc */
+    double bcf[4];           /* box: x0, y0, width, height; silo: hole radius, open time, wall fraction */
+    int bci[4];              /* box: friction bits (1 x, 2 y) for left, bottom, right, top */
+    int gravity_mode;        /* enum mpmg_gravity */
+    double gravity;          /* constant mode: body force per unit mass along y */
+    int store_transients;    /* nonzero: keep x_tt, y_tt, strain rates and nodal
+                                momentum/force for read-back (parity tests) */
+    double solver_tol;       /* fluidity PCG relative residual (default 1e-10) */
+    int solver_maxit;        /* fluidity PCG iteration cap (default 20000) */
+    int device;              /* CUDA device ordinal */
+} mpmg_config;
+
+typedef struct mpmg_ctx mpmg_ctx;
+
+/* Fills mp[MPMG_MP_COUNT] with the reference's constants for a material. */
+MPMG_API int mpmg_default_params(int material, double *mp);
+
+/* Fills cfg with defaults (reference inside bounds, tolerances, device 0). */
+MPMG_API int mpmg_config_init(mpmg_config *cfg);
+
+/*
+ * Creates a simulation from host arrays of n particles: mass, volume,
+ * position, velocity and in-plane stress, the columns of the reference's
+ * particle file (src/reader.c:66-99).  The arrays are copied; the caller keeps
+ * them.  On success *out holds the context.
+ */
+MPMG_API int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double *v,
+                const double *x, const double *y, const double *vx, const double *vy,
+                const double *sxx, const double *sxy, const double *syy, mpmg_ctx **out);
+MPMG_API int mpmg_destroy(mpmg_ctx *ctx);
+
+/* Advances nsteps time steps (each: USL step + load update), asynchronously
+   on the context's stream.  Errors found on the device are reported by the
+   next mpmg_synchronize or read-back. */
+MPMG_API int mpmg_step(mpmg_ctx *ctx, int nsteps);
+MPMG_API int mpmg_synchronize(mpmg_ctx *ctx);
+
+/* Named host read-back / write of one field (particle fields in the caller's
+   particle order, node fields in node-number order).  Particle fields: x y v
+   v0 m vx vy ax ay bx by sxx sxy syy ux uy exx exy eyy wxy xl yl Txx Txy Tyx
+   Tyy Tzz state0..state10.  Node fields: node_m node_mx node_my node_fx
+   node_fy node_vx node_vy node_ax node_ay node_gf. */
+MPMG_API int mpmg_get_field(mpmg_ctx *ctx, const char *name, double *host_out);
+MPMG_API int mpmg_set_field(mpmg_ctx *ctx, const char *name, const double *host_in);
+
+/* Element of each particle (-1 outside) and active flags
+   (job->in_element / job->active, process.h:145-146). */
+MPMG_API int mpmg_get_map(mpmg_ctx *ctx, int *in_element, int *active);
+MPMG_API int mpmg_set_map(mpmg_ctx *ctx, const int *in_element, const int *active);
+
+/* The last step's cell sort: sorted keys (element, or num_elements for
+   inactive particles), the permutation (sorted position -> particle index)
+   and per-element start offsets (num_elements + 1 entries). */
+MPMG_API int mpmg_get_sort(mpmg_ctx *ctx, int *sorted_keys, int *perm, int *cell_start);
+
+MPMG_API int mpmg_get_time(mpmg_ctx *ctx, double *t, int *step_number);
+MPMG_API int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number);
+MPMG_API int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *num_elements);
+
+/* Runs only the material update on every active particle from the current
+   strain rates (the per-particle path of the reference's tests/test_material.c).
+   Local materials only. */
+MPMG_API int mpmg_material_only(mpmg_ctx *ctx);
+
+/* The context's CUDA stream (a cudaStream_t) for callers that time or order
+   work against it. */
+MPMG_API int mpmg_get_stream(mpmg_ctx *ctx, void **stream);
+
+/* Per-phase GPU timing with CUDA events on the context's stream.  When
+   enabled, mpmg_step records events around each phase; mpmg_phase_times
+   returns accumulated milliseconds and launch counts per phase and resets
+   them.  Phase names: see mpmg_phase_name. */
+MPMG_API int mpmg_enable_phase_timing(mpmg_ctx *ctx, int enable);
+MPMG_API int mpmg_phase_count(void);
+MPMG_API const char *mpmg_phase_name(int phase);
+MPMG_API int mpmg_phase_times(mpmg_ctx *ctx, double *ms, long *launches);
+
+/* Fluidity solve statistics of the last step (nonlocal materials). */
+MPMG_API int mpmg_last_solve(mpmg_ctx *ctx, int *iterations, double *rel_residual);
+
+/* Number of kernel launches issued by the library since the context was
+   created (or since the last reset). */
+MPMG_API int mpmg_launch_count(mpmg_ctx *ctx, long *launches, int reset);
+
+MPMG_API const char *mpmg_status_string(int status);
+/* Text of the last error on this thread (CUDA error text or argument check). */
+MPMG_API const char *mpmg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

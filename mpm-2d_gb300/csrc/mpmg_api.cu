@@ -1,0 +1,705 @@
+// C ABI of the mpm_gb300 library: context lifecycle, host field I/O, stepping,
+// timing and error reporting.  See include/mpm_gb300.h for the contract.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "mpmg_internal.cuh"
+
+namespace {
+thread_local char g_last_error[512] = "";
+
+const char *kPhaseNames[PH_COUNT] = {"keys", "sort", "p2g", "grid", "g2p", "fluidity"};
+
+template <typename T>
+int dalloc(T **p, size_t count)
+{
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        mpmg_set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+        return MPMG_ERR_NOMEM;
+    }
+    return MPMG_OK;
+}
+
+int upload(mpmg_ctx *ctx, double *dst, const double *src, size_t n)
+{
+    if (n == 0) return MPMG_OK;
+    MPMG_CHECK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    return MPMG_OK;
+}
+
+int fill_zero(mpmg_ctx *ctx, void *p, size_t bytes)
+{
+    if (p == nullptr || bytes == 0) return MPMG_OK;
+    MPMG_CHECK(cudaMemsetAsync(p, 0, bytes, ctx->stream));
+    return MPMG_OK;
+}
+
+// Which state slots each material keeps (the reference's #define maps).
+bool material_uses_state(int material, int k)
+{
+    switch (material) {
+    case MPMG_G_LOCAL_MU2:      // g_local_mu2.c:43-53 (gammap, gammadotp)
+        return k == 9 || k == 10;
+    case MPMG_G_NONLOCAL_MU2:   // g_nonlocal_mu2.c:49-57
+        return k == 0 || k == 3 || k == 4 || k == 5 || k == 6 || k == 9 || k == 10;
+    case MPMG_G_NONLOCAL:       // g_nonlocal.c:51-61
+        return k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
+    default:
+        return false;
+    }
+}
+
+int sync_status(mpmg_ctx *ctx)
+{
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    int st = 0;
+    MPMG_CHECK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    MPMG_CHECK(cudaMemcpy(&ctx->h_params, ctx->d_params, sizeof(StepParams), cudaMemcpyDeviceToHost));
+    if (st & MPMG_DEV_ERR_SPIN) {
+        mpmg_set_error("a grid-wide wait in the fluidity solver timed out");
+        return MPMG_ERR_DEVICE;
+    }
+    if (st & MPMG_DEV_ERR_BOUNDS) {
+        mpmg_set_error("a kernel found an index out of range");
+        return MPMG_ERR_DEVICE;
+    }
+    if (st & MPMG_DEV_ERR_SOLVER) {
+        mpmg_set_error("fluidity solve did not reach the relative residual %g in %d iterations",
+                       ctx->cfg.solver_tol, ctx->cfg.solver_maxit);
+        return MPMG_ERR_SOLVER;
+    }
+    return MPMG_OK;
+}
+
+struct FieldRef {
+    double *ptr;        // device array, or nullptr for an all-zero / computed field
+    size_t count;
+    int kind;           // 0 device array, 1 zeros, 2 constant by (gravity)
+};
+
+int find_field(mpmg_ctx *ctx, const char *name, FieldRef *f, bool for_write)
+{
+    f->ptr = nullptr;
+    f->count = ctx->np;
+    f->kind = 0;
+    struct { const char *n; double *p; } pf[] = {
+        {"x", ctx->x}, {"y", ctx->y}, {"v", ctx->v}, {"v0", ctx->v0}, {"m", ctx->m},
+        {"vx", ctx->vx}, {"vy", ctx->vy}, {"sxx", ctx->sxx}, {"sxy", ctx->sxy}, {"syy", ctx->syy},
+        {"ux", ctx->ux}, {"uy", ctx->uy}, {"Txx", ctx->sxx}, {"Txy", ctx->sxy}, {"Tyx", ctx->sxy},
+        {"Tyy", ctx->syy}, {"ax", ctx->ax}, {"ay", ctx->ay}, {"exx", ctx->exx}, {"exy", ctx->exy},
+        {"eyy", ctx->eyy}, {"wxy", ctx->wxy}, {"xl", ctx->xl}, {"yl", ctx->yl}, {"Tzz", ctx->Tzz}};
+    for (auto &e : pf) {
+        if (strcmp(name, e.n) == 0) {
+            if (e.p == nullptr) {
+                if (for_write) {
+                    mpmg_set_error("field '%s' is not kept by this configuration", name);
+                    return MPMG_ERR_UNKNOWN_FIELD;
+                }
+                f->kind = 1;
+            }
+            f->ptr = e.p;
+            return MPMG_OK;
+        }
+    }
+    if (strcmp(name, "bx") == 0) {
+        f->kind = 1;
+        return for_write ? MPMG_ERR_UNKNOWN_FIELD : MPMG_OK;
+    }
+    if (strcmp(name, "by") == 0) {
+        f->kind = 2;
+        return for_write ? MPMG_ERR_UNKNOWN_FIELD : MPMG_OK;
+    }
+    if (strncmp(name, "state", 5) == 0 && name[5] != 0) {
+        char *end = nullptr;
+        long k = strtol(name + 5, &end, 10);
+        if (*end == 0 && k >= 0 && k < MPMG_DEPVAR) {
+            f->ptr = ctx->state[k];
+            if (f->ptr == nullptr) {
+                if (for_write) {
+                    mpmg_set_error("state slot %ld is not used by this material", k);
+                    return MPMG_ERR_UNKNOWN_FIELD;
+                }
+                f->kind = 1;
+            }
+            return MPMG_OK;
+        }
+    }
+    f->count = ctx->nn;
+    struct { const char *n; double *p; } nf[] = {
+        {"node_m", ctx->node_m}, {"node_mx", ctx->node_mx}, {"node_my", ctx->node_my},
+        {"node_fx", ctx->node_fx}, {"node_fy", ctx->node_fy}, {"node_vx", ctx->node_vx},
+        {"node_vy", ctx->node_vy}, {"node_ax", ctx->node_ax}, {"node_ay", ctx->node_ay},
+        {"node_gf", ctx->node_gf}};
+    for (auto &e : nf) {
+        if (strcmp(name, e.n) == 0) {
+            if (e.p == nullptr) {
+                if (for_write) {
+                    mpmg_set_error("field '%s' is not kept by this configuration", name);
+                    return MPMG_ERR_UNKNOWN_FIELD;
+                }
+                f->kind = 1;
+            }
+            f->ptr = e.p;
+            return MPMG_OK;
+        }
+    }
+    mpmg_set_error("unknown field '%s'", name);
+    return MPMG_ERR_UNKNOWN_FIELD;
+}
+
+// The body force the reference's time_varying_loads leaves in by after the
+// last completed step (loading.c:34-54), or initial_loads before any step.
+double current_by(const mpmg_ctx *ctx)
+{
+    const StepParams &p = ctx->h_params;
+    if (ctx->cfg.gravity_mode == MPMG_GRAVITY_CONSTANT) return ctx->cfg.gravity;
+    if (p.step_count == 0) return 0.0;
+    if ((0.1 + p.step_start_time) > p.t) return -9.8 * ((p.t - p.step_start_time) / 0.1);
+    return -9.8;
+}
+
+}  // namespace
+
+void mpmg_set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+int mpmg_cuda_status(cudaError_t e, const char *what)
+{
+    mpmg_set_error("%s: %s", what, cudaGetErrorString(e));
+    return (e == cudaErrorMemoryAllocation) ? MPMG_ERR_NOMEM : MPMG_ERR_CUDA;
+}
+
+void mpmg_phase_begin(mpmg_ctx *ctx, int phase)
+{
+    if (ctx->timing) cudaEventRecord(ctx->ev[2 * phase], ctx->stream);
+}
+
+void mpmg_phase_end(mpmg_ctx *ctx, int phase)
+{
+    if (ctx->timing) cudaEventRecord(ctx->ev[2 * phase + 1], ctx->stream);
+}
+
+extern "C" {
+
+const char *mpmg_last_error(void)
+{
+    return g_last_error;
+}
+
+const char *mpmg_status_string(int status)
+{
+    switch (status) {
+    case MPMG_OK: return "ok";
+    case MPMG_ERR_SOLVER: return "fluidity solve did not converge";
+    case MPMG_ERR_INVALID: return "invalid argument";
+    case MPMG_ERR_CUDA: return "CUDA error";
+    case MPMG_ERR_NOMEM: return "out of device memory";
+    case MPMG_ERR_UNKNOWN_FIELD: return "unknown field";
+    case MPMG_ERR_UNSUPPORTED: return "unsupported material or boundary condition";
+    case MPMG_ERR_DEVICE: return "device-side error";
+    case MPMG_ERR_SCRATCH_LIMIT: return "size exceeds the fixed scratch capacity";
+    default: return "unknown status";
+    }
+}
+
+int mpmg_default_params(int material, double *mp)
+{
+    if (mp == nullptr) return MPMG_ERR_INVALID;
+    for (int i = 0; i < MPMG_MP_COUNT; i++) mp[i] = 0.0;
+    mp[MPMG_MP_E] = 1e6;
+    mp[MPMG_MP_NU] = 0.3;
+    switch (material) {
+    case MPMG_ISOLIN:
+        return MPMG_OK;
+    case MPMG_G_LOCAL_MU2:      // g_local_mu2.c:30-41
+        mp[MPMG_MP_MU_S] = 0.3819;
+        mp[MPMG_MP_GRAINS_RHO] = 2450;
+        mp[MPMG_MP_MU_2] = 0.6435;
+        mp[MPMG_MP_I0] = 0.278 / 1.0;
+        mp[MPMG_MP_GRAINS_D] = 0.001 * 5;
+        mp[MPMG_MP_RHO_CRITICAL] = 1485.0f;
+        return MPMG_OK;
+    case MPMG_G_NONLOCAL_MU2:   // g_nonlocal_mu2.c:32-47
+        mp[MPMG_MP_MU_S] = 0.3819;
+        mp[MPMG_MP_GRAINS_RHO] = 2450;
+        mp[MPMG_MP_A] = 0.48;
+        mp[MPMG_MP_MU_2] = 0.6435;
+        mp[MPMG_MP_I0] = 0.278;
+        mp[MPMG_MP_GRAINS_D] = 0.005;
+        mp[MPMG_MP_RHO_CRITICAL] = 1485.0;
+        return MPMG_OK;
+    case MPMG_G_NONLOCAL:       // g_nonlocal.c:31-48
+        mp[MPMG_MP_E] = 1e8;
+        mp[MPMG_MP_NU] = 0.3;
+        mp[MPMG_MP_MU_S] = 0.3819;
+        mp[MPMG_MP_GRAINS_RHO] = 2450;
+        mp[MPMG_MP_B] = 0.9377 * 20;
+        mp[MPMG_MP_A] = 0.48;
+        mp[MPMG_MP_GRAINS_D] = 0.01 * 5;
+        mp[MPMG_MP_COHESION] = 1e-2;
+        return MPMG_OK;
+    default:
+        mpmg_set_error("unknown material kind %d", material);
+        return MPMG_ERR_UNSUPPORTED;
+    }
+}
+
+int mpmg_config_init(mpmg_config *cfg)
+{
+    if (cfg == nullptr) return MPMG_ERR_INVALID;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->xmax = 1.0;
+    cfg->ymax = 1.0;
+    cfg->solver_tol = 1e-10;
+    cfg->solver_maxit = 20000;
+    mpmg_default_params(MPMG_ISOLIN, cfg->mp);
+    return MPMG_OK;
+}
+
+int mpmg_destroy(mpmg_ctx *ctx)
+{
+    if (ctx == nullptr) return MPMG_OK;
+    cudaSetDevice(ctx->dev);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    double **dp[] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->m, &ctx->v, &ctx->v0, &ctx->sxx,
+                     &ctx->sxy, &ctx->syy, &ctx->ux, &ctx->uy, &ctx->Tzz, &ctx->ax, &ctx->ay,
+                     &ctx->exx, &ctx->exy, &ctx->eyy, &ctx->wxy, &ctx->xl, &ctx->yl, &ctx->cell_sums,
+                     &ctx->node_m, &ctx->node_ax, &ctx->node_ay, &ctx->node_vx, &ctx->node_vy,
+                     &ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy, &ctx->node_gf};
+    for (double **p : dp) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    for (int k = 0; k < MPMG_DEPVAR; k++) cudaFree(ctx->state[k]);
+    cudaFree(ctx->in_element);
+    cudaFree(ctx->active);
+    cudaFree(ctx->keys);
+    cudaFree(ctx->vals);
+    cudaFree(ctx->sorted_keys);
+    cudaFree(ctx->perm);
+    cudaFree(ctx->cell_start);
+    cudaFree(ctx->d_params);
+    cudaFree(ctx->d_status);
+    mpmg_sort_free(ctx);
+    mpmg_nonlocal_free(ctx);
+    for (int k = 0; k < 2 * PH_COUNT; k++)
+        if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MPMG_OK;
+}
+
+int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double *v, const double *x,
+                const double *y, const double *vx, const double *vy, const double *sxx,
+                const double *sxy, const double *syy, mpmg_ctx **out)
+{
+    if (out == nullptr || cfg == nullptr) {
+        mpmg_set_error("null configuration or output pointer");
+        return MPMG_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (cfg->Nx < 2 || cfg->Ny < 2 || !(cfg->h > 0) || !(cfg->dt > 0) || !(cfg->xmax > 0) ||
+        !(cfg->ymax > 0)) {
+        mpmg_set_error("grid needs Nx, Ny >= 2 and positive h, dt, xmax, ymax");
+        return MPMG_ERR_INVALID;
+    }
+    if ((double)(cfg->Nx - 1) * (double)(cfg->Ny - 1) >= 2147483647.0 || n >= 2147483647u) {
+        mpmg_set_error("grid or particle count exceeds 32-bit indexing");
+        return MPMG_ERR_INVALID;
+    }
+    if (cfg->material < MPMG_ISOLIN || cfg->material > MPMG_G_NONLOCAL) {
+        mpmg_set_error("unknown material kind %d", cfg->material);
+        return MPMG_ERR_UNSUPPORTED;
+    }
+    if (cfg->bc != MPMG_BOX && cfg->bc != MPMG_SQUARE_SILO) {
+        mpmg_set_error("unknown boundary-condition kind %d", cfg->bc);
+        return MPMG_ERR_UNSUPPORTED;
+    }
+    if (n > 0 && (!m || !v || !x || !y || !vx || !vy || !sxx || !sxy || !syy)) {
+        mpmg_set_error("null particle array");
+        return MPMG_ERR_INVALID;
+    }
+    if (cfg->bc == MPMG_BOX) {
+        // box.c:42-96 bc_validate
+        double x0 = cfg->bcf[0], y0 = cfg->bcf[1], w = cfg->bcf[2], hh = cfg->bcf[3];
+        if (x0 < 0 || y0 < 0 || x0 > 1.0 || y0 > 1.0 || w < 0 || hh < 0 || x0 + w > 1.0 || y0 + hh > 1.0) {
+            mpmg_set_error("box must lie inside the unit fractions of the grid");
+            return MPMG_ERR_INVALID;
+        }
+    }
+    int ndev = 0;
+    cudaError_t de = cudaGetDeviceCount(&ndev);
+    if (de != cudaSuccess || ndev <= cfg->device || cfg->device < 0) {
+        mpmg_set_error("no CUDA device %d available (%s)", cfg->device,
+                       de != cudaSuccess ? cudaGetErrorString(de) : "device count too small");
+        return MPMG_ERR_CUDA;
+    }
+
+    mpmg_ctx *ctx = new (std::nothrow) mpmg_ctx();
+    if (ctx == nullptr) return MPMG_ERR_NOMEM;
+    ctx->cfg = *cfg;
+    if (!(ctx->cfg.solver_tol > 0)) ctx->cfg.solver_tol = 1e-10;
+    if (ctx->cfg.solver_maxit <= 0) ctx->cfg.solver_maxit = 20000;
+    ctx->dev = cfg->device;
+    ctx->np = n;
+    ctx->Ex = cfg->Nx - 1;
+    ctx->Ey = cfg->Ny - 1;
+    ctx->nn = (size_t)cfg->Nx * (size_t)cfg->Ny;
+    ctx->ne = (size_t)ctx->Ex * (size_t)ctx->Ey;
+    ctx->inv_h = 1.0 / cfg->h;
+    int bits = 1;
+    while (((size_t)1 << bits) <= ctx->ne) bits++;
+    ctx->key_bits = bits;
+
+    // material_init (isolin.c:31-59 / g_local_mu2.c / g_nonlocal_mu2.c / g_nonlocal.c:34-35)
+    double E = cfg->mp[MPMG_MP_E], nu = cfg->mp[MPMG_MP_NU];
+    ctx->G = E / (2.0 * (1.0 + nu));
+    ctx->K = E / (3.0 * (1.0 - 2 * nu));
+    ctx->lambda = ctx->K - 2.0 * ctx->G / 3.0;
+
+    int rc;
+#define TRY(call)                        \
+    do {                                 \
+        rc = (call);                     \
+        if (rc != MPMG_OK) goto fail;    \
+    } while (0)
+
+    if (cudaSetDevice(ctx->dev) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        mpmg_set_error("cannot open CUDA device %d", ctx->dev);
+        rc = MPMG_ERR_CUDA;
+        goto fail;
+    }
+    for (int k = 0; k < 2 * PH_COUNT; k++) {
+        if (cudaEventCreate(&ctx->ev[k]) != cudaSuccess) {
+            rc = MPMG_ERR_CUDA;
+            goto fail;
+        }
+    }
+    {
+        const bool transients = cfg->store_transients != 0;
+        const bool nonlocal = cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL;
+        double **always[] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->m, &ctx->v, &ctx->v0,
+                             &ctx->sxx, &ctx->sxy, &ctx->syy, &ctx->ux, &ctx->uy};
+        for (double **p : always) TRY(dalloc(p, n));
+        if (cfg->material == MPMG_G_LOCAL_MU2) TRY(dalloc(&ctx->Tzz, n));
+        for (int k = 0; k < MPMG_DEPVAR; k++)
+            if (material_uses_state(cfg->material, k)) TRY(dalloc(&ctx->state[k], n));
+        if (transients) {
+            TRY(dalloc(&ctx->ax, n));
+            TRY(dalloc(&ctx->ay, n));
+        }
+        if (transients || nonlocal) {
+            double **sr[] = {&ctx->exx, &ctx->exy, &ctx->eyy, &ctx->wxy};
+            for (double **p : sr) TRY(dalloc(p, n));
+        }
+        if (transients || nonlocal) {
+            TRY(dalloc(&ctx->xl, n));
+            TRY(dalloc(&ctx->yl, n));
+        }
+        TRY(dalloc(&ctx->in_element, n));
+        TRY(dalloc(&ctx->active, n));
+        TRY(dalloc(&ctx->keys, n));
+        TRY(dalloc(&ctx->vals, n));
+        TRY(dalloc(&ctx->sorted_keys, n));
+        TRY(dalloc(&ctx->perm, n));
+        TRY(dalloc(&ctx->cell_start, ctx->ne + 1));
+        TRY(dalloc(&ctx->cell_sums, 20 * ctx->ne));
+        double **nodes[] = {&ctx->node_m, &ctx->node_ax, &ctx->node_ay, &ctx->node_vx, &ctx->node_vy,
+                            &ctx->node_gf};
+        for (double **p : nodes) TRY(dalloc(p, ctx->nn));
+        if (transients) {
+            double **tn[] = {&ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy};
+            for (double **p : tn) TRY(dalloc(p, ctx->nn));
+        }
+        TRY(dalloc(&ctx->d_params, 1));
+        TRY(dalloc(&ctx->d_status, 1));
+        TRY(mpmg_sort_init(ctx));
+        if (nonlocal) TRY(mpmg_nonlocal_init(ctx));
+
+        // mpm_init copies (process_usl.c:88-126) and material_init.
+        TRY(upload(ctx, ctx->m, m, n));
+        TRY(upload(ctx, ctx->v, v, n));
+        TRY(upload(ctx, ctx->v0, v, n));
+        TRY(upload(ctx, ctx->x, x, n));
+        TRY(upload(ctx, ctx->y, y, n));
+        TRY(upload(ctx, ctx->vx, vx, n));
+        TRY(upload(ctx, ctx->vy, vy, n));
+        TRY(upload(ctx, ctx->sxx, sxx, n));
+        TRY(upload(ctx, ctx->sxy, sxy, n));
+        TRY(upload(ctx, ctx->syy, syy, n));
+        TRY(fill_zero(ctx, ctx->ux, n * sizeof(double)));
+        TRY(fill_zero(ctx, ctx->uy, n * sizeof(double)));
+        TRY(fill_zero(ctx, ctx->Tzz, n * sizeof(double)));
+        for (int k = 0; k < MPMG_DEPVAR; k++) TRY(fill_zero(ctx, ctx->state[k], n * sizeof(double)));
+        double **zero_p[] = {&ctx->ax, &ctx->ay, &ctx->exx, &ctx->exy, &ctx->eyy, &ctx->wxy, &ctx->xl, &ctx->yl};
+        for (double **p : zero_p) TRY(fill_zero(ctx, *p, n * sizeof(double)));
+        double **zero_n[] = {&ctx->node_m, &ctx->node_ax, &ctx->node_ay, &ctx->node_vx, &ctx->node_vy,
+                             &ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy, &ctx->node_gf};
+        for (double **p : zero_n) TRY(fill_zero(ctx, *p, ctx->nn * sizeof(double)));
+        TRY(fill_zero(ctx, ctx->cell_start, (ctx->ne + 1) * sizeof(int)));
+        TRY(fill_zero(ctx, ctx->d_status, sizeof(int)));
+        StepParams p0 = {};
+        ctx->h_params = p0;
+        MPMG_CHECK(cudaMemcpyAsync(ctx->d_params, &ctx->h_params, sizeof(StepParams),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+
+        // Initial element map (process_usl.c:236-244) on the host copy of x, y.
+        int *emap = new (std::nothrow) int[n > 0 ? n : 1];
+        int *act = new (std::nothrow) int[n > 0 ? n : 1];
+        if (emap == nullptr || act == nullptr) {
+            delete[] emap;
+            delete[] act;
+            rc = MPMG_ERR_NOMEM;
+            goto fail;
+        }
+        for (size_t i = 0; i < n; i++) {
+            double xp = x[i], yp = y[i];
+            int e = -1;
+            if (xp < cfg->xmax && xp >= 0.0 && yp < cfg->ymax && yp >= 0.0) {
+                double fx = floor(xp / cfg->h), fy = floor(yp / cfg->h);
+                if (fx < (double)ctx->Ex && fy < (double)ctx->Ey) e = (int)(fx + fy * (double)ctx->Ex);
+            }
+            emap[i] = e;
+            act[i] = e < 0 ? 0 : 1;
+        }
+        cudaError_t ce = cudaMemcpy(ctx->in_element, emap, n * sizeof(int), cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess) ce = cudaMemcpy(ctx->active, act, n * sizeof(int), cudaMemcpyHostToDevice);
+        delete[] emap;
+        delete[] act;
+        if (ce != cudaSuccess) {
+            rc = mpmg_cuda_status(ce, "initial element map upload");
+            goto fail;
+        }
+        rc = sync_status(ctx);
+        if (rc != MPMG_OK) goto fail;
+    }
+#undef TRY
+    *out = ctx;
+    return MPMG_OK;
+fail:
+    mpmg_destroy(ctx);
+    return rc;
+}
+
+int mpmg_step(mpmg_ctx *ctx, int nsteps)
+{
+    if (ctx == nullptr || nsteps < 0) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    for (int k = 0; k < nsteps; k++) {
+        int rc = mpmg_launch_step(ctx);
+        if (rc != MPMG_OK) return rc;
+        if (ctx->timing) {
+            MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+            const bool nonlocal = ctx->cfg.material == MPMG_G_NONLOCAL_MU2 || ctx->cfg.material == MPMG_G_NONLOCAL;
+            for (int ph = 0; ph < PH_COUNT; ph++) {
+                if (ph == PH_FLUIDITY && !nonlocal) continue;
+                float ms = 0;
+                MPMG_CHECK(cudaEventElapsedTime(&ms, ctx->ev[2 * ph], ctx->ev[2 * ph + 1]));
+                ctx->phase_ms[ph] += ms;
+                ctx->phase_launches[ph] += 1;
+            }
+        }
+    }
+    return MPMG_OK;
+}
+
+int mpmg_synchronize(mpmg_ctx *ctx)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    return sync_status(ctx);
+}
+
+int mpmg_get_field(mpmg_ctx *ctx, const char *name, double *host_out)
+{
+    if (ctx == nullptr || name == nullptr || host_out == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    FieldRef f;
+    int rc = find_field(ctx, name, &f, false);
+    if (rc != MPMG_OK) return rc;
+    rc = sync_status(ctx);
+    if (rc != MPMG_OK && rc != MPMG_ERR_SOLVER) return rc;
+    if (f.kind == 1) {
+        for (size_t i = 0; i < f.count; i++) host_out[i] = 0.0;
+    } else if (f.kind == 2) {
+        double by = current_by(ctx);
+        for (size_t i = 0; i < f.count; i++) host_out[i] = by;
+    } else if (f.count > 0) {
+        MPMG_CHECK(cudaMemcpy(host_out, f.ptr, f.count * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return MPMG_OK;
+}
+
+int mpmg_set_field(mpmg_ctx *ctx, const char *name, const double *host_in)
+{
+    if (ctx == nullptr || name == nullptr || host_in == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    FieldRef f;
+    int rc = find_field(ctx, name, &f, true);
+    if (rc != MPMG_OK) return rc;
+    if (f.count > 0)
+        MPMG_CHECK(cudaMemcpyAsync(f.ptr, host_in, f.count * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    return MPMG_OK;
+}
+
+int mpmg_get_map(mpmg_ctx *ctx, int *in_element, int *active)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (in_element && ctx->np)
+        MPMG_CHECK(cudaMemcpy(in_element, ctx->in_element, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+    if (active && ctx->np)
+        MPMG_CHECK(cudaMemcpy(active, ctx->active, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+    return MPMG_OK;
+}
+
+int mpmg_set_map(mpmg_ctx *ctx, const int *in_element, const int *active)
+{
+    if (ctx == nullptr || in_element == nullptr || active == nullptr) return MPMG_ERR_INVALID;
+    for (size_t i = 0; i < ctx->np; i++) {
+        if (active[i] && (in_element[i] < 0 || (size_t)in_element[i] >= ctx->ne)) {
+            mpmg_set_error("active particle %zu has element %d outside the grid", i, in_element[i]);
+            return MPMG_ERR_INVALID;
+        }
+    }
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->np) {
+        MPMG_CHECK(cudaMemcpy(ctx->in_element, in_element, ctx->np * sizeof(int), cudaMemcpyHostToDevice));
+        MPMG_CHECK(cudaMemcpy(ctx->active, active, ctx->np * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    return MPMG_OK;
+}
+
+int mpmg_get_sort(mpmg_ctx *ctx, int *sorted_keys, int *perm, int *cell_start)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (sorted_keys && ctx->np)
+        MPMG_CHECK(cudaMemcpy(sorted_keys, ctx->sorted_keys, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+    if (perm && ctx->np)
+        MPMG_CHECK(cudaMemcpy(perm, ctx->perm, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+    if (cell_start)
+        MPMG_CHECK(cudaMemcpy(cell_start, ctx->cell_start, (ctx->ne + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    return MPMG_OK;
+}
+
+int mpmg_get_time(mpmg_ctx *ctx, double *t, int *step_number)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    int rc = sync_status(ctx);
+    if (rc != MPMG_OK && rc != MPMG_ERR_SOLVER) return rc;
+    if (t) *t = ctx->h_params.t;
+    if (step_number) *step_number = (int)ctx->h_params.step_count;
+    return MPMG_OK;
+}
+
+int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number)
+{
+    if (ctx == nullptr || step_number < 0) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    MPMG_CHECK(cudaMemcpy(&ctx->h_params, ctx->d_params, sizeof(StepParams), cudaMemcpyDeviceToHost));
+    ctx->h_params.t = t;
+    ctx->h_params.step_count = step_number;
+    MPMG_CHECK(cudaMemcpy(ctx->d_params, &ctx->h_params, sizeof(StepParams), cudaMemcpyHostToDevice));
+    return MPMG_OK;
+}
+
+int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *num_elements)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    if (num_particles) *num_particles = ctx->np;
+    if (num_nodes) *num_nodes = ctx->nn;
+    if (num_elements) *num_elements = ctx->ne;
+    return MPMG_OK;
+}
+
+int mpmg_material_only(mpmg_ctx *ctx)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    if (ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2) {
+        mpmg_set_error("material-only update is defined for local materials");
+        return MPMG_ERR_UNSUPPORTED;
+    }
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    int rc = mpmg_launch_material_only(ctx);
+    if (rc != MPMG_OK) return rc;
+    return sync_status(ctx);
+}
+
+int mpmg_get_stream(mpmg_ctx *ctx, void **stream)
+{
+    if (ctx == nullptr || stream == nullptr) return MPMG_ERR_INVALID;
+    *stream = (void *)ctx->stream;
+    return MPMG_OK;
+}
+
+int mpmg_enable_phase_timing(mpmg_ctx *ctx, int enable)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    ctx->timing = enable ? 1 : 0;
+    for (int k = 0; k < PH_COUNT; k++) {
+        ctx->phase_ms[k] = 0;
+        ctx->phase_launches[k] = 0;
+    }
+    return MPMG_OK;
+}
+
+int mpmg_phase_count(void)
+{
+    return PH_COUNT;
+}
+
+const char *mpmg_phase_name(int phase)
+{
+    return (phase >= 0 && phase < PH_COUNT) ? kPhaseNames[phase] : "";
+}
+
+int mpmg_phase_times(mpmg_ctx *ctx, double *ms, long *launches)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    for (int k = 0; k < PH_COUNT; k++) {
+        if (ms) ms[k] = ctx->phase_ms[k];
+        if (launches) launches[k] = ctx->phase_launches[k];
+        ctx->phase_ms[k] = 0;
+        ctx->phase_launches[k] = 0;
+    }
+    return MPMG_OK;
+}
+
+int mpmg_last_solve(mpmg_ctx *ctx, int *iterations, double *rel_residual)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    int rc = sync_status(ctx);
+    if (iterations) *iterations = ctx->h_params.solve_iters;
+    if (rel_residual) *rel_residual = ctx->h_params.solve_rel_resid;
+    return rc;
+}
+
+int mpmg_launch_count(mpmg_ctx *ctx, long *launches, int reset)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    if (launches) *launches = ctx->launches;
+    if (reset) ctx->launches = 0;
+    return MPMG_OK;
+}
+
+}  // extern "C"

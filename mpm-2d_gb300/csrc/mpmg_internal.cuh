@@ -1,0 +1,200 @@
+// Internal declarations of the mpm_gb300 library: the device context, the
+// per-step parameter block that lives in device memory, and small device
+// helpers shared by the kernels.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/mpm_gb300.h"
+
+#define MPMG_TOL 1e-10          // process_usl.c:25
+#define MPMG_NCOLORS 4
+#define MPMG_DEPVAR 11          // particle.h:13
+
+// Device status word bits (ctx->d_status); any nonzero value fails the step.
+#define MPMG_DEV_ERR_SOLVER 0x1
+#define MPMG_DEV_ERR_BOUNDS 0x2
+#define MPMG_DEV_ERR_SPIN 0x4
+
+// Step parameters updated on the device so that consecutive steps need no
+// host round trip (and can be captured in a CUDA graph).
+struct StepParams {
+    double t;               // simulation time at the start of the current step
+    double step_start_time; // job->step_start_time (0)
+    double gravity;         // body force per unit mass along y used by this step's P2G
+    long long step_count;   // completed steps
+    // fluidity solve bookkeeping
+    int solve_iters;
+    int solve_converged;
+    double solve_rel_resid;
+};
+
+enum Phase {
+    PH_KEYS = 0,
+    PH_SORT,
+    PH_P2G,
+    PH_GRID,
+    PH_G2P,
+    PH_FLUIDITY,
+    PH_COUNT
+};
+
+struct SortScratch {
+    uint32_t *keys_alt;
+    uint32_t *vals_alt;
+    uint32_t *tile_hist;   // [256 digits][num tiles], digit-major
+    uint32_t *digit_total; // [256]
+    int num_tiles;
+    int capacity;          // particles
+};
+
+struct mpmg_ctx {
+    mpmg_config cfg;
+    int dev;
+    cudaStream_t stream;
+    size_t np, nn, ne;
+    int Ex, Ey;            // elements per row / column
+    double inv_h;
+    int key_bits;          // bits in an element key (including the inactive sentinel)
+
+    // Derived elastic constants (the material plugins' material_init).
+    double G, K, lambda;
+
+    // Particle state, structure of arrays, caller's particle order.
+    double *x, *y, *vx, *vy, *m, *v, *v0, *sxx, *sxy, *syy, *ux, *uy;
+    double *Tzz;                    // g_local_mu2 out-of-plane stress
+    double *state[MPMG_DEPVAR];     // allocated per material (NULL = always zero)
+    double *ax, *ay, *exx, *exy, *eyy, *wxy, *xl, *yl;  // transients (store_transients)
+    int *in_element;
+    int *active;
+
+    // Cell sort.
+    uint32_t *keys;        // element key per particle (num_elements for inactive)
+    uint32_t *vals;        // particle index
+    uint32_t *sorted_keys;
+    uint32_t *perm;
+    int *cell_start;       // num_elements + 1
+    SortScratch sort;
+
+    // P2G per-element corner sums: 20 values per element, value-major.
+    double *cell_sums;
+
+    // Grid.
+    double *node_m, *node_ax, *node_ay, *node_vx, *node_vy;
+    double *node_mx, *node_my, *node_fx, *node_fy;   // store_transients
+    double *node_gf;
+
+    // Nonlocal fluidity solve.
+    double *elem_k;        // 10 matrix entries per element, value-major
+    double *elem_f;        // 4 RHS entries per element, value-major
+    double *cg_x, *cg_r, *cg_p, *cg_q, *cg_dinv;     // per node
+    double *cg_partials;   // per-block partial sums
+    unsigned int *cg_barrier;  // grid barrier counter + generation
+    int cg_blocks;
+
+    StepParams *d_params;
+    StepParams h_params;   // host mirror, refreshed on read-back
+    int *d_status;
+
+    // Timing.
+    int timing;
+    cudaEvent_t ev[2 * PH_COUNT];
+    double phase_ms[PH_COUNT];
+    long phase_launches[PH_COUNT];
+    long launches;
+};
+
+// Error helpers (host).
+void mpmg_set_error(const char *fmt, ...);
+int mpmg_cuda_status(cudaError_t e, const char *what);
+
+#define MPMG_CHECK(call)                                          \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return mpmg_cuda_status(_e, #call); \
+    } while (0)
+
+// Kernel launch helpers implemented per translation unit.
+int mpmg_sort_init(mpmg_ctx *ctx);
+void mpmg_sort_free(mpmg_ctx *ctx);
+int mpmg_sort_keys(mpmg_ctx *ctx);                // keys/vals -> sorted_keys/perm
+int mpmg_launch_step(mpmg_ctx *ctx);             // one full step
+int mpmg_nonlocal_init(mpmg_ctx *ctx);
+void mpmg_nonlocal_free(mpmg_ctx *ctx);
+int mpmg_launch_fluidity(mpmg_ctx *ctx);         // nonlocal: assembly, solve, stress
+int mpmg_launch_material_only(mpmg_ctx *ctx);
+
+void mpmg_phase_begin(mpmg_ctx *ctx, int phase);
+void mpmg_phase_end(mpmg_ctx *ctx, int phase);
+
+// ---------------------------------------------------------------------------
+// Device helpers.
+
+// Element containing (xp, yp), bit-exact with WHICH_ELEMENT4
+// (process_usl.c:43-44): e = (int)(floor(x/h) + floor(y/h) * (Nx - 1)) when
+// 0 <= x < xmax and 0 <= y < ymax, else -1.  x * (1/h) replaces the division
+// unless the quotient is within a relative 2^-44 of an integer, where the
+// correctly rounded division decides (both products are within 2^-51
+// relative of x/h).  Out-of-range results (x/h rounding up to Nx-1 just below
+// xmax) are reported as -1.
+__device__ __forceinline__ int mpmg_which_element(double xp, double yp, double h, double inv_h,
+                                                  double xmax, double ymax, int Ex, int Ey)
+{
+    if (!(xp < xmax && xp >= 0.0 && yp < ymax && yp >= 0.0)) return -1;
+    double qx = xp * inv_h;
+    double fx = floor(qx);
+    double rx = qx - fx;
+    if (rx < 0x1p-44 * (qx + 1.0) || (1.0 - rx) < 0x1p-44 * (qx + 1.0)) fx = floor(__ddiv_rn(xp, h));
+    double qy = yp * inv_h;
+    double fy = floor(qy);
+    double ry = qy - fy;
+    if (ry < 0x1p-44 * (qy + 1.0) || (1.0 - ry) < 0x1p-44 * (qy + 1.0)) fy = floor(__ddiv_rn(yp, h));
+    if (fx >= (double)Ex || fy >= (double)Ey) return -1;
+    return (int)(fx + fy * (double)Ex);
+}
+
+// Local coordinates in the element with bottom-left node at (xn, yn), with
+// the reference's snap to +-1 within 1e-10 (particle.c:14-30).
+__device__ __forceinline__ double mpmg_local_coord(double xp, double xn, double inv_h)
+{
+    double xl = (xp - xn) * inv_h;
+    double sg = copysign(1.0, xl);
+    if ((sg * xl) > 1.0 && ((sg * xl) - 1.0) < MPMG_TOL) xl = sg;
+    return xl;
+}
+
+// Grid barrier over all blocks of a cooperative launch.  Every wait is
+// bounded: after `limit` polls the barrier sets MPMG_DEV_ERR_SPIN in *status
+// and returns false, and the caller leaves the kernel.
+__device__ __forceinline__ bool mpmg_grid_barrier(unsigned int *bar, unsigned int nblocks,
+                                                  int *status, long long limit)
+{
+    __syncthreads();
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        volatile unsigned int *gen = bar + 1;
+        unsigned int g = *gen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(bar, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long polls = 0;
+            while (*gen == g) {
+                if (++polls > limit || *(volatile int *)status != 0) {
+                    atomicOr(status, MPMG_DEV_ERR_SPIN);
+                    ok = false;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok && (*(volatile int *)status & MPMG_DEV_ERR_SPIN) == 0;
+}

@@ -1,0 +1,295 @@
+// Per-particle constitutive updates as device functions.  Each follows its
+// reference plugin line by line; products, sums and quotients use the _rn
+// intrinsics so that nvcc cannot fuse them into multiply-adds, which keeps
+// the results bit-identical to the reference compiled without contraction.
+#pragma once
+
+#include "mpmg_internal.cuh"
+
+namespace mat {
+
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dadd_rn(a, -b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+struct Elastic {
+    double G, K, lambda, dt;
+};
+
+// isolin calculate_stress_threaded, materialsrc/isolin.c:75-116.
+__device__ __forceinline__ void isolin(const Elastic &el, double exx, double exy, double eyy,
+                                       double wxy, double &sxx, double &sxy, double &syy)
+{
+    const double twoG = mul(2.0, el.G);
+    double trD = add(exx, eyy);
+    double dsjxx = add(mul(el.lambda, trD), mul(twoG, exx));
+    double dsjxy = mul(twoG, exy);
+    double dsjyy = add(mul(el.lambda, trD), mul(twoG, eyy));
+    double w2s = mul(mul(2.0, wxy), sxy);
+    dsjxx = add(dsjxx, w2s);
+    dsjxy = sub(dsjxy, mul(wxy, sub(sxx, syy)));
+    dsjyy = sub(dsjyy, w2s);
+    sxx = add(sxx, mul(el.dt, dsjxx));
+    sxy = add(sxy, mul(el.dt, dsjxy));
+    syy = add(syy, mul(el.dt, dsjyy));
+}
+
+// negative_root, g_local_mu2.c:90-99 (also g_nonlocal_mu2.c:226-235).
+__device__ __forceinline__ double negative_root(double a, double b, double c)
+{
+    double disc = __dsqrt_rn(sub(mul(b, b), mul(mul(4.0, a), c)));
+    if (b > 0) return dvd(sub(-b, disc), mul(2.0, a));
+    return dvd(mul(2.0, c), add(-b, disc));
+}
+
+struct Mu2Params {
+    double mu_s, mu_2, I0, grains_rho, grains_d, rho_critical, A;
+};
+
+// g_local_mu2 calculate_stress_threaded, g_local_mu2.c:165-310, written for
+// the plane-strain stress it keeps: T = [[Txx, Txy, 0], [Txy, Tyy, 0],
+// [0, 0, Tzz]] (the z-shear components stay zero and T stays symmetric
+// because L has no z entries).  The expressions are the tensor.c sums with
+// their zero terms removed, in the same order.
+__device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &mp, double m,
+                                            double v, double exx, double exy, double eyy,
+                                            double wxy, double &Txx, double &Txy, double &Tyy,
+                                            double &Tzz, double &gammap, double &gammadotp)
+{
+    const double G = el.G, dt = el.dt;
+    const double lambda = sub(el.K, dvd(mul(2.0, G), 3.0));
+    // L (:191-199), W = skw(L), D = sym(L) (tensor.c:330-384)
+    double Lxy = add(exy, wxy), Lyx = sub(exy, wxy);
+    double Wxy = mul(0.5, sub(Lxy, Lyx));
+    double Dxx = mul(0.5, add(exx, exx));
+    double Dxy = mul(0.5, add(Lxy, Lyx));
+    double Dyy = mul(0.5, add(eyy, eyy));
+    double trD = add(Dxx, Dyy);
+    // Jaumann term JS = W T - T W (:209-212)
+    double JSxx = add(mul(Wxy, Txy), -mul(Txy, -Wxy));
+    double JSxy = add(mul(Wxy, Tyy), -mul(Txx, Wxy));
+    double JSyy = add(mul(-Wxy, Txy), -mul(Txy, Wxy));
+    // trial stress (:215-222)
+    const double twoG = mul(2.0, G);
+    double lt = mul(lambda, trD);
+    double Txx_tr = add(mul(add(add(mul(Dxx, twoG), lt), JSxx), dt), Txx);
+    double Txy_tr = add(mul(add(mul(Dxy, twoG), JSxy), dt), Txy);
+    double Tyy_tr = add(mul(add(add(mul(Dyy, twoG), lt), JSyy), dt), Tyy);
+    double Tzz_tr = add(mul(add(mul(0.0, twoG), lt), dt), Tzz);
+    // decompose and contract (:225-228; tensor.c:205-224, :422-437)
+    double p_tr = dvd(add(add(Txx_tr, Tyy_tr), Tzz_tr), 3.0);
+    double T0xx = sub(Txx_tr, p_tr), T0xy = Txy_tr, T0yy = sub(Tyy_tr, p_tr), T0zz = sub(Tzz_tr, p_tr);
+    double tt = add(add(add(add(mul(T0xx, T0xx), mul(T0xy, T0xy)), mul(T0xy, T0xy)), mul(T0yy, T0yy)),
+                    mul(T0zz, T0zz));
+    double tau_tr = __dsqrt_rn(mul(0.5, tt));
+    p_tr = mul(p_tr, -1.0);
+
+    const bool density_flag = dvd(m, v) < mp.rho_critical;
+    double nup_tau;
+    if (density_flag || p_tr <= 0) {
+        nup_tau = 0;
+        Txx = 0; Txy = 0; Tyy = 0; Tzz = 0;
+    } else if (p_tr > 0) {
+        double tau_tau, scale_factor;
+        double S0 = mul(mp.mu_s, p_tr);
+        if (tau_tr <= S0) {
+            tau_tau = tau_tr;
+            scale_factor = 1.0;
+        } else {
+            double S2 = mul(mp.mu_2, p_tr);
+            double alpha = dvd(mul(mul(mul(G, mp.I0), dt), __dsqrt_rn(dvd(p_tr, mp.grains_rho))), mp.grains_d);
+            double B = -add(add(S2, tau_tr), alpha);
+            double H = add(mul(S2, tau_tr), mul(S0, alpha));
+            tau_tau = negative_root(1.0, B, H);
+            scale_factor = dvd(tau_tau, tau_tr);
+        }
+        nup_tau = dvd(dvd(sub(tau_tr, tau_tau), G), dt);
+        Txx = sub(mul(T0xx, scale_factor), p_tr);
+        Txy = mul(T0xy, scale_factor);
+        Tyy = sub(mul(T0yy, scale_factor), p_tr);
+        Tzz = sub(mul(T0zz, scale_factor), p_tr);
+    } else {
+        nup_tau = 0;   // NaN pressure: the reference prints 'u' and keeps T
+    }
+    gammap = add(gammap, mul(nup_tau, dt));
+    gammadotp = nup_tau;
+}
+
+// Trial Jaumann stress of g_nonlocal_mu2.c:166-186 (and :271-290), with
+// lambda = K - 2G/3 (the reference leaves it uninitialised at :154).
+__device__ __forceinline__ void nonlocal_mu2_trial(const Elastic &el, double exx, double exy,
+                                                   double eyy, double wxy, double sxx, double sxy,
+                                                   double syy, double &p_tr, double &t0xx,
+                                                   double &t0xy, double &t0yy, double &tau_tr)
+{
+    const double G = el.G, dt = el.dt;
+    const double lambda = sub(el.K, dvd(mul(2.0, G), 3.0));
+    const double twoG = mul(2.0, G);
+    double trD = add(exx, eyy);
+    double dsjxx = add(mul(lambda, trD), mul(twoG, exx));
+    double dsjxy = mul(twoG, exy);
+    double dsjyy = add(mul(lambda, trD), mul(twoG, eyy));
+    double w2s = mul(mul(2.0, wxy), sxy);
+    dsjxx = add(dsjxx, w2s);
+    dsjxy = sub(dsjxy, mul(wxy, sub(sxx, syy)));
+    dsjyy = sub(dsjyy, w2s);
+    double sxx_tr = add(sxx, mul(dt, dsjxx));
+    double sxy_tr = add(sxy, mul(dt, dsjxy));
+    double syy_tr = add(syy, mul(dt, dsjyy));
+    p_tr = mul(-0.5, add(sxx_tr, syy_tr));
+    t0xx = add(sxx_tr, p_tr);
+    t0xy = sxy_tr;
+    t0yy = add(syy_tr, p_tr);
+    tau_tr = __dsqrt_rn(mul(0.5, add(add(mul(t0xx, t0xx), mul(mul(2.0, t0xy), t0xy)), mul(t0yy, t0yy))));
+}
+
+// calculate_bulk_granular_fluidity, g_nonlocal_mu2.c:238-321, for one
+// particle: dense flag, local fluidity and the inverse squared cooperativity
+// length.
+__device__ __forceinline__ void nonlocal_mu2_bulk(const Elastic &el, const Mu2Params &mp, double m,
+                                                  double v, double exx, double exy, double eyy,
+                                                  double wxy, double sxx, double sxy, double syy,
+                                                  double &dense, double &gf_local, double &xisq_inv)
+{
+    const double G = el.G, dt = el.dt;
+    double p_tr, t0xx, t0xy, t0yy, tau_tr;
+    nonlocal_mu2_trial(el, exx, exy, eyy, wxy, sxx, sxy, syy, p_tr, t0xx, t0xy, t0yy, tau_tr);
+    dense = (dvd(m, v) < mp.rho_critical || p_tr < 0) ? 0.0 : 1.0;
+    if (dense == 0 || p_tr <= 0) {
+        gf_local = 0;
+        xisq_inv = 0;
+    } else if (p_tr > 0) {
+        double tau_tau, scale_factor;
+        double S0 = mul(mp.mu_s, p_tr);
+        if (tau_tr <= S0) {
+            tau_tau = tau_tr;
+            scale_factor = 1.0;
+        } else {
+            double S2 = mul(mp.mu_2, p_tr);
+            double alpha = dvd(mul(mul(mul(G, mp.I0), dt), __dsqrt_rn(dvd(p_tr, mp.grains_rho))), mp.grains_d);
+            double B = -add(add(S2, tau_tr), alpha);
+            double H = add(mul(S2, tau_tr), mul(S0, alpha));
+            tau_tau = negative_root(1.0, B, H);
+            scale_factor = dvd(tau_tau, tau_tr);
+        }
+        gf_local = mul(dvd(p_tr, mul(G, dt)), sub(dvd(1.0, scale_factor), 1.0));
+        xisq_inv = dvd(fabs(sub(dvd(tau_tau, p_tr), mp.mu_s)),
+                       mul(mul(mul(mp.A, mp.A), mp.grains_d), mp.grains_d));
+    } else {
+        gf_local = 0;
+        xisq_inv = 0;
+    }
+}
+
+// Stress update after the fluidity solve, g_nonlocal_mu2.c:160-218.
+__device__ __forceinline__ void nonlocal_mu2_stress(const Elastic &el, double dense, double gf,
+                                                    double exx, double exy, double eyy, double wxy,
+                                                    double &sxx, double &sxy, double &syy,
+                                                    double &gammap, double &gammadotp)
+{
+    const double G = el.G, dt = el.dt;
+    double p_tr, t0xx, t0xy, t0yy, tau_tr, nup_tau;
+    nonlocal_mu2_trial(el, exx, exy, eyy, wxy, sxx, sxy, syy, p_tr, t0xx, t0xy, t0yy, tau_tr);
+    if (dense == 0 || p_tr <= 0) {
+        nup_tau = 0;
+        sxx = 0; sxy = 0; syy = 0;
+    } else if (p_tr > 0) {
+        double scale_factor = dvd(p_tr, add(mul(mul(G, dt), gf), p_tr));
+        double tau_tau = mul(tau_tr, scale_factor);
+        nup_tau = dvd(dvd(sub(tau_tr, tau_tau), G), dt);
+        sxx = sub(mul(scale_factor, t0xx), p_tr);
+        sxy = mul(scale_factor, t0xy);
+        syy = sub(mul(scale_factor, t0yy), p_tr);
+    } else {
+        nup_tau = 0;
+    }
+    gammap = add(gammap, mul(nup_tau, dt));
+    gammadotp = nup_tau;
+}
+
+struct NonlocalParams {
+    double E, nu, mu_s, grains_rho, B, A, grains_d, cohesion;
+};
+
+// calculate_bulk_granular_fluidity, g_nonlocal.c:306-352, for one particle
+// (the reference applies it to every particle, active or not).
+__device__ __forceinline__ void nonlocal_bulk(const NonlocalParams &np, double sxx, double sxy,
+                                              double syy, double &eta, double &gf_bulk,
+                                              double &xisq_inv)
+{
+    const double p_cap = 1e-2;
+    double p_t = mul(-0.5, add(sxx, syy));
+    double a = add(sxx, p_t), b = sxy, c = add(syy, p_t);
+    double tau_t = __dsqrt_rn(mul(0.5, add(add(mul(a, a), mul(mul(2.0, b), b)), mul(c, c))));
+    if (p_t < p_cap) p_t = p_cap;
+    double S0 = mul(p_t, np.mu_s);
+    eta = mul(mul(np.B, np.grains_d), __dsqrt_rn(mul(p_t, np.grains_rho)));
+    xisq_inv = dvd(fabs(sub(dvd(tau_t, p_t), np.mu_s)),
+                   mul(mul(mul(np.grains_d, np.grains_d), np.A), np.A));
+    gf_bulk = (tau_t > S0) ? mul(dvd(p_t, eta), sub(1.0, dvd(S0, tau_t))) : 0.0;
+}
+
+// Explicit stress update of g_nonlocal.c:154-298 (every particle).
+__device__ __forceinline__ void nonlocal_stress(const NonlocalParams &np, double G, double dt,
+                                                double t, double gf, double exx, double exy,
+                                                double eyy, double wxy, double &sxx, double &sxy,
+                                                double &syy, double &gammap)
+{
+    const double EMOD = np.E, NUMOD = np.nu, c = np.cohesion;
+    const double cA = dvd(EMOD, sub(1.0, mul(NUMOD, NUMOD)));
+    const double cB = dvd(EMOD, mul(2.0, add(1.0, NUMOD)));
+    double p_t = mul(-0.5, add(sxx, syy));
+    double a = add(sxx, p_t), b = sxy, cc = add(syy, p_t);
+    double tau_t;
+    double dsjxx = mul(mul(dt, cA), add(exx, mul(NUMOD, eyy)));
+    double dsjxy = mul(mul(dt, cB), exy);
+    double dsjyy = mul(mul(dt, cA), add(eyy, mul(NUMOD, exx)));
+    double jw = mul(mul(mul(2.0, dt), wxy), sxy);
+    dsjxx = sub(dsjxx, jw);
+    dsjxy = add(dsjxy, mul(mul(dt, wxy), sub(sxx, syy)));
+    dsjyy = add(dsjyy, jw);
+    double p_tr = mul(-0.5, add(add(sxx, dsjxx), add(syy, dsjyy)));
+    if (p_tr < c) {
+        sxx = dvd(mul(0.5, c), np.mu_s);
+        sxy = 0;
+        syy = dvd(mul(0.5, c), np.mu_s);
+        return;
+    }
+    tau_t = __dsqrt_rn(mul(0.5, add(add(mul(a, a), mul(mul(2.0, b), b)), mul(cc, cc))));
+    const double r = __dsqrt_rn(0.5);
+    double Npxx = dvd(mul(r, a), tau_t);
+    double Npxy = dvd(mul(r, b), tau_t);
+    double Npyy = dvd(mul(r, cc), tau_t);
+    double dxx0 = mul(0.5, sub(exx, eyy)), dxy0 = exy, dyy0 = mul(0.5, sub(eyy, exx));
+    double gammadot = __dsqrt_rn(mul(2.0, add(add(mul(dxx0, dxx0), mul(mul(2.0, dxy0), dxy0)),
+                                              mul(dyy0, dyy0))));
+    double nup_tau, dpxx, dpxy, dpyy;
+    if (p_t > c && gf > 0) {
+        nup_tau = dvd(mul(gf, tau_t), p_t);
+        if (nup_tau < 0) nup_tau = 0;
+        if (nup_tau > gammadot) nup_tau = gammadot;
+        dpxx = mul(mul(r, nup_tau), Npxx);
+        dpxy = mul(mul(r, nup_tau), Npxy);
+        dpyy = mul(mul(r, nup_tau), Npyy);
+    } else {
+        nup_tau = 0; dpxx = 0; dpxy = 0; dpyy = 0;
+    }
+    if (t == 0) {
+        nup_tau = 0; dpxx = 0; dpxy = 0; dpyy = 0;
+    }
+    double exx_e = sub(exx, dpxx), eyy_e = sub(eyy, dpyy);
+    dsjxx = mul(mul(dt, cA), add(exx_e, mul(NUMOD, eyy_e)));
+    dsjxy = mul(mul(dt, cB), sub(exy, dpxy));
+    dsjyy = mul(mul(dt, cA), add(eyy_e, mul(NUMOD, exx_e)));
+    dsjxx = sub(dsjxx, jw);
+    dsjxy = add(dsjxy, mul(mul(dt, wxy), sub(sxx, syy)));
+    dsjyy = add(dsjyy, jw);
+    gammap = add(gammap, mul(nup_tau, dt));
+    sxx = add(sxx, dsjxx);
+    sxy = add(sxy, dsjxy);
+    syy = add(syy, dsjyy);
+    (void)G;
+}
+
+}  // namespace mat

@@ -1,0 +1,479 @@
+// Nonlocal granular fluidity on the GPU (reference: solve_diffusion_part and
+// calculate_stress of materialsrc/g_nonlocal_mu2.c:126-578, and the older
+// operator variant materialsrc/g_nonlocal.c:103-592).
+//
+// The reference assembles a sparse matrix from particle quadrature every step
+// and factorises it with CXSparse's LU.  Here the same operator
+//     K = sum_p v_p [ xi_p^-2 N N^T + grad N grad N^T ]  (+ 1e-10 I for mu2)
+// is kept as 10 unique entries of each element's symmetric 4x4 block plus a
+// 4-entry right-hand side, summed over the element's particle segment in
+// sorted order (one thread per element, fixed order).  The system is solved
+// matrix-free by Jacobi-preconditioned CG in one cooperative persistent
+// kernel: every node applies its four elements' rows, inner products are
+// per-block partial sums reduced in a fixed order (deterministic), and all
+// grid-wide waits are bounded.  The unknowns are the nodes with mass above
+// the reference's threshold (g_nonlocal_mu2.c:365-381: m > 0; g_nonlocal.c:
+// m > 1e-10); the initial guess is the previous step's nodal fluidity.
+#include "mpmg_internal.cuh"
+#include "mpmg_materials.cuh"
+
+namespace {
+
+constexpr int kSolveThreads = 256;
+constexpr long long kSpinLimit = 20000000;   // polls per grid barrier (~1 s)
+
+// Upper-triangle index of (a, b) in the 10-entry symmetric block.
+__device__ __forceinline__ int sym_index(int a, int b)
+{
+    if (a > b) { int t = a; a = b; b = t; }
+    // rows: (0,0..3)=0..3, (1,1..3)=4..6, (2,2..3)=7..8, (3,3)=9
+    const int row_start[4] = {0, 4, 7, 9};
+    return row_start[a] + (b - a);
+}
+
+__global__ void nonlocal_bulk_kernel(int n, mat::NonlocalParams np, const double *__restrict__ sxx,
+                                     const double *__restrict__ sxy, const double *__restrict__ syy,
+                                     double *__restrict__ eta, double *__restrict__ gf_bulk,
+                                     double *__restrict__ xisq)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double e, g, xi;
+    mat::nonlocal_bulk(np, sxx[i], sxy[i], syy[i], e, g, xi);
+    eta[i] = e;
+    gf_bulk[i] = g;
+    xisq[i] = xi;
+}
+
+// Element blocks and right-hand sides (g_nonlocal_mu2.c:418-507).
+__global__ void __launch_bounds__(128) assemble_kernel(
+    int ne, int Ex, double inv_h, int dense_only, const int *__restrict__ cell_start,
+    const uint32_t *__restrict__ perm, const double *__restrict__ xl, const double *__restrict__ yl,
+    const double *__restrict__ v, const double *__restrict__ dense, const double *__restrict__ gfl,
+    const double *__restrict__ xisq, double *__restrict__ elem_k, double *__restrict__ elem_f)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int k0 = cell_start[e], k1 = cell_start[e + 1];
+    if (k0 == k1) return;
+    double K[10], F[4];
+#pragma unroll
+    for (int k = 0; k < 10; k++) K[k] = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = 0;
+    for (int k = k0; k < k1; k++) {
+        const int i = (int)perm[k];
+        if (dense_only && dense[i] == 0) continue;
+        const double a = xl[i], b = yl[i];
+        const double ox = 1 - a, oy = 1 - b;
+        const double s[4] = {ox * oy, a * oy, a * b, ox * b};
+        const double gx[4] = {-oy * inv_h, oy * inv_h, b * inv_h, -b * inv_h};
+        const double gy[4] = {-ox * inv_h, -a * inv_h, a * inv_h, ox * inv_h};
+        const double vol = v[i], xi = xisq[i];
+        const double fv = vol * gfl[i] * xi;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            F[r] += fv * s[r];
+#pragma unroll
+            for (int c = r; c < 4; c++) {
+                K[sym_index(r, c)] += vol * (xi * s[r] * s[c] + (gx[r] * gx[c] + gy[r] * gy[c]));
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 10; k++) elem_k[(size_t)k * ne + e] = K[k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) elem_f[(size_t)k * ne + e] = F[k];
+    (void)Ex;
+}
+
+struct SolveArgs {
+    int Nx, Ny, Ex, Ey, ne;
+    double dof_tol;      // node is an unknown when m > dof_tol
+    double shift;        // diagonal shift (1e-10 for g_nonlocal_mu2)
+    double tol;          // relative residual
+    int maxit;
+    const double *node_m;
+    const int *cell_start;
+    const double *elem_k, *elem_f;
+    double *x, *r, *p, *q, *dinv;
+    double *partials;    // [4][nblocks]
+    unsigned int *barrier;
+    int *status;
+    StepParams *sp;
+};
+
+// Row of node (i, j) applied to vector u over its (up to) four elements, in
+// colour order.  Also returns the diagonal and right-hand side when asked.
+// u is written by other blocks between grid barriers, so it is read through
+// L2 (__ldcg), never from a possibly stale L1 line.
+__device__ __forceinline__ double apply_row(const SolveArgs &S, int i, int j, const double *u,
+                                            double *diag, double *rhs)
+{
+    double acc = 0, d = 0, f = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+        int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        if (ci < 0 || cj < 0 || ci >= S.Ex || cj >= S.Ey) continue;
+        int e = cj * S.Ex + ci;
+        if (S.cell_start[e] == S.cell_start[e + 1]) continue;
+        int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+        int n0 = cj * S.Nx + ci;
+        int nb[4] = {n0, n0 + 1, n0 + 1 + S.Nx, n0 + S.Nx};
+        if (u != nullptr) {
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc += S.elem_k[(size_t)sym_index(a, b) * S.ne + e] * __ldcg(u + nb[b]);
+        }
+        if (diag != nullptr) {
+            d += S.elem_k[(size_t)sym_index(a, a) * S.ne + e];
+            f += S.elem_f[(size_t)a * S.ne + e];
+        }
+    }
+    if (diag != nullptr) {
+        *diag = d;
+        *rhs = f;
+    }
+    return acc;
+}
+
+// Block-wide sum of up to three values, fixed tree; result valid in thread 0.
+__device__ __forceinline__ void block_sum3(double &a, double &b, double &c)
+{
+    __shared__ double sh[3][kSolveThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+        c += __shfl_down_sync(0xffffffffu, c, off);
+    }
+    if (lane == 0) {
+        sh[0][w] = a;
+        sh[1][w] = b;
+        sh[2][w] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a = 0; b = 0; c = 0;
+        for (int k = 0; k < kSolveThreads / 32; k++) {
+            a += sh[0][k];
+            b += sh[1][k];
+            c += sh[2][k];
+        }
+    }
+    __syncthreads();
+}
+
+// Sums slot s of the per-block partials in a fixed order; every block gets
+// the same value.
+__device__ __forceinline__ double grid_total(const double *partials, int slot, int nblocks)
+{
+    __shared__ double sh[kSolveThreads / 32];
+    __shared__ double result;
+    double acc = 0;
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) acc += __ldcg(partials + (size_t)slot * nblocks + k);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) sh[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < kSolveThreads / 32; k++) t += sh[k];
+        result = t;
+    }
+    __syncthreads();
+    double out = result;
+    __syncthreads();
+    return out;
+}
+
+__global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
+{
+    const int nn = S.Nx * S.Ny;
+    const int nblocks = gridDim.x;
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+
+    // Set-up: unknown mask via dinv, right-hand side in r, warm start in x.
+    for (int n = tid; n < nn; n += stride) {
+        const int i = n % S.Nx, j = n / S.Nx;
+        double d = 0, f = 0;
+        if (S.node_m[n] > S.dof_tol) {
+            apply_row(S, i, j, nullptr, &d, &f);
+            d += S.shift;
+        }
+        if (S.node_m[n] > S.dof_tol && d > 0) {
+            S.dinv[n] = 1.0 / d;
+            S.r[n] = f;
+        } else {
+            S.dinv[n] = 0;
+            S.r[n] = 0;
+            S.x[n] = 0;
+        }
+    }
+    if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+
+    // r = b - A x, z = D^-1 r, p = z
+    double rz = 0, rr = 0, bb = 0;
+    for (int n = tid; n < nn; n += stride) {
+        if (S.dinv[n] == 0) {
+            S.p[n] = 0;
+            continue;
+        }
+        const int i = n % S.Nx, j = n / S.Nx;
+        double b = S.r[n];
+        double ax = apply_row(S, i, j, S.x, nullptr, nullptr) + S.shift * S.x[n];
+        double r = b - ax;
+        S.r[n] = r;
+        double z = S.dinv[n] * r;
+        S.p[n] = z;
+        rz += r * z;
+        rr += r * r;
+        bb += b * b;
+    }
+    block_sum3(rz, rr, bb);
+    if (threadIdx.x == 0) {
+        S.partials[0 * nblocks + blockIdx.x] = rz;
+        S.partials[1 * nblocks + blockIdx.x] = rr;
+        S.partials[2 * nblocks + blockIdx.x] = bb;
+    }
+    if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+    rz = grid_total(S.partials, 0, nblocks);
+    rr = grid_total(S.partials, 1, nblocks);
+    bb = grid_total(S.partials, 2, nblocks);
+    const double target = S.tol * S.tol * bb;
+
+    int it = 0;
+    bool converged = (rr <= target);
+    if (bb == 0) {
+        // No load: the solution is zero (the warm start is discarded).
+        for (int n = tid; n < nn; n += stride) S.x[n] = 0;
+        rr = 0;
+        converged = true;
+    }
+    while (!converged && it < S.maxit) {
+        // q = A p, <p, q>
+        double pq = 0, d1 = 0, d2 = 0;
+        for (int n = tid; n < nn; n += stride) {
+            if (S.dinv[n] == 0) continue;
+            const int i = n % S.Nx, j = n / S.Nx;
+            double q = apply_row(S, i, j, S.p, nullptr, nullptr) + S.shift * S.p[n];
+            S.q[n] = q;
+            pq += S.p[n] * q;
+        }
+        block_sum3(pq, d1, d2);
+        if (threadIdx.x == 0) S.partials[3 * nblocks + blockIdx.x] = pq;
+        if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+        pq = grid_total(S.partials, 3, nblocks);
+        const double alpha = rz / pq;
+
+        // x += alpha p, r -= alpha q, <r, z>, <r, r>
+        double rz_new = 0, rr_new = 0, d3 = 0;
+        for (int n = tid; n < nn; n += stride) {
+            if (S.dinv[n] == 0) continue;
+            S.x[n] += alpha * S.p[n];
+            double r = S.r[n] - alpha * S.q[n];
+            S.r[n] = r;
+            rz_new += r * (S.dinv[n] * r);
+            rr_new += r * r;
+        }
+        block_sum3(rz_new, rr_new, d3);
+        if (threadIdx.x == 0) {
+            S.partials[0 * nblocks + blockIdx.x] = rz_new;
+            S.partials[1 * nblocks + blockIdx.x] = rr_new;
+        }
+        if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+        rz_new = grid_total(S.partials, 0, nblocks);
+        rr = grid_total(S.partials, 1, nblocks);
+        it++;
+        if (!(rr <= target) && !(rr == rr)) break;   // NaN: give up
+        converged = (rr <= target);
+        if (converged) break;
+        const double beta = rz_new / rz;
+        rz = rz_new;
+        for (int n = tid; n < nn; n += stride) {
+            if (S.dinv[n] == 0) continue;
+            S.p[n] = S.dinv[n] * S.r[n] + beta * S.p[n];
+        }
+        if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+    }
+    if (tid == 0) {
+        S.sp->solve_iters = it;
+        S.sp->solve_converged = converged ? 1 : 0;
+        S.sp->solve_rel_resid = (bb > 0) ? sqrt(rr / bb) : 0.0;
+        if (!converged) atomicOr(S.status, MPMG_DEV_ERR_SOLVER);
+    }
+}
+
+// Nodal fluidity back to the particles, then the stress update
+// (g_nonlocal_mu2.c:545-564 and :160-218; g_nonlocal.c:559-578, :154-298).
+template <bool MU2>
+__global__ void __launch_bounds__(256) fluidity_stress_kernel(
+    int n, int Nx, int Ex, mat::Elastic el, mat::NonlocalParams np, const StepParams *__restrict__ sp,
+    const int *__restrict__ active, const int *__restrict__ in_element, const double *__restrict__ xl,
+    const double *__restrict__ yl, const double *__restrict__ node_gf, const double *__restrict__ exx,
+    const double *__restrict__ exy, const double *__restrict__ eyy, const double *__restrict__ wxy,
+    const double *__restrict__ dense, double *__restrict__ gf, double *__restrict__ sxx,
+    double *__restrict__ sxy, double *__restrict__ syy, double *__restrict__ gammap,
+    double *__restrict__ gammadotp)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool act = active[i] != 0;
+    if (act) {
+        const int e = in_element[i];
+        const int ci = e % Ex, cj = e / Ex;
+        const int n0 = cj * Nx + ci;
+        const double a = xl[i], b = yl[i];
+        const double ox = 1 - a, oy = 1 - b;
+        double g = 0;
+        g += node_gf[n0] * (ox * oy);
+        g += node_gf[n0 + 1] * (a * oy);
+        g += node_gf[n0 + 1 + Nx] * (a * b);
+        g += node_gf[n0 + Nx] * (ox * b);
+        gf[i] = g;
+    }
+    if (MU2) {
+        if (!act) return;
+        double s0 = sxx[i], s1 = sxy[i], s2 = syy[i], gp = gammap[i], gdp;
+        mat::nonlocal_mu2_stress(el, dense[i], gf[i], exx[i], exy[i], eyy[i], wxy[i], s0, s1, s2, gp, gdp);
+        sxx[i] = s0;
+        sxy[i] = s1;
+        syy[i] = s2;
+        gammap[i] = gp;
+        gammadotp[i] = gdp;
+    } else {
+        double s0 = sxx[i], s1 = sxy[i], s2 = syy[i], gp = gammap[i];
+        mat::nonlocal_stress(np, el.G, el.dt, sp->t, gf[i], exx[i], exy[i], eyy[i], wxy[i], s0, s1, s2, gp);
+        sxx[i] = s0;
+        sxy[i] = s1;
+        syy[i] = s2;
+        gammap[i] = gp;
+    }
+}
+
+inline int blocks_for(size_t n, int threads)
+{
+    size_t b = (n + (size_t)threads - 1) / (size_t)threads;
+    return (int)(b > 0 ? b : 1);
+}
+
+}  // namespace
+
+int mpmg_nonlocal_init(mpmg_ctx *ctx)
+{
+    const size_t ne = ctx->ne > 0 ? ctx->ne : 1, nn = ctx->nn;
+    MPMG_CHECK(cudaMalloc(&ctx->elem_k, 10 * ne * sizeof(double)));
+    MPMG_CHECK(cudaMalloc(&ctx->elem_f, 4 * ne * sizeof(double)));
+    double **vecs[] = {&ctx->cg_x, &ctx->cg_r, &ctx->cg_p, &ctx->cg_q, &ctx->cg_dinv};
+    for (double **v : vecs) {
+        MPMG_CHECK(cudaMalloc(v, nn * sizeof(double)));
+        MPMG_CHECK(cudaMemsetAsync(*v, 0, nn * sizeof(double), ctx->stream));
+    }
+    int per_sm = 0, sms = 0;
+    MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_kernel, kSolveThreads, 0));
+    MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
+    if (per_sm < 1) {
+        mpmg_set_error("fluidity solver kernel cannot be resident");
+        return MPMG_ERR_CUDA;
+    }
+    // One or two blocks per SM: enough to cover the nodes with grid-stride
+    // loops while keeping the grid barrier short.
+    int want = sms * (per_sm < 2 ? per_sm : 2);
+    int need = (int)((nn + kSolveThreads - 1) / kSolveThreads);
+    ctx->cg_blocks = want < need ? want : (need > 0 ? need : 1);
+    MPMG_CHECK(cudaMalloc(&ctx->cg_partials, 4 * (size_t)ctx->cg_blocks * sizeof(double)));
+    MPMG_CHECK(cudaMalloc(&ctx->cg_barrier, 2 * sizeof(unsigned int)));
+    MPMG_CHECK(cudaMemsetAsync(ctx->cg_barrier, 0, 2 * sizeof(unsigned int), ctx->stream));
+    return MPMG_OK;
+}
+
+void mpmg_nonlocal_free(mpmg_ctx *ctx)
+{
+    double **ptrs[] = {&ctx->elem_k, &ctx->elem_f, &ctx->cg_x, &ctx->cg_r, &ctx->cg_p, &ctx->cg_q,
+                       &ctx->cg_dinv, &ctx->cg_partials};
+    for (double **p : ptrs) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    cudaFree(ctx->cg_barrier);
+    ctx->cg_barrier = nullptr;
+}
+
+int mpmg_launch_fluidity(mpmg_ctx *ctx)
+{
+    cudaStream_t s = ctx->stream;
+    const mpmg_config &c = ctx->cfg;
+    const bool mu2 = c.material == MPMG_G_NONLOCAL_MU2;
+    const int n = (int)ctx->np, ne = (int)ctx->ne;
+    mat::NonlocalParams np;
+    np.E = c.mp[MPMG_MP_E];
+    np.nu = c.mp[MPMG_MP_NU];
+    np.mu_s = c.mp[MPMG_MP_MU_S];
+    np.grains_rho = c.mp[MPMG_MP_GRAINS_RHO];
+    np.B = c.mp[MPMG_MP_B];
+    np.A = c.mp[MPMG_MP_A];
+    np.grains_d = c.mp[MPMG_MP_GRAINS_D];
+    np.cohesion = c.mp[MPMG_MP_COHESION];
+    if (!mu2) {
+        nonlocal_bulk_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, np, ctx->sxx, ctx->sxy, ctx->syy,
+                                                                ctx->state[4], ctx->state[5], ctx->state[10]);
+        ctx->launches += 1;
+    }
+    const double *xisq = mu2 ? ctx->state[6] : ctx->state[10];
+    assemble_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(ne, ctx->Ex, ctx->inv_h, mu2 ? 1 : 0, ctx->cell_start,
+                                                        ctx->perm, ctx->xl, ctx->yl, ctx->v, ctx->state[0],
+                                                        ctx->state[5], xisq, ctx->elem_k, ctx->elem_f);
+    ctx->launches += 1;
+
+    SolveArgs S;
+    S.Nx = c.Nx;
+    S.Ny = c.Ny;
+    S.Ex = ctx->Ex;
+    S.Ey = ctx->Ey;
+    S.ne = ne;
+    S.dof_tol = mu2 ? 0.0 : MPMG_TOL;
+    S.shift = mu2 ? 1e-10 : 0.0;
+    S.tol = c.solver_tol;
+    S.maxit = c.solver_maxit;
+    S.node_m = ctx->node_m;
+    S.cell_start = ctx->cell_start;
+    S.elem_k = ctx->elem_k;
+    S.elem_f = ctx->elem_f;
+    S.x = ctx->node_gf;     // warm start from the previous step, result in place
+    S.r = ctx->cg_r;
+    S.p = ctx->cg_p;
+    S.q = ctx->cg_q;
+    S.dinv = ctx->cg_dinv;
+    S.partials = ctx->cg_partials;
+    S.barrier = ctx->cg_barrier;
+    S.status = ctx->d_status;
+    S.sp = ctx->d_params;
+    void *args[] = {&S};
+    MPMG_CHECK(cudaMemsetAsync(ctx->cg_barrier, 0, 2 * sizeof(unsigned int), s));
+    MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_kernel, dim3(ctx->cg_blocks),
+                                           dim3(kSolveThreads), args, 0, s));
+    ctx->launches += 1;
+
+    mat::Elastic el;
+    el.G = ctx->G;
+    el.K = ctx->K;
+    el.lambda = ctx->lambda;
+    el.dt = c.dt;
+    if (mu2) {
+        fluidity_stress_kernel<true><<<blocks_for(n, 256), 256, 0, s>>>(
+            n, c.Nx, ctx->Ex, el, np, ctx->d_params, ctx->active, ctx->in_element, ctx->xl, ctx->yl,
+            ctx->node_gf, ctx->exx, ctx->exy, ctx->eyy, ctx->wxy, ctx->state[0], ctx->state[3], ctx->sxx,
+            ctx->sxy, ctx->syy, ctx->state[9], ctx->state[10]);
+    } else {
+        fluidity_stress_kernel<false><<<blocks_for(n, 256), 256, 0, s>>>(
+            n, c.Nx, ctx->Ex, el, np, ctx->d_params, ctx->active, ctx->in_element, ctx->xl, ctx->yl,
+            ctx->node_gf, ctx->exx, ctx->exy, ctx->eyy, ctx->wxy, ctx->state[0], ctx->state[3], ctx->sxx,
+            ctx->sxy, ctx->syy, ctx->state[9], ctx->state[10]);
+    }
+    ctx->launches += 1;
+    MPMG_CHECK(cudaGetLastError());
+    return MPMG_OK;
+}

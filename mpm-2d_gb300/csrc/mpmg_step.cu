@@ -1,0 +1,548 @@
+// The explicit USL step on the GPU (reference: explicit_mpm_step_usl_threaded,
+// libmpm/process_usl.c:465-592, plus the driver's time_varying_loads tail,
+// src/main.c:975 and libmpm/loading.c:34-54).
+//
+//   keys      element of every particle (WHICH_ELEMENT4, :43-44 and :631-674);
+//             advances t and the gravity scalar in the device StepParams
+//   sort      stable radix sort of (element, particle) -> per-element
+//             particle segments (find_filled_elements, :677-723)
+//   p2g       one thread per element sums its particles' contributions to
+//             its four corners (map_to_grid_explicit_split, :812-910)
+//   grid      one thread per node adds the four adjacent elements' corner
+//             sums in colour order 0..3, applies the box / square-silo
+//             conditions and the nodal update (bc_momentum, bc_force,
+//             move_grid_split :596-625)
+//   g2p       one thread per particle: velocity and position update, strain
+//             rate, volume and the material law (move_particles :914-957,
+//             calculate_strainrate :764-808, update_densities :961-970,
+//             calculate_stress_threaded)
+//
+// Shape functions (tent / grad_tent, interpolate.c:23-65) are recomputed in
+// registers from the start-of-step position wherever they are needed.  No
+// floating-point atomics are used; every sum has a fixed order.
+#include "mpmg_internal.cuh"
+#include "mpmg_materials.cuh"
+
+namespace {
+
+struct GridGeom {
+    int Nx, Ny, Ex, Ey;
+    double h, inv_h, xmax, ymax;
+};
+
+struct BcParams {
+    int kind;
+    // box: wall columns / rows and friction bits
+    int left_col, right_col, bottom_row, top_row;
+    int lf, bf, rf, tf;
+    // silo
+    double hole_radius, open_time;
+    int wall_col;
+};
+
+// ---------------------------------------------------------------------------
+// keys
+
+__global__ void keys_kernel(GridGeom g, int n, const double *__restrict__ x,
+                            const double *__restrict__ y, int *__restrict__ in_element,
+                            int *__restrict__ active, uint32_t *__restrict__ keys,
+                            uint32_t *__restrict__ vals, uint32_t sentinel, StepParams *sp,
+                            double dt, int gravity_mode, double gravity_const)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // time_varying_loads (loading.c:34-54) of the previous step's tail, or
+        // initial_loads (loading.c:21-30) before the first step; then t += dt
+        // (process_usl.c:522).
+        double t = sp->t;
+        double grav;
+        if (gravity_mode == MPMG_GRAVITY_CONSTANT) {
+            grav = gravity_const;
+        } else if (sp->step_count == 0) {
+            grav = 0.0;
+        } else if ((0.1 + sp->step_start_time) > t) {
+            grav = -9.8 * ((t - sp->step_start_time) / 0.1);
+        } else {
+            grav = -9.8;
+        }
+        sp->gravity = grav;
+        sp->t = t + dt;
+        sp->step_count += 1;
+    }
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t key = sentinel;
+    if (active[i]) {
+        int e = mpmg_which_element(x[i], y[i], g.h, g.inv_h, g.xmax, g.ymax, g.Ex, g.Ey);
+        in_element[i] = e;
+        if (e < 0) {
+            active[i] = 0;   // process_usl.c:660-666: outside the grid for good
+        } else {
+            key = (uint32_t)e;
+        }
+    }
+    keys[i] = key;
+    vals[i] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------------
+// p2g: per-element corner sums over the element's particle segment.
+
+struct ShapeFns {
+    double s[4], gx[4], gy[4];
+};
+
+// tent and grad_tent (interpolate.c:23-65) at local coordinates (xl, yl);
+// node order BL, BR, TR, TL (process_usl.c:140-143).
+__device__ __forceinline__ ShapeFns shape(double xl, double yl, double inv_h)
+{
+    ShapeFns f;
+    double ox = 1 - xl, oy = 1 - yl;
+    f.s[0] = ox * oy;
+    f.s[1] = xl * oy;
+    f.s[2] = xl * yl;
+    f.s[3] = ox * yl;
+    f.gx[0] = -oy * inv_h;
+    f.gx[1] = oy * inv_h;
+    f.gx[2] = yl * inv_h;
+    f.gx[3] = -yl * inv_h;
+    f.gy[0] = -ox * inv_h;
+    f.gy[1] = -xl * inv_h;
+    f.gy[2] = xl * inv_h;
+    f.gy[3] = ox * inv_h;
+    return f;
+}
+
+__global__ void __launch_bounds__(128) p2g_cells_kernel(
+    GridGeom g, int ne, const int *__restrict__ cell_start, const uint32_t *__restrict__ perm,
+    const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ m,
+    const double *__restrict__ vx, const double *__restrict__ vy, const double *__restrict__ v,
+    const double *__restrict__ sxx, const double *__restrict__ sxy, const double *__restrict__ syy,
+    const StepParams *__restrict__ sp, double *__restrict__ cell_sums)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int k0 = cell_start[e], k1 = cell_start[e + 1];
+    if (k0 == k1) return;
+    const int ci = e % g.Ex, cj = e / g.Ex;
+    const double xn = ci * g.h, yn = cj * g.h;   // node_number_to_coords (element.c:10-19)
+    const double grav = sp->gravity;
+    // acc[corner][field], fields m, mx, my, fx, fy
+    double acc[4][5];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < 5; f++) acc[a][f] = 0.0;
+    for (int k = k0; k < k1; k++) {
+        const int i = (int)perm[k];
+        const double xl = mpmg_local_coord(x[i], xn, g.inv_h);
+        const double yl = mpmg_local_coord(y[i], yn, g.inv_h);
+        const ShapeFns f = shape(xl, yl, g.inv_h);
+        const double pm = m[i];
+        const double pmx = vx[i] * pm, pmy = vy[i] * pm, pby = grav * pm;
+        const double vol = v[i];
+        const double s0 = -sxx[i] * vol, s1 = -sxy[i] * vol, s2 = -syy[i] * vol;
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            acc[a][0] += f.s[a] * pm;
+            acc[a][1] += f.s[a] * pmx;
+            acc[a][2] += f.s[a] * pmy;
+            // body force bx is zero (loading.c:48): fx gets only the stress terms
+            acc[a][3] += f.gx[a] * s0;
+            acc[a][3] += f.gy[a] * s1;
+            acc[a][4] += f.s[a] * pby;
+            acc[a][4] += f.gx[a] * s1;
+            acc[a][4] += f.gy[a] * s2;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < 5; f++) cell_sums[(size_t)(a * 5 + f) * ne + e] = acc[a][f];
+}
+
+// ---------------------------------------------------------------------------
+// grid: finish P2G per node, boundary conditions, nodal update.
+
+__device__ __forceinline__ void bc_mask(const BcParams &bc, const GridGeom &g, int i, int j,
+                                        double t_now, bool &mx, bool &my)
+{
+    mx = false;
+    my = false;
+    if (bc.kind == MPMG_BOX) {
+        // box.c:106-167
+        bool on_row = (i >= bc.left_col && i <= bc.right_col);
+        bool on_col = (j >= bc.bottom_row && j <= bc.top_row);
+        if (on_row && j == bc.bottom_row) { mx |= (bc.bf & 1) != 0; my |= (bc.bf & 2) != 0; }
+        if (on_row && j == bc.top_row) { mx |= (bc.tf & 1) != 0; my |= (bc.tf & 2) != 0; }
+        if (on_col && i == bc.left_col) { mx |= (bc.lf & 1) != 0; my |= (bc.lf & 2) != 0; }
+        if (on_col && i == bc.right_col) { mx |= (bc.rf & 1) != 0; my |= (bc.rf & 2) != 0; }
+    } else {
+        // square_silo.c:58-91: floor (trapdoor open at x <= hole radius after
+        // the opening time), frictionless walls at column 0 and wall_col
+        if (j == 0) {
+            double xnode = i * g.h;
+            if (!(xnode <= bc.hole_radius && t_now > bc.open_time)) {
+                mx = true;
+                my = true;
+            }
+        }
+        if (i == 0 || i == bc.wall_col) mx = true;
+    }
+}
+
+__global__ void __launch_bounds__(256) grid_kernel(
+    GridGeom g, BcParams bc, int ne, const int *__restrict__ cell_start,
+    const double *__restrict__ cell_sums, const StepParams *__restrict__ sp, double dt,
+    double *__restrict__ node_m, double *__restrict__ node_ax, double *__restrict__ node_ay,
+    double *__restrict__ node_vx, double *__restrict__ node_vy, double *__restrict__ node_mx,
+    double *__restrict__ node_my, double *__restrict__ node_fx, double *__restrict__ node_fy)
+{
+    const int nn = g.Nx * g.Ny;
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    double sum[5] = {0, 0, 0, 0, 0};
+    // Colour c = 2 * (row % 2) + (col % 2) (process_usl.c:158); the four
+    // elements around a node have the four colours, summed in order 0..3.
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+        int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
+        int e = cj * g.Ex + ci;
+        if (cell_start[e] == cell_start[e + 1]) continue;
+        int corner = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+#pragma unroll
+        for (int f = 0; f < 5; f++) sum[f] += cell_sums[(size_t)(corner * 5 + f) * ne + e];
+    }
+    double m = sum[0], mx = sum[1], my = sum[2], fx = sum[3], fy = sum[4];
+    bool bx, by;
+    bc_mask(bc, g, i, j, sp->t, bx, by);
+    if (bx) { mx = 0; fx = 0; }
+    if (by) { my = 0; fy = 0; }
+    double ax = 0, ay = 0, vxn = 0, vyn = 0;
+    if (m > MPMG_TOL) {
+        ax = fx / m;
+        ay = fy / m;
+        mx += dt * fx;
+        my += dt * fy;
+        vxn = mx / m;
+        vyn = my / m;
+    }
+    node_m[n] = m;
+    node_ax[n] = ax;
+    node_ay[n] = ay;
+    node_vx[n] = vxn;
+    node_vy[n] = vyn;
+    if (node_mx != nullptr) {
+        node_mx[n] = mx;
+        node_my[n] = my;
+        node_fx[n] = fx;
+        node_fy[n] = fy;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// g2p + material
+
+struct G2PArgs {
+    GridGeom g;
+    int n;
+    double dt;
+    mat::Elastic el;
+    mat::Mu2Params mu2;
+    mat::NonlocalParams nl;
+    const int *in_element;
+    const int *active;
+    const double *node_ax, *node_ay, *node_vx, *node_vy;
+    double *x, *y, *vx, *vy, *ux, *uy, *v, *m;
+    double *sxx, *sxy, *syy, *Tzz;
+    double *st0, *st3, *st4, *st5, *st6, *st9, *st10;
+    double *ax, *ay, *exx, *exy, *eyy, *wxy, *xl_out, *yl_out;
+};
+
+template <int MATERIAL>
+__global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n || !A.active[i]) return;
+    const GridGeom &g = A.g;
+    const int e = A.in_element[i];
+    const int ci = e % g.Ex, cj = e / g.Ex;
+    const int n0 = cj * g.Nx + ci;
+    const int nd[4] = {n0, n0 + 1, n0 + 1 + g.Nx, n0 + g.Nx};
+    double px = A.x[i], py = A.y[i];
+    const double xl = mpmg_local_coord(px, ci * g.h, g.inv_h);
+    const double yl = mpmg_local_coord(py, cj * g.h, g.inv_h);
+    const ShapeFns f = shape(xl, yl, g.inv_h);
+
+    double nax[4], nay[4], nvx[4], nvy[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        nax[a] = A.node_ax[nd[a]];
+        nay[a] = A.node_ay[nd[a]];
+        nvx[a] = A.node_vx[nd[a]];
+        nvy[a] = A.node_vy[nd[a]];
+    }
+    // move_particles_explicit_usl_split (process_usl.c:914-957); light nodes
+    // (m <= 1e-10) carry zero acceleration and velocity.
+    double xtt = 0, ytt = 0, dux = 0, duy = 0;
+    double exx = 0, eyy = 0, dxdy = 0, dydx = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        xtt += f.s[a] * nax[a];
+        ytt += f.s[a] * nay[a];
+        dux += f.s[a] * nvx[a];
+        duy += f.s[a] * nvy[a];
+        // calculate_strainrate_split (process_usl.c:796-803)
+        exx += f.gx[a] * nvx[a];
+        eyy += f.gy[a] * nvy[a];
+        dxdy += f.gy[a] * nvx[a];
+        dydx += f.gx[a] * nvy[a];
+    }
+    const double dt = A.dt;
+    A.vx[i] += dt * xtt;
+    A.vy[i] += dt * ytt;
+    dux *= dt;
+    duy *= dt;
+    A.x[i] = px + dux;
+    A.y[i] = py + duy;
+    A.ux[i] += dux;
+    A.uy[i] += duy;
+    const double exy = 0.5 * (dxdy + dydx);
+    const double wxy = 0.5 * (dxdy - dydx);
+    // update_particle_densities_split (process_usl.c:961-970)
+    double vol = A.v[i] * exp(dt * (exx + eyy));
+    A.v[i] = vol;
+    if (A.ax != nullptr) {
+        A.ax[i] = xtt;
+        A.ay[i] = ytt;
+    }
+    if (A.exx != nullptr) {
+        A.exx[i] = exx;
+        A.exy[i] = exy;
+        A.eyy[i] = eyy;
+        A.wxy[i] = wxy;
+    }
+    if (A.xl_out != nullptr) {
+        A.xl_out[i] = xl;
+        A.yl_out[i] = yl;
+    }
+
+    if (MATERIAL == MPMG_ISOLIN) {
+        double sxx = A.sxx[i], sxy = A.sxy[i], syy = A.syy[i];
+        mat::isolin(A.el, exx, exy, eyy, wxy, sxx, sxy, syy);
+        A.sxx[i] = sxx;
+        A.sxy[i] = sxy;
+        A.syy[i] = syy;
+    } else if (MATERIAL == MPMG_G_LOCAL_MU2) {
+        double Txx = A.sxx[i], Txy = A.sxy[i], Tyy = A.syy[i], Tzz = A.Tzz[i];
+        double gp = A.st9[i], gdp;
+        mat::g_local_mu2(A.el, A.mu2, A.m[i], vol, exx, exy, eyy, wxy, Txx, Txy, Tyy, Tzz, gp, gdp);
+        A.sxx[i] = Txx;
+        A.sxy[i] = Txy;
+        A.syy[i] = Tyy;
+        A.Tzz[i] = Tzz;
+        A.st9[i] = gp;
+        A.st10[i] = gdp;
+    } else if (MATERIAL == MPMG_G_NONLOCAL_MU2) {
+        double dense, gfl, xisq;
+        mat::nonlocal_mu2_bulk(A.el, A.mu2, A.m[i], vol, exx, exy, eyy, wxy, A.sxx[i], A.sxy[i],
+                               A.syy[i], dense, gfl, xisq);
+        A.st0[i] = dense;
+        A.st5[i] = gfl;
+        A.st6[i] = xisq;
+    }
+    // MPMG_G_NONLOCAL computes its bulk fluidity over every particle in the
+    // fluidity phase (g_nonlocal.c:306-352).
+}
+
+__global__ void material_only_kernel(G2PArgs A, int material)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n || !A.active[i]) return;
+    double exx = A.exx[i], exy = A.exy[i], eyy = A.eyy[i], wxy = A.wxy[i];
+    if (material == MPMG_ISOLIN) {
+        double sxx = A.sxx[i], sxy = A.sxy[i], syy = A.syy[i];
+        mat::isolin(A.el, exx, exy, eyy, wxy, sxx, sxy, syy);
+        A.sxx[i] = sxx;
+        A.sxy[i] = sxy;
+        A.syy[i] = syy;
+    } else {
+        double Txx = A.sxx[i], Txy = A.sxy[i], Tyy = A.syy[i], Tzz = A.Tzz[i];
+        double gp = A.st9[i], gdp;
+        mat::g_local_mu2(A.el, A.mu2, A.m[i], A.v[i], exx, exy, eyy, wxy, Txx, Txy, Tyy, Tzz, gp, gdp);
+        A.sxx[i] = Txx;
+        A.sxy[i] = Txy;
+        A.syy[i] = Tyy;
+        A.Tzz[i] = Tzz;
+        A.st9[i] = gp;
+        A.st10[i] = gdp;
+    }
+}
+
+GridGeom make_geom(const mpmg_ctx *ctx)
+{
+    GridGeom g;
+    g.Nx = ctx->cfg.Nx;
+    g.Ny = ctx->cfg.Ny;
+    g.Ex = ctx->Ex;
+    g.Ey = ctx->Ey;
+    g.h = ctx->cfg.h;
+    g.inv_h = ctx->inv_h;
+    g.xmax = ctx->cfg.xmax;
+    g.ymax = ctx->cfg.ymax;
+    return g;
+}
+
+BcParams make_bc(const mpmg_ctx *ctx)
+{
+    BcParams b = {};
+    const mpmg_config &c = ctx->cfg;
+    b.kind = c.bc;
+    if (c.bc == MPMG_BOX) {
+        // box.c:92-95 (fractions of the grid's node span)
+        b.left_col = (int)(size_t)(c.bcf[0] * (double)(c.Nx - 1));
+        b.right_col = (int)(size_t)((c.bcf[0] + c.bcf[2]) * (double)(c.Nx - 1));
+        b.bottom_row = (int)(size_t)(c.bcf[1] * (double)(c.Ny - 1));
+        b.top_row = (int)(size_t)((c.bcf[1] + c.bcf[3]) * (double)(c.Ny - 1));
+        b.lf = c.bci[0];
+        b.bf = c.bci[1];
+        b.rf = c.bci[2];
+        b.tf = c.bci[3];
+    } else {
+        b.hole_radius = c.bcf[0];
+        b.open_time = c.bcf[1];
+        b.wall_col = (int)((double)(c.Nx - 1) * c.bcf[2]);   // square_silo.c:44
+    }
+    return b;
+}
+
+G2PArgs make_g2p_args(mpmg_ctx *ctx)
+{
+    G2PArgs A;
+    const mpmg_config &c = ctx->cfg;
+    A.g = make_geom(ctx);
+    A.n = (int)ctx->np;
+    A.dt = c.dt;
+    A.el.G = ctx->G;
+    A.el.K = ctx->K;
+    A.el.lambda = ctx->lambda;
+    A.el.dt = c.dt;
+    A.mu2.mu_s = c.mp[MPMG_MP_MU_S];
+    A.mu2.mu_2 = c.mp[MPMG_MP_MU_2];
+    A.mu2.I0 = c.mp[MPMG_MP_I0];
+    A.mu2.grains_rho = c.mp[MPMG_MP_GRAINS_RHO];
+    A.mu2.grains_d = c.mp[MPMG_MP_GRAINS_D];
+    A.mu2.rho_critical = c.mp[MPMG_MP_RHO_CRITICAL];
+    A.mu2.A = c.mp[MPMG_MP_A];
+    A.nl.E = c.mp[MPMG_MP_E];
+    A.nl.nu = c.mp[MPMG_MP_NU];
+    A.nl.mu_s = c.mp[MPMG_MP_MU_S];
+    A.nl.grains_rho = c.mp[MPMG_MP_GRAINS_RHO];
+    A.nl.B = c.mp[MPMG_MP_B];
+    A.nl.A = c.mp[MPMG_MP_A];
+    A.nl.grains_d = c.mp[MPMG_MP_GRAINS_D];
+    A.nl.cohesion = c.mp[MPMG_MP_COHESION];
+    A.in_element = ctx->in_element;
+    A.active = ctx->active;
+    A.node_ax = ctx->node_ax;
+    A.node_ay = ctx->node_ay;
+    A.node_vx = ctx->node_vx;
+    A.node_vy = ctx->node_vy;
+    A.x = ctx->x; A.y = ctx->y; A.vx = ctx->vx; A.vy = ctx->vy; A.ux = ctx->ux; A.uy = ctx->uy;
+    A.v = ctx->v; A.m = ctx->m;
+    A.sxx = ctx->sxx; A.sxy = ctx->sxy; A.syy = ctx->syy; A.Tzz = ctx->Tzz;
+    A.st0 = ctx->state[0]; A.st3 = ctx->state[3]; A.st4 = ctx->state[4]; A.st5 = ctx->state[5];
+    A.st6 = ctx->state[6]; A.st9 = ctx->state[9]; A.st10 = ctx->state[10];
+    A.ax = ctx->ax; A.ay = ctx->ay;
+    A.exx = ctx->exx; A.exy = ctx->exy; A.eyy = ctx->eyy; A.wxy = ctx->wxy;
+    A.xl_out = ctx->xl; A.yl_out = ctx->yl;
+    return A;
+}
+
+inline int blocks_for(size_t n, int threads)
+{
+    size_t b = (n + (size_t)threads - 1) / (size_t)threads;
+    return (int)(b > 0 ? b : 1);
+}
+
+}  // namespace
+
+int mpmg_launch_step(mpmg_ctx *ctx)
+{
+    cudaStream_t s = ctx->stream;
+    const mpmg_config &c = ctx->cfg;
+    const GridGeom g = make_geom(ctx);
+    const int n = (int)ctx->np;
+    const int ne = (int)ctx->ne;
+    const int nn = (int)ctx->nn;
+
+    mpmg_phase_begin(ctx, PH_KEYS);
+    keys_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, n, ctx->x, ctx->y, ctx->in_element, ctx->active,
+                                                   ctx->keys, ctx->vals, (uint32_t)ne, ctx->d_params,
+                                                   c.dt, c.gravity_mode, c.gravity);
+    ctx->launches += 1;
+    mpmg_phase_end(ctx, PH_KEYS);
+
+    mpmg_phase_begin(ctx, PH_SORT);
+    int rc = mpmg_sort_keys(ctx);
+    if (rc != MPMG_OK) return rc;
+    mpmg_phase_end(ctx, PH_SORT);
+
+    mpmg_phase_begin(ctx, PH_P2G);
+    p2g_cells_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(
+        g, ne, ctx->cell_start, ctx->perm, ctx->x, ctx->y, ctx->m, ctx->vx, ctx->vy, ctx->v, ctx->sxx,
+        ctx->sxy, ctx->syy, ctx->d_params, ctx->cell_sums);
+    ctx->launches += 1;
+    mpmg_phase_end(ctx, PH_P2G);
+
+    mpmg_phase_begin(ctx, PH_GRID);
+    grid_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(
+        g, make_bc(ctx), ne, ctx->cell_start, ctx->cell_sums, ctx->d_params, c.dt, ctx->node_m,
+        ctx->node_ax, ctx->node_ay, ctx->node_vx, ctx->node_vy, ctx->node_mx, ctx->node_my,
+        ctx->node_fx, ctx->node_fy);
+    ctx->launches += 1;
+    mpmg_phase_end(ctx, PH_GRID);
+
+    mpmg_phase_begin(ctx, PH_G2P);
+    G2PArgs A = make_g2p_args(ctx);
+    switch (c.material) {
+    case MPMG_ISOLIN:
+        g2p_kernel<MPMG_ISOLIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        break;
+    case MPMG_G_LOCAL_MU2:
+        g2p_kernel<MPMG_G_LOCAL_MU2><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        break;
+    case MPMG_G_NONLOCAL_MU2:
+        g2p_kernel<MPMG_G_NONLOCAL_MU2><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        break;
+    default:
+        g2p_kernel<MPMG_G_NONLOCAL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        break;
+    }
+    ctx->launches += 1;
+    mpmg_phase_end(ctx, PH_G2P);
+    MPMG_CHECK(cudaGetLastError());
+
+    if (c.material == MPMG_G_NONLOCAL_MU2 || c.material == MPMG_G_NONLOCAL) {
+        mpmg_phase_begin(ctx, PH_FLUIDITY);
+        rc = mpmg_launch_fluidity(ctx);
+        if (rc != MPMG_OK) return rc;
+        mpmg_phase_end(ctx, PH_FLUIDITY);
+    }
+    return MPMG_OK;
+}
+
+int mpmg_launch_material_only(mpmg_ctx *ctx)
+{
+    G2PArgs A = make_g2p_args(ctx);
+    if (A.exx == nullptr) {
+        mpmg_set_error("material-only update needs store_transients (strain-rate inputs)");
+        return MPMG_ERR_INVALID;
+    }
+    material_only_kernel<<<blocks_for(ctx->np, 256), 256, 0, ctx->stream>>>(A, ctx->cfg.material);
+    ctx->launches += 1;
+    MPMG_CHECK(cudaGetLastError());
+    return MPMG_OK;
+}

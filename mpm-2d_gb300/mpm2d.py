@@ -1,0 +1,254 @@
+"""Python binding of the mpm_gb300 C ABI (include/mpm_gb300.h) over ctypes.
+
+``Simulation`` holds one device-resident mpm-2d simulation: the reference's
+explicit USL step (libmpm/process_usl.c:465-592) with one of its material
+plugins (isolin, g_local_mu2, g_nonlocal_mu2, g_nonlocal) and boundary
+plugins (box, square_silo), run as sm_103a kernels.  There is no CPU path:
+loading fails loudly when the shared library or a GPU is missing.
+
+A scene is a dict:
+  Nx, Ny, h           grid nodes per row / column and element size
+  xmax, ymax          element-map inside bounds (default 1.0 as the reference)
+  dt                  time step
+  material            "isolin" | "g_local_mu2" | "g_nonlocal_mu2" | "g_nonlocal"
+  props               [E, nu] (the configuration file's material properties)
+  mp                  {slot: value} overrides of the material constants
+  bc                  "box" | "square_silo"
+  bcf, bci            boundary properties / integer properties
+  gravity             None for the reference ramp, else a constant body force
+  particles           dict of arrays m, v, x, y, vx, vy, sxx, sxy, syy
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+import mpmg_build as _build
+
+MATERIALS = {"isolin": 0, "g_local_mu2": 1, "g_nonlocal_mu2": 2, "g_nonlocal": 3}
+BCS = {"box": 0, "square_silo": 1}
+MP_COUNT = 16
+MP = {"E": 0, "nu": 1, "mu_s": 2, "mu_2": 3, "I0": 4, "grains_rho": 5, "grains_d": 6, "A": 7,
+      "rho_critical": 8, "B": 9, "cohesion": 10}
+STATUS_SOLVER = 2
+
+
+class MpmError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("mpm_gb300 status %d: %s" % (status, message))
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("Nx", C.c_int), ("Ny", C.c_int), ("h", C.c_double), ("xmax", C.c_double),
+                ("ymax", C.c_double), ("dt", C.c_double), ("material", C.c_int),
+                ("mp", C.c_double * MP_COUNT), ("bc", C.c_int), ("bcf", C.c_double * 4),
+                ("bci", C.c_int * 4), ("gravity_mode", C.c_int), ("gravity", C.c_double),
+                ("store_transients", C.c_int), ("solver_tol", C.c_double),
+                ("solver_maxit", C.c_int), ("device", C.c_int)]
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=True):
+    """Loads libmpm_gb300.so (building it first when missing or stale)."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build_if_missing else _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError("libmpm_gb300.so not built")
+        L = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int)
+        vp = C.c_void_p
+        L.mpmg_default_params.argtypes = [C.c_int, dp]
+        L.mpmg_config_init.argtypes = [C.POINTER(Config)]
+        L.mpmg_create.argtypes = [C.POINTER(Config), C.c_size_t] + [dp] * 9 + [C.POINTER(vp)]
+        L.mpmg_destroy.argtypes = [vp]
+        L.mpmg_step.argtypes = [vp, C.c_int]
+        L.mpmg_synchronize.argtypes = [vp]
+        L.mpmg_get_field.argtypes = [vp, C.c_char_p, dp]
+        L.mpmg_set_field.argtypes = [vp, C.c_char_p, dp]
+        L.mpmg_get_map.argtypes = [vp, ip, ip]
+        L.mpmg_set_map.argtypes = [vp, ip, ip]
+        L.mpmg_get_sort.argtypes = [vp, ip, ip, ip]
+        L.mpmg_get_time.argtypes = [vp, dp, ip]
+        L.mpmg_set_time.argtypes = [vp, C.c_double, C.c_int]
+        L.mpmg_sizes.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+        L.mpmg_material_only.argtypes = [vp]
+        L.mpmg_get_stream.argtypes = [vp, C.POINTER(vp)]
+        L.mpmg_enable_phase_timing.argtypes = [vp, C.c_int]
+        L.mpmg_phase_count.argtypes = []
+        L.mpmg_phase_name.argtypes = [C.c_int]
+        L.mpmg_phase_name.restype = C.c_char_p
+        L.mpmg_phase_times.argtypes = [vp, dp, C.POINTER(C.c_long)]
+        L.mpmg_last_solve.argtypes = [vp, ip, dp]
+        L.mpmg_launch_count.argtypes = [vp, C.POINTER(C.c_long), C.c_int]
+        L.mpmg_status_string.argtypes = [C.c_int]
+        L.mpmg_status_string.restype = C.c_char_p
+        L.mpmg_last_error.argtypes = []
+        L.mpmg_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        L = lib()
+        raise MpmError(rc, "%s (%s)" % (L.mpmg_status_string(rc).decode(), L.mpmg_last_error().decode()))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def default_params(material):
+    mp = np.zeros(MP_COUNT)
+    _check(lib().mpmg_default_params(MATERIALS[material], _dptr(mp)))
+    return mp
+
+
+def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0):
+    cfg = Config()
+    _check(lib().mpmg_config_init(C.byref(cfg)))
+    cfg.Nx, cfg.Ny, cfg.h = scene["Nx"], scene["Ny"], scene["h"]
+    cfg.xmax, cfg.ymax = scene.get("xmax", 1.0), scene.get("ymax", 1.0)
+    cfg.dt = scene["dt"]
+    cfg.material = MATERIALS[scene["material"]]
+    mp = default_params(scene["material"])
+    props = scene.get("props")
+    if props is not None:
+        mp[0], mp[1] = props[0], props[1]
+    for k, val in scene.get("mp", {}).items():
+        mp[MP[k] if isinstance(k, str) else k] = val
+    for k in range(MP_COUNT):
+        cfg.mp[k] = mp[k]
+    cfg.bc = BCS[scene["bc"]]
+    for k, val in enumerate(scene.get("bcf", [])):
+        cfg.bcf[k] = val
+    for k, val in enumerate(scene.get("bci", [])):
+        cfg.bci[k] = val
+    cfg.gravity_mode = 1 if scene.get("gravity") is not None else 0
+    cfg.gravity = scene.get("gravity") or 0.0
+    cfg.store_transients = 1 if store_transients else 0
+    cfg.solver_tol = solver_tol
+    cfg.solver_maxit = solver_maxit
+    cfg.device = device
+    return cfg
+
+
+class Simulation:
+    """One simulation resident on the GPU."""
+
+    def __init__(self, scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0):
+        L = lib()
+        cfg = make_config(scene, store_transients, solver_tol, solver_maxit, device)
+        p = scene["particles"]
+        self.n = len(p["x"])
+        arrs = [np.ascontiguousarray(p[k], dtype=np.float64)
+                for k in ("m", "v", "x", "y", "vx", "vy", "sxx", "sxy", "syy")]
+        h = C.c_void_p()
+        _check(L.mpmg_create(C.byref(cfg), self.n, *[_dptr(a) for a in arrs], C.byref(h)))
+        self._h = h
+        npart, nn, ne = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        _check(L.mpmg_sizes(self._h, C.byref(npart), C.byref(nn), C.byref(ne)))
+        self.nn, self.ne = nn.value, ne.value
+        self.scene = scene
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mpmg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def step(self, n=1):
+        _check(lib().mpmg_step(self._h, n))
+
+    def synchronize(self):
+        _check(lib().mpmg_synchronize(self._h))
+
+    def get(self, name):
+        n = self.nn if name.startswith("node_") else self.n
+        out = np.empty(n)
+        _check(lib().mpmg_get_field(self._h, name.encode(), _dptr(out)))
+        return out
+
+    def set(self, name, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        _check(lib().mpmg_set_field(self._h, name.encode(), _dptr(a)))
+
+    def get_map(self):
+        e = np.empty(self.n, dtype=np.int32)
+        a = np.empty(self.n, dtype=np.int32)
+        _check(lib().mpmg_get_map(self._h, _iptr(e), _iptr(a)))
+        return e, a
+
+    def set_map(self, in_element, active):
+        e = np.ascontiguousarray(in_element, dtype=np.int32)
+        a = np.ascontiguousarray(active, dtype=np.int32)
+        _check(lib().mpmg_set_map(self._h, _iptr(e), _iptr(a)))
+
+    def get_sort(self):
+        k = np.empty(self.n, dtype=np.int32)
+        p = np.empty(self.n, dtype=np.int32)
+        c = np.empty(self.ne + 1, dtype=np.int32)
+        _check(lib().mpmg_get_sort(self._h, _iptr(k), _iptr(p), _iptr(c)))
+        return k, p, c
+
+    @property
+    def t(self):
+        t = C.c_double()
+        s = C.c_int()
+        _check(lib().mpmg_get_time(self._h, C.byref(t), C.byref(s)))
+        return t.value
+
+    @property
+    def step_count(self):
+        t = C.c_double()
+        s = C.c_int()
+        _check(lib().mpmg_get_time(self._h, C.byref(t), C.byref(s)))
+        return s.value
+
+    def set_time(self, t, step_number):
+        _check(lib().mpmg_set_time(self._h, t, step_number))
+
+    def material_only(self):
+        _check(lib().mpmg_material_only(self._h))
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(lib().mpmg_get_stream(self._h, C.byref(s)))
+        return s.value
+
+    def enable_phase_timing(self, on=True):
+        _check(lib().mpmg_enable_phase_timing(self._h, 1 if on else 0))
+
+    def phase_times(self):
+        L = lib()
+        n = L.mpmg_phase_count()
+        ms = np.zeros(n)
+        cnt = (C.c_long * n)()
+        _check(L.mpmg_phase_times(self._h, _dptr(ms), cnt))
+        return {L.mpmg_phase_name(k).decode(): (ms[k], cnt[k]) for k in range(n)}
+
+    def last_solve(self):
+        it = C.c_int()
+        r = C.c_double()
+        rc = lib().mpmg_last_solve(self._h, C.byref(it), C.byref(r))
+        return rc, it.value, r.value
+
+    def launch_count(self, reset=False):
+        n = C.c_long()
+        _check(lib().mpmg_launch_count(self._h, C.byref(n), 1 if reset else 0))
+        return n.value

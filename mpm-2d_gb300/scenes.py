@@ -1,0 +1,106 @@
+"""Seeded synthetic inputs in the layouts the reference's generators use.
+
+The reference ships particle generators (generate_block_particles.py:26-51,
+examples/silo/generate_silo_particles.py): material points on a regular
+lattice of spacing s at (k + 1/2) s from the block's lower-left corner,
+ordered x-major, with mass rho s^2 and volume s^2.  The reference publishes no
+benchmark inputs, so every workload here is synthetic with those layouts.
+
+Workloads (sizes follow the configurations the benchmark plan names):
+  config1        isolin block in a box: 65x65 nodes on the unit square, block
+                 [0.25, 0.75] x [0, 0.5] at 2x2 particles per element (4096),
+                 jittered +-1e-3 (seeded), rho 1500, E 1e6, nu 0.3, dt 1e-5
+  box_fill       1 048 576 particles: 513x513 nodes, the whole unit square at
+                 2x2 per element, box walls (the "1 M particles" workload)
+  column         granular column collapse (g_local_mu2 constants of the
+                 benchmark: rho 2450, d 5.3e-4) on an Nx x Ny grid
+  silo           square-silo discharge fill (x < wall fraction, 2x2 per element)
+"""
+import numpy as np
+
+
+def block_particles(x0, y0, width, height, spacing, rho, jitter=0.0, seed=0, reflect_y=True):
+    """Lattice block in x-major order (generate_block_particles.py:26-51)."""
+    nx = int(np.floor(width / spacing + 1e-9))
+    ny = int(np.floor(height / spacing + 1e-9))
+    sx = (0.5 + np.arange(nx)) * spacing + x0
+    sy = (0.5 + np.arange(ny)) * spacing + y0
+    X, Y = np.meshgrid(sx, sy, indexing="ij")     # x-major: y varies fastest
+    x = X.ravel().copy()
+    y = Y.ravel().copy()
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        x += rng.uniform(-jitter, jitter, size=x.shape)
+        y += rng.uniform(-jitter, jitter, size=y.shape)
+        if reflect_y:
+            y = np.abs(y)
+    n = x.size
+    return {
+        "m": np.full(n, rho * spacing * spacing),
+        "v": np.full(n, spacing * spacing),
+        "x": x, "y": y,
+        "vx": np.zeros(n), "vy": np.zeros(n),
+        "sxx": np.zeros(n), "sxy": np.zeros(n), "syy": np.zeros(n),
+    }
+
+
+def config1(seed=0, gravity=None):
+    """Plain FP64 USL, isolin block in the box BC (4096 particles, 65^2 nodes)."""
+    N = 65
+    h = 1.0 / (N - 1)
+    p = block_particles(0.25, 0.0, 0.5, 0.5, h / 2, 1500.0, jitter=1e-3, seed=seed)
+    return {"Nx": N, "Ny": N, "h": h, "dt": 1e-5, "material": "isolin", "props": [1e6, 0.3],
+            "bc": "box", "bcf": [0.0, 0.0, 1.0, 1.0], "bci": [1, 3, 1, 0], "gravity": gravity,
+            "particles": p, "steps": 1000}
+
+
+def box_fill(cells=512, ppc_1d=2, material="g_local_mu2", rho=2450.0, props=(1e6, 0.3), dt=2e-6,
+             gravity=None, mp=None):
+    """The whole unit square filled at ppc_1d^2 particles per element."""
+    N = cells + 1
+    h = 1.0 / cells
+    p = block_particles(0.0, 0.0, 1.0, 1.0, h / ppc_1d, rho)
+    scene = {"Nx": N, "Ny": N, "h": h, "dt": dt, "material": material, "props": list(props),
+             "bc": "box", "bcf": [0.0, 0.0, 1.0, 1.0], "bci": [1, 3, 1, 0], "gravity": gravity,
+             "particles": p}
+    if mp:
+        scene["mp"] = dict(mp)
+    return scene
+
+
+def column(Nx=65, Ny=65, h=1.0 / 64, width=0.25, height=0.5, ppc_1d=2, material="g_local_mu2",
+           rho=2450.0, props=(1e6, 0.3), dt=1e-5, gravity=None, mp=None, jitter=0.0, seed=0):
+    """Granular column at the left wall of an Nx x Ny grid (box walls)."""
+    p = block_particles(0.0, 0.0, width, height, h / ppc_1d, rho, jitter=jitter, seed=seed)
+    scene = {"Nx": Nx, "Ny": Ny, "h": h, "xmax": (Nx - 1) * h if Nx != Ny else 1.0,
+             "ymax": (Ny - 1) * h if Nx != Ny else 1.0, "dt": dt, "material": material,
+             "props": list(props), "bc": "box", "bcf": [0.0, 0.0, 1.0, 1.0], "bci": [1, 3, 1, 0],
+             "gravity": gravity, "particles": p}
+    if mp:
+        scene["mp"] = dict(mp)
+    return scene
+
+
+def silo(cells=512, ppc_1d=2, hole_radius=0.06, open_time=0.1, wall_frac=0.8,
+         material="g_nonlocal_mu2", rho=2450.0, props=(1e6, 0.3), dt=1e-6, fill_height=None,
+         gravity=None, mp=None):
+    """Silo fill left of the wall column (square_silo.c:44), 2x2 per element."""
+    N = cells + 1
+    h = 1.0 / cells
+    wall_col = int((N - 1) * wall_frac)
+    width = wall_col * h
+    height = (cells - 1) * h if fill_height is None else fill_height
+    p = block_particles(0.0, 0.0, width, height, h / ppc_1d, rho)
+    scene = {"Nx": N, "Ny": N, "h": h, "dt": dt, "material": material, "props": list(props),
+             "bc": "square_silo", "bcf": [hole_radius, open_time, wall_frac], "bci": [],
+             "gravity": gravity, "particles": p}
+    if mp:
+        scene["mp"] = dict(mp)
+    return scene
+
+
+def with_particles(scene, idx):
+    """A copy of scene keeping only particles idx (for bounded samples)."""
+    out = dict(scene)
+    out["particles"] = {k: np.ascontiguousarray(v[idx]) for k, v in scene["particles"].items()}
+    return out
