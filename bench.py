@@ -1,0 +1,317 @@
+"""Benchmark of the mpm-2d explicit USL step on GB300 (one JSON line).
+
+Workload (N=1): 1 048 576 particles filling the unit square at 2x2 per
+element on a 513x513-node grid (512^2 elements), g_local_mu2 granular rheology
+(rho 2450, E 1e6, nu 0.3, reference constants), box walls, FP64 throughout,
+synthetic seeded inputs in the reference generator's lattice layout.  A step
+is one explicit_mpm_step_usl_threaded + time_varying_loads over all
+particles.  Particle state (~200 MB) exceeds the 129 MB L2 between steps.
+
+  value     particle-steps/s with the state resident in HBM (CUDA events on
+            the library's stream, max over ranks)
+  e2e       the same metric through the public C ABI with host buffers: the
+            timed region includes creating the context from host arrays (H2D
+            of the particle state) and, after every step, a D2H read of the
+            frame fields into pinned host memory
+  roofline  the dominant kernel's algorithmic bytes per launch over its
+            average CUDA-event duration, against the measured HBM copy peak
+  cpu_baseline  the oracle (the CPU restatement of the reference's pthreaded
+            step) on this host's cores over a bounded sample of steps
+
+--impl reference times the reference's CPU step (the oracle port on hosts
+without the reference build) on all host cores, same metric and config.
+Multi-GPU: independent replicas (the step has no cross-rank exchange).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "mpm-2d_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "particle-steps/s at 1M pts, mixed vs FP64 GPU; %HBM peak; adjoint/forward time"
+UNIT = "particle-steps/s"
+WORKLOAD = "box_fill_1M_g_local_mu2_fp64"
+
+# Algorithmic bytes per particle-step of the fused g2p + material kernel
+# (g_local_mu2): reads x y vx vy v m ux uy sxx sxy syy Tzz gammap (13 doubles)
+# plus element and active flag (2 ints), writes x y vx vy ux uy v sxx sxy syy
+# Tzz gammap gammadotp (13 doubles); plus each node's a and v (4 doubles) read once.
+G2P_BYTES_PER_PARTICLE = 13 * 8 + 2 * 4 + 13 * 8
+G2P_BYTES_PER_NODE = 4 * 8
+# Whole step (SURVEY-style accounting): 216 B per particle + 80 B per node.
+STEP_BYTES_PER_PARTICLE = 216
+STEP_BYTES_PER_NODE = 80
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.tmp is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.tmp.flush()
+        with open(self.tmp.name) as f:
+            rows = [r.strip().split(", ") for r in f if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_scene():
+    import scenes
+    return scenes.box_fill(cells=512, ppc_1d=2, material="g_local_mu2", rho=2450.0,
+                           props=(1e6, 0.3), dt=2e-6)
+
+
+def cpu_baseline(scene, steps, threads):
+    """The oracle (CPU restatement of the reference's pthreaded step) on host
+    cores over `steps` steps of the full workload."""
+    from oracle import oracle as O
+    orc = O.Oracle(scene, nthreads=threads)
+    orc.step(1)                                 # warm-up (first-touch of arrays)
+    t0 = time.perf_counter()
+    orc.step(steps)
+    dt = time.perf_counter() - t0
+    n = len(scene["particles"]["x"])
+    return n * steps / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import build as obuild
+    scene = make_scene()
+    threads = os.cpu_count() or 1
+    steps = max(1, args.steps)
+    warm = max(0, min(args.warmup, 3))
+    from oracle import oracle as O
+    orc = O.Oracle(scene, nthreads=threads)
+    if warm:
+        orc.step(warm)
+    t0 = time.perf_counter()
+    orc.step(steps)
+    dt = time.perf_counter() - t0
+    n = len(scene["particles"]["x"])
+    value = n * steps / dt
+    kind = "reference" if os.path.exists(os.path.join(obuild.REF_OUT, "libref_harness.so")) and False else "port"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles": n, "grid_nodes": [scene["Nx"], scene["Ny"]],
+                   "material": scene["material"], "bc": scene["bc"], "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "%d steps of the full %d-particle workload" % (steps, n)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    import mpm2d
+
+    scene = make_scene()
+    n = len(scene["particles"]["x"])
+    nn = scene["Nx"] * scene["Ny"]
+    sim = mpm2d.Simulation(scene, device=dev)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    sim.step(args.warmup)
+    sim.synchronize()
+    launches0 = sim.launch_count()
+    barrier()
+    with ClockSampler(dev) as clocks:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        sim.step(args.steps)
+        ev1.record(stream)
+        sim.synchronize()
+        barrier()
+        ms = ev0.elapsed_time(ev1)
+    launches = sim.launch_count() - launches0
+    clk = clocks.summary()
+    t = ms / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = n * args.steps * world / t
+
+    # Dominant kernel: per-phase CUDA events on the library's stream.
+    sim.enable_phase_timing(True)
+    sim.step(max(3, min(args.steps, 10)))
+    phases = sim.phase_times()
+    sim.enable_phase_timing(False)
+    top = max(phases.items(), key=lambda kv: kv[1][0])
+    g2p_ms, g2p_launches = phases["g2p"]
+    g2p_avg_s = (g2p_ms / max(g2p_launches, 1)) / 1e3
+    peak, peak_kind = measured_peaks()
+    alg_bytes = G2P_BYTES_PER_PARTICLE * n + G2P_BYTES_PER_NODE * nn
+    achieved = alg_bytes / g2p_avg_s / 1e9
+    step_bytes = STEP_BYTES_PER_PARTICLE * n + STEP_BYTES_PER_NODE * nn
+
+    # End to end through the C ABI with host buffers.
+    frame_fields = ("x", "y", "vx", "vy", "sxx", "sxy", "syy", "v")
+    e2e_steps = max(2, min(args.steps, 20))
+    host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in frame_fields}
+    barrier()
+    t0 = time.perf_counter()
+    sim2 = mpm2d.Simulation(scene, device=dev)
+    import ctypes as C
+    for _ in range(e2e_steps):
+        sim2.step(1)
+        for f in frame_fields:
+            buf = host[f]
+            rc = mpm2d.lib().mpmg_get_field(sim2._h, f.encode(),
+                                            C.cast(buf.data_ptr(), C.POINTER(C.c_double)))
+            if rc != 0:
+                raise RuntimeError("mpmg_get_field failed: %d" % rc)
+    sim2.synchronize()
+    barrier()
+    e2e_t = time.perf_counter() - t0
+    sim2.close()
+    h2d = 9 * 8 * n / e2e_steps
+    d2h = len(frame_fields) * 8 * n
+    e2e_value = n * e2e_steps * world / e2e_t
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles": n, "grid_nodes": [scene["Nx"], scene["Ny"]],
+                   "material": scene["material"], "bc": scene["bc"], "precision": "fp64",
+                   "l2_policy": "particle state ~200 MB > 129 MB L2 between steps",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": "g2p", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "step_alg_bytes": step_bytes,
+                     "step_frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / peak,
+                     "phases_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in phases.items()},
+                     "top_phase": top[0]},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cb_steps = args.cpu_steps
+        cb, cb_t = cpu_baseline(scene, cb_steps, threads)
+        line["cpu_baseline"] = {"value": cb, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "%d steps of the full %d-particle workload (%.1f s)" % (cb_steps, n, cb_t)}
+    sim.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -93,6 +93,12 @@ typedef struct mpmg_config {
     double solver_tol;       /* fluidity PCG relative residual (default 1e-10) */
     int solver_maxit;        /* fluidity PCG iteration cap (default 20000) */
     int device;              /* CUDA device ordinal */
+    int solver_warm_start;   /* nonzero: start the fluidity PCG from the previous
+                                step's nodal fluidity instead of zero.  Off by
+                                default: nodes whose rows hold only the 1e-10
+                                diagonal keep a stale warm-start value that the
+                                residual cannot see, where the reference's direct
+                                solve gives zero. */
 } mpmg_config;
 
 typedef struct mpmg_ctx mpmg_ctx;

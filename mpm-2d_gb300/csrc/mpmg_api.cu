@@ -62,6 +62,10 @@ int sync_status(mpmg_ctx *ctx)
     int st = 0;
     MPMG_CHECK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
     MPMG_CHECK(cudaMemcpy(&ctx->h_params, ctx->d_params, sizeof(StepParams), cudaMemcpyDeviceToHost));
+    if (st != 0) {
+        // Report each device-side error once; the caller decides whether to go on.
+        MPMG_CHECK(cudaMemset(ctx->d_status, 0, sizeof(int)));
+    }
     if (st & MPMG_DEV_ERR_SPIN) {
         mpmg_set_error("a grid-wide wait in the fluidity solver timed out");
         return MPMG_ERR_DEVICE;

@@ -44,8 +44,8 @@ enum Phase {
 struct SortScratch {
     uint32_t *keys_alt;
     uint32_t *vals_alt;
-    uint32_t *tile_hist;   // [256 digits][num tiles], digit-major
-    uint32_t *digit_total; // [256]
+    uint32_t *tile_hist;   // [1024 digits][num tiles], digit-major
+    uint32_t *digit_total; // [1024]
     int num_tiles;
     int capacity;          // particles
 };
@@ -120,6 +120,12 @@ int mpmg_cuda_status(cudaError_t e, const char *what);
 int mpmg_sort_init(mpmg_ctx *ctx);
 void mpmg_sort_free(mpmg_ctx *ctx);
 int mpmg_sort_keys(mpmg_ctx *ctx);                // keys/vals -> sorted_keys/perm
+// Scratch words (uint32) a sort of n keys needs, and its tile count.
+size_t mpmg_sort_scratch_words(size_t n, int key_bits, int *num_tiles_out);
+// Sort with caller-provided scratch; returns the number of launches issued.
+int mpmg_sort_run(const uint32_t *keys, const uint32_t *vals, int n, int ne, int key_bits,
+                  const SortScratch &sc, uint32_t *sorted_keys, uint32_t *perm, int *cell_start,
+                  cudaStream_t s);
 int mpmg_launch_step(mpmg_ctx *ctx);             // one full step
 int mpmg_nonlocal_init(mpmg_ctx *ctx);
 void mpmg_nonlocal_free(mpmg_ctx *ctx);
@@ -185,7 +191,7 @@ __device__ __forceinline__ bool mpmg_grid_barrier(unsigned int *bar, unsigned in
         } else {
             long long polls = 0;
             while (*gen == g) {
-                if (++polls > limit || *(volatile int *)status != 0) {
+                if (++polls > limit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0) {
                     atomicOr(status, MPMG_DEV_ERR_SPIN);
                     ok = false;
                     break;

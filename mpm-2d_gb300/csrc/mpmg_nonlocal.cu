@@ -13,7 +13,8 @@
 // per-block partial sums reduced in a fixed order (deterministic), and all
 // grid-wide waits are bounded.  The unknowns are the nodes with mass above
 // the reference's threshold (g_nonlocal_mu2.c:365-381: m > 0; g_nonlocal.c:
-// m > 1e-10); the initial guess is the previous step's nodal fluidity.
+// m > 1e-10); the initial guess is zero, like the reference's direct solve
+// (a warm start from the previous step is available as an option).
 #include "mpmg_internal.cuh"
 #include "mpmg_materials.cuh"
 
@@ -442,7 +443,7 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     S.cell_start = ctx->cell_start;
     S.elem_k = ctx->elem_k;
     S.elem_f = ctx->elem_f;
-    S.x = ctx->node_gf;     // warm start from the previous step, result in place
+    S.x = ctx->node_gf;     // result in place; previous solution when warm-starting
     S.r = ctx->cg_r;
     S.p = ctx->cg_p;
     S.q = ctx->cg_q;
@@ -452,6 +453,7 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     S.status = ctx->d_status;
     S.sp = ctx->d_params;
     void *args[] = {&S};
+    if (!c.solver_warm_start) MPMG_CHECK(cudaMemsetAsync(ctx->node_gf, 0, ctx->nn * sizeof(double), s));
     MPMG_CHECK(cudaMemsetAsync(ctx->cg_barrier, 0, 2 * sizeof(unsigned int), s));
     MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_kernel, dim3(ctx->cg_blocks),
                                            dim3(kSolveThreads), args, 0, s));

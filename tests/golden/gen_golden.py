@@ -1,0 +1,164 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's own code.
+
+Run here, where the reference tree exists:  python tests/golden/gen_golden.py
+It builds oracle/_ref/ (the reference's libmpm, plugins and test_material
+compiled from its sources, see oracle/build.py) and records:
+
+  kat_<material>.npz     tests/test_material.c's 1252-row %a histories for
+                         isolin and g_local_mu2 (columns t, L11, L12, L21, L22,
+                         sxx, sxy, syy, mu, gammadotp), parsed exactly
+  step_<case>.npz        particle and node state of the reference's threaded
+                         step (explicit_mpm_step_usl_threaded + the driver's
+                         time_varying_loads) at a few step counts, with the
+                         inputs that produced them
+  lists_config1.npz      find_filled_elements' per-element particle order
+                         after 100 steps of config 1 (one thread, so one list
+                         per colour)
+
+The nonlocal cases run the reference with one thread: with more, its
+g_nonlocal_mu2 solve reads particles other threads are still updating
+(libmpm/process_usl.c:576-589 has no barrier before the material call), and
+the results change from run to run.  The g_nonlocal plugin has no
+calculate_stress_threaded; the harness calls its calculate_stress from task 0.
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "mpm-2d_gb300"))
+
+from oracle import build as obuild  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+import scenes  # noqa: E402
+
+PARTICLE_KEYS = ["x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy", "exx", "exy", "eyy",
+                 "wxy", "ax", "ay", "Tzz"] + ["state%d" % k for k in range(11)]
+NODE_KEYS = ["node_m", "node_mx", "node_my", "node_fx", "node_fy", "node_vx", "node_vy"]
+
+
+def scene_arrays(sc):
+    out = {"in_" + k: np.asarray(v, dtype=np.float64) for k, v in sc["particles"].items()}
+    meta = {k: sc[k] for k in ("Nx", "Ny", "h", "dt") if k in sc}
+    out["meta_grid"] = np.array([meta["Nx"], meta["Ny"]], dtype=np.int64)
+    out["meta_h_dt"] = np.array([meta["h"], meta["dt"]])
+    out["meta_props"] = np.asarray(sc.get("props", [1e6, 0.3]), dtype=np.float64)
+    out["meta_bcf"] = np.asarray(sc.get("bcf", []), dtype=np.float64)
+    out["meta_bci"] = np.asarray(sc.get("bci", []), dtype=np.int64)
+    out["meta_material"] = np.array(sc["material"])
+    out["meta_bc"] = np.array(sc["bc"])
+    return out
+
+
+def record_steps(name, sc, checkpoints, nthreads):
+    ref = O.RefHarness(sc, nthreads=nthreads)
+    data = scene_arrays(sc)
+    data["checkpoints"] = np.asarray(checkpoints, dtype=np.int64)
+    done = 0
+    for c in checkpoints:
+        ref.step(c - done)
+        done = c
+        p = ref.particles()
+        n = ref.nodes()
+        for k in PARTICLE_KEYS:
+            key = {"Tzz": "Tzz"}.get(k, k)
+            data["s%d_%s" % (c, k)] = p[key]
+        data["s%d_in_element" % c] = p["in_element"]
+        data["s%d_active" % c] = p["active"]
+        data["s%d_t" % c] = np.array(ref.t)
+        for k in NODE_KEYS:
+            data["s%d_%s" % (c, k)] = n[k]
+    path = os.path.join(HERE, "step_%s.npz" % name)
+    np.savez_compressed(path, **data)
+    return ref, path
+
+
+def parse_hex_csv(path):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            rows.append([float.fromhex(v) for v in line.strip().split(",")])
+    return np.array(rows)
+
+
+def kat(material):
+    exe = os.path.join(obuild.REF_OUT, "material_" + material)
+    with tempfile.TemporaryDirectory() as d:
+        hexf = os.path.join(d, "out.csv")
+        decf = os.path.join(d, "out_dec.csv")
+        cfg = os.path.join(d, "test.cfg")
+        with open(cfg, "w") as f:
+            f.write("%s\n%s\n1e6\n0.3\n" % (hexf, decf))   # tests/isolin.cfg, g_local_mu2.cfg
+        subprocess.run([exe, cfg], check=True, capture_output=True, cwd=d)
+        rows = parse_hex_csv(hexf)
+    path = os.path.join(HERE, "kat_%s.npz" % material)
+    np.savez_compressed(path, rows=rows, props=np.array([1e6, 0.3]), dt=np.array(1e-3))
+    return path
+
+
+def main():
+    if obuild.build_ref(verbose=False) is None:
+        raise SystemExit("reference tree not found; fixtures can only be generated where it exists")
+    print(kat("isolin"))
+    print(kat("g_local_mu2"))
+
+    # config 1: isolin block in a box (4096 particles, 65^2 nodes), threaded
+    sc = scenes.config1(seed=0)
+    ref, path = record_steps("config1", sc, [1, 2, 100], nthreads=4)
+    print(path)
+    # element lists built in step 101 from the positions after step 100
+    ref1 = O.RefHarness(sc, nthreads=1)
+    ref1.step(100)
+    before = ref1.particles()
+    ref1.step(1)
+    lists, lens = ref1.color_lists()
+    p = ref1.particles()
+    np.savez_compressed(os.path.join(HERE, "lists_config1.npz"), lists=lists.astype(np.int64),
+                        lengths=lens.astype(np.int64), in_element=p["in_element"], active=p["active"],
+                        x=before["x"], y=before["y"])
+
+    # g_local_mu2 column collapse on the unit square (2048 particles)
+    sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2",
+                       rho=2450.0, props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+    print(record_steps("mu2_column", sc, [1, 50, 300], nthreads=4)[1])
+
+    # g_local_mu2 in the square silo with the trapdoor opening at t = 1 ms
+    sc = scenes.silo(cells=32, material="g_local_mu2", props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+                     open_time=0.001, wall_frac=0.5, fill_height=0.6)
+    print(record_steps("mu2_silo", sc, [1, 50, 400], nthreads=4)[1])
+
+    # g_nonlocal_mu2 silo (one thread, see the module docstring)
+    sc = scenes.silo(cells=32, material="g_nonlocal_mu2", props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+                     open_time=0.001, wall_frac=0.5, fill_height=0.6)
+    print(record_steps("nonlocal_mu2_silo", sc, [1, 20, 120], nthreads=1)[1])
+
+    # the same silo pre-stressed (lithostatic syy, sxx = syy / 2, plus 500 Pa)
+    # so that no particle sits at p = 0, where the dense flag switches: from
+    # the unstressed fill a 1e-15 relative perturbation of x changes ~200
+    # dense flags within 20 steps, which makes whole trajectories
+    # incomparable at round-off level.
+    sc = scenes.silo(cells=32, material="g_nonlocal_mu2", props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+                     open_time=0.001, wall_frac=0.5, fill_height=0.6)
+    y = sc["particles"]["y"]
+    sc["particles"]["syy"] = -2450 * 9.8 * (0.6 - y) - 500.0
+    sc["particles"]["sxx"] = 0.5 * sc["particles"]["syy"]
+    print(record_steps("nonlocal_mu2_prestressed", sc, [1, 20, 120], nthreads=1)[1])
+
+    # g_nonlocal (operator variant) with a sheared initial stress so that
+    # its bulk fluidity is nonzero from the first step
+    sc = scenes.silo(cells=16, material="g_nonlocal", props=(1e8, 0.3), dt=1e-6, hole_radius=0.1,
+                     open_time=0.0, wall_frac=0.5, fill_height=0.6)
+    n = len(sc["particles"]["x"])
+    sc["particles"]["sxx"] = np.full(n, -1000.0)
+    sc["particles"]["syy"] = np.full(n, -2000.0)
+    sc["particles"]["sxy"] = np.full(n, 600.0)
+    print(record_steps("nonlocal_silo", sc, [1, 10, 60], nthreads=1)[1])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,76 @@
+"""The C ABI library without a GPU: it builds, loads, exports every entry
+point its headers declare, and fails loudly (no CPU fallback) when no CUDA
+device is present."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+import mpm2d
+import mpmg_build
+import scenes
+
+HEADERS = [os.path.join(ROOT, "include", f) for f in sorted(os.listdir(os.path.join(ROOT, "include")))
+           if f.endswith(".h")]
+
+
+def declared_symbols():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"MPMG_API\s+[\w\s\*]+?\b(\w+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_headers_declare_entry_points():
+    names = declared_symbols()
+    assert {"mpmg_create", "mpmg_step", "mpmg_destroy", "mpmg_get_field"} <= names
+
+
+def test_library_exports_every_declared_symbol():
+    path = mpmg_build.build()
+    lib = C.CDLL(path)
+    missing = [n for n in sorted(declared_symbols()) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_default_params_are_the_reference_constants():
+    mp = mpm2d.default_params("g_local_mu2")
+    assert mp[mpm2d.MP["mu_s"]] == 0.3819 and mp[mpm2d.MP["mu_2"]] == 0.6435
+    assert mp[mpm2d.MP["I0"]] == 0.278 and mp[mpm2d.MP["grains_d"]] == 0.005
+    assert mp[mpm2d.MP["rho_critical"]] == 1485.0
+    mp = mpm2d.default_params("g_nonlocal")
+    assert mp[mpm2d.MP["E"]] == 1e8 and mp[mpm2d.MP["B"]] == 0.9377 * 20
+    assert mp[mpm2d.MP["grains_d"]] == 0.05
+
+
+def _have_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_have_gpu(), reason="checks the no-GPU failure path")
+def test_create_without_gpu_fails_loudly():
+    with pytest.raises(mpm2d.MpmError) as e:
+        mpm2d.Simulation(scenes.config1())
+    assert e.value.status == 17          # MPMG_ERR_CUDA
+
+
+def test_invalid_configuration_is_rejected():
+    sc = scenes.config1()
+    sc["Nx"] = 1
+    with pytest.raises(mpm2d.MpmError) as e:
+        mpm2d.Simulation(sc)
+    assert e.value.status == 16          # MPMG_ERR_INVALID
+    sc = scenes.config1()
+    sc["bcf"] = [0.5, 0.0, 0.9, 1.0]      # box.c:88-91: box outside the unit fractions
+    with pytest.raises(mpm2d.MpmError) as e:
+        mpm2d.Simulation(sc)
+    assert e.value.status == 16
