@@ -173,6 +173,34 @@ MPMG_API int mpmg_last_solve(mpmg_ctx *ctx, int *iterations, double *rel_residua
    created (or since the last reset). */
 MPMG_API int mpmg_launch_count(mpmg_ctx *ctx, long *launches, int reset);
 
+/*
+ * Cell sort without any allocation.  No counterpart in the reference: it is
+ * the element binning every mpmg_step performs (the GPU form of
+ * find_filled_elements, libmpm/process_usl.c:677-723), offered to callers
+ * that cannot call cudaMalloc -- code inside a CUDA stream capture, hosts
+ * whose device memory belongs to their own pool allocator, and the
+ * reference's dlopen'd plugins, which own no device memory.
+ *
+ * d_keys holds n element keys on the device (num_elements marks a particle
+ * outside the grid).  Outputs, also device arrays the caller provides: the
+ * keys sorted stably (d_sorted_keys, n), the permutation from sorted
+ * position to particle index (d_perm, n) and the start of every element's
+ * run (d_cell_start, num_elements + 1).  Work is queued on `stream` (a
+ * cudaStream_t; NULL for the default stream) and is complete when the
+ * stream is.
+ *
+ * Scratch is a fixed device array inside this library, held by every GPU that
+ * loads it until the process exits; n above MPMG_NOALLOC_MAX_PARTICLES is
+ * rejected with MPMG_ERR_SCRATCH_LIMIT.  The first call on a device looks up
+ * that array's device address, so make the first call on each device before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race, so serialise them.  The entry point calls no cudaMalloc or
+ * cudaFree.
+ */
+#define MPMG_NOALLOC_MAX_PARTICLES (1u << 20)
+MPMG_API int mpmg_sort_cells_noalloc(const int *d_keys, int n, int num_elements, int *d_sorted_keys,
+                                     int *d_perm, int *d_cell_start, void *stream);
+
 MPMG_API const char *mpmg_status_string(int status);
 /* Text of the last error on this thread (CUDA error text or argument check). */
 MPMG_API const char *mpmg_last_error(void);
