@@ -11,7 +11,7 @@
  *
  * Reference interfaces each call replaces (paths inside neocpp89/mpm-2d):
  *   mpmg_create      mpm_init (libmpm/process_usl.c:68-280) + material_init
- *                    (materialsrc/*.c) + bc_validate (bcsrc/*.c), with the
+ *                    (the material plugins) + bc_validate (the BC plugins), with the
  *                    driver's dt (src/main.c:742)
  *   mpmg_step        the driver loop body (src/main.c:946-977):
  *                    explicit_mpm_step_usl_threaded (process_usl.c:465-592)

@@ -18,7 +18,8 @@ LIB = os.path.join(OUT, "libmpm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-I", INCLUDE]
-CU_SOURCES = ["mpmg_api.cu", "mpmg_step.cu", "mpmg_sort.cu", "mpmg_nonlocal.cu", "mpmg_sort_noalloc.cu"]
+CU_SOURCES = ["mpmg_api.cu", "mpmg_step.cu", "mpmg_sort.cu", "mpmg_nonlocal.cu", "mpmg_sort_noalloc.cu",
+              "mpmg_libmpm.cu"]
 CPP_SOURCES = []
 
 
