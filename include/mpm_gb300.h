@@ -67,6 +67,17 @@ enum mpmg_gravity {
     MPMG_GRAVITY_CONSTANT = 1         /* mpmg_config.gravity from step 1 on */
 };
 
+/* Arithmetic of the step.  MPMG_PRECISION_FP64 is the reference's (FP64
+   everywhere).  MPMG_PRECISION_MIXED keeps particle state, shape functions,
+   P2G and G2P contributions and the material update in FP32, and nodal mass
+   and momentum sums and the division by nodal mass in FP64; particles are
+   kept in element order on the device (read-back returns the caller's
+   order).  Mixed supports the local materials (isolin, g_local_mu2). */
+enum mpmg_precision {
+    MPMG_PRECISION_FP64 = 0,
+    MPMG_PRECISION_MIXED = 1
+};
+
 /* Material parameter slots (mpmg_config.mp).  mpmg_default_params fills the
    reference's compile-time constants for a material kind. */
 enum mpmg_mparam {
@@ -99,6 +110,7 @@ typedef struct mpmg_config {
                                 diagonal keep a stale warm-start value that the
                                 residual cannot see, where the reference's direct
                                 solve gives zero. */
+    int precision;           /* enum mpmg_precision */
 } mpmg_config;
 
 typedef struct mpmg_ctx mpmg_ctx;

@@ -187,7 +187,10 @@ int mpmg_cuda_status(cudaError_t e, const char *what)
 
 void mpmg_phase_begin(mpmg_ctx *ctx, int phase)
 {
-    if (ctx->timing) cudaEventRecord(ctx->ev[2 * phase], ctx->stream);
+    if (ctx->timing) {
+        cudaEventRecord(ctx->ev[2 * phase], ctx->stream);
+        ctx->phase_used[phase] = 1;
+    }
 }
 
 void mpmg_phase_end(mpmg_ctx *ctx, int phase)
@@ -298,6 +301,7 @@ int mpmg_destroy(mpmg_ctx *ctx)
     cudaFree(ctx->d_status);
     mpmg_sort_free(ctx);
     mpmg_nonlocal_free(ctx);
+    mpmg_mixed_free(ctx);
     for (int k = 0; k < 2 * PH_COUNT; k++)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -394,6 +398,43 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
     {
         const bool transients = cfg->store_transients != 0;
         const bool nonlocal = cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL;
+        const bool mixed = cfg->precision == MPMG_PRECISION_MIXED;
+        if (mixed && nonlocal) {
+            mpmg_set_error("mixed precision supports isolin and g_local_mu2");
+            rc = MPMG_ERR_UNSUPPORTED;
+            goto fail;
+        }
+        if (mixed) {
+            // FP32 particle state lives in ctx->mixed; the context keeps the
+            // sort, the FP64 nodal mass and the step parameters.
+            TRY(dalloc(&ctx->in_element, n));
+            TRY(dalloc(&ctx->active, n));
+            TRY(dalloc(&ctx->vals, n));
+            TRY(dalloc(&ctx->sorted_keys, n));
+            TRY(dalloc(&ctx->perm, n));
+            TRY(dalloc(&ctx->cell_start, ctx->ne + 1));
+            TRY(dalloc(&ctx->node_m, ctx->nn));
+            if (transients) {
+                double **tn[] = {&ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy};
+                for (double **p : tn) TRY(dalloc(p, ctx->nn));
+            }
+            TRY(dalloc(&ctx->d_params, 1));
+            TRY(dalloc(&ctx->d_status, 1));
+            TRY(mpmg_sort_init(ctx));
+            TRY(fill_zero(ctx, ctx->cell_start, (ctx->ne + 1) * sizeof(int)));
+            TRY(fill_zero(ctx, ctx->node_m, ctx->nn * sizeof(double)));
+            TRY(fill_zero(ctx, ctx->d_status, sizeof(int)));
+            StepParams p0 = {};
+            p0.gravity = (cfg->gravity_mode == MPMG_GRAVITY_CONSTANT) ? cfg->gravity : 0.0;
+            ctx->h_params = p0;
+            MPMG_CHECK(cudaMemcpyAsync(ctx->d_params, &ctx->h_params, sizeof(StepParams),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+            TRY(mpmg_mixed_init(ctx, m, v, x, y, vx, vy, sxx, sxy, syy));
+            rc = sync_status(ctx);
+            if (rc != MPMG_OK) goto fail;
+            *out = ctx;
+            return MPMG_OK;
+        }
         double **always[] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->m, &ctx->v, &ctx->v0,
                              &ctx->sxx, &ctx->sxy, &ctx->syy, &ctx->ux, &ctx->uy};
         for (double **p : always) TRY(dalloc(p, n));
@@ -502,13 +543,13 @@ int mpmg_step(mpmg_ctx *ctx, int nsteps)
     if (ctx == nullptr || nsteps < 0) return MPMG_ERR_INVALID;
     MPMG_CHECK(cudaSetDevice(ctx->dev));
     for (int k = 0; k < nsteps; k++) {
-        int rc = mpmg_launch_step(ctx);
+        for (int ph = 0; ph < PH_COUNT; ph++) ctx->phase_used[ph] = 0;
+        int rc = ctx->mixed ? mpmg_mixed_step(ctx) : mpmg_launch_step(ctx);
         if (rc != MPMG_OK) return rc;
         if (ctx->timing) {
             MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
-            const bool nonlocal = ctx->cfg.material == MPMG_G_NONLOCAL_MU2 || ctx->cfg.material == MPMG_G_NONLOCAL;
             for (int ph = 0; ph < PH_COUNT; ph++) {
-                if (ph == PH_FLUIDITY && !nonlocal) continue;
+                if (!ctx->phase_used[ph]) continue;
                 float ms = 0;
                 MPMG_CHECK(cudaEventElapsedTime(&ms, ctx->ev[2 * ph], ctx->ev[2 * ph + 1]));
                 ctx->phase_ms[ph] += ms;
@@ -531,7 +572,14 @@ int mpmg_get_field(mpmg_ctx *ctx, const char *name, double *host_out)
     if (ctx == nullptr || name == nullptr || host_out == nullptr) return MPMG_ERR_INVALID;
     MPMG_CHECK(cudaSetDevice(ctx->dev));
     FieldRef f;
-    int rc = find_field(ctx, name, &f, false);
+    int rc;
+    if (ctx->mixed) {
+        rc = sync_status(ctx);
+        if (rc != MPMG_OK) return rc;
+        rc = mpmg_mixed_get(ctx, name, host_out);
+        if (rc != MPMG_ERR_UNKNOWN_FIELD) return rc;
+    }
+    rc = find_field(ctx, name, &f, false);
     if (rc != MPMG_OK) return rc;
     rc = sync_status(ctx);
     if (rc != MPMG_OK && rc != MPMG_ERR_SOLVER) return rc;
@@ -550,6 +598,7 @@ int mpmg_set_field(mpmg_ctx *ctx, const char *name, const double *host_in)
 {
     if (ctx == nullptr || name == nullptr || host_in == nullptr) return MPMG_ERR_INVALID;
     MPMG_CHECK(cudaSetDevice(ctx->dev));
+    if (ctx->mixed) return mpmg_mixed_set(ctx, name, host_in);
     FieldRef f;
     int rc = find_field(ctx, name, &f, true);
     if (rc != MPMG_OK) return rc;
@@ -563,6 +612,7 @@ int mpmg_get_map(mpmg_ctx *ctx, int *in_element, int *active)
 {
     if (ctx == nullptr) return MPMG_ERR_INVALID;
     MPMG_CHECK(cudaSetDevice(ctx->dev));
+    if (ctx->mixed) return mpmg_mixed_get_map(ctx, in_element, active);
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
     if (in_element && ctx->np)
         MPMG_CHECK(cudaMemcpy(in_element, ctx->in_element, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
@@ -574,6 +624,10 @@ int mpmg_get_map(mpmg_ctx *ctx, int *in_element, int *active)
 int mpmg_set_map(mpmg_ctx *ctx, const int *in_element, const int *active)
 {
     if (ctx == nullptr || in_element == nullptr || active == nullptr) return MPMG_ERR_INVALID;
+    if (ctx->mixed) {
+        mpmg_set_error("the mixed-precision form derives the element map from positions");
+        return MPMG_ERR_UNSUPPORTED;
+    }
     for (size_t i = 0; i < ctx->np; i++) {
         if (active[i] && (in_element[i] < 0 || (size_t)in_element[i] >= ctx->ne)) {
             mpmg_set_error("active particle %zu has element %d outside the grid", i, in_element[i]);
@@ -596,8 +650,20 @@ int mpmg_get_sort(mpmg_ctx *ctx, int *sorted_keys, int *perm, int *cell_start)
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
     if (sorted_keys && ctx->np)
         MPMG_CHECK(cudaMemcpy(sorted_keys, ctx->sorted_keys, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
-    if (perm && ctx->np)
+    if (perm && ctx->np) {
         MPMG_CHECK(cudaMemcpy(perm, ctx->perm, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+        if (ctx->mixed) {
+            // The mixed form's permutation indexes the storage it sorted (the
+            // buffer before the last step's swap); report particle indices.
+            int *pid = new int[ctx->np];
+            cudaError_t e = cudaMemcpy(pid, ctx->mixed->pid[1 - ctx->mixed->cur], ctx->np * sizeof(int),
+                                       cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess)
+                for (size_t k = 0; k < ctx->np; k++) perm[k] = pid[perm[k]];
+            delete[] pid;
+            if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed permutation read-back");
+        }
+    }
     if (cell_start)
         MPMG_CHECK(cudaMemcpy(cell_start, ctx->cell_start, (ctx->ne + 1) * sizeof(int), cudaMemcpyDeviceToHost));
     return MPMG_OK;
@@ -622,6 +688,12 @@ int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number)
     MPMG_CHECK(cudaMemcpy(&ctx->h_params, ctx->d_params, sizeof(StepParams), cudaMemcpyDeviceToHost));
     ctx->h_params.t = t;
     ctx->h_params.step_count = step_number;
+    // body force the next step uses (the FP64 form recomputes it on the device)
+    if (ctx->cfg.gravity_mode == MPMG_GRAVITY_CONSTANT) ctx->h_params.gravity = ctx->cfg.gravity;
+    else if (step_number == 0) ctx->h_params.gravity = 0.0;
+    else if ((0.1 + ctx->h_params.step_start_time) > t)
+        ctx->h_params.gravity = -9.8 * ((t - ctx->h_params.step_start_time) / 0.1);
+    else ctx->h_params.gravity = -9.8;
     MPMG_CHECK(cudaMemcpy(ctx->d_params, &ctx->h_params, sizeof(StepParams), cudaMemcpyHostToDevice));
     return MPMG_OK;
 }
@@ -638,8 +710,8 @@ int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *
 int mpmg_material_only(mpmg_ctx *ctx)
 {
     if (ctx == nullptr) return MPMG_ERR_INVALID;
-    if (ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2) {
-        mpmg_set_error("material-only update is defined for local materials");
+    if ((ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2) || ctx->mixed) {
+        mpmg_set_error("material-only update is defined for local materials in FP64");
         return MPMG_ERR_UNSUPPORTED;
     }
     MPMG_CHECK(cudaSetDevice(ctx->dev));

@@ -50,6 +50,19 @@ struct SortScratch {
     int capacity;          // particles
 };
 
+// Mixed-precision particle storage: FP32 structure of arrays kept in element
+// order, double-buffered (the G2P reads buffer `cur` through the sort's
+// permutation and writes buffer 1 - cur in sorted order).
+struct MixedState {
+    float *x[2], *y[2], *vx[2], *vy[2], *m[2], *v[2], *sxx[2], *sxy[2], *syy[2];
+    float *ux[2], *uy[2], *Tzz[2], *gp[2], *gdp[2];
+    int *pid[2];           // caller's particle index of each stored particle
+    int cur;
+    int keys_valid;        // keys/vals hold the element keys of buffer cur
+    float *cell_sums;      // 20 FP32 corner sums per element, value-major
+    float *node_ax, *node_ay, *node_vx, *node_vy;
+};
+
 struct mpmg_ctx {
     mpmg_config cfg;
     int dev;
@@ -98,8 +111,12 @@ struct mpmg_ctx {
     StepParams h_params;   // host mirror, refreshed on read-back
     int *d_status;
 
+    // Mixed precision (cfg.precision == MPMG_PRECISION_MIXED).
+    MixedState *mixed;
+
     // Timing.
     int timing;
+    int phase_used[PH_COUNT];
     cudaEvent_t ev[2 * PH_COUNT];
     double phase_ms[PH_COUNT];
     long phase_launches[PH_COUNT];
@@ -131,6 +148,16 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx);
 void mpmg_nonlocal_free(mpmg_ctx *ctx);
 int mpmg_launch_fluidity(mpmg_ctx *ctx);         // nonlocal: assembly, solve, stress
 int mpmg_launch_material_only(mpmg_ctx *ctx);
+int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const double *x, const double *y,
+                    const double *vx, const double *vy, const double *sxx, const double *sxy,
+                    const double *syy);
+void mpmg_mixed_free(mpmg_ctx *ctx);
+int mpmg_mixed_step(mpmg_ctx *ctx);
+// Host read-back / write of a mixed particle or node field; returns
+// MPMG_ERR_UNKNOWN_FIELD for names the mixed state does not hold.
+int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out);
+int mpmg_mixed_set(mpmg_ctx *ctx, const char *name, const double *in);
+int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active);
 
 void mpmg_phase_begin(mpmg_ctx *ctx, int phase);
 void mpmg_phase_end(mpmg_ctx *ctx, int phase);

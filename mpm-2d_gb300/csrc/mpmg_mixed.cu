@@ -1,0 +1,720 @@
+// Mixed-precision explicit USL step (MPMG_PRECISION_MIXED).
+//
+// Same phases as the FP64 step (mpmg_step.cu), re-laid out for bandwidth:
+//   * Particle state is FP32.  Positions are stored as the element index plus
+//     FP32 local coordinates xl, yl in [0, 1) (the coordinates the reference's
+//     shape functions use, particle.c:14-30), so the shape functions need no
+//     subtraction and a position keeps ~1e-7 h of resolution anywhere in the
+//     domain.  A particle that leaves the grid (process_usl.c:660-666) keeps
+//     its global position in the xl, yl slots and the element sentinel.
+//   * The stored element index is the sort key: there is no separate keys
+//     pass, and the permutation's values are the constant storage positions.
+//   * The G2P runs over sorted positions and writes every particle to its
+//     sorted position in the other buffer, so the storage stays in element
+//     order from step to step at no extra traffic and the next step's gathers
+//     through the permutation are nearly sequential.
+//   * P2G corner sums of an element's particle segment are FP32 (a few
+//     particles each); the four elements around a node are summed in FP64 for
+//     mass and momentum, the momentum update and the division by nodal mass
+//     are FP64, and the node's acceleration and velocity are stored in FP32
+//     for the gathers.
+// Time and gravity advance on the device: the G2P's first thread moves t and
+// the next step's gravity (loading.c:34-54) once all reads of them are done.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "mpmg_internal.cuh"
+
+namespace {
+
+struct GeomM {
+    int Nx, Ny, Ex, Ey, ne;
+    float hf, inv_hf;
+    double h;
+    float xmaxf, ymaxf;
+};
+
+struct BcM {
+    int kind;
+    int left_col, right_col, bottom_row, top_row, lf, bf, rf, tf;
+    double hole_radius, open_time;
+    int wall_col;
+};
+
+struct Buf {
+    float *xl, *yl, *vx, *vy, *m, *v, *sxx, *sxy, *syy, *ux, *uy, *Tzz, *gp, *gdp;
+    int *pid;
+};
+
+Buf buf(const MixedState *s, int b)
+{
+    Buf o;
+    o.xl = s->x[b]; o.yl = s->y[b]; o.vx = s->vx[b]; o.vy = s->vy[b]; o.m = s->m[b]; o.v = s->v[b];
+    o.sxx = s->sxx[b]; o.sxy = s->sxy[b]; o.syy = s->syy[b]; o.ux = s->ux[b]; o.uy = s->uy[b];
+    o.Tzz = s->Tzz[b]; o.gp = s->gp[b]; o.gdp = s->gdp[b];
+    o.pid = s->pid[b];
+    return o;
+}
+
+struct MatF {
+    float G, K, lambda, dt;
+    float mu_s, mu_2, I0, grains_rho, grains_d, rho_critical;
+};
+
+// isolin (isolin.c:75-116) in FP32.
+__device__ __forceinline__ void isolin_f(const MatF &p, float exx, float exy, float eyy, float wxy,
+                                         float &sxx, float &sxy, float &syy)
+{
+    float trD = exx + eyy;
+    float twoG = 2.0f * p.G;
+    float dsjxx = p.lambda * trD + twoG * exx + 2.0f * wxy * sxy;
+    float dsjxy = twoG * exy - wxy * (sxx - syy);
+    float dsjyy = p.lambda * trD + twoG * eyy - 2.0f * wxy * sxy;
+    sxx += p.dt * dsjxx;
+    sxy += p.dt * dsjxy;
+    syy += p.dt * dsjyy;
+}
+
+// g_local_mu2 (g_local_mu2.c:165-310) in FP32, plane-strain stress
+// [[Txx, Txy, 0], [Txy, Tyy, 0], [0, 0, Tzz]].
+__device__ __forceinline__ void g_local_mu2_f(const MatF &p, float m, float v, float exx, float exy,
+                                              float eyy, float wxy, float &Txx, float &Txy, float &Tyy,
+                                              float &Tzz, float &gp, float &gdp)
+{
+    const float G = p.G, dt = p.dt;
+    const float twoG = 2.0f * G;
+    const float trD = exx + eyy;
+    const float lt = p.lambda * trD;
+    // Jaumann terms W T - T W with W_xy = wxy
+    const float JSxx = 2.0f * wxy * Txy;
+    const float JSxy = wxy * (Tyy - Txx);
+    const float JSyy = -2.0f * wxy * Txy;
+    const float Txx_tr = (exx * twoG + lt + JSxx) * dt + Txx;
+    const float Txy_tr = (exy * twoG + JSxy) * dt + Txy;
+    const float Tyy_tr = (eyy * twoG + lt + JSyy) * dt + Tyy;
+    const float Tzz_tr = lt * dt + Tzz;
+    const float pm = (Txx_tr + Tyy_tr + Tzz_tr) * (1.0f / 3.0f);
+    const float T0xx = Txx_tr - pm, T0yy = Tyy_tr - pm, T0zz = Tzz_tr - pm, T0xy = Txy_tr;
+    const float tau_tr = sqrtf(0.5f * (T0xx * T0xx + 2.0f * T0xy * T0xy + T0yy * T0yy + T0zz * T0zz));
+    const float p_tr = -pm;
+    float nup = 0.0f;
+    if (m / v < p.rho_critical || p_tr <= 0.0f) {
+        Txx = Txy = Tyy = Tzz = 0.0f;
+    } else if (p_tr > 0.0f) {
+        const float S0 = p.mu_s * p_tr;
+        float tau_tau = tau_tr, scale = 1.0f;
+        if (tau_tr > S0) {
+            const float S2 = p.mu_2 * p_tr;
+            const float alpha = G * p.I0 * dt * sqrtf(p_tr / p.grains_rho) / p.grains_d;
+            const float B = -(S2 + tau_tr + alpha);
+            const float H = S2 * tau_tr + S0 * alpha;
+            const float disc = sqrtf(B * B - 4.0f * H);
+            tau_tau = (B > 0.0f) ? (-B - disc) * 0.5f : (2.0f * H) / (-B + disc);
+            scale = tau_tau / tau_tr;
+        }
+        nup = (tau_tr - tau_tau) / G / dt;
+        Txx = T0xx * scale - p_tr;
+        Txy = T0xy * scale;
+        Tyy = T0yy * scale - p_tr;
+        Tzz = T0zz * scale - p_tr;
+    }
+    gp += nup * dt;
+    gdp = nup;
+}
+
+__device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double h, double t_now, bool &mx,
+                                          bool &my)
+{
+    mx = false;
+    my = false;
+    if (bc.kind == MPMG_BOX) {
+        bool on_row = (i >= bc.left_col && i <= bc.right_col);
+        bool on_col = (j >= bc.bottom_row && j <= bc.top_row);
+        if (on_row && j == bc.bottom_row) { mx |= (bc.bf & 1) != 0; my |= (bc.bf & 2) != 0; }
+        if (on_row && j == bc.top_row) { mx |= (bc.tf & 1) != 0; my |= (bc.tf & 2) != 0; }
+        if (on_col && i == bc.left_col) { mx |= (bc.lf & 1) != 0; my |= (bc.lf & 2) != 0; }
+        if (on_col && i == bc.right_col) { mx |= (bc.rf & 1) != 0; my |= (bc.rf & 2) != 0; }
+    } else {
+        if (j == 0 && !((i * h) <= bc.hole_radius && t_now > bc.open_time)) {
+            mx = true;
+            my = true;
+        }
+        if (i == 0 || i == bc.wall_col) mx = true;
+    }
+}
+
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) mx_p2g_kernel(GeomM g, const int *__restrict__ cell_start,
+                                                     const uint32_t *__restrict__ perm, Buf P,
+                                                     const StepParams *__restrict__ sp,
+                                                     float *__restrict__ cell_sums)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.ne) return;
+    const int k0 = cell_start[e], k1 = cell_start[e + 1];
+    if (k0 == k1) return;
+    const float grav = (float)sp->gravity;
+    const float ih = g.inv_hf;
+    float acc[4][5];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
+    for (int k = k0; k < k1; k++) {
+        const int i = (int)perm[k];
+        const float xl = P.xl[i], yl = P.yl[i], m = P.m[i], vol = P.v[i];
+        const float ox = 1.0f - xl, oy = 1.0f - yl;
+        const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
+        const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
+        const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
+        const float pmx = P.vx[i] * m, pmy = P.vy[i] * m, pby = grav * m;
+        const float s0 = -P.sxx[i] * vol, s1 = -P.sxy[i] * vol, s2 = -P.syy[i] * vol;
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            acc[a][0] += s[a] * m;
+            acc[a][1] += s[a] * pmx;
+            acc[a][2] += s[a] * pmy;
+            acc[a][3] += gx[a] * s0 + gy[a] * s1;
+            acc[a][4] += s[a] * pby + gx[a] * s1 + gy[a] * s2;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < 5; f++) cell_sums[(size_t)(a * 5 + f) * g.ne + e] = acc[a][f];
+}
+
+__global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int *__restrict__ cell_start,
+                                                      const float *__restrict__ cell_sums,
+                                                      const StepParams *__restrict__ sp, double dt,
+                                                      double *__restrict__ node_m, float *__restrict__ node_ax,
+                                                      float *__restrict__ node_ay, float *__restrict__ node_vx,
+                                                      float *__restrict__ node_vy, double *__restrict__ node_mx,
+                                                      double *__restrict__ node_my, double *__restrict__ node_fx,
+                                                      double *__restrict__ node_fy)
+{
+    const int nn = g.Nx * g.Ny;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    double m = 0, mx = 0, my = 0;
+    float fx = 0, fy = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+        int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
+        int e = cj * g.Ex + ci;
+        if (cell_start[e] == cell_start[e + 1]) continue;
+        int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+        const float *cs = cell_sums + (size_t)(a * 5) * g.ne + e;
+        m += (double)cs[0];
+        mx += (double)cs[(size_t)g.ne];
+        my += (double)cs[(size_t)2 * g.ne];
+        fx += cs[(size_t)3 * g.ne];
+        fy += cs[(size_t)4 * g.ne];
+    }
+    bool bx, by;
+    bc_mask_m(bc, i, j, g.h, sp->t + dt, bx, by);
+    if (bx) { mx = 0; fx = 0; }
+    if (by) { my = 0; fy = 0; }
+    float ax = 0, ay = 0, vxn = 0, vyn = 0;
+    if (m > MPMG_TOL) {
+        const float mf = (float)m;
+        ax = fx / mf;
+        ay = fy / mf;
+        mx += dt * (double)fx;
+        my += dt * (double)fy;
+        vxn = (float)(mx / m);
+        vyn = (float)(my / m);
+    }
+    node_m[n] = m;
+    node_ax[n] = ax;
+    node_ay[n] = ay;
+    node_vx[n] = vxn;
+    node_vy[n] = vyn;
+    if (node_mx != nullptr) {
+        node_mx[n] = mx;
+        node_my[n] = my;
+        node_fx[n] = fx;
+        node_fy[n] = fy;
+    }
+}
+
+template <int MATERIAL>
+__global__ void __launch_bounds__(256) mx_g2p_kernel(GeomM g, int n, MatF mp, const int *__restrict__ cell_start,
+                                                     const uint32_t *__restrict__ perm,
+                                                     const uint32_t *__restrict__ sorted_keys, Buf S, Buf D,
+                                                     const int *__restrict__ cell_src, int *__restrict__ cell_dst,
+                                                     const float *__restrict__ node_ax,
+                                                     const float *__restrict__ node_ay,
+                                                     const float *__restrict__ node_vx,
+                                                     const float *__restrict__ node_vy, StepParams *sp,
+                                                     double dt, int gravity_mode, double gravity_const)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) {
+        // Advance t and compute the next step's body force (the driver's
+        // time_varying_loads, loading.c:34-54).  No kernel of this step reads
+        // them after this point.
+        const double t = sp->t + dt;
+        sp->t = t;
+        sp->step_count += 1;
+        double grav;
+        if (gravity_mode == MPMG_GRAVITY_CONSTANT) grav = gravity_const;
+        else if ((0.1 + sp->step_start_time) > t) grav = -9.8 * ((t - sp->step_start_time) / 0.1);
+        else grav = -9.8;
+        sp->gravity = grav;
+    }
+    if (k >= n) return;
+    const int i = (int)perm[k];
+    const int active_end = cell_start[g.ne];
+    D.pid[k] = S.pid[i];
+    if (k >= active_end) {
+        // outside the grid: carried along unchanged
+        D.xl[k] = S.xl[i]; D.yl[k] = S.yl[i]; D.vx[k] = S.vx[i]; D.vy[k] = S.vy[i];
+        D.m[k] = S.m[i]; D.v[k] = S.v[i]; D.sxx[k] = S.sxx[i]; D.sxy[k] = S.sxy[i]; D.syy[k] = S.syy[i];
+        D.ux[k] = S.ux[i]; D.uy[k] = S.uy[i];
+        if (MATERIAL == MPMG_G_LOCAL_MU2) {
+            D.Tzz[k] = S.Tzz[i]; D.gp[k] = S.gp[i]; D.gdp[k] = S.gdp[i];
+        }
+        cell_dst[k] = cell_src[i];
+        return;
+    }
+    const int e = (int)sorted_keys[k];
+    const int ci = e % g.Ex, cj = e / g.Ex;
+    const int n0 = cj * g.Nx + ci;
+    const int nd[4] = {n0, n0 + 1, n0 + 1 + g.Nx, n0 + g.Nx};
+    const float ih = g.inv_hf;
+    const float xl = S.xl[i], yl = S.yl[i];
+    const float ox = 1.0f - xl, oy = 1.0f - yl;
+    const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
+    const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
+    const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
+    float xtt = 0, ytt = 0, dux = 0, duy = 0, exx = 0, eyy = 0, dxdy = 0, dydx = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const float ax = node_ax[nd[a]], ay = node_ay[nd[a]], vx = node_vx[nd[a]], vy = node_vy[nd[a]];
+        xtt += s[a] * ax;
+        ytt += s[a] * ay;
+        dux += s[a] * vx;
+        duy += s[a] * vy;
+        exx += gx[a] * vx;
+        eyy += gy[a] * vy;
+        dxdy += gy[a] * vx;
+        dydx += gx[a] * vy;
+    }
+    const float dtf = mp.dt;
+    D.vx[k] = S.vx[i] + dtf * xtt;
+    D.vy[k] = S.vy[i] + dtf * ytt;
+    dux *= dtf;
+    duy *= dtf;
+    D.ux[k] = S.ux[i] + dux;
+    D.uy[k] = S.uy[i] + duy;
+    const float exy = 0.5f * (dxdy + dydx), wxy = 0.5f * (dxdy - dydx);
+    const float m = S.m[i];
+    const float vol = S.v[i] * expf(dtf * (exx + eyy));
+    D.m[k] = m;
+    D.v[k] = vol;
+    float sxx = S.sxx[i], sxy = S.sxy[i], syy = S.syy[i];
+    if (MATERIAL == MPMG_ISOLIN) {
+        isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
+    } else {
+        float Tzz = S.Tzz[i], gp = S.gp[i], gdp;
+        g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
+        D.Tzz[k] = Tzz;
+        D.gp[k] = gp;
+        D.gdp[k] = gdp;
+    }
+    D.sxx[k] = sxx;
+    D.sxy[k] = sxy;
+    D.syy[k] = syy;
+
+    // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
+    float nxl = xl + dux * ih, nyl = yl + duy * ih;
+    const float fxl = floorf(nxl), fyl = floorf(nyl);
+    const int nci = ci + (int)fxl, ncj = cj + (int)fyl;
+    nxl -= fxl;
+    nyl -= fyl;
+    const float xg = ((float)nci + nxl) * g.hf, yg = ((float)ncj + nyl) * g.hf;
+    const bool inside = nci >= 0 && ncj >= 0 && nci < g.Ex && ncj < g.Ey && xg < g.xmaxf && yg < g.ymaxf &&
+                        xg >= 0.0f && yg >= 0.0f;
+    if (inside) {
+        D.xl[k] = nxl;
+        D.yl[k] = nyl;
+        cell_dst[k] = ncj * g.Ex + nci;
+    } else {
+        D.xl[k] = xg;      // global position of a particle that left the grid
+        D.yl[k] = yg;
+        cell_dst[k] = g.ne;
+    }
+}
+
+__global__ void iota_kernel(uint32_t *v, int n)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (uint32_t)i;
+}
+
+inline int blocks_for(size_t n, int threads)
+{
+    size_t b = (n + (size_t)threads - 1) / (size_t)threads;
+    return (int)(b > 0 ? b : 1);
+}
+
+GeomM make_geom(const mpmg_ctx *ctx)
+{
+    GeomM g;
+    g.Nx = ctx->cfg.Nx;
+    g.Ny = ctx->cfg.Ny;
+    g.Ex = ctx->Ex;
+    g.Ey = ctx->Ey;
+    g.ne = (int)ctx->ne;
+    g.h = ctx->cfg.h;
+    g.hf = (float)ctx->cfg.h;
+    g.inv_hf = (float)ctx->inv_h;
+    g.xmaxf = (float)ctx->cfg.xmax;
+    g.ymaxf = (float)ctx->cfg.ymax;
+    return g;
+}
+
+BcM make_bc(const mpmg_ctx *ctx)
+{
+    BcM b = {};
+    const mpmg_config &c = ctx->cfg;
+    b.kind = c.bc;
+    if (c.bc == MPMG_BOX) {
+        b.left_col = (int)(size_t)(c.bcf[0] * (double)(c.Nx - 1));
+        b.right_col = (int)(size_t)((c.bcf[0] + c.bcf[2]) * (double)(c.Nx - 1));
+        b.bottom_row = (int)(size_t)(c.bcf[1] * (double)(c.Ny - 1));
+        b.top_row = (int)(size_t)((c.bcf[1] + c.bcf[3]) * (double)(c.Ny - 1));
+        b.lf = c.bci[0];
+        b.bf = c.bci[1];
+        b.rf = c.bci[2];
+        b.tf = c.bci[3];
+    } else {
+        b.hole_radius = c.bcf[0];
+        b.open_time = c.bcf[1];
+        b.wall_col = (int)((double)(c.Nx - 1) * c.bcf[2]);
+    }
+    return b;
+}
+
+MatF make_mat(const mpmg_ctx *ctx)
+{
+    MatF p;
+    const mpmg_config &c = ctx->cfg;
+    p.G = (float)ctx->G;
+    p.K = (float)ctx->K;
+    p.lambda = (float)(ctx->K - 2.0 * ctx->G / 3.0);
+    p.dt = (float)c.dt;
+    p.mu_s = (float)c.mp[MPMG_MP_MU_S];
+    p.mu_2 = (float)c.mp[MPMG_MP_MU_2];
+    p.I0 = (float)c.mp[MPMG_MP_I0];
+    p.grains_rho = (float)c.mp[MPMG_MP_GRAINS_RHO];
+    p.grains_d = (float)c.mp[MPMG_MP_GRAINS_D];
+    p.rho_critical = (float)c.mp[MPMG_MP_RHO_CRITICAL];
+    if (c.material == MPMG_ISOLIN) p.lambda = (float)ctx->lambda;
+    return p;
+}
+
+template <typename T>
+int dalloc(T **p, size_t count)
+{
+    cudaError_t e = cudaMalloc((void **)p, (count ? count : 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return mpmg_cuda_status(e, "cudaMalloc (mixed state)");
+    }
+    return MPMG_OK;
+}
+
+// Cell and local coordinates of a host position (FP64, as WHICH_ELEMENT4).
+void locate(const mpmg_ctx *ctx, double x, double y, int *cell, float *xl, float *yl)
+{
+    const mpmg_config &c = ctx->cfg;
+    if (x < c.xmax && x >= 0.0 && y < c.ymax && y >= 0.0) {
+        double fx = floor(x / c.h), fy = floor(y / c.h);
+        if (fx < (double)ctx->Ex && fy < (double)ctx->Ey) {
+            *cell = (int)(fx + fy * (double)ctx->Ex);
+            double lx = (x - fx * c.h) / c.h, ly = (y - fy * c.h) / c.h;
+            float fxl = (float)lx, fyl = (float)ly;
+            if (fxl >= 1.0f) fxl = nextafterf(1.0f, 0.0f);
+            if (fyl >= 1.0f) fyl = nextafterf(1.0f, 0.0f);
+            *xl = fxl;
+            *yl = fyl;
+            return;
+        }
+    }
+    *cell = (int)ctx->ne;
+    *xl = (float)x;
+    *yl = (float)y;
+}
+
+}  // namespace
+
+int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const double *x, const double *y,
+                    const double *vx, const double *vy, const double *sxx, const double *sxy, const double *syy)
+{
+    if (ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2) {
+        mpmg_set_error("mixed precision supports isolin and g_local_mu2");
+        return MPMG_ERR_UNSUPPORTED;
+    }
+    MixedState *s = new MixedState();
+    memset(s, 0, sizeof(*s));
+    ctx->mixed = s;
+    const size_t n = ctx->np;
+    const bool mu2 = ctx->cfg.material == MPMG_G_LOCAL_MU2;
+    int rc;
+    for (int b = 0; b < 2; b++) {
+        float **f[] = {&s->x[b], &s->y[b], &s->vx[b], &s->vy[b], &s->m[b], &s->v[b], &s->sxx[b], &s->sxy[b],
+                       &s->syy[b], &s->ux[b], &s->uy[b]};
+        for (float **p : f)
+            if ((rc = dalloc(p, n)) != MPMG_OK) return rc;
+        if (mu2) {
+            if ((rc = dalloc(&s->Tzz[b], n)) != MPMG_OK) return rc;
+            if ((rc = dalloc(&s->gp[b], n)) != MPMG_OK) return rc;
+            if ((rc = dalloc(&s->gdp[b], n)) != MPMG_OK) return rc;
+        }
+        if ((rc = dalloc(&s->pid[b], n)) != MPMG_OK) return rc;
+    }
+    if ((rc = dalloc(&s->cell_sums, 20 * ctx->ne)) != MPMG_OK) return rc;
+    float **nf[] = {&s->node_ax, &s->node_ay, &s->node_vx, &s->node_vy};
+    for (float **p : nf)
+        if ((rc = dalloc(p, ctx->nn)) != MPMG_OK) return rc;
+
+    // host staging
+    std::vector<float> hx(n ? n : 1), hy(n ? n : 1), tmp(n ? n : 1);
+    std::vector<int> cell(n ? n : 1), pid(n ? n : 1);
+    for (size_t i = 0; i < n; i++) {
+        locate(ctx, x[i], y[i], &cell[i], &hx[i], &hy[i]);
+        pid[i] = (int)i;
+    }
+    auto up = [&](float *dst, const float *src) {
+        return cudaMemcpy(dst, src, n * sizeof(float), cudaMemcpyHostToDevice);
+    };
+    auto upd = [&](float *dst, const double *src) {
+        for (size_t i = 0; i < n; i++) tmp[i] = (float)src[i];
+        return cudaMemcpy(dst, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    };
+    cudaError_t e = cudaSuccess;
+    if (n > 0) {
+        e = up(s->x[0], hx.data());
+        if (e == cudaSuccess) e = up(s->y[0], hy.data());
+        if (e == cudaSuccess) e = upd(s->vx[0], vx);
+        if (e == cudaSuccess) e = upd(s->vy[0], vy);
+        if (e == cudaSuccess) e = upd(s->m[0], m);
+        if (e == cudaSuccess) e = upd(s->v[0], v);
+        if (e == cudaSuccess) e = upd(s->sxx[0], sxx);
+        if (e == cudaSuccess) e = upd(s->sxy[0], sxy);
+        if (e == cudaSuccess) e = upd(s->syy[0], syy);
+        if (e == cudaSuccess) e = cudaMemset(s->ux[0], 0, n * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(s->uy[0], 0, n * sizeof(float));
+        if (e == cudaSuccess && mu2) e = cudaMemset(s->Tzz[0], 0, n * sizeof(float));
+        if (e == cudaSuccess && mu2) e = cudaMemset(s->gp[0], 0, n * sizeof(float));
+        if (e == cudaSuccess && mu2) e = cudaMemset(s->gdp[0], 0, n * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemcpy(s->pid[0], pid.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+        // element index of the stored particles of buffer 0 (see cell_array)
+        if (e == cudaSuccess) e = cudaMemcpy(ctx->in_element, cell.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed state upload");
+    iota_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(ctx->vals, (int)n);
+    ctx->launches += 1;
+    s->cur = 0;
+    s->keys_valid = 1;
+    MPMG_CHECK(cudaGetLastError());
+    return MPMG_OK;
+}
+
+void mpmg_mixed_free(mpmg_ctx *ctx)
+{
+    MixedState *s = ctx->mixed;
+    if (s == nullptr) return;
+    for (int b = 0; b < 2; b++) {
+        float *f[] = {s->x[b], s->y[b], s->vx[b], s->vy[b], s->m[b], s->v[b], s->sxx[b], s->sxy[b], s->syy[b],
+                      s->ux[b], s->uy[b], s->Tzz[b], s->gp[b], s->gdp[b]};
+        for (float *p : f) cudaFree(p);
+        cudaFree(s->pid[b]);
+    }
+    cudaFree(s->cell_sums);
+    cudaFree(s->node_ax);
+    cudaFree(s->node_ay);
+    cudaFree(s->node_vx);
+    cudaFree(s->node_vy);
+    delete s;
+    ctx->mixed = nullptr;
+}
+
+// Element index array of buffer b (buffer 0 uses ctx->in_element, buffer 1
+// ctx->active: in the mixed form those two int arrays hold the stored
+// particles' elements).
+static int *cell_array(mpmg_ctx *ctx, int b)
+{
+    return b == 0 ? ctx->in_element : ctx->active;
+}
+
+int mpmg_mixed_step(mpmg_ctx *ctx)
+{
+    MixedState *s = ctx->mixed;
+    cudaStream_t st = ctx->stream;
+    const mpmg_config &c = ctx->cfg;
+    const GeomM g = make_geom(ctx);
+    const int n = (int)ctx->np;
+    const int cur = s->cur, nxt = 1 - cur;
+
+    mpmg_phase_begin(ctx, PH_SORT);
+    ctx->launches += mpmg_sort_run((const uint32_t *)cell_array(ctx, cur), ctx->vals, n, (int)ctx->ne, ctx->key_bits,
+                                   ctx->sort, ctx->sorted_keys, ctx->perm, ctx->cell_start, st);
+    mpmg_phase_end(ctx, PH_SORT);
+
+    Buf S = buf(s, cur), D = buf(s, nxt);
+    mpmg_phase_begin(ctx, PH_P2G);
+    mx_p2g_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(g, ctx->cell_start, ctx->perm, S, ctx->d_params,
+                                                            s->cell_sums);
+    mpmg_phase_end(ctx, PH_P2G);
+
+    mpmg_phase_begin(ctx, PH_GRID);
+    mx_grid_kernel<<<blocks_for(ctx->nn, 256), 256, 0, st>>>(
+        g, make_bc(ctx), ctx->cell_start, s->cell_sums, ctx->d_params, c.dt, ctx->node_m, s->node_ax, s->node_ay,
+        s->node_vx, s->node_vy, ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy);
+    mpmg_phase_end(ctx, PH_GRID);
+
+    mpmg_phase_begin(ctx, PH_G2P);
+    const MatF mp = make_mat(ctx);
+    if (c.material == MPMG_ISOLIN) {
+        mx_g2p_kernel<MPMG_ISOLIN><<<blocks_for(n, 256), 256, 0, st>>>(
+            g, n, mp, ctx->cell_start, ctx->perm, ctx->sorted_keys, S, D, cell_array(ctx, cur), cell_array(ctx, nxt),
+            s->node_ax, s->node_ay, s->node_vx, s->node_vy, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+    } else {
+        mx_g2p_kernel<MPMG_G_LOCAL_MU2><<<blocks_for(n, 256), 256, 0, st>>>(
+            g, n, mp, ctx->cell_start, ctx->perm, ctx->sorted_keys, S, D, cell_array(ctx, cur), cell_array(ctx, nxt),
+            s->node_ax, s->node_ay, s->node_vx, s->node_vy, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+    }
+    mpmg_phase_end(ctx, PH_G2P);
+    ctx->launches += 3;
+    s->cur = nxt;
+    MPMG_CHECK(cudaGetLastError());
+    return MPMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host read-back.
+
+namespace {
+
+int download_f(mpmg_ctx *ctx, const float *d, std::vector<float> &h)
+{
+    h.resize(ctx->np ? ctx->np : 1);
+    if (ctx->np == 0) return MPMG_OK;
+    MPMG_CHECK(cudaMemcpy(h.data(), d, ctx->np * sizeof(float), cudaMemcpyDeviceToHost));
+    return MPMG_OK;
+}
+
+int download_i(mpmg_ctx *ctx, const int *d, std::vector<int> &h)
+{
+    h.resize(ctx->np ? ctx->np : 1);
+    if (ctx->np == 0) return MPMG_OK;
+    MPMG_CHECK(cudaMemcpy(h.data(), d, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+    return MPMG_OK;
+}
+
+}  // namespace
+
+int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active)
+{
+    MixedState *s = ctx->mixed;
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    std::vector<int> cell, pid;
+    int rc;
+    if ((rc = download_i(ctx, cell_array(ctx, s->cur), cell)) != MPMG_OK) return rc;
+    if ((rc = download_i(ctx, s->pid[s->cur], pid)) != MPMG_OK) return rc;
+    for (size_t k = 0; k < ctx->np; k++) {
+        int e = cell[k] < (int)ctx->ne ? cell[k] : -1;
+        if (in_element) in_element[pid[k]] = e;
+        if (active) active[pid[k]] = e >= 0 ? 1 : 0;
+    }
+    return MPMG_OK;
+}
+
+int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out)
+{
+    MixedState *s = ctx->mixed;
+    const int b = s->cur;
+    const size_t n = ctx->np;
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    std::vector<int> pid, cell;
+    std::vector<float> a, bb;
+    int rc;
+    if (strncmp(name, "node_", 5) == 0) {
+        const float *src = nullptr;
+        if (strcmp(name, "node_ax") == 0) src = s->node_ax;
+        else if (strcmp(name, "node_ay") == 0) src = s->node_ay;
+        else if (strcmp(name, "node_vx") == 0) src = s->node_vx;
+        else if (strcmp(name, "node_vy") == 0) src = s->node_vy;
+        if (src == nullptr) return MPMG_ERR_UNKNOWN_FIELD;   // FP64 node arrays: the common path
+        std::vector<float> h(ctx->nn);
+        MPMG_CHECK(cudaMemcpy(h.data(), src, ctx->nn * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < ctx->nn; k++) out[k] = h[k];
+        return MPMG_OK;
+    }
+    if ((rc = download_i(ctx, s->pid[b], pid)) != MPMG_OK) return rc;
+    if (strcmp(name, "x") == 0 || strcmp(name, "y") == 0) {
+        const bool isx = name[0] == 'x';
+        if ((rc = download_i(ctx, cell_array(ctx, b), cell)) != MPMG_OK) return rc;
+        if ((rc = download_f(ctx, isx ? s->x[b] : s->y[b], a)) != MPMG_OK) return rc;
+        for (size_t k = 0; k < n; k++) {
+            if (cell[k] < (int)ctx->ne) {
+                int c = isx ? cell[k] % ctx->Ex : cell[k] / ctx->Ex;
+                out[pid[k]] = ((double)c + (double)a[k]) * ctx->cfg.h;
+            } else {
+                out[pid[k]] = (double)a[k];
+            }
+        }
+        return MPMG_OK;
+    }
+    struct { const char *n; float *p; } f[] = {
+        {"vx", s->vx[b]}, {"vy", s->vy[b]}, {"m", s->m[b]}, {"v", s->v[b]}, {"sxx", s->sxx[b]},
+        {"sxy", s->sxy[b]}, {"syy", s->syy[b]}, {"ux", s->ux[b]}, {"uy", s->uy[b]}, {"Txx", s->sxx[b]},
+        {"Txy", s->sxy[b]}, {"Tyx", s->sxy[b]}, {"Tyy", s->syy[b]}, {"Tzz", s->Tzz[b]},
+        {"state9", s->gp[b]}, {"state10", s->gdp[b]}};
+    for (auto &fe : f) {
+        if (strcmp(name, fe.n) == 0) {
+            if (fe.p == nullptr) {
+                for (size_t k = 0; k < n; k++) out[k] = 0.0;
+                return MPMG_OK;
+            }
+            if ((rc = download_f(ctx, fe.p, a)) != MPMG_OK) return rc;
+            for (size_t k = 0; k < n; k++) out[pid[k]] = (double)a[k];
+            return MPMG_OK;
+        }
+    }
+    return MPMG_ERR_UNKNOWN_FIELD;
+}
+
+int mpmg_mixed_set(mpmg_ctx *ctx, const char *name, const double *in)
+{
+    MixedState *s = ctx->mixed;
+    const int b = s->cur;
+    const size_t n = ctx->np;
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    struct { const char *n; float *p; } f[] = {
+        {"vx", s->vx[b]}, {"vy", s->vy[b]}, {"m", s->m[b]}, {"v", s->v[b]}, {"sxx", s->sxx[b]},
+        {"sxy", s->sxy[b]}, {"syy", s->syy[b]}, {"ux", s->ux[b]}, {"uy", s->uy[b]}, {"Tzz", s->Tzz[b]},
+        {"state9", s->gp[b]}, {"state10", s->gdp[b]}};
+    for (auto &fe : f) {
+        if (strcmp(name, fe.n) == 0 && fe.p != nullptr) {
+            std::vector<int> pid;
+            int rc;
+            if ((rc = download_i(ctx, s->pid[b], pid)) != MPMG_OK) return rc;
+            std::vector<float> h(n ? n : 1);
+            for (size_t k = 0; k < n; k++) h[k] = (float)in[pid[k]];
+            if (n) MPMG_CHECK(cudaMemcpy(fe.p, h.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+            return MPMG_OK;
+        }
+    }
+    mpmg_set_error("field '%s' cannot be written in the mixed-precision form", name);
+    return MPMG_ERR_UNKNOWN_FIELD;
+}

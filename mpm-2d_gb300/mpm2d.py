@@ -45,7 +45,8 @@ class Config(C.Structure):
                 ("mp", C.c_double * MP_COUNT), ("bc", C.c_int), ("bcf", C.c_double * 4),
                 ("bci", C.c_int * 4), ("gravity_mode", C.c_int), ("gravity", C.c_double),
                 ("store_transients", C.c_int), ("solver_tol", C.c_double),
-                ("solver_maxit", C.c_int), ("device", C.c_int), ("solver_warm_start", C.c_int)]
+                ("solver_maxit", C.c_int), ("device", C.c_int), ("solver_warm_start", C.c_int),
+                ("precision", C.c_int)]
 
 
 _lib = None
@@ -117,8 +118,11 @@ def default_params(material):
     return mp
 
 
+PRECISIONS = {"fp64": 0, "mixed": 1}
+
+
 def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0,
-                warm_start=False):
+                warm_start=False, precision="fp64"):
     cfg = Config()
     _check(lib().mpmg_config_init(C.byref(cfg)))
     cfg.Nx, cfg.Ny, cfg.h = scene["Nx"], scene["Ny"], scene["h"]
@@ -145,6 +149,7 @@ def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20
     cfg.solver_maxit = solver_maxit
     cfg.device = device
     cfg.solver_warm_start = 1 if warm_start else 0
+    cfg.precision = PRECISIONS[precision]
     return cfg
 
 
@@ -152,9 +157,10 @@ class Simulation:
     """One simulation resident on the GPU."""
 
     def __init__(self, scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0,
-                 warm_start=False):
+                 warm_start=False, precision="fp64"):
         L = lib()
-        cfg = make_config(scene, store_transients, solver_tol, solver_maxit, device, warm_start)
+        cfg = make_config(scene, store_transients, solver_tol, solver_maxit, device, warm_start, precision)
+        self.precision = precision
         p = scene["particles"]
         self.n = len(p["x"])
         arrs = [np.ascontiguousarray(p[k], dtype=np.float64)

@@ -1,0 +1,139 @@
+"""The mixed-precision form (FP32 particle state, shape functions, P2G/G2P
+and material; FP64 nodal mass and momentum sums and division by nodal mass)
+against the FP64 form and the oracle.
+
+Criteria (the mixed form's contract):
+  * relative L2 error per field, ||a - b|| / ||b||, after 100 steps <= 1e-4;
+  * silo discharge rate (minus the slope of the active mass over the steady
+    window, the reference's examples/silo/write_active_mass.py measure) and
+    column runout (largest x of an active particle) within 1 %;
+  * bit-identical repeat runs; permutation and mass invariants at 1 M.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+import mpm2d
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy")
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
+
+
+def group_rel_l2(sim_get, ref_get, f):
+    groups = {"sxy": ("sxx", "syy"), "vx": ("vx", "vy"), "vy": ("vx", "vy"), "ux": ("ux", "uy"),
+              "uy": ("ux", "uy")}
+    a, b = sim_get(f), ref_get(f)
+    if f in groups:
+        scale = max(np.linalg.norm(ref_get(g)) for g in groups[f])
+        return float(np.linalg.norm(a - b) / scale)
+    return rel_l2(a, b)
+
+
+def column_scene():
+    # granular column (g_local_mu2 with the benchmark's grain size) on a 129^2 grid
+    return scenes.column(Nx=129, Ny=129, h=1 / 128, width=0.25, height=0.4, material="g_local_mu2",
+                         rho=2450.0, props=(1e6, 0.3), dt=1e-5, mp={"grains_d": 5.3e-4}, jitter=1e-3, seed=4)
+
+
+@pytest.mark.parametrize("which", ["isolin_block", "mu2_column"])
+def test_mixed_vs_fp64_after_100_steps(which):
+    sc = scenes.config1(seed=3) if which == "isolin_block" else column_scene()
+    mixed = mpm2d.Simulation(sc, precision="mixed")
+    fp64 = mpm2d.Simulation(sc, precision="fp64")
+    mixed.step(100)
+    fp64.step(100)
+    assert mixed.t == fp64.t
+    errs = {f: group_rel_l2(mixed.get, fp64.get, f) for f in FIELDS}
+    for f, e in errs.items():
+        assert e <= 1e-4, (which, f, e)
+    ea, aa = mixed.get_map()
+    eb, ab = fp64.get_map()
+    assert np.array_equal(aa, ab)
+    assert np.mean(ea == eb) > 0.999
+
+
+def test_mixed_vs_oracle_isolin():
+    sc = scenes.config1(seed=6)
+    mixed = mpm2d.Simulation(sc, precision="mixed")
+    orc = O.Oracle(sc, nthreads=2)
+    mixed.step(100)
+    orc.step(100)
+    for f in FIELDS:
+        assert group_rel_l2(mixed.get, orc.get, f) <= 1e-4, f
+
+
+def active_mass_history(sim, m, steps, every):
+    out = []
+    for _ in range(steps // every):
+        sim.step(every)
+        _, a = sim.get_map()
+        out.append((sim.t, float(m[a == 1].sum())))
+    return np.array(out)
+
+
+def discharge_rate(hist):
+    t, m = hist[:, 0], hist[:, 1]
+    flowing = m < m[0] * (1 - 1e-9)
+    t, m = t[flowing], m[flowing]
+    lo, hi = int(0.25 * len(t)), int(0.9 * len(t))
+    slope = np.polyfit(t[lo:hi], m[lo:hi], 1)[0]
+    return -slope
+
+
+def test_mixed_silo_discharge_rate_within_1pct():
+    sc = scenes.silo(cells=48, material="g_local_mu2", props=(1e6, 0.3), dt=1e-4, hole_radius=0.12,
+                     open_time=0.05, wall_frac=0.5, fill_height=0.5, mp={"grains_d": 5.3e-4})
+    m = sc["particles"]["m"]
+    mixed = mpm2d.Simulation(sc, precision="mixed")
+    fp64 = mpm2d.Simulation(sc, precision="fp64")
+    hm = active_mass_history(mixed, m, 3000, 50)
+    hf = active_mass_history(fp64, m, 3000, 50)
+    qm, qf = discharge_rate(hm), discharge_rate(hf)
+    assert qf > 0
+    assert abs(qm - qf) <= 0.01 * qf, (qm, qf)
+
+
+def test_mixed_column_runout_within_1pct():
+    sc = column_scene()
+    mixed = mpm2d.Simulation(sc, precision="mixed")
+    fp64 = mpm2d.Simulation(sc, precision="fp64")
+    mixed.step(3000)
+    fp64.step(3000)
+    xm = mixed.get("x")[mixed.get_map()[1] == 1].max()
+    xf = fp64.get("x")[fp64.get_map()[1] == 1].max()
+    x0 = sc["particles"]["x"].max()
+    assert xf > x0                         # the column spread
+    assert abs(xm - xf) <= 0.01 * xf, (xm, xf)
+
+
+def test_mixed_deterministic():
+    sc = column_scene()
+    runs = []
+    for _ in range(2):
+        sim = mpm2d.Simulation(sc, precision="mixed")
+        sim.step(150)
+        runs.append([sim.get(f) for f in ("x", "y", "sxx", "syy")])
+    for a, b in zip(*runs):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_mixed_full_size_invariants():
+    sc = scenes.box_fill(cells=512, material="g_local_mu2")
+    sim = mpm2d.Simulation(sc, precision="mixed")
+    sim.step(5)
+    keys, perm, start = sim.get_sort()
+    assert np.all(np.diff(keys) >= 0)
+    assert np.array_equal(np.bincount(perm, minlength=len(perm)), np.ones(len(perm), dtype=np.int64))
+    e, a = sim.get_map()
+    m_nodes = sim.get("node_m").sum()
+    m_parts = sc["particles"]["m"][a == 1].sum()
+    assert abs(m_nodes - m_parts) <= 1e-6 * m_parts
+    x = sim.get("x")
+    assert np.all((x >= 0) & (x < 1))
