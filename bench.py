@@ -2,13 +2,16 @@
 
 Workload (N=1): 1 048 576 particles filling the unit square at 2x2 per
 element on a 513x513-node grid (512^2 elements), g_local_mu2 granular rheology
-(rho 2450, E 1e6, nu 0.3, reference constants), box walls, FP64 throughout,
-synthetic seeded inputs in the reference generator's lattice layout.  A step
-is one explicit_mpm_step_usl_threaded + time_varying_loads over all
-particles.  Particle state (~200 MB) exceeds the 129 MB L2 between steps.
+(rho 2450, E 1e6, nu 0.3, reference constants), box walls, synthetic seeded
+inputs in the reference generator's lattice layout.  A step is one
+explicit_mpm_step_usl_threaded + time_varying_loads over all particles.  The
+headline runs the mixed-precision form (FP32 particle state and particle
+arithmetic, FP64 nodal mass/momentum sums and division); the plain FP64 form
+is measured beside it ("fp64").  Particle state and per-step scratch exceed
+the 129 MB L2 (~170 MB mixed, ~300 MB FP64), so no flush is needed.
 
-  value     particle-steps/s with the state resident in HBM (CUDA events on
-            the library's stream, max over ranks)
+  value     particle-steps/s of the mixed form with the state resident in HBM
+            (CUDA events on the library's stream, max over ranks)
   e2e       the same metric through the public C ABI with host buffers: the
             timed region includes creating the context from host arrays (H2D
             of the particle state) and, after every step, a D2H read of the
@@ -41,17 +44,41 @@ for _p in (ROOT, PKG):
 
 METRIC = "particle-steps/s at 1M pts, mixed vs FP64 GPU; %HBM peak; adjoint/forward time"
 UNIT = "particle-steps/s"
-WORKLOAD = "box_fill_1M_g_local_mu2_fp64"
+WORKLOAD = "box_fill_1M_g_local_mu2"
 
-# Algorithmic bytes per particle-step of the fused g2p + material kernel
-# (g_local_mu2): reads x y vx vy v m ux uy sxx sxy syy Tzz gammap (13 doubles)
-# plus element and active flag (2 ints), writes x y vx vy ux uy v sxx sxy syy
-# Tzz gammap gammadotp (13 doubles); plus each node's a and v (4 doubles) read once.
-G2P_BYTES_PER_PARTICLE = 13 * 8 + 2 * 4 + 13 * 8
-G2P_BYTES_PER_NODE = 4 * 8
-# Whole step (SURVEY-style accounting): 216 B per particle + 80 B per node.
-STEP_BYTES_PER_PARTICLE = 216
-STEP_BYTES_PER_NODE = 80
+# Algorithmic bytes per unit of work of each phase (each array read or written
+# once per use; node gathers counted once per node).  Mixed form, g_local_mu2:
+#   bin   count fused into the previous G2P; scatter reads the key (4 B) and
+#         writes slot + sorted key (8 B); the P2G's ordering reads the slot and
+#         writes perm (8 B): 20 B per particle; scan: bins read + cursor,
+#         cell_start written, bins zeroed (16 B per element)
+#   p2g   perm 4 + xl yl m vx vy v sxx sxy syy 36 = 40 B per particle; 20
+#         FP32 corner sums written = 80 B per element
+#   grid  80 B of corner sums per element read; FP64 mass + float4 node = 24 B
+#         per node written
+#   g2p   perm 4 + sorted key 4 + 13 floats 52 + pid 4 read, 14 floats 56 +
+#         element 4 + pid 4 written = 128 B per particle; float4 node 16 B per
+#         node read
+MIXED_BYTES = {
+    "sort": (20, 16, 0),    # (per particle, per element, per node)
+    "p2g": (40, 80, 0),
+    "grid": (0, 80, 24),
+    "g2p": (128, 0, 16),
+}
+# FP64 form, g_local_mu2: keys read x y active (20 B) and write element,
+# active, key (12 B) per particle; the rest as above with 8-byte values.
+FP64_BYTES = {
+    "keys": (32, 0, 0),
+    "sort": (20, 16, 0),
+    "p2g": (4 + 9 * 8, 160, 0),
+    "grid": (0, 160, 40),
+    "g2p": (13 * 8 + 8 + 13 * 8, 0, 32),
+}
+
+
+def phase_bytes(table, phase, n, ne, nn):
+    a, b, c = table.get(phase, (0, 0, 0))
+    return a * n + b * ne + c * nn
 
 
 def dist_env():
@@ -180,6 +207,34 @@ def run_reference(args):
     return 0
 
 
+def time_steps(sim, steps, stream, torch):
+    """CUDA-event time of `steps` steps on the library's stream (ms)."""
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    sim.step(steps)
+    ev1.record(stream)
+    sim.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def phase_profile(sim, steps, table, n, ne, nn):
+    """Per-phase CUDA-event times (eager launches, events around each phase)
+    and the achieved algorithmic bandwidth of each phase."""
+    sim.enable_phase_timing(True)
+    sim.step(steps)
+    ph = sim.phase_times()
+    sim.enable_phase_timing(False)
+    out = {}
+    for k, (ms, cnt) in ph.items():
+        if cnt == 0:
+            continue
+        avg_s = ms / cnt / 1e3
+        b = phase_bytes(table, k, n, ne, nn)
+        out[k] = {"ms": ms / cnt, "alg_bytes": b, "gbs": (b / avg_s / 1e9) if b else None}
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -194,8 +249,8 @@ def run_gpu(args):
     scene = make_scene()
     n = len(scene["particles"]["x"])
     nn = scene["Nx"] * scene["Ny"]
-    sim = mpm2d.Simulation(scene, device=dev)
-    stream = torch.cuda.ExternalStream(sim.stream(), device=dev)
+    ne = (scene["Nx"] - 1) * (scene["Ny"] - 1)
+    peak, peak_kind = measured_peaks()
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -203,84 +258,93 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
+    def max_over_ranks(t):
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([t], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            return float(tt.item())
+        return t
+
+    # --- mixed precision (headline) ---------------------------------------
+    sim = mpm2d.Simulation(scene, device=dev, precision="mixed")
+    stream = torch.cuda.ExternalStream(sim.stream(), device=dev)
     sim.step(args.warmup)
     sim.synchronize()
     launches0 = sim.launch_count()
     barrier()
     with ClockSampler(dev) as clocks:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        sim.step(args.steps)
-        ev1.record(stream)
-        sim.synchronize()
+        ms = time_steps(sim, args.steps, stream, torch)
         barrier()
-        ms = ev0.elapsed_time(ev1)
     launches = sim.launch_count() - launches0
     clk = clocks.summary()
-    t = ms / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t = max_over_ranks(ms / 1e3)
     value = n * args.steps * world / t
+    phases = phase_profile(sim, max(3, min(args.steps, 10)), MIXED_BYTES, n, ne, nn)
+    top = max(phases.items(), key=lambda kv: kv[1]["ms"])
+    step_bytes = sum(phase_bytes(MIXED_BYTES, k, n, ne, nn) for k in MIXED_BYTES)
+    g2p = phases["g2p"]
 
-    # Dominant kernel: per-phase CUDA events on the library's stream.
-    sim.enable_phase_timing(True)
-    sim.step(max(3, min(args.steps, 10)))
-    phases = sim.phase_times()
-    sim.enable_phase_timing(False)
-    top = max(phases.items(), key=lambda kv: kv[1][0])
-    g2p_ms, g2p_launches = phases["g2p"]
-    g2p_avg_s = (g2p_ms / max(g2p_launches, 1)) / 1e3
-    peak, peak_kind = measured_peaks()
-    alg_bytes = G2P_BYTES_PER_PARTICLE * n + G2P_BYTES_PER_NODE * nn
-    achieved = alg_bytes / g2p_avg_s / 1e9
-    step_bytes = STEP_BYTES_PER_PARTICLE * n + STEP_BYTES_PER_NODE * nn
+    # --- plain FP64 form, same workload --------------------------------------
+    sim64 = mpm2d.Simulation(scene, device=dev, precision="fp64")
+    stream64 = torch.cuda.ExternalStream(sim64.stream(), device=dev)
+    sim64.step(args.warmup)
+    sim64.synchronize()
+    fp64_steps = max(3, min(args.steps, 20))
+    barrier()
+    ms64 = time_steps(sim64, fp64_steps, stream64, torch)
+    barrier()
+    t64 = max_over_ranks(ms64 / 1e3)
+    value64 = n * fp64_steps * world / t64
+    phases64 = phase_profile(sim64, 3, FP64_BYTES, n, ne, nn)
+    sim64.close()
 
-    # End to end through the C ABI with host buffers.
+    # --- end to end through the C ABI with host buffers (mixed) ---------------
+    import ctypes as C
     frame_fields = ("x", "y", "vx", "vy", "sxx", "sxy", "syy", "v")
     e2e_steps = max(2, min(args.steps, 20))
     host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in frame_fields}
     barrier()
     t0 = time.perf_counter()
-    sim2 = mpm2d.Simulation(scene, device=dev)
-    import ctypes as C
+    sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
     for _ in range(e2e_steps):
         sim2.step(1)
         for f in frame_fields:
-            buf = host[f]
             rc = mpm2d.lib().mpmg_get_field(sim2._h, f.encode(),
-                                            C.cast(buf.data_ptr(), C.POINTER(C.c_double)))
+                                            C.cast(host[f].data_ptr(), C.POINTER(C.c_double)))
             if rc != 0:
                 raise RuntimeError("mpmg_get_field failed: %d" % rc)
     sim2.synchronize()
     barrier()
-    e2e_t = time.perf_counter() - t0
+    e2e_t = max_over_ranks(time.perf_counter() - t0)
     sim2.close()
-    h2d = 9 * 8 * n / e2e_steps
-    d2h = len(frame_fields) * 8 * n
     e2e_value = n * e2e_steps * world / e2e_t
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "particles": n, "grid_nodes": [scene["Nx"], scene["Ny"]],
-                   "material": scene["material"], "bc": scene["bc"], "precision": "fp64",
-                   "l2_policy": "particle state ~200 MB > 129 MB L2 between steps",
+                   "material": scene["material"], "bc": scene["bc"], "precision": "mixed",
+                   "l2_policy": "state and step scratch exceed the 129 MB L2 between steps",
+                   "step_launch": "CUDA graphs of 8 steps",
                    "parallelism": "replicas" if world > 1 else "single"},
         "gpu_launches": int(launches),
         "clocks": clk,
-        "roofline": {"bound": "hbm", "kernel": "g2p", "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+        "roofline": {"bound": "hbm", "kernel": "g2p", "achieved": g2p["gbs"], "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": g2p["gbs"] / peak, "traffic": None,
+                     "top_phase": top[0],
                      "step_alg_bytes": step_bytes,
+                     "step_achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9,
                      "step_frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / peak,
-                     "phases_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in phases.items()},
-                     "top_phase": top[0]},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps},
+                     "phases": phases},
+        "fp64": {"value": value64, "unit": UNIT, "steps": fp64_steps, "ms_per_step": ms64 / fp64_steps,
+                 "dtype": "f64", "phases": phases64,
+                 "bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s)"},
+        "mixed_over_fp64": value / value64,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 9 * 8 * n / e2e_steps,
+                "d2h_bytes_per_step": len(frame_fields) * 8 * n, "steps": e2e_steps,
+                "path": "mpmg_create from host arrays + per-step mpmg_get_field of 8 frame fields"},
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -303,7 +367,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

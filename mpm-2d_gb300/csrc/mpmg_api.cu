@@ -293,15 +293,18 @@ int mpmg_destroy(mpmg_ctx *ctx)
     cudaFree(ctx->in_element);
     cudaFree(ctx->active);
     cudaFree(ctx->keys);
-    cudaFree(ctx->vals);
     cudaFree(ctx->sorted_keys);
     cudaFree(ctx->perm);
     cudaFree(ctx->cell_start);
     cudaFree(ctx->d_params);
     cudaFree(ctx->d_status);
-    mpmg_sort_free(ctx);
+    mpmg_bin_free(ctx);
     mpmg_nonlocal_free(ctx);
     mpmg_mixed_free(ctx);
+    for (int p = 0; p < 2; p++) {
+        if (ctx->graph_chunk[p]) cudaGraphExecDestroy(ctx->graph_chunk[p]);
+        if (ctx->graph_single[p]) cudaGraphExecDestroy(ctx->graph_single[p]);
+    }
     for (int k = 0; k < 2 * PH_COUNT; k++)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -409,7 +412,6 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             // sort, the FP64 nodal mass and the step parameters.
             TRY(dalloc(&ctx->in_element, n));
             TRY(dalloc(&ctx->active, n));
-            TRY(dalloc(&ctx->vals, n));
             TRY(dalloc(&ctx->sorted_keys, n));
             TRY(dalloc(&ctx->perm, n));
             TRY(dalloc(&ctx->cell_start, ctx->ne + 1));
@@ -420,7 +422,7 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             }
             TRY(dalloc(&ctx->d_params, 1));
             TRY(dalloc(&ctx->d_status, 1));
-            TRY(mpmg_sort_init(ctx));
+            TRY(mpmg_bin_init(ctx));
             TRY(fill_zero(ctx, ctx->cell_start, (ctx->ne + 1) * sizeof(int)));
             TRY(fill_zero(ctx, ctx->node_m, ctx->nn * sizeof(double)));
             TRY(fill_zero(ctx, ctx->d_status, sizeof(int)));
@@ -456,7 +458,6 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
         TRY(dalloc(&ctx->in_element, n));
         TRY(dalloc(&ctx->active, n));
         TRY(dalloc(&ctx->keys, n));
-        TRY(dalloc(&ctx->vals, n));
         TRY(dalloc(&ctx->sorted_keys, n));
         TRY(dalloc(&ctx->perm, n));
         TRY(dalloc(&ctx->cell_start, ctx->ne + 1));
@@ -470,7 +471,7 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
         }
         TRY(dalloc(&ctx->d_params, 1));
         TRY(dalloc(&ctx->d_status, 1));
-        TRY(mpmg_sort_init(ctx));
+        TRY(mpmg_bin_init(ctx));
         if (nonlocal) TRY(mpmg_nonlocal_init(ctx));
 
         // mpm_init copies (process_usl.c:88-126) and material_init.
@@ -538,10 +539,84 @@ fail:
     return rc;
 }
 
+}  // extern "C"
+
+namespace {
+
+int launch_one_step(mpmg_ctx *ctx)
+{
+    return ctx->mixed ? mpmg_mixed_step(ctx) : mpmg_launch_step(ctx);
+}
+
+int parity(const mpmg_ctx *ctx)
+{
+    return ctx->mixed ? ctx->mixed->cur : 0;
+}
+
+// Captures `steps` consecutive steps (starting at the current buffer parity)
+// into an executable graph.  Capturing runs nothing, so the host-side parity
+// is put back afterwards.
+int capture_steps(mpmg_ctx *ctx, int steps, cudaGraphExec_t *out, long *launches)
+{
+    const int p0 = parity(ctx);
+    const long l0 = ctx->launches;
+    MPMG_CHECK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = MPMG_OK;
+    for (int k = 0; k < steps && rc == MPMG_OK; k++) rc = launch_one_step(ctx);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (ctx->mixed) ctx->mixed->cur = p0;
+    *launches = ctx->launches - l0;
+    ctx->launches = l0;
+    if (rc != MPMG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return mpmg_cuda_status(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return mpmg_cuda_status(e, "cudaGraphInstantiate");
+    return MPMG_OK;
+}
+
+// Steps through CUDA graphs: chunks of MPMG_GRAPH_CHUNK steps, then single
+// steps.  The nonlocal materials (a cooperative solver launch per step) and
+// phase timing run eagerly instead.
+bool graphs_apply(const mpmg_ctx *ctx)
+{
+    const bool nonlocal = ctx->cfg.material == MPMG_G_NONLOCAL_MU2 || ctx->cfg.material == MPMG_G_NONLOCAL;
+    return !nonlocal && !ctx->timing;
+}
+
+int step_with_graphs(mpmg_ctx *ctx, int nsteps)
+{
+    while (nsteps > 0) {
+        const int p = parity(ctx);
+        const bool chunk = nsteps >= MPMG_GRAPH_CHUNK;
+        cudaGraphExec_t *g = chunk ? &ctx->graph_chunk[p] : &ctx->graph_single[p];
+        long *gl = chunk ? &ctx->graph_chunk_launches[p] : &ctx->graph_single_launches[p];
+        if (*g == nullptr) {
+            int rc = capture_steps(ctx, chunk ? MPMG_GRAPH_CHUNK : 1, g, gl);
+            if (rc != MPMG_OK) return rc;
+        }
+        MPMG_CHECK(cudaGraphLaunch(*g, ctx->stream));
+        ctx->launches += *gl;
+        const int done = chunk ? MPMG_GRAPH_CHUNK : 1;
+        if (ctx->mixed && (done & 1)) ctx->mixed->cur ^= 1;
+        nsteps -= done;
+    }
+    return MPMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int mpmg_step(mpmg_ctx *ctx, int nsteps)
 {
     if (ctx == nullptr || nsteps < 0) return MPMG_ERR_INVALID;
     MPMG_CHECK(cudaSetDevice(ctx->dev));
+    if (graphs_apply(ctx)) return step_with_graphs(ctx, nsteps);
     for (int k = 0; k < nsteps; k++) {
         for (int ph = 0; ph < PH_COUNT; ph++) ctx->phase_used[ph] = 0;
         int rc = ctx->mixed ? mpmg_mixed_step(ctx) : mpmg_launch_step(ctx);

@@ -12,6 +12,7 @@
 #define MPMG_TOL 1e-10          // process_usl.c:25
 #define MPMG_NCOLORS 4
 #define MPMG_DEPVAR 11          // particle.h:13
+#define MPMG_GRAPH_CHUNK 8      // steps per replayed CUDA graph
 
 // Device status word bits (ctx->d_status); any nonzero value fails the step.
 #define MPMG_DEV_ERR_SOLVER 0x1
@@ -58,9 +59,19 @@ struct MixedState {
     float *ux[2], *uy[2], *Tzz[2], *gp[2], *gdp[2];
     int *pid[2];           // caller's particle index of each stored particle
     int cur;
-    int keys_valid;        // keys/vals hold the element keys of buffer cur
     float *cell_sums;      // 20 FP32 corner sums per element, value-major
-    float *node_ax, *node_ay, *node_vx, *node_vy;
+    float4 *node4;         // per node: ax, ay, vx, vy (FP32) for the gathers
+};
+
+// Counting-sort binning scratch (mpmg_bin.cu).  Bins 0..ne-1 count the keys
+// of each element, bin ne + b the keys outside the grid in 256-key block b.
+struct BinScratch {
+    uint32_t *counts;      // bins (zero between steps)
+    uint32_t *cursor;      // scatter cursors (exclusive prefix of the bins)
+    uint32_t *tile_sums;   // per 2048-bin tile
+    uint32_t *slots;       // n scattered storage positions, unordered within elements
+    int bins;
+    int tiles;
 };
 
 struct mpmg_ctx {
@@ -85,11 +96,10 @@ struct mpmg_ctx {
 
     // Cell sort.
     uint32_t *keys;        // element key per particle (num_elements for inactive)
-    uint32_t *vals;        // particle index
     uint32_t *sorted_keys;
     uint32_t *perm;
     int *cell_start;       // num_elements + 1
-    SortScratch sort;
+    BinScratch bin;
 
     // P2G per-element corner sums: 20 values per element, value-major.
     double *cell_sums;
@@ -114,6 +124,13 @@ struct mpmg_ctx {
     // Mixed precision (cfg.precision == MPMG_PRECISION_MIXED).
     MixedState *mixed;
 
+    // CUDA graphs of whole steps (index: buffer parity of the mixed form):
+    // a chunk of MPMG_GRAPH_CHUNK steps and a single step, captured on first use.
+    cudaGraphExec_t graph_chunk[2];
+    cudaGraphExec_t graph_single[2];
+    long graph_chunk_launches[2];
+    long graph_single_launches[2];
+
     // Timing.
     int timing;
     int phase_used[PH_COUNT];
@@ -134,9 +151,6 @@ int mpmg_cuda_status(cudaError_t e, const char *what);
     } while (0)
 
 // Kernel launch helpers implemented per translation unit.
-int mpmg_sort_init(mpmg_ctx *ctx);
-void mpmg_sort_free(mpmg_ctx *ctx);
-int mpmg_sort_keys(mpmg_ctx *ctx);                // keys/vals -> sorted_keys/perm
 // Scratch words (uint32) a sort of n keys needs, and its tile count.
 size_t mpmg_sort_scratch_words(size_t n, int key_bits, int *num_tiles_out);
 // Sort with caller-provided scratch; returns the number of launches issued.
@@ -144,6 +158,14 @@ int mpmg_sort_run(const uint32_t *keys, const uint32_t *vals, int n, int ne, int
                   const SortScratch &sc, uint32_t *sorted_keys, uint32_t *perm, int *cell_start,
                   cudaStream_t s);
 int mpmg_launch_step(mpmg_ctx *ctx);             // one full step
+int mpmg_bin_init(mpmg_ctx *ctx);
+void mpmg_bin_free(mpmg_ctx *ctx);
+// Stand-alone count of keys[n] (<= ne) into the bins.
+int mpmg_bin_count(mpmg_ctx *ctx, const uint32_t *keys);
+// Scan of the counted bins and scatter: cell_start, sorted_keys, and perm
+// for keys outside the grid; element slots stay unordered in bin.slots until
+// a P2G kernel orders them into perm (mpmg_order_segment).
+int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys);
 int mpmg_nonlocal_init(mpmg_ctx *ctx);
 void mpmg_nonlocal_free(mpmg_ctx *ctx);
 int mpmg_launch_fluidity(mpmg_ctx *ctx);         // nonlocal: assembly, solve, stress
@@ -196,6 +218,47 @@ __device__ __forceinline__ double mpmg_local_coord(double xp, double xn, double 
     double sg = copysign(1.0, xl);
     if ((sg * xl) > 1.0 && ((sg * xl) - 1.0) < MPMG_TOL) xl = sg;
     return xl;
+}
+
+// Counts one key per thread into the bins (see BinScratch).  Every thread of
+// a 256-thread block must call it, with the block covering storage positions
+// 256 * blockIdx.x ... + 255 in thread order.
+__device__ __forceinline__ void mpmg_bin_count_block(uint32_t key, bool valid, uint32_t sentinel, uint32_t *bins)
+{
+    __shared__ uint32_t warp_out[8];
+    const int lane = threadIdx.x & 31;
+    const bool out = valid && key == sentinel;
+    const bool in = valid && key != sentinel;
+    const uint32_t outside = __ballot_sync(0xffffffffu, out);
+    const uint32_t inmask = __ballot_sync(0xffffffffu, in);
+    if (in) {
+        const uint32_t peers = __match_any_sync(inmask, key);
+        if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&bins[key], (uint32_t)__popc(peers));
+    }
+    if (lane == 0) warp_out[threadIdx.x >> 5] = __popc(outside);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int w = 0; w < 8; w++) t += warp_out[w];
+        bins[sentinel + blockIdx.x] = t;
+    }
+}
+
+// perm[k0..k1) = slots[k0..k1) in ascending order (insertion sort: elements
+// hold a handful of particles).
+__device__ __forceinline__ void mpmg_order_segment(const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm,
+                                                   int k0, int k1)
+{
+    for (int j = k0; j < k1; j++) {
+        const uint32_t x = slots[j];
+        int i = j - 1;
+        while (i >= k0 && perm[i] > x) {
+            perm[i + 1] = perm[i];
+            i--;
+        }
+        perm[i + 1] = x;
+    }
 }
 
 // Grid barrier over all blocks of a cooperative launch.  Every wait is

@@ -8,7 +8,7 @@
 //     domain.  A particle that leaves the grid (process_usl.c:660-666) keeps
 //     its global position in the xl, yl slots and the element sentinel.
 //   * The stored element index is the sort key: there is no separate keys
-//     pass, and the permutation's values are the constant storage positions.
+//     pass; the binning (mpmg_bin.cu) sorts storage positions by it.
 //   * The G2P runs over sorted positions and writes every particle to its
 //     sorted position in the other buffer, so the storage stays in element
 //     order from step to step at no extra traffic and the next step's gathers
@@ -148,14 +148,15 @@ __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double h,
 // ---------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(128) mx_p2g_kernel(GeomM g, const int *__restrict__ cell_start,
-                                                     const uint32_t *__restrict__ perm, Buf P,
-                                                     const StepParams *__restrict__ sp,
+                                                     const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm,
+                                                     Buf P, const StepParams *__restrict__ sp,
                                                      float *__restrict__ cell_sums)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= g.ne) return;
     const int k0 = cell_start[e], k1 = cell_start[e + 1];
     if (k0 == k1) return;
+    mpmg_order_segment(slots, perm, k0, k1);
     const float grav = (float)sp->gravity;
     const float ih = g.inv_hf;
     float acc[4][5];
@@ -190,9 +191,8 @@ __global__ void __launch_bounds__(128) mx_p2g_kernel(GeomM g, const int *__restr
 __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int *__restrict__ cell_start,
                                                       const float *__restrict__ cell_sums,
                                                       const StepParams *__restrict__ sp, double dt,
-                                                      double *__restrict__ node_m, float *__restrict__ node_ax,
-                                                      float *__restrict__ node_ay, float *__restrict__ node_vx,
-                                                      float *__restrict__ node_vy, double *__restrict__ node_mx,
+                                                      double *__restrict__ node_m, float4 *__restrict__ node4,
+                                                      double *__restrict__ node_mx,
                                                       double *__restrict__ node_my, double *__restrict__ node_fx,
                                                       double *__restrict__ node_fy)
 {
@@ -221,21 +221,23 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
     bc_mask_m(bc, i, j, g.h, sp->t + dt, bx, by);
     if (bx) { mx = 0; fx = 0; }
     if (by) { my = 0; fy = 0; }
-    float ax = 0, ay = 0, vxn = 0, vyn = 0;
+    float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
     if (m > MPMG_TOL) {
-        const float mf = (float)m;
-        ax = fx / mf;
-        ay = fy / mf;
+        // 1/m in FP64: FP32 reciprocal refined by one Newton-Raphson step
+        // r <- r + r (1 - m r), relative error ~(2^-23)^2, ample for the FP32
+        // results it scales.
+        double r = (double)__frcp_rn((float)m);
+        r = fma(r, fma(-m, r, 1.0), r);
         mx += dt * (double)fx;
         my += dt * (double)fy;
-        vxn = (float)(mx / m);
-        vyn = (float)(my / m);
+        const float rf = (float)r;
+        nd.x = fx * rf;
+        nd.y = fy * rf;
+        nd.z = (float)(mx * r);
+        nd.w = (float)(my * r);
     }
     node_m[n] = m;
-    node_ax[n] = ax;
-    node_ay[n] = ay;
-    node_vx[n] = vxn;
-    node_vy[n] = vyn;
+    node4[n] = nd;
     if (node_mx != nullptr) {
         node_mx[n] = mx;
         node_my[n] = my;
@@ -249,11 +251,9 @@ __global__ void __launch_bounds__(256) mx_g2p_kernel(GeomM g, int n, MatF mp, co
                                                      const uint32_t *__restrict__ perm,
                                                      const uint32_t *__restrict__ sorted_keys, Buf S, Buf D,
                                                      const int *__restrict__ cell_src, int *__restrict__ cell_dst,
-                                                     const float *__restrict__ node_ax,
-                                                     const float *__restrict__ node_ay,
-                                                     const float *__restrict__ node_vx,
-                                                     const float *__restrict__ node_vy, StepParams *sp,
-                                                     double dt, int gravity_mode, double gravity_const)
+                                                     const float4 *__restrict__ node4, uint32_t *__restrict__ bins,
+                                                     StepParams *sp, double dt, int gravity_mode,
+                                                     double gravity_const)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) {
@@ -269,94 +269,90 @@ __global__ void __launch_bounds__(256) mx_g2p_kernel(GeomM g, int n, MatF mp, co
         else grav = -9.8;
         sp->gravity = grav;
     }
-    if (k >= n) return;
-    const int i = (int)perm[k];
-    const int active_end = cell_start[g.ne];
-    D.pid[k] = S.pid[i];
-    if (k >= active_end) {
-        // outside the grid: carried along unchanged
-        D.xl[k] = S.xl[i]; D.yl[k] = S.yl[i]; D.vx[k] = S.vx[i]; D.vy[k] = S.vy[i];
-        D.m[k] = S.m[i]; D.v[k] = S.v[i]; D.sxx[k] = S.sxx[i]; D.sxy[k] = S.sxy[i]; D.syy[k] = S.syy[i];
-        D.ux[k] = S.ux[i]; D.uy[k] = S.uy[i];
-        if (MATERIAL == MPMG_G_LOCAL_MU2) {
-            D.Tzz[k] = S.Tzz[i]; D.gp[k] = S.gp[i]; D.gdp[k] = S.gdp[i];
-        }
-        cell_dst[k] = cell_src[i];
-        return;
-    }
-    const int e = (int)sorted_keys[k];
-    const int ci = e % g.Ex, cj = e / g.Ex;
-    const int n0 = cj * g.Nx + ci;
-    const int nd[4] = {n0, n0 + 1, n0 + 1 + g.Nx, n0 + g.Nx};
-    const float ih = g.inv_hf;
-    const float xl = S.xl[i], yl = S.yl[i];
-    const float ox = 1.0f - xl, oy = 1.0f - yl;
-    const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
-    const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
-    const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
-    float xtt = 0, ytt = 0, dux = 0, duy = 0, exx = 0, eyy = 0, dxdy = 0, dydx = 0;
+    uint32_t new_key = (uint32_t)g.ne;
+    if (k < n) {
+        const int i = (int)perm[k];
+        D.pid[k] = S.pid[i];
+        if (k >= cell_start[g.ne]) {
+            // outside the grid: carried along unchanged
+            D.xl[k] = S.xl[i]; D.yl[k] = S.yl[i]; D.vx[k] = S.vx[i]; D.vy[k] = S.vy[i];
+            D.m[k] = S.m[i]; D.v[k] = S.v[i]; D.sxx[k] = S.sxx[i]; D.sxy[k] = S.sxy[i]; D.syy[k] = S.syy[i];
+            D.ux[k] = S.ux[i]; D.uy[k] = S.uy[i];
+            if (MATERIAL == MPMG_G_LOCAL_MU2) {
+                D.Tzz[k] = S.Tzz[i]; D.gp[k] = S.gp[i]; D.gdp[k] = S.gdp[i];
+            }
+            cell_dst[k] = cell_src[i];
+        } else {
+            const int e = (int)sorted_keys[k];
+            const int ci = e % g.Ex, cj = e / g.Ex;
+            const int n0 = cj * g.Nx + ci;
+            const float ih = g.inv_hf;
+            const float xl = S.xl[i], yl = S.yl[i];
+            const float ox = 1.0f - xl, oy = 1.0f - yl;
+            const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
+            const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
+            const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
+            const float4 nq[4] = {node4[n0], node4[n0 + 1], node4[n0 + 1 + g.Nx], node4[n0 + g.Nx]};
+            float xtt = 0, ytt = 0, dux = 0, duy = 0, exx = 0, eyy = 0, dxdy = 0, dydx = 0;
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
-        const float ax = node_ax[nd[a]], ay = node_ay[nd[a]], vx = node_vx[nd[a]], vy = node_vy[nd[a]];
-        xtt += s[a] * ax;
-        ytt += s[a] * ay;
-        dux += s[a] * vx;
-        duy += s[a] * vy;
-        exx += gx[a] * vx;
-        eyy += gy[a] * vy;
-        dxdy += gy[a] * vx;
-        dydx += gx[a] * vy;
-    }
-    const float dtf = mp.dt;
-    D.vx[k] = S.vx[i] + dtf * xtt;
-    D.vy[k] = S.vy[i] + dtf * ytt;
-    dux *= dtf;
-    duy *= dtf;
-    D.ux[k] = S.ux[i] + dux;
-    D.uy[k] = S.uy[i] + duy;
-    const float exy = 0.5f * (dxdy + dydx), wxy = 0.5f * (dxdy - dydx);
-    const float m = S.m[i];
-    const float vol = S.v[i] * expf(dtf * (exx + eyy));
-    D.m[k] = m;
-    D.v[k] = vol;
-    float sxx = S.sxx[i], sxy = S.sxy[i], syy = S.syy[i];
-    if (MATERIAL == MPMG_ISOLIN) {
-        isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
-    } else {
-        float Tzz = S.Tzz[i], gp = S.gp[i], gdp;
-        g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
-        D.Tzz[k] = Tzz;
-        D.gp[k] = gp;
-        D.gdp[k] = gdp;
-    }
-    D.sxx[k] = sxx;
-    D.sxy[k] = sxy;
-    D.syy[k] = syy;
+            for (int a = 0; a < 4; a++) {
+                xtt += s[a] * nq[a].x;
+                ytt += s[a] * nq[a].y;
+                dux += s[a] * nq[a].z;
+                duy += s[a] * nq[a].w;
+                exx += gx[a] * nq[a].z;
+                eyy += gy[a] * nq[a].w;
+                dxdy += gy[a] * nq[a].z;
+                dydx += gx[a] * nq[a].w;
+            }
+            const float dtf = mp.dt;
+            D.vx[k] = S.vx[i] + dtf * xtt;
+            D.vy[k] = S.vy[i] + dtf * ytt;
+            dux *= dtf;
+            duy *= dtf;
+            D.ux[k] = S.ux[i] + dux;
+            D.uy[k] = S.uy[i] + duy;
+            const float exy = 0.5f * (dxdy + dydx), wxy = 0.5f * (dxdy - dydx);
+            const float m = S.m[i];
+            const float vol = S.v[i] * expf(dtf * (exx + eyy));
+            D.m[k] = m;
+            D.v[k] = vol;
+            float sxx = S.sxx[i], sxy = S.sxy[i], syy = S.syy[i];
+            if (MATERIAL == MPMG_ISOLIN) {
+                isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
+            } else {
+                float Tzz = S.Tzz[i], gp = S.gp[i], gdp;
+                g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
+                D.Tzz[k] = Tzz;
+                D.gp[k] = gp;
+                D.gdp[k] = gdp;
+            }
+            D.sxx[k] = sxx;
+            D.sxy[k] = sxy;
+            D.syy[k] = syy;
 
-    // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
-    float nxl = xl + dux * ih, nyl = yl + duy * ih;
-    const float fxl = floorf(nxl), fyl = floorf(nyl);
-    const int nci = ci + (int)fxl, ncj = cj + (int)fyl;
-    nxl -= fxl;
-    nyl -= fyl;
-    const float xg = ((float)nci + nxl) * g.hf, yg = ((float)ncj + nyl) * g.hf;
-    const bool inside = nci >= 0 && ncj >= 0 && nci < g.Ex && ncj < g.Ey && xg < g.xmaxf && yg < g.ymaxf &&
-                        xg >= 0.0f && yg >= 0.0f;
-    if (inside) {
-        D.xl[k] = nxl;
-        D.yl[k] = nyl;
-        cell_dst[k] = ncj * g.Ex + nci;
-    } else {
-        D.xl[k] = xg;      // global position of a particle that left the grid
-        D.yl[k] = yg;
-        cell_dst[k] = g.ne;
+            // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
+            float nxl = xl + dux * ih, nyl = yl + duy * ih;
+            const float fxl = floorf(nxl), fyl = floorf(nyl);
+            const int nci = ci + (int)fxl, ncj = cj + (int)fyl;
+            nxl -= fxl;
+            nyl -= fyl;
+            const float xg = ((float)nci + nxl) * g.hf, yg = ((float)ncj + nyl) * g.hf;
+            const bool inside = nci >= 0 && ncj >= 0 && nci < g.Ex && ncj < g.Ey && xg < g.xmaxf &&
+                                yg < g.ymaxf && xg >= 0.0f && yg >= 0.0f;
+            if (inside) {
+                D.xl[k] = nxl;
+                D.yl[k] = nyl;
+                new_key = (uint32_t)(ncj * g.Ex + nci);
+            } else {
+                D.xl[k] = xg;      // global position of a particle that left the grid
+                D.yl[k] = yg;
+            }
+            cell_dst[k] = (int)new_key;
+        }
     }
-}
-
-__global__ void iota_kernel(uint32_t *v, int n)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) v[i] = (uint32_t)i;
+    // the next step's element counts (the binning's first phase)
+    mpmg_bin_count_block(new_key, k < n, (uint32_t)g.ne, bins);
 }
 
 inline int blocks_for(size_t n, int threads)
@@ -482,9 +478,7 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
         if ((rc = dalloc(&s->pid[b], n)) != MPMG_OK) return rc;
     }
     if ((rc = dalloc(&s->cell_sums, 20 * ctx->ne)) != MPMG_OK) return rc;
-    float **nf[] = {&s->node_ax, &s->node_ay, &s->node_vx, &s->node_vy};
-    for (float **p : nf)
-        if ((rc = dalloc(p, ctx->nn)) != MPMG_OK) return rc;
+    if ((rc = dalloc(&s->node4, ctx->nn)) != MPMG_OK) return rc;
 
     // host staging
     std::vector<float> hx(n ? n : 1), hy(n ? n : 1), tmp(n ? n : 1);
@@ -521,10 +515,10 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
         if (e == cudaSuccess) e = cudaMemcpy(ctx->in_element, cell.data(), n * sizeof(int), cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed state upload");
-    iota_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(ctx->vals, (int)n);
-    ctx->launches += 1;
     s->cur = 0;
-    s->keys_valid = 1;
+    // the first step's element counts; every G2P counts the next step's
+    int rcc = mpmg_bin_count(ctx, (const uint32_t *)ctx->in_element);
+    if (rcc != MPMG_OK) return rcc;
     MPMG_CHECK(cudaGetLastError());
     return MPMG_OK;
 }
@@ -540,10 +534,7 @@ void mpmg_mixed_free(mpmg_ctx *ctx)
         cudaFree(s->pid[b]);
     }
     cudaFree(s->cell_sums);
-    cudaFree(s->node_ax);
-    cudaFree(s->node_ay);
-    cudaFree(s->node_vx);
-    cudaFree(s->node_vy);
+    cudaFree(s->node4);
     delete s;
     ctx->mixed = nullptr;
 }
@@ -566,20 +557,20 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     const int cur = s->cur, nxt = 1 - cur;
 
     mpmg_phase_begin(ctx, PH_SORT);
-    ctx->launches += mpmg_sort_run((const uint32_t *)cell_array(ctx, cur), ctx->vals, n, (int)ctx->ne, ctx->key_bits,
-                                   ctx->sort, ctx->sorted_keys, ctx->perm, ctx->cell_start, st);
+    int rc = mpmg_bin_scan_scatter(ctx, (const uint32_t *)cell_array(ctx, cur));
+    if (rc != MPMG_OK) return rc;
     mpmg_phase_end(ctx, PH_SORT);
 
     Buf S = buf(s, cur), D = buf(s, nxt);
     mpmg_phase_begin(ctx, PH_P2G);
-    mx_p2g_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(g, ctx->cell_start, ctx->perm, S, ctx->d_params,
-                                                            s->cell_sums);
+    mx_p2g_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(g, ctx->cell_start, ctx->bin.slots, ctx->perm, S,
+                                                            ctx->d_params, s->cell_sums);
     mpmg_phase_end(ctx, PH_P2G);
 
     mpmg_phase_begin(ctx, PH_GRID);
     mx_grid_kernel<<<blocks_for(ctx->nn, 256), 256, 0, st>>>(
-        g, make_bc(ctx), ctx->cell_start, s->cell_sums, ctx->d_params, c.dt, ctx->node_m, s->node_ax, s->node_ay,
-        s->node_vx, s->node_vy, ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy);
+        g, make_bc(ctx), ctx->cell_start, s->cell_sums, ctx->d_params, c.dt, ctx->node_m, s->node4,
+        ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy);
     mpmg_phase_end(ctx, PH_GRID);
 
     mpmg_phase_begin(ctx, PH_G2P);
@@ -587,11 +578,11 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     if (c.material == MPMG_ISOLIN) {
         mx_g2p_kernel<MPMG_ISOLIN><<<blocks_for(n, 256), 256, 0, st>>>(
             g, n, mp, ctx->cell_start, ctx->perm, ctx->sorted_keys, S, D, cell_array(ctx, cur), cell_array(ctx, nxt),
-            s->node_ax, s->node_ay, s->node_vx, s->node_vy, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+            s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
     } else {
         mx_g2p_kernel<MPMG_G_LOCAL_MU2><<<blocks_for(n, 256), 256, 0, st>>>(
             g, n, mp, ctx->cell_start, ctx->perm, ctx->sorted_keys, S, D, cell_array(ctx, cur), cell_array(ctx, nxt),
-            s->node_ax, s->node_ay, s->node_vx, s->node_vy, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+            s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
     }
     mpmg_phase_end(ctx, PH_G2P);
     ctx->launches += 3;
@@ -649,15 +640,18 @@ int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out)
     std::vector<float> a, bb;
     int rc;
     if (strncmp(name, "node_", 5) == 0) {
-        const float *src = nullptr;
-        if (strcmp(name, "node_ax") == 0) src = s->node_ax;
-        else if (strcmp(name, "node_ay") == 0) src = s->node_ay;
-        else if (strcmp(name, "node_vx") == 0) src = s->node_vx;
-        else if (strcmp(name, "node_vy") == 0) src = s->node_vy;
-        if (src == nullptr) return MPMG_ERR_UNKNOWN_FIELD;   // FP64 node arrays: the common path
-        std::vector<float> h(ctx->nn);
-        MPMG_CHECK(cudaMemcpy(h.data(), src, ctx->nn * sizeof(float), cudaMemcpyDeviceToHost));
-        for (size_t k = 0; k < ctx->nn; k++) out[k] = h[k];
+        int comp = -1;
+        if (strcmp(name, "node_ax") == 0) comp = 0;
+        else if (strcmp(name, "node_ay") == 0) comp = 1;
+        else if (strcmp(name, "node_vx") == 0) comp = 2;
+        else if (strcmp(name, "node_vy") == 0) comp = 3;
+        if (comp < 0) return MPMG_ERR_UNKNOWN_FIELD;   // FP64 node arrays: the common path
+        std::vector<float4> h(ctx->nn);
+        MPMG_CHECK(cudaMemcpy(h.data(), s->node4, ctx->nn * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < ctx->nn; k++) {
+            const float4 v = h[k];
+            out[k] = comp == 0 ? v.x : comp == 1 ? v.y : comp == 2 ? v.z : v.w;
+        }
         return MPMG_OK;
     }
     if ((rc = download_i(ctx, s->pid[b], pid)) != MPMG_OK) return rc;

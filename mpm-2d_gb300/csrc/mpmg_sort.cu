@@ -1,5 +1,8 @@
 // Stable LSD radix sort of (element key, particle index) pairs, and the
-// per-element start offsets of the sorted order.
+// per-element start offsets of the sorted order.  The allocation-free entry
+// point (mpmg_sort_noalloc.cu) runs it on its fixed scratch; the step bins
+// particles with the counting sort of mpmg_bin.cu, which gives the same
+// order.
 //
 // The reference groups particles by element in find_filled_elements
 // (libmpm/process_usl.c:677-723): for each element, its particles in
@@ -192,30 +195,6 @@ size_t mpmg_sort_scratch_words(size_t n, int key_bits, int *num_tiles_out)
     return 2 * (n > 0 ? n : 1) + (size_t)kMaxRadix * tiles + kMaxRadix;
 }
 
-int mpmg_sort_init(mpmg_ctx *ctx)
-{
-    size_t n = ctx->np;
-    int tiles = 1;
-    mpmg_sort_scratch_words(n, ctx->key_bits, &tiles);
-    ctx->sort.num_tiles = tiles;
-    ctx->sort.capacity = (int)n;
-    size_t cap = n > 0 ? n : 1;
-    MPMG_CHECK(cudaMalloc(&ctx->sort.keys_alt, cap * sizeof(uint32_t)));
-    MPMG_CHECK(cudaMalloc(&ctx->sort.vals_alt, cap * sizeof(uint32_t)));
-    MPMG_CHECK(cudaMalloc(&ctx->sort.tile_hist, (size_t)kMaxRadix * tiles * sizeof(uint32_t)));
-    MPMG_CHECK(cudaMalloc(&ctx->sort.digit_total, (size_t)kMaxRadix * sizeof(uint32_t)));
-    return MPMG_OK;
-}
-
-void mpmg_sort_free(mpmg_ctx *ctx)
-{
-    cudaFree(ctx->sort.keys_alt);
-    cudaFree(ctx->sort.vals_alt);
-    cudaFree(ctx->sort.tile_hist);
-    cudaFree(ctx->sort.digit_total);
-    ctx->sort.keys_alt = ctx->sort.vals_alt = ctx->sort.tile_hist = ctx->sort.digit_total = nullptr;
-}
-
 // Sorts keys/vals (n entries, keys < 2^key_bits) into sorted_keys/perm using
 // the given scratch, then fills cell_start[0..ne].  Returns launches issued.
 int mpmg_sort_run(const uint32_t *keys, const uint32_t *vals, int n, int ne, int key_bits,
@@ -248,14 +227,4 @@ int mpmg_sort_run(const uint32_t *keys, const uint32_t *vals, int n, int ne, int
     }
     cell_start_kernel<<<(ne + 1 + 255) / 256, 256, 0, s>>>(sorted_keys, n, ne, cell_start);
     return launches + 1;
-}
-
-// Sorts (ctx->keys, ctx->vals) into (ctx->sorted_keys, ctx->perm) and fills
-// ctx->cell_start.
-int mpmg_sort_keys(mpmg_ctx *ctx)
-{
-    ctx->launches += mpmg_sort_run(ctx->keys, ctx->vals, (int)ctx->np, (int)ctx->ne, ctx->key_bits, ctx->sort,
-                                   ctx->sorted_keys, ctx->perm, ctx->cell_start, ctx->stream);
-    MPMG_CHECK(cudaGetLastError());
-    return MPMG_OK;
 }

@@ -5,9 +5,10 @@
 // memory to its own pool allocator may forbid any other allocation; and a
 // plugin that the reference's C driver dlopens (materials and boundary
 // conditions) has no handle on device memory management at all.  This entry
-// point serves them.  It runs the same stable radix sort and element offsets
-// that every mpmg_step performs, on device arrays the caller passes in and
-// out.  Its scratch lives in one fixed, file-scope device array.
+// point serves them.  It produces the same stable element order and offsets
+// as the binning every mpmg_step performs, with the LSD radix sort of
+// mpmg_sort.cu, on device arrays the caller passes in and out.  Its scratch
+// lives in one fixed, file-scope device array.
 //
 // The scratch array below is held by every GPU that loads this library, for
 // the life of the process.  Its capacity is MPMG_NOALLOC_MAX_PARTICLES keys

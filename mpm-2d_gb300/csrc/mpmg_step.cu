@@ -4,8 +4,8 @@
 //
 //   keys      element of every particle (WHICH_ELEMENT4, :43-44 and :631-674);
 //             advances t and the gravity scalar in the device StepParams
-//   sort      stable radix sort of (element, particle) -> per-element
-//             particle segments (find_filled_elements, :677-723)
+//   bin       stable counting sort of (element, particle) -> per-element
+//             particle segments (find_filled_elements, :677-723; mpmg_bin.cu)
 //   p2g       one thread per element sums its particles' contributions to
 //             its four corners (map_to_grid_explicit_split, :812-910)
 //   grid      one thread per node adds the four adjacent elements' corner
@@ -43,11 +43,11 @@ struct BcParams {
 // ---------------------------------------------------------------------------
 // keys
 
-__global__ void keys_kernel(GridGeom g, int n, const double *__restrict__ x,
-                            const double *__restrict__ y, int *__restrict__ in_element,
-                            int *__restrict__ active, uint32_t *__restrict__ keys,
-                            uint32_t *__restrict__ vals, uint32_t sentinel, StepParams *sp,
-                            double dt, int gravity_mode, double gravity_const)
+__global__ void __launch_bounds__(256) keys_kernel(GridGeom g, int n, const double *__restrict__ x,
+                                                   const double *__restrict__ y, int *__restrict__ in_element,
+                                                   int *__restrict__ active, uint32_t *__restrict__ keys,
+                                                   uint32_t sentinel, uint32_t *__restrict__ bins, StepParams *sp,
+                                                   double dt, int gravity_mode, double gravity_const)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         // time_varying_loads (loading.c:34-54) of the previous step's tail, or
@@ -68,20 +68,21 @@ __global__ void keys_kernel(GridGeom g, int n, const double *__restrict__ x,
         sp->t = t + dt;
         sp->step_count += 1;
     }
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t key = sentinel;
-    if (active[i]) {
-        int e = mpmg_which_element(x[i], y[i], g.h, g.inv_h, g.xmax, g.ymax, g.Ex, g.Ey);
-        in_element[i] = e;
-        if (e < 0) {
-            active[i] = 0;   // process_usl.c:660-666: outside the grid for good
-        } else {
-            key = (uint32_t)e;
+    if (i < n) {
+        if (active[i]) {
+            int e = mpmg_which_element(x[i], y[i], g.h, g.inv_h, g.xmax, g.ymax, g.Ex, g.Ey);
+            in_element[i] = e;
+            if (e < 0) {
+                active[i] = 0;   // process_usl.c:660-666: outside the grid for good
+            } else {
+                key = (uint32_t)e;
+            }
         }
+        keys[i] = key;
     }
-    keys[i] = key;
-    vals[i] = (uint32_t)i;
+    mpmg_bin_count_block(key, i < n, sentinel, bins);
 }
 
 // ---------------------------------------------------------------------------
@@ -113,7 +114,8 @@ __device__ __forceinline__ ShapeFns shape(double xl, double yl, double inv_h)
 }
 
 __global__ void __launch_bounds__(128) p2g_cells_kernel(
-    GridGeom g, int ne, const int *__restrict__ cell_start, const uint32_t *__restrict__ perm,
+    GridGeom g, int ne, const int *__restrict__ cell_start, const uint32_t *__restrict__ slots,
+    uint32_t *__restrict__ perm,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ m,
     const double *__restrict__ vx, const double *__restrict__ vy, const double *__restrict__ v,
     const double *__restrict__ sxx, const double *__restrict__ sxy, const double *__restrict__ syy,
@@ -123,6 +125,7 @@ __global__ void __launch_bounds__(128) p2g_cells_kernel(
     if (e >= ne) return;
     const int k0 = cell_start[e], k1 = cell_start[e + 1];
     if (k0 == k1) return;
+    mpmg_order_segment(slots, perm, k0, k1);     // ascending particle index, as the reference's lists
     const int ci = e % g.Ex, cj = e / g.Ex;
     const double xn = ci * g.h, yn = cj * g.h;   // node_number_to_coords (element.c:10-19)
     const double grav = sp->gravity;
@@ -480,19 +483,19 @@ int mpmg_launch_step(mpmg_ctx *ctx)
 
     mpmg_phase_begin(ctx, PH_KEYS);
     keys_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, n, ctx->x, ctx->y, ctx->in_element, ctx->active,
-                                                   ctx->keys, ctx->vals, (uint32_t)ne, ctx->d_params,
+                                                   ctx->keys, (uint32_t)ne, ctx->bin.counts, ctx->d_params,
                                                    c.dt, c.gravity_mode, c.gravity);
     ctx->launches += 1;
     mpmg_phase_end(ctx, PH_KEYS);
 
     mpmg_phase_begin(ctx, PH_SORT);
-    int rc = mpmg_sort_keys(ctx);
+    int rc = mpmg_bin_scan_scatter(ctx, ctx->keys);
     if (rc != MPMG_OK) return rc;
     mpmg_phase_end(ctx, PH_SORT);
 
     mpmg_phase_begin(ctx, PH_P2G);
     p2g_cells_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(
-        g, ne, ctx->cell_start, ctx->perm, ctx->x, ctx->y, ctx->m, ctx->vx, ctx->vy, ctx->v, ctx->sxx,
+        g, ne, ctx->cell_start, ctx->bin.slots, ctx->perm, ctx->x, ctx->y, ctx->m, ctx->vx, ctx->vy, ctx->v, ctx->sxx,
         ctx->sxy, ctx->syy, ctx->d_params, ctx->cell_sums);
     ctx->launches += 1;
     mpmg_phase_end(ctx, PH_P2G);
