@@ -186,9 +186,9 @@ MPMG_API int mpmg_last_solve(mpmg_ctx *ctx, int *iterations, double *rel_residua
 MPMG_API int mpmg_launch_count(mpmg_ctx *ctx, long *launches, int reset);
 
 /*
- * Cell sort without any allocation.  No counterpart in the reference: it is
- * the element binning every mpmg_step performs (the GPU form of
- * find_filled_elements, libmpm/process_usl.c:677-723), offered to callers
+ * Cell sort without any allocation.  No counterpart in the reference: it
+ * gives the same element order as the binning every mpmg_step performs (the
+ * GPU form of find_filled_elements, libmpm/process_usl.c:677-723), to callers
  * that cannot call cudaMalloc -- code inside a CUDA stream capture, hosts
  * whose device memory belongs to their own pool allocator, and the
  * reference's dlopen'd plugins, which own no device memory.

@@ -730,12 +730,12 @@ int mpmg_get_sort(mpmg_ctx *ctx, int *sorted_keys, int *perm, int *cell_start)
         if (ctx->mixed) {
             // The mixed form's permutation indexes the storage it sorted (the
             // buffer before the last step's swap); report particle indices.
-            int *pid = new int[ctx->np];
-            cudaError_t e = cudaMemcpy(pid, ctx->mixed->pid[1 - ctx->mixed->cur], ctx->np * sizeof(int),
+            float4 *rec = new float4[ctx->np];
+            cudaError_t e = cudaMemcpy(rec, ctx->mixed->D[1 - ctx->mixed->cur], ctx->np * sizeof(float4),
                                        cudaMemcpyDeviceToHost);
             if (e == cudaSuccess)
-                for (size_t k = 0; k < ctx->np; k++) perm[k] = pid[perm[k]];
-            delete[] pid;
+                for (size_t k = 0; k < ctx->np; k++) perm[k] = mpmg_float_bits(rec[perm[k]].z);
+            delete[] rec;
             if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed permutation read-back");
         }
     }

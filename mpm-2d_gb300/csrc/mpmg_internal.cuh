@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/mpm_gb300.h"
 
@@ -51,25 +52,28 @@ struct SortScratch {
     int capacity;          // particles
 };
 
-// Mixed-precision particle storage: FP32 structure of arrays kept in element
-// order, double-buffered (the G2P reads buffer `cur` through the sort's
-// permutation and writes buffer 1 - cur in sorted order).
+// Mixed-precision particle storage: four float4 records per particle, kept
+// in element order and double-buffered (the G2P reads buffer `cur` and writes
+// each particle to its sorted position in buffer 1 - cur):
+//   A = {xl, yl, vx, vy}   B = {m, v, sxx, sxy}
+//   C = {syy, ux, uy, Tzz} D = {gammap, gammadotp, pid (int bits), 0}
+// The P2G reads A, B, C; the G2P reads and writes all four.
 struct MixedState {
-    float *x[2], *y[2], *vx[2], *vy[2], *m[2], *v[2], *sxx[2], *sxy[2], *syy[2];
-    float *ux[2], *uy[2], *Tzz[2], *gp[2], *gdp[2];
-    int *pid[2];           // caller's particle index of each stored particle
+    float4 *A[2], *B[2], *C[2], *D[2];
     int cur;
     float *cell_sums;      // 20 FP32 corner sums per element, value-major
     float4 *node4;         // per node: ax, ay, vx, vy (FP32) for the gathers
 };
 
 // Counting-sort binning scratch (mpmg_bin.cu).  Bins 0..ne-1 count the keys
-// of each element, bin ne + b the keys outside the grid in 256-key block b.
+// of each element, bin ne + g the keys outside the grid at storage positions
+// 32 g .. 32 g + 31.
 struct BinScratch {
     uint32_t *counts;      // bins (zero between steps)
     uint32_t *cursor;      // scatter cursors (exclusive prefix of the bins)
-    uint32_t *tile_sums;   // per 2048-bin tile
+    unsigned long long *tile_state;   // per 2048-bin tile: look-back flag + value, then a ticket
     uint32_t *slots;       // n scattered storage positions, unordered within elements
+    uint32_t *rank;        // n: sorted position of each storage position
     int bins;
     int tiles;
 };
@@ -139,6 +143,21 @@ struct mpmg_ctx {
     long phase_launches[PH_COUNT];
     long launches;
 };
+
+// Bit casts usable in host code (particle ids travel in float4 records).
+static inline int mpmg_float_bits(float f)
+{
+    int i;
+    memcpy(&i, &f, sizeof(i));
+    return i;
+}
+
+static inline float mpmg_bits_float(int i)
+{
+    float f;
+    memcpy(&f, &i, sizeof(f));
+    return f;
+}
 
 // Error helpers (host).
 void mpmg_set_error(const char *fmt, ...);
@@ -220,35 +239,27 @@ __device__ __forceinline__ double mpmg_local_coord(double xp, double xn, double 
     return xl;
 }
 
-// Counts one key per thread into the bins (see BinScratch).  Every thread of
-// a 256-thread block must call it, with the block covering storage positions
-// 256 * blockIdx.x ... + 255 in thread order.
-__device__ __forceinline__ void mpmg_bin_count_block(uint32_t key, bool valid, uint32_t sentinel, uint32_t *bins)
+// Counts one key into the bins (see BinScratch): bins[key] for keys inside
+// the grid, bins[sentinel + group] for keys outside it, where group is the
+// key's destination position / 32.  Equal bins within a warp are aggregated
+// into one atomic.  Every lane of the warp must call it (valid marks lanes
+// that carry a key).
+__device__ __forceinline__ void mpmg_bin_count(uint32_t key, bool valid, uint32_t sentinel, uint32_t group,
+                                               uint32_t *bins)
 {
-    __shared__ uint32_t warp_out[8];
-    const int lane = threadIdx.x & 31;
-    const bool out = valid && key == sentinel;
-    const bool in = valid && key != sentinel;
-    const uint32_t outside = __ballot_sync(0xffffffffu, out);
-    const uint32_t inmask = __ballot_sync(0xffffffffu, in);
-    if (in) {
-        const uint32_t peers = __match_any_sync(inmask, key);
-        if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&bins[key], (uint32_t)__popc(peers));
-    }
-    if (lane == 0) warp_out[threadIdx.x >> 5] = __popc(outside);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t t = 0;
-#pragma unroll
-        for (int w = 0; w < 8; w++) t += warp_out[w];
-        bins[sentinel + blockIdx.x] = t;
+    const uint32_t bin = (key == sentinel) ? sentinel + group : key;
+    const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+        const uint32_t peers = __match_any_sync(vmask, bin);
+        const int lane = threadIdx.x & 31;
+        if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&bins[bin], (uint32_t)__popc(peers));
     }
 }
 
 // perm[k0..k1) = slots[k0..k1) in ascending order (insertion sort: elements
-// hold a handful of particles).
+// hold a handful of particles), and rank[perm[k]] = k when rank is given.
 __device__ __forceinline__ void mpmg_order_segment(const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm,
-                                                   int k0, int k1)
+                                                   uint32_t *__restrict__ rank, int k0, int k1)
 {
     for (int j = k0; j < k1; j++) {
         const uint32_t x = slots[j];
@@ -259,6 +270,8 @@ __device__ __forceinline__ void mpmg_order_segment(const uint32_t *__restrict__ 
         }
         perm[i + 1] = x;
     }
+    if (rank != nullptr)
+        for (int j = k0; j < k1; j++) rank[perm[j]] = (uint32_t)j;
 }
 
 // Grid barrier over all blocks of a cooperative launch.  Every wait is

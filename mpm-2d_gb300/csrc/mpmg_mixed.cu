@@ -9,10 +9,11 @@
 //     its global position in the xl, yl slots and the element sentinel.
 //   * The stored element index is the sort key: there is no separate keys
 //     pass; the binning (mpmg_bin.cu) sorts storage positions by it.
-//   * The G2P runs over sorted positions and writes every particle to its
-//     sorted position in the other buffer, so the storage stays in element
-//     order from step to step at no extra traffic and the next step's gathers
-//     through the permutation are nearly sequential.
+//   * The G2P runs over stored particles (independent, coalesced loads) and
+//     writes each one to its sorted position (the binning's inverse
+//     permutation) in the other buffer, so the storage stays in element order
+//     from step to step at no extra traffic and the next step's gathers are
+//     nearly sequential.
 //   * P2G corner sums of an element's particle segment are FP32 (a few
 //     particles each); the four elements around a node are summed in FP64 for
 //     mass and momentum, the momentum update and the division by nodal mass
@@ -44,17 +45,16 @@ struct BcM {
 };
 
 struct Buf {
-    float *xl, *yl, *vx, *vy, *m, *v, *sxx, *sxy, *syy, *ux, *uy, *Tzz, *gp, *gdp;
-    int *pid;
+    float4 *A, *B, *C, *D;
 };
 
 Buf buf(const MixedState *s, int b)
 {
     Buf o;
-    o.xl = s->x[b]; o.yl = s->y[b]; o.vx = s->vx[b]; o.vy = s->vy[b]; o.m = s->m[b]; o.v = s->v[b];
-    o.sxx = s->sxx[b]; o.sxy = s->sxy[b]; o.syy = s->syy[b]; o.ux = s->ux[b]; o.uy = s->uy[b];
-    o.Tzz = s->Tzz[b]; o.gp = s->gp[b]; o.gdp = s->gdp[b];
-    o.pid = s->pid[b];
+    o.A = s->A[b];
+    o.B = s->B[b];
+    o.C = s->C[b];
+    o.D = s->D[b];
     return o;
 }
 
@@ -124,6 +124,23 @@ __device__ __forceinline__ void g_local_mu2_f(const MatF &p, float m, float v, f
     gdp = nup;
 }
 
+// Exact FP32 -> FP64 widening on the integer pipe (IEEE 754 field
+// re-encoding: the exponent bias moves from 127 to 1023, the 23-bit fraction
+// moves to the top of the 52-bit one).  FP32 subnormals (below 1.2e-38, far
+// under any nodal mass or momentum here) become zero; infinities and NaNs
+// take the hardware conversion.  GB300's FP64 pipe is the grid kernel's
+// bottleneck, and twelve widenings per node would otherwise run on it.
+__device__ __forceinline__ double widen(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0xffu) return (double)f;
+    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+    if (e == 0u) return __longlong_as_double((long long)sign);
+    const uint64_t bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
 __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double h, double t_now, bool &mx,
                                           bool &my)
 {
@@ -147,16 +164,17 @@ __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double h,
 
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128) mx_p2g_kernel(GeomM g, const int *__restrict__ cell_start,
+__global__ void __launch_bounds__(128, 8) mx_p2g_kernel(GeomM g, const int *__restrict__ cell_start,
                                                      const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm,
-                                                     Buf P, const StepParams *__restrict__ sp,
+                                                     uint32_t *__restrict__ rank, Buf P,
+                                                     const StepParams *__restrict__ sp,
                                                      float *__restrict__ cell_sums)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= g.ne) return;
     const int k0 = cell_start[e], k1 = cell_start[e + 1];
     if (k0 == k1) return;
-    mpmg_order_segment(slots, perm, k0, k1);
+    mpmg_order_segment(slots, perm, rank, k0, k1);
     const float grav = (float)sp->gravity;
     const float ih = g.inv_hf;
     float acc[4][5];
@@ -166,13 +184,15 @@ __global__ void __launch_bounds__(128) mx_p2g_kernel(GeomM g, const int *__restr
         for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
     for (int k = k0; k < k1; k++) {
         const int i = (int)perm[k];
-        const float xl = P.xl[i], yl = P.yl[i], m = P.m[i], vol = P.v[i];
+        const float4 a4 = P.A[i], b4 = P.B[i];
+        const float syy = P.C[i].x;
+        const float xl = a4.x, yl = a4.y, m = b4.x, vol = b4.y;
         const float ox = 1.0f - xl, oy = 1.0f - yl;
         const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
         const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
         const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
-        const float pmx = P.vx[i] * m, pmy = P.vy[i] * m, pby = grav * m;
-        const float s0 = -P.sxx[i] * vol, s1 = -P.sxy[i] * vol, s2 = -P.syy[i] * vol;
+        const float pmx = a4.z * m, pmy = a4.w * m, pby = grav * m;
+        const float s0 = -b4.z * vol, s1 = -b4.w * vol, s2 = -syy * vol;
 #pragma unroll
         for (int a = 0; a < 4; a++) {
             acc[a][0] += s[a] * m;
@@ -211,9 +231,9 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
         if (cell_start[e] == cell_start[e + 1]) continue;
         int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
         const float *cs = cell_sums + (size_t)(a * 5) * g.ne + e;
-        m += (double)cs[0];
-        mx += (double)cs[(size_t)g.ne];
-        my += (double)cs[(size_t)2 * g.ne];
+        m += widen(cs[0]);
+        mx += widen(cs[(size_t)g.ne]);
+        my += widen(cs[(size_t)2 * g.ne]);
         fx += cs[(size_t)3 * g.ne];
         fy += cs[(size_t)4 * g.ne];
     }
@@ -246,17 +266,17 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
     }
 }
 
+// One thread per stored particle i (coalesced, independent loads); the
+// particle is written to its sorted position rank[i] of the other buffer.
 template <int MATERIAL>
-__global__ void __launch_bounds__(256) mx_g2p_kernel(GeomM g, int n, MatF mp, const int *__restrict__ cell_start,
-                                                     const uint32_t *__restrict__ perm,
-                                                     const uint32_t *__restrict__ sorted_keys, Buf S, Buf D,
-                                                     const int *__restrict__ cell_src, int *__restrict__ cell_dst,
-                                                     const float4 *__restrict__ node4, uint32_t *__restrict__ bins,
-                                                     StepParams *sp, double dt, int gravity_mode,
-                                                     double gravity_const)
+__global__ void __launch_bounds__(256, 4) mx_g2p_kernel(GeomM g, int n, MatF mp, const uint32_t *__restrict__ rank,
+                                                     Buf S, Buf D, const int *__restrict__ cell_src,
+                                                     int *__restrict__ cell_dst, const float4 *__restrict__ node4,
+                                                     uint32_t *__restrict__ bins, StepParams *sp, double dt,
+                                                     int gravity_mode, double gravity_const)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
         // Advance t and compute the next step's body force (the driver's
         // time_varying_loads, loading.c:34-54).  No kernel of this step reads
         // them after this point.
@@ -270,24 +290,23 @@ __global__ void __launch_bounds__(256) mx_g2p_kernel(GeomM g, int n, MatF mp, co
         sp->gravity = grav;
     }
     uint32_t new_key = (uint32_t)g.ne;
-    if (k < n) {
-        const int i = (int)perm[k];
-        D.pid[k] = S.pid[i];
-        if (k >= cell_start[g.ne]) {
+    uint32_t dst = 0;
+    if (i < n) {
+        dst = rank[i];
+        const int e = cell_src[i];
+        const float4 a4 = S.A[i], b4 = S.B[i], c4 = S.C[i], d4 = S.D[i];
+        if (e >= g.ne) {
             // outside the grid: carried along unchanged
-            D.xl[k] = S.xl[i]; D.yl[k] = S.yl[i]; D.vx[k] = S.vx[i]; D.vy[k] = S.vy[i];
-            D.m[k] = S.m[i]; D.v[k] = S.v[i]; D.sxx[k] = S.sxx[i]; D.sxy[k] = S.sxy[i]; D.syy[k] = S.syy[i];
-            D.ux[k] = S.ux[i]; D.uy[k] = S.uy[i];
-            if (MATERIAL == MPMG_G_LOCAL_MU2) {
-                D.Tzz[k] = S.Tzz[i]; D.gp[k] = S.gp[i]; D.gdp[k] = S.gdp[i];
-            }
-            cell_dst[k] = cell_src[i];
+            D.A[dst] = a4;
+            D.B[dst] = b4;
+            D.C[dst] = c4;
+            D.D[dst] = d4;
+            cell_dst[dst] = g.ne;
         } else {
-            const int e = (int)sorted_keys[k];
             const int ci = e % g.Ex, cj = e / g.Ex;
             const int n0 = cj * g.Nx + ci;
             const float ih = g.inv_hf;
-            const float xl = S.xl[i], yl = S.yl[i];
+            const float xl = a4.x, yl = a4.y;
             const float ox = 1.0f - xl, oy = 1.0f - yl;
             const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
             const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
@@ -306,30 +325,18 @@ __global__ void __launch_bounds__(256) mx_g2p_kernel(GeomM g, int n, MatF mp, co
                 dydx += gx[a] * nq[a].w;
             }
             const float dtf = mp.dt;
-            D.vx[k] = S.vx[i] + dtf * xtt;
-            D.vy[k] = S.vy[i] + dtf * ytt;
+            const float vx = a4.z + dtf * xtt, vy = a4.w + dtf * ytt;
             dux *= dtf;
             duy *= dtf;
-            D.ux[k] = S.ux[i] + dux;
-            D.uy[k] = S.uy[i] + duy;
             const float exy = 0.5f * (dxdy + dydx), wxy = 0.5f * (dxdy - dydx);
-            const float m = S.m[i];
-            const float vol = S.v[i] * expf(dtf * (exx + eyy));
-            D.m[k] = m;
-            D.v[k] = vol;
-            float sxx = S.sxx[i], sxy = S.sxy[i], syy = S.syy[i];
+            const float m = b4.x;
+            const float vol = b4.y * expf(dtf * (exx + eyy));
+            float sxx = b4.z, sxy = b4.w, syy = c4.x, Tzz = c4.w, gp = d4.x, gdp = d4.y;
             if (MATERIAL == MPMG_ISOLIN) {
                 isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
             } else {
-                float Tzz = S.Tzz[i], gp = S.gp[i], gdp;
                 g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
-                D.Tzz[k] = Tzz;
-                D.gp[k] = gp;
-                D.gdp[k] = gdp;
             }
-            D.sxx[k] = sxx;
-            D.sxy[k] = sxy;
-            D.syy[k] = syy;
 
             // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
             float nxl = xl + dux * ih, nyl = yl + duy * ih;
@@ -341,18 +348,20 @@ __global__ void __launch_bounds__(256) mx_g2p_kernel(GeomM g, int n, MatF mp, co
             const bool inside = nci >= 0 && ncj >= 0 && nci < g.Ex && ncj < g.Ey && xg < g.xmaxf &&
                                 yg < g.ymaxf && xg >= 0.0f && yg >= 0.0f;
             if (inside) {
-                D.xl[k] = nxl;
-                D.yl[k] = nyl;
                 new_key = (uint32_t)(ncj * g.Ex + nci);
             } else {
-                D.xl[k] = xg;      // global position of a particle that left the grid
-                D.yl[k] = yg;
+                nxl = xg;      // global position of a particle that left the grid
+                nyl = yg;
             }
-            cell_dst[k] = (int)new_key;
+            D.A[dst] = make_float4(nxl, nyl, vx, vy);
+            D.B[dst] = make_float4(m, vol, sxx, sxy);
+            D.C[dst] = make_float4(syy, c4.y + dux, c4.z + duy, Tzz);
+            D.D[dst] = make_float4(gp, gdp, d4.z, 0.0f);
+            cell_dst[dst] = (int)new_key;
         }
     }
-    // the next step's element counts (the binning's first phase)
-    mpmg_bin_count_block(new_key, k < n, (uint32_t)g.ne, bins);
+    // the next step's bins, by destination position (the binning's first phase)
+    mpmg_bin_count(new_key, i < n, (uint32_t)g.ne, dst >> 5, bins);
 }
 
 inline int blocks_for(size_t n, int threads)
@@ -463,64 +472,39 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     memset(s, 0, sizeof(*s));
     ctx->mixed = s;
     const size_t n = ctx->np;
-    const bool mu2 = ctx->cfg.material == MPMG_G_LOCAL_MU2;
     int rc;
     for (int b = 0; b < 2; b++) {
-        float **f[] = {&s->x[b], &s->y[b], &s->vx[b], &s->vy[b], &s->m[b], &s->v[b], &s->sxx[b], &s->sxy[b],
-                       &s->syy[b], &s->ux[b], &s->uy[b]};
-        for (float **p : f)
+        float4 **f[] = {&s->A[b], &s->B[b], &s->C[b], &s->D[b]};
+        for (float4 **p : f)
             if ((rc = dalloc(p, n)) != MPMG_OK) return rc;
-        if (mu2) {
-            if ((rc = dalloc(&s->Tzz[b], n)) != MPMG_OK) return rc;
-            if ((rc = dalloc(&s->gp[b], n)) != MPMG_OK) return rc;
-            if ((rc = dalloc(&s->gdp[b], n)) != MPMG_OK) return rc;
-        }
-        if ((rc = dalloc(&s->pid[b], n)) != MPMG_OK) return rc;
     }
     if ((rc = dalloc(&s->cell_sums, 20 * ctx->ne)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->node4, ctx->nn)) != MPMG_OK) return rc;
 
-    // host staging
-    std::vector<float> hx(n ? n : 1), hy(n ? n : 1), tmp(n ? n : 1);
-    std::vector<int> cell(n ? n : 1), pid(n ? n : 1);
+    // host staging: element, local coordinates, records
+    std::vector<float4> ha(n ? n : 1), hb(n ? n : 1), hc(n ? n : 1), hd(n ? n : 1);
+    std::vector<int> cell(n ? n : 1);
     for (size_t i = 0; i < n; i++) {
-        locate(ctx, x[i], y[i], &cell[i], &hx[i], &hy[i]);
-        pid[i] = (int)i;
+        float xl, yl;
+        locate(ctx, x[i], y[i], &cell[i], &xl, &yl);
+        ha[i] = make_float4(xl, yl, (float)vx[i], (float)vy[i]);
+        hb[i] = make_float4((float)m[i], (float)v[i], (float)sxx[i], (float)sxy[i]);
+        hc[i] = make_float4((float)syy[i], 0.0f, 0.0f, 0.0f);
+        hd[i] = make_float4(0.0f, 0.0f, mpmg_bits_float((int)i), 0.0f);
     }
-    auto up = [&](float *dst, const float *src) {
-        return cudaMemcpy(dst, src, n * sizeof(float), cudaMemcpyHostToDevice);
-    };
-    auto upd = [&](float *dst, const double *src) {
-        for (size_t i = 0; i < n; i++) tmp[i] = (float)src[i];
-        return cudaMemcpy(dst, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice);
-    };
     cudaError_t e = cudaSuccess;
     if (n > 0) {
-        e = up(s->x[0], hx.data());
-        if (e == cudaSuccess) e = up(s->y[0], hy.data());
-        if (e == cudaSuccess) e = upd(s->vx[0], vx);
-        if (e == cudaSuccess) e = upd(s->vy[0], vy);
-        if (e == cudaSuccess) e = upd(s->m[0], m);
-        if (e == cudaSuccess) e = upd(s->v[0], v);
-        if (e == cudaSuccess) e = upd(s->sxx[0], sxx);
-        if (e == cudaSuccess) e = upd(s->sxy[0], sxy);
-        if (e == cudaSuccess) e = upd(s->syy[0], syy);
-        if (e == cudaSuccess) e = cudaMemset(s->ux[0], 0, n * sizeof(float));
-        if (e == cudaSuccess) e = cudaMemset(s->uy[0], 0, n * sizeof(float));
-        if (e == cudaSuccess && mu2) e = cudaMemset(s->Tzz[0], 0, n * sizeof(float));
-        if (e == cudaSuccess && mu2) e = cudaMemset(s->gp[0], 0, n * sizeof(float));
-        if (e == cudaSuccess && mu2) e = cudaMemset(s->gdp[0], 0, n * sizeof(float));
-        if (e == cudaSuccess) e = cudaMemcpy(s->pid[0], pid.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(s->A[0], ha.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(s->B[0], hb.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(s->C[0], hc.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(s->D[0], hd.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
         // element index of the stored particles of buffer 0 (see cell_array)
         if (e == cudaSuccess) e = cudaMemcpy(ctx->in_element, cell.data(), n * sizeof(int), cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed state upload");
     s->cur = 0;
     // the first step's element counts; every G2P counts the next step's
-    int rcc = mpmg_bin_count(ctx, (const uint32_t *)ctx->in_element);
-    if (rcc != MPMG_OK) return rcc;
-    MPMG_CHECK(cudaGetLastError());
-    return MPMG_OK;
+    return mpmg_bin_count(ctx, (const uint32_t *)ctx->in_element);
 }
 
 void mpmg_mixed_free(mpmg_ctx *ctx)
@@ -528,10 +512,10 @@ void mpmg_mixed_free(mpmg_ctx *ctx)
     MixedState *s = ctx->mixed;
     if (s == nullptr) return;
     for (int b = 0; b < 2; b++) {
-        float *f[] = {s->x[b], s->y[b], s->vx[b], s->vy[b], s->m[b], s->v[b], s->sxx[b], s->sxy[b], s->syy[b],
-                      s->ux[b], s->uy[b], s->Tzz[b], s->gp[b], s->gdp[b]};
-        for (float *p : f) cudaFree(p);
-        cudaFree(s->pid[b]);
+        cudaFree(s->A[b]);
+        cudaFree(s->B[b]);
+        cudaFree(s->C[b]);
+        cudaFree(s->D[b]);
     }
     cudaFree(s->cell_sums);
     cudaFree(s->node4);
@@ -563,8 +547,8 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
 
     Buf S = buf(s, cur), D = buf(s, nxt);
     mpmg_phase_begin(ctx, PH_P2G);
-    mx_p2g_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(g, ctx->cell_start, ctx->bin.slots, ctx->perm, S,
-                                                            ctx->d_params, s->cell_sums);
+    mx_p2g_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(g, ctx->cell_start, ctx->bin.slots, ctx->perm,
+                                                            ctx->bin.rank, S, ctx->d_params, s->cell_sums);
     mpmg_phase_end(ctx, PH_P2G);
 
     mpmg_phase_begin(ctx, PH_GRID);
@@ -577,12 +561,12 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     const MatF mp = make_mat(ctx);
     if (c.material == MPMG_ISOLIN) {
         mx_g2p_kernel<MPMG_ISOLIN><<<blocks_for(n, 256), 256, 0, st>>>(
-            g, n, mp, ctx->cell_start, ctx->perm, ctx->sorted_keys, S, D, cell_array(ctx, cur), cell_array(ctx, nxt),
-            s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+            g, n, mp, ctx->bin.rank, S, D, cell_array(ctx, cur), cell_array(ctx, nxt), s->node4, ctx->bin.counts,
+            ctx->d_params, c.dt, c.gravity_mode, c.gravity);
     } else {
         mx_g2p_kernel<MPMG_G_LOCAL_MU2><<<blocks_for(n, 256), 256, 0, st>>>(
-            g, n, mp, ctx->cell_start, ctx->perm, ctx->sorted_keys, S, D, cell_array(ctx, cur), cell_array(ctx, nxt),
-            s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+            g, n, mp, ctx->bin.rank, S, D, cell_array(ctx, cur), cell_array(ctx, nxt), s->node4, ctx->bin.counts,
+            ctx->d_params, c.dt, c.gravity_mode, c.gravity);
     }
     mpmg_phase_end(ctx, PH_G2P);
     ctx->launches += 3;
@@ -596,11 +580,11 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
 
 namespace {
 
-int download_f(mpmg_ctx *ctx, const float *d, std::vector<float> &h)
+int download4(mpmg_ctx *ctx, const float4 *d, std::vector<float4> &h)
 {
     h.resize(ctx->np ? ctx->np : 1);
     if (ctx->np == 0) return MPMG_OK;
-    MPMG_CHECK(cudaMemcpy(h.data(), d, ctx->np * sizeof(float), cudaMemcpyDeviceToHost));
+    MPMG_CHECK(cudaMemcpy(h.data(), d, ctx->np * sizeof(float4), cudaMemcpyDeviceToHost));
     return MPMG_OK;
 }
 
@@ -612,6 +596,51 @@ int download_i(mpmg_ctx *ctx, const int *d, std::vector<int> &h)
     return MPMG_OK;
 }
 
+int pids(mpmg_ctx *ctx, std::vector<int> &pid)
+{
+    std::vector<float4> d;
+    int rc = download4(ctx, ctx->mixed->D[ctx->mixed->cur], d);
+    if (rc != MPMG_OK) return rc;
+    pid.resize(d.size());
+    for (size_t k = 0; k < ctx->np; k++) pid[k] = mpmg_float_bits(d[k].z);
+    return MPMG_OK;
+}
+
+// Record and component of each writable particle field.
+bool field_slot(const char *name, int *rec, int *comp)
+{
+    struct { const char *n; int r, c; } f[] = {
+        {"vx", 0, 2}, {"vy", 0, 3}, {"m", 1, 0}, {"v", 1, 1}, {"sxx", 1, 2}, {"sxy", 1, 3}, {"Txx", 1, 2},
+        {"Txy", 1, 3}, {"Tyx", 1, 3}, {"syy", 2, 0}, {"Tyy", 2, 0}, {"ux", 2, 1}, {"uy", 2, 2}, {"Tzz", 2, 3},
+        {"state9", 3, 0}, {"state10", 3, 1}};
+    for (auto &e : f) {
+        if (strcmp(name, e.n) == 0) {
+            *rec = e.r;
+            *comp = e.c;
+            return true;
+        }
+    }
+    return false;
+}
+
+float4 *record(MixedState *s, int b, int rec)
+{
+    return rec == 0 ? s->A[b] : rec == 1 ? s->B[b] : rec == 2 ? s->C[b] : s->D[b];
+}
+
+float get_comp(const float4 &v, int c)
+{
+    return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+}
+
+void set_comp(float4 &v, int c, float x)
+{
+    if (c == 0) v.x = x;
+    else if (c == 1) v.y = x;
+    else if (c == 2) v.z = x;
+    else v.w = x;
+}
+
 }  // namespace
 
 int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active)
@@ -621,7 +650,7 @@ int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active)
     std::vector<int> cell, pid;
     int rc;
     if ((rc = download_i(ctx, cell_array(ctx, s->cur), cell)) != MPMG_OK) return rc;
-    if ((rc = download_i(ctx, s->pid[s->cur], pid)) != MPMG_OK) return rc;
+    if ((rc = pids(ctx, pid)) != MPMG_OK) return rc;
     for (size_t k = 0; k < ctx->np; k++) {
         int e = cell[k] < (int)ctx->ne ? cell[k] : -1;
         if (in_element) in_element[pid[k]] = e;
@@ -636,8 +665,6 @@ int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out)
     const int b = s->cur;
     const size_t n = ctx->np;
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
-    std::vector<int> pid, cell;
-    std::vector<float> a, bb;
     int rc;
     if (strncmp(name, "node_", 5) == 0) {
         int comp = -1;
@@ -648,44 +675,33 @@ int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out)
         if (comp < 0) return MPMG_ERR_UNKNOWN_FIELD;   // FP64 node arrays: the common path
         std::vector<float4> h(ctx->nn);
         MPMG_CHECK(cudaMemcpy(h.data(), s->node4, ctx->nn * sizeof(float4), cudaMemcpyDeviceToHost));
-        for (size_t k = 0; k < ctx->nn; k++) {
-            const float4 v = h[k];
-            out[k] = comp == 0 ? v.x : comp == 1 ? v.y : comp == 2 ? v.z : v.w;
-        }
+        for (size_t k = 0; k < ctx->nn; k++) out[k] = get_comp(h[k], comp);
         return MPMG_OK;
     }
-    if ((rc = download_i(ctx, s->pid[b], pid)) != MPMG_OK) return rc;
+    std::vector<int> pid, cell;
+    if ((rc = pids(ctx, pid)) != MPMG_OK) return rc;
     if (strcmp(name, "x") == 0 || strcmp(name, "y") == 0) {
         const bool isx = name[0] == 'x';
+        std::vector<float4> a;
         if ((rc = download_i(ctx, cell_array(ctx, b), cell)) != MPMG_OK) return rc;
-        if ((rc = download_f(ctx, isx ? s->x[b] : s->y[b], a)) != MPMG_OK) return rc;
+        if ((rc = download4(ctx, s->A[b], a)) != MPMG_OK) return rc;
         for (size_t k = 0; k < n; k++) {
+            const double local = isx ? a[k].x : a[k].y;
             if (cell[k] < (int)ctx->ne) {
                 int c = isx ? cell[k] % ctx->Ex : cell[k] / ctx->Ex;
-                out[pid[k]] = ((double)c + (double)a[k]) * ctx->cfg.h;
+                out[pid[k]] = ((double)c + local) * ctx->cfg.h;
             } else {
-                out[pid[k]] = (double)a[k];
+                out[pid[k]] = local;
             }
         }
         return MPMG_OK;
     }
-    struct { const char *n; float *p; } f[] = {
-        {"vx", s->vx[b]}, {"vy", s->vy[b]}, {"m", s->m[b]}, {"v", s->v[b]}, {"sxx", s->sxx[b]},
-        {"sxy", s->sxy[b]}, {"syy", s->syy[b]}, {"ux", s->ux[b]}, {"uy", s->uy[b]}, {"Txx", s->sxx[b]},
-        {"Txy", s->sxy[b]}, {"Tyx", s->sxy[b]}, {"Tyy", s->syy[b]}, {"Tzz", s->Tzz[b]},
-        {"state9", s->gp[b]}, {"state10", s->gdp[b]}};
-    for (auto &fe : f) {
-        if (strcmp(name, fe.n) == 0) {
-            if (fe.p == nullptr) {
-                for (size_t k = 0; k < n; k++) out[k] = 0.0;
-                return MPMG_OK;
-            }
-            if ((rc = download_f(ctx, fe.p, a)) != MPMG_OK) return rc;
-            for (size_t k = 0; k < n; k++) out[pid[k]] = (double)a[k];
-            return MPMG_OK;
-        }
-    }
-    return MPMG_ERR_UNKNOWN_FIELD;
+    int rec, comp;
+    if (!field_slot(name, &rec, &comp)) return MPMG_ERR_UNKNOWN_FIELD;
+    std::vector<float4> a;
+    if ((rc = download4(ctx, record(s, b, rec), a)) != MPMG_OK) return rc;
+    for (size_t k = 0; k < n; k++) out[pid[k]] = (double)get_comp(a[k], comp);
+    return MPMG_OK;
 }
 
 int mpmg_mixed_set(mpmg_ctx *ctx, const char *name, const double *in)
@@ -694,21 +710,17 @@ int mpmg_mixed_set(mpmg_ctx *ctx, const char *name, const double *in)
     const int b = s->cur;
     const size_t n = ctx->np;
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
-    struct { const char *n; float *p; } f[] = {
-        {"vx", s->vx[b]}, {"vy", s->vy[b]}, {"m", s->m[b]}, {"v", s->v[b]}, {"sxx", s->sxx[b]},
-        {"sxy", s->sxy[b]}, {"syy", s->syy[b]}, {"ux", s->ux[b]}, {"uy", s->uy[b]}, {"Tzz", s->Tzz[b]},
-        {"state9", s->gp[b]}, {"state10", s->gdp[b]}};
-    for (auto &fe : f) {
-        if (strcmp(name, fe.n) == 0 && fe.p != nullptr) {
-            std::vector<int> pid;
-            int rc;
-            if ((rc = download_i(ctx, s->pid[b], pid)) != MPMG_OK) return rc;
-            std::vector<float> h(n ? n : 1);
-            for (size_t k = 0; k < n; k++) h[k] = (float)in[pid[k]];
-            if (n) MPMG_CHECK(cudaMemcpy(fe.p, h.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-            return MPMG_OK;
-        }
+    int rec, comp;
+    if (!field_slot(name, &rec, &comp)) {
+        mpmg_set_error("field '%s' cannot be written in the mixed-precision form", name);
+        return MPMG_ERR_UNKNOWN_FIELD;
     }
-    mpmg_set_error("field '%s' cannot be written in the mixed-precision form", name);
-    return MPMG_ERR_UNKNOWN_FIELD;
+    std::vector<int> pid;
+    std::vector<float4> a;
+    int rc;
+    if ((rc = pids(ctx, pid)) != MPMG_OK) return rc;
+    if ((rc = download4(ctx, record(s, b, rec), a)) != MPMG_OK) return rc;
+    for (size_t k = 0; k < n; k++) set_comp(a[k], comp, (float)in[pid[k]]);
+    if (n) MPMG_CHECK(cudaMemcpy(record(s, b, rec), a.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    return MPMG_OK;
 }

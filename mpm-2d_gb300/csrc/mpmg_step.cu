@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(256) keys_kernel(GridGeom g, int n, const doub
         }
         keys[i] = key;
     }
-    mpmg_bin_count_block(key, i < n, sentinel, bins);
+    mpmg_bin_count(key, i < n, sentinel, (uint32_t)i >> 5, bins);
 }
 
 // ---------------------------------------------------------------------------
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(128) p2g_cells_kernel(
     if (e >= ne) return;
     const int k0 = cell_start[e], k1 = cell_start[e + 1];
     if (k0 == k1) return;
-    mpmg_order_segment(slots, perm, k0, k1);     // ascending particle index, as the reference's lists
+    mpmg_order_segment(slots, perm, nullptr, k0, k1);   // ascending particle index, as the reference's lists
     const int ci = e % g.Ex, cj = e / g.Ex;
     const double xn = ci * g.h, yn = cj * g.h;   // node_number_to_coords (element.c:10-19)
     const double grav = sp->gravity;
