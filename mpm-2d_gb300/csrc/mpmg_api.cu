@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <new>
+#include <vector>
 
 #include "mpmg_internal.cuh"
 
@@ -67,7 +68,8 @@ int sync_status(mpmg_ctx *ctx)
         MPMG_CHECK(cudaMemset(ctx->d_status, 0, sizeof(int)));
     }
     if (st & MPMG_DEV_ERR_SPIN) {
-        mpmg_set_error("a grid-wide wait in the fluidity solver timed out");
+        mpmg_bin_reset(ctx);
+        mpmg_set_error("a grid-wide wait (binning scan or fluidity solver) timed out");
         return MPMG_ERR_DEVICE;
     }
     if (st & MPMG_DEV_ERR_BOUNDS) {
@@ -723,8 +725,20 @@ int mpmg_get_sort(mpmg_ctx *ctx, int *sorted_keys, int *perm, int *cell_start)
     if (ctx == nullptr) return MPMG_ERR_INVALID;
     MPMG_CHECK(cudaSetDevice(ctx->dev));
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
-    if (sorted_keys && ctx->np)
-        MPMG_CHECK(cudaMemcpy(sorted_keys, ctx->sorted_keys, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+    if (sorted_keys && ctx->np) {
+        if (ctx->mixed) {
+            // The mixed step does not store the sorted keys: they are the keys
+            // it sorted (the element array of the buffer before the last
+            // step's swap), taken in permutation order.
+            std::vector<int> p(ctx->np), k(ctx->np);
+            const int *keys = ctx->mixed->cur ? ctx->in_element : ctx->active;
+            MPMG_CHECK(cudaMemcpy(p.data(), ctx->perm, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+            MPMG_CHECK(cudaMemcpy(k.data(), keys, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+            for (size_t j = 0; j < ctx->np; j++) sorted_keys[j] = k[p[j]];
+        } else {
+            MPMG_CHECK(cudaMemcpy(sorted_keys, ctx->sorted_keys, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
+        }
+    }
     if (perm && ctx->np) {
         MPMG_CHECK(cudaMemcpy(perm, ctx->perm, ctx->np * sizeof(int), cudaMemcpyDeviceToHost));
         if (ctx->mixed) {

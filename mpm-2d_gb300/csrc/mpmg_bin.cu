@@ -8,7 +8,8 @@
 //            (mpmg_bin_count); the count kernel here runs it stand-alone.
 //   scan     exclusive prefix of all bins in one pass (decoupled
 //            look-back): element starts (cell_start) and scatter cursors; the
-//            bins go back to zero for the next step.
+//            bins go back to zero for the next step, and nothing else needs
+//            clearing between steps.
 //   scatter  every key takes a slot of its element (warp-aggregated
 //            atomics); keys outside the grid go straight to their final
 //            place in storage order (group start + rank in the group).
@@ -21,8 +22,8 @@
 
 namespace {
 
-constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__ keys, int n, uint32_t sentinel,
@@ -32,44 +33,72 @@ __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__
     mpmg_bin_count(k < n ? keys[k] : 0u, k < n, sentinel, (uint32_t)k >> 5, bins);
 }
 
-// Single-pass exclusive scan of the bins (decoupled look-back): each block
-// takes the next tile by ticket, publishes its tile total, then walks back
-// over earlier tiles' published totals (or inclusive prefixes) to find its
-// offset, publishes its inclusive prefix, and writes cursors, cell_start and
-// zeroed bins.  Tiles are taken in ticket order, so every tile a block waits
-// for belongs to a block that started earlier; each wait is still bounded,
-// and on a timeout the kernel sets MPMG_DEV_ERR_SPIN and stops.
+// Single-pass exclusive scan of the bins (decoupled look-back).  Each block
+// takes the next tile by ticket (atomicInc wraps the ticket back to 0 after
+// the last tile, so it never needs resetting), publishes its tile total, and
+// warp 0 looks back over the previous 32 tiles at a time: it folds in
+// published totals until it reaches an inclusive prefix.  Tiles are taken in
+// ticket order, so every tile a block waits for belongs to a block that
+// started earlier; each wait is still bounded, and on a timeout the kernel
+// sets MPMG_DEV_ERR_SPIN and stops.
+//
+// A tile state word is  flag (2 bits) | epoch (30 bits) | value (32 bits).
+// The epoch is a launch counter kept after the ticket: states written by an
+// earlier launch carry an older epoch and read as "not yet published", so
+// the states need no clearing between launches.  The block that takes the
+// last tile advances the epoch once its own look-back is complete, which
+// happens only after every tile of the launch has published (and so has
+// read the epoch).
 constexpr uint64_t kFlagAggregate = 1ull << 62;
 constexpr uint64_t kFlagInclusive = 2ull << 62;
-constexpr uint64_t kValueMask = (1ull << 62) - 1;
-constexpr long long kLookbackSpinLimit = 1 << 24;
+constexpr uint64_t kFlagMask = 3ull << 62;
+constexpr uint32_t kEpochMask = (1u << 30) - 1u;
+constexpr long long kLookbackSpinLimit = 1 << 22;
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
 
 __global__ void __launch_bounds__(kScanThreads) scan_kernel(uint32_t *__restrict__ bins, int m, int ne,
                                                             unsigned long long *__restrict__ tile_state,
-                                                            unsigned int *__restrict__ ticket,
+                                                            unsigned int *__restrict__ ticket_epoch,
                                                             int *__restrict__ cell_start,
                                                             uint32_t *__restrict__ cursor, int *status)
 {
     __shared__ uint32_t warp_tot[kScanThreads / 32];
     __shared__ int tile_s;
+    __shared__ uint32_t epoch_s;
     __shared__ uint32_t prefix_s;
     __shared__ int abort_s;
     if (threadIdx.x == 0) {
-        tile_s = (int)atomicAdd(ticket, 1u);
+        tile_s = (int)atomicInc(&ticket_epoch[0], gridDim.x - 1u);
+        epoch_s = *(volatile unsigned int *)&ticket_epoch[1] & kEpochMask;
         abort_s = 0;
     }
     __syncthreads();
     const int tile = tile_s;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int base = tile * kScanTile + threadIdx.x * kScanItems;   // 8 consecutive bins per thread
+    const int base = tile * kScanTile + threadIdx.x * kScanItems;   // 16 consecutive bins per thread
     uint32_t v[kScanItems];
     uint32_t sum = 0;
+    if (base + kScanItems <= m) {
 #pragma unroll
-    for (int j = 0; j < kScanItems; j++) {
-        const int idx = base + j;
-        v[j] = idx < m ? bins[idx] : 0u;
-        sum += v[j];
+        for (int j = 0; j < kScanItems; j += 4) {
+            const uint4 q = *reinterpret_cast<const uint4 *>(bins + base + j);
+            v[j] = q.x;
+            v[j + 1] = q.y;
+            v[j + 2] = q.z;
+            v[j + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kScanItems; j++) v[j] = base + j < m ? bins[base + j] : 0u;
     }
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) sum += v[j];
     uint32_t incl = sum;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
@@ -78,56 +107,93 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(uint32_t *__restrict
     }
     if (lane == 31) warp_tot[w] = incl;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t total = 0;
-        for (int j = 0; j < kScanThreads / 32; j++) total += warp_tot[j];
+    if (w == 0) {
+        const uint32_t epoch = epoch_s;
+        const uint64_t tag = (uint64_t)epoch << 32;
+        const uint32_t total = warp_sum(lane < kScanThreads / 32 ? warp_tot[lane] : 0u);
         volatile unsigned long long *st = tile_state;
+        uint32_t prefix = 0;
+        bool ok = true;
         if (tile == 0) {
-            st[0] = kFlagInclusive | total;
-            prefix_s = 0;
+            if (lane == 0) st[0] = kFlagInclusive | tag | total;
         } else {
-            st[tile] = kFlagAggregate | total;
-            __threadfence();
-            uint32_t prefix = 0;
-            int p = tile - 1;
-            long long spins = 0;
-            while (p >= 0) {
-                const unsigned long long word = st[p];
-                if ((word & ~kValueMask) == 0) {
-                    if (++spins > kLookbackSpinLimit) {
-                        atomicOr(status, MPMG_DEV_ERR_SPIN);
-                        abort_s = 1;
+            if (lane == 0) st[tile] = kFlagAggregate | tag | total;
+            int p = tile - 1;      // newest tile not yet folded in
+            long long polls = 0;
+            while (true) {
+                const int q = p - lane;
+                const uint64_t word = q >= 0 ? st[q] : (kFlagInclusive | tag);   // before tile 0: zero
+                const bool ready = (word & kFlagMask) != 0 && (uint32_t)((word >> 32) & kEpochMask) == epoch;
+                const uint32_t incl_mask = __ballot_sync(0xffffffffu, ready && (word & kFlagInclusive) != 0);
+                const int last = incl_mask ? __ffs(incl_mask) - 1 : 31;   // lanes 0..last are needed
+                const uint32_t need = (2u << last) - 1u;
+                const uint32_t ready_mask = __ballot_sync(0xffffffffu, ready);
+                if ((ready_mask & need) != need) {
+                    if (++polls > kLookbackSpinLimit) {
+                        ok = false;
                         break;
                     }
                     continue;
                 }
-                prefix += (uint32_t)(word & kValueMask);
-                if (word & kFlagInclusive) break;
-                p--;
+                prefix += warp_sum(lane <= last ? (uint32_t)word : 0u);
+                if (incl_mask) break;
+                p -= 32;
             }
-            __threadfence();
-            st[tile] = kFlagInclusive | (unsigned long long)(prefix + total);
+            // flag and value travel in one word, and the value depends on
+            // every state folded in, so no fence is needed before it
+            if (ok && lane == 0) st[tile] = kFlagInclusive | tag | (uint64_t)(uint32_t)(prefix + total);
+        }
+        if (lane == 0) {
             prefix_s = prefix;
+            if (!ok) {
+                atomicOr(status, MPMG_DEV_ERR_SPIN);
+                abort_s = 1;
+            } else if (tile == (int)gridDim.x - 1) {
+                // every tile has published: the next launch may start a new epoch
+                __threadfence();
+                *(volatile unsigned int *)&ticket_epoch[1] = (epoch + 1u) & kEpochMask;
+            }
         }
     }
     __syncthreads();
     if (abort_s) return;
     uint32_t run = prefix_s + incl - sum;
     for (int j = 0; j < w; j++) run += warp_tot[j];
+    uint32_t ex[kScanItems];
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
-        const int idx = base + j;
-        if (idx < m) {
-            if (idx <= ne) cell_start[idx] = (int)run;
-            cursor[idx] = run;
-            bins[idx] = 0;
-        }
+        ex[j] = run;
         run += v[j];
+    }
+    if (base + kScanItems <= m) {
+#pragma unroll
+        for (int j = 0; j < kScanItems; j += 4) {
+            *reinterpret_cast<uint4 *>(cursor + base + j) = make_uint4(ex[j], ex[j + 1], ex[j + 2], ex[j + 3]);
+            *reinterpret_cast<uint4 *>(bins + base + j) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kScanItems; j++)
+            if (base + j < m) {
+                cursor[base + j] = ex[j];
+                bins[base + j] = 0u;
+            }
+    }
+    if (base + kScanItems <= ne + 1) {
+#pragma unroll
+        for (int j = 0; j < kScanItems; j += 4)
+            *reinterpret_cast<int4 *>(cell_start + base + j) =
+                make_int4((int)ex[j], (int)ex[j + 1], (int)ex[j + 2], (int)ex[j + 3]);
+    } else if (base <= ne) {
+#pragma unroll
+        for (int j = 0; j < kScanItems; j++)
+            if (base + j <= ne) cell_start[base + j] = (int)ex[j];
     }
 }
 
-// Each warp scatters 4 consecutive groups of 32 keys (independent
-// iterations: several atomics and stores in flight per lane).
+// Each warp scatters 4 consecutive groups of 32 keys.  The groups' keys,
+// peer sets and cursor atomics are all issued before any result is used, so
+// a lane has its four atomics in flight at once.
 constexpr int kScatterGroups = 4;
 
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict__ keys, int n, uint32_t sentinel,
@@ -138,31 +204,39 @@ __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict
     const int lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t key[kScatterGroups], peers[kScatterGroups], base[kScatterGroups], outside[kScatterGroups];
+#pragma unroll
+    for (int j = 0; j < kScatterGroups; j++) {
+        const int k = (warp_global * kScatterGroups + j) * 32 + lane;
+        key[j] = k < n ? keys[k] : sentinel + 1u;     // sentinel + 1: no key
+    }
+#pragma unroll
+    for (int j = 0; j < kScatterGroups; j++) {
+        const bool in = key[j] < sentinel;
+        outside[j] = __ballot_sync(0xffffffffu, key[j] == sentinel);
+        const uint32_t inmask = __ballot_sync(0xffffffffu, in);
+        peers[j] = in ? __match_any_sync(inmask, key[j]) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kScatterGroups; j++) {
+        base[j] = 0;
+        if (peers[j] != 0u && lane == __ffs(peers[j]) - 1)
+            base[j] = atomicAdd(&cursor[key[j]], (uint32_t)__popc(peers[j]));
+    }
 #pragma unroll
     for (int j = 0; j < kScatterGroups; j++) {
         const int group = warp_global * kScatterGroups + j;
         const int k = group * 32 + lane;
-        const bool valid = k < n;
-        const uint32_t key = valid ? keys[k] : 0u;
-        const bool out = valid && key == sentinel;
-        const bool in = valid && key != sentinel;
-        const uint32_t outside = __ballot_sync(0xffffffffu, out);
-        const uint32_t inmask = __ballot_sync(0xffffffffu, in);
-        if (out) {
-            const uint32_t pos = cursor[sentinel + group] + __popc(outside & lt);
+        if (key[j] == sentinel) {
+            const uint32_t pos = cursor[sentinel + group] + __popc(outside[j] & lt);
             perm[pos] = (uint32_t)k;      // final: storage order within the group's run
             rank[k] = pos;
-            sorted_keys[pos] = key;
-        }
-        if (in) {
-            const uint32_t peers = __match_any_sync(inmask, key);
-            const int leader = __ffs(peers) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(&cursor[key], (uint32_t)__popc(peers));
-            base = __shfl_sync(peers, base, leader);
-            const uint32_t pos = base + __popc(peers & lt);
+            if (sorted_keys != nullptr) sorted_keys[pos] = key[j];
+        } else if (peers[j] != 0u) {
+            const uint32_t b = __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1);
+            const uint32_t pos = b + __popc(peers[j] & lt);
             slots[pos] = (uint32_t)k;
-            sorted_keys[pos] = key;
+            if (sorted_keys != nullptr) sorted_keys[pos] = key[j];
         }
     }
 }
@@ -180,6 +254,9 @@ int mpmg_bin_init(mpmg_ctx *ctx)
     MPMG_CHECK(cudaMalloc(&ctx->bin.slots, (ctx->np ? ctx->np : 1) * sizeof(uint32_t)));
     MPMG_CHECK(cudaMalloc(&ctx->bin.rank, (ctx->np ? ctx->np : 1) * sizeof(uint32_t)));
     MPMG_CHECK(cudaMemsetAsync(ctx->bin.counts, 0, m * sizeof(uint32_t), ctx->stream));
+    // tile states, ticket and epoch start at zero (no tile published)
+    MPMG_CHECK(cudaMemsetAsync(ctx->bin.tile_state, 0, (tiles ? tiles : 1) * sizeof(unsigned long long) + 16,
+                               ctx->stream));
     ctx->bin.bins = (int)m;
     ctx->bin.tiles = (int)tiles;
     return MPMG_OK;
@@ -206,25 +283,34 @@ int mpmg_bin_count(mpmg_ctx *ctx, const uint32_t *keys)
     return MPMG_OK;
 }
 
+// Back to the initial look-back state, after a launch that stopped on a
+// timed-out wait left some tiles of its epoch unpublished.
+int mpmg_bin_reset(mpmg_ctx *ctx)
+{
+    if (ctx->bin.tile_state == nullptr) return MPMG_OK;
+    MPMG_CHECK(cudaMemset(ctx->bin.tile_state, 0,
+                          (size_t)(ctx->bin.tiles ? ctx->bin.tiles : 1) * sizeof(unsigned long long) + 16));
+    MPMG_CHECK(cudaMemset(ctx->bin.counts, 0, (size_t)ctx->bin.bins * sizeof(uint32_t)));
+    return MPMG_OK;
+}
+
 // Scan of the counted bins and scatter of keys[n]: cell_start[ne + 1],
-// sorted_keys[n], perm and rank for keys outside the grid, and bin.slots
-// (unordered within each element) for the rest.
-int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys)
+// perm and rank for keys outside the grid, bin.slots (unordered within each
+// element) for the rest, and sorted_keys[n] unless it is null.
+int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys, uint32_t *sorted_keys)
 {
     cudaStream_t s = ctx->stream;
     const int n = (int)ctx->np;
     const int m = ctx->bin.bins;
     const int tiles = ctx->bin.tiles;
-    // tile states and the ticket counter (right after them) start at zero
-    MPMG_CHECK(cudaMemsetAsync(ctx->bin.tile_state, 0, (size_t)tiles * sizeof(unsigned long long) + 16, s));
-    unsigned int *ticket = (unsigned int *)(ctx->bin.tile_state + tiles);
-    scan_kernel<<<tiles, kScanThreads, 0, s>>>(ctx->bin.counts, m, (int)ctx->ne, ctx->bin.tile_state, ticket,
+    unsigned int *ticket_epoch = (unsigned int *)(ctx->bin.tile_state + tiles);
+    scan_kernel<<<tiles, kScanThreads, 0, s>>>(ctx->bin.counts, m, (int)ctx->ne, ctx->bin.tile_state, ticket_epoch,
                                                ctx->cell_start, ctx->bin.cursor, ctx->d_status);
     ctx->launches += 1;
     if (n > 0) {
         const int keys_per_block = 256 * kScatterGroups;
         scatter_kernel<<<(n + keys_per_block - 1) / keys_per_block, 256, 0, s>>>(
-            keys, n, (uint32_t)ctx->ne, ctx->bin.cursor, ctx->bin.slots, ctx->perm, ctx->bin.rank, ctx->sorted_keys);
+            keys, n, (uint32_t)ctx->ne, ctx->bin.cursor, ctx->bin.slots, ctx->perm, ctx->bin.rank, sorted_keys);
         ctx->launches += 1;
     }
     MPMG_CHECK(cudaGetLastError());

@@ -63,6 +63,7 @@ struct MixedState {
     int cur;
     float *cell_sums;      // 20 FP32 corner sums per element, value-major
     float4 *node4;         // per node: ax, ay, vx, vy (FP32) for the gathers
+    float2 *node_mass;     // per node: mass as float-float (hi, lo)
 };
 
 // Counting-sort binning scratch (mpmg_bin.cu).  Bins 0..ne-1 count the keys
@@ -71,7 +72,7 @@ struct MixedState {
 struct BinScratch {
     uint32_t *counts;      // bins (zero between steps)
     uint32_t *cursor;      // scatter cursors (exclusive prefix of the bins)
-    unsigned long long *tile_state;   // per 2048-bin tile: look-back flag + value, then a ticket
+    unsigned long long *tile_state;   // per 2048-bin tile: look-back word; then ticket and epoch
     uint32_t *slots;       // n scattered storage positions, unordered within elements
     uint32_t *rank;        // n: sorted position of each storage position
     int bins;
@@ -181,10 +182,12 @@ int mpmg_bin_init(mpmg_ctx *ctx);
 void mpmg_bin_free(mpmg_ctx *ctx);
 // Stand-alone count of keys[n] (<= ne) into the bins.
 int mpmg_bin_count(mpmg_ctx *ctx, const uint32_t *keys);
-// Scan of the counted bins and scatter: cell_start, sorted_keys, and perm
-// for keys outside the grid; element slots stay unordered in bin.slots until
-// a P2G kernel orders them into perm (mpmg_order_segment).
-int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys);
+// Scan of the counted bins and scatter: cell_start, sorted_keys (unless
+// null), and perm for keys outside the grid; element slots stay unordered in
+// bin.slots until a P2G kernel orders them into perm (mpmg_order_segment).
+// mpmg_bin_reset restores the look-back state after a timed-out wait.
+int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys, uint32_t *sorted_keys);
+int mpmg_bin_reset(mpmg_ctx *ctx);
 int mpmg_nonlocal_init(mpmg_ctx *ctx);
 void mpmg_nonlocal_free(mpmg_ctx *ctx);
 int mpmg_launch_fluidity(mpmg_ctx *ctx);         // nonlocal: assembly, solve, stress

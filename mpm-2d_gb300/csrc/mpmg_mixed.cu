@@ -15,10 +15,11 @@
 //     from step to step at no extra traffic and the next step's gathers are
 //     nearly sequential.
 //   * P2G corner sums of an element's particle segment are FP32 (a few
-//     particles each); the four elements around a node are summed in FP64 for
-//     mass and momentum, the momentum update and the division by nodal mass
-//     are FP64, and the node's acceleration and velocity are stored in FP32
-//     for the gathers.
+//     particles each); the four elements around a node are summed in
+//     float-float (an unevaluated sum of two FP32 values, ~48 bits) for mass
+//     and momentum, the momentum update and the division by nodal mass are
+//     float-float as well, all on the FP32 pipe, and the node's acceleration
+//     and velocity are stored in FP32 for the gathers.
 // Time and gravity advance on the device: the G2P's first thread moves t and
 // the next step's gravity (loading.c:34-54) once all reads of them are done.
 #include <math.h>
@@ -40,7 +41,8 @@ struct GeomM {
 struct BcM {
     int kind;
     int left_col, right_col, bottom_row, top_row, lf, bf, rf, tf;
-    double hole_radius, open_time;
+    double open_time;
+    int hole_last_col;     // last column i with i h <= hole radius (square_silo.c)
     int wall_col;
 };
 
@@ -124,25 +126,7 @@ __device__ __forceinline__ void g_local_mu2_f(const MatF &p, float m, float v, f
     gdp = nup;
 }
 
-// Exact FP32 -> FP64 widening on the integer pipe (IEEE 754 field
-// re-encoding: the exponent bias moves from 127 to 1023, the 23-bit fraction
-// moves to the top of the 52-bit one).  FP32 subnormals (below 1.2e-38, far
-// under any nodal mass or momentum here) become zero; infinities and NaNs
-// take the hardware conversion.  GB300's FP64 pipe is the grid kernel's
-// bottleneck, and twelve widenings per node would otherwise run on it.
-__device__ __forceinline__ double widen(float f)
-{
-    const uint32_t b = __float_as_uint(f);
-    const uint32_t e = (b >> 23) & 0xffu;
-    if (e == 0xffu) return (double)f;
-    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
-    if (e == 0u) return __longlong_as_double((long long)sign);
-    const uint64_t bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
-}
-
-__device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double h, double t_now, bool &mx,
-                                          bool &my)
+__device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double t_now, bool &mx, bool &my)
 {
     mx = false;
     my = false;
@@ -154,7 +138,7 @@ __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double h,
         if (on_col && i == bc.left_col) { mx |= (bc.lf & 1) != 0; my |= (bc.lf & 2) != 0; }
         if (on_col && i == bc.right_col) { mx |= (bc.rf & 1) != 0; my |= (bc.rf & 2) != 0; }
     } else {
-        if (j == 0 && !((i * h) <= bc.hole_radius && t_now > bc.open_time)) {
+        if (j == 0 && !(i <= bc.hole_last_col && t_now > bc.open_time)) {
             mx = true;
             my = true;
         }
@@ -164,54 +148,193 @@ __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double h,
 
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128, 8) mx_p2g_kernel(GeomM g, const int *__restrict__ cell_start,
-                                                     const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm,
-                                                     uint32_t *__restrict__ rank, Buf P,
-                                                     const StepParams *__restrict__ sp,
-                                                     float *__restrict__ cell_sums)
+// P2G: a block takes 256 consecutive elements, one thread each, and works
+// through them in passes of whole elements whose particles (a contiguous
+// range of the binned order) fit a 1024-particle shared-memory stage.  Each
+// pass stages slots and particle records with coalesced, batched loads (the
+// slots are close to the identity because the storage is kept in element
+// order); then every thread orders its element's stage indices by storage
+// position (insertion sort in shared memory: the deterministic,
+// launch-order-independent order), writes perm and rank, and sums its
+// particles in that order: 4 corners x (m, mvx, mvy, fx, fy) in FP32
+// (process_usl.c:491-522 per particle, regrouped per element).  An element
+// with more particles than the stage is summed alone from global memory.
+constexpr int kP2GThreads = 256;
+constexpr int kP2GChunk = 1024;
+constexpr int kP2GBatch = 2;        // particles per thread whose loads are in flight together
+
+__device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, float grav, float xl, float yl,
+                                               float vx, float vy, float m, float vol, float sxx, float sxy,
+                                               float syy)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= g.ne) return;
-    const int k0 = cell_start[e], k1 = cell_start[e + 1];
-    if (k0 == k1) return;
-    mpmg_order_segment(slots, perm, rank, k0, k1);
-    const float grav = (float)sp->gravity;
-    const float ih = g.inv_hf;
-    float acc[4][5];
+    const float ox = 1.0f - xl, oy = 1.0f - yl;
+    const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
+    const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
+    const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
+    const float pmx = vx * m, pmy = vy * m, pby = grav * m;
+    const float s0 = -sxx * vol, s1 = -sxy * vol, s2 = -syy * vol;
 #pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
-    for (int k = k0; k < k1; k++) {
-        const int i = (int)perm[k];
-        const float4 a4 = P.A[i], b4 = P.B[i];
-        const float syy = P.C[i].x;
-        const float xl = a4.x, yl = a4.y, m = b4.x, vol = b4.y;
-        const float ox = 1.0f - xl, oy = 1.0f - yl;
-        const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
-        const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
-        const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
-        const float pmx = a4.z * m, pmy = a4.w * m, pby = grav * m;
-        const float s0 = -b4.z * vol, s1 = -b4.w * vol, s2 = -syy * vol;
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-            acc[a][0] += s[a] * m;
-            acc[a][1] += s[a] * pmx;
-            acc[a][2] += s[a] * pmy;
-            acc[a][3] += gx[a] * s0 + gy[a] * s1;
-            acc[a][4] += s[a] * pby + gx[a] * s1 + gy[a] * s2;
-        }
+    for (int a = 0; a < 4; a++) {
+        acc[a][0] += s[a] * m;
+        acc[a][1] += s[a] * pmx;
+        acc[a][2] += s[a] * pmy;
+        acc[a][3] += gx[a] * s0 + gy[a] * s1;
+        acc[a][4] += s[a] * pby + gx[a] * s1 + gy[a] * s2;
     }
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int f = 0; f < 5; f++) cell_sums[(size_t)(a * 5 + f) * g.ne + e] = acc[a][f];
 }
 
+__global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const int *__restrict__ cell_start,
+                                                                const uint32_t *__restrict__ slots,
+                                                                uint32_t *__restrict__ perm,
+                                                                uint32_t *__restrict__ rank, Buf P,
+                                                                const StepParams *__restrict__ sp,
+                                                                float *__restrict__ cell_sums)
+{
+    __shared__ float sh[9][kP2GChunk];
+    __shared__ uint32_t sh_slot[kP2GChunk];
+    __shared__ uint16_t sh_ord[kP2GChunk];
+    __shared__ int sh_cs[kP2GThreads + 1];
+    const int e0 = blockIdx.x * kP2GThreads;
+    const int ne_blk = min(kP2GThreads, g.ne - e0);
+    for (int t = threadIdx.x; t <= ne_blk; t += kP2GThreads) sh_cs[t] = cell_start[e0 + t];
+    __syncthreads();
+    const int me = threadIdx.x;
+    const int k0 = me < ne_blk ? sh_cs[me] : 0, k1 = me < ne_blk ? sh_cs[me + 1] : 0;
+    const float grav = (float)sp->gravity;
+    const float ih = g.inv_hf;
+    int ea = 0;
+    while (ea < ne_blk) {
+        // elements [ea, eb) of this pass: the most whose particles fit the stage
+        const int limit = sh_cs[ea] + kP2GChunk;
+        int lo = ea + 1, hi = ne_blk;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sh_cs[mid] <= limit) lo = mid;
+            else hi = mid - 1;
+        }
+        const int eb = lo;
+        const int base = sh_cs[ea], end = sh_cs[eb];
+        const bool mine = me >= ea && me < eb && k1 > k0;
+        float acc[4][5];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
+        if (end - base <= kP2GChunk) {
+            for (int k = base + (int)threadIdx.x; k < end; k += kP2GBatch * kP2GThreads) {
+                uint32_t sl[kP2GBatch];
+                float4 a4[kP2GBatch], b4[kP2GBatch];
+                float c[kP2GBatch];
+#pragma unroll
+                for (int u = 0; u < kP2GBatch; u++) {
+                    const int kk = k + u * kP2GThreads;
+                    sl[u] = kk < end ? slots[kk] : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < kP2GBatch; u++) {
+                    if (k + u * kP2GThreads < end) {
+                        a4[u] = P.A[sl[u]];
+                        b4[u] = P.B[sl[u]];
+                        c[u] = P.C[sl[u]].x;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kP2GBatch; u++) {
+                    const int j = k + u * kP2GThreads - base;
+                    if (j < end - base) {
+                        sh_slot[j] = sl[u];
+                        sh[0][j] = a4[u].x;
+                        sh[1][j] = a4[u].y;
+                        sh[2][j] = a4[u].z;
+                        sh[3][j] = a4[u].w;
+                        sh[4][j] = b4[u].x;
+                        sh[5][j] = b4[u].y;
+                        sh[6][j] = b4[u].z;
+                        sh[7][j] = b4[u].w;
+                        sh[8][j] = c[u];
+                    }
+                }
+            }
+            __syncthreads();
+            if (mine) {
+                const int j0 = k0 - base, j1 = k1 - base;
+                for (int j = j0; j < j1; j++) {
+                    const uint32_t x = sh_slot[j];
+                    int t = j - 1;
+                    while (t >= j0 && sh_slot[sh_ord[t]] > x) {
+                        sh_ord[t + 1] = sh_ord[t];
+                        t--;
+                    }
+                    sh_ord[t + 1] = (uint16_t)j;
+                }
+                for (int j = j0; j < j1; j++) {
+                    const int q = sh_ord[j];
+                    const uint32_t i = sh_slot[q];
+                    perm[base + j] = i;
+                    rank[i] = (uint32_t)(base + j);
+                    p2g_accumulate(acc, ih, grav, sh[0][q], sh[1][q], sh[2][q], sh[3][q], sh[4][q], sh[5][q],
+                                   sh[6][q], sh[7][q], sh[8][q]);
+                }
+            }
+            __syncthreads();
+        } else if (mine) {
+            // a single element larger than the stage
+            mpmg_order_segment(slots, perm, rank, k0, k1);
+            for (int k = k0; k < k1; k++) {
+                const uint32_t i = perm[k];
+                const float4 a4 = P.A[i], b4 = P.B[i];
+                p2g_accumulate(acc, ih, grav, a4.x, a4.y, a4.z, a4.w, b4.x, b4.y, b4.z, b4.w, P.C[i].x);
+            }
+        }
+        if (mine) {
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int f = 0; f < 5; f++) cell_sums[(size_t)(a * 5 + f) * g.ne + e0 + me] = acc[a][f];
+        }
+        ea = eb;
+    }
+}
+
+// Double-FP32 ("float-float") helpers: a value is hi + lo with |lo| <= ulp(hi)/2,
+// about 48 significant bits, on the FP32 pipe (GB300's FP64 rate is 1/64 of
+// its FP32 rate).  TwoSum is Knuth's error-free addition.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float v)
+{
+    const float s = __fadd_rn(hi, v);
+    const float bv = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(v, bv));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
+__device__ __forceinline__ void ff_norm(float &hi, float &lo)
+{
+    const float s = __fadd_rn(hi, lo);
+    lo = __fsub_rn(lo, __fsub_rn(s, hi));
+    hi = s;
+}
+
+// (nh + nl) / (dh + dl) rounded to FP32: one Newton correction of the FP32
+// quotient with the exact residual nh - q dh (FMA).
+__device__ __forceinline__ float ff_div(float nh, float nl, float dh, float dl, float r)
+{
+    const float q = __fmul_rn(nh, r);
+    float res = __fmaf_rn(-q, dh, nh);
+    res = __fadd_rn(res, nl);
+    res = __fmaf_rn(-q, dl, res);
+    return __fmaf_rn(res, r, q);
+}
+
+// Grid update, one thread per node: the four elements' corner sums in
+// colour order (process_usl.c:524-540), float-float for mass and momentum;
+// boundary masks; momentum update and nodal velocity / acceleration
+// (process_usl.c:542-566).
 __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int *__restrict__ cell_start,
                                                       const float *__restrict__ cell_sums,
                                                       const StepParams *__restrict__ sp, double dt,
-                                                      double *__restrict__ node_m, float4 *__restrict__ node4,
+                                                      float dt_hi, float dt_lo, float tol,
+                                                      float2 *__restrict__ node_mass, float4 *__restrict__ node4,
                                                       double *__restrict__ node_mx,
                                                       double *__restrict__ node_my, double *__restrict__ node_fx,
                                                       double *__restrict__ node_fy)
@@ -220,7 +343,7 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nn) return;
     const int i = n % g.Nx, j = n / g.Nx;
-    double m = 0, mx = 0, my = 0;
+    float mh = 0, ml = 0, xh = 0, xl = 0, yh = 0, yl = 0;
     float fx = 0, fy = 0;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
@@ -231,36 +354,42 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
         if (cell_start[e] == cell_start[e + 1]) continue;
         int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
         const float *cs = cell_sums + (size_t)(a * 5) * g.ne + e;
-        m += widen(cs[0]);
-        mx += widen(cs[(size_t)g.ne]);
-        my += widen(cs[(size_t)2 * g.ne]);
+        ff_add(mh, ml, cs[0]);
+        ff_add(xh, xl, cs[(size_t)g.ne]);
+        ff_add(yh, yl, cs[(size_t)2 * g.ne]);
         fx += cs[(size_t)3 * g.ne];
         fy += cs[(size_t)4 * g.ne];
     }
+    ff_norm(mh, ml);
     bool bx, by;
-    bc_mask_m(bc, i, j, g.h, sp->t + dt, bx, by);
-    if (bx) { mx = 0; fx = 0; }
-    if (by) { my = 0; fy = 0; }
+    bc_mask_m(bc, i, j, sp->t + dt, bx, by);
+    if (bx) { xh = 0; xl = 0; fx = 0; }
+    if (by) { yh = 0; yl = 0; fy = 0; }
     float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (m > MPMG_TOL) {
-        // 1/m in FP64: FP32 reciprocal refined by one Newton-Raphson step
-        // r <- r + r (1 - m r), relative error ~(2^-23)^2, ample for the FP32
-        // results it scales.
-        double r = (double)__frcp_rn((float)m);
-        r = fma(r, fma(-m, r, 1.0), r);
-        mx += dt * (double)fx;
-        my += dt * (double)fy;
-        const float rf = (float)r;
-        nd.x = fx * rf;
-        nd.y = fy * rf;
-        nd.z = (float)(mx * r);
-        nd.w = (float)(my * r);
+    if (mh > tol) {
+        // 1/m to ~FP32 accuracy of the float-float mass, then
+        // p += dt f with dt = dt_hi + dt_lo and the exact product error.
+        float r = __frcp_rn(mh);
+        r = __fmaf_rn(r, __fmaf_rn(-ml, r, __fmaf_rn(-mh, r, 1.0f)), r);
+        const float px = __fmul_rn(dt_hi, fx), py = __fmul_rn(dt_hi, fy);
+        const float ex = __fmaf_rn(dt_lo, fx, __fmaf_rn(dt_hi, fx, -px));
+        const float ey = __fmaf_rn(dt_lo, fy, __fmaf_rn(dt_hi, fy, -py));
+        ff_add(xh, xl, px);
+        xl = __fadd_rn(xl, ex);
+        ff_add(yh, yl, py);
+        yl = __fadd_rn(yl, ey);
+        ff_norm(xh, xl);
+        ff_norm(yh, yl);
+        nd.x = fx * r;
+        nd.y = fy * r;
+        nd.z = ff_div(xh, xl, mh, ml, r);
+        nd.w = ff_div(yh, yl, mh, ml, r);
     }
-    node_m[n] = m;
+    node_mass[n] = make_float2(mh, ml);
     node4[n] = nd;
     if (node_mx != nullptr) {
-        node_mx[n] = mx;
-        node_my[n] = my;
+        node_mx[n] = (double)xh + (double)xl;
+        node_my[n] = (double)yh + (double)yl;
         node_fx[n] = fx;
         node_fy[n] = fy;
     }
@@ -401,7 +530,9 @@ BcM make_bc(const mpmg_ctx *ctx)
         b.rf = c.bci[2];
         b.tf = c.bci[3];
     } else {
-        b.hole_radius = c.bcf[0];
+        // the largest i with (i h <= radius), the reference's test, in FP64
+        b.hole_last_col = -1;
+        for (int i = 0; i < c.Nx && ((double)i * c.h) <= c.bcf[0]; i++) b.hole_last_col = i;
         b.open_time = c.bcf[1];
         b.wall_col = (int)((double)(c.Nx - 1) * c.bcf[2]);
     }
@@ -480,6 +611,8 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     }
     if ((rc = dalloc(&s->cell_sums, 20 * ctx->ne)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->node4, ctx->nn)) != MPMG_OK) return rc;
+    if ((rc = dalloc(&s->node_mass, ctx->nn)) != MPMG_OK) return rc;
+    MPMG_CHECK(cudaMemset(s->node_mass, 0, ctx->nn * sizeof(float2)));
 
     // host staging: element, local coordinates, records
     std::vector<float4> ha(n ? n : 1), hb(n ? n : 1), hc(n ? n : 1), hd(n ? n : 1);
@@ -519,6 +652,7 @@ void mpmg_mixed_free(mpmg_ctx *ctx)
     }
     cudaFree(s->cell_sums);
     cudaFree(s->node4);
+    cudaFree(s->node_mass);
     delete s;
     ctx->mixed = nullptr;
 }
@@ -539,22 +673,23 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     const GeomM g = make_geom(ctx);
     const int n = (int)ctx->np;
     const int cur = s->cur, nxt = 1 - cur;
+    const float dt_hi = (float)c.dt, dt_lo = (float)(c.dt - (double)dt_hi);
 
     mpmg_phase_begin(ctx, PH_SORT);
-    int rc = mpmg_bin_scan_scatter(ctx, (const uint32_t *)cell_array(ctx, cur));
+    int rc = mpmg_bin_scan_scatter(ctx, (const uint32_t *)cell_array(ctx, cur), nullptr);
     if (rc != MPMG_OK) return rc;
     mpmg_phase_end(ctx, PH_SORT);
 
     Buf S = buf(s, cur), D = buf(s, nxt);
     mpmg_phase_begin(ctx, PH_P2G);
-    mx_p2g_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(g, ctx->cell_start, ctx->bin.slots, ctx->perm,
-                                                            ctx->bin.rank, S, ctx->d_params, s->cell_sums);
+    mx_p2g_kernel<<<blocks_for(ctx->ne, kP2GThreads), kP2GThreads, 0, st>>>(
+        g, ctx->cell_start, ctx->bin.slots, ctx->perm, ctx->bin.rank, S, ctx->d_params, s->cell_sums);
     mpmg_phase_end(ctx, PH_P2G);
 
     mpmg_phase_begin(ctx, PH_GRID);
     mx_grid_kernel<<<blocks_for(ctx->nn, 256), 256, 0, st>>>(
-        g, make_bc(ctx), ctx->cell_start, s->cell_sums, ctx->d_params, c.dt, ctx->node_m, s->node4,
-        ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy);
+        g, make_bc(ctx), ctx->cell_start, s->cell_sums, ctx->d_params, c.dt, dt_hi, dt_lo, (float)MPMG_TOL,
+        s->node_mass, s->node4, ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy);
     mpmg_phase_end(ctx, PH_GRID);
 
     mpmg_phase_begin(ctx, PH_G2P);
@@ -672,6 +807,12 @@ int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out)
         else if (strcmp(name, "node_ay") == 0) comp = 1;
         else if (strcmp(name, "node_vx") == 0) comp = 2;
         else if (strcmp(name, "node_vy") == 0) comp = 3;
+        if (strcmp(name, "node_m") == 0) {
+            std::vector<float2> h(ctx->nn);
+            MPMG_CHECK(cudaMemcpy(h.data(), s->node_mass, ctx->nn * sizeof(float2), cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < ctx->nn; k++) out[k] = (double)h[k].x + (double)h[k].y;
+            return MPMG_OK;
+        }
         if (comp < 0) return MPMG_ERR_UNKNOWN_FIELD;   // FP64 node arrays: the common path
         std::vector<float4> h(ctx->nn);
         MPMG_CHECK(cudaMemcpy(h.data(), s->node4, ctx->nn * sizeof(float4), cudaMemcpyDeviceToHost));

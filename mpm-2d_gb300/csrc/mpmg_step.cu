@@ -489,7 +489,7 @@ int mpmg_launch_step(mpmg_ctx *ctx)
     mpmg_phase_end(ctx, PH_KEYS);
 
     mpmg_phase_begin(ctx, PH_SORT);
-    int rc = mpmg_bin_scan_scatter(ctx, ctx->keys);
+    int rc = mpmg_bin_scan_scatter(ctx, ctx->keys, ctx->sorted_keys);
     if (rc != MPMG_OK) return rc;
     mpmg_phase_end(ctx, PH_SORT);
 
