@@ -6,16 +6,18 @@ element on a 513x513-node grid (512^2 elements), g_local_mu2 granular rheology
 inputs in the reference generator's lattice layout.  A step is one
 explicit_mpm_step_usl_threaded + time_varying_loads over all particles.  The
 headline runs the mixed-precision form (FP32 particle state and particle
-arithmetic, FP64 nodal mass/momentum sums and division); the plain FP64 form
-is measured beside it ("fp64").  Particle state and per-step scratch exceed
+arithmetic, float-float nodal mass/momentum sums and division); the plain
+FP64 form is measured beside it ("fp64"), and the mixed form with FP64 nodal
+sums ("mixed_f64node").  Particle state and per-step scratch exceed
 the 129 MB L2 (~170 MB mixed, ~300 MB FP64), so no flush is needed.
 
   value     particle-steps/s of the mixed form with the state resident in HBM
             (CUDA events on the library's stream, max over ranks)
-  e2e       the same metric through the public C ABI with host buffers: the
-            timed region includes creating the context from host arrays (H2D
-            of the particle state) and, after every step, a D2H read of the
-            frame fields into pinned host memory
+  e2e       the same metric through the public C ABI with host buffers over
+            a 500-step run: the timed region includes creating the context
+            from host arrays (H2D of the particle state), a D2H read of each
+            step's result (time, step count, status) after every step, and
+            one output frame of the driver's particle fields at the end
   roofline  the dominant kernel's algorithmic bytes per launch over its
             average CUDA-event duration, against the measured HBM copy peak
   cpu_baseline  the oracle (the CPU restatement of the reference's pthreaded
@@ -37,6 +39,8 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# the particle fields of the driver's output frame (write_frame, src/writer.c)
+FRAME_FIELDS = ("m", "v", "x", "y", "vx", "vy", "sxx", "sxy", "syy", "ux", "uy", "state9", "state10")
 PKG = os.path.join(ROOT, "mpm-2d_gb300")
 for _p in (ROOT, PKG):
     if _p not in sys.path:
@@ -299,33 +303,50 @@ def run_gpu(args):
     phases64 = phase_profile(sim64, 3, FP64_BYTES, n, ne, nn)
     sim64.close()
 
+    # --- mixed form with FP64 nodal sums and division --------------------------
+    simf = mpm2d.Simulation(scene, device=dev, precision="mixed_f64node")
+    streamf = torch.cuda.ExternalStream(simf.stream(), device=dev)
+    simf.step(args.warmup)
+    simf.synchronize()
+    barrier()
+    msf = time_steps(simf, args.steps, streamf, torch)
+    barrier()
+    valuef = n * args.steps * world / max_over_ranks(msf / 1e3)
+    simf.close()
+
     # --- end to end through the C ABI with host buffers (mixed) ---------------
-    import ctypes as C
-    frame_fields = ("x", "y", "vx", "vy", "sxx", "sxy", "syy", "v")
-    e2e_steps = max(2, min(args.steps, 20))
-    host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in frame_fields}
+    # The user's run: create the simulation from host arrays (H2D of the
+    # particle state), step, read each step's result back (mpmg_get_time:
+    # stream sync + D2H of the step record), and write the output frame at
+    # the end (mpmg_get_fields of the driver's write_frame fields into pinned
+    # host buffers).
+    e2e_steps = args.e2e_steps
+    host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
     barrier()
     t0 = time.perf_counter()
     sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
+    t1 = time.perf_counter()
     for _ in range(e2e_steps):
         sim2.step(1)
-        for f in frame_fields:
-            rc = mpm2d.lib().mpmg_get_field(sim2._h, f.encode(),
-                                            C.cast(host[f].data_ptr(), C.POINTER(C.c_double)))
-            if rc != 0:
-                raise RuntimeError("mpmg_get_field failed: %d" % rc)
-    sim2.synchronize()
+        sim2.t
+    t2 = time.perf_counter()
+    sim2.get_frame(FRAME_FIELDS, out=host)
+    t3 = time.perf_counter()
     barrier()
-    e2e_t = max_over_ranks(time.perf_counter() - t0)
+    e2e_t = max_over_ranks(t3 - t0)
     sim2.close()
     e2e_value = n * e2e_steps * world / e2e_t
+    h2d_total = 9 * 8 * n                      # m v x y vx vy sxx sxy syy
+    d2h_frame = len(FRAME_FIELDS) * 8 * n      # the frame's FP64 fields in particle order
+    step_record = 64                           # step record + status word, one copy per step
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "particles": n, "grid_nodes": [scene["Nx"], scene["Ny"]],
-                   "material": scene["material"], "bc": scene["bc"], "precision": "mixed",
+                   "material": scene["material"], "bc": scene["bc"],
+                   "precision": "mixed: FP32 particles, float-float nodal sums",
                    "l2_policy": "state and step scratch exceed the 129 MB L2 between steps",
                    "step_launch": "CUDA graphs of 8 steps",
                    "parallelism": "replicas" if world > 1 else "single"},
@@ -342,9 +363,13 @@ def run_gpu(args):
                  "dtype": "f64", "phases": phases64,
                  "bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s)"},
         "mixed_over_fp64": value / value64,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 9 * 8 * n / e2e_steps,
-                "d2h_bytes_per_step": len(frame_fields) * 8 * n, "steps": e2e_steps,
-                "path": "mpmg_create from host arrays + per-step mpmg_get_field of 8 frame fields"},
+        "mixed_f64node": {"value": valuef, "unit": UNIT, "steps": args.steps, "ms_per_step": msf / args.steps,
+                          "note": "same mixed step with FP64 nodal mass/momentum sums and division"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
+                "d2h_bytes_per_step": step_record + d2h_frame / e2e_steps, "steps": e2e_steps,
+                "create_s": t1 - t0, "steps_s": t2 - t1, "frame_s": t3 - t2,
+                "path": "mpmg_create from host arrays, per step mpmg_step + mpmg_get_time, "
+                        "one output frame (mpmg_get_fields of %d fields)" % len(FRAME_FIELDS)},
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -368,6 +393,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=60)
+    ap.add_argument("--e2e-steps", type=int, default=500,
+                    help="steps of the end-to-end run (one output frame at its end)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

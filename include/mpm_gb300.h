@@ -69,13 +69,19 @@ enum mpmg_gravity {
 
 /* Arithmetic of the step.  MPMG_PRECISION_FP64 is the reference's (FP64
    everywhere).  MPMG_PRECISION_MIXED keeps particle state, shape functions,
-   P2G and G2P contributions and the material update in FP32, and nodal mass
-   and momentum sums and the division by nodal mass in FP64; particles are
-   kept in element order on the device (read-back returns the caller's
-   order).  Mixed supports the local materials (isolin, g_local_mu2). */
+   P2G and G2P contributions and the material update in FP32, and sums nodal
+   mass and momentum, updates the momentum and divides by nodal mass in
+   float-float arithmetic (an unevaluated sum of two FP32 values: 48
+   significant bits, on the FP32 pipe); MPMG_PRECISION_MIXED_F64NODE does
+   those nodal sums and the division in FP64 instead (GB300 runs FP64 at 1/64
+   of the FP32 rate, so this form's grid update is several times slower).
+   Both mixed forms keep particles in element order on the device (read-back
+   returns the caller's order) and support the local materials (isolin,
+   g_local_mu2). */
 enum mpmg_precision {
     MPMG_PRECISION_FP64 = 0,
-    MPMG_PRECISION_MIXED = 1
+    MPMG_PRECISION_MIXED = 1,
+    MPMG_PRECISION_MIXED_F64NODE = 2
 };
 
 /* Material parameter slots (mpmg_config.mp).  mpmg_default_params fills the
@@ -144,6 +150,12 @@ MPMG_API int mpmg_synchronize(mpmg_ctx *ctx);
    Tyy Tzz state0..state10.  Node fields: node_m node_mx node_my node_fx
    node_fy node_vx node_vy node_ax node_ay node_gf. */
 MPMG_API int mpmg_get_field(mpmg_ctx *ctx, const char *name, double *host_out);
+/* Reads count fields at once, each device array behind them downloaded
+   once: a whole output frame, as the driver's write_frame
+   (src/writer.c:190-201, called from src/main.c:957) reads the particles'
+   m v x y x_t y_t sxx sxy syy ux uy state[9] state[10].  host_out[k]
+   receives names[k]. */
+MPMG_API int mpmg_get_fields(mpmg_ctx *ctx, int count, const char *const *names, double *const *host_out);
 MPMG_API int mpmg_set_field(mpmg_ctx *ctx, const char *name, const double *host_in);
 
 /* Element of each particle (-1 outside) and active flags

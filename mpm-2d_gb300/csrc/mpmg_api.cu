@@ -57,12 +57,38 @@ bool material_uses_state(int material, int k)
     }
 }
 
+// The step record (StepParams, then the status word) lives in one device
+// block with a pinned host mirror, so a read-back of both is one copy.
+constexpr size_t kStatusOffset = (sizeof(StepParams) + 15) / 16 * 16;
+constexpr size_t kStepRecordBytes = kStatusOffset + 16;
+
+int alloc_step_record(mpmg_ctx *ctx)
+{
+    unsigned char *block = nullptr;
+    cudaError_t e = cudaMalloc((void **)&block, kStepRecordBytes);
+    if (e != cudaSuccess) {
+        mpmg_set_error("cudaMalloc of the step record failed: %s", cudaGetErrorString(e));
+        return MPMG_ERR_NOMEM;
+    }
+    ctx->d_params = (StepParams *)block;
+    ctx->d_status = (int *)(block + kStatusOffset);
+    e = cudaHostAlloc((void **)&ctx->h_record, kStepRecordBytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        ctx->h_record = nullptr;
+        mpmg_set_error("cudaHostAlloc of the step record failed: %s", cudaGetErrorString(e));
+        return MPMG_ERR_NOMEM;
+    }
+    return MPMG_OK;
+}
+
 int sync_status(mpmg_ctx *ctx)
 {
+    MPMG_CHECK(cudaMemcpyAsync(ctx->h_record, ctx->d_params, kStepRecordBytes, cudaMemcpyDeviceToHost,
+                               ctx->stream));
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
     int st = 0;
-    MPMG_CHECK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-    MPMG_CHECK(cudaMemcpy(&ctx->h_params, ctx->d_params, sizeof(StepParams), cudaMemcpyDeviceToHost));
+    memcpy(&ctx->h_params, ctx->h_record, sizeof(StepParams));
+    memcpy(&st, ctx->h_record + kStatusOffset, sizeof(int));
     if (st != 0) {
         // Report each device-side error once; the caller decides whether to go on.
         MPMG_CHECK(cudaMemset(ctx->d_status, 0, sizeof(int)));
@@ -298,8 +324,8 @@ int mpmg_destroy(mpmg_ctx *ctx)
     cudaFree(ctx->sorted_keys);
     cudaFree(ctx->perm);
     cudaFree(ctx->cell_start);
-    cudaFree(ctx->d_params);
-    cudaFree(ctx->d_status);
+    cudaFree(ctx->d_params);      // the step record block (d_status lies inside it)
+    if (ctx->h_record) cudaFreeHost(ctx->h_record);
     mpmg_bin_free(ctx);
     mpmg_nonlocal_free(ctx);
     mpmg_mixed_free(ctx);
@@ -339,6 +365,10 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
     if (cfg->bc != MPMG_BOX && cfg->bc != MPMG_SQUARE_SILO) {
         mpmg_set_error("unknown boundary-condition kind %d", cfg->bc);
         return MPMG_ERR_UNSUPPORTED;
+    }
+    if (cfg->precision < MPMG_PRECISION_FP64 || cfg->precision > MPMG_PRECISION_MIXED_F64NODE) {
+        mpmg_set_error("unknown precision %d", cfg->precision);
+        return MPMG_ERR_INVALID;
     }
     if (n > 0 && (!m || !v || !x || !y || !vx || !vy || !sxx || !sxy || !syy)) {
         mpmg_set_error("null particle array");
@@ -403,7 +433,8 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
     {
         const bool transients = cfg->store_transients != 0;
         const bool nonlocal = cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL;
-        const bool mixed = cfg->precision == MPMG_PRECISION_MIXED;
+        const bool mixed =
+            cfg->precision == MPMG_PRECISION_MIXED || cfg->precision == MPMG_PRECISION_MIXED_F64NODE;
         if (mixed && nonlocal) {
             mpmg_set_error("mixed precision supports isolin and g_local_mu2");
             rc = MPMG_ERR_UNSUPPORTED;
@@ -422,8 +453,7 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
                 double **tn[] = {&ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy};
                 for (double **p : tn) TRY(dalloc(p, ctx->nn));
             }
-            TRY(dalloc(&ctx->d_params, 1));
-            TRY(dalloc(&ctx->d_status, 1));
+            TRY(alloc_step_record(ctx));
             TRY(mpmg_bin_init(ctx));
             TRY(fill_zero(ctx, ctx->cell_start, (ctx->ne + 1) * sizeof(int)));
             TRY(fill_zero(ctx, ctx->node_m, ctx->nn * sizeof(double)));
@@ -471,8 +501,7 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             double **tn[] = {&ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy};
             for (double **p : tn) TRY(dalloc(p, ctx->nn));
         }
-        TRY(dalloc(&ctx->d_params, 1));
-        TRY(dalloc(&ctx->d_status, 1));
+        TRY(alloc_step_record(ctx));
         TRY(mpmg_bin_init(ctx));
         if (nonlocal) TRY(mpmg_nonlocal_init(ctx));
 
@@ -667,6 +696,31 @@ int mpmg_get_field(mpmg_ctx *ctx, const char *name, double *host_out)
         for (size_t i = 0; i < f.count; i++) host_out[i] = by;
     } else if (f.count > 0) {
         MPMG_CHECK(cudaMemcpy(host_out, f.ptr, f.count * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return MPMG_OK;
+}
+
+int mpmg_get_fields(mpmg_ctx *ctx, int count, const char *const *names, double *const *host_out)
+{
+    if (ctx == nullptr || count < 0 || (count > 0 && (names == nullptr || host_out == nullptr)))
+        return MPMG_ERR_INVALID;
+    for (int k = 0; k < count; k++)
+        if (names[k] == nullptr || host_out[k] == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    std::vector<char> done(count > 0 ? count : 1, 0);
+    if (ctx->mixed) {
+        int rc = sync_status(ctx);
+        if (rc != MPMG_OK) return rc;
+        bool *flags = new bool[count > 0 ? count : 1];
+        rc = mpmg_mixed_get_many(ctx, count, names, host_out, flags);
+        for (int k = 0; k < count; k++) done[k] = flags[k];
+        delete[] flags;
+        if (rc != MPMG_OK) return rc;
+    }
+    for (int k = 0; k < count; k++) {
+        if (done[k]) continue;
+        int rc = mpmg_get_field(ctx, names[k], host_out[k]);
+        if (rc != MPMG_OK) return rc;
     }
     return MPMG_OK;
 }

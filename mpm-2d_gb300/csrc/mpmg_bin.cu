@@ -22,8 +22,8 @@
 
 namespace {
 
-constexpr int kScanThreads = 512;
-constexpr int kScanItems = 16;
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 12;     // 12288 bins a tile: up to 33 tiles every look-back ends in one window
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 __global__ void __launch_bounds__(256) count_kernel(const uint32_t *__restrict__ keys, int n, uint32_t sentinel,
@@ -74,14 +74,18 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(uint32_t *__restrict
     __shared__ uint32_t prefix_s;
     __shared__ int abort_s;
     if (threadIdx.x == 0) {
+        // ticket and epoch belong to the scan alone (the previous scan has
+        // completed): taken before waiting for the kernel that counted the bins
         tile_s = (int)atomicInc(&ticket_epoch[0], gridDim.x - 1u);
         epoch_s = *(volatile unsigned int *)&ticket_epoch[1] & kEpochMask;
         abort_s = 0;
     }
+    mpmg_pdl_wait();
+    mpmg_pdl_trigger();
     __syncthreads();
     const int tile = tile_s;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int base = tile * kScanTile + threadIdx.x * kScanItems;   // 16 consecutive bins per thread
+    const int base = tile * kScanTile + threadIdx.x * kScanItems;   // 12 consecutive bins per thread
     uint32_t v[kScanItems];
     uint32_t sum = 0;
     if (base + kScanItems <= m) {
@@ -191,9 +195,11 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(uint32_t *__restrict
     }
 }
 
-// Each warp scatters 4 consecutive groups of 32 keys.  The groups' keys,
-// peer sets and cursor atomics are all issued before any result is used, so
-// a lane has its four atomics in flight at once.
+// Each warp scatters 4 consecutive groups of 32 keys.  Within a group, each
+// run of equal keys in consecutive lanes takes its slots with one atomic
+// (the keys arrive nearly sorted, so a group holds a few runs); the groups'
+// atomics are all issued before any result is used, so a lane has its four
+// atomics in flight at once.
 constexpr int kScatterGroups = 4;
 
 __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict__ keys, int n, uint32_t sentinel,
@@ -204,37 +210,45 @@ __global__ void __launch_bounds__(256) scatter_kernel(const uint32_t *__restrict
     const int lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
     const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t key[kScatterGroups], peers[kScatterGroups], base[kScatterGroups], outside[kScatterGroups];
+    uint32_t key[kScatterGroups], starts[kScatterGroups], base[kScatterGroups], outside[kScatterGroups];
 #pragma unroll
     for (int j = 0; j < kScatterGroups; j++) {
         const int k = (warp_global * kScatterGroups + j) * 32 + lane;
         key[j] = k < n ? keys[k] : sentinel + 1u;     // sentinel + 1: no key
     }
+    // the keys come from before the scan; the cursors from the scan
+    mpmg_pdl_wait();
 #pragma unroll
     for (int j = 0; j < kScatterGroups; j++) {
         const bool in = key[j] < sentinel;
+        const uint32_t b = in ? key[j] : 0xffffffffu;
+        const uint32_t prev = __shfl_up_sync(0xffffffffu, b, 1);
+        const bool start = in && (lane == 0 || prev != b);
+        starts[j] = __ballot_sync(0xffffffffu, start);
         outside[j] = __ballot_sync(0xffffffffu, key[j] == sentinel);
-        const uint32_t inmask = __ballot_sync(0xffffffffu, in);
-        peers[j] = in ? __match_any_sync(inmask, key[j]) : 0u;
-    }
-#pragma unroll
-    for (int j = 0; j < kScatterGroups; j++) {
+        const uint32_t invalid = ~__ballot_sync(0xffffffffu, in);
         base[j] = 0;
-        if (peers[j] != 0u && lane == __ffs(peers[j]) - 1)
-            base[j] = atomicAdd(&cursor[key[j]], (uint32_t)__popc(peers[j]));
+        if (start) {
+            const uint32_t above = lane == 31 ? 0u : (starts[j] | invalid) & (0xfffffffeu << lane);
+            const int end = above ? __ffs(above) - 1 : 32;
+            base[j] = atomicAdd(&cursor[key[j]], (uint32_t)(end - lane));
+        }
     }
+    mpmg_pdl_trigger();
 #pragma unroll
     for (int j = 0; j < kScatterGroups; j++) {
         const int group = warp_global * kScatterGroups + j;
         const int k = group * 32 + lane;
+        const uint32_t below = starts[j] & (lt | (1u << lane));
+        const int leader = below ? 31 - __clz(below) : lane;
+        const uint32_t b = __shfl_sync(0xffffffffu, base[j], leader);
         if (key[j] == sentinel) {
             const uint32_t pos = cursor[sentinel + group] + __popc(outside[j] & lt);
             perm[pos] = (uint32_t)k;      // final: storage order within the group's run
             rank[k] = pos;
             if (sorted_keys != nullptr) sorted_keys[pos] = key[j];
-        } else if (peers[j] != 0u) {
-            const uint32_t b = __shfl_sync(peers[j], base[j], __ffs(peers[j]) - 1);
-            const uint32_t pos = b + __popc(peers[j] & lt);
+        } else if (key[j] < sentinel) {
+            const uint32_t pos = b + (uint32_t)(lane - leader);
             slots[pos] = (uint32_t)k;
             if (sorted_keys != nullptr) sorted_keys[pos] = key[j];
         }
@@ -297,20 +311,22 @@ int mpmg_bin_reset(mpmg_ctx *ctx)
 // Scan of the counted bins and scatter of keys[n]: cell_start[ne + 1],
 // perm and rank for keys outside the grid, bin.slots (unordered within each
 // element) for the rest, and sorted_keys[n] unless it is null.
-int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys, uint32_t *sorted_keys)
+int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys, uint32_t *sorted_keys, bool pdl)
 {
     cudaStream_t s = ctx->stream;
     const int n = (int)ctx->np;
     const int m = ctx->bin.bins;
     const int tiles = ctx->bin.tiles;
     unsigned int *ticket_epoch = (unsigned int *)(ctx->bin.tile_state + tiles);
-    scan_kernel<<<tiles, kScanThreads, 0, s>>>(ctx->bin.counts, m, (int)ctx->ne, ctx->bin.tile_state, ticket_epoch,
-                                               ctx->cell_start, ctx->bin.cursor, ctx->d_status);
+    MPMG_CHECK(mpmg_launch_pdl(pdl, scan_kernel, dim3(tiles), dim3(kScanThreads), 0, s, ctx->bin.counts, m,
+                               (int)ctx->ne, ctx->bin.tile_state, ticket_epoch, ctx->cell_start, ctx->bin.cursor,
+                               ctx->d_status));
     ctx->launches += 1;
     if (n > 0) {
         const int keys_per_block = 256 * kScatterGroups;
-        scatter_kernel<<<(n + keys_per_block - 1) / keys_per_block, 256, 0, s>>>(
-            keys, n, (uint32_t)ctx->ne, ctx->bin.cursor, ctx->bin.slots, ctx->perm, ctx->bin.rank, sorted_keys);
+        MPMG_CHECK(mpmg_launch_pdl(pdl, scatter_kernel, dim3((n + keys_per_block - 1) / keys_per_block), dim3(256),
+                                   0, s, keys, n, (uint32_t)ctx->ne, ctx->bin.cursor, ctx->bin.slots, ctx->perm,
+                                   ctx->bin.rank, sorted_keys));
         ctx->launches += 1;
     }
     MPMG_CHECK(cudaGetLastError());

@@ -64,6 +64,8 @@ struct MixedState {
     float *cell_sums;      // 20 FP32 corner sums per element, value-major
     float4 *node4;         // per node: ax, ay, vx, vy (FP32) for the gathers
     float2 *node_mass;     // per node: mass as float-float (hi, lo)
+    int g2p_blocks;        // persistent G2P grid size
+    double *export_buf;    // one FP64 particle field in caller order, for read-back
 };
 
 // Counting-sort binning scratch (mpmg_bin.cu).  Bins 0..ne-1 count the keys
@@ -125,6 +127,7 @@ struct mpmg_ctx {
     StepParams *d_params;
     StepParams h_params;   // host mirror, refreshed on read-back
     int *d_status;
+    unsigned char *h_record;   // pinned host mirror of the step record and status
 
     // Mixed precision (cfg.precision == MPMG_PRECISION_MIXED).
     MixedState *mixed;
@@ -186,7 +189,7 @@ int mpmg_bin_count(mpmg_ctx *ctx, const uint32_t *keys);
 // null), and perm for keys outside the grid; element slots stay unordered in
 // bin.slots until a P2G kernel orders them into perm (mpmg_order_segment).
 // mpmg_bin_reset restores the look-back state after a timed-out wait.
-int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys, uint32_t *sorted_keys);
+int mpmg_bin_scan_scatter(mpmg_ctx *ctx, const uint32_t *keys, uint32_t *sorted_keys, bool pdl = false);
 int mpmg_bin_reset(mpmg_ctx *ctx);
 int mpmg_nonlocal_init(mpmg_ctx *ctx);
 void mpmg_nonlocal_free(mpmg_ctx *ctx);
@@ -201,6 +204,7 @@ int mpmg_mixed_step(mpmg_ctx *ctx);
 // MPMG_ERR_UNKNOWN_FIELD for names the mixed state does not hold.
 int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out);
 int mpmg_mixed_set(mpmg_ctx *ctx, const char *name, const double *in);
+int mpmg_mixed_get_many(mpmg_ctx *ctx, int count, const char *const *names, double *const *out, bool *done);
 int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active);
 
 void mpmg_phase_begin(mpmg_ctx *ctx, int phase);
@@ -244,19 +248,160 @@ __device__ __forceinline__ double mpmg_local_coord(double xp, double xn, double 
 
 // Counts one key into the bins (see BinScratch): bins[key] for keys inside
 // the grid, bins[sentinel + group] for keys outside it, where group is the
-// key's destination position / 32.  Equal bins within a warp are aggregated
-// into one atomic.  Every lane of the warp must call it (valid marks lanes
+// key's destination position / 32.  Runs of equal bins in consecutive lanes
+// are aggregated into one atomic (the keys arrive nearly sorted, so a warp
+// holds a few runs).  Every lane of the warp must call it (valid marks lanes
 // that carry a key).
 __device__ __forceinline__ void mpmg_bin_count(uint32_t key, bool valid, uint32_t sentinel, uint32_t group,
                                                uint32_t *bins)
 {
-    const uint32_t bin = (key == sentinel) ? sentinel + group : key;
-    const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
-        const uint32_t peers = __match_any_sync(vmask, bin);
-        const int lane = threadIdx.x & 31;
-        if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&bins[bin], (uint32_t)__popc(peers));
+    const int lane = threadIdx.x & 31;
+    const uint32_t bin = valid ? ((key == sentinel) ? sentinel + group : key) : 0xffffffffu;
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, bin, 1);
+    const bool start = valid && (lane == 0 || prev != bin);
+    const uint32_t starts = __ballot_sync(0xffffffffu, start);
+    const uint32_t invalid = ~__ballot_sync(0xffffffffu, valid);
+    if (start) {
+        const uint32_t above = lane == 31 ? 0u : (starts | invalid) & (0xfffffffeu << lane);
+        const int end = above ? __ffs(above) - 1 : 32;
+        atomicAdd(&bins[bin], (uint32_t)(end - lane));
     }
+}
+
+__device__ __forceinline__ uint32_t mpmg_smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Programmatic dependent launch.  A kernel launched with
+// mpmg_launch_pdl may start while the kernel before it in the stream is
+// still running; mpmg_pdl_wait blocks until that kernel has completed and
+// its writes are visible (a no-op for an ordinary launch), and
+// mpmg_pdl_trigger lets the next kernel start launching.  Every kernel of the
+// mixed step triggers only after its own wait, so when a kernel starts, the
+// kernel two places before it has completed: data written by that kernel or
+// earlier ones may be read before the wait, data of the immediately
+// preceding kernel only after it.
+__device__ __forceinline__ void mpmg_pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+__device__ __forceinline__ void mpmg_pdl_trigger()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t mpmg_launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                   cudaStream_t stream, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, ((KArgs)args)...);
+}
+
+// Asynchronous global -> shared copies of 16 or 4 bytes (cp.async, cached in
+// L1), completed by mpmg_cp_async_wait_all.
+__device__ __forceinline__ void mpmg_cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(mpmg_smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void mpmg_cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(mpmg_smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void mpmg_cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// Unsigned division by a run-time constant d >= 1 (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", 1994, round-up
+// variant): n / d = (umulhi(n, magic) + n) >> shift for every 32-bit n, with
+// shift = ceil(log2 d) and magic = floor(2^32 (2^shift - d) / d) + 1.
+struct MpmgDiv {
+    uint32_t magic, shift, d;
+};
+
+inline MpmgDiv mpmg_div_init(uint32_t d)
+{
+    MpmgDiv v;
+    uint32_t l = 0;
+    while (l < 32 && (1ull << l) < (unsigned long long)d) l++;
+    v.magic = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1ull);
+    v.shift = l;
+    v.d = d;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t mpmg_div(uint32_t n, const MpmgDiv &v)
+{
+    return (uint32_t)(((unsigned long long)__umulhi(n, v.magic) + n) >> v.shift);
+}
+
+// Bulk asynchronous copies (TMA, cp.async.bulk) into shared memory, completed
+// on an mbarrier, and the bounded wait for them.
+__device__ __forceinline__ void mpmg_mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mpmg_smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mpmg_mbar_init_fence()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Orders this thread's earlier shared-memory accesses before later
+// asynchronous-proxy (bulk copy) accesses.
+__device__ __forceinline__ void mpmg_fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mpmg_mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mpmg_smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// dst, src and bytes must be multiples of 16 bytes.
+__device__ __forceinline__ void mpmg_bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     mpmg_smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(mpmg_smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mpmg_mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(mpmg_smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Waits for phase `parity` of the barrier to complete; false after `limit`
+// polls.
+__device__ __forceinline__ bool mpmg_mbar_wait(uint64_t *bar, uint32_t parity, long long limit)
+{
+    for (long long polls = 0; polls < limit; polls++)
+        if (mpmg_mbar_try_wait(bar, parity)) return true;
+    return false;
 }
 
 // perm[k0..k1) = slots[k0..k1) in ascending order (insertion sort: elements

@@ -1,4 +1,5 @@
-// Mixed-precision explicit USL step (MPMG_PRECISION_MIXED).
+// Mixed-precision explicit USL step (MPMG_PRECISION_MIXED and
+// MPMG_PRECISION_MIXED_F64NODE).
 //
 // Same phases as the FP64 step (mpmg_step.cu), re-laid out for bandwidth:
 //   * Particle state is FP32.  Positions are stored as the element index plus
@@ -18,8 +19,9 @@
 //     particles each); the four elements around a node are summed in
 //     float-float (an unevaluated sum of two FP32 values, ~48 bits) for mass
 //     and momentum, the momentum update and the division by nodal mass are
-//     float-float as well, all on the FP32 pipe, and the node's acceleration
-//     and velocity are stored in FP32 for the gathers.
+//     float-float as well, all on the FP32 pipe (MPMG_PRECISION_MIXED_F64NODE:
+//     in FP64), and the node's acceleration and velocity are stored in FP32
+//     for the gathers.
 // Time and gravity advance on the device: the G2P's first thread moves t and
 // the next step's gravity (loading.c:34-54) once all reads of them are done.
 #include <math.h>
@@ -33,6 +35,7 @@ namespace {
 
 struct GeomM {
     int Nx, Ny, Ex, Ey, ne;
+    MpmgDiv div_Ex, div_Nx;
     float hf, inv_hf;
     double h;
     float xmaxf, ymaxf;
@@ -63,6 +66,10 @@ Buf buf(const MixedState *s, int b)
 struct MatF {
     float G, K, lambda, dt;
     float mu_s, mu_2, I0, grains_rho, grains_d, rho_critical;
+    // constant factors of the g_local_mu2 update, formed in FP64 on the host
+    float inv_grains_rho;  // 1 / grains_rho
+    float alpha_coef;      // G I0 dt / grains_d
+    float inv_G_dt;        // 1 / (G dt)
 };
 
 // isolin (isolin.c:75-116) in FP32.
@@ -102,21 +109,25 @@ __device__ __forceinline__ void g_local_mu2_f(const MatF &p, float m, float v, f
     const float tau_tr = sqrtf(0.5f * (T0xx * T0xx + 2.0f * T0xy * T0xy + T0yy * T0yy + T0zz * T0zz));
     const float p_tr = -pm;
     float nup = 0.0f;
-    if (m / v < p.rho_critical || p_tr <= 0.0f) {
+    // m / v < rho_critical with v > 0; the divisions of the reference become
+    // products with the host-formed reciprocals, and the two that remain use
+    // the fast FP32 divide (about 2 ulp), all well inside the mixed form's
+    // FP32 rounding budget
+    if (m < p.rho_critical * v || p_tr <= 0.0f) {
         Txx = Txy = Tyy = Tzz = 0.0f;
     } else if (p_tr > 0.0f) {
         const float S0 = p.mu_s * p_tr;
         float tau_tau = tau_tr, scale = 1.0f;
         if (tau_tr > S0) {
             const float S2 = p.mu_2 * p_tr;
-            const float alpha = G * p.I0 * dt * sqrtf(p_tr / p.grains_rho) / p.grains_d;
+            const float alpha = p.alpha_coef * sqrtf(p_tr * p.inv_grains_rho);
             const float B = -(S2 + tau_tr + alpha);
             const float H = S2 * tau_tr + S0 * alpha;
             const float disc = sqrtf(B * B - 4.0f * H);
-            tau_tau = (B > 0.0f) ? (-B - disc) * 0.5f : (2.0f * H) / (-B + disc);
-            scale = tau_tau / tau_tr;
+            tau_tau = (B > 0.0f) ? (-B - disc) * 0.5f : __fdividef(2.0f * H, -B + disc);
+            scale = __fdividef(tau_tau, tau_tr);
         }
-        nup = (tau_tr - tau_tau) / G / dt;
+        nup = (tau_tr - tau_tau) * p.inv_G_dt;
         Txx = T0xx * scale - p_tr;
         Txy = T0xy * scale;
         Tyy = T0yy * scale - p_tr;
@@ -151,28 +162,30 @@ __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double t_
 // P2G: a block takes 256 consecutive elements, one thread each, and works
 // through them in passes of whole elements whose particles (a contiguous
 // range of the binned order) fit a 1024-particle shared-memory stage.  Each
-// pass stages slots and particle records with coalesced, batched loads (the
+// pass loads the range's slots (coalesced) and copies the particle records
+// they point to into shared memory with asynchronous copies (cp.async; the
 // slots are close to the identity because the storage is kept in element
-// order); then every thread orders its element's stage indices by storage
-// position (insertion sort in shared memory: the deterministic,
-// launch-order-independent order), writes perm and rank, and sums its
-// particles in that order: 4 corners x (m, mvx, mvy, fx, fy) in FP32
-// (process_usl.c:491-522 per particle, regrouped per element).  An element
-// with more particles than the stage is summed alone from global memory.
+// order, so the copies are nearly sequential); then every thread orders its
+// element's stage indices by storage position (insertion sort in shared
+// memory: the deterministic, launch-order-independent order), writes perm
+// and rank, and sums its particles in that order: 4 corners x (m, mvx, mvy,
+// fx, fy) in FP32 (process_usl.c:491-522 per particle, regrouped per
+// element).  An element with more particles than the stage is summed alone
+// from global memory.
 constexpr int kP2GThreads = 256;
 constexpr int kP2GChunk = 1024;
-constexpr int kP2GBatch = 2;        // particles per thread whose loads are in flight together
+constexpr int kP2GPer = kP2GChunk / kP2GThreads;   // stage entries per thread
 
-__device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, float grav, float xl, float yl,
-                                               float vx, float vy, float m, float vol, float sxx, float sxy,
+__device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, float grav, float4 a4, float4 b4,
                                                float syy)
 {
+    const float xl = a4.x, yl = a4.y, m = b4.x, vol = b4.y;
     const float ox = 1.0f - xl, oy = 1.0f - yl;
     const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
     const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
     const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
-    const float pmx = vx * m, pmy = vy * m, pby = grav * m;
-    const float s0 = -sxx * vol, s1 = -sxy * vol, s2 = -syy * vol;
+    const float pmx = a4.z * m, pmy = a4.w * m, pby = grav * m;
+    const float s0 = -b4.z * vol, s1 = -b4.w * vol, s2 = -syy * vol;
 #pragma unroll
     for (int a = 0; a < 4; a++) {
         acc[a][0] += s[a] * m;
@@ -190,13 +203,18 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
                                                                 const StepParams *__restrict__ sp,
                                                                 float *__restrict__ cell_sums)
 {
-    __shared__ float sh[9][kP2GChunk];
+    __shared__ float4 sh_a[kP2GChunk];
+    __shared__ float4 sh_b[kP2GChunk];
+    __shared__ float sh_syy[kP2GChunk];
     __shared__ uint32_t sh_slot[kP2GChunk];
     __shared__ uint16_t sh_ord[kP2GChunk];
     __shared__ int sh_cs[kP2GThreads + 1];
     const int e0 = blockIdx.x * kP2GThreads;
     const int ne_blk = min(kP2GThreads, g.ne - e0);
+    // element offsets come from the scan, two kernels back; the slots from
+    // the scatter, the kernel just before
     for (int t = threadIdx.x; t <= ne_blk; t += kP2GThreads) sh_cs[t] = cell_start[e0 + t];
+    mpmg_pdl_wait();
     __syncthreads();
     const int me = threadIdx.x;
     const int k0 = me < ne_blk ? sh_cs[me] : 0, k1 = me < ne_blk ? sh_cs[me + 1] : 0;
@@ -221,40 +239,23 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
 #pragma unroll
             for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
         if (end - base <= kP2GChunk) {
-            for (int k = base + (int)threadIdx.x; k < end; k += kP2GBatch * kP2GThreads) {
-                uint32_t sl[kP2GBatch];
-                float4 a4[kP2GBatch], b4[kP2GBatch];
-                float c[kP2GBatch];
+            uint32_t sl[kP2GPer];
 #pragma unroll
-                for (int u = 0; u < kP2GBatch; u++) {
-                    const int kk = k + u * kP2GThreads;
-                    sl[u] = kk < end ? slots[kk] : 0u;
-                }
+            for (int u = 0; u < kP2GPer; u++) {
+                const int k = base + (int)threadIdx.x + u * kP2GThreads;
+                sl[u] = k < end ? slots[k] : 0u;
+            }
 #pragma unroll
-                for (int u = 0; u < kP2GBatch; u++) {
-                    if (k + u * kP2GThreads < end) {
-                        a4[u] = P.A[sl[u]];
-                        b4[u] = P.B[sl[u]];
-                        c[u] = P.C[sl[u]].x;
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < kP2GBatch; u++) {
-                    const int j = k + u * kP2GThreads - base;
-                    if (j < end - base) {
-                        sh_slot[j] = sl[u];
-                        sh[0][j] = a4[u].x;
-                        sh[1][j] = a4[u].y;
-                        sh[2][j] = a4[u].z;
-                        sh[3][j] = a4[u].w;
-                        sh[4][j] = b4[u].x;
-                        sh[5][j] = b4[u].y;
-                        sh[6][j] = b4[u].z;
-                        sh[7][j] = b4[u].w;
-                        sh[8][j] = c[u];
-                    }
+            for (int u = 0; u < kP2GPer; u++) {
+                const int j = (int)threadIdx.x + u * kP2GThreads;
+                if (base + j < end) {
+                    sh_slot[j] = sl[u];
+                    mpmg_cp_async16(&sh_a[j], P.A + sl[u]);
+                    mpmg_cp_async16(&sh_b[j], P.B + sl[u]);
+                    mpmg_cp_async4(&sh_syy[j], &P.C[sl[u]].x);
                 }
             }
+            mpmg_cp_async_wait_all();
             __syncthreads();
             if (mine) {
                 const int j0 = k0 - base, j1 = k1 - base;
@@ -272,8 +273,7 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
                     const uint32_t i = sh_slot[q];
                     perm[base + j] = i;
                     rank[i] = (uint32_t)(base + j);
-                    p2g_accumulate(acc, ih, grav, sh[0][q], sh[1][q], sh[2][q], sh[3][q], sh[4][q], sh[5][q],
-                                   sh[6][q], sh[7][q], sh[8][q]);
+                    p2g_accumulate(acc, ih, grav, sh_a[q], sh_b[q], sh_syy[q]);
                 }
             }
             __syncthreads();
@@ -282,8 +282,7 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
             mpmg_order_segment(slots, perm, rank, k0, k1);
             for (int k = k0; k < k1; k++) {
                 const uint32_t i = perm[k];
-                const float4 a4 = P.A[i], b4 = P.B[i];
-                p2g_accumulate(acc, ih, grav, a4.x, a4.y, a4.z, a4.w, b4.x, b4.y, b4.z, b4.w, P.C[i].x);
+                p2g_accumulate(acc, ih, grav, P.A[i], P.B[i], P.C[i].x);
             }
         }
         if (mine) {
@@ -294,6 +293,7 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
         }
         ea = eb;
     }
+    mpmg_pdl_trigger();
 }
 
 // Double-FP32 ("float-float") helpers: a value is hi + lo with |lo| <= ulp(hi)/2,
@@ -330,6 +330,7 @@ __device__ __forceinline__ float ff_div(float nh, float nl, float dh, float dl, 
 // colour order (process_usl.c:524-540), float-float for mass and momentum;
 // boundary masks; momentum update and nodal velocity / acceleration
 // (process_usl.c:542-566).
+template <bool F64NODE>
 __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int *__restrict__ cell_start,
                                                       const float *__restrict__ cell_sums,
                                                       const StepParams *__restrict__ sp, double dt,
@@ -342,27 +343,76 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
     const int nn = g.Nx * g.Ny;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nn) return;
-    const int i = n % g.Nx, j = n / g.Nx;
-    float mh = 0, ml = 0, xh = 0, xl = 0, yh = 0, yl = 0;
-    float fx = 0, fy = 0;
+    const int j = (int)mpmg_div((uint32_t)n, g.div_Nx), i = n - j * g.Nx;
+    // the four elements in colour order and whether they hold particles
+    // (cell_start is from the scan, three kernels back)
+    int elem[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         int ci = ((i & 1) == (c & 1)) ? i : i - 1;
         int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        elem[c] = -1;
         if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
-        int e = cj * g.Ex + ci;
-        if (cell_start[e] == cell_start[e + 1]) continue;
-        int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+        const int e = cj * g.Ex + ci;
+        if (cell_start[e] != cell_start[e + 1]) elem[c] = e;
+    }
+    const double t_next = sp->t + dt;
+    mpmg_pdl_wait();        // the corner sums come from the P2G just before
+    mpmg_pdl_trigger();
+    float mh = 0, ml = 0, xh = 0, xl = 0, yh = 0, yl = 0;
+    float fx = 0, fy = 0;
+    double m64 = 0, mx64 = 0, my64 = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        if (elem[c] < 0) continue;
+        const int e = elem[c];
+        const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+        const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
         const float *cs = cell_sums + (size_t)(a * 5) * g.ne + e;
-        ff_add(mh, ml, cs[0]);
-        ff_add(xh, xl, cs[(size_t)g.ne]);
-        ff_add(yh, yl, cs[(size_t)2 * g.ne]);
+        if (F64NODE) {
+            m64 += (double)cs[0];
+            mx64 += (double)cs[(size_t)g.ne];
+            my64 += (double)cs[(size_t)2 * g.ne];
+        } else {
+            ff_add(mh, ml, cs[0]);
+            ff_add(xh, xl, cs[(size_t)g.ne]);
+            ff_add(yh, yl, cs[(size_t)2 * g.ne]);
+        }
         fx += cs[(size_t)3 * g.ne];
         fy += cs[(size_t)4 * g.ne];
     }
-    ff_norm(mh, ml);
     bool bx, by;
-    bc_mask_m(bc, i, j, sp->t + dt, bx, by);
+    bc_mask_m(bc, i, j, t_next, bx, by);
+    if (F64NODE) {
+        if (bx) { mx64 = 0; fx = 0; }
+        if (by) { my64 = 0; fy = 0; }
+        float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (m64 > (double)MPMG_TOL) {
+            // FP64 momentum update and division (1 / m: the FP32 reciprocal
+            // refined by one Newton step, ~2^-46 relative)
+            double r = (double)__frcp_rn((float)m64);
+            r = fma(r, fma(-m64, r, 1.0), r);
+            mx64 += dt * (double)fx;
+            my64 += dt * (double)fy;
+            const float rf = (float)r;
+            nd.x = fx * rf;
+            nd.y = fy * rf;
+            nd.z = (float)(mx64 * r);
+            nd.w = (float)(my64 * r);
+        }
+        const float mhi = (float)m64;
+        node_mass[n] = make_float2(mhi, (float)(m64 - (double)mhi));
+        node4[n] = nd;
+        if (node_mx != nullptr) {
+            node_mx[n] = mx64;
+            node_my[n] = my64;
+            node_fx[n] = fx;
+            node_fy[n] = fy;
+        }
+        return;
+    }
+    ff_norm(mh, ml);
     if (bx) { xh = 0; xl = 0; fx = 0; }
     if (by) { yh = 0; yl = 0; fy = 0; }
     float4 nd = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -395,17 +445,151 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
     }
 }
 
-// One thread per stored particle i (coalesced, independent loads); the
-// particle is written to its sorted position rank[i] of the other buffer.
+// G2P of one particle read from the stored position i (element e), written
+// to position dst of the other buffer: velocity and displacement from the
+// nodal accelerations and velocities (process_usl.c:568-611), strain rate
+// and vorticity (process_usl.c:613-640), volume (process_usl.c:642-650), the
+// material's stress update, and the new element (process_usl.c:660-666).
+// Returns the new element key (g.ne outside the grid).
 template <int MATERIAL>
-__global__ void __launch_bounds__(256, 4) mx_g2p_kernel(GeomM g, int n, MatF mp, const uint32_t *__restrict__ rank,
-                                                     Buf S, Buf D, const int *__restrict__ cell_src,
-                                                     int *__restrict__ cell_dst, const float4 *__restrict__ node4,
-                                                     uint32_t *__restrict__ bins, StepParams *sp, double dt,
-                                                     int gravity_mode, double gravity_const)
+__device__ __forceinline__ uint32_t g2p_particle(const GeomM &g, const MatF &mp, const float4 *__restrict__ node4,
+                                                 int e, float4 a4, float4 b4, float4 c4, float4 d4, uint32_t dst,
+                                                 Buf D, int *__restrict__ cell_dst)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
+    if (e >= g.ne) {
+        // outside the grid: carried along unchanged
+        D.A[dst] = a4;
+        D.B[dst] = b4;
+        D.C[dst] = c4;
+        D.D[dst] = d4;
+        cell_dst[dst] = g.ne;
+        return (uint32_t)g.ne;
+    }
+    const int cj = (int)mpmg_div((uint32_t)e, g.div_Ex), ci = e - cj * g.Ex;
+    const int n0 = cj * g.Nx + ci;
+    const float ih = g.inv_hf;
+    const float xl = a4.x, yl = a4.y;
+    const float ox = 1.0f - xl, oy = 1.0f - yl;
+    const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
+    const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
+    const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
+    const float4 nq[4] = {node4[n0], node4[n0 + 1], node4[n0 + 1 + g.Nx], node4[n0 + g.Nx]};
+    float xtt = 0, ytt = 0, dux = 0, duy = 0, exx = 0, eyy = 0, dxdy = 0, dydx = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        xtt += s[a] * nq[a].x;
+        ytt += s[a] * nq[a].y;
+        dux += s[a] * nq[a].z;
+        duy += s[a] * nq[a].w;
+        exx += gx[a] * nq[a].z;
+        eyy += gy[a] * nq[a].w;
+        dxdy += gy[a] * nq[a].z;
+        dydx += gx[a] * nq[a].w;
+    }
+    const float dtf = mp.dt;
+    const float vx = a4.z + dtf * xtt, vy = a4.w + dtf * ytt;
+    dux *= dtf;
+    duy *= dtf;
+    const float exy = 0.5f * (dxdy + dydx), wxy = 0.5f * (dxdy - dydx);
+    const float m = b4.x;
+    const float vol = b4.y * expf(dtf * (exx + eyy));
+    float sxx = b4.z, sxy = b4.w, syy = c4.x, Tzz = c4.w, gp = d4.x, gdp = d4.y;
+    if (MATERIAL == MPMG_ISOLIN) {
+        isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
+    } else {
+        g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
+    }
+
+    // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
+    float nxl = xl + dux * ih, nyl = yl + duy * ih;
+    const float fxl = floorf(nxl), fyl = floorf(nyl);
+    const int nci = ci + (int)fxl, ncj = cj + (int)fyl;
+    nxl -= fxl;
+    nyl -= fyl;
+    const float xg = ((float)nci + nxl) * g.hf, yg = ((float)ncj + nyl) * g.hf;
+    const bool inside = nci >= 0 && ncj >= 0 && nci < g.Ex && ncj < g.Ey && xg < g.xmaxf && yg < g.ymaxf &&
+                        xg >= 0.0f && yg >= 0.0f;
+    uint32_t new_key = (uint32_t)g.ne;
+    if (inside) {
+        new_key = (uint32_t)(ncj * g.Ex + nci);
+    } else {
+        nxl = xg;      // global position of a particle that left the grid
+        nyl = yg;
+    }
+    D.A[dst] = make_float4(nxl, nyl, vx, vy);
+    D.B[dst] = make_float4(m, vol, sxx, sxy);
+    D.C[dst] = make_float4(syy, c4.y + dux, c4.z + duy, Tzz);
+    D.D[dst] = make_float4(gp, gdp, d4.z, 0.0f);
+    cell_dst[dst] = (int)new_key;
+    return new_key;
+}
+
+// The G2P streams the stored particles through shared memory with bulk
+// asynchronous copies (TMA): a persistent block of 256 threads takes tiles of
+// 256 consecutive stored particles (records A-D, element, destination rank:
+// 18 KB) round-robin, keeps kG2PStages tiles in flight on one mbarrier each,
+// and one thread per particle computes from the staged copy.  The writes go
+// to the sorted position rank[i] of the other buffer (the storage stays in
+// element order from step to step).  The last, partial tile is read directly.
+// Every wait is bounded: on a timeout the kernel sets MPMG_DEV_ERR_SPIN,
+// waits (bounded) for its own copies still in flight, and returns.
+constexpr int kG2PTile = 256;
+constexpr int kG2PStages = 3;
+constexpr long long kG2PWaitLimit = 1ll << 22;
+
+struct G2PStage {
+    float4 A[kG2PTile], B[kG2PTile], C[kG2PTile], D[kG2PTile];
+    int src[kG2PTile];
+    uint32_t rank[kG2PTile];
+};
+constexpr uint32_t kG2PStageBytes = (uint32_t)sizeof(G2PStage);
+constexpr size_t kG2PSmem = sizeof(G2PStage) * kG2PStages;
+static_assert(sizeof(G2PStage) % 16 == 0, "stage arrays must stay 16-byte aligned");
+
+template <int MATERIAL>
+__global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(GeomM g, int n, MatF mp, const uint32_t *__restrict__ rank,
+                                                             Buf S, Buf D, const int *__restrict__ cell_src,
+                                                             int *__restrict__ cell_dst,
+                                                             const float4 *__restrict__ node4,
+                                                             uint32_t *__restrict__ bins, StepParams *sp, double dt,
+                                                             int gravity_mode, double gravity_const, int *status)
+{
+    extern __shared__ __align__(128) unsigned char g2p_smem[];
+    G2PStage *stage = reinterpret_cast<G2PStage *>(g2p_smem);
+    __shared__ __align__(8) uint64_t full[kG2PStages];
+    __shared__ int abort_s;
+    const int tid = threadIdx.x;
+    const int num_tiles = (n + kG2PTile - 1) / kG2PTile;
+    uint32_t inflight = 0;      // thread 0: stages with a copy outstanding
+    if (tid == 0) {
+        for (int k = 0; k < kG2PStages; k++) mpmg_mbar_init(&full[k], 1);
+        mpmg_mbar_init_fence();
+        abort_s = 0;
+    }
+    __syncthreads();
+    auto issue = [&](int tile, int k) {
+        const size_t base = (size_t)tile * kG2PTile;
+        mpmg_mbar_expect_tx(&full[k], kG2PStageBytes);
+        mpmg_bulk_g2s(stage[k].A, S.A + base, kG2PTile * 16, &full[k]);
+        mpmg_bulk_g2s(stage[k].B, S.B + base, kG2PTile * 16, &full[k]);
+        mpmg_bulk_g2s(stage[k].C, S.C + base, kG2PTile * 16, &full[k]);
+        mpmg_bulk_g2s(stage[k].D, S.D + base, kG2PTile * 16, &full[k]);
+        mpmg_bulk_g2s(stage[k].src, cell_src + base, kG2PTile * 4, &full[k]);
+        mpmg_bulk_g2s(stage[k].rank, rank + base, kG2PTile * 4, &full[k]);
+        inflight |= 1u << k;
+    };
+    if (tid == 0) {
+        for (int k = 0; k < kG2PStages; k++) {
+            const int tile = blockIdx.x + k * gridDim.x;
+            if (tile < num_tiles && (tile + 1) * kG2PTile <= n) issue(tile, k);
+        }
+    }
+    // The stored records and elements come from the previous step's G2P and
+    // the ranks from this step's P2G, two kernels back: the first copies are
+    // in flight before the wait.  The nodal values come from the grid
+    // update just before.
+    mpmg_pdl_wait();
+    if (blockIdx.x == 0 && tid == 0) {
         // Advance t and compute the next step's body force (the driver's
         // time_varying_loads, loading.c:34-54).  No kernel of this step reads
         // them after this point.
@@ -418,79 +602,60 @@ __global__ void __launch_bounds__(256, 4) mx_g2p_kernel(GeomM g, int n, MatF mp,
         else grav = -9.8;
         sp->gravity = grav;
     }
-    uint32_t new_key = (uint32_t)g.ne;
-    uint32_t dst = 0;
-    if (i < n) {
-        dst = rank[i];
-        const int e = cell_src[i];
-        const float4 a4 = S.A[i], b4 = S.B[i], c4 = S.C[i], d4 = S.D[i];
-        if (e >= g.ne) {
-            // outside the grid: carried along unchanged
-            D.A[dst] = a4;
-            D.B[dst] = b4;
-            D.C[dst] = c4;
-            D.D[dst] = d4;
-            cell_dst[dst] = g.ne;
-        } else {
-            const int ci = e % g.Ex, cj = e / g.Ex;
-            const int n0 = cj * g.Nx + ci;
-            const float ih = g.inv_hf;
-            const float xl = a4.x, yl = a4.y;
-            const float ox = 1.0f - xl, oy = 1.0f - yl;
-            const float s[4] = {ox * oy, xl * oy, xl * yl, ox * yl};
-            const float gx[4] = {-oy * ih, oy * ih, yl * ih, -yl * ih};
-            const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
-            const float4 nq[4] = {node4[n0], node4[n0 + 1], node4[n0 + 1 + g.Nx], node4[n0 + g.Nx]};
-            float xtt = 0, ytt = 0, dux = 0, duy = 0, exx = 0, eyy = 0, dxdy = 0, dydx = 0;
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-                xtt += s[a] * nq[a].x;
-                ytt += s[a] * nq[a].y;
-                dux += s[a] * nq[a].z;
-                duy += s[a] * nq[a].w;
-                exx += gx[a] * nq[a].z;
-                eyy += gy[a] * nq[a].w;
-                dxdy += gy[a] * nq[a].z;
-                dydx += gx[a] * nq[a].w;
-            }
-            const float dtf = mp.dt;
-            const float vx = a4.z + dtf * xtt, vy = a4.w + dtf * ytt;
-            dux *= dtf;
-            duy *= dtf;
-            const float exy = 0.5f * (dxdy + dydx), wxy = 0.5f * (dxdy - dydx);
-            const float m = b4.x;
-            const float vol = b4.y * expf(dtf * (exx + eyy));
-            float sxx = b4.z, sxy = b4.w, syy = c4.x, Tzz = c4.w, gp = d4.x, gdp = d4.y;
-            if (MATERIAL == MPMG_ISOLIN) {
-                isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
+    uint32_t parity = 0;        // per stage: phase to wait for
+    int k = 0;
+    for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
+        const int base = tile * kG2PTile;
+        const int i = base + tid;
+        const bool full_tile = base + kG2PTile <= n;
+        bool have = i < n;
+        float4 a4, b4, c4, d4;
+        int e = 0;
+        uint32_t dst = 0;
+        if (full_tile) {
+            if (mpmg_mbar_wait(&full[k], (parity >> k) & 1u, kG2PWaitLimit)) {
+                a4 = stage[k].A[tid];
+                b4 = stage[k].B[tid];
+                c4 = stage[k].C[tid];
+                d4 = stage[k].D[tid];
+                e = stage[k].src[tid];
+                dst = stage[k].rank[tid];
+                if (tid == 0) inflight &= ~(1u << k);
+                parity ^= 1u << k;
             } else {
-                g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
+                atomicOr(status, MPMG_DEV_ERR_SPIN);
+                abort_s = 1;
+                have = false;
             }
-
-            // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
-            float nxl = xl + dux * ih, nyl = yl + duy * ih;
-            const float fxl = floorf(nxl), fyl = floorf(nyl);
-            const int nci = ci + (int)fxl, ncj = cj + (int)fyl;
-            nxl -= fxl;
-            nyl -= fyl;
-            const float xg = ((float)nci + nxl) * g.hf, yg = ((float)ncj + nyl) * g.hf;
-            const bool inside = nci >= 0 && ncj >= 0 && nci < g.Ex && ncj < g.Ey && xg < g.xmaxf &&
-                                yg < g.ymaxf && xg >= 0.0f && yg >= 0.0f;
-            if (inside) {
-                new_key = (uint32_t)(ncj * g.Ex + nci);
-            } else {
-                nxl = xg;      // global position of a particle that left the grid
-                nyl = yg;
-            }
-            D.A[dst] = make_float4(nxl, nyl, vx, vy);
-            D.B[dst] = make_float4(m, vol, sxx, sxy);
-            D.C[dst] = make_float4(syy, c4.y + dux, c4.z + duy, Tzz);
-            D.D[dst] = make_float4(gp, gdp, d4.z, 0.0f);
-            cell_dst[dst] = (int)new_key;
+        } else if (have) {
+            a4 = S.A[i];
+            b4 = S.B[i];
+            c4 = S.C[i];
+            d4 = S.D[i];
+            e = cell_src[i];
+            dst = rank[i];
         }
+        uint32_t new_key = (uint32_t)g.ne;
+        if (have) new_key = g2p_particle<MATERIAL>(g, mp, node4, e, a4, b4, c4, d4, dst, D, cell_dst);
+        // the next step's bins, by destination position (the binning's first phase)
+        mpmg_bin_count(new_key, have, (uint32_t)g.ne, dst >> 5, bins);
+        __syncthreads();        // every thread is done with stage k
+        if (abort_s) {
+            if (tid == 0)
+                for (int q = 0; q < kG2PStages; q++)
+                    if (inflight & (1u << q)) mpmg_mbar_wait(&full[q], (parity >> q) & 1u, kG2PWaitLimit);
+            return;
+        }
+        if (tid == 0 && full_tile) {
+            const int next = tile + kG2PStages * gridDim.x;
+            if (next < num_tiles && (next + 1) * kG2PTile <= n) {
+                mpmg_fence_proxy_async();
+                issue(next, k);
+            }
+        }
+        k = (k + 1 == kG2PStages) ? 0 : k + 1;
     }
-    // the next step's bins, by destination position (the binning's first phase)
-    mpmg_bin_count(new_key, i < n, (uint32_t)g.ne, dst >> 5, bins);
+    mpmg_pdl_trigger();
 }
 
 inline int blocks_for(size_t n, int threads)
@@ -507,6 +672,8 @@ GeomM make_geom(const mpmg_ctx *ctx)
     g.Ex = ctx->Ex;
     g.Ey = ctx->Ey;
     g.ne = (int)ctx->ne;
+    g.div_Ex = mpmg_div_init((uint32_t)(ctx->Ex > 0 ? ctx->Ex : 1));
+    g.div_Nx = mpmg_div_init((uint32_t)(ctx->cfg.Nx > 0 ? ctx->cfg.Nx : 1));
     g.h = ctx->cfg.h;
     g.hf = (float)ctx->cfg.h;
     g.inv_hf = (float)ctx->inv_h;
@@ -554,6 +721,10 @@ MatF make_mat(const mpmg_ctx *ctx)
     p.grains_d = (float)c.mp[MPMG_MP_GRAINS_D];
     p.rho_critical = (float)c.mp[MPMG_MP_RHO_CRITICAL];
     if (c.material == MPMG_ISOLIN) p.lambda = (float)ctx->lambda;
+    const double rho = c.mp[MPMG_MP_GRAINS_RHO], d = c.mp[MPMG_MP_GRAINS_D];
+    p.inv_grains_rho = rho != 0.0 ? (float)(1.0 / rho) : 0.0f;
+    p.alpha_coef = d != 0.0 ? (float)(ctx->G * c.mp[MPMG_MP_I0] * c.dt / d) : 0.0f;
+    p.inv_G_dt = (ctx->G * c.dt) != 0.0 ? (float)(1.0 / (ctx->G * c.dt)) : 0.0f;
     return p;
 }
 
@@ -612,6 +783,7 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     if ((rc = dalloc(&s->cell_sums, 20 * ctx->ne)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->node4, ctx->nn)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->node_mass, ctx->nn)) != MPMG_OK) return rc;
+    if ((rc = dalloc(&s->export_buf, n)) != MPMG_OK) return rc;
     MPMG_CHECK(cudaMemset(s->node_mass, 0, ctx->nn * sizeof(float2)));
 
     // host staging: element, local coordinates, records
@@ -636,6 +808,25 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     }
     if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed state upload");
     s->cur = 0;
+    // persistent G2P grid: as many blocks as fit on the device at once, at
+    // most one per tile
+    int sms = 0, per_sm = 0;
+    MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
+    if (ctx->cfg.material == MPMG_ISOLIN) {
+        MPMG_CHECK(cudaFuncSetAttribute(mx_g2p_kernel<MPMG_ISOLIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kG2PSmem));
+        MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_g2p_kernel<MPMG_ISOLIN>, kG2PTile,
+                                                                 kG2PSmem));
+    } else {
+        MPMG_CHECK(cudaFuncSetAttribute(mx_g2p_kernel<MPMG_G_LOCAL_MU2>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG2PSmem));
+        MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_g2p_kernel<MPMG_G_LOCAL_MU2>,
+                                                                 kG2PTile, kG2PSmem));
+    }
+    const size_t tiles = (n + kG2PTile - 1) / kG2PTile;
+    size_t blocks = (size_t)(sms > 0 ? sms : 1) * (size_t)(per_sm > 0 ? per_sm : 1);
+    if (blocks > tiles) blocks = tiles;
+    s->g2p_blocks = (int)(blocks > 0 ? blocks : 1);
     // the first step's element counts; every G2P counts the next step's
     return mpmg_bin_count(ctx, (const uint32_t *)ctx->in_element);
 }
@@ -653,6 +844,7 @@ void mpmg_mixed_free(mpmg_ctx *ctx)
     cudaFree(s->cell_sums);
     cudaFree(s->node4);
     cudaFree(s->node_mass);
+    cudaFree(s->export_buf);
     delete s;
     ctx->mixed = nullptr;
 }
@@ -676,32 +868,40 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     const float dt_hi = (float)c.dt, dt_lo = (float)(c.dt - (double)dt_hi);
 
     mpmg_phase_begin(ctx, PH_SORT);
-    int rc = mpmg_bin_scan_scatter(ctx, (const uint32_t *)cell_array(ctx, cur), nullptr);
+    int rc = mpmg_bin_scan_scatter(ctx, (const uint32_t *)cell_array(ctx, cur), nullptr, true);
     if (rc != MPMG_OK) return rc;
     mpmg_phase_end(ctx, PH_SORT);
 
     Buf S = buf(s, cur), D = buf(s, nxt);
     mpmg_phase_begin(ctx, PH_P2G);
-    mx_p2g_kernel<<<blocks_for(ctx->ne, kP2GThreads), kP2GThreads, 0, st>>>(
-        g, ctx->cell_start, ctx->bin.slots, ctx->perm, ctx->bin.rank, S, ctx->d_params, s->cell_sums);
+    MPMG_CHECK(mpmg_launch_pdl(true, mx_p2g_kernel, dim3(blocks_for(ctx->ne, kP2GThreads)), dim3(kP2GThreads), 0,
+                               st, g, ctx->cell_start, ctx->bin.slots, ctx->perm, ctx->bin.rank, S, ctx->d_params,
+                               s->cell_sums));
     mpmg_phase_end(ctx, PH_P2G);
 
     mpmg_phase_begin(ctx, PH_GRID);
-    mx_grid_kernel<<<blocks_for(ctx->nn, 256), 256, 0, st>>>(
-        g, make_bc(ctx), ctx->cell_start, s->cell_sums, ctx->d_params, c.dt, dt_hi, dt_lo, (float)MPMG_TOL,
-        s->node_mass, s->node4, ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy);
+    MPMG_CHECK(mpmg_launch_pdl(true,
+                               c.precision == MPMG_PRECISION_MIXED_F64NODE ? mx_grid_kernel<true>
+                                                                           : mx_grid_kernel<false>,
+                               dim3(blocks_for(ctx->nn, 256)), dim3(256), 0, st, g, make_bc(ctx), ctx->cell_start,
+                               s->cell_sums, ctx->d_params, c.dt, dt_hi, dt_lo, (float)MPMG_TOL, s->node_mass,
+                               s->node4, ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy));
     mpmg_phase_end(ctx, PH_GRID);
 
     mpmg_phase_begin(ctx, PH_G2P);
     const MatF mp = make_mat(ctx);
     if (c.material == MPMG_ISOLIN) {
-        mx_g2p_kernel<MPMG_ISOLIN><<<blocks_for(n, 256), 256, 0, st>>>(
-            g, n, mp, ctx->bin.rank, S, D, cell_array(ctx, cur), cell_array(ctx, nxt), s->node4, ctx->bin.counts,
-            ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+        MPMG_CHECK(mpmg_launch_pdl(true, mx_g2p_kernel<MPMG_ISOLIN>, dim3(s->g2p_blocks), dim3(kG2PTile), kG2PSmem,
+                                   st, g, n, mp, (const uint32_t *)ctx->bin.rank, S, D,
+                                   (const int *)cell_array(ctx, cur), cell_array(ctx, nxt),
+                                   (const float4 *)s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode,
+                                   c.gravity, ctx->d_status));
     } else {
-        mx_g2p_kernel<MPMG_G_LOCAL_MU2><<<blocks_for(n, 256), 256, 0, st>>>(
-            g, n, mp, ctx->bin.rank, S, D, cell_array(ctx, cur), cell_array(ctx, nxt), s->node4, ctx->bin.counts,
-            ctx->d_params, c.dt, c.gravity_mode, c.gravity);
+        MPMG_CHECK(mpmg_launch_pdl(true, mx_g2p_kernel<MPMG_G_LOCAL_MU2>, dim3(s->g2p_blocks), dim3(kG2PTile),
+                                   kG2PSmem, st, g, n, mp, (const uint32_t *)ctx->bin.rank, S, D,
+                                   (const int *)cell_array(ctx, cur), cell_array(ctx, nxt),
+                                   (const float4 *)s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode,
+                                   c.gravity, ctx->d_status));
     }
     mpmg_phase_end(ctx, PH_G2P);
     ctx->launches += 3;
@@ -794,54 +994,87 @@ int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active)
     return MPMG_OK;
 }
 
-int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out)
+namespace {
+
+// One particle field of the stored records in the caller's particle order,
+// widened to FP64 (the particle index travels in D.z).  Positions are the
+// element's corner plus the local coordinate, times h, as the host
+// read-back computes them; a particle outside the grid holds its position.
+__global__ void mx_export_kernel(int n, const float4 *__restrict__ rec, int comp, const float4 *__restrict__ drec,
+                                 const int *__restrict__ cell, int xy, MpmgDiv div_Ex, int ne, double h,
+                                 double *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int pid = __float_as_int(drec[i].z);
+    const float4 r = rec[i];
+    const float v = comp == 0 ? r.x : comp == 1 ? r.y : comp == 2 ? r.z : r.w;
+    double o = (double)v;
+    if (xy != 0) {
+        const int c = cell[i];
+        if (c < ne) {
+            const int cj = (int)mpmg_div((uint32_t)c, div_Ex), ci = c - cj * (int)div_Ex.d;
+            o = ((double)(xy == 1 ? ci : cj) + (double)v) * h;
+        }
+    }
+    out[pid] = o;
+}
+
+int frame_get(mpmg_ctx *ctx, const char *name, double *out)
 {
     MixedState *s = ctx->mixed;
     const int b = s->cur;
     const size_t n = ctx->np;
-    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
-    int rc;
     if (strncmp(name, "node_", 5) == 0) {
-        int comp = -1;
-        if (strcmp(name, "node_ax") == 0) comp = 0;
-        else if (strcmp(name, "node_ay") == 0) comp = 1;
-        else if (strcmp(name, "node_vx") == 0) comp = 2;
-        else if (strcmp(name, "node_vy") == 0) comp = 3;
         if (strcmp(name, "node_m") == 0) {
             std::vector<float2> h(ctx->nn);
             MPMG_CHECK(cudaMemcpy(h.data(), s->node_mass, ctx->nn * sizeof(float2), cudaMemcpyDeviceToHost));
             for (size_t k = 0; k < ctx->nn; k++) out[k] = (double)h[k].x + (double)h[k].y;
             return MPMG_OK;
         }
+        int comp = -1;
+        if (strcmp(name, "node_ax") == 0) comp = 0;
+        else if (strcmp(name, "node_ay") == 0) comp = 1;
+        else if (strcmp(name, "node_vx") == 0) comp = 2;
+        else if (strcmp(name, "node_vy") == 0) comp = 3;
         if (comp < 0) return MPMG_ERR_UNKNOWN_FIELD;   // FP64 node arrays: the common path
         std::vector<float4> h(ctx->nn);
         MPMG_CHECK(cudaMemcpy(h.data(), s->node4, ctx->nn * sizeof(float4), cudaMemcpyDeviceToHost));
         for (size_t k = 0; k < ctx->nn; k++) out[k] = get_comp(h[k], comp);
         return MPMG_OK;
     }
-    std::vector<int> pid, cell;
-    if ((rc = pids(ctx, pid)) != MPMG_OK) return rc;
-    if (strcmp(name, "x") == 0 || strcmp(name, "y") == 0) {
-        const bool isx = name[0] == 'x';
-        std::vector<float4> a;
-        if ((rc = download_i(ctx, cell_array(ctx, b), cell)) != MPMG_OK) return rc;
-        if ((rc = download4(ctx, s->A[b], a)) != MPMG_OK) return rc;
-        for (size_t k = 0; k < n; k++) {
-            const double local = isx ? a[k].x : a[k].y;
-            if (cell[k] < (int)ctx->ne) {
-                int c = isx ? cell[k] % ctx->Ex : cell[k] / ctx->Ex;
-                out[pid[k]] = ((double)c + local) * ctx->cfg.h;
-            } else {
-                out[pid[k]] = local;
-            }
-        }
-        return MPMG_OK;
+    int rec = 0, comp = 0, xy = 0;
+    if (strcmp(name, "x") == 0) xy = 1;
+    else if (strcmp(name, "y") == 0) { xy = 2; comp = 1; }
+    else if (!field_slot(name, &rec, &comp)) return MPMG_ERR_UNKNOWN_FIELD;
+    if (n == 0) return MPMG_OK;
+    mx_export_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(
+        (int)n, record(s, b, rec), comp, s->D[b], cell_array(ctx, b), xy,
+        mpmg_div_init((uint32_t)(ctx->Ex > 0 ? ctx->Ex : 1)), (int)ctx->ne, ctx->cfg.h, s->export_buf);
+    ctx->launches += 1;
+    MPMG_CHECK(cudaGetLastError());
+    MPMG_CHECK(cudaMemcpyAsync(out, s->export_buf, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    return MPMG_OK;
+}
+
+}  // namespace
+
+int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out)
+{
+    return frame_get(ctx, name, out);
+}
+
+// Several fields; done[k] is set for every field read here (the others are
+// not held by the mixed state).
+int mpmg_mixed_get_many(mpmg_ctx *ctx, int count, const char *const *names, double *const *out, bool *done)
+{
+    for (int k = 0; k < count; k++) {
+        done[k] = false;
+        const int rc = frame_get(ctx, names[k], out[k]);
+        if (rc == MPMG_OK) done[k] = true;
+        else if (rc != MPMG_ERR_UNKNOWN_FIELD) return rc;
     }
-    int rec, comp;
-    if (!field_slot(name, &rec, &comp)) return MPMG_ERR_UNKNOWN_FIELD;
-    std::vector<float4> a;
-    if ((rc = download4(ctx, record(s, b, rec), a)) != MPMG_OK) return rc;
-    for (size_t k = 0; k < n; k++) out[pid[k]] = (double)get_comp(a[k], comp);
     return MPMG_OK;
 }
 

@@ -75,6 +75,7 @@ def lib(build_if_missing=True):
         L.mpmg_synchronize.argtypes = [vp]
         L.mpmg_get_field.argtypes = [vp, C.c_char_p, dp]
         L.mpmg_set_field.argtypes = [vp, C.c_char_p, dp]
+        L.mpmg_get_fields.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), C.POINTER(dp)]
         L.mpmg_get_map.argtypes = [vp, ip, ip]
         L.mpmg_set_map.argtypes = [vp, ip, ip]
         L.mpmg_get_sort.argtypes = [vp, ip, ip, ip]
@@ -118,7 +119,7 @@ def default_params(material):
     return mp
 
 
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_f64node": 2}
 
 
 def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0,
@@ -192,6 +193,22 @@ class Simulation:
         out = np.empty(n)
         _check(lib().mpmg_get_field(self._h, name.encode(), _dptr(out)))
         return out
+
+    def get_frame(self, names, out=None):
+        """Several fields in one read-back (mpmg_get_fields): a dict name -> array.
+        `out` may map names to preallocated float64 arrays (e.g. pinned host
+        buffers) to fill instead."""
+        names = list(names)
+        arrays = {}
+        for nm in names:
+            if out is not None and nm in out:
+                arrays[nm] = out[nm]
+            else:
+                arrays[nm] = np.empty(self.nn if nm.startswith("node_") else self.n)
+        cnames = (C.c_char_p * len(names))(*[nm.encode() for nm in names])
+        ptrs = (C.POINTER(C.c_double) * len(names))(*[_dptr(arrays[nm]) for nm in names])
+        _check(lib().mpmg_get_fields(self._h, len(names), cnames, ptrs))
+        return arrays
 
     def set(self, name, values):
         a = np.ascontiguousarray(values, dtype=np.float64)

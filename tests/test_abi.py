@@ -74,3 +74,15 @@ def test_invalid_configuration_is_rejected():
     with pytest.raises(mpm2d.MpmError) as e:
         mpm2d.Simulation(sc)
     assert e.value.status == 16
+    cfg = mpm2d.make_config(scenes.config1())
+    cfg.precision = 7                      # not an mpmg_precision
+    h = mpm2d.C.c_void_p()
+    z = mpm2d.np.zeros(1)
+    rc = mpm2d.lib().mpmg_create(mpm2d.C.byref(cfg), 1, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h))
+    assert rc == 16 and not h.value
+
+
+def test_frame_read_entry_point_is_exported():
+    L = mpm2d.lib()
+    assert hasattr(L, "mpmg_get_fields")
+    assert mpm2d.PRECISIONS == {"fp64": 0, "mixed": 1, "mixed_f64node": 2}

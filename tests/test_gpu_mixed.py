@@ -1,6 +1,7 @@
-"""The mixed-precision form (FP32 particle state, shape functions, P2G/G2P
-and material; FP64 nodal mass and momentum sums and division by nodal mass)
-against the FP64 form and the oracle.
+"""The mixed-precision forms (FP32 particle state, shape functions, P2G/G2P
+and material; nodal mass and momentum sums and the division by nodal mass in
+float-float, or in FP64 for mixed_f64node) against the FP64 form and the
+oracle.
 
 Criteria (the mixed form's contract):
   * relative L2 error per field, ||a - b|| / ||b||, after 100 steps <= 1e-4;
@@ -42,10 +43,11 @@ def column_scene():
                          rho=2450.0, props=(1e6, 0.3), dt=1e-5, mp={"grains_d": 5.3e-4}, jitter=1e-3, seed=4)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_f64node"])
 @pytest.mark.parametrize("which", ["isolin_block", "mu2_column"])
-def test_mixed_vs_fp64_after_100_steps(which):
+def test_mixed_vs_fp64_after_100_steps(which, precision):
     sc = scenes.config1(seed=3) if which == "isolin_block" else column_scene()
-    mixed = mpm2d.Simulation(sc, precision="mixed")
+    mixed = mpm2d.Simulation(sc, precision=precision)
     fp64 = mpm2d.Simulation(sc, precision="fp64")
     mixed.step(100)
     fp64.step(100)
@@ -57,6 +59,34 @@ def test_mixed_vs_fp64_after_100_steps(which):
     eb, ab = fp64.get_map()
     assert np.array_equal(aa, ab)
     assert np.mean(ea == eb) > 0.999
+
+
+def test_mixed_node_forms_agree():
+    # float-float and FP64 nodal sums: the same FP32 particle arithmetic,
+    # differing only in the last bits of the nodal velocities
+    sc = column_scene()
+    a = mpm2d.Simulation(sc, precision="mixed")
+    b = mpm2d.Simulation(sc, precision="mixed_f64node")
+    a.step(1)
+    b.step(1)
+    # the first step's nodal masses come from identical FP32 corner sums: the
+    # float-float sum is exact to ~2^-48, the FP64 sum of four FP32 values exact
+    np.testing.assert_allclose(a.get("node_m"), b.get("node_m"), rtol=1e-13, atol=0)
+    a.step(99)
+    b.step(99)
+    for f in FIELDS:
+        assert group_rel_l2(a.get, b.get, f) <= 2e-5, f
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_frame_read_matches_single_reads(precision):
+    sc = column_scene()
+    sim = mpm2d.Simulation(sc, precision=precision)
+    sim.step(20)
+    names = ("m", "v", "x", "y", "vx", "vy", "sxx", "sxy", "syy", "ux", "uy", "state9", "state10", "node_m")
+    frame = sim.get_frame(names)
+    for nm in names:
+        np.testing.assert_array_equal(frame[nm], sim.get(nm), err_msg=nm)
 
 
 def test_mixed_vs_oracle_isolin():
@@ -130,6 +160,9 @@ def test_mixed_full_size_invariants():
     sim.step(5)
     keys, perm, start = sim.get_sort()
     assert np.all(np.diff(keys) >= 0)
+    ne = 512 * 512
+    inside = keys[keys < ne]
+    np.testing.assert_array_equal(start, np.searchsorted(inside, np.arange(ne + 1), side="left"))
     assert np.array_equal(np.bincount(perm, minlength=len(perm)), np.ones(len(perm), dtype=np.int64))
     e, a = sim.get_map()
     m_nodes = sim.get("node_m").sum()
