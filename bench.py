@@ -80,6 +80,13 @@ FP64_BYTES = {
 }
 
 
+# DRAM bytes (read + write) of one mx_g2p_kernel launch on this workload from
+# one ncu capture (profiles/ncu_mixed_step_box_fill_1M_g_local_mu2.md):
+# 80.8 MB read + 18.1 MB written; writes still in L2 at the kernel's end are
+# not in the figure.
+G2P_TRAFFIC_BYTES = 98.9e6
+
+
 def phase_bytes(table, phase, n, ne, nn):
     a, b, c = table.get(phase, (0, 0, 0))
     return a * n + b * ne + c * nn
@@ -353,7 +360,8 @@ def run_gpu(args):
         "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": {"bound": "hbm", "kernel": "g2p", "achieved": g2p["gbs"], "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": g2p["gbs"] / peak, "traffic": None,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": g2p["gbs"] / peak,
+                     "traffic": G2P_TRAFFIC_BYTES if n == 1048576 else None,
                      "top_phase": top[0],
                      "step_alg_bytes": step_bytes,
                      "step_achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9,
