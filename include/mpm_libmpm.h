@@ -11,7 +11,7 @@
  * 152 bytes), element_t (libmpm/element.h:29-67, 1504 bytes), job_t
  * (libmpm/process.h:116-213, 800 bytes) and threadtask_t
  * (libmpm/process.h:215-249, 96 bytes) on LP64.  The sizes are checked at
- * compile time in csrc/mpmg_libmpm.cpp.
+ * compile time in csrc/mpmg_libmpm.cu.
  *
  * Entry points (reference declarations they replace):
  *   mpm_init                          libmpm/process_usl.c:68   (process.h:251)
