@@ -256,6 +256,7 @@ def run_gpu(args):
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
     import mpm2d
+    import scenes
 
     scene = make_scene()
     n = len(scene["particles"]["x"])
@@ -321,6 +322,39 @@ def run_gpu(args):
     valuef = n * args.steps * world / max_over_ranks(msf / 1e3)
     simf.close()
 
+    # --- batched ensemble: 256 independent silo / heap runs in one context ------
+    batch_line = None
+    if not args.no_batch:
+        ens = scenes.ensemble(count=256, seed=1)
+        nb = sum(len(sc["particles"]["x"]) for sc in ens)
+        bsim = mpm2d.Batch(ens)
+        bstream = torch.cuda.ExternalStream(bsim.stream(), device=dev)
+        bsim.step(args.warmup)
+        bsim.synchronize()
+        bsteps = max(3, min(args.steps, 20))
+        barrier()
+        msb = time_steps(bsim, bsteps, bstream, torch)
+        barrier()
+        bsim.close()
+        value_b = nb * bsteps * world / max_over_ranks(msb / 1e3)
+        # the same members one at a time (each its own context and step graphs)
+        seq_ms = 0.0
+        for sc in ens:
+            one = mpm2d.Simulation(sc, device=dev, precision="mixed")
+            ostream = torch.cuda.ExternalStream(one.stream(), device=dev)
+            one.step(3)
+            one.synchronize()
+            seq_ms += time_steps(one, 5, ostream, torch) / 5
+            one.close()
+        value_seq = nb / (seq_ms / 1e3)
+        batch_line = {"value": value_b, "unit": UNIT, "members": len(ens), "particles": nb,
+                      "elements": int(sum((sc["Nx"] - 1) * (sc["Ny"] - 1) for sc in ens)),
+                      "steps": bsteps, "ms_per_step": msb / bsteps,
+                      "sequential_value": value_seq, "batch_over_sequential": value_b / value_seq,
+                      "workload": "ensemble of 256 g_local_mu2 runs (silo / heap), grids 64^2-384^2 "
+                                  "elements, 5k-200k particles log-uniform, outlet 0.02-0.12, mu_s 0.30-0.45 "
+                                  "(seed 1), mixed precision"}
+
     # --- end to end through the C ABI with host buffers (mixed) ---------------
     # The user's run: create the simulation from host arrays (H2D of the
     # particle state), step, read each step's result back (mpmg_get_time:
@@ -371,6 +405,7 @@ def run_gpu(args):
                  "dtype": "f64", "phases": phases64,
                  "bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s)"},
         "mixed_over_fp64": value / value64,
+        "batch": batch_line,
         "mixed_f64node": {"value": valuef, "unit": UNIT, "steps": args.steps, "ms_per_step": msf / args.steps,
                           "note": "same mixed step with FP64 nodal mass/momentum sums and division"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
@@ -401,6 +436,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=60)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--e2e-steps", type=int, default=500,
                     help="steps of the end-to-end run (one output frame at its end)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

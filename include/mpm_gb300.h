@@ -172,6 +172,29 @@ MPMG_API int mpmg_get_time(mpmg_ctx *ctx, double *t, int *step_number);
 MPMG_API int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number);
 MPMG_API int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *num_elements);
 
+/* Batched ensembles (no counterpart in the reference, which runs one job per
+   process: its plugins keep static state).  count independent simulations
+   in one context, each with its own configuration: grid size and spacing,
+   material parameters (mu_s, ...), boundary conditions (box or square silo,
+   e.g. an outlet-width sweep), time step and gravity.  The members share the
+   precision (a mixed form), the material kind (isolin or g_local_mu2) and the
+   device.  Member k's counts[k] particles follow member k-1's in the
+   particle arrays.  mpmg_step advances every member by nsteps of its own
+   dt, all members in the same kernel launches (one CUDA graph per step or
+   chunk of steps).  Particle and node fields read back concatenated in
+   member order (mpmg_batch_member gives each member's offsets and sizes);
+   mpmg_get_map reports elements local to each member; mpmg_get_time and
+   mpmg_set_time act on member 0 and on all members. */
+MPMG_API int mpmg_batch_create(int count, const mpmg_config *cfgs, const size_t *counts, const double *m,
+                               const double *v, const double *x, const double *y, const double *vx,
+                               const double *vy, const double *sxx, const double *sxy, const double *syy,
+                               mpmg_ctx **out);
+MPMG_API int mpmg_batch_count(mpmg_ctx *ctx, int *count);
+MPMG_API int mpmg_batch_member(mpmg_ctx *ctx, int member, size_t *first_particle, size_t *num_particles,
+                               size_t *first_node, size_t *num_nodes, size_t *first_element,
+                               size_t *num_elements);
+MPMG_API int mpmg_batch_get_time(mpmg_ctx *ctx, int member, double *t, int *step_number);
+
 /* Runs only the material update on every active particle from the current
    strain rates (the per-particle path of the reference's tests/test_material.c).
    Local materials only. */

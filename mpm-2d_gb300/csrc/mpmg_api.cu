@@ -57,22 +57,26 @@ bool material_uses_state(int material, int k)
     }
 }
 
-// The step record (StepParams, then the status word) lives in one device
-// block with a pinned host mirror, so a read-back of both is one copy.
-constexpr size_t kStatusOffset = (sizeof(StepParams) + 15) / 16 * 16;
-constexpr size_t kStepRecordBytes = kStatusOffset + 16;
-
-int alloc_step_record(mpmg_ctx *ctx)
+// The step records (one StepParams per simulation, then the status word)
+// live in one device block with a pinned host mirror, so a read-back of all
+// of them is one copy.
+size_t step_record_bytes(const mpmg_ctx *ctx)
 {
+    return ctx->status_offset + 16;
+}
+
+int alloc_step_record(mpmg_ctx *ctx, int count)
+{
+    ctx->status_offset = ((size_t)count * sizeof(StepParams) + 15) / 16 * 16;
     unsigned char *block = nullptr;
-    cudaError_t e = cudaMalloc((void **)&block, kStepRecordBytes);
+    cudaError_t e = cudaMalloc((void **)&block, step_record_bytes(ctx));
     if (e != cudaSuccess) {
         mpmg_set_error("cudaMalloc of the step record failed: %s", cudaGetErrorString(e));
         return MPMG_ERR_NOMEM;
     }
     ctx->d_params = (StepParams *)block;
-    ctx->d_status = (int *)(block + kStatusOffset);
-    e = cudaHostAlloc((void **)&ctx->h_record, kStepRecordBytes, cudaHostAllocDefault);
+    ctx->d_status = (int *)(block + ctx->status_offset);
+    e = cudaHostAlloc((void **)&ctx->h_record, step_record_bytes(ctx), cudaHostAllocDefault);
     if (e != cudaSuccess) {
         ctx->h_record = nullptr;
         mpmg_set_error("cudaHostAlloc of the step record failed: %s", cudaGetErrorString(e));
@@ -83,12 +87,12 @@ int alloc_step_record(mpmg_ctx *ctx)
 
 int sync_status(mpmg_ctx *ctx)
 {
-    MPMG_CHECK(cudaMemcpyAsync(ctx->h_record, ctx->d_params, kStepRecordBytes, cudaMemcpyDeviceToHost,
+    MPMG_CHECK(cudaMemcpyAsync(ctx->h_record, ctx->d_params, step_record_bytes(ctx), cudaMemcpyDeviceToHost,
                                ctx->stream));
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
     int st = 0;
     memcpy(&ctx->h_params, ctx->h_record, sizeof(StepParams));
-    memcpy(&st, ctx->h_record + kStatusOffset, sizeof(int));
+    memcpy(&st, ctx->h_record + ctx->status_offset, sizeof(int));
     if (st != 0) {
         // Report each device-side error once; the caller decides whether to go on.
         MPMG_CHECK(cudaMemset(ctx->d_status, 0, sizeof(int)));
@@ -329,6 +333,13 @@ int mpmg_destroy(mpmg_ctx *ctx)
     mpmg_bin_free(ctx);
     mpmg_nonlocal_free(ctx);
     mpmg_mixed_free(ctx);
+    if (ctx->batch) {
+        cudaFree(ctx->batch->d_members);
+        cudaFree(ctx->batch->d_elem_off);
+        cudaFree(ctx->batch->d_node_off);
+        delete ctx->batch;
+        ctx->batch = nullptr;
+    }
     for (int p = 0; p < 2; p++) {
         if (ctx->graph_chunk[p]) cudaGraphExecDestroy(ctx->graph_chunk[p]);
         if (ctx->graph_single[p]) cudaGraphExecDestroy(ctx->graph_single[p]);
@@ -340,15 +351,12 @@ int mpmg_destroy(mpmg_ctx *ctx)
     return MPMG_OK;
 }
 
-int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double *v, const double *x,
-                const double *y, const double *vx, const double *vy, const double *sxx,
-                const double *sxy, const double *syy, mpmg_ctx **out)
+namespace {
+
+// Checks one simulation's configuration (mpm_init's and the plugins'
+// bc_validate checks); n is its particle count.
+int validate_config(const mpmg_config *cfg, size_t n)
 {
-    if (out == nullptr || cfg == nullptr) {
-        mpmg_set_error("null configuration or output pointer");
-        return MPMG_ERR_INVALID;
-    }
-    *out = nullptr;
     if (cfg->Nx < 2 || cfg->Ny < 2 || !(cfg->h > 0) || !(cfg->dt > 0) || !(cfg->xmax > 0) ||
         !(cfg->ymax > 0)) {
         mpmg_set_error("grid needs Nx, Ny >= 2 and positive h, dt, xmax, ymax");
@@ -370,10 +378,6 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
         mpmg_set_error("unknown precision %d", cfg->precision);
         return MPMG_ERR_INVALID;
     }
-    if (n > 0 && (!m || !v || !x || !y || !vx || !vy || !sxx || !sxy || !syy)) {
-        mpmg_set_error("null particle array");
-        return MPMG_ERR_INVALID;
-    }
     if (cfg->bc == MPMG_BOX) {
         // box.c:42-96 bc_validate
         double x0 = cfg->bcf[0], y0 = cfg->bcf[1], w = cfg->bcf[2], hh = cfg->bcf[3];
@@ -382,13 +386,77 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             return MPMG_ERR_INVALID;
         }
     }
+    return MPMG_OK;
+}
+
+int check_device(int device)
+{
     int ndev = 0;
     cudaError_t de = cudaGetDeviceCount(&ndev);
-    if (de != cudaSuccess || ndev <= cfg->device || cfg->device < 0) {
-        mpmg_set_error("no CUDA device %d available (%s)", cfg->device,
+    if (de != cudaSuccess || ndev <= device || device < 0) {
+        mpmg_set_error("no CUDA device %d available (%s)", device,
                        de != cudaSuccess ? cudaGetErrorString(de) : "device count too small");
         return MPMG_ERR_CUDA;
     }
+    return MPMG_OK;
+}
+
+}  // namespace
+
+// Device state of the mixed form (one simulation or a batch): FP32 particle
+// state lives in ctx->mixed; the context keeps the sort, the step records
+// (one per simulation) and the status word.
+static int init_mixed_context(mpmg_ctx *ctx, const double *m, const double *v, const double *x, const double *y,
+                       const double *vx, const double *vy, const double *sxx, const double *sxy,
+                       const double *syy)
+{
+    const size_t n = ctx->np;
+    const int count = ctx->batch ? ctx->batch->count : 1;
+    int rc;
+    if ((rc = dalloc(&ctx->in_element, n)) != MPMG_OK) return rc;
+    if ((rc = dalloc(&ctx->active, n)) != MPMG_OK) return rc;
+    if ((rc = dalloc(&ctx->sorted_keys, n)) != MPMG_OK) return rc;
+    if ((rc = dalloc(&ctx->perm, n)) != MPMG_OK) return rc;
+    if ((rc = dalloc(&ctx->cell_start, ctx->ne + 1)) != MPMG_OK) return rc;
+    if (ctx->cfg.store_transients) {
+        double **tn[] = {&ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy};
+        for (double **p : tn)
+            if ((rc = dalloc(p, ctx->nn)) != MPMG_OK) return rc;
+    }
+    if ((rc = alloc_step_record(ctx, count)) != MPMG_OK) return rc;
+    if ((rc = mpmg_bin_init(ctx)) != MPMG_OK) return rc;
+    if ((rc = fill_zero(ctx, ctx->cell_start, (ctx->ne + 1) * sizeof(int))) != MPMG_OK) return rc;
+    if ((rc = fill_zero(ctx, ctx->d_status, sizeof(int))) != MPMG_OK) return rc;
+    std::vector<StepParams> p0(count);
+    for (int k = 0; k < count; k++) {
+        const mpmg_config &c = ctx->batch ? ctx->batch->cfg[k] : ctx->cfg;
+        p0[k] = StepParams{};
+        p0[k].gravity = (c.gravity_mode == MPMG_GRAVITY_CONSTANT) ? c.gravity : 0.0;
+    }
+    ctx->h_params = p0[0];
+    MPMG_CHECK(cudaMemcpyAsync(ctx->d_params, p0.data(), count * sizeof(StepParams), cudaMemcpyHostToDevice,
+                               ctx->stream));
+    if ((rc = mpmg_mixed_init(ctx, m, v, x, y, vx, vy, sxx, sxy, syy)) != MPMG_OK) return rc;
+    return sync_status(ctx);
+}
+
+int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double *v, const double *x,
+                const double *y, const double *vx, const double *vy, const double *sxx,
+                const double *sxy, const double *syy, mpmg_ctx **out)
+{
+    if (out == nullptr || cfg == nullptr) {
+        mpmg_set_error("null configuration or output pointer");
+        return MPMG_ERR_INVALID;
+    }
+    *out = nullptr;
+    int vrc = validate_config(cfg, n);
+    if (vrc != MPMG_OK) return vrc;
+    if (n > 0 && (!m || !v || !x || !y || !vx || !vy || !sxx || !sxy || !syy)) {
+        mpmg_set_error("null particle array");
+        return MPMG_ERR_INVALID;
+    }
+    vrc = check_device(cfg->device);
+    if (vrc != MPMG_OK) return vrc;
 
     mpmg_ctx *ctx = new (std::nothrow) mpmg_ctx();
     if (ctx == nullptr) return MPMG_ERR_NOMEM;
@@ -441,31 +509,7 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             goto fail;
         }
         if (mixed) {
-            // FP32 particle state lives in ctx->mixed; the context keeps the
-            // sort, the FP64 nodal mass and the step parameters.
-            TRY(dalloc(&ctx->in_element, n));
-            TRY(dalloc(&ctx->active, n));
-            TRY(dalloc(&ctx->sorted_keys, n));
-            TRY(dalloc(&ctx->perm, n));
-            TRY(dalloc(&ctx->cell_start, ctx->ne + 1));
-            TRY(dalloc(&ctx->node_m, ctx->nn));
-            if (transients) {
-                double **tn[] = {&ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy};
-                for (double **p : tn) TRY(dalloc(p, ctx->nn));
-            }
-            TRY(alloc_step_record(ctx));
-            TRY(mpmg_bin_init(ctx));
-            TRY(fill_zero(ctx, ctx->cell_start, (ctx->ne + 1) * sizeof(int)));
-            TRY(fill_zero(ctx, ctx->node_m, ctx->nn * sizeof(double)));
-            TRY(fill_zero(ctx, ctx->d_status, sizeof(int)));
-            StepParams p0 = {};
-            p0.gravity = (cfg->gravity_mode == MPMG_GRAVITY_CONSTANT) ? cfg->gravity : 0.0;
-            ctx->h_params = p0;
-            MPMG_CHECK(cudaMemcpyAsync(ctx->d_params, &ctx->h_params, sizeof(StepParams),
-                                       cudaMemcpyHostToDevice, ctx->stream));
-            TRY(mpmg_mixed_init(ctx, m, v, x, y, vx, vy, sxx, sxy, syy));
-            rc = sync_status(ctx);
-            if (rc != MPMG_OK) goto fail;
+            TRY(init_mixed_context(ctx, m, v, x, y, vx, vy, sxx, sxy, syy));
             *out = ctx;
             return MPMG_OK;
         }
@@ -501,7 +545,7 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             double **tn[] = {&ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy};
             for (double **p : tn) TRY(dalloc(p, ctx->nn));
         }
-        TRY(alloc_step_record(ctx));
+        TRY(alloc_step_record(ctx, 1));
         TRY(mpmg_bin_init(ctx));
         if (nonlocal) TRY(mpmg_nonlocal_init(ctx));
 
@@ -568,6 +612,156 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
 fail:
     mpmg_destroy(ctx);
     return rc;
+}
+
+int mpmg_batch_create(int count, const mpmg_config *cfgs, const size_t *counts, const double *m,
+                      const double *v, const double *x, const double *y, const double *vx, const double *vy,
+                      const double *sxx, const double *sxy, const double *syy, mpmg_ctx **out)
+{
+    if (out == nullptr || cfgs == nullptr || counts == nullptr || count < 1) {
+        mpmg_set_error("batch needs at least one configuration, the particle counts and an output pointer");
+        return MPMG_ERR_INVALID;
+    }
+    *out = nullptr;
+    size_t np = 0, ne = 0, nn = 0;
+    for (int k = 0; k < count; k++) {
+        const mpmg_config &c = cfgs[k];
+        int vrc = validate_config(&c, counts[k]);
+        if (vrc != MPMG_OK) return vrc;
+        if (c.precision != MPMG_PRECISION_MIXED && c.precision != MPMG_PRECISION_MIXED_F64NODE) {
+            mpmg_set_error("batch member %d: batches run the mixed-precision form", k);
+            return MPMG_ERR_UNSUPPORTED;
+        }
+        if (c.material != MPMG_ISOLIN && c.material != MPMG_G_LOCAL_MU2) {
+            mpmg_set_error("batch member %d: mixed precision supports isolin and g_local_mu2", k);
+            return MPMG_ERR_UNSUPPORTED;
+        }
+        if (c.precision != cfgs[0].precision || c.material != cfgs[0].material || c.device != cfgs[0].device ||
+            c.store_transients != cfgs[0].store_transients) {
+            mpmg_set_error("batch member %d: members share the precision, material kind, device and "
+                           "transient storage; their grids, parameters, boundaries and time steps may differ",
+                           k);
+            return MPMG_ERR_INVALID;
+        }
+        np += counts[k];
+        ne += (size_t)(c.Nx - 1) * (size_t)(c.Ny - 1);
+        nn += (size_t)c.Nx * (size_t)c.Ny;
+    }
+    if (np >= 2147483647u || ne >= 2147483647u || nn >= 2147483647u) {
+        mpmg_set_error("batch totals exceed 32-bit indexing");
+        return MPMG_ERR_INVALID;
+    }
+    if (np > 0 && (!m || !v || !x || !y || !vx || !vy || !sxx || !sxy || !syy)) {
+        mpmg_set_error("null particle array");
+        return MPMG_ERR_INVALID;
+    }
+    int rc = check_device(cfgs[0].device);
+    if (rc != MPMG_OK) return rc;
+
+    mpmg_ctx *ctx = new (std::nothrow) mpmg_ctx();
+    if (ctx == nullptr) return MPMG_ERR_NOMEM;
+    ctx->cfg = cfgs[0];
+    ctx->dev = cfgs[0].device;
+    ctx->np = np;
+    ctx->ne = ne;
+    ctx->nn = nn;
+    ctx->Ex = cfgs[0].Nx - 1;
+    ctx->Ey = cfgs[0].Ny - 1;
+    ctx->inv_h = 1.0 / cfgs[0].h;
+    int bits = 1;
+    while (((size_t)1 << bits) <= ctx->ne) bits++;
+    ctx->key_bits = bits;
+    {
+        const double E = cfgs[0].mp[MPMG_MP_E], nu = cfgs[0].mp[MPMG_MP_NU];
+        ctx->G = E / (2.0 * (1.0 + nu));
+        ctx->K = E / (3.0 * (1.0 - 2 * nu));
+        ctx->lambda = ctx->K - 2.0 * ctx->G / 3.0;
+    }
+    BatchInfo *b = new (std::nothrow) BatchInfo();
+    if (b == nullptr) {
+        delete ctx;
+        return MPMG_ERR_NOMEM;
+    }
+    ctx->batch = b;
+    b->count = count;
+    b->cfg.assign(cfgs, cfgs + count);
+    b->poff.assign(count + 1, 0);
+    b->eoff.assign(count + 1, 0);
+    b->noff.assign(count + 1, 0);
+    for (int k = 0; k < count; k++) {
+        b->poff[k + 1] = b->poff[k] + counts[k];
+        b->eoff[k + 1] = b->eoff[k] + (size_t)(cfgs[k].Nx - 1) * (size_t)(cfgs[k].Ny - 1);
+        b->noff[k + 1] = b->noff[k] + (size_t)cfgs[k].Nx * (size_t)cfgs[k].Ny;
+    }
+    if (cudaSetDevice(ctx->dev) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        mpmg_set_error("cannot open CUDA device %d", ctx->dev);
+        rc = MPMG_ERR_CUDA;
+        goto fail;
+    }
+    for (int k = 0; k < 2 * PH_COUNT; k++) {
+        if (cudaEventCreate(&ctx->ev[k]) != cudaSuccess) {
+            rc = MPMG_ERR_CUDA;
+            goto fail;
+        }
+    }
+    rc = init_mixed_context(ctx, m, v, x, y, vx, vy, sxx, sxy, syy);
+    if (rc != MPMG_OK) goto fail;
+    *out = ctx;
+    return MPMG_OK;
+fail:
+    mpmg_destroy(ctx);
+    return rc;
+}
+
+int mpmg_batch_count(mpmg_ctx *ctx, int *count)
+{
+    if (ctx == nullptr || count == nullptr) return MPMG_ERR_INVALID;
+    *count = ctx->batch ? ctx->batch->count : 1;
+    return MPMG_OK;
+}
+
+int mpmg_batch_member(mpmg_ctx *ctx, int member, size_t *first_particle, size_t *num_particles,
+                      size_t *first_node, size_t *num_nodes, size_t *first_element, size_t *num_elements)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    const int count = ctx->batch ? ctx->batch->count : 1;
+    if (member < 0 || member >= count) {
+        mpmg_set_error("member %d outside a batch of %d", member, count);
+        return MPMG_ERR_INVALID;
+    }
+    size_t p0 = 0, p1 = ctx->np, n0 = 0, n1 = ctx->nn, e0 = 0, e1 = ctx->ne;
+    if (ctx->batch) {
+        const BatchInfo &b = *ctx->batch;
+        p0 = b.poff[member], p1 = b.poff[member + 1];
+        n0 = b.noff[member], n1 = b.noff[member + 1];
+        e0 = b.eoff[member], e1 = b.eoff[member + 1];
+    }
+    if (first_particle) *first_particle = p0;
+    if (num_particles) *num_particles = p1 - p0;
+    if (first_node) *first_node = n0;
+    if (num_nodes) *num_nodes = n1 - n0;
+    if (first_element) *first_element = e0;
+    if (num_elements) *num_elements = e1 - e0;
+    return MPMG_OK;
+}
+
+int mpmg_batch_get_time(mpmg_ctx *ctx, int member, double *t, int *step_number)
+{
+    if (ctx == nullptr) return MPMG_ERR_INVALID;
+    const int count = ctx->batch ? ctx->batch->count : 1;
+    if (member < 0 || member >= count) {
+        mpmg_set_error("member %d outside a batch of %d", member, count);
+        return MPMG_ERR_INVALID;
+    }
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    int rc = sync_status(ctx);
+    if (rc != MPMG_OK && rc != MPMG_ERR_SOLVER) return rc;
+    StepParams p;
+    memcpy(&p, ctx->h_record + (size_t)member * sizeof(StepParams), sizeof(StepParams));
+    if (t) *t = p.t;
+    if (step_number) *step_number = (int)p.step_count;
+    return MPMG_OK;
 }
 
 }  // extern "C"
@@ -828,16 +1022,21 @@ int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number)
     if (ctx == nullptr || step_number < 0) return MPMG_ERR_INVALID;
     MPMG_CHECK(cudaSetDevice(ctx->dev));
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
-    MPMG_CHECK(cudaMemcpy(&ctx->h_params, ctx->d_params, sizeof(StepParams), cudaMemcpyDeviceToHost));
-    ctx->h_params.t = t;
-    ctx->h_params.step_count = step_number;
-    // body force the next step uses (the FP64 form recomputes it on the device)
-    if (ctx->cfg.gravity_mode == MPMG_GRAVITY_CONSTANT) ctx->h_params.gravity = ctx->cfg.gravity;
-    else if (step_number == 0) ctx->h_params.gravity = 0.0;
-    else if ((0.1 + ctx->h_params.step_start_time) > t)
-        ctx->h_params.gravity = -9.8 * ((t - ctx->h_params.step_start_time) / 0.1);
-    else ctx->h_params.gravity = -9.8;
-    MPMG_CHECK(cudaMemcpy(ctx->d_params, &ctx->h_params, sizeof(StepParams), cudaMemcpyHostToDevice));
+    const int count = ctx->batch ? ctx->batch->count : 1;
+    std::vector<StepParams> p(count);
+    MPMG_CHECK(cudaMemcpy(p.data(), ctx->d_params, count * sizeof(StepParams), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < count; k++) {
+        const mpmg_config &c = ctx->batch ? ctx->batch->cfg[k] : ctx->cfg;
+        p[k].t = t;
+        p[k].step_count = step_number;
+        // body force the next step uses (the FP64 form recomputes it on the device)
+        if (c.gravity_mode == MPMG_GRAVITY_CONSTANT) p[k].gravity = c.gravity;
+        else if (step_number == 0) p[k].gravity = 0.0;
+        else if ((0.1 + p[k].step_start_time) > t) p[k].gravity = -9.8 * ((t - p[k].step_start_time) / 0.1);
+        else p[k].gravity = -9.8;
+    }
+    ctx->h_params = p[0];
+    MPMG_CHECK(cudaMemcpy(ctx->d_params, p.data(), count * sizeof(StepParams), cudaMemcpyHostToDevice));
     return MPMG_OK;
 }
 

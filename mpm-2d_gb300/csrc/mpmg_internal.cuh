@@ -8,6 +8,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <vector>
+
 #include "../../include/mpm_gb300.h"
 
 #define MPMG_TOL 1e-10          // process_usl.c:25
@@ -68,6 +70,20 @@ struct MixedState {
     double *export_buf;    // one FP64 particle field in caller order, for read-back
 };
 
+// A batch of independent simulations sharing one context: their particles,
+// elements and nodes are concatenated (member k first at poff[k], eoff[k],
+// noff[k]; each offset array has count + 1 entries), so the binning, the
+// graphs and the step orchestration are those of one simulation, and the
+// mixed kernels look each index's member up in the offset tables.
+struct BatchInfo {
+    int count;
+    std::vector<mpmg_config> cfg;
+    std::vector<size_t> poff, eoff, noff;
+    void *d_members;       // device table of per-member constants (mpmg_mixed.cu)
+    int *d_elem_off;       // eoff as int32, count + 1
+    int *d_node_off;       // noff as int32, count + 1
+};
+
 // Counting-sort binning scratch (mpmg_bin.cu).  Bins 0..ne-1 count the keys
 // of each element, bin ne + g the keys outside the grid at storage positions
 // 32 g .. 32 g + 31.
@@ -124,10 +140,15 @@ struct mpmg_ctx {
     unsigned int *cg_barrier;  // grid barrier counter + generation
     int cg_blocks;
 
-    StepParams *d_params;
-    StepParams h_params;   // host mirror, refreshed on read-back
+    StepParams *d_params;  // one record per simulation (a batch holds several)
+    StepParams h_params;   // host mirror of the first, refreshed on read-back
     int *d_status;
-    unsigned char *h_record;   // pinned host mirror of the step record and status
+    unsigned char *h_record;   // pinned host mirror of the step records and status
+    size_t status_offset;      // byte offset of the status word in the record block
+
+    // Batched ensemble (mpmg_batch_create): several independent simulations
+    // in one context, NULL for a single simulation.
+    BatchInfo *batch;
 
     // Mixed precision (cfg.precision == MPMG_PRECISION_MIXED).
     MixedState *mixed;

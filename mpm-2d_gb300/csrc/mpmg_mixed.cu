@@ -157,6 +157,40 @@ __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double t_
     }
 }
 
+// One simulation's constants.  A single simulation passes its own as a kernel
+// parameter; a batch (several simulations concatenated in one context) keeps
+// a device table of them and looks an element's or node's member up in the
+// first-index tables.
+struct MemberM {
+    GeomM g;
+    BcM bc;
+    MatF mat;
+    double dt;
+    float dt_hi, dt_lo;    // dt = dt_hi + dt_lo (float-float)
+    int gravity_mode;
+    double gravity_const;
+    int e0, nd0;           // first global element and node of the member
+};
+
+struct BatchView {
+    const MemberM *m;
+    const int *elem_off;   // first global element of each member, then the total
+    const int *node_off;   // first global node of each member, then the total
+    int count;
+};
+
+// The member holding global index x: the largest k with off[k] <= x.
+__device__ __forceinline__ int find_member(const int *__restrict__ off, int count, int x)
+{
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------------------
 
 // P2G: a block takes 256 consecutive elements, one thread each, and works
@@ -196,7 +230,9 @@ __device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, flo
     }
 }
 
-__global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const int *__restrict__ cell_start,
+template <bool BATCH>
+__global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(const __grid_constant__ MemberM m0, BatchView bv,
+                                                                int ne_total, const int *__restrict__ cell_start,
                                                                 const uint32_t *__restrict__ slots,
                                                                 uint32_t *__restrict__ perm,
                                                                 uint32_t *__restrict__ rank, Buf P,
@@ -210,7 +246,7 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
     __shared__ uint16_t sh_ord[kP2GChunk];
     __shared__ int sh_cs[kP2GThreads + 1];
     const int e0 = blockIdx.x * kP2GThreads;
-    const int ne_blk = min(kP2GThreads, g.ne - e0);
+    const int ne_blk = min(kP2GThreads, ne_total - e0);
     // element offsets come from the scan, two kernels back; the slots from
     // the scatter, the kernel just before
     for (int t = threadIdx.x; t <= ne_blk; t += kP2GThreads) sh_cs[t] = cell_start[e0 + t];
@@ -218,8 +254,15 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
     __syncthreads();
     const int me = threadIdx.x;
     const int k0 = me < ne_blk ? sh_cs[me] : 0, k1 = me < ne_blk ? sh_cs[me + 1] : 0;
-    const float grav = (float)sp->gravity;
-    const float ih = g.inv_hf;
+    float grav, ih;
+    if (BATCH) {
+        const int k = find_member(bv.elem_off, bv.count, min(e0 + me, ne_total - 1));
+        grav = (float)sp[k].gravity;
+        ih = bv.m[k].g.inv_hf;
+    } else {
+        grav = (float)sp->gravity;
+        ih = m0.g.inv_hf;
+    }
     int ea = 0;
     while (ea < ne_blk) {
         // elements [ea, eb) of this pass: the most whose particles fit the stage
@@ -289,7 +332,7 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(GeomM g, const i
 #pragma unroll
             for (int a = 0; a < 4; a++)
 #pragma unroll
-                for (int f = 0; f < 5; f++) cell_sums[(size_t)(a * 5 + f) * g.ne + e0 + me] = acc[a][f];
+                for (int f = 0; f < 5; f++) cell_sums[(size_t)(a * 5 + f) * ne_total + e0 + me] = acc[a][f];
         }
         ea = eb;
     }
@@ -330,20 +373,26 @@ __device__ __forceinline__ float ff_div(float nh, float nl, float dh, float dl, 
 // colour order (process_usl.c:524-540), float-float for mass and momentum;
 // boundary masks; momentum update and nodal velocity / acceleration
 // (process_usl.c:542-566).
-template <bool F64NODE>
-__global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int *__restrict__ cell_start,
+template <bool F64NODE, bool BATCH>
+__global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ MemberM m0, BatchView bv, int ne_total,
+                                                      int nn_total, const int *__restrict__ cell_start,
                                                       const float *__restrict__ cell_sums,
-                                                      const StepParams *__restrict__ sp, double dt,
-                                                      float dt_hi, float dt_lo, float tol,
+                                                      const StepParams *__restrict__ sp, float tol,
                                                       float2 *__restrict__ node_mass, float4 *__restrict__ node4,
                                                       double *__restrict__ node_mx,
                                                       double *__restrict__ node_my, double *__restrict__ node_fx,
                                                       double *__restrict__ node_fy)
 {
-    const int nn = g.Nx * g.Ny;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nn) return;
-    const int j = (int)mpmg_div((uint32_t)n, g.div_Nx), i = n - j * g.Nx;
+    if (n >= nn_total) return;
+    const int k = BATCH ? find_member(bv.node_off, bv.count, n) : 0;
+    const MemberM &M = BATCH ? bv.m[k] : m0;
+    const GeomM &g = M.g;
+    const BcM &bc = M.bc;
+    const double dt = M.dt;
+    const float dt_hi = M.dt_hi, dt_lo = M.dt_lo;
+    const int ln = n - M.nd0;
+    const int j = (int)mpmg_div((uint32_t)ln, g.div_Nx), i = ln - j * g.Nx;
     // the four elements in colour order and whether they hold particles
     // (cell_start is from the scan, three kernels back)
     int elem[4];
@@ -353,10 +402,10 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
         int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
         elem[c] = -1;
         if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
-        const int e = cj * g.Ex + ci;
+        const int e = M.e0 + cj * g.Ex + ci;
         if (cell_start[e] != cell_start[e + 1]) elem[c] = e;
     }
-    const double t_next = sp->t + dt;
+    const double t_next = sp[k].t + dt;
     mpmg_pdl_wait();        // the corner sums come from the P2G just before
     mpmg_pdl_trigger();
     float mh = 0, ml = 0, xh = 0, xl = 0, yh = 0, yl = 0;
@@ -369,18 +418,18 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
         const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
         const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
         const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
-        const float *cs = cell_sums + (size_t)(a * 5) * g.ne + e;
+        const float *cs = cell_sums + (size_t)(a * 5) * ne_total + e;
         if (F64NODE) {
             m64 += (double)cs[0];
-            mx64 += (double)cs[(size_t)g.ne];
-            my64 += (double)cs[(size_t)2 * g.ne];
+            mx64 += (double)cs[(size_t)ne_total];
+            my64 += (double)cs[(size_t)2 * ne_total];
         } else {
             ff_add(mh, ml, cs[0]);
-            ff_add(xh, xl, cs[(size_t)g.ne]);
-            ff_add(yh, yl, cs[(size_t)2 * g.ne]);
+            ff_add(xh, xl, cs[(size_t)ne_total]);
+            ff_add(yh, yl, cs[(size_t)2 * ne_total]);
         }
-        fx += cs[(size_t)3 * g.ne];
-        fy += cs[(size_t)4 * g.ne];
+        fx += cs[(size_t)3 * ne_total];
+        fy += cs[(size_t)4 * ne_total];
     }
     bool bx, by;
     bc_mask_m(bc, i, j, t_next, bx, by);
@@ -445,28 +494,22 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(GeomM g, BcM bc, const int
     }
 }
 
-// G2P of one particle read from the stored position i (element e), written
-// to position dst of the other buffer: velocity and displacement from the
+// G2P of one particle read from the stored position i (element e of member
+// M, local to it), written to position dst of the other buffer: velocity and displacement from the
 // nodal accelerations and velocities (process_usl.c:568-611), strain rate
 // and vorticity (process_usl.c:613-640), volume (process_usl.c:642-650), the
 // material's stress update, and the new element (process_usl.c:660-666).
-// Returns the new element key (g.ne outside the grid).
+// Returns the new global element key (sentinel outside the grid).
 template <int MATERIAL>
-__device__ __forceinline__ uint32_t g2p_particle(const GeomM &g, const MatF &mp, const float4 *__restrict__ node4,
-                                                 int e, float4 a4, float4 b4, float4 c4, float4 d4, uint32_t dst,
-                                                 Buf D, int *__restrict__ cell_dst)
+__device__ __forceinline__ uint32_t g2p_particle(const MemberM &M, uint32_t sentinel,
+                                                 const float4 *__restrict__ node4, int e, float4 a4, float4 b4,
+                                                 float4 c4, float4 d4, uint32_t dst, Buf D,
+                                                 int *__restrict__ cell_dst)
 {
-    if (e >= g.ne) {
-        // outside the grid: carried along unchanged
-        D.A[dst] = a4;
-        D.B[dst] = b4;
-        D.C[dst] = c4;
-        D.D[dst] = d4;
-        cell_dst[dst] = g.ne;
-        return (uint32_t)g.ne;
-    }
+    const GeomM &g = M.g;
+    const MatF &mp = M.mat;
     const int cj = (int)mpmg_div((uint32_t)e, g.div_Ex), ci = e - cj * g.Ex;
-    const int n0 = cj * g.Nx + ci;
+    const int n0 = M.nd0 + cj * g.Nx + ci;
     const float ih = g.inv_hf;
     const float xl = a4.x, yl = a4.y;
     const float ox = 1.0f - xl, oy = 1.0f - yl;
@@ -509,9 +552,9 @@ __device__ __forceinline__ uint32_t g2p_particle(const GeomM &g, const MatF &mp,
     const float xg = ((float)nci + nxl) * g.hf, yg = ((float)ncj + nyl) * g.hf;
     const bool inside = nci >= 0 && ncj >= 0 && nci < g.Ex && ncj < g.Ey && xg < g.xmaxf && yg < g.ymaxf &&
                         xg >= 0.0f && yg >= 0.0f;
-    uint32_t new_key = (uint32_t)g.ne;
+    uint32_t new_key = sentinel;
     if (inside) {
-        new_key = (uint32_t)(ncj * g.Ex + nci);
+        new_key = (uint32_t)(M.e0 + ncj * g.Ex + nci);
     } else {
         nxl = xg;      // global position of a particle that left the grid
         nyl = yg;
@@ -546,13 +589,14 @@ constexpr uint32_t kG2PStageBytes = (uint32_t)sizeof(G2PStage);
 constexpr size_t kG2PSmem = sizeof(G2PStage) * kG2PStages;
 static_assert(sizeof(G2PStage) % 16 == 0, "stage arrays must stay 16-byte aligned");
 
-template <int MATERIAL>
-__global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(GeomM g, int n, MatF mp, const uint32_t *__restrict__ rank,
+template <int MATERIAL, bool BATCH>
+__global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(const __grid_constant__ MemberM m0, BatchView bv,
+                                                             int ne_total, int n, const uint32_t *__restrict__ rank,
                                                              Buf S, Buf D, const int *__restrict__ cell_src,
                                                              int *__restrict__ cell_dst,
                                                              const float4 *__restrict__ node4,
-                                                             uint32_t *__restrict__ bins, StepParams *sp, double dt,
-                                                             int gravity_mode, double gravity_const, int *status)
+                                                             uint32_t *__restrict__ bins, StepParams *sp,
+                                                             int *status)
 {
     extern __shared__ __align__(128) unsigned char g2p_smem[];
     G2PStage *stage = reinterpret_cast<G2PStage *>(g2p_smem);
@@ -589,18 +633,22 @@ __global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(GeomM g, int n, Mat
     // in flight before the wait.  The nodal values come from the grid
     // update just before.
     mpmg_pdl_wait();
-    if (blockIdx.x == 0 && tid == 0) {
+    if (blockIdx.x == 0) {
         // Advance t and compute the next step's body force (the driver's
-        // time_varying_loads, loading.c:34-54).  No kernel of this step reads
-        // them after this point.
-        const double t = sp->t + dt;
-        sp->t = t;
-        sp->step_count += 1;
-        double grav;
-        if (gravity_mode == MPMG_GRAVITY_CONSTANT) grav = gravity_const;
-        else if ((0.1 + sp->step_start_time) > t) grav = -9.8 * ((t - sp->step_start_time) / 0.1);
-        else grav = -9.8;
-        sp->gravity = grav;
+        // time_varying_loads, loading.c:34-54), one thread per member.  No
+        // kernel of this step reads them after this point.
+        for (int k = tid; k < (BATCH ? bv.count : 1); k += kG2PTile) {
+            const MemberM &M = BATCH ? bv.m[k] : m0;
+            StepParams *p = sp + k;
+            const double t = p->t + M.dt;
+            p->t = t;
+            p->step_count += 1;
+            double grav;
+            if (M.gravity_mode == MPMG_GRAVITY_CONSTANT) grav = M.gravity_const;
+            else if ((0.1 + p->step_start_time) > t) grav = -9.8 * ((t - p->step_start_time) / 0.1);
+            else grav = -9.8;
+            p->gravity = grav;
+        }
     }
     uint32_t parity = 0;        // per stage: phase to wait for
     int k = 0;
@@ -635,10 +683,24 @@ __global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(GeomM g, int n, Mat
             e = cell_src[i];
             dst = rank[i];
         }
-        uint32_t new_key = (uint32_t)g.ne;
-        if (have) new_key = g2p_particle<MATERIAL>(g, mp, node4, e, a4, b4, c4, d4, dst, D, cell_dst);
+        const uint32_t sentinel = (uint32_t)ne_total;
+        uint32_t new_key = sentinel;
+        if (have) {
+            if (e >= ne_total) {
+                // outside the grid: carried along unchanged
+                D.A[dst] = a4;
+                D.B[dst] = b4;
+                D.C[dst] = c4;
+                D.D[dst] = d4;
+                cell_dst[dst] = ne_total;
+            } else {
+                const int mk = BATCH ? find_member(bv.elem_off, bv.count, e) : 0;
+                const MemberM &M = BATCH ? bv.m[mk] : m0;
+                new_key = g2p_particle<MATERIAL>(M, sentinel, node4, e - M.e0, a4, b4, c4, d4, dst, D, cell_dst);
+            }
+        }
         // the next step's bins, by destination position (the binning's first phase)
-        mpmg_bin_count(new_key, have, (uint32_t)g.ne, dst >> 5, bins);
+        mpmg_bin_count(new_key, have, sentinel, dst >> 5, bins);
         __syncthreads();        // every thread is done with stage k
         if (abort_s) {
             if (tid == 0)
@@ -664,28 +726,27 @@ inline int blocks_for(size_t n, int threads)
     return (int)(b > 0 ? b : 1);
 }
 
-GeomM make_geom(const mpmg_ctx *ctx)
+GeomM make_geom(const mpmg_config &c)
 {
     GeomM g;
-    g.Nx = ctx->cfg.Nx;
-    g.Ny = ctx->cfg.Ny;
-    g.Ex = ctx->Ex;
-    g.Ey = ctx->Ey;
-    g.ne = (int)ctx->ne;
-    g.div_Ex = mpmg_div_init((uint32_t)(ctx->Ex > 0 ? ctx->Ex : 1));
-    g.div_Nx = mpmg_div_init((uint32_t)(ctx->cfg.Nx > 0 ? ctx->cfg.Nx : 1));
-    g.h = ctx->cfg.h;
-    g.hf = (float)ctx->cfg.h;
-    g.inv_hf = (float)ctx->inv_h;
-    g.xmaxf = (float)ctx->cfg.xmax;
-    g.ymaxf = (float)ctx->cfg.ymax;
+    g.Nx = c.Nx;
+    g.Ny = c.Ny;
+    g.Ex = c.Nx - 1;
+    g.Ey = c.Ny - 1;
+    g.ne = g.Ex * g.Ey;
+    g.div_Ex = mpmg_div_init((uint32_t)(g.Ex > 0 ? g.Ex : 1));
+    g.div_Nx = mpmg_div_init((uint32_t)(c.Nx > 0 ? c.Nx : 1));
+    g.h = c.h;
+    g.hf = (float)c.h;
+    g.inv_hf = (float)(1.0 / c.h);
+    g.xmaxf = (float)c.xmax;
+    g.ymaxf = (float)c.ymax;
     return g;
 }
 
-BcM make_bc(const mpmg_ctx *ctx)
+BcM make_bc(const mpmg_config &c)
 {
     BcM b = {};
-    const mpmg_config &c = ctx->cfg;
     b.kind = c.bc;
     if (c.bc == MPMG_BOX) {
         b.left_col = (int)(size_t)(c.bcf[0] * (double)(c.Nx - 1));
@@ -706,13 +767,16 @@ BcM make_bc(const mpmg_ctx *ctx)
     return b;
 }
 
-MatF make_mat(const mpmg_ctx *ctx)
+// material_init (isolin.c:31-59, g_local_mu2.c:126-160) in FP32 form.
+MatF make_mat(const mpmg_config &c)
 {
     MatF p;
-    const mpmg_config &c = ctx->cfg;
-    p.G = (float)ctx->G;
-    p.K = (float)ctx->K;
-    p.lambda = (float)(ctx->K - 2.0 * ctx->G / 3.0);
+    const double E = c.mp[MPMG_MP_E], nu = c.mp[MPMG_MP_NU];
+    const double G = E / (2.0 * (1.0 + nu));
+    const double K = E / (3.0 * (1.0 - 2 * nu));
+    p.G = (float)G;
+    p.K = (float)K;
+    p.lambda = (float)(K - 2.0 * G / 3.0);
     p.dt = (float)c.dt;
     p.mu_s = (float)c.mp[MPMG_MP_MU_S];
     p.mu_2 = (float)c.mp[MPMG_MP_MU_2];
@@ -720,12 +784,27 @@ MatF make_mat(const mpmg_ctx *ctx)
     p.grains_rho = (float)c.mp[MPMG_MP_GRAINS_RHO];
     p.grains_d = (float)c.mp[MPMG_MP_GRAINS_D];
     p.rho_critical = (float)c.mp[MPMG_MP_RHO_CRITICAL];
-    if (c.material == MPMG_ISOLIN) p.lambda = (float)ctx->lambda;
     const double rho = c.mp[MPMG_MP_GRAINS_RHO], d = c.mp[MPMG_MP_GRAINS_D];
     p.inv_grains_rho = rho != 0.0 ? (float)(1.0 / rho) : 0.0f;
-    p.alpha_coef = d != 0.0 ? (float)(ctx->G * c.mp[MPMG_MP_I0] * c.dt / d) : 0.0f;
-    p.inv_G_dt = (ctx->G * c.dt) != 0.0 ? (float)(1.0 / (ctx->G * c.dt)) : 0.0f;
+    p.alpha_coef = d != 0.0 ? (float)(G * c.mp[MPMG_MP_I0] * c.dt / d) : 0.0f;
+    p.inv_G_dt = (G * c.dt) != 0.0 ? (float)(1.0 / (G * c.dt)) : 0.0f;
     return p;
+}
+
+MemberM make_member(const mpmg_config &c, size_t e0, size_t nd0)
+{
+    MemberM M;
+    M.g = make_geom(c);
+    M.bc = make_bc(c);
+    M.mat = make_mat(c);
+    M.dt = c.dt;
+    M.dt_hi = (float)c.dt;
+    M.dt_lo = (float)(c.dt - (double)M.dt_hi);
+    M.gravity_mode = c.gravity_mode;
+    M.gravity_const = c.gravity;
+    M.e0 = (int)e0;
+    M.nd0 = (int)nd0;
+    return M;
 }
 
 template <typename T>
@@ -739,14 +818,16 @@ int dalloc(T **p, size_t count)
     return MPMG_OK;
 }
 
-// Cell and local coordinates of a host position (FP64, as WHICH_ELEMENT4).
-void locate(const mpmg_ctx *ctx, double x, double y, int *cell, float *xl, float *yl)
+// Element (local to the simulation) and local coordinates of a host
+// position (FP64, as WHICH_ELEMENT4); -1 outside the grid, where xl, yl
+// keep the position.
+void locate(const mpmg_config &c, double x, double y, int *cell, float *xl, float *yl)
 {
-    const mpmg_config &c = ctx->cfg;
+    const int Ex = c.Nx - 1, Ey = c.Ny - 1;
     if (x < c.xmax && x >= 0.0 && y < c.ymax && y >= 0.0) {
         double fx = floor(x / c.h), fy = floor(y / c.h);
-        if (fx < (double)ctx->Ex && fy < (double)ctx->Ey) {
-            *cell = (int)(fx + fy * (double)ctx->Ex);
+        if (fx < (double)Ex && fy < (double)Ey) {
+            *cell = (int)(fx + fy * (double)Ex);
             double lx = (x - fx * c.h) / c.h, ly = (y - fy * c.h) / c.h;
             float fxl = (float)lx, fyl = (float)ly;
             if (fxl >= 1.0f) fxl = nextafterf(1.0f, 0.0f);
@@ -756,9 +837,18 @@ void locate(const mpmg_ctx *ctx, double x, double y, int *cell, float *xl, float
             return;
         }
     }
-    *cell = (int)ctx->ne;
+    *cell = -1;
     *xl = (float)x;
     *yl = (float)y;
+}
+
+using G2PKernel = void (*)(MemberM, BatchView, int, int, const uint32_t *, Buf, Buf, const int *, int *,
+                          const float4 *, uint32_t *, StepParams *, int *);
+
+G2PKernel g2p_variant(int material, bool batch)
+{
+    if (material == MPMG_ISOLIN) return batch ? mx_g2p_kernel<MPMG_ISOLIN, true> : mx_g2p_kernel<MPMG_ISOLIN, false>;
+    return batch ? mx_g2p_kernel<MPMG_G_LOCAL_MU2, true> : mx_g2p_kernel<MPMG_G_LOCAL_MU2, false>;
 }
 
 }  // namespace
@@ -786,12 +876,38 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     if ((rc = dalloc(&s->export_buf, n)) != MPMG_OK) return rc;
     MPMG_CHECK(cudaMemset(s->node_mass, 0, ctx->nn * sizeof(float2)));
 
+    // members: one, or the batch's (their constants and first-index tables)
+    BatchInfo *bt = ctx->batch;
+    const int count = bt ? bt->count : 1;
+    if (bt) {
+        std::vector<MemberM> hm(count);
+        std::vector<int> eo(count + 1), no(count + 1);
+        for (int k = 0; k < count; k++) hm[k] = make_member(bt->cfg[k], bt->eoff[k], bt->noff[k]);
+        for (int k = 0; k <= count; k++) {
+            eo[k] = (int)bt->eoff[k];
+            no[k] = (int)bt->noff[k];
+        }
+        MemberM *dm = nullptr;
+        if ((rc = dalloc(&dm, count)) != MPMG_OK) return rc;
+        bt->d_members = dm;
+        if ((rc = dalloc(&bt->d_elem_off, count + 1)) != MPMG_OK) return rc;
+        if ((rc = dalloc(&bt->d_node_off, count + 1)) != MPMG_OK) return rc;
+        MPMG_CHECK(cudaMemcpy(dm, hm.data(), count * sizeof(MemberM), cudaMemcpyHostToDevice));
+        MPMG_CHECK(cudaMemcpy(bt->d_elem_off, eo.data(), (count + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        MPMG_CHECK(cudaMemcpy(bt->d_node_off, no.data(), (count + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    }
+
     // host staging: element, local coordinates, records
     std::vector<float4> ha(n ? n : 1), hb(n ? n : 1), hc(n ? n : 1), hd(n ? n : 1);
     std::vector<int> cell(n ? n : 1);
+    int member = 0;
     for (size_t i = 0; i < n; i++) {
+        while (bt && i >= bt->poff[member + 1]) member++;
+        const mpmg_config &c = bt ? bt->cfg[member] : ctx->cfg;
         float xl, yl;
-        locate(ctx, x[i], y[i], &cell[i], &xl, &yl);
+        int local;
+        locate(c, x[i], y[i], &local, &xl, &yl);
+        cell[i] = local < 0 ? (int)ctx->ne : (int)((bt ? bt->eoff[member] : 0) + (size_t)local);
         ha[i] = make_float4(xl, yl, (float)vx[i], (float)vy[i]);
         hb[i] = make_float4((float)m[i], (float)v[i], (float)sxx[i], (float)sxy[i]);
         hc[i] = make_float4((float)syy[i], 0.0f, 0.0f, 0.0f);
@@ -812,17 +928,10 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     // most one per tile
     int sms = 0, per_sm = 0;
     MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
-    if (ctx->cfg.material == MPMG_ISOLIN) {
-        MPMG_CHECK(cudaFuncSetAttribute(mx_g2p_kernel<MPMG_ISOLIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)kG2PSmem));
-        MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_g2p_kernel<MPMG_ISOLIN>, kG2PTile,
-                                                                 kG2PSmem));
-    } else {
-        MPMG_CHECK(cudaFuncSetAttribute(mx_g2p_kernel<MPMG_G_LOCAL_MU2>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG2PSmem));
-        MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_g2p_kernel<MPMG_G_LOCAL_MU2>,
-                                                                 kG2PTile, kG2PSmem));
-    }
+    void (*g2p)(MemberM, BatchView, int, int, const uint32_t *, Buf, Buf, const int *, int *, const float4 *,
+                uint32_t *, StepParams *, int *) = g2p_variant(ctx->cfg.material, bt != nullptr);
+    MPMG_CHECK(cudaFuncSetAttribute(g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG2PSmem));
+    MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g2p, kG2PTile, kG2PSmem));
     const size_t tiles = (n + kG2PTile - 1) / kG2PTile;
     size_t blocks = (size_t)(sms > 0 ? sms : 1) * (size_t)(per_sm > 0 ? per_sm : 1);
     if (blocks > tiles) blocks = tiles;
@@ -857,15 +966,29 @@ static int *cell_array(mpmg_ctx *ctx, int b)
     return b == 0 ? ctx->in_element : ctx->active;
 }
 
+// The batch view of a context (a single simulation: one member, no tables).
+static BatchView batch_view(const mpmg_ctx *ctx)
+{
+    BatchView bv = {nullptr, nullptr, nullptr, 1};
+    if (ctx->batch) {
+        bv.m = (const MemberM *)ctx->batch->d_members;
+        bv.elem_off = ctx->batch->d_elem_off;
+        bv.node_off = ctx->batch->d_node_off;
+        bv.count = ctx->batch->count;
+    }
+    return bv;
+}
+
 int mpmg_mixed_step(mpmg_ctx *ctx)
 {
     MixedState *s = ctx->mixed;
     cudaStream_t st = ctx->stream;
     const mpmg_config &c = ctx->cfg;
-    const GeomM g = make_geom(ctx);
-    const int n = (int)ctx->np;
+    const bool batch = ctx->batch != nullptr;
+    const MemberM m0 = make_member(batch ? ctx->batch->cfg[0] : c, 0, 0);
+    const BatchView bv = batch_view(ctx);
+    const int n = (int)ctx->np, ne = (int)ctx->ne, nn = (int)ctx->nn;
     const int cur = s->cur, nxt = 1 - cur;
-    const float dt_hi = (float)c.dt, dt_lo = (float)(c.dt - (double)dt_hi);
 
     mpmg_phase_begin(ctx, PH_SORT);
     int rc = mpmg_bin_scan_scatter(ctx, (const uint32_t *)cell_array(ctx, cur), nullptr, true);
@@ -874,35 +997,27 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
 
     Buf S = buf(s, cur), D = buf(s, nxt);
     mpmg_phase_begin(ctx, PH_P2G);
-    MPMG_CHECK(mpmg_launch_pdl(true, mx_p2g_kernel, dim3(blocks_for(ctx->ne, kP2GThreads)), dim3(kP2GThreads), 0,
-                               st, g, ctx->cell_start, ctx->bin.slots, ctx->perm, ctx->bin.rank, S, ctx->d_params,
-                               s->cell_sums));
+    MPMG_CHECK(mpmg_launch_pdl(true, batch ? mx_p2g_kernel<true> : mx_p2g_kernel<false>,
+                               dim3(blocks_for(ctx->ne, kP2GThreads)), dim3(kP2GThreads), 0, st, m0, bv, ne,
+                               (const int *)ctx->cell_start, (const uint32_t *)ctx->bin.slots, ctx->perm,
+                               ctx->bin.rank, S, (const StepParams *)ctx->d_params, s->cell_sums));
     mpmg_phase_end(ctx, PH_P2G);
 
     mpmg_phase_begin(ctx, PH_GRID);
-    MPMG_CHECK(mpmg_launch_pdl(true,
-                               c.precision == MPMG_PRECISION_MIXED_F64NODE ? mx_grid_kernel<true>
-                                                                           : mx_grid_kernel<false>,
-                               dim3(blocks_for(ctx->nn, 256)), dim3(256), 0, st, g, make_bc(ctx), ctx->cell_start,
-                               s->cell_sums, ctx->d_params, c.dt, dt_hi, dt_lo, (float)MPMG_TOL, s->node_mass,
-                               s->node4, ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy));
+    const bool f64 = c.precision == MPMG_PRECISION_MIXED_F64NODE;
+    auto grid = f64 ? (batch ? mx_grid_kernel<true, true> : mx_grid_kernel<true, false>)
+                    : (batch ? mx_grid_kernel<false, true> : mx_grid_kernel<false, false>);
+    MPMG_CHECK(mpmg_launch_pdl(true, grid, dim3(blocks_for(ctx->nn, 256)), dim3(256), 0, st, m0, bv, ne, nn,
+                               (const int *)ctx->cell_start, (const float *)s->cell_sums,
+                               (const StepParams *)ctx->d_params, (float)MPMG_TOL, s->node_mass, s->node4,
+                               ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy));
     mpmg_phase_end(ctx, PH_GRID);
 
     mpmg_phase_begin(ctx, PH_G2P);
-    const MatF mp = make_mat(ctx);
-    if (c.material == MPMG_ISOLIN) {
-        MPMG_CHECK(mpmg_launch_pdl(true, mx_g2p_kernel<MPMG_ISOLIN>, dim3(s->g2p_blocks), dim3(kG2PTile), kG2PSmem,
-                                   st, g, n, mp, (const uint32_t *)ctx->bin.rank, S, D,
-                                   (const int *)cell_array(ctx, cur), cell_array(ctx, nxt),
-                                   (const float4 *)s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode,
-                                   c.gravity, ctx->d_status));
-    } else {
-        MPMG_CHECK(mpmg_launch_pdl(true, mx_g2p_kernel<MPMG_G_LOCAL_MU2>, dim3(s->g2p_blocks), dim3(kG2PTile),
-                                   kG2PSmem, st, g, n, mp, (const uint32_t *)ctx->bin.rank, S, D,
-                                   (const int *)cell_array(ctx, cur), cell_array(ctx, nxt),
-                                   (const float4 *)s->node4, ctx->bin.counts, ctx->d_params, c.dt, c.gravity_mode,
-                                   c.gravity, ctx->d_status));
-    }
+    MPMG_CHECK(mpmg_launch_pdl(true, g2p_variant(c.material, batch), dim3(s->g2p_blocks), dim3(kG2PTile),
+                               kG2PSmem, st, m0, bv, ne, n, (const uint32_t *)ctx->bin.rank, S, D,
+                               (const int *)cell_array(ctx, cur), cell_array(ctx, nxt), (const float4 *)s->node4,
+                               ctx->bin.counts, ctx->d_params, ctx->d_status));
     mpmg_phase_end(ctx, PH_G2P);
     ctx->launches += 3;
     s->cur = nxt;
@@ -986,8 +1101,20 @@ int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active)
     int rc;
     if ((rc = download_i(ctx, cell_array(ctx, s->cur), cell)) != MPMG_OK) return rc;
     if ((rc = pids(ctx, pid)) != MPMG_OK) return rc;
+    const BatchInfo *bt = ctx->batch;
     for (size_t k = 0; k < ctx->np; k++) {
         int e = cell[k] < (int)ctx->ne ? cell[k] : -1;
+        if (e >= 0 && bt) {
+            // element local to the particle's member
+            const size_t ge = (size_t)e;
+            int lo = 0, hi = bt->count - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if (bt->eoff[mid] <= ge) lo = mid;
+                else hi = mid - 1;
+            }
+            e = (int)(ge - bt->eoff[lo]);
+        }
         if (in_element) in_element[pid[k]] = e;
         if (active) active[pid[k]] = e >= 0 ? 1 : 0;
     }
@@ -1001,8 +1128,8 @@ namespace {
 // element's corner plus the local coordinate, times h, as the host
 // read-back computes them; a particle outside the grid holds its position.
 __global__ void mx_export_kernel(int n, const float4 *__restrict__ rec, int comp, const float4 *__restrict__ drec,
-                                 const int *__restrict__ cell, int xy, MpmgDiv div_Ex, int ne, double h,
-                                 double *__restrict__ out)
+                                 const int *__restrict__ cell, int xy, const __grid_constant__ MemberM m0,
+                                 BatchView bv, int ne, double *__restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1013,8 +1140,10 @@ __global__ void mx_export_kernel(int n, const float4 *__restrict__ rec, int comp
     if (xy != 0) {
         const int c = cell[i];
         if (c < ne) {
-            const int cj = (int)mpmg_div((uint32_t)c, div_Ex), ci = c - cj * (int)div_Ex.d;
-            o = ((double)(xy == 1 ? ci : cj) + (double)v) * h;
+            const MemberM &M = bv.count > 1 ? bv.m[find_member(bv.elem_off, bv.count, c)] : m0;
+            const int lc = c - M.e0;
+            const int cj = (int)mpmg_div((uint32_t)lc, M.g.div_Ex), ci = lc - cj * M.g.Ex;
+            o = ((double)(xy == 1 ? ci : cj) + (double)v) * M.g.h;
         }
     }
     out[pid] = o;
@@ -1048,9 +1177,10 @@ int frame_get(mpmg_ctx *ctx, const char *name, double *out)
     else if (strcmp(name, "y") == 0) { xy = 2; comp = 1; }
     else if (!field_slot(name, &rec, &comp)) return MPMG_ERR_UNKNOWN_FIELD;
     if (n == 0) return MPMG_OK;
-    mx_export_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(
-        (int)n, record(s, b, rec), comp, s->D[b], cell_array(ctx, b), xy,
-        mpmg_div_init((uint32_t)(ctx->Ex > 0 ? ctx->Ex : 1)), (int)ctx->ne, ctx->cfg.h, s->export_buf);
+    const MemberM m0 = make_member(ctx->batch ? ctx->batch->cfg[0] : ctx->cfg, 0, 0);
+    mx_export_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>((int)n, record(s, b, rec), comp, s->D[b],
+                                                                   cell_array(ctx, b), xy, m0, batch_view(ctx),
+                                                                   (int)ctx->ne, s->export_buf);
     ctx->launches += 1;
     MPMG_CHECK(cudaGetLastError());
     MPMG_CHECK(cudaMemcpyAsync(out, s->export_buf, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

@@ -76,6 +76,11 @@ def lib(build_if_missing=True):
         L.mpmg_get_field.argtypes = [vp, C.c_char_p, dp]
         L.mpmg_set_field.argtypes = [vp, C.c_char_p, dp]
         L.mpmg_get_fields.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), C.POINTER(dp)]
+        L.mpmg_batch_create.argtypes = ([C.c_int, C.POINTER(Config), C.POINTER(C.c_size_t)] + [dp] * 9
+                                        + [C.POINTER(vp)])
+        L.mpmg_batch_count.argtypes = [vp, ip]
+        L.mpmg_batch_member.argtypes = [vp, C.c_int] + [C.POINTER(C.c_size_t)] * 6
+        L.mpmg_batch_get_time.argtypes = [vp, C.c_int, dp, ip]
         L.mpmg_get_map.argtypes = [vp, ip, ip]
         L.mpmg_set_map.argtypes = [vp, ip, ip]
         L.mpmg_get_sort.argtypes = [vp, ip, ip, ip]
@@ -278,3 +283,52 @@ class Simulation:
         n = C.c_long()
         _check(lib().mpmg_launch_count(self._h, C.byref(n), 1 if reset else 0))
         return n.value
+
+
+class Batch(Simulation):
+    """Several independent simulations in one context (mpmg_batch_create):
+    one set of kernel launches steps them all.  Fields read back concatenated
+    in member order; `member(k)` gives member k's slices."""
+
+    def __init__(self, scenes, precision="mixed", device=0, store_transients=False):
+        L = lib()
+        count = len(scenes)
+        cfgs = (Config * count)(*[make_config(sc, store_transients, device=device, precision=precision)
+                                  for sc in scenes])
+        counts = (C.c_size_t * count)(*[len(sc["particles"]["x"]) for sc in scenes])
+        arrs = [np.ascontiguousarray(np.concatenate([np.asarray(sc["particles"][k], dtype=np.float64)
+                                                     for sc in scenes]))
+                for k in ("m", "v", "x", "y", "vx", "vy", "sxx", "sxy", "syy")]
+        h = C.c_void_p()
+        _check(L.mpmg_batch_create(count, cfgs, counts, *[_dptr(a) for a in arrs], C.byref(h)))
+        self._h = h
+        self.precision = precision
+        self.count = count
+        self.scenes = list(scenes)
+        self.scene = scenes[0]
+        npart, nn, ne = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        _check(L.mpmg_sizes(self._h, C.byref(npart), C.byref(nn), C.byref(ne)))
+        self.n, self.nn, self.ne = npart.value, nn.value, ne.value
+        self.members = []
+        for k in range(count):
+            v = [C.c_size_t() for _ in range(6)]
+            _check(L.mpmg_batch_member(self._h, k, *[C.byref(x) for x in v]))
+            p0, np_, n0, nn_, e0, ne_ = [x.value for x in v]
+            self.members.append({"particles": slice(p0, p0 + np_), "nodes": slice(n0, n0 + nn_),
+                                 "elements": slice(e0, e0 + ne_)})
+
+    def member_get(self, k, name):
+        a = self.get(name)
+        return a[self.members[k]["nodes" if name.startswith("node_") else "particles"]]
+
+    def member_map(self, k):
+        e, a = self.get_map()
+        sl = self.members[k]["particles"]
+        return e[sl], a[sl]
+
+    def member_time(self, k):
+        t = C.c_double()
+        s = C.c_int()
+        _check(lib().mpmg_batch_get_time(self._h, k, C.byref(t), C.byref(s)))
+        return t.value, s.value
+

@@ -104,3 +104,44 @@ def with_particles(scene, idx):
     out = dict(scene)
     out["particles"] = {k: np.ascontiguousarray(v[idx]) for k, v in scene["particles"].items()}
     return out
+
+
+def ensemble(count=256, seed=1, ppc_1d=2, cells_range=(64, 384), particles_range=(5e3, 2e5),
+             outlet_range=(0.02, 0.12), mu_s_range=(0.30, 0.45), dt=5e-6, rho=2450.0, props=(1e6, 0.3),
+             grains_d=5.3e-4):
+    """Independent silo and heap runs of uneven sizes for a batch: per member a
+    grid of n x n elements (n uniform in cells_range), a target particle count
+    log-uniform in particles_range (a silo fill left of the wall or a column
+    on the floor of a box, 2x2 per element, clipped to the domain), a silo
+    outlet (hole radius) uniform in outlet_range and mu_s uniform in
+    mu_s_range; g_local_mu2 with the benchmark's grain size."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(rng.integers(cells_range[0], cells_range[1] + 1))
+        target = float(np.exp(rng.uniform(np.log(particles_range[0]), np.log(particles_range[1]))))
+        outlet = float(rng.uniform(*outlet_range))
+        mu_s = float(rng.uniform(*mu_s_range))
+        h = 1.0 / n
+        s = h / ppc_1d
+        mp = {"mu_s": mu_s, "grains_d": grains_d}
+        if k % 2 == 0:
+            wall_frac = 0.8
+            width = int(n * wall_frac) * h
+            cols = int(width / s)
+            rows = max(1, min(int(round(target / cols)), int((1.0 - 2 * h) / s)))
+            p = block_particles(0.0, 0.0, width, rows * s, s, rho)
+            sc = {"Nx": n + 1, "Ny": n + 1, "h": h, "dt": dt, "material": "g_local_mu2", "props": list(props),
+                  "bc": "square_silo", "bcf": [outlet, 0.0, wall_frac], "bci": [], "gravity": None,
+                  "particles": p, "mp": mp}
+        else:
+            width = float(rng.uniform(0.2, 0.5))
+            cols = int(width / s)
+            rows = max(1, min(int(round(target / cols)), int((1.0 - 2 * h) / s)))
+            p = block_particles(0.0, 0.0, width, rows * s, s, rho)
+            sc = {"Nx": n + 1, "Ny": n + 1, "h": h, "dt": dt, "material": "g_local_mu2", "props": list(props),
+                  "bc": "box", "bcf": [0.0, 0.0, 1.0, 1.0], "bci": [1, 3, 1, 0], "gravity": None,
+                  "particles": p, "mp": mp}
+        out.append(sc)
+    return out
+

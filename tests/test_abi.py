@@ -82,6 +82,24 @@ def test_invalid_configuration_is_rejected():
     assert rc == 16 and not h.value
 
 
+def test_batch_configuration_is_rejected():
+    ens = scenes.ensemble(count=2, seed=1, cells_range=(16, 16), particles_range=(100, 200))
+    cfgs = (mpm2d.Config * 2)(*[mpm2d.make_config(sc, precision="mixed") for sc in ens])
+    counts = (mpm2d.C.c_size_t * 2)(*[len(sc["particles"]["x"]) for sc in ens])
+    z = mpm2d.np.zeros(sum(counts))
+    h = mpm2d.C.c_void_p()
+    L = mpm2d.lib()
+    cfgs[1].precision = 0                  # the FP64 form does not batch
+    assert L.mpmg_batch_create(2, cfgs, counts, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h)) == 20
+    cfgs[1].precision = 2                  # members must share the precision
+    assert L.mpmg_batch_create(2, cfgs, counts, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h)) == 16
+    cfgs[1].precision = 1
+    cfgs[1].material = 0                   # and the material kind
+    assert L.mpmg_batch_create(2, cfgs, counts, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h)) == 16
+    assert L.mpmg_batch_create(0, cfgs, counts, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h)) == 16
+    assert not h.value
+
+
 def test_frame_read_entry_point_is_exported():
     L = mpm2d.lib()
     assert hasattr(L, "mpmg_get_fields")
