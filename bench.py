@@ -355,6 +355,58 @@ def run_gpu(args):
                                   "elements, 5k-200k particles log-uniform, outlet 0.02-0.12, mu_s 0.30-0.45 "
                                   "(seed 1), mixed precision"}
 
+    # --- adjoint: gradient of a trajectory loss w.r.t. (mu_s, mu_2, I0, E) -----
+    adjoint_line = None
+    if not args.no_adjoint:
+        adj_steps, adj_k = 2000, 100
+        theta0 = np.array([0.3819, 0.6435, 0.278, 1e6])
+        theta_t = theta0 + np.array([0.02, -0.03, 0.0, 0.0])
+        theta_t[3] *= 1.1
+
+        def final_xy(theta):
+            s_ = mpm2d.Simulation(scenes.adjoint_column(theta), device=dev)
+            s_.step(adj_steps)
+            xy = (s_.get("x"), s_.get("y"))
+            s_.close()
+            return xy
+
+        xt, yt = final_xy(theta_t)
+        s_ = mpm2d.Simulation(scenes.adjoint_column(theta0), device=dev)
+        s_.step(3)
+        s_.synchronize()
+        t0 = time.perf_counter()
+        s_.step(adj_steps)
+        s_.synchronize()
+        t_fwd = time.perf_counter() - t0
+        s_.close()
+        s_ = mpm2d.Simulation(scenes.adjoint_column(theta0), device=dev)
+        t0 = time.perf_counter()
+        s_.adj_forward_tape(adj_steps, adj_k)
+        t_tape = time.perf_counter() - t0
+        xa, ya = s_.get("x"), s_.get("y")
+        t0 = time.perf_counter()
+        grad = s_.adj_backward(2 * (xa - xt), 2 * (ya - yt))
+        t_bwd = time.perf_counter() - t0
+        s_.close()
+        fd = []
+        for k in range(4):
+            hk = 1e-4 * theta0[k]
+            tp, tm = theta0.copy(), theta0.copy()
+            tp[k] += hk
+            tm[k] -= hk
+            (xp, yp), (xm, ym) = final_xy(tp), final_xy(tm)
+            fd.append((np.sum((xp - xt) ** 2 + (yp - yt) ** 2) - np.sum((xm - xt) ** 2 + (ym - yt) ** 2))
+                      / (2 * hk))
+        names = ("mu_s", "mu_2", "I0", "E")
+        adjoint_line = {
+            "workload": "g_local_mu2 column, 65 536 particles, 256x128 elements, dt 2e-6, 2000 steps, "
+                        "loss = sum |x(T) - x_target(T)|^2 against mu_s+0.02, mu_2-0.03, E*1.1",
+            "dtype": "f64", "steps": adj_steps, "checkpoint_every": adj_k,
+            "forward_s": t_fwd, "tape_forward_s": t_tape, "backward_s": t_bwd,
+            "adjoint_over_forward": t_bwd / t_fwd,
+            "grad": dict(zip(names, map(float, grad))), "fd_central_1e-4": dict(zip(names, map(float, fd))),
+            "max_rel_err_vs_fd": float(max(abs(g - f) / abs(f) for g, f in zip(grad, fd) if f != 0))}
+
     # --- end to end through the C ABI with host buffers (mixed) ---------------
     # The user's run: create the simulation from host arrays (H2D of the
     # particle state), step, read each step's result back (mpmg_get_time:
@@ -406,6 +458,7 @@ def run_gpu(args):
                  "bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s)"},
         "mixed_over_fp64": value / value64,
         "batch": batch_line,
+        "adjoint": adjoint_line,
         "mixed_f64node": {"value": valuef, "unit": UNIT, "steps": args.steps, "ms_per_step": msf / args.steps,
                           "note": "same mixed step with FP64 nodal mass/momentum sums and division"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
@@ -437,6 +490,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=60)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--e2e-steps", type=int, default=500,
                     help="steps of the end-to-end run (one output frame at its end)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

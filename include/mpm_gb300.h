@@ -195,6 +195,24 @@ MPMG_API int mpmg_batch_member(mpmg_ctx *ctx, int member, size_t *first_particle
                                size_t *num_elements);
 MPMG_API int mpmg_batch_get_time(mpmg_ctx *ctx, int member, double *t, int *step_number);
 
+/* Reverse-mode adjoint of the FP64 step (no counterpart in the reference).
+   mpmg_adj_forward_tape advances nsteps ordinary steps from the current
+   state, keeping the particle state every checkpoint_every steps.
+   mpmg_adj_backward takes the gradient of a loss with respect to the final
+   positions (dl_dx, dl_dy, particle order) and returns in dl_dtheta[4] its
+   gradient with respect to the material parameters mu_s, mu_2, I0 (the
+   g_local_mu2 constants, mpmg_config.mp) and E; each checkpoint segment is
+   run forward again with its steps recorded on the device, then reversed by
+   hand-written adjoint kernels of the material update, G2P, grid update and
+   P2G.  The context is left at the taped run's final state.  The element of
+   each particle and the branches of the material law are held fixed within
+   a step.  mpmg_adj_state then reads the adjoint of a field of the run's
+   initial state: x y vx vy v sxx sxy syy Tzz.  FP64 form, isolin or
+   g_local_mu2, one simulation. */
+MPMG_API int mpmg_adj_forward_tape(mpmg_ctx *ctx, int nsteps, int checkpoint_every);
+MPMG_API int mpmg_adj_backward(mpmg_ctx *ctx, const double *dl_dx, const double *dl_dy, double *dl_dtheta);
+MPMG_API int mpmg_adj_state(mpmg_ctx *ctx, const char *name, double *host_out);
+
 /* Runs only the material update on every active particle from the current
    strain rates (the per-particle path of the reference's tests/test_material.c).
    Local materials only. */

@@ -19,8 +19,9 @@
  *   find_filled_elements              libmpm/process_usl.c:677  (process_usl.h:18)
  *   mpm_cleanup                       libmpm/process_usl.c:974  (process.h:253)
  *   initial_loads, time_varying_loads libmpm/loading.c:21,34
- * plus four additions that return an int status instead of exiting:
- *   mpm_gpu_attach, mpm_gpu_step, mpm_gpu_sync_host, mpm_gpu_detach.
+ * plus additions that return an int status instead of exiting:
+ *   mpm_gpu_attach, mpm_gpu_step, mpm_gpu_sync_host, mpm_gpu_detach, and the
+ *   adjoint pair mpm_adj_forward_tape, mpm_adj_backward.
  */
 #ifndef MPM_LIBMPM_H
 #define MPM_LIBMPM_H
@@ -274,6 +275,14 @@ MPMG_API int mpm_gpu_attach(job_t *job);
 MPMG_API int mpm_gpu_step(job_t *job, int nsteps);
 MPMG_API int mpm_gpu_sync_host(job_t *job);
 MPMG_API int mpm_gpu_detach(job_t *job);
+
+/* The adjoint pair on a job (see mpmg_adj_forward_tape / mpmg_adj_backward in
+   mpm_gb300.h): nsteps taped steps from the job's current state (job->t
+   advances), then the gradient of a loss on the final positions with respect
+   to (mu_s, mu_2, I0, E).  The host particles are not refreshed by either;
+   call mpm_gpu_sync_host for them. */
+MPMG_API int mpm_adj_forward_tape(job_t *job, int nsteps, int checkpoint_every);
+MPMG_API int mpm_adj_backward(job_t *job, const double *dl_dx, const double *dl_dy, double *dl_dtheta);
 
 #ifdef __cplusplus
 }

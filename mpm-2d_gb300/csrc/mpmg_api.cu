@@ -333,6 +333,7 @@ int mpmg_destroy(mpmg_ctx *ctx)
     mpmg_bin_free(ctx);
     mpmg_nonlocal_free(ctx);
     mpmg_mixed_free(ctx);
+    mpmg_adj_free(ctx);
     if (ctx->batch) {
         cudaFree(ctx->batch->d_members);
         cudaFree(ctx->batch->d_elem_off);

@@ -150,6 +150,9 @@ struct mpmg_ctx {
     // in one context, NULL for a single simulation.
     BatchInfo *batch;
 
+    // Tape of the last mpmg_adj_forward_tape run (mpmg_adjoint.cu).
+    struct AdjTape *adj;
+
     // Mixed precision (cfg.precision == MPMG_PRECISION_MIXED).
     MixedState *mixed;
 
@@ -227,6 +230,7 @@ int mpmg_mixed_get(mpmg_ctx *ctx, const char *name, double *out);
 int mpmg_mixed_set(mpmg_ctx *ctx, const char *name, const double *in);
 int mpmg_mixed_get_many(mpmg_ctx *ctx, int count, const char *const *names, double *const *out, bool *done);
 int mpmg_mixed_get_map(mpmg_ctx *ctx, int *in_element, int *active);
+void mpmg_adj_free(mpmg_ctx *ctx);
 
 void mpmg_phase_begin(mpmg_ctx *ctx, int phase);
 void mpmg_phase_end(mpmg_ctx *ctx, int phase);

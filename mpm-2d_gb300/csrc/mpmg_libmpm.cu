@@ -426,6 +426,27 @@ int mpm_gpu_step(job_t *job, int nsteps)
     return mpmg_synchronize(gj->ctx);
 }
 
+int mpm_adj_forward_tape(job_t *job, int nsteps, int checkpoint_every)
+{
+    int rc = mpm_gpu_attach(job);
+    if (rc != MPMG_OK) return rc;
+    GpuJob *gj = find_job(job);
+    rc = mpmg_adj_forward_tape(gj->ctx, nsteps, checkpoint_every);
+    if (rc != MPMG_OK) return rc;
+    for (int k = 0; k < nsteps; k++) job->t += job->dt;   // process_usl.c:522, step by step
+    return MPMG_OK;
+}
+
+int mpm_adj_backward(job_t *job, const double *dl_dx, const double *dl_dy, double *dl_dtheta)
+{
+    GpuJob *gj = find_job(job);
+    if (gj == nullptr || gj->ctx == nullptr) {
+        mpmg_set_error("job has no taped GPU run (mpm_adj_forward_tape)");
+        return MPMG_ERR_INVALID;
+    }
+    return mpmg_adj_backward(gj->ctx, dl_dx, dl_dy, dl_dtheta);
+}
+
 int mpm_gpu_detach(job_t *job)
 {
     mpmg_ctx *ctx = nullptr;

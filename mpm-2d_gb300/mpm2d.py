@@ -81,6 +81,9 @@ def lib(build_if_missing=True):
         L.mpmg_batch_count.argtypes = [vp, ip]
         L.mpmg_batch_member.argtypes = [vp, C.c_int] + [C.POINTER(C.c_size_t)] * 6
         L.mpmg_batch_get_time.argtypes = [vp, C.c_int, dp, ip]
+        L.mpmg_adj_forward_tape.argtypes = [vp, C.c_int, C.c_int]
+        L.mpmg_adj_backward.argtypes = [vp, dp, dp, dp]
+        L.mpmg_adj_state.argtypes = [vp, C.c_char_p, dp]
         L.mpmg_get_map.argtypes = [vp, ip, ip]
         L.mpmg_set_map.argtypes = [vp, ip, ip]
         L.mpmg_get_sort.argtypes = [vp, ip, ip, ip]
@@ -197,6 +200,25 @@ class Simulation:
         n = self.nn if name.startswith("node_") else self.n
         out = np.empty(n)
         _check(lib().mpmg_get_field(self._h, name.encode(), _dptr(out)))
+        return out
+
+    def adj_forward_tape(self, nsteps, checkpoint_every=100):
+        """Advance nsteps FP64 steps keeping checkpoints for mpmg_adj_backward."""
+        _check(lib().mpmg_adj_forward_tape(self._h, nsteps, checkpoint_every))
+
+    def adj_backward(self, dl_dx, dl_dy):
+        """Gradient of a loss on the taped run's final positions with respect to
+        (mu_s, mu_2, I0, E), given dL/dx and dL/dy per particle."""
+        gx = np.ascontiguousarray(dl_dx, dtype=np.float64)
+        gy = np.ascontiguousarray(dl_dy, dtype=np.float64)
+        out = np.zeros(4)
+        _check(lib().mpmg_adj_backward(self._h, _dptr(gx), _dptr(gy), _dptr(out)))
+        return out
+
+    def adj_state(self, name):
+        """Adjoint of one field of the taped run's initial state."""
+        out = np.empty(self.n)
+        _check(lib().mpmg_adj_state(self._h, name.encode(), _dptr(out)))
         return out
 
     def get_frame(self, names, out=None):

@@ -145,3 +145,13 @@ def ensemble(count=256, seed=1, ppc_1d=2, cells_range=(64, 384), particles_range
         out.append(sc)
     return out
 
+
+def adjoint_column(theta=(0.3819, 0.6435, 0.278, 1e6), seed=2):
+    """The adjoint benchmark: a 0.25 x 0.25 m g_local_mu2 column (64 x 64
+    elements at 4 x 4 particles each: 65 536 particles) in a 1 x 0.5 m box of
+    256 x 128 elements, dt 2e-6; theta = (mu_s, mu_2, I0, E)."""
+    return column(Nx=257, Ny=129, h=1.0 / 256, width=0.25, height=0.25, ppc_1d=4, material="g_local_mu2",
+                  rho=2450.0, props=(theta[3], 0.3), dt=2e-6,
+                  mp={"grains_d": 5.3e-4, "mu_s": theta[0], "mu_2": theta[1], "I0": theta[2]},
+                  jitter=1e-4, seed=seed)
+
