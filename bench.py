@@ -355,6 +355,45 @@ def run_gpu(args):
                                   "elements, 5k-200k particles log-uniform, outlet 0.02-0.12, mu_s 0.30-0.45 "
                                   "(seed 1), mixed precision"}
 
+    # --- nonlocal silo (g_nonlocal_mu2, FP64, fluidity PCG every step) -------------
+    nonlocal_line = None
+    if not args.no_nonlocal:
+        nsc = scenes.silo_prestressed(cells=512)
+        nnl = len(nsc["particles"]["x"])
+        nsim = mpm2d.Simulation(nsc, device=dev)
+        nstream = torch.cuda.ExternalStream(nsim.stream(), device=dev)
+        nsim.step(args.warmup)
+        nsim.synchronize()
+        nsteps_nl = max(3, min(args.steps, 10))
+        barrier()
+        msn = time_steps(nsim, nsteps_nl, nstream, torch)
+        barrier()
+        iters = []
+        nsim.enable_phase_timing(True)
+        for _ in range(3):
+            nsim.step(1)
+            nsim.synchronize()
+            rc_s, it, res = nsim.last_solve()
+            iters.append(it)
+        pt = nsim.phase_times()
+        nsim.enable_phase_timing(False)
+        e_map, a_map = nsim.get_map()
+        filled = int(np.unique(e_map[a_map == 1]).size)
+        nsim.close()
+        solve_ms = pt["fluidity"][0] / max(pt["fluidity"][1], 1)
+        it_mean = float(np.mean(iters))
+        dofs = nsc["Nx"] * nsc["Ny"]
+        iter_bytes = 80 * filled + 80 * dofs
+        nonlocal_line = {
+            "workload": "g_nonlocal_mu2 square silo, 835 996 particles, 513x513 nodes, outlet radius 0.06, "
+                        "lithostatic start, PCG to relative residual 1e-10 every step",
+            "dtype": "f64", "value": nnl * nsteps_nl / (msn / 1e3), "unit": UNIT,
+            "ms_per_step": msn / nsteps_nl, "pcg_iterations_per_step": it_mean,
+            "fluidity_ms_per_step": solve_ms,
+            "pcg_iteration_gbs": iter_bytes * it_mean / (solve_ms / 1e3) / 1e9 if solve_ms > 0 else None,
+            "pcg_iteration_bytes": iter_bytes,
+            "note": "fluidity phase = bulk fluidity, element assembly, cooperative Jacobi-PCG, stress update"}
+
     # --- adjoint: gradient of a trajectory loss w.r.t. (mu_s, mu_2, I0, E) -----
     adjoint_line = None
     if not args.no_adjoint:
@@ -459,6 +498,7 @@ def run_gpu(args):
         "mixed_over_fp64": value / value64,
         "batch": batch_line,
         "adjoint": adjoint_line,
+        "nonlocal_silo": nonlocal_line,
         "mixed_f64node": {"value": valuef, "unit": UNIT, "steps": args.steps, "ms_per_step": msf / args.steps,
                           "note": "same mixed step with FP64 nodal mass/momentum sums and division"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
@@ -491,6 +531,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=60)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
+    ap.add_argument("--no-nonlocal", action="store_true", help="skip the nonlocal silo measurement")
     ap.add_argument("--e2e-steps", type=int, default=500,
                     help="steps of the end-to-end run (one output frame at its end)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -155,3 +155,21 @@ def adjoint_column(theta=(0.3819, 0.6435, 0.278, 1e6), seed=2):
                   mp={"grains_d": 5.3e-4, "mu_s": theta[0], "mu_2": theta[1], "I0": theta[2]},
                   jitter=1e-4, seed=seed)
 
+
+def silo_prestressed(cells=512, material="g_nonlocal_mu2", hole_radius=0.06, open_time=0.0, wall_frac=0.8,
+                     dt=1e-6, rho=2450.0, props=(1e6, 0.3), mp=None, surcharge=500.0, k0=0.4):
+    """The nonlocal silo benchmark (513^2 nodes, 835 996 particles at 2x2 per
+    element left of the wall column) starting from a lithostatic stress
+    (syy = -rho g (H - y) - surcharge, sxx = k0 syy) under constant gravity,
+    with the outlet open.  With k0 = 0.4 the stress ratio tau / p = 0.43
+    exceeds mu_s everywhere, so the fluidity solve is non-trivial from the
+    first step."""
+    sc = silo(cells=cells, material=material, hole_radius=hole_radius, open_time=open_time,
+              wall_frac=wall_frac, rho=rho, props=props, dt=dt, gravity=-9.8,
+              mp=mp if mp is not None else {"grains_d": 5.3e-4, "A": 0.48})
+    p = sc["particles"]
+    H = float(np.max(p["y"])) + 0.5 / cells
+    p["syy"] = -rho * 9.8 * (H - p["y"]) - surcharge
+    p["sxx"] = k0 * p["syy"]
+    return sc
+
