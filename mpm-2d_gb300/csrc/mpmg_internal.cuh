@@ -135,7 +135,8 @@ struct mpmg_ctx {
     // Nonlocal fluidity solve.
     double *elem_k;        // 10 matrix entries per element, value-major
     double *elem_f;        // 4 RHS entries per element, value-major
-    double *cg_x, *cg_r, *cg_p, *cg_q, *cg_dinv;     // per node
+    double *cg_x, *cg_r, *cg_p, *cg_q, *cg_dinv, *cg_w;   // per node
+    double *cg_coef;       // 9-point rows of the assembled matrix, 9 per node
     double *cg_partials;   // per-block partial sums
     unsigned int *cg_barrier;  // grid barrier counter + generation
     int cg_blocks;

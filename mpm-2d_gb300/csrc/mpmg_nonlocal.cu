@@ -98,45 +98,14 @@ struct SolveArgs {
     const int *cell_start;
     const double *elem_k, *elem_f;
     double *x, *r, *p, *q, *dinv;
+    double *w;           // A u of the current residual
+    double *u;           // D^-1 r
+    double *coef;        // 9-point rows, coef[k * nn + n], k = 3 (dj + 1) + (di + 1)
     double *partials;    // [4][nblocks]
     unsigned int *barrier;
     int *status;
     StepParams *sp;
 };
-
-// Row of node (i, j) applied to vector u over its (up to) four elements, in
-// colour order.  Also returns the diagonal and right-hand side when asked.
-// u is written by other blocks between grid barriers, so it is read through
-// L2 (__ldcg), never from a possibly stale L1 line.
-__device__ __forceinline__ double apply_row(const SolveArgs &S, int i, int j, const double *u,
-                                            double *diag, double *rhs)
-{
-    double acc = 0, d = 0, f = 0;
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-        int ci = ((i & 1) == (c & 1)) ? i : i - 1;
-        int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
-        if (ci < 0 || cj < 0 || ci >= S.Ex || cj >= S.Ey) continue;
-        int e = cj * S.Ex + ci;
-        if (S.cell_start[e] == S.cell_start[e + 1]) continue;
-        int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
-        int n0 = cj * S.Nx + ci;
-        int nb[4] = {n0, n0 + 1, n0 + 1 + S.Nx, n0 + S.Nx};
-        if (u != nullptr) {
-#pragma unroll
-            for (int b = 0; b < 4; b++) acc += S.elem_k[(size_t)sym_index(a, b) * S.ne + e] * __ldcg(u + nb[b]);
-        }
-        if (diag != nullptr) {
-            d += S.elem_k[(size_t)sym_index(a, a) * S.ne + e];
-            f += S.elem_f[(size_t)a * S.ne + e];
-        }
-    }
-    if (diag != nullptr) {
-        *diag = d;
-        *rhs = f;
-    }
-    return acc;
-}
 
 // Block-wide sum of up to three values, fixed tree; result valid in thread 0.
 __device__ __forceinline__ void block_sum3(double &a, double &b, double &c)
@@ -190,6 +159,68 @@ __device__ __forceinline__ double grid_total(const double *partials, int slot, i
     return out;
 }
 
+// Row of node (i, j) as a 9-point stencil and its right-hand side: the four
+// elements around the node (south-west, south-east, north-west, north-east),
+// each element's corners in order.  The node is corner a = TR, TL, BR, BL of
+// them; corner b of an element lies at offset (bx, by) from its BL node, so
+// every stencil index is a compile-time constant.
+__device__ __forceinline__ void build_row(const SolveArgs &S, int i, int j, double cf[9], double *rhs)
+{
+    constexpr int qx[4] = {-1, 0, -1, 0}, qy[4] = {-1, -1, 0, 0};   // element offset of each quadrant
+    constexpr int qa[4] = {2, 3, 1, 0};                             // the node's corner in it
+    constexpr int bx[4] = {0, 1, 1, 0}, by[4] = {0, 0, 1, 1};       // corner offsets BL BR TR TL
+    double f = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int ci = i + qx[q], cj = j + qy[q];
+        if (ci < 0 || cj < 0 || ci >= S.Ex || cj >= S.Ey) continue;
+        const int e = cj * S.Ex + ci;
+        if (S.cell_start[e] == S.cell_start[e + 1]) continue;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int di = qx[q] + bx[b], dj = qy[q] + by[b];
+            cf[3 * (dj + 1) + (di + 1)] += S.elem_k[(size_t)sym_index(qa[q], b) * S.ne + e];
+        }
+        f += S.elem_f[(size_t)qa[q] * S.ne + e];
+    }
+    *rhs = f;
+}
+
+// dinv == +0 (not an unknown) tested on the integer pipe: dinv is either a
+// positive reciprocal or +0 by construction.
+__device__ __forceinline__ bool is_zero(double d)
+{
+    return __double_as_longlong(d) == 0;
+}
+
+// (A v)(n) from the stored 9-point row.  v of the neighbours is written by
+// other blocks between grid barriers, so it is read through L2 (__ldcg).
+// Missing neighbours (outside the grid) have zero coefficients and are
+// skipped by index, so the row costs nine FP64 FMAs and no comparisons on the
+// FP64 pipe (GB300 runs FP64 at 1/64 of the FP32 rate).
+__device__ __forceinline__ double apply_stencil(const SolveArgs &S, int n, int i, int j, const double *v)
+{
+    const int nn = S.Nx * S.Ny;
+    double acc = 0;
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++) {
+        if (j + dj < 0 || j + dj >= S.Ny) continue;
+#pragma unroll
+        for (int di = -1; di <= 1; di++) {
+            if (i + di < 0 || i + di >= S.Nx) continue;
+            acc = fma(S.coef[(size_t)(3 * (dj + 1) + (di + 1)) * nn + n], __ldcg(v + n + dj * S.Nx + di), acc);
+        }
+    }
+    return acc;
+}
+
+// Jacobi-preconditioned conjugate gradients in the Chronopoulos-Gear form
+// (Chronopoulos and Gear, 1989): the two inner products of an iteration are
+// taken together, so an iteration needs two grid-wide synchronisations (one
+// for the new residual, one for the reduction) instead of three.
+//   p = u + beta p;  s = w + beta s;  x += alpha p;  r -= alpha s
+//   u = D^-1 r;  w = A u;  gamma' = <r, u>;  delta = <w, u>
+//   beta = gamma' / gamma;  alpha = gamma' / (delta - beta gamma' / alpha)
 __global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
 {
     const int nn = S.Nx * S.Ny;
@@ -197,53 +228,78 @@ __global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
     const int stride = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
 
-    // Set-up: unknown mask via dinv, right-hand side in r, warm start in x.
+    // Set-up: 9-point rows (with the diagonal shift), unknown mask via dinv,
+    // right-hand side in r, warm start in x.
     for (int n = tid; n < nn; n += stride) {
-        const int i = n % S.Nx, j = n / S.Nx;
-        double d = 0, f = 0;
-        if (S.node_m[n] > S.dof_tol) {
-            apply_row(S, i, j, nullptr, &d, &f);
-            d += S.shift;
+        const int j = n / S.Nx, i = n - j * S.Nx;
+        double cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        double f = 0;
+        const bool dof = S.node_m[n] > S.dof_tol;
+        if (dof) {
+            build_row(S, i, j, cf, &f);
+            cf[4] += S.shift;
         }
-        if (S.node_m[n] > S.dof_tol && d > 0) {
-            S.dinv[n] = 1.0 / d;
+        if (dof && cf[4] > 0) {
+            S.dinv[n] = 1.0 / cf[4];
             S.r[n] = f;
         } else {
             S.dinv[n] = 0;
             S.r[n] = 0;
             S.x[n] = 0;
+#pragma unroll
+            for (int k = 0; k < 9; k++) cf[k] = 0;
         }
+#pragma unroll
+        for (int k = 0; k < 9; k++) S.coef[(size_t)k * nn + n] = cf[k];
     }
     if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
 
-    // r = b - A x, z = D^-1 r, p = z
-    double rz = 0, rr = 0, bb = 0;
+    // r = b - A x (x of the neighbours is final since the set-up barrier; r
+    // is read only at its own node here)
+    double bb = 0, d1 = 0, d2 = 0;
     for (int n = tid; n < nn; n += stride) {
-        if (S.dinv[n] == 0) {
-            S.p[n] = 0;
-            continue;
-        }
-        const int i = n % S.Nx, j = n / S.Nx;
-        double b = S.r[n];
-        double ax = apply_row(S, i, j, S.x, nullptr, nullptr) + S.shift * S.x[n];
-        double r = b - ax;
-        S.r[n] = r;
-        double z = S.dinv[n] * r;
-        S.p[n] = z;
-        rz += r * z;
-        rr += r * r;
+        if (is_zero(S.dinv[n])) continue;
+        const int j = n / S.Nx, i = n - j * S.Nx;
+        const double b = S.r[n];
+        S.r[n] = b - apply_stencil(S, n, i, j, S.x);
         bb += b * b;
     }
-    block_sum3(rz, rr, bb);
+    block_sum3(bb, d1, d2);
+    if (threadIdx.x == 0) S.partials[2 * nblocks + blockIdx.x] = bb;
+    if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+    bb = grid_total(S.partials, 2, nblocks);
+    for (int n = tid; n < nn; n += stride) S.u[n] = S.dinv[n] * S.r[n];
+    if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+
+    // u = D^-1 r, w = A u, gamma = <r, u>, delta = <w, u>, <r, r>
+    double gamma = 0, delta = 0, rr = 0;
+    for (int n = tid; n < nn; n += stride) {
+        if (is_zero(S.dinv[n])) {
+            S.w[n] = 0;
+            S.p[n] = 0;
+            S.q[n] = 0;
+            continue;
+        }
+        const int j = n / S.Nx, i = n - j * S.Nx;
+        const double r = S.r[n], u = S.u[n];
+        const double w = apply_stencil(S, n, i, j, S.u);
+        S.w[n] = w;
+        S.p[n] = 0;      // p, s (in q) start at zero: the first update sets p = u, s = w
+        S.q[n] = 0;
+        gamma += r * u;
+        delta += w * u;
+        rr += r * r;
+    }
+    block_sum3(gamma, delta, rr);
     if (threadIdx.x == 0) {
-        S.partials[0 * nblocks + blockIdx.x] = rz;
-        S.partials[1 * nblocks + blockIdx.x] = rr;
-        S.partials[2 * nblocks + blockIdx.x] = bb;
+        S.partials[0 * nblocks + blockIdx.x] = gamma;
+        S.partials[1 * nblocks + blockIdx.x] = delta;
+        S.partials[3 * nblocks + blockIdx.x] = rr;
     }
     if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
-    rz = grid_total(S.partials, 0, nblocks);
-    rr = grid_total(S.partials, 1, nblocks);
-    bb = grid_total(S.partials, 2, nblocks);
+    gamma = grid_total(S.partials, 0, nblocks);
+    delta = grid_total(S.partials, 1, nblocks);
+    rr = grid_total(S.partials, 3, nblocks);
     const double target = S.tol * S.tol * bb;
 
     int it = 0;
@@ -254,51 +310,52 @@ __global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
         rr = 0;
         converged = true;
     }
+    double alpha = gamma / delta, beta = 0;
     while (!converged && it < S.maxit) {
-        // q = A p, <p, q>
-        double pq = 0, d1 = 0, d2 = 0;
+        // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s (own nodes)
         for (int n = tid; n < nn; n += stride) {
-            if (S.dinv[n] == 0) continue;
-            const int i = n % S.Nx, j = n / S.Nx;
-            double q = apply_row(S, i, j, S.p, nullptr, nullptr) + S.shift * S.p[n];
-            S.q[n] = q;
-            pq += S.p[n] * q;
-        }
-        block_sum3(pq, d1, d2);
-        if (threadIdx.x == 0) S.partials[3 * nblocks + blockIdx.x] = pq;
-        if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
-        pq = grid_total(S.partials, 3, nblocks);
-        const double alpha = rz / pq;
-
-        // x += alpha p, r -= alpha q, <r, z>, <r, r>
-        double rz_new = 0, rr_new = 0, d3 = 0;
-        for (int n = tid; n < nn; n += stride) {
-            if (S.dinv[n] == 0) continue;
-            S.x[n] += alpha * S.p[n];
-            double r = S.r[n] - alpha * S.q[n];
+            const double dv = S.dinv[n];
+            if (is_zero(dv)) continue;
+            const double p = fma(beta, S.p[n], S.u[n]);
+            const double sv = fma(beta, S.q[n], S.w[n]);
+            const double r = fma(-alpha, sv, S.r[n]);
+            S.p[n] = p;
+            S.q[n] = sv;
+            S.x[n] = fma(alpha, p, S.x[n]);
             S.r[n] = r;
-            rz_new += r * (S.dinv[n] * r);
-            rr_new += r * r;
-        }
-        block_sum3(rz_new, rr_new, d3);
-        if (threadIdx.x == 0) {
-            S.partials[0 * nblocks + blockIdx.x] = rz_new;
-            S.partials[1 * nblocks + blockIdx.x] = rr_new;
+            S.u[n] = dv * r;
         }
         if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
-        rz_new = grid_total(S.partials, 0, nblocks);
-        rr = grid_total(S.partials, 1, nblocks);
+        double gn = 0, dl = 0, rn = 0;
+        for (int n = tid; n < nn; n += stride) {
+            if (is_zero(S.dinv[n])) continue;
+            const int j = n / S.Nx, i = n - j * S.Nx;
+            const double r = S.r[n], u = S.u[n];
+            const double w = apply_stencil(S, n, i, j, S.u);
+            S.w[n] = w;
+            gn = fma(r, u, gn);
+            dl = fma(w, u, dl);
+            rn = fma(r, r, rn);
+        }
+        block_sum3(gn, dl, rn);
+        if (threadIdx.x == 0) {
+            S.partials[0 * nblocks + blockIdx.x] = gn;
+            S.partials[1 * nblocks + blockIdx.x] = dl;
+            S.partials[3 * nblocks + blockIdx.x] = rn;
+        }
+        if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+        gn = grid_total(S.partials, 0, nblocks);
+        dl = grid_total(S.partials, 1, nblocks);
+        rr = grid_total(S.partials, 3, nblocks);
         it++;
-        if (!(rr <= target) && !(rr == rr)) break;   // NaN: give up
+        if (!(rr == rr)) break;   // NaN: give up
         converged = (rr <= target);
         if (converged) break;
-        const double beta = rz_new / rz;
-        rz = rz_new;
-        for (int n = tid; n < nn; n += stride) {
-            if (S.dinv[n] == 0) continue;
-            S.p[n] = S.dinv[n] * S.r[n] + beta * S.p[n];
-        }
-        if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
+        beta = gn / gamma;
+        const double eta = dl - beta * gn / alpha;
+        if (!(eta > 0)) break;    // breakdown of the recurrence: report non-convergence
+        alpha = gn / eta;
+        gamma = gn;
     }
     if (tid == 0) {
         S.sp->solve_iters = it;
@@ -368,11 +425,12 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
     const size_t ne = ctx->ne > 0 ? ctx->ne : 1, nn = ctx->nn;
     MPMG_CHECK(cudaMalloc(&ctx->elem_k, 10 * ne * sizeof(double)));
     MPMG_CHECK(cudaMalloc(&ctx->elem_f, 4 * ne * sizeof(double)));
-    double **vecs[] = {&ctx->cg_x, &ctx->cg_r, &ctx->cg_p, &ctx->cg_q, &ctx->cg_dinv};
+    double **vecs[] = {&ctx->cg_x, &ctx->cg_r, &ctx->cg_p, &ctx->cg_q, &ctx->cg_dinv, &ctx->cg_w};
     for (double **v : vecs) {
         MPMG_CHECK(cudaMalloc(v, nn * sizeof(double)));
         MPMG_CHECK(cudaMemsetAsync(*v, 0, nn * sizeof(double), ctx->stream));
     }
+    MPMG_CHECK(cudaMalloc(&ctx->cg_coef, 9 * nn * sizeof(double)));
     int per_sm = 0, sms = 0;
     MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_kernel, kSolveThreads, 0));
     MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
@@ -394,7 +452,7 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
 void mpmg_nonlocal_free(mpmg_ctx *ctx)
 {
     double **ptrs[] = {&ctx->elem_k, &ctx->elem_f, &ctx->cg_x, &ctx->cg_r, &ctx->cg_p, &ctx->cg_q,
-                       &ctx->cg_dinv, &ctx->cg_partials};
+                       &ctx->cg_dinv, &ctx->cg_w, &ctx->cg_coef, &ctx->cg_partials};
     for (double **p : ptrs) {
         cudaFree(*p);
         *p = nullptr;
@@ -448,6 +506,9 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     S.p = ctx->cg_p;
     S.q = ctx->cg_q;
     S.dinv = ctx->cg_dinv;
+    S.w = ctx->cg_w;
+    S.u = ctx->cg_x;
+    S.coef = ctx->cg_coef;
     S.partials = ctx->cg_partials;
     S.barrier = ctx->cg_barrier;
     S.status = ctx->d_status;
