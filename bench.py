@@ -380,6 +380,15 @@ def run_gpu(args):
         e_map, a_map = nsim.get_map()
         filled = int(np.unique(e_map[a_map == 1]).size)
         nsim.close()
+        # the same silo in the mixed form (FP32 step, FP64 fluidity solve)
+        msim = mpm2d.Simulation(nsc, device=dev, precision="mixed")
+        mstream = torch.cuda.ExternalStream(msim.stream(), device=dev)
+        msim.step(args.warmup)
+        msim.synchronize()
+        barrier()
+        msm = time_steps(msim, nsteps_nl, mstream, torch)
+        barrier()
+        msim.close()
         solve_ms = pt["fluidity"][0] / max(pt["fluidity"][1], 1)
         it_mean = float(np.mean(iters))
         dofs = nsc["Nx"] * nsc["Ny"]
@@ -389,6 +398,7 @@ def run_gpu(args):
                         "lithostatic start, PCG to relative residual 1e-10 every step",
             "dtype": "f64", "value": nnl * nsteps_nl / (msn / 1e3), "unit": UNIT,
             "ms_per_step": msn / nsteps_nl, "pcg_iterations_per_step": it_mean,
+            "mixed_value": nnl * nsteps_nl / (msm / 1e3), "mixed_ms_per_step": msm / nsteps_nl,
             "fluidity_ms_per_step": solve_ms,
             "pcg_iteration_gbs": iter_bytes * it_mean / (solve_ms / 1e3) / 1e9 if solve_ms > 0 else None,
             "pcg_iteration_bytes": iter_bytes,

@@ -76,8 +76,9 @@ enum mpmg_gravity {
    those nodal sums and the division in FP64 instead (GB300 runs FP64 at 1/64
    of the FP32 rate, so this form's grid update is several times slower).
    Both mixed forms keep particles in element order on the device (read-back
-   returns the caller's order) and support the local materials (isolin,
-   g_local_mu2). */
+   returns the caller's order) and support isolin, g_local_mu2 and
+   g_nonlocal_mu2 (whose material law evaluates in FP64 from the FP32 state,
+   and whose fluidity solve stays FP64). */
 enum mpmg_precision {
     MPMG_PRECISION_FP64 = 0,
     MPMG_PRECISION_MIXED = 1,

@@ -504,8 +504,8 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
         const bool nonlocal = cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL;
         const bool mixed =
             cfg->precision == MPMG_PRECISION_MIXED || cfg->precision == MPMG_PRECISION_MIXED_F64NODE;
-        if (mixed && nonlocal) {
-            mpmg_set_error("mixed precision supports isolin and g_local_mu2");
+        if (mixed && cfg->material == MPMG_G_NONLOCAL) {
+            mpmg_set_error("mixed precision supports isolin, g_local_mu2 and g_nonlocal_mu2");
             rc = MPMG_ERR_UNSUPPORTED;
             goto fail;
         }

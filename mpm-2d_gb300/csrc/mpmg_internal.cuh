@@ -68,6 +68,7 @@ struct MixedState {
     float2 *node_mass;     // per node: mass as float-float (hi, lo)
     int g2p_blocks;        // persistent G2P grid size
     double *export_buf;    // one FP64 particle field in caller order, for read-back
+    float4 *nl_E, *nl_F;   // g_nonlocal_mu2: strain rate and bulk fluidity per stored particle
 };
 
 // A batch of independent simulations sharing one context: their particles,
@@ -219,6 +220,7 @@ int mpmg_bin_reset(mpmg_ctx *ctx);
 int mpmg_nonlocal_init(mpmg_ctx *ctx);
 void mpmg_nonlocal_free(mpmg_ctx *ctx);
 int mpmg_launch_fluidity(mpmg_ctx *ctx);         // nonlocal: assembly, solve, stress
+int mpmg_launch_solve(mpmg_ctx *ctx);            // nonlocal: the fluidity PCG alone
 int mpmg_launch_material_only(mpmg_ctx *ctx);
 int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const double *x, const double *y,
                     const double *vx, const double *vy, const double *sxx, const double *sxy,

@@ -70,6 +70,7 @@ struct MatF {
     float inv_grains_rho;  // 1 / grains_rho
     float alpha_coef;      // G I0 dt / grains_d
     float inv_G_dt;        // 1 / (G dt)
+    float inv_A2d2;        // 1 / (A^2 d^2), the nonlocal cooperativity scale (g_nonlocal_mu2)
 };
 
 // isolin (isolin.c:75-116) in FP32.
@@ -136,6 +137,79 @@ __device__ __forceinline__ void g_local_mu2_f(const MatF &p, float m, float v, f
     gp += nup * dt;
     gdp = nup;
 }
+
+// g_nonlocal_mu2 on the FP32 state: the 2D trial Jaumann stress
+// (g_nonlocal_mu2.c:166-186, with lambda = K - 2G/3 where the reference
+// leaves it uninitialised), the bulk fluidity of
+// calculate_bulk_granular_fluidity (:238-321) and the stress update once the
+// nodal fluidity is known (:160-218).  These evaluate in FP64 (about sixty
+// FP64 operations per particle, small beside the fluidity solve): the local
+// fluidity p / (G dt) (1 / scale - 1) cancels near yield, and in FP32 that
+// cancellation biased the flow (an 8 % faster silo discharge than the FP64
+// form; within the FP64 form's own round-off spread once evaluated in FP64).
+__device__ __forceinline__ void nonlocal_mu2_trial_f(const MatF &p, float exx, float exy, float eyy, float wxy,
+                                                     float sxx, float sxy, float syy, float &p_tr, float &t0xx,
+                                                     float &t0xy, float &t0yy, float &tau_tr)
+{
+    const double twoG = 2.0 * (double)p.G, trD = (double)exx + eyy, dt = p.dt, lam = p.lambda;
+    const double w2s = 2.0 * (double)wxy * sxy;
+    const double sxx_tr = sxx + dt * (lam * trD + twoG * exx + w2s);
+    const double sxy_tr = sxy + dt * (twoG * exy - (double)wxy * ((double)sxx - syy));
+    const double syy_tr = syy + dt * (lam * trD + twoG * eyy - w2s);
+    const double pt = -0.5 * (sxx_tr + syy_tr);
+    const double a = sxx_tr + pt, b = sxy_tr, c = syy_tr + pt;
+    p_tr = (float)pt; t0xx = (float)a; t0xy = (float)b; t0yy = (float)c;
+    tau_tr = (float)sqrt(0.5 * (a * a + 2.0 * b * b + c * c));
+}
+
+__device__ __forceinline__ void nonlocal_mu2_bulk_f(const MatF &p, float m, float v, float p_tr, float tau_tr,
+                                                    float &dense, float &gf_local, float &xisq_inv)
+{
+    dense = (m < p.rho_critical * v || p_tr < 0.0f) ? 0.0f : 1.0f;
+    gf_local = 0.0f;
+    xisq_inv = 0.0f;
+    if (dense != 0.0f && p_tr > 0.0f) {
+        const double pr = p_tr, tau = tau_tr;
+        const double S0 = (double)p.mu_s * pr;
+        double tau_tau = tau, scale = 1.0;
+        if (tau > S0) {
+            const double S2 = (double)p.mu_2 * pr;
+            const double alpha = (double)p.alpha_coef * sqrt(pr * (double)p.inv_grains_rho);
+            const double B = -(S2 + tau + alpha);
+            const double H = S2 * tau + S0 * alpha;
+            const double disc = sqrt(B * B - 4.0 * H);
+            tau_tau = (B > 0.0) ? (-B - disc) * 0.5 : (2.0 * H) / (-B + disc);
+            scale = tau_tau / tau;
+        }
+        gf_local = (float)(pr * (double)p.inv_G_dt * (1.0 / scale - 1.0));
+        xisq_inv = (float)(fabs(tau_tau / pr - (double)p.mu_s) * (double)p.inv_A2d2);
+    }
+}
+
+__device__ __forceinline__ void nonlocal_mu2_stress_f(const MatF &p, float dense, float gf, float p_tr, float t0xx,
+                                                      float t0xy, float t0yy, float tau_tr, float &sxx, float &sxy,
+                                                      float &syy, float &gp, float &gdp)
+{
+    float nup = 0.0f;
+    if (dense == 0.0f || !(p_tr > 0.0f)) {
+        sxx = sxy = syy = 0.0f;
+    } else {
+        const double scale = (double)p_tr / ((double)p.G * p.dt * gf + p_tr);
+        nup = (float)((tau_tr - tau_tr * scale) * (double)p.inv_G_dt);
+        sxx = (float)(scale * t0xx - p_tr);
+        sxy = (float)(scale * t0xy);
+        syy = (float)(scale * t0yy - p_tr);
+    }
+    gp += nup * p.dt;
+    gdp = nup;
+}
+
+// Per-particle values the nonlocal step keeps from the G2P to the stress
+// update after the fluidity solve, indexed by stored position:
+// E = {exx, exy, eyy, wxy}, F = {dense, gf_local, xisq_inv, updated volume}.
+struct NLOut {
+    float4 *E, *F;
+};
 
 __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double t_now, bool &mx, bool &my)
 {
@@ -381,7 +455,7 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ Me
                                                       float2 *__restrict__ node_mass, float4 *__restrict__ node4,
                                                       double *__restrict__ node_mx,
                                                       double *__restrict__ node_my, double *__restrict__ node_fx,
-                                                      double *__restrict__ node_fy)
+                                                      double *__restrict__ node_fy, double *__restrict__ node_m64)
 {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nn_total) return;
@@ -452,6 +526,7 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ Me
         }
         const float mhi = (float)m64;
         node_mass[n] = make_float2(mhi, (float)(m64 - (double)mhi));
+        if (node_m64 != nullptr) node_m64[n] = m64;
         node4[n] = nd;
         if (node_mx != nullptr) {
             node_mx[n] = mx64;
@@ -485,6 +560,7 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ Me
         nd.w = ff_div(yh, yl, mh, ml, r);
     }
     node_mass[n] = make_float2(mh, ml);
+    if (node_m64 != nullptr) node_m64[n] = (double)mh + (double)ml;
     node4[n] = nd;
     if (node_mx != nullptr) {
         node_mx[n] = (double)xh + (double)xl;
@@ -504,7 +580,7 @@ template <int MATERIAL>
 __device__ __forceinline__ uint32_t g2p_particle(const MemberM &M, uint32_t sentinel,
                                                  const float4 *__restrict__ node4, int e, float4 a4, float4 b4,
                                                  float4 c4, float4 d4, uint32_t dst, Buf D,
-                                                 int *__restrict__ cell_dst)
+                                                 int *__restrict__ cell_dst, int src, NLOut nl)
 {
     const GeomM &g = M.g;
     const MatF &mp = M.mat;
@@ -539,8 +615,15 @@ __device__ __forceinline__ uint32_t g2p_particle(const MemberM &M, uint32_t sent
     float sxx = b4.z, sxy = b4.w, syy = c4.x, Tzz = c4.w, gp = d4.x, gdp = d4.y;
     if (MATERIAL == MPMG_ISOLIN) {
         isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
-    } else {
+    } else if (MATERIAL == MPMG_G_LOCAL_MU2) {
         g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
+    } else {
+        // g_nonlocal_mu2: bulk fluidity now; the stress waits for the solve
+        float p_tr, t0xx, t0xy, t0yy, tau_tr, dense, gfl, xisq;
+        nonlocal_mu2_trial_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy, p_tr, t0xx, t0xy, t0yy, tau_tr);
+        nonlocal_mu2_bulk_f(mp, m, vol, p_tr, tau_tr, dense, gfl, xisq);
+        nl.E[src] = make_float4(exx, exy, eyy, wxy);
+        nl.F[src] = make_float4(dense, gfl, xisq, vol);
     }
 
     // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
@@ -562,7 +645,7 @@ __device__ __forceinline__ uint32_t g2p_particle(const MemberM &M, uint32_t sent
     D.A[dst] = make_float4(nxl, nyl, vx, vy);
     D.B[dst] = make_float4(m, vol, sxx, sxy);
     D.C[dst] = make_float4(syy, c4.y + dux, c4.z + duy, Tzz);
-    D.D[dst] = make_float4(gp, gdp, d4.z, 0.0f);
+    D.D[dst] = make_float4(gp, gdp, d4.z, d4.w);
     cell_dst[dst] = (int)new_key;
     return new_key;
 }
@@ -596,7 +679,7 @@ __global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(const __grid_consta
                                                              int *__restrict__ cell_dst,
                                                              const float4 *__restrict__ node4,
                                                              uint32_t *__restrict__ bins, StepParams *sp,
-                                                             int *status)
+                                                             int *status, NLOut nl)
 {
     extern __shared__ __align__(128) unsigned char g2p_smem[];
     G2PStage *stage = reinterpret_cast<G2PStage *>(g2p_smem);
@@ -696,7 +779,8 @@ __global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(const __grid_consta
             } else {
                 const int mk = BATCH ? find_member(bv.elem_off, bv.count, e) : 0;
                 const MemberM &M = BATCH ? bv.m[mk] : m0;
-                new_key = g2p_particle<MATERIAL>(M, sentinel, node4, e - M.e0, a4, b4, c4, d4, dst, D, cell_dst);
+                new_key = g2p_particle<MATERIAL>(M, sentinel, node4, e - M.e0, a4, b4, c4, d4, dst, D, cell_dst,
+                                                 i, nl);
             }
         }
         // the next step's bins, by destination position (the binning's first phase)
@@ -718,6 +802,95 @@ __global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(const __grid_consta
         k = (k + 1 == kG2PStages) ? 0 : k + 1;
     }
     mpmg_pdl_trigger();
+}
+
+// g_nonlocal_mu2 element blocks and right-hand sides (g_nonlocal_mu2.c:418-507)
+// from the stored particles of this step's binned order: start-of-step shape
+// functions (the local coordinates still in S.A), updated volume, dense flag,
+// local fluidity and cooperativity from the G2P.  FP32 sums of an element's
+// few particles, stored in FP64 for the solver.
+__device__ __forceinline__ int sym_index_m(int a, int b)
+{
+    if (a > b) {
+        const int t = a;
+        a = b;
+        b = t;
+    }
+    const int row_start[4] = {0, 4, 7, 9};
+    return row_start[a] + (b - a);
+}
+
+__global__ void __launch_bounds__(128) mx_assemble_kernel(int ne, float inv_h, const int *__restrict__ cell_start,
+                                                          const uint32_t *__restrict__ perm,
+                                                          const float4 *__restrict__ SA, NLOut nl,
+                                                          double *__restrict__ elem_k, double *__restrict__ elem_f)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int k0 = cell_start[e], k1 = cell_start[e + 1];
+    if (k0 == k1) return;
+    float K[10], F[4];
+#pragma unroll
+    for (int k = 0; k < 10; k++) K[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = 0.0f;
+    for (int k = k0; k < k1; k++) {
+        const uint32_t i = perm[k];
+        const float4 f4 = nl.F[i];
+        if (f4.x == 0.0f) continue;      // not dense
+        const float4 a4 = SA[i];
+        const float a = a4.x, b = a4.y, ox = 1.0f - a, oy = 1.0f - b;
+        const float sf[4] = {ox * oy, a * oy, a * b, ox * b};
+        const float gx[4] = {-oy * inv_h, oy * inv_h, b * inv_h, -b * inv_h};
+        const float gy[4] = {-ox * inv_h, -a * inv_h, a * inv_h, ox * inv_h};
+        const float vol = f4.w, xi = f4.z, fv = vol * f4.y * xi;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            F[r] += fv * sf[r];
+#pragma unroll
+            for (int c = r; c < 4; c++) K[sym_index_m(r, c)] += vol * (xi * sf[r] * sf[c] + (gx[r] * gx[c] + gy[r] * gy[c]));
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 10; k++) elem_k[(size_t)k * ne + e] = (double)K[k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) elem_f[(size_t)k * ne + e] = (double)F[k];
+}
+
+// After the solve: the nodal fluidity at each particle's start-of-step
+// position (g_nonlocal_mu2.c:545-564) and the stress update (:160-218),
+// written over the record the G2P put at the particle's new position.
+__global__ void __launch_bounds__(256) mx_fluidity_stress_kernel(GeomM g, MatF mp, int n, Buf S, Buf D,
+                                                                 const uint32_t *__restrict__ rank,
+                                                                 const int *__restrict__ cell_src,
+                                                                 const double *__restrict__ node_gf, NLOut nl)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int e = cell_src[i];
+    if (e >= g.ne) return;
+    const uint32_t dst = rank[i];
+    const int cj = (int)mpmg_div((uint32_t)e, g.div_Ex), ci = e - cj * g.Ex;
+    const int n0 = cj * g.Nx + ci;
+    const float4 a4 = S.A[i], b4 = S.B[i];
+    const float syy0 = S.C[i].x, gp0 = S.D[i].x;
+    const float a = a4.x, b = a4.y, ox = 1.0f - a, oy = 1.0f - b;
+    const float gf = (float)node_gf[n0] * (ox * oy) + (float)node_gf[n0 + 1] * (a * oy) +
+                     (float)node_gf[n0 + 1 + g.Nx] * (a * b) + (float)node_gf[n0 + g.Nx] * (ox * b);
+    const float4 e4 = nl.E[i], f4 = nl.F[i];
+    float p_tr, t0xx, t0xy, t0yy, tau_tr;
+    nonlocal_mu2_trial_f(mp, e4.x, e4.y, e4.z, e4.w, b4.z, b4.w, syy0, p_tr, t0xx, t0xy, t0yy, tau_tr);
+    float sxx, sxy, syy, gp = gp0, gdp;
+    nonlocal_mu2_stress_f(mp, f4.x, gf, p_tr, t0xx, t0xy, t0yy, tau_tr, sxx, sxy, syy, gp, gdp);
+    float *Bd = reinterpret_cast<float *>(D.B + dst);
+    float *Cd = reinterpret_cast<float *>(D.C + dst);
+    float *Dd = reinterpret_cast<float *>(D.D + dst);
+    Bd[2] = sxx;
+    Bd[3] = sxy;
+    Cd[0] = syy;
+    Dd[0] = gp;
+    Dd[1] = gdp;
+    Dd[3] = gf;
 }
 
 inline int blocks_for(size_t n, int threads)
@@ -788,6 +961,8 @@ MatF make_mat(const mpmg_config &c)
     p.inv_grains_rho = rho != 0.0 ? (float)(1.0 / rho) : 0.0f;
     p.alpha_coef = d != 0.0 ? (float)(G * c.mp[MPMG_MP_I0] * c.dt / d) : 0.0f;
     p.inv_G_dt = (G * c.dt) != 0.0 ? (float)(1.0 / (G * c.dt)) : 0.0f;
+    const double A = c.mp[MPMG_MP_A];
+    p.inv_A2d2 = (A * A * d * d) != 0.0 ? (float)(1.0 / (A * A * d * d)) : 0.0f;
     return p;
 }
 
@@ -843,11 +1018,12 @@ void locate(const mpmg_config &c, double x, double y, int *cell, float *xl, floa
 }
 
 using G2PKernel = void (*)(MemberM, BatchView, int, int, const uint32_t *, Buf, Buf, const int *, int *,
-                          const float4 *, uint32_t *, StepParams *, int *);
+                          const float4 *, uint32_t *, StepParams *, int *, NLOut);
 
 G2PKernel g2p_variant(int material, bool batch)
 {
     if (material == MPMG_ISOLIN) return batch ? mx_g2p_kernel<MPMG_ISOLIN, true> : mx_g2p_kernel<MPMG_ISOLIN, false>;
+    if (material == MPMG_G_NONLOCAL_MU2) return mx_g2p_kernel<MPMG_G_NONLOCAL_MU2, false>;
     return batch ? mx_g2p_kernel<MPMG_G_LOCAL_MU2, true> : mx_g2p_kernel<MPMG_G_LOCAL_MU2, false>;
 }
 
@@ -856,8 +1032,9 @@ G2PKernel g2p_variant(int material, bool batch)
 int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const double *x, const double *y,
                     const double *vx, const double *vy, const double *sxx, const double *sxy, const double *syy)
 {
-    if (ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2) {
-        mpmg_set_error("mixed precision supports isolin and g_local_mu2");
+    const int mat = ctx->cfg.material;
+    if (mat != MPMG_ISOLIN && mat != MPMG_G_LOCAL_MU2 && !(mat == MPMG_G_NONLOCAL_MU2 && ctx->batch == nullptr)) {
+        mpmg_set_error("mixed precision supports isolin, g_local_mu2 and (outside batches) g_nonlocal_mu2");
         return MPMG_ERR_UNSUPPORTED;
     }
     MixedState *s = new MixedState();
@@ -874,6 +1051,16 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     if ((rc = dalloc(&s->node4, ctx->nn)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->node_mass, ctx->nn)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->export_buf, n)) != MPMG_OK) return rc;
+    if (mat == MPMG_G_NONLOCAL_MU2) {
+        // the fluidity solve: FP64 nodal mass (unknown mask), nodal fluidity,
+        // element blocks and Krylov vectors, and the per-particle G2P values
+        if ((rc = dalloc(&s->nl_E, n)) != MPMG_OK) return rc;
+        if ((rc = dalloc(&s->nl_F, n)) != MPMG_OK) return rc;
+        if ((rc = dalloc(&ctx->node_m, ctx->nn)) != MPMG_OK) return rc;
+        if ((rc = dalloc(&ctx->node_gf, ctx->nn)) != MPMG_OK) return rc;
+        MPMG_CHECK(cudaMemset(ctx->node_gf, 0, ctx->nn * sizeof(double)));
+        if ((rc = mpmg_nonlocal_init(ctx)) != MPMG_OK) return rc;
+    }
     MPMG_CHECK(cudaMemset(s->node_mass, 0, ctx->nn * sizeof(float2)));
 
     // members: one, or the batch's (their constants and first-index tables)
@@ -928,8 +1115,7 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     // most one per tile
     int sms = 0, per_sm = 0;
     MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
-    void (*g2p)(MemberM, BatchView, int, int, const uint32_t *, Buf, Buf, const int *, int *, const float4 *,
-                uint32_t *, StepParams *, int *) = g2p_variant(ctx->cfg.material, bt != nullptr);
+    G2PKernel g2p = g2p_variant(ctx->cfg.material, bt != nullptr);
     MPMG_CHECK(cudaFuncSetAttribute(g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG2PSmem));
     MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g2p, kG2PTile, kG2PSmem));
     const size_t tiles = (n + kG2PTile - 1) / kG2PTile;
@@ -954,6 +1140,8 @@ void mpmg_mixed_free(mpmg_ctx *ctx)
     cudaFree(s->node4);
     cudaFree(s->node_mass);
     cudaFree(s->export_buf);
+    cudaFree(s->nl_E);
+    cudaFree(s->nl_F);
     delete s;
     ctx->mixed = nullptr;
 }
@@ -1007,19 +1195,34 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     const bool f64 = c.precision == MPMG_PRECISION_MIXED_F64NODE;
     auto grid = f64 ? (batch ? mx_grid_kernel<true, true> : mx_grid_kernel<true, false>)
                     : (batch ? mx_grid_kernel<false, true> : mx_grid_kernel<false, false>);
+    const bool nonlocal = c.material == MPMG_G_NONLOCAL_MU2;
     MPMG_CHECK(mpmg_launch_pdl(true, grid, dim3(blocks_for(ctx->nn, 256)), dim3(256), 0, st, m0, bv, ne, nn,
                                (const int *)ctx->cell_start, (const float *)s->cell_sums,
                                (const StepParams *)ctx->d_params, (float)MPMG_TOL, s->node_mass, s->node4,
-                               ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy));
+                               ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy,
+                               nonlocal ? ctx->node_m : (double *)nullptr));
     mpmg_phase_end(ctx, PH_GRID);
 
     mpmg_phase_begin(ctx, PH_G2P);
     MPMG_CHECK(mpmg_launch_pdl(true, g2p_variant(c.material, batch), dim3(s->g2p_blocks), dim3(kG2PTile),
                                kG2PSmem, st, m0, bv, ne, n, (const uint32_t *)ctx->bin.rank, S, D,
                                (const int *)cell_array(ctx, cur), cell_array(ctx, nxt), (const float4 *)s->node4,
-                               ctx->bin.counts, ctx->d_params, ctx->d_status));
+                               ctx->bin.counts, ctx->d_params, ctx->d_status, NLOut{s->nl_E, s->nl_F}));
     mpmg_phase_end(ctx, PH_G2P);
     ctx->launches += 3;
+    if (nonlocal) {
+        // the fluidity solve (FP64 Krylov) and the stress update
+        mpmg_phase_begin(ctx, PH_FLUIDITY);
+        mx_assemble_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(
+            ne, m0.g.inv_hf, ctx->cell_start, ctx->perm, S.A, NLOut{s->nl_E, s->nl_F}, ctx->elem_k, ctx->elem_f);
+        rc = mpmg_launch_solve(ctx);
+        if (rc != MPMG_OK) return rc;
+        mx_fluidity_stress_kernel<<<blocks_for(n, 256), 256, 0, st>>>(m0.g, m0.mat, n, S, D, ctx->bin.rank,
+                                                                      cell_array(ctx, cur), ctx->node_gf,
+                                                                      NLOut{s->nl_E, s->nl_F});
+        mpmg_phase_end(ctx, PH_FLUIDITY);
+        ctx->launches += 2;
+    }
     s->cur = nxt;
     MPMG_CHECK(cudaGetLastError());
     return MPMG_OK;
@@ -1062,7 +1265,7 @@ bool field_slot(const char *name, int *rec, int *comp)
     struct { const char *n; int r, c; } f[] = {
         {"vx", 0, 2}, {"vy", 0, 3}, {"m", 1, 0}, {"v", 1, 1}, {"sxx", 1, 2}, {"sxy", 1, 3}, {"Txx", 1, 2},
         {"Txy", 1, 3}, {"Tyx", 1, 3}, {"syy", 2, 0}, {"Tyy", 2, 0}, {"ux", 2, 1}, {"uy", 2, 2}, {"Tzz", 2, 3},
-        {"state9", 3, 0}, {"state10", 3, 1}};
+        {"state9", 3, 0}, {"state10", 3, 1}, {"state3", 3, 3}};
     for (auto &e : f) {
         if (strcmp(name, e.n) == 0) {
             *rec = e.r;

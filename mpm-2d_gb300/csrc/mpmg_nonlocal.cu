@@ -461,32 +461,16 @@ void mpmg_nonlocal_free(mpmg_ctx *ctx)
     ctx->cg_barrier = nullptr;
 }
 
-int mpmg_launch_fluidity(mpmg_ctx *ctx)
+// The fluidity solve on the assembled element blocks (ctx->elem_k,
+// ctx->elem_f): one cooperative launch of the PCG; the nodal fluidity lands
+// in ctx->node_gf, unknowns are the nodes with ctx->node_m above the
+// material's threshold.
+int mpmg_launch_solve(mpmg_ctx *ctx)
 {
     cudaStream_t s = ctx->stream;
     const mpmg_config &c = ctx->cfg;
     const bool mu2 = c.material == MPMG_G_NONLOCAL_MU2;
-    const int n = (int)ctx->np, ne = (int)ctx->ne;
-    mat::NonlocalParams np;
-    np.E = c.mp[MPMG_MP_E];
-    np.nu = c.mp[MPMG_MP_NU];
-    np.mu_s = c.mp[MPMG_MP_MU_S];
-    np.grains_rho = c.mp[MPMG_MP_GRAINS_RHO];
-    np.B = c.mp[MPMG_MP_B];
-    np.A = c.mp[MPMG_MP_A];
-    np.grains_d = c.mp[MPMG_MP_GRAINS_D];
-    np.cohesion = c.mp[MPMG_MP_COHESION];
-    if (!mu2) {
-        nonlocal_bulk_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, np, ctx->sxx, ctx->sxy, ctx->syy,
-                                                                ctx->state[4], ctx->state[5], ctx->state[10]);
-        ctx->launches += 1;
-    }
-    const double *xisq = mu2 ? ctx->state[6] : ctx->state[10];
-    assemble_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(ne, ctx->Ex, ctx->inv_h, mu2 ? 1 : 0, ctx->cell_start,
-                                                        ctx->perm, ctx->xl, ctx->yl, ctx->v, ctx->state[0],
-                                                        ctx->state[5], xisq, ctx->elem_k, ctx->elem_f);
-    ctx->launches += 1;
-
+    const int ne = (int)ctx->ne;
     SolveArgs S;
     S.Nx = c.Nx;
     S.Ny = c.Ny;
@@ -519,6 +503,39 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_kernel, dim3(ctx->cg_blocks),
                                            dim3(kSolveThreads), args, 0, s));
     ctx->launches += 1;
+
+    MPMG_CHECK(cudaGetLastError());
+    return MPMG_OK;
+}
+
+int mpmg_launch_fluidity(mpmg_ctx *ctx)
+{
+    cudaStream_t s = ctx->stream;
+    const mpmg_config &c = ctx->cfg;
+    const bool mu2 = c.material == MPMG_G_NONLOCAL_MU2;
+    const int n = (int)ctx->np, ne = (int)ctx->ne;
+    mat::NonlocalParams np;
+    np.E = c.mp[MPMG_MP_E];
+    np.nu = c.mp[MPMG_MP_NU];
+    np.mu_s = c.mp[MPMG_MP_MU_S];
+    np.grains_rho = c.mp[MPMG_MP_GRAINS_RHO];
+    np.B = c.mp[MPMG_MP_B];
+    np.A = c.mp[MPMG_MP_A];
+    np.grains_d = c.mp[MPMG_MP_GRAINS_D];
+    np.cohesion = c.mp[MPMG_MP_COHESION];
+    if (!mu2) {
+        nonlocal_bulk_kernel<<<blocks_for(n, 256), 256, 0, s>>>(n, np, ctx->sxx, ctx->sxy, ctx->syy,
+                                                                ctx->state[4], ctx->state[5], ctx->state[10]);
+        ctx->launches += 1;
+    }
+    const double *xisq = mu2 ? ctx->state[6] : ctx->state[10];
+    assemble_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(ne, ctx->Ex, ctx->inv_h, mu2 ? 1 : 0, ctx->cell_start,
+                                                        ctx->perm, ctx->xl, ctx->yl, ctx->v, ctx->state[0],
+                                                        ctx->state[5], xisq, ctx->elem_k, ctx->elem_f);
+    ctx->launches += 1;
+
+    int rc = mpmg_launch_solve(ctx);
+    if (rc != MPMG_OK) return rc;
 
     mat::Elastic el;
     el.G = ctx->G;

@@ -143,6 +143,56 @@ def test_mixed_column_runout_within_1pct():
     assert abs(xm - xf) <= 0.01 * xf, (xm, xf)
 
 
+def nonlocal_silo(cells=32):
+    # the pre-stressed nonlocal silo of the golden fixtures: lithostatic syy,
+    # no particle at p = 0 where the dense flag switches on round-off
+    sc = scenes.silo(cells=cells, material="g_nonlocal_mu2", props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+                     open_time=0.001, wall_frac=0.5, fill_height=0.6)
+    y = sc["particles"]["y"]
+    sc["particles"]["syy"] = -2450 * 9.8 * (0.6 - y) - 500.0
+    sc["particles"]["sxx"] = 0.5 * sc["particles"]["syy"]
+    return sc
+
+
+def test_mixed_nonlocal_vs_fp64_after_100_steps():
+    sc = nonlocal_silo()
+    mixed = mpm2d.Simulation(sc, precision="mixed")
+    fp64 = mpm2d.Simulation(sc, precision="fp64")
+    mixed.step(100)
+    fp64.step(100)
+    rc, it, res = mixed.last_solve()
+    assert rc == 0 and res <= 1e-10
+    for f in FIELDS:
+        assert group_rel_l2(mixed.get, fp64.get, f) <= 1e-4, f
+    # the nodal fluidity of the last solve
+    ga, gb = mixed.get("node_gf"), fp64.get("node_gf")
+    assert np.linalg.norm(ga - gb) <= 1e-3 * np.linalg.norm(gb)
+
+
+def test_mixed_nonlocal_silo_discharge_within_fp64_spread():
+    # The nonlocal silo's discharge is chaotic at the FP64 level: 1e-9 m
+    # perturbations of the fill change the FP64 form's rate by several per
+    # cent (the nodal fluidity undershoots below zero near the outlet and
+    # the stress update p / (p + G dt gf) then swings).  The mixed form's
+    # rate must lie within the FP64 form's own spread over perturbed fills,
+    # widened by 1 %.
+    def silo(seed):
+        sc = scenes.silo(cells=32, material="g_nonlocal_mu2", props=(1e6, 0.3), dt=1e-4, hole_radius=0.12,
+                         open_time=0.05, wall_frac=0.5, fill_height=0.5, mp={"grains_d": 5.3e-4})
+        if seed is not None:
+            rng = np.random.default_rng(seed)
+            sc["particles"]["x"] = sc["particles"]["x"] + 1e-9 * rng.uniform(-1, 1, size=sc["particles"]["x"].shape)
+        return sc
+
+    sc = silo(None)
+    m = sc["particles"]["m"]
+    qf = [discharge_rate(active_mass_history(mpm2d.Simulation(silo(sd), precision="fp64"), m, 3000, 50))
+          for sd in (None, 0, 2)]
+    qm = discharge_rate(active_mass_history(mpm2d.Simulation(sc, precision="mixed"), m, 3000, 50))
+    assert min(qf) > 0
+    assert 0.99 * min(qf) <= qm <= 1.01 * max(qf), (qm, qf)
+
+
 def test_mixed_deterministic():
     sc = column_scene()
     runs = []
