@@ -23,6 +23,7 @@
 #define MPM_GB300_H
 
 #include <stddef.h>
+#include <stdio.h>
 
 #if defined(__GNUC__)
 #define MPMG_API __attribute__((visibility("default")))
@@ -157,6 +158,21 @@ MPMG_API int mpmg_get_field(mpmg_ctx *ctx, const char *name, double *host_out);
    m v x y x_t y_t sxx sxy syy ux uy state[9] state[10].  host_out[k]
    receives names[k]. */
 MPMG_API int mpmg_get_fields(mpmg_ctx *ctx, int count, const char *const *names, double *const *host_out);
+
+/* The driver's output files.  mpmg_write_frame writes one write_frame block
+   (src/writer.c:190-201: a "frame t n" line, then write_particle's row per
+   particle, src/writer.c:169-186) to fd, formatted on several host threads
+   from one batched device read.  mpmg_write_state writes write_state's file
+   (src/writer.c:266-380) with every value in %.17g, so that a restart is
+   exact; mpmg_read_state reads such a file (and the reference's own, in
+   %lg) into a new context whose grid size, spacing and dt come from the
+   file and the rest from base (read_state, src/reader.c:123-243, which also
+   fails to allocate job->active; here activity is restored with the
+   particles).  Color, the deformation gradient and the CPDI corners are
+   written as mpm_init leaves them (0, identity, 0). */
+MPMG_API int mpmg_write_frame(mpmg_ctx *ctx, FILE *fd, size_t frame, double t);
+MPMG_API int mpmg_write_state(mpmg_ctx *ctx, FILE *fd, double t_stop);
+MPMG_API int mpmg_read_state(FILE *fd, const mpmg_config *base, mpmg_ctx **out);
 MPMG_API int mpmg_set_field(mpmg_ctx *ctx, const char *name, const double *host_in);
 
 /* Element of each particle (-1 outside) and active flags

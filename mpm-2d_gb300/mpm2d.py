@@ -81,6 +81,9 @@ def lib(build_if_missing=True):
         L.mpmg_batch_count.argtypes = [vp, ip]
         L.mpmg_batch_member.argtypes = [vp, C.c_int] + [C.POINTER(C.c_size_t)] * 6
         L.mpmg_batch_get_time.argtypes = [vp, C.c_int, dp, ip]
+        L.mpmg_write_frame.argtypes = [vp, vp, C.c_size_t, C.c_double]
+        L.mpmg_write_state.argtypes = [vp, vp, C.c_double]
+        L.mpmg_read_state.argtypes = [vp, C.POINTER(Config), C.POINTER(vp)]
         L.mpmg_adj_forward_tape.argtypes = [vp, C.c_int, C.c_int]
         L.mpmg_adj_backward.argtypes = [vp, dp, dp, dp]
         L.mpmg_adj_state.argtypes = [vp, C.c_char_p, dp]
@@ -111,6 +114,30 @@ def _check(rc):
     if rc != 0:
         L = lib()
         raise MpmError(rc, "%s (%s)" % (L.mpmg_status_string(rc).decode(), L.mpmg_last_error().decode()))
+
+
+def _libc():
+    c = C.CDLL(None)
+    c.fopen.restype = C.c_void_p
+    c.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    c.fclose.argtypes = [C.c_void_p]
+    return c
+
+
+class _File:
+    """A C FILE* for the frame and state entry points."""
+
+    def __init__(self, path, mode):
+        self.libc = _libc()
+        self.fp = self.libc.fopen(str(path).encode(), mode.encode())
+        if not self.fp:
+            raise OSError("cannot open %s" % path)
+
+    def __enter__(self):
+        return self.fp
+
+    def __exit__(self, *exc):
+        self.libc.fclose(self.fp)
 
 
 def _dptr(a):
@@ -201,6 +228,35 @@ class Simulation:
         out = np.empty(n)
         _check(lib().mpmg_get_field(self._h, name.encode(), _dptr(out)))
         return out
+
+    def write_frame(self, path, frame, t=None, mode="w"):
+        """Append one write_frame block (the driver's particle output) to path."""
+        if t is None:
+            t = self.t
+        with _File(path, mode) as fp:
+            _check(lib().mpmg_write_frame(self._h, fp, frame, t))
+
+    def write_state(self, path, t_stop=0.0):
+        """The driver's state (restart) file, exact to FP64."""
+        with _File(path, "w") as fp:
+            _check(lib().mpmg_write_state(self._h, fp, t_stop))
+
+    @classmethod
+    def read_state(cls, path, scene, precision="fp64", device=0, store_transients=False):
+        """A simulation restarted from a state file; material and boundary
+        conditions come from scene (its grid and dt come from the file)."""
+        cfg = make_config(scene, store_transients, device=device, precision=precision)
+        h = C.c_void_p()
+        with _File(path, "r") as fp:
+            _check(lib().mpmg_read_state(fp, C.byref(cfg), C.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        self.precision = precision
+        self.scene = scene
+        npart, nn, ne = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        _check(lib().mpmg_sizes(self._h, C.byref(npart), C.byref(nn), C.byref(ne)))
+        self.n, self.nn, self.ne = npart.value, nn.value, ne.value
+        return self
 
     def adj_forward_tape(self, nsteps, checkpoint_every=100):
         """Advance nsteps FP64 steps keeping checkpoints for mpmg_adj_backward."""

@@ -1,0 +1,95 @@
+"""Frame and state files (mpmg_write_frame, mpmg_write_state,
+mpmg_read_state) against the reference driver's formats (src/writer.c,
+src/reader.c): a restart from a state file continues bit for bit in the FP64
+form, and frame rows carry write_particle's columns."""
+import numpy as np
+import pytest
+
+import mpm2d
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy")
+
+
+@pytest.mark.parametrize("which", ["isolin", "mu2_column"])
+def test_fp64_restart_is_exact(tmp_path, which):
+    if which == "isolin":
+        sc = scenes.config1(seed=2)
+        fields = FIELDS
+    else:
+        sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2", rho=2450.0,
+                           props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+        fields = FIELDS + ("Tzz", "state9", "state10")
+    a = mpm2d.Simulation(sc)
+    a.step(60)
+    path = tmp_path / "state.txt"
+    a.write_state(path, t_stop=1.0)
+    a.step(40)
+    b = mpm2d.Simulation.read_state(path, sc)
+    b.step(40)
+    assert b.t == a.t
+    for f in fields:
+        np.testing.assert_array_equal(b.get(f), a.get(f), err_msg=f)
+    ea, aa = a.get_map()
+    eb, ab = b.get_map()
+    np.testing.assert_array_equal(ab, aa)
+    np.testing.assert_array_equal(eb, ea)
+
+
+def test_restart_keeps_retired_particles_retired(tmp_path):
+    # a silo that has discharged: particles below the floor are inactive
+    sc = scenes.silo(cells=32, material="g_local_mu2", props=(1e6, 0.3), dt=1e-4, hole_radius=0.12,
+                     open_time=0.0, wall_frac=0.5, fill_height=0.5, gravity=-9.8)
+    a = mpm2d.Simulation(sc)
+    a.step(1500)
+    _, act = a.get_map()
+    assert (act == 0).any()
+    path = tmp_path / "state.txt"
+    a.write_state(path)
+    b = mpm2d.Simulation.read_state(path, sc)
+    np.testing.assert_array_equal(b.get_map()[1], act)
+    a.step(20)
+    b.step(20)
+    np.testing.assert_array_equal(b.get("y"), a.get("y"))
+
+
+def test_mixed_state_round_trip(tmp_path):
+    sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2", rho=2450.0,
+                       props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+    a = mpm2d.Simulation(sc, precision="mixed")
+    a.step(50)
+    path = tmp_path / "state.txt"
+    a.write_state(path)
+    b = mpm2d.Simulation.read_state(path, sc, precision="mixed")
+    for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "Tzz", "state9"):
+        np.testing.assert_array_equal(b.get(f), a.get(f), err_msg=f)
+    assert b.t == a.t
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_frame_rows(tmp_path, precision):
+    sc = scenes.config1(seed=4)
+    s = mpm2d.Simulation(sc, precision=precision)
+    s.step(30)
+    path = tmp_path / "frames.txt"
+    s.write_frame(path, 7)
+    s.step(10)
+    s.write_frame(path, 8, mode="a")
+    lines = path.read_text().splitlines()
+    n = s.n
+    assert len(lines) == 2 * (n + 1)
+    head = lines[n + 1].split()
+    assert int(head[0]) == 8 and int(head[2]) == n and abs(float(head[1]) - s.t) <= 1e-6 * s.t
+    rows = np.array([[float(v) for v in ln.split()] for ln in lines[n + 2:]])
+    assert rows.shape == (n, 23)
+    cols = {"m": 0, "v": 1, "x": 2, "y": 3, "vx": 4, "vy": 5, "sxx": 6, "sxy": 7, "syy": 8, "ux": 9, "uy": 10}
+    for f, c in cols.items():
+        ref = s.get(f)
+        # %lg keeps six significant digits
+        np.testing.assert_allclose(rows[:, c], ref, rtol=6e-6, atol=1e-300 + 6e-6 * np.abs(ref).max() * 1e-3,
+                                   err_msg=f)
+    _, act = s.get_map()
+    np.testing.assert_array_equal(rows[:, 14], act)
+    assert np.all(rows[:, 12] == 0) and np.all(rows[:, 15:] == 0)
