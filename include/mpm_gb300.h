@@ -86,6 +86,19 @@ enum mpmg_precision {
     MPMG_PRECISION_MIXED_F64NODE = 2
 };
 
+/* Step scheme.  MPMG_SCHEME_USL is explicit_mpm_step_usl_threaded
+   (process_usl.c:465-592).  MPMG_SCHEME_MUSL is
+   explicit_mpm_step_musl_threaded (process_usl.c:284-462): after the particles
+   move, their updated momentum is mapped to the nodes again with the
+   start-of-step shape functions, and the strain rate uses the nodal
+   velocities of that second projection (the reference applies its momentum
+   boundary conditions only after those velocities are formed, and so does
+   this library).  MUSL runs in the FP64 form, for isolin and g_local_mu2. */
+enum mpmg_scheme {
+    MPMG_SCHEME_USL = 0,
+    MPMG_SCHEME_MUSL = 1
+};
+
 /* Material parameter slots (mpmg_config.mp).  mpmg_default_params fills the
    reference's compile-time constants for a material kind. */
 enum mpmg_mparam {
@@ -119,6 +132,7 @@ typedef struct mpmg_config {
                                 residual cannot see, where the reference's direct
                                 solve gives zero. */
     int precision;           /* enum mpmg_precision */
+    int scheme;              /* enum mpmg_scheme */
 } mpmg_config;
 
 typedef struct mpmg_ctx mpmg_ctx;

@@ -16,6 +16,7 @@
  * Entry points (reference declarations they replace):
  *   mpm_init                          libmpm/process_usl.c:68   (process.h:251)
  *   explicit_mpm_step_usl_threaded    libmpm/process_usl.c:465  (process_usl.h:15)
+ *   explicit_mpm_step_musl_threaded   libmpm/process_usl.c:284  (process_usl.h:13)
  *   find_filled_elements              libmpm/process_usl.c:677  (process_usl.h:18)
  *   mpm_cleanup                       libmpm/process_usl.c:974  (process.h:253)
  *   initial_loads, time_varying_loads libmpm/loading.c:21,34
@@ -257,6 +258,10 @@ MPMG_API job_t *mpm_init(int N, double h, particle_t *particles, size_t num_part
  * fluidity solve, EXIT_ERROR_MATERIAL_FILE for an unsupported plugin).
  */
 MPMG_API void explicit_mpm_step_usl_threaded(void *task);
+/* The MUSL step (second projection of the moved particles' momentum before
+   the strain rate); the job's GPU context is created with the scheme of the
+   first step entry called. */
+MPMG_API void explicit_mpm_step_musl_threaded(void *task);
 
 /* The reference's per-(thread, colour) particle lists (host; the driver calls
    it once before the time loop). */

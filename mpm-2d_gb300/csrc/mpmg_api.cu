@@ -379,6 +379,16 @@ int validate_config(const mpmg_config *cfg, size_t n)
         mpmg_set_error("unknown precision %d", cfg->precision);
         return MPMG_ERR_INVALID;
     }
+    if (cfg->scheme != MPMG_SCHEME_USL && cfg->scheme != MPMG_SCHEME_MUSL) {
+        mpmg_set_error("unknown step scheme %d", cfg->scheme);
+        return MPMG_ERR_INVALID;
+    }
+    if (cfg->scheme == MPMG_SCHEME_MUSL &&
+        (cfg->precision != MPMG_PRECISION_FP64 ||
+         (cfg->material != MPMG_ISOLIN && cfg->material != MPMG_G_LOCAL_MU2))) {
+        mpmg_set_error("the MUSL step runs in the FP64 form for isolin and g_local_mu2");
+        return MPMG_ERR_UNSUPPORTED;
+    }
     if (cfg->bc == MPMG_BOX) {
         // box.c:42-96 bc_validate
         double x0 = cfg->bcf[0], y0 = cfg->bcf[1], w = cfg->bcf[2], hh = cfg->bcf[3];
@@ -524,11 +534,11 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             TRY(dalloc(&ctx->ax, n));
             TRY(dalloc(&ctx->ay, n));
         }
-        if (transients || nonlocal) {
+        if (transients || nonlocal || cfg->scheme == MPMG_SCHEME_MUSL) {
             double **sr[] = {&ctx->exx, &ctx->exy, &ctx->eyy, &ctx->wxy};
             for (double **p : sr) TRY(dalloc(p, n));
         }
-        if (transients || nonlocal) {
+        if (transients || nonlocal || cfg->scheme == MPMG_SCHEME_MUSL) {
             TRY(dalloc(&ctx->xl, n));
             TRY(dalloc(&ctx->yl, n));
         }

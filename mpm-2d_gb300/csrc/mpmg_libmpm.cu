@@ -280,6 +280,11 @@ void time_varying_loads(job_t *job)
     }
 }
 
+// The step scheme a job's context is created with: the entry point the
+// driver calls decides (explicit_mpm_step_usl_threaded or
+// explicit_mpm_step_musl_threaded).
+static thread_local int t_attach_scheme = MPMG_SCHEME_USL;
+
 int mpm_gpu_attach(job_t *job)
 {
     if (job == nullptr) return MPMG_ERR_INVALID;
@@ -294,6 +299,7 @@ int mpm_gpu_attach(job_t *job)
     }
     mpmg_config cfg;
     mpmg_config_init(&cfg);
+    cfg.scheme = t_attach_scheme;
     cfg.Nx = cfg.Ny = (int)job->N;
     cfg.h = job->h;
     cfg.dt = job->dt;
@@ -460,14 +466,15 @@ int mpm_gpu_detach(job_t *job)
     return mpmg_destroy(ctx);
 }
 
-void explicit_mpm_step_usl_threaded(void *arg)
+static void threaded_step(threadtask_t *task, int scheme)
 {
-    threadtask_t *task = (threadtask_t *)arg;
     job_t *job = task->job;
     int serial = (job->serialize_barrier == NULL) ? 1 : (pthread_barrier_wait(job->serialize_barrier) ==
                                                          PTHREAD_BARRIER_SERIAL_THREAD);
     if (serial) {
+        t_attach_scheme = scheme;
         int rc = mpm_gpu_step(job, 1);
+        t_attach_scheme = MPMG_SCHEME_USL;
         // The driver writes a frame after this step when t reaches the next
         // sample time (src/main.c:955), and the state when the run ends.
         if (rc == MPMG_OK) {
@@ -481,6 +488,16 @@ void explicit_mpm_step_usl_threaded(void *arg)
         }
     }
     if (job->serialize_barrier != NULL) pthread_barrier_wait(job->serialize_barrier);
+}
+
+void explicit_mpm_step_usl_threaded(void *arg)
+{
+    threaded_step((threadtask_t *)arg, MPMG_SCHEME_USL);
+}
+
+void explicit_mpm_step_musl_threaded(void *arg)
+{
+    threaded_step((threadtask_t *)arg, MPMG_SCHEME_MUSL);
 }
 
 void mpm_cleanup(job_t *job)

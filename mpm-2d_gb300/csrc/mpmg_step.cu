@@ -206,7 +206,13 @@ struct G2PArgs {
     double *ax, *ay, *exx, *exy, *eyy, *wxy, *xl_out, *yl_out;
 };
 
-template <int MATERIAL>
+// G2P phases.  USL (process_usl.c:465-592) runs them all in one pass; MUSL
+// (process_usl.c:284-462) runs the move first, maps the moved particles'
+// momentum to the nodes again (p2g_momentum_kernel, node_velocity_kernel),
+// then the strain phase with the nodal velocities of that second projection.
+enum { G2P_FULL = 0, G2P_MOVE = 1, G2P_STRAIN = 2 };
+
+template <int MATERIAL, int PHASE>
 __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -216,62 +222,72 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
     const int ci = e % g.Ex, cj = e / g.Ex;
     const int n0 = cj * g.Nx + ci;
     const int nd[4] = {n0, n0 + 1, n0 + 1 + g.Nx, n0 + g.Nx};
-    double px = A.x[i], py = A.y[i];
-    const double xl = mpmg_local_coord(px, ci * g.h, g.inv_h);
-    const double yl = mpmg_local_coord(py, cj * g.h, g.inv_h);
+    double xl, yl;
+    if (PHASE == G2P_STRAIN) {
+        // the start-of-step local coordinates the move phase kept
+        xl = A.xl_out[i];
+        yl = A.yl_out[i];
+    } else {
+        xl = mpmg_local_coord(A.x[i], ci * g.h, g.inv_h);
+        yl = mpmg_local_coord(A.y[i], cj * g.h, g.inv_h);
+    }
     const ShapeFns f = shape(xl, yl, g.inv_h);
+    const double dt = A.dt;
 
-    double nax[4], nay[4], nvx[4], nvy[4];
+    double nvx[4], nvy[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-        nax[a] = A.node_ax[nd[a]];
-        nay[a] = A.node_ay[nd[a]];
         nvx[a] = A.node_vx[nd[a]];
         nvy[a] = A.node_vy[nd[a]];
     }
-    // move_particles_explicit_usl_split (process_usl.c:914-957); light nodes
-    // (m <= 1e-10) carry zero acceleration and velocity.
-    double xtt = 0, ytt = 0, dux = 0, duy = 0;
+    if (PHASE != G2P_STRAIN) {
+        // move_particles_explicit_usl_split (process_usl.c:914-957); light
+        // nodes (m <= 1e-10) carry zero acceleration and velocity.
+        double xtt = 0, ytt = 0, dux = 0, duy = 0;
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            xtt += f.s[a] * A.node_ax[nd[a]];
+            ytt += f.s[a] * A.node_ay[nd[a]];
+            dux += f.s[a] * nvx[a];
+            duy += f.s[a] * nvy[a];
+        }
+        A.vx[i] += dt * xtt;
+        A.vy[i] += dt * ytt;
+        dux *= dt;
+        duy *= dt;
+        A.x[i] += dux;
+        A.y[i] += duy;
+        A.ux[i] += dux;
+        A.uy[i] += duy;
+        if (A.ax != nullptr) {
+            A.ax[i] = xtt;
+            A.ay[i] = ytt;
+        }
+        if (A.xl_out != nullptr) {
+            A.xl_out[i] = xl;
+            A.yl_out[i] = yl;
+        }
+        if (PHASE == G2P_MOVE) return;
+    }
+    // calculate_strainrate_split (process_usl.c:796-803)
     double exx = 0, eyy = 0, dxdy = 0, dydx = 0;
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-        xtt += f.s[a] * nax[a];
-        ytt += f.s[a] * nay[a];
-        dux += f.s[a] * nvx[a];
-        duy += f.s[a] * nvy[a];
-        // calculate_strainrate_split (process_usl.c:796-803)
         exx += f.gx[a] * nvx[a];
         eyy += f.gy[a] * nvy[a];
         dxdy += f.gy[a] * nvx[a];
         dydx += f.gx[a] * nvy[a];
     }
-    const double dt = A.dt;
-    A.vx[i] += dt * xtt;
-    A.vy[i] += dt * ytt;
-    dux *= dt;
-    duy *= dt;
-    A.x[i] = px + dux;
-    A.y[i] = py + duy;
-    A.ux[i] += dux;
-    A.uy[i] += duy;
     const double exy = 0.5 * (dxdy + dydx);
     const double wxy = 0.5 * (dxdy - dydx);
     // update_particle_densities_split (process_usl.c:961-970)
     double vol = A.v[i] * exp(dt * (exx + eyy));
     A.v[i] = vol;
-    if (A.ax != nullptr) {
-        A.ax[i] = xtt;
-        A.ay[i] = ytt;
-    }
     if (A.exx != nullptr) {
         A.exx[i] = exx;
         A.exy[i] = exy;
         A.eyy[i] = eyy;
         A.wxy[i] = wxy;
-    }
-    if (A.xl_out != nullptr) {
-        A.xl_out[i] = xl;
-        A.yl_out[i] = yl;
     }
 
     if (MATERIAL == MPMG_ISOLIN) {
@@ -300,6 +316,80 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
     }
     // MPMG_G_NONLOCAL computes its bulk fluidity over every particle in the
     // fluidity phase (g_nonlocal.c:306-352).
+}
+
+// MUSL's second projection (process_usl.c:424-431): per element, the moved
+// particles' mass and momentum with their start-of-step shape functions, in
+// the binned order of the step (perm is already ordered by the P2G).
+__global__ void __launch_bounds__(128) p2g_momentum_kernel(
+    int ne, double inv_h, const int *__restrict__ cell_start, const uint32_t *__restrict__ perm,
+    const double *__restrict__ xl, const double *__restrict__ yl, const double *__restrict__ m,
+    const double *__restrict__ vx, const double *__restrict__ vy, double *__restrict__ cell_sums)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int k0 = cell_start[e], k1 = cell_start[e + 1];
+    if (k0 == k1) return;
+    double acc[4][3];
+#pragma unroll
+    for (int a = 0; a < 4; a++) acc[a][0] = acc[a][1] = acc[a][2] = 0.0;
+    for (int k = k0; k < k1; k++) {
+        const int i = (int)perm[k];
+        const ShapeFns f = shape(xl[i], yl[i], inv_h);
+        const double pm = m[i], pmx = vx[i] * pm, pmy = vy[i] * pm;
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            acc[a][0] += f.s[a] * pm;
+            acc[a][1] += f.s[a] * pmx;
+            acc[a][2] += f.s[a] * pmy;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) cell_sums[(size_t)(a * 3 + q) * ne + e] = acc[a][q];
+}
+
+// MUSL nodal velocities of the second projection (process_usl.c:433-447):
+// v = p / m where m > 1e-10, else 0.  The reference zeroes the constrained
+// momenta only after forming v, so the boundary conditions do not reach v;
+// the zeroed momenta are what it keeps in the nodes (node_mx, node_my).
+__global__ void __launch_bounds__(256) node_velocity_kernel(
+    GridGeom g, BcParams bc, int ne, const int *__restrict__ cell_start, const double *__restrict__ cell_sums,
+    const StepParams *__restrict__ sp, double *__restrict__ node_m, double *__restrict__ node_vx,
+    double *__restrict__ node_vy, double *__restrict__ node_mx, double *__restrict__ node_my)
+{
+    const int nn = g.Nx * g.Ny;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    double sum[3] = {0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+        const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
+        const int e = cj * g.Ex + ci;
+        if (cell_start[e] == cell_start[e + 1]) continue;
+        const int corner = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+#pragma unroll
+        for (int q = 0; q < 3; q++) sum[q] += cell_sums[(size_t)(corner * 3 + q) * ne + e];
+    }
+    const double m = sum[0];
+    double vxn = 0, vyn = 0;
+    if (m > MPMG_TOL) {
+        vxn = sum[1] / m;
+        vyn = sum[2] / m;
+    }
+    node_m[n] = m;
+    node_vx[n] = vxn;
+    node_vy[n] = vyn;
+    if (node_mx != nullptr) {
+        bool bx, by;
+        bc_mask(bc, g, i, j, sp->t, bx, by);
+        node_mx[n] = bx ? 0.0 : sum[1];
+        node_my[n] = by ? 0.0 : sum[2];
+    }
 }
 
 __global__ void material_only_kernel(G2PArgs A, int material)
@@ -415,21 +505,36 @@ int mpmg_launch_step(mpmg_ctx *ctx)
 
     mpmg_phase_begin(ctx, PH_G2P);
     G2PArgs A = make_g2p_args(ctx);
-    switch (c.material) {
-    case MPMG_ISOLIN:
-        g2p_kernel<MPMG_ISOLIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
-        break;
-    case MPMG_G_LOCAL_MU2:
-        g2p_kernel<MPMG_G_LOCAL_MU2><<<blocks_for(n, 256), 256, 0, s>>>(A);
-        break;
-    case MPMG_G_NONLOCAL_MU2:
-        g2p_kernel<MPMG_G_NONLOCAL_MU2><<<blocks_for(n, 256), 256, 0, s>>>(A);
-        break;
-    default:
-        g2p_kernel<MPMG_G_NONLOCAL><<<blocks_for(n, 256), 256, 0, s>>>(A);
-        break;
+    if (c.scheme == MPMG_SCHEME_MUSL) {
+        // move, second projection of the moved momentum, then strain
+        if (c.material == MPMG_ISOLIN) g2p_kernel<MPMG_ISOLIN, G2P_MOVE><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        else g2p_kernel<MPMG_G_LOCAL_MU2, G2P_MOVE><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        p2g_momentum_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(ne, ctx->inv_h, ctx->cell_start, ctx->perm, ctx->xl,
+                                                                ctx->yl, ctx->m, ctx->vx, ctx->vy, ctx->cell_sums);
+        node_velocity_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(g, make_bc(ctx), ne, ctx->cell_start,
+                                                                 ctx->cell_sums, ctx->d_params, ctx->node_m,
+                                                                 ctx->node_vx, ctx->node_vy, ctx->node_mx,
+                                                                 ctx->node_my);
+        if (c.material == MPMG_ISOLIN) g2p_kernel<MPMG_ISOLIN, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        else g2p_kernel<MPMG_G_LOCAL_MU2, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        ctx->launches += 4;
+    } else {
+        switch (c.material) {
+        case MPMG_ISOLIN:
+            g2p_kernel<MPMG_ISOLIN, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_G_LOCAL_MU2:
+            g2p_kernel<MPMG_G_LOCAL_MU2, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_G_NONLOCAL_MU2:
+            g2p_kernel<MPMG_G_NONLOCAL_MU2, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        default:
+            g2p_kernel<MPMG_G_NONLOCAL, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        }
+        ctx->launches += 1;
     }
-    ctx->launches += 1;
     mpmg_phase_end(ctx, PH_G2P);
     MPMG_CHECK(cudaGetLastError());
 

@@ -46,7 +46,7 @@ class Config(C.Structure):
                 ("bci", C.c_int * 4), ("gravity_mode", C.c_int), ("gravity", C.c_double),
                 ("store_transients", C.c_int), ("solver_tol", C.c_double),
                 ("solver_maxit", C.c_int), ("device", C.c_int), ("solver_warm_start", C.c_int),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("scheme", C.c_int)]
 
 
 _lib = None
@@ -155,6 +155,7 @@ def default_params(material):
 
 
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_f64node": 2}
+SCHEMES = {"usl": 0, "musl": 1}
 
 
 def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0,
@@ -186,6 +187,7 @@ def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20
     cfg.device = device
     cfg.solver_warm_start = 1 if warm_start else 0
     cfg.precision = PRECISIONS[precision]
+    cfg.scheme = SCHEMES[scene.get("scheme", "usl")]
     return cfg
 
 

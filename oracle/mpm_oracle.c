@@ -1060,6 +1060,56 @@ static int g_nonlocal_stress(orc_sim *s)
 }
 
 /*---------------------------------------------------------------------------*/
+/* map_to_grid_explicit_split (process_usl.c:812-910; map.c:85-104): each
+   thread adds its (thread, colour) list's particles to the nodes, with a
+   barrier after each colour. */
+static void p2g_by_colour(orc_task *task)
+{
+    orc_sim *s = task->s;
+    for (int c = 0; c < NCOLORS; c++) {
+        size_t tc = task->id * NCOLORS + (size_t)c;
+        for (size_t k = 0; k < s->list_len[tc]; k++) {
+            size_t i = s->lists[tc][k];
+            const int *nn = s->enodes + 4 * s->in_element[i];
+            double sv[4] = {s->h1[i], s->h2[i], s->h3[i], s->h4[i]};
+            double pdata[7];
+            pdata[0] = s->m[i];
+            pdata[1] = s->vx[i] * s->m[i];
+            pdata[2] = s->vy[i] * s->m[i];
+            pdata[3] = s->ax[i] * s->m[i];
+            pdata[4] = s->ay[i] * s->m[i];
+            pdata[5] = s->bx[i] * s->m[i];
+            pdata[6] = s->by[i] * s->m[i];
+            double sd[3];
+            sd[0] = -s->sxx[i] * s->v[i];
+            sd[1] = -s->sxy[i] * s->v[i];
+            sd[2] = -s->syy[i] * s->v[i];
+            for (int a = 0; a < 4; a++) {
+                int nd = nn[a];
+                s->nm[nd] += sv[a] * pdata[0];
+                s->nmx[nd] += sv[a] * pdata[1];
+                s->nmy[nd] += sv[a] * pdata[2];
+                s->nmxx[nd] += sv[a] * pdata[3];
+                s->nmyy[nd] += sv[a] * pdata[4];
+                s->nfx[nd] += sv[a] * pdata[5];
+                s->nfy[nd] += sv[a] * pdata[6];
+            }
+            double d1[4] = {s->b11[i], s->b12[i], s->b13[i], s->b14[i]};
+            for (int a = 0; a < 4; a++) {
+                s->nfx[nn[a]] += d1[a] * sd[0];
+                s->nfy[nn[a]] += d1[a] * sd[1];
+            }
+            double d2[4] = {s->b21[i], s->b22[i], s->b23[i], s->b24[i]};
+            for (int a = 0; a < 4; a++) {
+                s->nfx[nn[a]] += d2[a] * sd[1];
+                s->nfy[nn[a]] += d2[a] * sd[2];
+            }
+        }
+        pthread_barrier_wait(&s->bar);
+    }
+
+}
+
 /* Thread-team phases of explicit_mpm_step_usl_threaded, process_usl.c:465-592. */
 
 static void step_thread(orc_task *task)
@@ -1149,47 +1199,7 @@ static void step_thread(orc_task *task)
     pthread_barrier_wait(&s->bar);
 
     /* P2G by colour, process_usl.c:812-910; map.c:85-104 */
-    for (int c = 0; c < NCOLORS; c++) {
-        size_t tc = task->id * NCOLORS + (size_t)c;
-        for (size_t k = 0; k < s->list_len[tc]; k++) {
-            size_t i = s->lists[tc][k];
-            const int *nn = s->enodes + 4 * s->in_element[i];
-            double sv[4] = {s->h1[i], s->h2[i], s->h3[i], s->h4[i]};
-            double pdata[7];
-            pdata[0] = s->m[i];
-            pdata[1] = s->vx[i] * s->m[i];
-            pdata[2] = s->vy[i] * s->m[i];
-            pdata[3] = s->ax[i] * s->m[i];
-            pdata[4] = s->ay[i] * s->m[i];
-            pdata[5] = s->bx[i] * s->m[i];
-            pdata[6] = s->by[i] * s->m[i];
-            double sd[3];
-            sd[0] = -s->sxx[i] * s->v[i];
-            sd[1] = -s->sxy[i] * s->v[i];
-            sd[2] = -s->syy[i] * s->v[i];
-            for (int a = 0; a < 4; a++) {
-                int nd = nn[a];
-                s->nm[nd] += sv[a] * pdata[0];
-                s->nmx[nd] += sv[a] * pdata[1];
-                s->nmy[nd] += sv[a] * pdata[2];
-                s->nmxx[nd] += sv[a] * pdata[3];
-                s->nmyy[nd] += sv[a] * pdata[4];
-                s->nfx[nd] += sv[a] * pdata[5];
-                s->nfy[nd] += sv[a] * pdata[6];
-            }
-            double d1[4] = {s->b11[i], s->b12[i], s->b13[i], s->b14[i]};
-            for (int a = 0; a < 4; a++) {
-                s->nfx[nn[a]] += d1[a] * sd[0];
-                s->nfy[nn[a]] += d1[a] * sd[1];
-            }
-            double d2[4] = {s->b21[i], s->b22[i], s->b23[i], s->b24[i]};
-            for (int a = 0; a < 4; a++) {
-                s->nfx[nn[a]] += d2[a] * sd[1];
-                s->nfy[nn[a]] += d2[a] * sd[2];
-            }
-        }
-        pthread_barrier_wait(&s->bar);
-    }
+    p2g_by_colour(task);
 
     /* serial: bc_momentum, bc_force, process_usl.c:552-567; box.c:183-224 */
     if (pthread_barrier_wait(&s->bar) == PTHREAD_BARRIER_SERIAL_THREAD) {
@@ -1259,6 +1269,39 @@ static void step_thread(orc_task *task)
         s->y[i] += duy;
         s->ux[i] += dux;
         s->uy[i] += duy;
+    }
+
+    if (s->c.scheme == ORC_MUSL) {
+        /* explicit_mpm_step_musl_threaded, process_usl.c:398-444: clear the
+           nodes, map the moved particles' momentum to them again with the
+           start-of-step shape functions, take nodal velocities from it.  The
+           reference zeroes the constrained momenta (bc_momentum) after the
+           velocities are formed, so the constraint does not reach them. */
+        pthread_barrier_wait(&s->bar);
+        for (size_t i = task->n0; i < task->n1; i++) {
+            s->nm[i] = 0; s->nmx[i] = 0; s->nmy[i] = 0; s->nmxx[i] = 0; s->nmyy[i] = 0;
+            s->nvx[i] = 0; s->nvy[i] = 0; s->nax[i] = 0; s->nay[i] = 0; s->nfx[i] = 0;
+            s->nfy[i] = 0; s->nux[i] = 0; s->nuy[i] = 0;
+        }
+        pthread_barrier_wait(&s->bar);
+        p2g_by_colour(task);
+        pthread_barrier_wait(&s->bar);
+        for (size_t i = task->n0; i < task->n1; i++) {
+            if (s->nm[i] > TOL) {
+                s->nvx[i] = s->nmx[i] / s->nm[i];
+                s->nvy[i] = s->nmy[i] / s->nm[i];
+            } else {
+                s->nvx[i] = 0;
+                s->nvy[i] = 0;
+            }
+        }
+        if (pthread_barrier_wait(&s->bar) == PTHREAD_BARRIER_SERIAL_THREAD) {
+            for (size_t i = 0; i < s->nn; i++) {
+                if (s->mask[3 * i + 0]) s->nmx[i] = 0;
+                if (s->mask[3 * i + 1]) s->nmy[i] = 0;
+            }
+        }
+        pthread_barrier_wait(&s->bar);
     }
 
     /* calculate_strainrate_split, process_usl.c:764-808 (non-CPDI branch) */

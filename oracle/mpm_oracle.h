@@ -35,6 +35,12 @@ enum orc_mparam {
     ORC_MP_COUNT = 16
 };
 
+/* Step scheme: update stress last (explicit_mpm_step_usl_threaded,
+   process_usl.c:465-592) or the modified form with a second projection of
+   the updated particle momentum (explicit_mpm_step_musl_threaded,
+   process_usl.c:284-462). */
+enum orc_scheme { ORC_USL = 0, ORC_MUSL = 1 };
+
 typedef struct orc_config {
     int Nx, Ny;          /* nodes per grid row / column */
     double h;            /* element edge length */
@@ -51,6 +57,7 @@ typedef struct orc_config {
     int solver;          /* enum orc_solver (nonlocal materials) */
     double cg_tol;       /* relative residual for ORC_SOLVER_PCG */
     int cg_maxit;
+    int scheme;          /* enum orc_scheme */
 } orc_config;
 
 typedef struct orc_sim orc_sim;
@@ -63,7 +70,7 @@ orc_sim *orc_create(const orc_config *cfg, size_t n, const double *m, const doub
                     const double *sxx, const double *sxy, const double *syy);
 void orc_destroy(orc_sim *s);
 
-/* Runs nsteps of the driver loop: USL step, then the serial tail
+/* Runs nsteps of the driver loop: USL (or MUSL) step, then the serial tail
    (time_varying_loads).  Returns 0, or a nonzero status on a solver failure. */
 int orc_step(orc_sim *s, int nsteps);
 

@@ -31,7 +31,9 @@ class OrcConfig(C.Structure):
                 ("mp", C.c_double * MP_COUNT), ("bc", C.c_int), ("bcf", C.c_double * 4),
                 ("bci", C.c_int * 4), ("gravity_mode", C.c_int), ("gravity", C.c_double),
                 ("nthreads", C.c_int), ("solver", C.c_int), ("cg_tol", C.c_double),
-                ("cg_maxit", C.c_int)]
+                ("cg_maxit", C.c_int), ("scheme", C.c_int)]
+
+SCHEMES = {"usl": 0, "musl": 1}
 
 
 _lib = None
@@ -117,6 +119,7 @@ class Oracle:
         cfg.solver = 0 if solver == "direct" else 1
         cfg.cg_tol = cg_tol
         cfg.cg_maxit = cg_maxit
+        cfg.scheme = SCHEMES[scene.get("scheme", "usl")]
         p = scene["particles"]
         self.n = len(p["x"])
         arrs = [np.ascontiguousarray(p[k], dtype=np.float64)
@@ -219,6 +222,7 @@ def ref_lib():
                                   C.c_size_t, C.c_char_p, dp, C.c_size_t, ip, C.c_size_t,
                                   C.c_double, C.c_int]
         L.refh_step.argtypes = [C.c_void_p, C.c_int]
+        L.refh_set_scheme.argtypes = [C.c_void_p, C.c_int]
         L.refh_time.argtypes = [C.c_void_p]
         L.refh_time.restype = C.c_double
         L.refh_get_particles.argtypes = [C.c_void_p, dp, ip, ip]
@@ -254,6 +258,8 @@ class RefHarness:
         self._h = L.refh_create(scene["Nx"], scene["h"], self.n, _dptr(pin), mat_so,
                                 _dptr(mprops), len(mprops), bc_so, _dptr(bprops), len(bprops),
                                 _iptr(biprops), len(biprops), scene["dt"], nthreads)
+        if self._h:
+            L.refh_set_scheme(self._h, SCHEMES[scene.get("scheme", "usl")])
         if not self._h:
             raise RuntimeError("refh_create failed")
         self.N = scene["Nx"]

@@ -36,6 +36,7 @@ void initial_loads(job_t *job);
 void time_varying_loads(job_t *job);
 
 typedef struct refh_s {
+    int musl;        /* 1: explicit_mpm_step_musl_threaded instead of the USL step */
     job_t *job;
     threadtask_t *tasks;
     int nthreads;
@@ -205,6 +206,9 @@ refh_t *refh_create(int N, double h, size_t n, const double *pin,
     return r;
 }
 
+/* The scheme of the team refh_step runs (one team at a time). */
+static int g_musl = 0;
+
 static void *run_steps(void *arg)
 {
     threadtask_t *task = (threadtask_t *)arg;
@@ -212,7 +216,11 @@ static void *run_steps(void *arg)
     /* refh_step stores the step count in job->stepcount before the team starts. */
     int nsteps = job->stepcount;
     for (int k = 0; k < nsteps; k++) {
-        explicit_mpm_step_usl_threaded(task);
+        if (g_musl) {
+            explicit_mpm_step_musl_threaded(task);
+        } else {
+            explicit_mpm_step_usl_threaded(task);
+        }
         int rc = pthread_barrier_wait(job->serialize_barrier);
         if (rc == PTHREAD_BARRIER_SERIAL_THREAD) {
             time_varying_loads(job);
@@ -222,10 +230,16 @@ static void *run_steps(void *arg)
 }
 
 /* Runs nsteps of the driver's time loop on the harness's thread team. */
+void refh_set_scheme(refh_t *r, int musl)
+{
+    r->musl = musl;
+}
+
 int refh_step(refh_t *r, int nsteps)
 {
     job_t *job = r->job;
     job->stepcount = nsteps;
+    g_musl = r->musl;
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)r->nthreads);
     for (int i = 0; i < r->nthreads - 1; i++) {
         pthread_create(&th[i], NULL, run_steps, &r->tasks[i]);

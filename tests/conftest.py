@@ -34,6 +34,8 @@ def load_golden(name):
         "gravity": None,
         "particles": {k[3:]: d[k] for k in d.files if k.startswith("in_")},
     }
+    if "meta_scheme" in d.files:
+        scene["scheme"] = str(d["meta_scheme"])
     return scene, d
 
 

@@ -14,6 +14,9 @@ compiled from its sources, see oracle/build.py) and records:
   lists_config1.npz      find_filled_elements' per-element particle order
                          after 100 steps of config 1 (one thread, so one list
                          per colour)
+  step_musl_<case>.npz   the same for explicit_mpm_step_musl_threaded
+                         (python tests/golden/gen_golden.py musl records only
+                         these)
 
 The nonlocal cases run the reference with one thread: with more, its
 g_nonlocal_mu2 solve reads particles other threads are still updating
@@ -52,6 +55,7 @@ def scene_arrays(sc):
     out["meta_bci"] = np.asarray(sc.get("bci", []), dtype=np.int64)
     out["meta_material"] = np.array(sc["material"])
     out["meta_bc"] = np.array(sc["bc"])
+    out["meta_scheme"] = np.array(sc.get("scheme", "usl"))
     return out
 
 
@@ -101,9 +105,23 @@ def kat(material):
     return path
 
 
+def musl_cases():
+    # explicit_mpm_step_musl_threaded (process_usl.c:284-462), threaded
+    sc = scenes.config1(seed=0)
+    sc["scheme"] = "musl"
+    print(record_steps("musl_config1", sc, [1, 2, 100], nthreads=4)[1])
+    sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2",
+                       rho=2450.0, props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+    sc["scheme"] = "musl"
+    print(record_steps("musl_mu2_column", sc, [1, 50, 300], nthreads=4)[1])
+
+
 def main():
     if obuild.build_ref(verbose=False) is None:
         raise SystemExit("reference tree not found; fixtures can only be generated where it exists")
+    if sys.argv[1:] == ["musl"]:
+        musl_cases()
+        return
     print(kat("isolin"))
     print(kat("g_local_mu2"))
 
@@ -158,6 +176,7 @@ def main():
     sc["particles"]["syy"] = np.full(n, -2000.0)
     sc["particles"]["sxy"] = np.full(n, 600.0)
     print(record_steps("nonlocal_silo", sc, [1, 10, 60], nthreads=1)[1])
+    musl_cases()
 
 
 if __name__ == "__main__":

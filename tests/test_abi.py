@@ -80,6 +80,11 @@ def test_invalid_configuration_is_rejected():
     z = mpm2d.np.zeros(1)
     rc = mpm2d.lib().mpmg_create(mpm2d.C.byref(cfg), 1, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h))
     assert rc == 16 and not h.value
+    cfg = mpm2d.make_config(scenes.config1())
+    cfg.scheme = 1
+    cfg.precision = 1                      # MUSL runs in the FP64 form
+    rc = mpm2d.lib().mpmg_create(mpm2d.C.byref(cfg), 1, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h))
+    assert rc == 20 and not h.value
 
 
 def test_batch_configuration_is_rejected():

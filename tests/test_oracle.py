@@ -12,7 +12,7 @@ from oracle import oracle as O
 import scenes
 
 CASES = ["config1", "mu2_column", "mu2_silo", "nonlocal_mu2_silo", "nonlocal_mu2_prestressed",
-         "nonlocal_silo"]
+         "nonlocal_silo", "musl_config1", "musl_mu2_column"]
 COMPARE = ["x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy", "exx", "exy", "eyy", "wxy",
            "ax", "ay"]
 
