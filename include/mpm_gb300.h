@@ -54,7 +54,11 @@ enum mpmg_material {
     MPMG_ISOLIN = 0,              /* materialsrc/isolin.c */
     MPMG_G_LOCAL_MU2 = 1,         /* materialsrc/g_local_mu2.c */
     MPMG_G_NONLOCAL_MU2 = 2,      /* materialsrc/g_nonlocal_mu2.c */
-    MPMG_G_NONLOCAL = 3           /* materialsrc/g_nonlocal.c */
+    MPMG_G_NONLOCAL = 3,          /* materialsrc/g_nonlocal.c */
+    MPMG_DP_RI_MT = 4,            /* materialsrc/dp_ri_mt.c */
+    MPMG_G_LOCAL_MU2_PLANE_STRAIN = 5,  /* materialsrc/g_local_mu2_plane_strain.c */
+    MPMG_G_LOCAL_MU2_TRUE_2D = 6,       /* materialsrc/g_local_mu2_true_2d.c */
+    MPMG_G_LOCAL_MU2_EXT = 7            /* materialsrc/g_local_mu2_ext.c */
 };
 
 /* Boundary-condition kinds: the reference plugins with a device implementation. */

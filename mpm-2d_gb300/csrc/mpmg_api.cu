@@ -52,6 +52,14 @@ bool material_uses_state(int material, int k)
         return k == 0 || k == 3 || k == 4 || k == 5 || k == 6 || k == 9 || k == 10;
     case MPMG_G_NONLOCAL:       // g_nonlocal.c:51-61
         return k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
+    case MPMG_DP_RI_MT:         // dp_ri_mt.c:27-29 (szz, gammap, gammadotp)
+        return k == 1 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_PLANE_STRAIN:   // g_local_mu2_plane_strain.c:43-51 (szz, beta, gammap, gammadotp)
+        return k == 1 || k == 5 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_TRUE_2D:        // g_local_mu2_true_2d.c:43-51 (beta, gammap, gammadotp)
+        return k == 5 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_EXT:            // g_local_mu2_ext.c:47-57 (mu_t, gf, gflocal, beta, gammap, gammadotp)
+        return k == 0 || k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
     default:
         return false;
     }
@@ -279,6 +287,28 @@ int mpmg_default_params(int material, double *mp)
         mp[MPMG_MP_GRAINS_D] = 0.005;
         mp[MPMG_MP_RHO_CRITICAL] = 1485.0;
         return MPMG_OK;
+    case MPMG_DP_RI_MT:         // dp_ri_mt.c:66-76 reads E, nu, mu_s from the configuration
+        mp[MPMG_MP_MU_S] = 0.3819;
+        mp[MPMG_MP_RHO_CRITICAL] = 1485.0f;   // dp_ri_mt.c:159 literal
+        return MPMG_OK;
+    case MPMG_G_LOCAL_MU2_PLANE_STRAIN:   // g_local_mu2_plane_strain.c:27-39 (compile-time there)
+    case MPMG_G_LOCAL_MU2_TRUE_2D:        // g_local_mu2_true_2d.c:27-39
+        mp[MPMG_MP_MU_S] = 0.3819;
+        mp[MPMG_MP_GRAINS_RHO] = 2450;
+        mp[MPMG_MP_MU_2] = 0.6435;
+        mp[MPMG_MP_I0] = 0.278 / 1.0;
+        mp[MPMG_MP_GRAINS_D] = material == MPMG_G_LOCAL_MU2_TRUE_2D ? 0.01 * 5 : 0.001 * 5;
+        mp[MPMG_MP_RHO_CRITICAL] = 1485.0f;
+        return MPMG_OK;
+    case MPMG_G_LOCAL_MU2_EXT:            // g_local_mu2_ext.c:26-45 (compile-time there)
+        mp[MPMG_MP_MU_S] = 0.3819;
+        mp[MPMG_MP_GRAINS_RHO] = 2450;
+        mp[MPMG_MP_A] = 4.8;
+        mp[MPMG_MP_MU_2] = 0.6435;
+        mp[MPMG_MP_I0] = 0.278 / 1.0;
+        mp[MPMG_MP_GRAINS_D] = 0.01 * 5;
+        mp[MPMG_MP_RHO_CRITICAL] = 1485.0f;
+        return MPMG_OK;
     case MPMG_G_NONLOCAL:       // g_nonlocal.c:31-48
         mp[MPMG_MP_E] = 1e8;
         mp[MPMG_MP_NU] = 0.3;
@@ -367,7 +397,7 @@ int validate_config(const mpmg_config *cfg, size_t n)
         mpmg_set_error("grid or particle count exceeds 32-bit indexing");
         return MPMG_ERR_INVALID;
     }
-    if (cfg->material < MPMG_ISOLIN || cfg->material > MPMG_G_NONLOCAL) {
+    if (cfg->material < MPMG_ISOLIN || cfg->material > MPMG_G_LOCAL_MU2_EXT) {
         mpmg_set_error("unknown material kind %d", cfg->material);
         return MPMG_ERR_UNSUPPORTED;
     }
@@ -385,8 +415,9 @@ int validate_config(const mpmg_config *cfg, size_t n)
     }
     if (cfg->scheme == MPMG_SCHEME_MUSL &&
         (cfg->precision != MPMG_PRECISION_FP64 ||
-         (cfg->material != MPMG_ISOLIN && cfg->material != MPMG_G_LOCAL_MU2))) {
-        mpmg_set_error("the MUSL step runs in the FP64 form for isolin and g_local_mu2");
+         cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL ||
+         cfg->material == MPMG_G_LOCAL_MU2_EXT)) {
+        mpmg_set_error("the MUSL step runs in the FP64 form for the particle-local materials");
         return MPMG_ERR_UNSUPPORTED;
     }
     if (cfg->bc == MPMG_BOX) {
@@ -534,11 +565,14 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
             TRY(dalloc(&ctx->ax, n));
             TRY(dalloc(&ctx->ay, n));
         }
-        if (transients || nonlocal || cfg->scheme == MPMG_SCHEME_MUSL) {
+        // strain rates and start-of-step local coordinates outlive the G2P
+        // where a later phase reads them: the nonlocal solve, MUSL's second
+        // projection and g_local_mu2_ext's nodal fluidity Laplacian
+        const bool keep_rates = transients || nonlocal || cfg->scheme == MPMG_SCHEME_MUSL ||
+                                cfg->material == MPMG_G_LOCAL_MU2_EXT;
+        if (keep_rates) {
             double **sr[] = {&ctx->exx, &ctx->exy, &ctx->eyy, &ctx->wxy};
             for (double **p : sr) TRY(dalloc(p, n));
-        }
-        if (transients || nonlocal || cfg->scheme == MPMG_SCHEME_MUSL) {
             TRY(dalloc(&ctx->xl, n));
             TRY(dalloc(&ctx->yl, n));
         }
@@ -643,8 +677,8 @@ int mpmg_batch_create(int count, const mpmg_config *cfgs, const size_t *counts, 
             mpmg_set_error("batch member %d: batches run the mixed-precision form", k);
             return MPMG_ERR_UNSUPPORTED;
         }
-        if (c.material != MPMG_ISOLIN && c.material != MPMG_G_LOCAL_MU2) {
-            mpmg_set_error("batch member %d: mixed precision supports isolin and g_local_mu2", k);
+        if (c.material != MPMG_ISOLIN && c.material != MPMG_G_LOCAL_MU2 && c.material != MPMG_DP_RI_MT) {
+            mpmg_set_error("batch member %d: batches support isolin, g_local_mu2 and dp_ri_mt", k);
             return MPMG_ERR_UNSUPPORTED;
         }
         if (c.precision != cfgs[0].precision || c.material != cfgs[0].material || c.device != cfgs[0].device ||
@@ -1063,7 +1097,8 @@ int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *
 int mpmg_material_only(mpmg_ctx *ctx)
 {
     if (ctx == nullptr) return MPMG_ERR_INVALID;
-    if ((ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2) || ctx->mixed) {
+    if (ctx->cfg.material == MPMG_G_NONLOCAL_MU2 || ctx->cfg.material == MPMG_G_NONLOCAL ||
+        ctx->cfg.material == MPMG_G_LOCAL_MU2_EXT || ctx->mixed) {
         mpmg_set_error("material-only update is defined for local materials in FP64");
         return MPMG_ERR_UNSUPPORTED;
     }

@@ -71,6 +71,10 @@ int material_kind(const char *file)
     if (b == "g_local_mu2") return MPMG_G_LOCAL_MU2;
     if (b == "g_nonlocal_mu2") return MPMG_G_NONLOCAL_MU2;
     if (b == "g_nonlocal") return MPMG_G_NONLOCAL;
+    if (b == "dp_ri_mt") return MPMG_DP_RI_MT;
+    if (b == "g_local_mu2_plane_strain") return MPMG_G_LOCAL_MU2_PLANE_STRAIN;
+    if (b == "g_local_mu2_true_2d") return MPMG_G_LOCAL_MU2_TRUE_2D;
+    if (b == "g_local_mu2_ext") return MPMG_G_LOCAL_MU2_EXT;
     return -1;
 }
 
@@ -89,6 +93,10 @@ bool uses_state(int material, int k)
     case MPMG_G_LOCAL_MU2: return k == 9 || k == 10;
     case MPMG_G_NONLOCAL_MU2: return k == 0 || k == 3 || k == 4 || k == 5 || k == 6 || k == 9 || k == 10;
     case MPMG_G_NONLOCAL: return k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
+    case MPMG_DP_RI_MT: return k == 1 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_PLANE_STRAIN: return k == 1 || k == 5 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_TRUE_2D: return k == 5 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_EXT: return k == 0 || k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
     default: return false;
     }
 }
@@ -314,6 +322,14 @@ int mpm_gpu_attach(job_t *job)
         }
         cfg.mp[MPMG_MP_E] = job->material.fp64_props[0];
         cfg.mp[MPMG_MP_NU] = job->material.fp64_props[1];
+    }
+    if (mat == MPMG_DP_RI_MT) {
+        // dp_ri_mt.c:66-76
+        if (job->material.num_fp64_props < 3) {
+            mpmg_set_error("dp_ri_mt needs at least 3 properties (E, nu, mu_s)");
+            return MPMG_ERR_INVALID;
+        }
+        cfg.mp[MPMG_MP_MU_S] = job->material.fp64_props[2];
     }
     cfg.bc = bc;
     size_t need_f = (bc == MPMG_BOX) ? 4 : 3, need_i = (bc == MPMG_BOX) ? 4 : 0;

@@ -116,6 +116,177 @@ __device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &
     gammadotp = nup_tau;
 }
 
+// The plane-stress-form local returns that share one structure:
+//   dp_ri_mt                  dp_ri_mt.c:99-200                  3D trial, Drucker-Prager return
+//   g_local_mu2_plane_strain  g_local_mu2_plane_strain.c:157-265 3D trial, mu(I) return, beta
+//   g_local_mu2_true_2d       g_local_mu2_true_2d.c:157-260      2D trial, mu(I) return, beta
+// A 3D trial carries the out-of-plane stress szz (state[1]) and takes
+// p = -(sxx + syy + szz) / 3; the 2D trial takes p = -(sxx + syy) / 2.  The
+// Drucker-Prager return caps tau at mu_s p; the mu(I) return takes the
+// negative root of g_local_mu2's quadratic.  Dilute particles (m / v below
+// the literal 1485.0f) and particles in tension drop their stress and record
+// the whole trial shear as plastic flow, and the beta variants record
+// -p / (K dt) in state[5].  state[9] accumulates the plastic strain and
+// state[10] holds its rate.
+struct ReturnParams {
+    double mu_s, mu_2, I0, grains_rho, grains_d, rho_critical;
+};
+
+template <bool TRIAL3D, bool MU_I, bool BETA>
+__device__ __forceinline__ void plane_return(const Elastic &el, const ReturnParams &rp, double m, double v,
+                                             double exx, double exy, double eyy, double wxy, double &sxx,
+                                             double &sxy, double &syy, double &szz, double &beta,
+                                             double &gammap, double &gammadotp)
+{
+    const double G = el.G, K = el.K, dt = el.dt;
+    const double lambda = sub(K, dvd(mul(2.0, G), 3.0));
+    const double twoG = mul(2.0, G);
+    double trD = add(exx, eyy);
+    double dsjxx = add(mul(lambda, trD), mul(twoG, exx));
+    double dsjxy = mul(twoG, exy);
+    double dsjyy = add(mul(lambda, trD), mul(twoG, eyy));
+    double w2s = mul(mul(2.0, wxy), sxy);
+    dsjxx = add(dsjxx, w2s);
+    dsjxy = sub(dsjxy, mul(wxy, sub(sxx, syy)));
+    dsjyy = sub(dsjyy, w2s);
+    double sxx_tr = add(sxx, mul(dt, dsjxx));
+    double sxy_tr = add(sxy, mul(dt, dsjxy));
+    double syy_tr = add(syy, mul(dt, dsjyy));
+    double p_tr, t0zz = 0, szz_tr = 0;
+    if (TRIAL3D) {
+        szz_tr = add(szz, mul(mul(dt, lambda), trD));
+        p_tr = dvd(-add(add(sxx_tr, syy_tr), szz_tr), 3.0);
+    } else {
+        p_tr = mul(-0.5, add(sxx_tr, syy_tr));
+    }
+    double t0xx = add(sxx_tr, p_tr), t0xy = sxy_tr, t0yy = add(syy_tr, p_tr);
+    double tt = add(add(mul(t0xx, t0xx), mul(mul(2.0, t0xy), t0xy)), mul(t0yy, t0yy));
+    if (TRIAL3D) {
+        t0zz = add(szz_tr, p_tr);
+        tt = add(tt, mul(t0zz, t0zz));
+    }
+    double tau_tr = __dsqrt_rn(mul(0.5, tt));
+
+    const bool density_flag = dvd(m, v) < rp.rho_critical;
+    double nup_tau;
+    if (density_flag || p_tr <= 0) {
+        nup_tau = dvd(tau_tr, mul(G, dt));
+        if (BETA) beta = dvd(-p_tr, mul(K, dt));
+        sxx = 0; sxy = 0; syy = 0;
+        if (TRIAL3D) szz = 0;
+    } else if (p_tr > 0) {
+        double S0 = mul(rp.mu_s, p_tr);
+        double tau_tau, scale_factor;
+        if (tau_tr <= S0) {
+            tau_tau = tau_tr;
+            scale_factor = 1.0;
+        } else if (MU_I) {
+            double S2 = mul(rp.mu_2, p_tr);
+            double alpha = dvd(mul(mul(mul(G, rp.I0), dt), __dsqrt_rn(dvd(p_tr, rp.grains_rho))), rp.grains_d);
+            double B = -add(add(S2, tau_tr), alpha);
+            double H = add(mul(S2, tau_tr), mul(S0, alpha));
+            tau_tau = negative_root(1.0, B, H);
+            scale_factor = dvd(tau_tau, tau_tr);
+        } else {
+            tau_tau = S0;
+            scale_factor = dvd(tau_tau, tau_tr);
+        }
+        nup_tau = dvd(dvd(sub(tau_tr, tau_tau), G), dt);
+        if (BETA) beta = 0;
+        sxx = sub(mul(scale_factor, t0xx), p_tr);
+        sxy = mul(scale_factor, t0xy);
+        syy = sub(mul(scale_factor, t0yy), p_tr);
+        if (TRIAL3D) szz = sub(mul(scale_factor, t0zz), p_tr);
+    } else {
+        nup_tau = 0;   // NaN pressure: the reference prints 'u' and keeps s
+    }
+    gammap = add(gammap, mul(nup_tau, dt));
+    gammadotp = nup_tau;
+}
+
+// mu_from_gammadot, g_local_mu2_ext.c:75-95.
+__device__ __forceinline__ double mu_from_gammadot(double gammadot, double p, double dsqrtrhos, double mu_s,
+                                                   double mu_2, double inum_0)
+{
+    if (p <= 0) return mu_2;
+    double inum = dvd(mul(dsqrtrhos, gammadot), __dsqrt_rn(p));
+    if (inum <= 0) return mu_s;
+    return add(mu_s, dvd(sub(mu_2, mu_s), add(dvd(inum_0, inum), 1.0)));
+}
+
+// g_local_mu2_ext, first phase (g_local_mu2_ext.c:214-230): the local
+// fluidity gammadotp / mu_t from the start-of-step pressure.  mu_t keeps its
+// previous value where gammadotp is 0.
+__device__ __forceinline__ void ext_local_fluidity(const Mu2Params &mp, double sxx, double syy, double gammadotp,
+                                                   double &mu_t, double &gflocal)
+{
+    double p_t = mul(-0.5, add(sxx, syy));
+    if (gammadotp == 0) {
+        gflocal = 0;
+    } else {
+        mu_t = mu_from_gammadot(gammadotp, p_t, mul(mp.grains_d, __dsqrt_rn(mp.grains_rho)), mp.mu_s, mp.mu_2,
+                                mp.I0);
+        gflocal = dvd(gammadotp, mu_t);
+    }
+}
+
+// g_local_mu2_ext, third phase (g_local_mu2_ext.c:292-368): plane-stress
+// elastic trial with the Jaumann terms, returned to mu(gammadotp) (p + c)
+// with c = 1e-2.
+__device__ __forceinline__ void ext_stress(const Elastic &el, const Mu2Params &mp, double E, double nu, double m,
+                                           double v, double exx, double exy, double eyy, double wxy, double &sxx,
+                                           double &sxy, double &syy, double &mu_t, double &beta, double &gammap,
+                                           double &gammadotp)
+{
+    const double G = el.G, K = el.K, dt = el.dt, c = 1e-2;
+    double p_t = mul(-0.5, add(sxx, syy));
+    const double Ep = dvd(E, sub(1.0, mul(nu, nu)));
+    const double Gp = dvd(E, mul(2.0, add(1.0, nu)));
+    double dsjxx = mul(mul(dt, Ep), add(exx, mul(nu, eyy)));
+    double dsjxy = mul(mul(dt, Gp), exy);
+    double dsjyy = mul(mul(dt, Ep), add(eyy, mul(nu, exx)));
+    double w2 = mul(mul(mul(2.0, dt), wxy), sxy);
+    dsjxx = sub(dsjxx, w2);
+    dsjxy = add(dsjxy, mul(mul(dt, wxy), sub(sxx, syy)));
+    dsjyy = add(dsjyy, w2);
+    double sxx_tr = add(sxx, dsjxx), sxy_tr = add(sxy, dsjxy), syy_tr = add(syy, dsjyy);
+    double p_tr = mul(-0.5, add(sxx_tr, syy_tr));
+    double t0xx = add(sxx_tr, p_tr), t0xy = sxy_tr, t0yy = add(syy_tr, p_tr);
+    double tau_tr = __dsqrt_rn(mul(0.5, add(add(mul(t0xx, t0xx), mul(mul(2.0, t0xy), t0xy)), mul(t0yy, t0yy))));
+    mu_t = mu_from_gammadot(gammadotp, p_t, mul(mp.grains_d, __dsqrt_rn(mp.grains_rho)), mp.mu_s, mp.mu_2, mp.I0);
+    double tau_tau = mul(mu_t, add(p_tr, c));
+    double f = sub(tau_tr, tau_tau);
+    const bool density_flag = dvd(m, v) < mp.rho_critical;
+    const double pmin = dvd(-c, mu_t);   // -c / mu_t, the reference's -c/mu_t
+    double nup_tau;
+    if (density_flag) {
+        nup_tau = dvd(tau_tr, mul(G, dt));
+        beta = dvd(-p_tr, mul(K, dt));
+        sxx = 0; sxy = 0; syy = 0;
+    } else if (f < 0) {
+        nup_tau = 0;
+        beta = 0;
+        sxx = sub(t0xx, p_tr);
+        sxy = t0xy;
+        syy = sub(t0yy, p_tr);
+    } else if (f >= 0 && p_tr > pmin) {
+        nup_tau = dvd(sub(tau_tr, tau_tau), mul(G, dt));
+        beta = 0;
+        double scale_factor = dvd(tau_tau, tau_tr);
+        sxx = sub(mul(scale_factor, t0xx), p_tr);
+        sxy = mul(scale_factor, t0xy);
+        syy = sub(mul(scale_factor, t0yy), p_tr);
+    } else if (p_tr <= pmin) {
+        nup_tau = dvd(tau_tr, mul(G, dt));
+        beta = dvd(sub(dvd(c, mu_t), p_tr), mul(K, dt));
+        sxx = 0; sxy = 0; syy = 0;
+    } else {
+        nup_tau = 0;   // NaN: the reference prints the particle and keeps s
+    }
+    gammap = add(gammap, mul(nup_tau, dt));
+    gammadotp = nup_tau;
+}
+
 // Trial Jaumann stress of g_nonlocal_mu2.c:166-186 (and :271-290), with
 // lambda = K - 2G/3 (the reference leaves it uninitialised at :154).
 __device__ __forceinline__ void nonlocal_mu2_trial(const Elastic &el, double exx, double exy,

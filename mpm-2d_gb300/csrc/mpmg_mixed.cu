@@ -87,6 +87,43 @@ __device__ __forceinline__ void isolin_f(const MatF &p, float exx, float exy, fl
     syy += p.dt * dsjyy;
 }
 
+// dp_ri_mt (dp_ri_mt.c:99-200) in FP32; szz travels where g_local_mu2 keeps
+// Tzz.
+__device__ __forceinline__ void dp_ri_mt_f(const MatF &p, float m, float v, float exx, float exy,
+                                           float eyy, float wxy, float &sxx, float &sxy, float &syy,
+                                           float &szz, float &gp, float &gdp)
+{
+    const float twoG = 2.0f * p.G, dt = p.dt;
+    const float trD = exx + eyy;
+    const float lt = p.lambda * trD;
+    const float sxx_tr = sxx + dt * (lt + twoG * exx + 2.0f * wxy * sxy);
+    const float sxy_tr = sxy + dt * (twoG * exy - wxy * (sxx - syy));
+    const float syy_tr = syy + dt * (lt + twoG * eyy - 2.0f * wxy * sxy);
+    const float szz_tr = szz + dt * lt;
+    const float p_tr = -(sxx_tr + syy_tr + szz_tr) * (1.0f / 3.0f);
+    const float t0xx = sxx_tr + p_tr, t0xy = sxy_tr, t0yy = syy_tr + p_tr, t0zz = szz_tr + p_tr;
+    const float tau_tr = sqrtf(0.5f * (t0xx * t0xx + 2.0f * t0xy * t0xy + t0yy * t0yy + t0zz * t0zz));
+    float nup = 0.0f;
+    if (m < p.rho_critical * v || p_tr <= 0.0f) {
+        nup = tau_tr * p.inv_G_dt;
+        sxx = sxy = syy = szz = 0.0f;
+    } else if (p_tr > 0.0f) {
+        const float S0 = p.mu_s * p_tr;
+        float tau_tau = tau_tr, scale = 1.0f;
+        if (tau_tr > S0) {
+            tau_tau = S0;
+            scale = __fdividef(S0, tau_tr);
+        }
+        nup = (tau_tr - tau_tau) * p.inv_G_dt;
+        sxx = scale * t0xx - p_tr;
+        sxy = scale * t0xy;
+        syy = scale * t0yy - p_tr;
+        szz = scale * t0zz - p_tr;
+    }
+    gp += nup * dt;
+    gdp = nup;
+}
+
 // g_local_mu2 (g_local_mu2.c:165-310) in FP32, plane-strain stress
 // [[Txx, Txy, 0], [Txy, Tyy, 0], [0, 0, Tzz]].
 __device__ __forceinline__ void g_local_mu2_f(const MatF &p, float m, float v, float exx, float exy,
@@ -617,6 +654,8 @@ __device__ __forceinline__ uint32_t g2p_particle(const MemberM &M, uint32_t sent
         isolin_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy);
     } else if (MATERIAL == MPMG_G_LOCAL_MU2) {
         g_local_mu2_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
+    } else if (MATERIAL == MPMG_DP_RI_MT) {
+        dp_ri_mt_f(mp, m, vol, exx, exy, eyy, wxy, sxx, sxy, syy, Tzz, gp, gdp);
     } else {
         // g_nonlocal_mu2: bulk fluidity now; the stress waits for the solve
         float p_tr, t0xx, t0xy, t0yy, tau_tr, dense, gfl, xisq;
@@ -1024,6 +1063,7 @@ G2PKernel g2p_variant(int material, bool batch)
 {
     if (material == MPMG_ISOLIN) return batch ? mx_g2p_kernel<MPMG_ISOLIN, true> : mx_g2p_kernel<MPMG_ISOLIN, false>;
     if (material == MPMG_G_NONLOCAL_MU2) return mx_g2p_kernel<MPMG_G_NONLOCAL_MU2, false>;
+    if (material == MPMG_DP_RI_MT) return batch ? mx_g2p_kernel<MPMG_DP_RI_MT, true> : mx_g2p_kernel<MPMG_DP_RI_MT, false>;
     return batch ? mx_g2p_kernel<MPMG_G_LOCAL_MU2, true> : mx_g2p_kernel<MPMG_G_LOCAL_MU2, false>;
 }
 
@@ -1033,8 +1073,9 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
                     const double *vx, const double *vy, const double *sxx, const double *sxy, const double *syy)
 {
     const int mat = ctx->cfg.material;
-    if (mat != MPMG_ISOLIN && mat != MPMG_G_LOCAL_MU2 && !(mat == MPMG_G_NONLOCAL_MU2 && ctx->batch == nullptr)) {
-        mpmg_set_error("mixed precision supports isolin, g_local_mu2 and (outside batches) g_nonlocal_mu2");
+    if (mat != MPMG_ISOLIN && mat != MPMG_G_LOCAL_MU2 && mat != MPMG_DP_RI_MT &&
+        !(mat == MPMG_G_NONLOCAL_MU2 && ctx->batch == nullptr)) {
+        mpmg_set_error("mixed precision supports isolin, g_local_mu2, dp_ri_mt and (outside batches) g_nonlocal_mu2");
         return MPMG_ERR_UNSUPPORTED;
     }
     MixedState *s = new MixedState();
@@ -1260,8 +1301,13 @@ int pids(mpmg_ctx *ctx, std::vector<int> &pid)
 }
 
 // Record and component of each writable particle field.
-bool field_slot(const char *name, int *rec, int *comp)
+bool field_slot(int material, const char *name, int *rec, int *comp)
 {
+    if (material == MPMG_DP_RI_MT && strcmp(name, "state1") == 0) {
+        *rec = 2;    // szz (dp_ri_mt.c:27) sits in the Tzz slot
+        *comp = 3;
+        return true;
+    }
     struct { const char *n; int r, c; } f[] = {
         {"vx", 0, 2}, {"vy", 0, 3}, {"m", 1, 0}, {"v", 1, 1}, {"sxx", 1, 2}, {"sxy", 1, 3}, {"Txx", 1, 2},
         {"Txy", 1, 3}, {"Tyx", 1, 3}, {"syy", 2, 0}, {"Tyy", 2, 0}, {"ux", 2, 1}, {"uy", 2, 2}, {"Tzz", 2, 3},
@@ -1378,7 +1424,7 @@ int frame_get(mpmg_ctx *ctx, const char *name, double *out)
     int rec = 0, comp = 0, xy = 0;
     if (strcmp(name, "x") == 0) xy = 1;
     else if (strcmp(name, "y") == 0) { xy = 2; comp = 1; }
-    else if (!field_slot(name, &rec, &comp)) return MPMG_ERR_UNKNOWN_FIELD;
+    else if (!field_slot(ctx->cfg.material, name, &rec, &comp)) return MPMG_ERR_UNKNOWN_FIELD;
     if (n == 0) return MPMG_OK;
     const MemberM m0 = make_member(ctx->batch ? ctx->batch->cfg[0] : ctx->cfg, 0, 0);
     mx_export_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>((int)n, record(s, b, rec), comp, s->D[b],
@@ -1418,7 +1464,7 @@ int mpmg_mixed_set(mpmg_ctx *ctx, const char *name, const double *in)
     const size_t n = ctx->np;
     MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
     int rec, comp;
-    if (!field_slot(name, &rec, &comp)) {
+    if (!field_slot(ctx->cfg.material, name, &rec, &comp)) {
         mpmg_set_error("field '%s' cannot be written in the mixed-precision form", name);
         return MPMG_ERR_UNKNOWN_FIELD;
     }

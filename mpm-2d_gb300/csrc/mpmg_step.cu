@@ -202,7 +202,7 @@ struct G2PArgs {
     const double *node_ax, *node_ay, *node_vx, *node_vy;
     double *x, *y, *vx, *vy, *ux, *uy, *v, *m;
     double *sxx, *sxy, *syy, *Tzz;
-    double *st0, *st3, *st4, *st5, *st6, *st9, *st10;
+    double *st0, *st1, *st3, *st4, *st5, *st6, *st9, *st10;
     double *ax, *ay, *exx, *exy, *eyy, *wxy, *xl_out, *yl_out;
 };
 
@@ -211,6 +211,32 @@ struct G2PArgs {
 // momentum to the nodes again (p2g_momentum_kernel, node_velocity_kernel),
 // then the strain phase with the nodal velocities of that second projection.
 enum { G2P_FULL = 0, G2P_MOVE = 1, G2P_STRAIN = 2 };
+
+// The in-plane local returns on particle i (mat::plane_return): szz in
+// state[1] (dp_ri_mt.c:27, g_local_mu2_plane_strain.c:43), beta in state[5],
+// gammap in state[9], gammadotp in state[10].
+template <int MATERIAL>
+__device__ __forceinline__ void plane_return_particle(const G2PArgs &A, int i, double vol, double exx,
+                                                      double exy, double eyy, double wxy)
+{
+    constexpr bool trial3d = MATERIAL != MPMG_G_LOCAL_MU2_TRUE_2D;
+    constexpr bool mu_i = MATERIAL != MPMG_DP_RI_MT;
+    constexpr bool beta = MATERIAL != MPMG_DP_RI_MT;
+    const mat::ReturnParams rp = {A.mu2.mu_s, A.mu2.mu_2, A.mu2.I0, A.mu2.grains_rho, A.mu2.grains_d,
+                                  A.mu2.rho_critical};
+    double sxx = A.sxx[i], sxy = A.sxy[i], syy = A.syy[i];
+    double szz = trial3d ? A.st1[i] : 0.0, b = beta ? A.st5[i] : 0.0;
+    double gp = A.st9[i], gdp;
+    mat::plane_return<trial3d, mu_i, beta>(A.el, rp, A.m[i], vol, exx, exy, eyy, wxy, sxx, sxy, syy, szz, b,
+                                           gp, gdp);
+    A.sxx[i] = sxx;
+    A.sxy[i] = sxy;
+    A.syy[i] = syy;
+    if (trial3d) A.st1[i] = szz;
+    if (beta) A.st5[i] = b;
+    A.st9[i] = gp;
+    A.st10[i] = gdp;
+}
 
 template <int MATERIAL, int PHASE>
 __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
@@ -306,6 +332,15 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
         A.Tzz[i] = Tzz;
         A.st9[i] = gp;
         A.st10[i] = gdp;
+    } else if (MATERIAL == MPMG_DP_RI_MT || MATERIAL == MPMG_G_LOCAL_MU2_PLANE_STRAIN ||
+               MATERIAL == MPMG_G_LOCAL_MU2_TRUE_2D) {
+        plane_return_particle<MATERIAL>(A, i, vol, exx, exy, eyy, wxy);
+    } else if (MATERIAL == MPMG_G_LOCAL_MU2_EXT) {
+        // first phase only; the stress waits for the nodal Laplacian
+        double mu_t = A.st0[i], gfl;
+        mat::ext_local_fluidity(A.mu2, A.sxx[i], A.syy[i], A.st10[i], mu_t, gfl);
+        A.st0[i] = mu_t;
+        A.st4[i] = gfl;
     } else if (MATERIAL == MPMG_G_NONLOCAL_MU2) {
         double dense, gfl, xisq;
         mat::nonlocal_mu2_bulk(A.el, A.mu2, A.m[i], vol, exx, exy, eyy, wxy, A.sxx[i], A.sxy[i],
@@ -316,6 +351,85 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
     }
     // MPMG_G_NONLOCAL computes its bulk fluidity over every particle in the
     // fluidity phase (g_nonlocal.c:306-352).
+}
+
+// g_local_mu2_ext's second phase (g_local_mu2_ext.c:232-265): per element,
+// each particle's -v gflocal |grad N_j|^2 summed per corner in the binned
+// order of the step, with the start-of-step shape-function gradients.
+__global__ void __launch_bounds__(128) ext_cells_kernel(
+    int ne, double inv_h, const int *__restrict__ cell_start, const uint32_t *__restrict__ perm,
+    const double *__restrict__ xl, const double *__restrict__ yl, const double *__restrict__ v,
+    const double *__restrict__ gflocal, double *__restrict__ cell_sums)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int k0 = cell_start[e], k1 = cell_start[e + 1];
+    double acc[4] = {0, 0, 0, 0};
+    for (int k = k0; k < k1; k++) {
+        const int i = (int)perm[k];
+        const ShapeFns f = shape(xl[i], yl[i], inv_h);
+        const double q = mat::mul(-v[i], gflocal[i]);
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const double sj = mat::add(mat::mul(f.gx[a], f.gx[a]), mat::mul(f.gy[a], f.gy[a]));
+            acc[a] = mat::add(acc[a], mat::mul(q, sj));
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++) cell_sums[(size_t)a * ne + e] = acc[a];
+}
+
+// The nodal sums of ext_cells_kernel's corners in colour order.
+__global__ void __launch_bounds__(256) ext_nodes_kernel(GridGeom g, int ne, const double *__restrict__ cell_sums,
+                                                        double *__restrict__ d2)
+{
+    const int nn = g.Nx * g.Ny;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const int i = n % g.Nx, j = n / g.Nx;
+    double sum = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+        const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
+        const int e = cj * g.Ex + ci;
+        const int corner = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+        sum = mat::add(sum, cell_sums[(size_t)corner * ne + e]);
+    }
+    d2[n] = sum;
+}
+
+// g_local_mu2_ext's gf and gammadotp correction (g_local_mu2_ext.c:268-290)
+// and the stress (mat::ext_stress).
+__global__ void __launch_bounds__(256) ext_stress_kernel(G2PArgs A, const double *__restrict__ d2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n || !A.active[i]) return;
+    const GridGeom &g = A.g;
+    const int e = A.in_element[i];
+    const int ci = e % g.Ex, cj = e / g.Ex;
+    const int n0 = cj * g.Nx + ci;
+    const int nd[4] = {n0, n0 + 1, n0 + 1 + g.Nx, n0 + g.Nx};
+    double gf = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) gf = mat::add(gf, mat::mul(0.25, d2[nd[a]]));
+    double mu_t = A.st0[i], gdp = A.st10[i];
+    const double Ad = A.mu2.A, d = A.mu2.grains_d;
+    gf = mat::mul(mat::mul(mat::mul(mat::mul(mat::mul(Ad, Ad), d), d), mu_t), gf);
+    if (mu_t > A.mu2.mu_s) gdp = mat::sub(gdp, mat::dvd(gf, fabs(mat::sub(mu_t, A.mu2.mu_s))));
+    if (gdp < 0) gdp = 0;
+    A.st3[i] = gf;
+    double sxx = A.sxx[i], sxy = A.sxy[i], syy = A.syy[i], beta = A.st5[i], gp = A.st9[i];
+    mat::ext_stress(A.el, A.mu2, A.nl.E, A.nl.nu, A.m[i], A.v[i], A.exx[i], A.exy[i], A.eyy[i], A.wxy[i], sxx, sxy,
+                    syy, mu_t, beta, gp, gdp);
+    A.sxx[i] = sxx;
+    A.sxy[i] = sxy;
+    A.syy[i] = syy;
+    A.st0[i] = mu_t;
+    A.st5[i] = beta;
+    A.st9[i] = gp;
+    A.st10[i] = gdp;
 }
 
 // MUSL's second projection (process_usl.c:424-431): per element, the moved
@@ -403,6 +517,12 @@ __global__ void material_only_kernel(G2PArgs A, int material)
         A.sxx[i] = sxx;
         A.sxy[i] = sxy;
         A.syy[i] = syy;
+    } else if (material == MPMG_DP_RI_MT) {
+        plane_return_particle<MPMG_DP_RI_MT>(A, i, A.v[i], exx, exy, eyy, wxy);
+    } else if (material == MPMG_G_LOCAL_MU2_PLANE_STRAIN) {
+        plane_return_particle<MPMG_G_LOCAL_MU2_PLANE_STRAIN>(A, i, A.v[i], exx, exy, eyy, wxy);
+    } else if (material == MPMG_G_LOCAL_MU2_TRUE_2D) {
+        plane_return_particle<MPMG_G_LOCAL_MU2_TRUE_2D>(A, i, A.v[i], exx, exy, eyy, wxy);
     } else {
         double Txx = A.sxx[i], Txy = A.sxy[i], Tyy = A.syy[i], Tzz = A.Tzz[i];
         double gp = A.st9[i], gdp;
@@ -451,7 +571,7 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.x = ctx->x; A.y = ctx->y; A.vx = ctx->vx; A.vy = ctx->vy; A.ux = ctx->ux; A.uy = ctx->uy;
     A.v = ctx->v; A.m = ctx->m;
     A.sxx = ctx->sxx; A.sxy = ctx->sxy; A.syy = ctx->syy; A.Tzz = ctx->Tzz;
-    A.st0 = ctx->state[0]; A.st3 = ctx->state[3]; A.st4 = ctx->state[4]; A.st5 = ctx->state[5];
+    A.st0 = ctx->state[0]; A.st1 = ctx->state[1]; A.st3 = ctx->state[3]; A.st4 = ctx->state[4]; A.st5 = ctx->state[5];
     A.st6 = ctx->state[6]; A.st9 = ctx->state[9]; A.st10 = ctx->state[10];
     A.ax = ctx->ax; A.ay = ctx->ay;
     A.exx = ctx->exx; A.exy = ctx->exy; A.eyy = ctx->eyy; A.wxy = ctx->wxy;
@@ -507,16 +627,25 @@ int mpmg_launch_step(mpmg_ctx *ctx)
     G2PArgs A = make_g2p_args(ctx);
     if (c.scheme == MPMG_SCHEME_MUSL) {
         // move, second projection of the moved momentum, then strain
-        if (c.material == MPMG_ISOLIN) g2p_kernel<MPMG_ISOLIN, G2P_MOVE><<<blocks_for(n, 256), 256, 0, s>>>(A);
-        else g2p_kernel<MPMG_G_LOCAL_MU2, G2P_MOVE><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        // the move phase does not depend on the material
+        g2p_kernel<MPMG_ISOLIN, G2P_MOVE><<<blocks_for(n, 256), 256, 0, s>>>(A);
         p2g_momentum_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(ne, ctx->inv_h, ctx->cell_start, ctx->perm, ctx->xl,
                                                                 ctx->yl, ctx->m, ctx->vx, ctx->vy, ctx->cell_sums);
         node_velocity_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(g, make_bc(ctx), ne, ctx->cell_start,
                                                                  ctx->cell_sums, ctx->d_params, ctx->node_m,
                                                                  ctx->node_vx, ctx->node_vy, ctx->node_mx,
                                                                  ctx->node_my);
-        if (c.material == MPMG_ISOLIN) g2p_kernel<MPMG_ISOLIN, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
-        else g2p_kernel<MPMG_G_LOCAL_MU2, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
+        switch (c.material) {
+        case MPMG_ISOLIN: g2p_kernel<MPMG_ISOLIN, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A); break;
+        case MPMG_DP_RI_MT: g2p_kernel<MPMG_DP_RI_MT, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A); break;
+        case MPMG_G_LOCAL_MU2_PLANE_STRAIN:
+            g2p_kernel<MPMG_G_LOCAL_MU2_PLANE_STRAIN, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_G_LOCAL_MU2_TRUE_2D:
+            g2p_kernel<MPMG_G_LOCAL_MU2_TRUE_2D, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        default: g2p_kernel<MPMG_G_LOCAL_MU2, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A); break;
+        }
         ctx->launches += 4;
     } else {
         switch (c.material) {
@@ -525,6 +654,23 @@ int mpmg_launch_step(mpmg_ctx *ctx)
             break;
         case MPMG_G_LOCAL_MU2:
             g2p_kernel<MPMG_G_LOCAL_MU2, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_DP_RI_MT:
+            g2p_kernel<MPMG_DP_RI_MT, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_G_LOCAL_MU2_PLANE_STRAIN:
+            g2p_kernel<MPMG_G_LOCAL_MU2_PLANE_STRAIN, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_G_LOCAL_MU2_TRUE_2D:
+            g2p_kernel<MPMG_G_LOCAL_MU2_TRUE_2D, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_G_LOCAL_MU2_EXT:
+            g2p_kernel<MPMG_G_LOCAL_MU2_EXT, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            ext_cells_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(ne, ctx->inv_h, ctx->cell_start, ctx->perm, ctx->xl,
+                                                                ctx->yl, ctx->v, ctx->state[4], ctx->cell_sums);
+            ext_nodes_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(g, ne, ctx->cell_sums, ctx->node_gf);
+            ext_stress_kernel<<<blocks_for(n, 256), 256, 0, s>>>(A, ctx->node_gf);
+            ctx->launches += 3;
             break;
         case MPMG_G_NONLOCAL_MU2:
             g2p_kernel<MPMG_G_NONLOCAL_MU2, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);

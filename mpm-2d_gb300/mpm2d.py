@@ -25,7 +25,9 @@ import numpy as np
 
 import mpmg_build as _build
 
-MATERIALS = {"isolin": 0, "g_local_mu2": 1, "g_nonlocal_mu2": 2, "g_nonlocal": 3}
+MATERIALS = {"isolin": 0, "g_local_mu2": 1, "g_nonlocal_mu2": 2, "g_nonlocal": 3, "dp_ri_mt": 4,
+             "g_local_mu2_plane_strain": 5, "g_local_mu2_true_2d": 6,
+             "g_local_mu2_ext": 7}
 BCS = {"box": 0, "square_silo": 1}
 MP_COUNT = 16
 MP = {"E": 0, "nu": 1, "mu_s": 2, "mu_2": 3, "I0": 4, "grains_rho": 5, "grains_d": 6, "A": 7,
@@ -170,6 +172,8 @@ def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20
     props = scene.get("props")
     if props is not None:
         mp[0], mp[1] = props[0], props[1]
+        if scene["material"] == "dp_ri_mt" and len(props) > 2:
+            mp[MP["mu_s"]] = props[2]   # dp_ri_mt.c:73 fp64_props[2] = mu_s
     for k, val in scene.get("mp", {}).items():
         mp[MP[k] if isinstance(k, str) else k] = val
     for k in range(MP_COUNT):

@@ -31,7 +31,10 @@ CFLAGS = ["-O2", "-std=gnu99", "-fPIC", "-ffp-contract=off", "-w"]
 
 LIBMPM_SOURCES = ["element.c", "interpolate.c", "loading.c", "map.c", "material.c",
                   "particle.c", "process_usl.c", "rtsafe.c", "tensor.c"]
-LOCAL_MATERIALS = ["isolin", "g_local_mu2"]
+KAT_MATERIALS = ["isolin", "g_local_mu2", "dp_ri_mt", "g_local_mu2_plane_strain", "g_local_mu2_true_2d"]
+# g_local_mu2_ext needs the team's element lists and barrier, which
+# tests/test_material.c does not set up: plugin only
+LOCAL_MATERIALS = KAT_MATERIALS + ["g_local_mu2_ext"]
 NONLOCAL_MATERIALS = ["g_nonlocal_mu2", "g_nonlocal"]
 BCS = ["box", "square_silo"]
 
@@ -118,7 +121,7 @@ def build_ref(verbose=False):
     sh(["gcc"] + CFLAGS + inc + ["-shared", "-o", os.path.join(REF_OUT, "libref_harness.so"),
                                  os.path.join(HERE, "ref", "ref_harness.c")] + link_mpm + ["-ldl", "-lpthread", "-lm"])
 
-    for mat in LOCAL_MATERIALS:
+    for mat in KAT_MATERIALS:
         sh(["gcc"] + CFLAGS + inc + ["-o", os.path.join(REF_OUT, "material_" + mat),
                                      os.path.join(ref, "tests", "test_material.c"),
                                      os.path.join(ref, "materialsrc", mat + ".c")] + link_mpm + ["-lm", "-lpthread"])

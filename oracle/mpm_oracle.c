@@ -115,6 +115,28 @@ void orc_default_params(int material, double *mp)
         mp[ORC_MP_GRAINS_D] = 0.005;
         mp[ORC_MP_RHO_CRITICAL] = 1485.0;
         break;
+    case ORC_DP_RI_MT:                /* dp_ri_mt.c:66-76 reads E, nu, mu_s */
+        mp[ORC_MP_MU_S] = 0.3819;
+        mp[ORC_MP_RHO_CRITICAL] = 1485.0f; /* dp_ri_mt.c:159 literal */
+        break;
+    case ORC_G_LOCAL_MU2_PLANE_STRAIN: /* g_local_mu2_plane_strain.c:27-38 */
+    case ORC_G_LOCAL_MU2_TRUE_2D:      /* g_local_mu2_true_2d.c:27-38 */
+        mp[ORC_MP_MU_S] = 0.3819;
+        mp[ORC_MP_GRAINS_RHO] = 2450;
+        mp[ORC_MP_MU_2] = 0.6435;
+        mp[ORC_MP_I0] = 0.278 / 1.0;
+        mp[ORC_MP_GRAINS_D] = material == ORC_G_LOCAL_MU2_TRUE_2D ? 0.01 * 5 : 0.001 * 5;
+        mp[ORC_MP_RHO_CRITICAL] = 1485.0f;
+        break;
+    case ORC_G_LOCAL_MU2_EXT:          /* g_local_mu2_ext.c:26-45 */
+        mp[ORC_MP_MU_S] = 0.3819;
+        mp[ORC_MP_GRAINS_RHO] = 2450;
+        mp[ORC_MP_A] = 4.8;
+        mp[ORC_MP_MU_2] = 0.6435;
+        mp[ORC_MP_I0] = 0.278 / 1.0;
+        mp[ORC_MP_GRAINS_D] = 0.01 * 5;
+        mp[ORC_MP_RHO_CRITICAL] = 1485.0f;
+        break;
     case ORC_G_NONLOCAL:              /* g_nonlocal.c:31-48 */
         mp[ORC_MP_E] = 1e8;
         mp[ORC_MP_NU] = 0.3;
@@ -619,6 +641,267 @@ static void g_local_mu2_range(orc_sim *s, size_t p0, size_t p1)
         s->sxx[i] = T[XX];
         s->sxy[i] = T[XY];
         s->syy[i] = T[YY];
+        st[9] += nup_tau * dt;
+        st[10] = nup_tau;
+    }
+}
+
+/* The local returns written on the in-plane stress (sxx, sxy, syy):
+     dp_ri_mt                  dp_ri_mt.c:99-200                   trial3d, Drucker-Prager
+     g_local_mu2_plane_strain  g_local_mu2_plane_strain.c:157-265  trial3d, mu(I), beta
+     g_local_mu2_true_2d       g_local_mu2_true_2d.c:157-260       2D trial, mu(I), beta
+   trial3d carries szz in state[1] and takes p = -(sxx + syy + szz) / 3, the
+   2D trial p = -(sxx + syy) / 2.  beta (state[5]) records -p / (K dt) on the
+   dilute branch.  state[9] accumulates the plastic strain, state[10] holds
+   its rate. */
+static void plane_return_range(orc_sim *s, size_t p0, size_t p1, int trial3d, int mu_i, int with_beta)
+{
+    const double G = s->G, K = s->K, dt = s->c.dt;
+    const double *mp = s->c.mp;
+    const double lambda = K - 2.0 * G / 3.0;
+    for (size_t i = p0; i < p1; i++) {
+        if (s->active[i] == 0) {
+            continue;
+        }
+        double *st = s->state + DEPVAR * i;
+        double trD = s->exx[i] + s->eyy[i];
+        double dsjxx = lambda * trD + 2.0 * G * s->exx[i];
+        double dsjxy = 2.0 * G * s->exy[i];
+        double dsjyy = lambda * trD + 2.0 * G * s->eyy[i];
+        dsjxx += 2 * s->wxy[i] * s->sxy[i];
+        dsjxy -= s->wxy[i] * (s->sxx[i] - s->syy[i]);
+        dsjyy -= 2 * s->wxy[i] * s->sxy[i];
+        double sxx_tr = s->sxx[i] + dt * dsjxx;
+        double sxy_tr = s->sxy[i] + dt * dsjxy;
+        double syy_tr = s->syy[i] + dt * dsjyy;
+        double szz_tr = 0, p_tr, t0zz = 0, tau_tr;
+        if (trial3d) {
+            szz_tr = st[1] + dt * lambda * trD;
+            p_tr = -(sxx_tr + syy_tr + szz_tr) / 3.0;
+        } else {
+            p_tr = -0.5 * (sxx_tr + syy_tr);
+        }
+        double t0xx = sxx_tr + p_tr;
+        double t0xy = sxy_tr;
+        double t0yy = syy_tr + p_tr;
+        if (trial3d) {
+            t0zz = szz_tr + p_tr;
+            tau_tr = sqrt(0.5 * (t0xx * t0xx + 2 * t0xy * t0xy + t0yy * t0yy + t0zz * t0zz));
+        } else {
+            tau_tr = sqrt(0.5 * (t0xx * t0xx + 2 * t0xy * t0xy + t0yy * t0yy));
+        }
+        int density_flag = (s->m[i] / s->v[i]) < mp[ORC_MP_RHO_CRITICAL];
+        double nup_tau;
+        if (density_flag || p_tr <= 0) {
+            nup_tau = tau_tr / (G * dt);
+            if (with_beta) {
+                st[5] = -p_tr / (K * dt);
+            }
+            s->sxx[i] = 0;
+            s->sxy[i] = 0;
+            s->syy[i] = 0;
+            if (trial3d) {
+                st[1] = 0;
+            }
+        } else if (p_tr > 0) {
+            double S0 = mp[ORC_MP_MU_S] * p_tr;
+            double tau_tau, scale_factor;
+            if (tau_tr <= S0) {
+                tau_tau = tau_tr;
+                scale_factor = 1.0;
+            } else if (mu_i) {
+                double S2 = mp[ORC_MP_MU_2] * p_tr;
+                double alpha = G * mp[ORC_MP_I0] * dt * sqrt(p_tr / mp[ORC_MP_GRAINS_RHO])
+                               / mp[ORC_MP_GRAINS_D];
+                double B = -(S2 + tau_tr + alpha);
+                double H = S2 * tau_tr + S0 * alpha;
+                tau_tau = negative_root(1.0, B, H);
+                scale_factor = (tau_tau / tau_tr);
+            } else {
+                tau_tau = S0;
+                scale_factor = tau_tau / tau_tr;
+            }
+            nup_tau = ((tau_tr - tau_tau) / G) / dt;
+            if (with_beta) {
+                st[5] = 0;
+            }
+            s->sxx[i] = scale_factor * t0xx - p_tr;
+            s->sxy[i] = scale_factor * t0xy;
+            s->syy[i] = scale_factor * t0yy - p_tr;
+            if (trial3d) {
+                st[1] = scale_factor * t0zz - p_tr;
+            }
+        } else {
+            nup_tau = 0;   /* p_tr is NaN */
+        }
+        st[9] += nup_tau * dt;
+        st[10] = nup_tau;
+    }
+}
+
+static int plane_return_material(int material, size_t p0, size_t p1, orc_sim *s)
+{
+    switch (material) {
+    case ORC_DP_RI_MT:
+        plane_return_range(s, p0, p1, 1, 0, 0);
+        return 1;
+    case ORC_G_LOCAL_MU2_PLANE_STRAIN:
+        plane_return_range(s, p0, p1, 1, 1, 1);
+        return 1;
+    case ORC_G_LOCAL_MU2_TRUE_2D:
+        plane_return_range(s, p0, p1, 0, 1, 1);
+        return 1;
+    default:
+        return 0;
+    }
+}
+
+/* mu_from_gammadot, g_local_mu2_ext.c:75-95 */
+static double mu_from_gammadot(double gammadot, double p, double dsqrtrhos, double mu_s, double mu_2,
+                               double inum_0)
+{
+    double mu;
+    if (p <= 0) {
+        mu = mu_2;
+    } else {
+        double inum = dsqrtrhos * gammadot / sqrt(p);
+        if (inum <= 0) {
+            mu = mu_s;
+        } else {
+            mu = mu_s + (mu_2 - mu_s) / ((inum_0 / inum) + 1.0);
+        }
+    }
+    return mu;
+}
+
+/* g_local_mu2_ext calculate_stress_threaded, g_local_mu2_ext.c:165-368, run
+   by every thread of the team.  Three phases separated by team barriers:
+   (1) the local fluidity gammadotp / mu_t from the start-of-step pressure
+   (state[0] mu_t, state[4] gflocal); (2) per colour, each particle adds
+   -v gflocal |grad N_j|^2 to its element's nodes (the team's per-(thread,
+   colour) lists, a barrier per colour), then gf = A^2 d^2 mu_t times the
+   element average (state[3]) lowers gammadotp where mu_t > mu_s; (3) a
+   plane-stress elastic trial with the Jaumann terms, returned to
+   mu(gammadotp) (p + c) with c = 1e-2.  Node values live in gf_nodes. */
+static void g_local_mu2_ext_thread(orc_task *task)
+{
+    orc_sim *s = task->s;
+    const double *mp = s->c.mp;
+    const double E = mp[ORC_MP_E], nu = mp[ORC_MP_NU], G = s->G, K = s->K, dt = s->c.dt;
+    const double mu_s = mp[ORC_MP_MU_S], mu_2 = mp[ORC_MP_MU_2], I0 = mp[ORC_MP_I0];
+    const double d = mp[ORC_MP_GRAINS_D], Acoef = mp[ORC_MP_A];
+    const double dsqrtrhos = d * sqrt(mp[ORC_MP_GRAINS_RHO]);
+    const double c = 1e-2;
+    double *d2 = s->gf_nodes;
+
+    for (size_t i = task->n0; i < task->n1; i++) {
+        d2[i] = 0;
+    }
+    for (size_t i = task->p0; i < task->p1; i++) {
+        if (s->active[i] == 0) {
+            continue;
+        }
+        double *st = s->state + DEPVAR * i;
+        double p_t = -0.5 * (s->sxx[i] + s->syy[i]);
+        if (st[10] == 0) {
+            st[4] = 0;
+        } else {
+            st[0] = mu_from_gammadot(st[10], p_t, dsqrtrhos, mu_s, mu_2, I0);
+            st[4] = st[10] / st[0];
+        }
+    }
+    pthread_barrier_wait(&s->bar);
+
+    for (int cc = 0; cc < NCOLORS; cc++) {
+        size_t tc = task->id * NCOLORS + (size_t)cc;
+        for (size_t k = 0; k < s->list_len[tc]; k++) {
+            size_t i = s->lists[tc][k];
+            const int *nn = s->enodes + 4 * s->in_element[i];
+            double sj[4];
+            sj[0] = s->b11[i] * s->b11[i] + s->b21[i] * s->b21[i];
+            sj[1] = s->b12[i] * s->b12[i] + s->b22[i] * s->b22[i];
+            sj[2] = s->b13[i] * s->b13[i] + s->b23[i] * s->b23[i];
+            sj[3] = s->b14[i] * s->b14[i] + s->b24[i] * s->b24[i];
+            for (int j = 0; j < 4; j++) {
+                d2[nn[j]] += -s->v[i] * s->state[DEPVAR * i + 4] * sj[j];
+            }
+        }
+        pthread_barrier_wait(&s->bar);
+    }
+
+    for (size_t i = task->p0; i < task->p1; i++) {
+        if (s->active[i] == 0) {
+            continue;
+        }
+        double *st = s->state + DEPVAR * i;
+        const int *nn = s->enodes + 4 * s->in_element[i];
+        st[3] = 0;
+        for (int j = 0; j < 4; j++) {
+            st[3] += 0.25 * d2[nn[j]];
+        }
+        st[3] = Acoef * Acoef * d * d * st[0] * st[3];
+        if (st[0] > mu_s) {
+            st[10] = st[10] - (st[3] / fabs(st[0] - mu_s));
+        }
+        if (st[10] < 0) {
+            st[10] = 0;
+        }
+    }
+    pthread_barrier_wait(&s->bar);
+
+    for (size_t i = task->p0; i < task->p1; i++) {
+        if (s->active[i] == 0) {
+            continue;
+        }
+        double *st = s->state + DEPVAR * i;
+        double p_t = -0.5 * (s->sxx[i] + s->syy[i]);
+        double dsjxx = dt * (E / (1 - nu * nu)) * ((s->exx[i]) + nu * (s->eyy[i]));
+        double dsjxy = dt * (E / (2 * (1 + nu))) * (s->exy[i]);
+        double dsjyy = dt * (E / (1 - nu * nu)) * ((s->eyy[i]) + nu * (s->exx[i]));
+        dsjxx -= 2 * dt * s->wxy[i] * s->sxy[i];
+        dsjxy += dt * s->wxy[i] * (s->sxx[i] - s->syy[i]);
+        dsjyy += 2 * dt * s->wxy[i] * s->sxy[i];
+        double sxx_tr = s->sxx[i] + dsjxx;
+        double sxy_tr = s->sxy[i] + dsjxy;
+        double syy_tr = s->syy[i] + dsjyy;
+        double p_tr = -0.5 * (sxx_tr + syy_tr);
+        double t0xx = sxx_tr + p_tr;
+        double t0xy = sxy_tr;
+        double t0yy = syy_tr + p_tr;
+        double tau_tr = sqrt(0.5 * (t0xx * t0xx + 2 * t0xy * t0xy + t0yy * t0yy));
+        st[0] = mu_from_gammadot(st[10], p_t, dsqrtrhos, mu_s, mu_2, I0);
+        double tau_tau = st[0] * (p_tr + c);
+        double f = tau_tr - tau_tau;
+        int density_flag = (s->m[i] / s->v[i]) < mp[ORC_MP_RHO_CRITICAL];
+        double nup_tau;
+        if (density_flag) {
+            nup_tau = (tau_tr) / (G * dt);
+            st[5] = -p_tr / (K * dt);
+            s->sxx[i] = 0;
+            s->sxy[i] = 0;
+            s->syy[i] = 0;
+        } else if (f < 0) {
+            nup_tau = 0;
+            st[5] = 0;
+            s->sxx[i] = t0xx - p_tr;
+            s->sxy[i] = t0xy;
+            s->syy[i] = t0yy - p_tr;
+        } else if (f >= 0 && p_tr > -c / st[0]) {
+            nup_tau = (tau_tr - tau_tau) / (G * dt);
+            st[5] = 0;
+            double scale_factor = (tau_tau / tau_tr);
+            s->sxx[i] = scale_factor * t0xx - p_tr;
+            s->sxy[i] = scale_factor * t0xy;
+            s->syy[i] = scale_factor * t0yy - p_tr;
+        } else if (p_tr <= -c / st[0]) {
+            nup_tau = tau_tr / (G * dt);
+            st[5] = ((c / st[0]) - p_tr) / (K * dt);
+            s->sxx[i] = 0;
+            s->sxy[i] = 0;
+            s->syy[i] = 0;
+        } else {
+            nup_tau = 0;   /* NaN: the reference prints the particle and keeps s */
+        }
         st[9] += nup_tau * dt;
         st[10] = nup_tau;
     }
@@ -1344,6 +1627,14 @@ static void step_thread(orc_task *task)
     case ORC_G_LOCAL_MU2:
         g_local_mu2_range(s, task->p0, task->p1);
         break;
+    case ORC_DP_RI_MT:
+    case ORC_G_LOCAL_MU2_PLANE_STRAIN:
+    case ORC_G_LOCAL_MU2_TRUE_2D:
+        plane_return_material(s->c.material, task->p0, task->p1, s);
+        break;
+    case ORC_G_LOCAL_MU2_EXT:
+        g_local_mu2_ext_thread(task);
+        break;
     case ORC_G_NONLOCAL_MU2:
         /* g_nonlocal_mu2.c:113-123: thread 0 solves for everyone.  The
            reference has no barrier here, so with more than one thread its
@@ -1408,6 +1699,11 @@ int orc_material_only(orc_sim *s)
         return 0;
     case ORC_G_LOCAL_MU2:
         g_local_mu2_range(s, 0, s->np);
+        return 0;
+    case ORC_DP_RI_MT:
+    case ORC_G_LOCAL_MU2_PLANE_STRAIN:
+    case ORC_G_LOCAL_MU2_TRUE_2D:
+        plane_return_material(s->c.material, 0, s->np, s);
         return 0;
     default:
         return 1;

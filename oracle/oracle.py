@@ -15,7 +15,9 @@ import numpy as np
 
 from . import build as _build
 
-MATERIALS = {"isolin": 0, "g_local_mu2": 1, "g_nonlocal_mu2": 2, "g_nonlocal": 3}
+MATERIALS = {"isolin": 0, "g_local_mu2": 1, "g_nonlocal_mu2": 2, "g_nonlocal": 3, "dp_ri_mt": 4,
+             "g_local_mu2_plane_strain": 5, "g_local_mu2_true_2d": 6,
+             "g_local_mu2_ext": 7}
 BCS = {"box": 0, "square_silo": 1}
 MP_COUNT = 16
 PARTICLE_FIELDS = ["x", "y", "xl", "yl", "v", "v0", "m", "vx", "vy", "ax", "ay", "bx", "by",
@@ -104,6 +106,8 @@ class Oracle:
         props = scene.get("props")
         if props is not None:
             mp[0], mp[1] = props[0], props[1]
+            if scene["material"] == "dp_ri_mt" and len(props) > 2:
+                mp[2] = props[2]   # dp_ri_mt.c:73 fp64_props[2] = mu_s
         for k, val in scene.get("mp", {}).items():
             mp[k] = val
         for k in range(MP_COUNT):

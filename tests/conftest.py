@@ -82,6 +82,10 @@ FIELD_GROUPS = {
     "node_mx": ("node_mx", "node_my"), "node_my": ("node_mx", "node_my"),
     "node_fx": ("node_fx", "node_fy"), "node_fy": ("node_fx", "node_fy"),
     "node_vx": ("node_vx", "node_vy"), "node_vy": ("node_vx", "node_vy"),
+    # szz of the 3D-trial materials; beta = -p / (K dt) (tensile branch, zero
+    # up to round-off at a free surface) against the plastic-rate scale
+    "state1": ("sxx", "syy", "state1"),
+    "state5": ("state5", "state10"),
 }
 
 

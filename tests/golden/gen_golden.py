@@ -90,19 +90,60 @@ def parse_hex_csv(path):
     return np.array(rows)
 
 
-def kat(material):
+def kat(material, props=(1e6, 0.3)):
+    """The reference's tests/test_material.c run with the properties of
+    tests/<material>.cfg (isolin, g_local_mu2: E, nu; dp_ri_mt: E, nu, mu_s)."""
     exe = os.path.join(obuild.REF_OUT, "material_" + material)
     with tempfile.TemporaryDirectory() as d:
         hexf = os.path.join(d, "out.csv")
         decf = os.path.join(d, "out_dec.csv")
         cfg = os.path.join(d, "test.cfg")
         with open(cfg, "w") as f:
-            f.write("%s\n%s\n1e6\n0.3\n" % (hexf, decf))   # tests/isolin.cfg, g_local_mu2.cfg
+            f.write("%s\n%s\n" % (hexf, decf) + "".join("%r\n" % p for p in props))
         subprocess.run([exe, cfg], check=True, capture_output=True, cwd=d)
         rows = parse_hex_csv(hexf)
     path = os.path.join(HERE, "kat_%s.npz" % material)
-    np.savez_compressed(path, rows=rows, props=np.array([1e6, 0.3]), dt=np.array(1e-3))
+    np.savez_compressed(path, rows=rows, props=np.array(props, dtype=np.float64), dt=np.array(1e-3))
     return path
+
+
+def dp_cases():
+    # dp_ri_mt (materialsrc/dp_ri_mt.c): known answers and two trajectories
+    print(kat("dp_ri_mt", props=(1e6, 0.3, 0.3819)))
+    sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="dp_ri_mt",
+                       rho=2450.0, props=(1e6, 0.3, 0.3819), dt=1e-5, jitter=5e-4, seed=1)
+    print(record_steps("dp_column", sc, [1, 50, 300], nthreads=4)[1])
+    sc = scenes.silo(cells=32, material="dp_ri_mt", props=(1e6, 0.3, 0.3819), dt=1e-5, hole_radius=0.1,
+                     open_time=0.001, wall_frac=0.5, fill_height=0.6)
+    print(record_steps("dp_silo", sc, [1, 50, 400], nthreads=4)[1])
+    sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="dp_ri_mt",
+                       rho=2450.0, props=(1e6, 0.3, 0.3819), dt=1e-5, jitter=5e-4, seed=1)
+    sc["scheme"] = "musl"
+    print(record_steps("musl_dp_column", sc, [1, 50, 300], nthreads=4)[1])
+
+
+def plane_cases():
+    # g_local_mu2_plane_strain and g_local_mu2_true_2d (E, nu from the
+    # configuration; the mu(I) constants are compile-time in the plugins)
+    for mat, tag in (("g_local_mu2_plane_strain", "ps"), ("g_local_mu2_true_2d", "t2d")):
+        print(kat(mat))
+        sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material=mat,
+                           rho=2450.0, props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+        print(record_steps("%s_column" % tag, sc, [1, 50, 300], nthreads=4)[1])
+        sc = scenes.silo(cells=32, material=mat, props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+                         open_time=0.001, wall_frac=0.5, fill_height=0.6)
+        print(record_steps("%s_silo" % tag, sc, [1, 50, 400], nthreads=4)[1])
+
+
+def ext_cases():
+    # g_local_mu2_ext: the nodal Laplacian of the local fluidity (threaded,
+    # with the team's element lists and barriers)
+    sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2_ext",
+                       rho=2450.0, props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+    print(record_steps("ext_column", sc, [1, 50, 300], nthreads=4)[1])
+    sc = scenes.silo(cells=32, material="g_local_mu2_ext", props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+                     open_time=0.001, wall_frac=0.5, fill_height=0.6)
+    print(record_steps("ext_silo", sc, [1, 50, 400], nthreads=4)[1])
 
 
 def musl_cases():
@@ -121,6 +162,15 @@ def main():
         raise SystemExit("reference tree not found; fixtures can only be generated where it exists")
     if sys.argv[1:] == ["musl"]:
         musl_cases()
+        return
+    if sys.argv[1:] == ["dp"]:
+        dp_cases()
+        return
+    if sys.argv[1:] == ["plane"]:
+        plane_cases()
+        return
+    if sys.argv[1:] == ["ext"]:
+        ext_cases()
         return
     print(kat("isolin"))
     print(kat("g_local_mu2"))
@@ -177,6 +227,9 @@ def main():
     sc["particles"]["sxy"] = np.full(n, 600.0)
     print(record_steps("nonlocal_silo", sc, [1, 10, 60], nthreads=1)[1])
     musl_cases()
+    dp_cases()
+    plane_cases()
+    ext_cases()
 
 
 if __name__ == "__main__":

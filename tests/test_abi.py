@@ -43,6 +43,8 @@ def test_default_params_are_the_reference_constants():
     assert mp[mpm2d.MP["mu_s"]] == 0.3819 and mp[mpm2d.MP["mu_2"]] == 0.6435
     assert mp[mpm2d.MP["I0"]] == 0.278 and mp[mpm2d.MP["grains_d"]] == 0.005
     assert mp[mpm2d.MP["rho_critical"]] == 1485.0
+    mp = mpm2d.default_params("dp_ri_mt")
+    assert mp[mpm2d.MP["mu_s"]] == 0.3819 and mp[mpm2d.MP["rho_critical"]] == 1485.0
     mp = mpm2d.default_params("g_nonlocal")
     assert mp[mpm2d.MP["E"]] == 1e8 and mp[mpm2d.MP["B"]] == 0.9377 * 20
     assert mp[mpm2d.MP["grains_d"]] == 0.05
@@ -74,6 +76,12 @@ def test_invalid_configuration_is_rejected():
     with pytest.raises(mpm2d.MpmError) as e:
         mpm2d.Simulation(sc)
     assert e.value.status == 16
+    cfg = mpm2d.make_config(scenes.config1())
+    cfg.material = 8                       # not an mpmg_material
+    h = mpm2d.C.c_void_p()
+    z = mpm2d.np.zeros(1)
+    rc = mpm2d.lib().mpmg_create(mpm2d.C.byref(cfg), 1, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h))
+    assert rc == 20 and not h.value
     cfg = mpm2d.make_config(scenes.config1())
     cfg.precision = 7                      # not an mpmg_precision
     h = mpm2d.C.c_void_p()

@@ -59,12 +59,16 @@ def run_driver(driver, tmp_path, scene, threads, steps, sample_rate):
     return t, frames, out
 
 
-@pytest.mark.parametrize("case", ["isolin_box", "mu2_silo"])
+@pytest.mark.parametrize("case", ["isolin_box", "mu2_silo", "dp_silo", "t2d_silo", "ext_silo"])
 def test_drop_in_driver_matches_oracle(driver, tmp_path, case):
     if case == "isolin_box":
         scene, steps = scenes.config1(seed=2), 200
     else:
-        scene = scenes.silo(cells=32, material="g_local_mu2", props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+        material, props = {"mu2_silo": ("g_local_mu2", (1e6, 0.3)),
+                           "dp_silo": ("dp_ri_mt", (1e6, 0.3, 0.3819)),
+                           "t2d_silo": ("g_local_mu2_true_2d", (1e6, 0.3)),
+                           "ext_silo": ("g_local_mu2_ext", (1e6, 0.3))}[case]
+        scene = scenes.silo(cells=32, material=material, props=props, dt=1e-5, hole_radius=0.1,
                             open_time=0.001, wall_frac=0.5, fill_height=0.6)
         steps = 300
     threads = 3
@@ -79,6 +83,6 @@ def test_drop_in_driver_matches_oracle(driver, tmp_path, case):
     e, a = orc.get_map()
     np.testing.assert_array_equal(got["active"], a)
     np.testing.assert_array_equal(got["in_element"][a == 1], e[a == 1])
-    if scene["material"] == "g_local_mu2":
+    if scene["material"] != "isolin":
         for f in ("state9", "state10"):
             assert field_err(got[f], orc.get, f) <= 1e-8, (case, f)

@@ -13,11 +13,19 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy")
 
 
-@pytest.mark.parametrize("which", ["isolin", "mu2_column"])
+@pytest.mark.parametrize("which", ["isolin", "mu2_column", "dp_column", "ext_column"])
 def test_fp64_restart_is_exact(tmp_path, which):
     if which == "isolin":
         sc = scenes.config1(seed=2)
         fields = FIELDS
+    elif which == "dp_column":
+        sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="dp_ri_mt", rho=2450.0,
+                           props=(1e6, 0.3, 0.3819), dt=1e-5, jitter=5e-4, seed=1)
+        fields = FIELDS + ("state1", "state9", "state10")
+    elif which == "ext_column":
+        sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2_ext",
+                           rho=2450.0, props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+        fields = FIELDS + ("state0", "state3", "state4", "state5", "state9", "state10")
     else:
         sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2", rho=2450.0,
                            props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)

@@ -43,10 +43,17 @@ def column_scene():
                          rho=2450.0, props=(1e6, 0.3), dt=1e-5, mp={"grains_d": 5.3e-4}, jitter=1e-3, seed=4)
 
 
+def dp_column_scene():
+    # the same column with the rate-independent Drucker-Prager law (dp_ri_mt)
+    return scenes.column(Nx=129, Ny=129, h=1 / 128, width=0.25, height=0.4, material="dp_ri_mt",
+                         rho=2450.0, props=(1e6, 0.3, 0.3819), dt=1e-5, jitter=1e-3, seed=4)
+
+
 @pytest.mark.parametrize("precision", ["mixed", "mixed_f64node"])
-@pytest.mark.parametrize("which", ["isolin_block", "mu2_column"])
+@pytest.mark.parametrize("which", ["isolin_block", "mu2_column", "dp_column"])
 def test_mixed_vs_fp64_after_100_steps(which, precision):
-    sc = scenes.config1(seed=3) if which == "isolin_block" else column_scene()
+    sc = {"isolin_block": lambda: scenes.config1(seed=3), "mu2_column": column_scene,
+          "dp_column": dp_column_scene}[which]()
     mixed = mpm2d.Simulation(sc, precision=precision)
     fp64 = mpm2d.Simulation(sc, precision="fp64")
     mixed.step(100)

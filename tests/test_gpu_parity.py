@@ -28,6 +28,27 @@ pytestmark = pytest.mark.gpu
 ONE_STEP_TOL = 1e-10
 TRAJ_TOL = 1e-9
 
+# material state compared besides the particle fields (the plugins' #define maps)
+EXTRA_STATE = {"g_local_mu2": ("Tzz", "state9", "state10"),
+               "dp_ri_mt": ("state1", "state9", "state10"),
+               "g_local_mu2_plane_strain": ("state1", "state5", "state9", "state10"),
+               "g_local_mu2_true_2d": ("state5", "state9", "state10"),
+               "g_local_mu2_ext": ("state0", "state3", "state4", "state5", "state9", "state10")}
+
+
+def check_mu_t(got, want, tol, mu_s=0.3819, mu_2=0.6435):
+    """g_local_mu2_ext's mu_t (state[0]).  With gammadotp = 0,
+    mu_from_gammadot (g_local_mu2_ext.c:75-95) returns mu_2 for p <= 0 and
+    mu_s otherwise, so a particle whose start-of-step pressure is zero up to
+    round-off can land on either constant.  In these short runs under the
+    start of the gravity ramp that is most of the column (after 299 steps
+    1152 of 2048 particles have |p| below 1e-9 of the largest; many carry an
+    exactly zeroed stress).  Particles where both values are branch constants
+    are exempt; every other particle agrees to tol."""
+    bad = np.abs(got - want) > tol * np.max(np.abs(want))
+    consts = np.array([mu_s, mu_2])
+    assert np.all(np.isin(got[bad], consts) & np.isin(want[bad], consts)), (got[bad], want[bad])
+
 
 def restart_sim(scene, d, step, store_transients=True, **kw):
     """GPU simulation restarted from the reference's state after `step`."""
@@ -97,7 +118,8 @@ def test_gpu_one_step_from_reference_state(case, step, material):
         assert field_err(sim.get(f), want, f) <= ONE_STEP_TOL, f
 
 
-@pytest.mark.parametrize("case", ["config1", "mu2_column", "mu2_silo"])
+@pytest.mark.parametrize("case", ["config1", "mu2_column", "mu2_silo", "dp_column", "dp_silo", "ps_column",
+                                  "ps_silo", "t2d_column", "t2d_silo", "ext_column", "ext_silo"])
 def test_gpu_trajectory_matches_golden(case):
     scene, d = load_golden(case)
     sim = mpm2d.Simulation(scene, store_transients=True)
@@ -112,16 +134,19 @@ def test_gpu_trajectory_matches_golden(case):
             assert field_err(sim.get(f), want, f) <= tol, (case, c, f, field_err(sim.get(f), want, f))
         for f in ("node_m", "node_mx", "node_my", "node_fx", "node_fy"):
             assert field_err(sim.get(f), want, f) <= tol, (case, c, f, field_err(sim.get(f), want, f))
-        if scene["material"] == "g_local_mu2":
-            for f in ("Tzz", "state9", "state10"):
-                assert field_err(sim.get(f), want, f) <= max(tol, 1e-8), (case, c, f)
+        extra = EXTRA_STATE.get(scene["material"], ())
+        for f in extra:
+            if scene["material"] == "g_local_mu2_ext" and f == "state0":
+                check_mu_t(sim.get(f), want(f), max(tol, 1e-8))
+                continue
+            assert field_err(sim.get(f), want, f) <= max(tol, 1e-8), (case, c, f)
         e, a = sim.get_map()
         np.testing.assert_array_equal(a, d["s%d_active" % c])
         np.testing.assert_array_equal(e[a == 1], d["s%d_in_element" % c][a == 1])
         assert sim.t == float(d["s%d_t" % c])
 
 
-@pytest.mark.parametrize("case", ["musl_config1", "musl_mu2_column"])
+@pytest.mark.parametrize("case", ["musl_config1", "musl_mu2_column", "musl_dp_column"])
 def test_gpu_musl_trajectory_matches_golden(case):
     """explicit_mpm_step_musl_threaded (process_usl.c:284-462) against the
     reference's own MUSL run.  The reference's nodal forces after a MUSL
@@ -141,9 +166,9 @@ def test_gpu_musl_trajectory_matches_golden(case):
             assert field_err(sim.get(f), want, f) <= tol, (case, c, f, field_err(sim.get(f), want, f))
         for f in ("node_m", "node_mx", "node_my", "node_vx", "node_vy"):
             assert field_err(sim.get(f), want, f) <= tol, (case, c, f, field_err(sim.get(f), want, f))
-        if scene["material"] == "g_local_mu2":
-            for f in ("Tzz", "state9", "state10"):
-                assert field_err(sim.get(f), want, f) <= max(tol, 1e-8), (case, c, f)
+        extra = EXTRA_STATE.get(scene["material"], ())
+        for f in extra:
+            assert field_err(sim.get(f), want, f) <= max(tol, 1e-8), (case, c, f)
         e, a = sim.get_map()
         np.testing.assert_array_equal(a, d["s%d_active" % c])
         assert sim.t == float(d["s%d_t" % c])
@@ -196,7 +221,8 @@ def test_gpu_one_step_vs_oracle_from_checkpoint(case):
             assert e <= ONE_STEP_TOL, (case, step, f, e)
 
 
-@pytest.mark.parametrize("kind", ["isolin", "g_local_mu2"])
+@pytest.mark.parametrize("kind", ["isolin", "g_local_mu2", "dp_ri_mt", "g_local_mu2_plane_strain",
+                                  "g_local_mu2_true_2d"])
 def test_gpu_material_known_answers_bit_exact(kind):
     """The device material functions reproduce tests/test_material.c's %a
     output exactly."""
