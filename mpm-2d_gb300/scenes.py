@@ -146,6 +146,20 @@ def ensemble(count=256, seed=1, ppc_1d=2, cells_range=(64, 384), particles_range
     return out
 
 
+def column_2x05(fine=False, gravity=-9.81):
+    """The rectangular column-collapse workload: a 0.4 x 0.3 m g_local_mu2
+    column (mu(I) constants of the reference, grain size 5.3e-4 m) at 2 x 2
+    particles per element in a 2 x 0.5 m box, dt 2e-6.  fine=False: 512 x 128
+    elements (h = 1/256, 31 212 particles); fine=True: 1024 x 256 elements
+    (h = 1/512, 125 563 particles).  Constant gravity by default (the
+    reference's ramp reaches only a tenth of g in the 5000 steps the workload
+    runs)."""
+    n = 1024 if fine else 512
+    h = 2.0 / n
+    return column(Nx=n + 1, Ny=n // 4 + 1, h=h, width=0.4, height=0.3, ppc_1d=2, material="g_local_mu2",
+                  rho=2450.0, props=(1e6, 0.3), dt=2e-6, gravity=gravity, mp={"grains_d": 5.3e-4})
+
+
 def adjoint_column(theta=(0.3819, 0.6435, 0.278, 1e6), seed=2):
     """The adjoint benchmark: a 0.25 x 0.25 m g_local_mu2 column (64 x 64
     elements at 4 x 4 particles each: 65 536 particles) in a 1 x 0.5 m box of

@@ -19,6 +19,9 @@ MATERIALS = {"isolin": 0, "g_local_mu2": 1, "g_nonlocal_mu2": 2, "g_nonlocal": 3
              "g_local_mu2_plane_strain": 5, "g_local_mu2_true_2d": 6,
              "g_local_mu2_ext": 7}
 BCS = {"box": 0, "square_silo": 1}
+# material parameter slots by name (enum orc_mparam)
+MP = {"E": 0, "nu": 1, "mu_s": 2, "mu_2": 3, "I0": 4, "grains_rho": 5, "grains_d": 6, "A": 7,
+      "rho_critical": 8, "B": 9, "cohesion": 10}
 MP_COUNT = 16
 PARTICLE_FIELDS = ["x", "y", "xl", "yl", "v", "v0", "m", "vx", "vy", "ax", "ay", "bx", "by",
                    "sxx", "sxy", "syy", "ux", "uy", "exx", "exy", "eyy", "wxy",
@@ -109,7 +112,7 @@ class Oracle:
             if scene["material"] == "dp_ri_mt" and len(props) > 2:
                 mp[2] = props[2]   # dp_ri_mt.c:73 fp64_props[2] = mu_s
         for k, val in scene.get("mp", {}).items():
-            mp[k] = val
+            mp[MP[k] if isinstance(k, str) else k] = val
         for k in range(MP_COUNT):
             cfg.mp[k] = mp[k]
         cfg.bc = BCS[scene["bc"]]

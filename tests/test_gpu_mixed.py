@@ -150,6 +150,29 @@ def test_mixed_column_runout_within_1pct():
     assert abs(xm - xf) <= 0.01 * xf, (xm, xf)
 
 
+@pytest.mark.parametrize("fine", [False, True])
+def test_mixed_rectangular_column_full_run(fine):
+    """The rectangular column-collapse workload run for its full 5000 steps
+    (0.01 s) in both forms: 512 x 128 elements with 31 212 particles, and
+    1024 x 256 elements with 125 563; the mixed form against the FP64 form
+    to the mixed form's 1e-4, same active set."""
+    sc = scenes.column_2x05(fine=fine)
+    mixed = mpm2d.Simulation(sc, precision="mixed")
+    fp64 = mpm2d.Simulation(sc, precision="fp64")
+    mixed.step(5000)
+    fp64.step(5000)
+    assert mixed.t == fp64.t
+    for f in FIELDS:
+        assert group_rel_l2(mixed.get, fp64.get, f) <= 1e-4, (fine, f, group_rel_l2(mixed.get, fp64.get, f))
+    em, am = mixed.get_map()
+    ef, af = fp64.get_map()
+    assert np.array_equal(am, af)
+    assert np.mean(em == ef) > 0.999
+    # the column has started to move: its top has dropped
+    y0 = sc["particles"]["y"].max()
+    assert fp64.get("y").max() < y0
+
+
 def nonlocal_silo(cells=32):
     # the pre-stressed nonlocal silo of the golden fixtures: lithostatic syy,
     # no particle at p = 0 where the dense flag switches on round-off

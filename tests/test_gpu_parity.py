@@ -146,6 +146,31 @@ def test_gpu_trajectory_matches_golden(case):
         assert sim.t == float(d["s%d_t" % c])
 
 
+def test_gpu_rectangular_domain_vs_oracle():
+    """The 2 x 0.5 m column on 512 x 128 elements (31 212 particles), the
+    rectangular workload: FP64 GPU against the oracle (whose element map
+    follows WHICH_ELEMENT4 with the domain's own extent; the reference's
+    hard-codes the unit square) over 200 steps."""
+    sc = scenes.column_2x05()
+    assert (sc["Nx"], sc["Ny"], len(sc["particles"]["x"])) == (513, 129, 31212)
+    sim = mpm2d.Simulation(sc, store_transients=True)
+    orc = O.Oracle(sc, nthreads=4)
+    done = 0
+    for c in (1, 50, 200):
+        sim.step(c - done)
+        orc.step(c - done)
+        done = c
+        tol = ONE_STEP_TOL if c == 1 else TRAJ_TOL
+        for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy"):
+            assert field_err(sim.get(f), orc.get, f) <= tol, (c, f, field_err(sim.get(f), orc.get, f))
+        for f in ("node_m", "node_mx", "node_my", "node_fx", "node_fy"):
+            assert field_err(sim.get(f), orc.get, f) <= tol, (c, f)
+        e, a = sim.get_map()
+        oe, oa = orc.get_map()
+        np.testing.assert_array_equal(a, oa)
+        np.testing.assert_array_equal(e[a == 1], oe[oa == 1])
+
+
 @pytest.mark.parametrize("case", ["musl_config1", "musl_mu2_column", "musl_dp_column"])
 def test_gpu_musl_trajectory_matches_golden(case):
     """explicit_mpm_step_musl_threaded (process_usl.c:284-462) against the
