@@ -203,6 +203,23 @@ MPMG_API int mpmg_set_map(mpmg_ctx *ctx, const int *in_element, const int *activ
    and per-element start offsets (num_elements + 1 entries). */
 MPMG_API int mpmg_get_sort(mpmg_ctx *ctx, int *sorted_keys, int *perm, int *cell_start);
 
+/* Online tuning of a mixed-form context's launch shape (no counterpart in the
+   reference): the persistent G2P grid (1 up to as many blocks per SM as fit)
+   and the steps per replayed CUDA graph (4, 8, 16).  Every candidate runs the simulation itself
+   (a warm-up graph, then steps_per_trial steps rounded up to whole graphs,
+   timed with CUDA events) and the fastest is kept for later steps.  Neither
+   knob changes any result: the trajectory is the untuned one, advanced by
+   steps_advanced steps. */
+typedef struct mpmg_tuning {
+    int g2p_blocks_per_sm;
+    int graph_steps;
+    double ms_per_step;          /* of the configuration kept */
+    double default_ms_per_step;  /* of the default (all G2P blocks that fit, 8 steps per graph) */
+    int candidates;
+    int steps_advanced;
+} mpmg_tuning;
+MPMG_API int mpmg_autotune(mpmg_ctx *ctx, int steps_per_trial, mpmg_tuning *best);
+
 MPMG_API int mpmg_get_time(mpmg_ctx *ctx, double *t, int *step_number);
 MPMG_API int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number);
 MPMG_API int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *num_elements);

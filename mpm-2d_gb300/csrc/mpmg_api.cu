@@ -11,6 +11,8 @@
 #include "mpmg_internal.cuh"
 
 namespace {
+
+void drop_graphs(mpmg_ctx *ctx);   // cached step graphs, recaptured on next use
 thread_local char g_last_error[512] = "";
 
 const char *kPhaseNames[PH_COUNT] = {"keys", "sort", "p2g", "grid", "g2p", "fluidity"};
@@ -371,10 +373,7 @@ int mpmg_destroy(mpmg_ctx *ctx)
         delete ctx->batch;
         ctx->batch = nullptr;
     }
-    for (int p = 0; p < 2; p++) {
-        if (ctx->graph_chunk[p]) cudaGraphExecDestroy(ctx->graph_chunk[p]);
-        if (ctx->graph_single[p]) cudaGraphExecDestroy(ctx->graph_single[p]);
-    }
+    drop_graphs(ctx);
     for (int k = 0; k < 2 * PH_COUNT; k++)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -858,20 +857,30 @@ bool graphs_apply(const mpmg_ctx *ctx)
     return !nonlocal && !ctx->timing;
 }
 
+void drop_graphs(mpmg_ctx *ctx)
+{
+    for (int p = 0; p < 2; p++) {
+        if (ctx->graph_chunk[p]) cudaGraphExecDestroy(ctx->graph_chunk[p]);
+        if (ctx->graph_single[p]) cudaGraphExecDestroy(ctx->graph_single[p]);
+        ctx->graph_chunk[p] = ctx->graph_single[p] = nullptr;
+    }
+}
+
 int step_with_graphs(mpmg_ctx *ctx, int nsteps)
 {
+    const int chunk_steps = ctx->graph_steps > 0 ? ctx->graph_steps : MPMG_GRAPH_CHUNK;
     while (nsteps > 0) {
         const int p = parity(ctx);
-        const bool chunk = nsteps >= MPMG_GRAPH_CHUNK;
+        const bool chunk = nsteps >= chunk_steps;
         cudaGraphExec_t *g = chunk ? &ctx->graph_chunk[p] : &ctx->graph_single[p];
         long *gl = chunk ? &ctx->graph_chunk_launches[p] : &ctx->graph_single_launches[p];
         if (*g == nullptr) {
-            int rc = capture_steps(ctx, chunk ? MPMG_GRAPH_CHUNK : 1, g, gl);
+            int rc = capture_steps(ctx, chunk ? chunk_steps : 1, g, gl);
             if (rc != MPMG_OK) return rc;
         }
         MPMG_CHECK(cudaGraphLaunch(*g, ctx->stream));
         ctx->launches += *gl;
-        const int done = chunk ? MPMG_GRAPH_CHUNK : 1;
+        const int done = chunk ? chunk_steps : 1;
         if (ctx->mixed && (done & 1)) ctx->mixed->cur ^= 1;
         nsteps -= done;
     }
@@ -881,6 +890,80 @@ int step_with_graphs(mpmg_ctx *ctx, int nsteps)
 }  // namespace
 
 extern "C" {
+
+// Online tuning of the mixed step's launch shape.  Each candidate (G2P
+// blocks per SM x steps per graph) runs the simulation itself for a warm-up
+// graph and then steps_per_trial steps (rounded up to whole graphs) timed
+// with CUDA events; the fastest is kept.  Neither knob changes any result,
+// so the trajectory is the one an untuned run takes; it advances by every
+// trial's steps.
+int mpmg_autotune(mpmg_ctx *ctx, int steps_per_trial, mpmg_tuning *best)
+{
+    if (ctx == nullptr || best == nullptr || steps_per_trial < 1) return MPMG_ERR_INVALID;
+    if (ctx->mixed == nullptr || !graphs_apply(ctx)) {
+        mpmg_set_error("autotuning applies to the mixed forms stepped through CUDA graphs");
+        return MPMG_ERR_UNSUPPORTED;
+    }
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    memset(best, 0, sizeof(*best));
+    const int chunk_opts[3] = {4, 8, 16};
+    const int per_sm_max = ctx->mixed->g2p_per_sm_max;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    MPMG_CHECK(cudaEventCreate(&e0));
+    MPMG_CHECK(cudaEventCreate(&e1));
+    int rc = MPMG_OK;
+    double best_ms = 1e30, default_ms = 0;
+    int best_ps = 0, best_ch = 0, tried = 0, advanced = 0, last_ps = -1;
+    for (int a = 1; a <= per_sm_max && rc == MPMG_OK; a++) {
+        const int ps = mpmg_mixed_set_g2p_per_sm(ctx, a);
+        if (ps == last_ps) continue;   // clamped to one already tried
+        last_ps = ps;
+        for (int b = 0; b < 3 && rc == MPMG_OK; b++) {
+            const int ch = chunk_opts[b];
+            ctx->graph_steps = ch;
+            drop_graphs(ctx);
+            const int trial = ((steps_per_trial + ch - 1) / ch) * ch;
+            rc = step_with_graphs(ctx, ch);                    // capture and warm up
+            if (rc != MPMG_OK) break;
+            if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { rc = MPMG_ERR_CUDA; break; }
+            rc = step_with_graphs(ctx, trial);
+            if (rc != MPMG_OK) break;
+            if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = MPMG_ERR_CUDA;
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            const double per = ms / trial;
+            advanced += ch + trial;
+            tried += 1;
+            if (ps == per_sm_max && ch == MPMG_GRAPH_CHUNK) default_ms = per;
+            if (per < best_ms) {
+                best_ms = per;
+                best_ps = ps;
+                best_ch = ch;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == MPMG_OK) rc = sync_status(ctx);
+    if (tried > 0) {
+        mpmg_mixed_set_g2p_per_sm(ctx, best_ps);
+        ctx->graph_steps = best_ch;
+    } else {
+        mpmg_mixed_set_g2p_per_sm(ctx, ctx->mixed->g2p_per_sm_max);
+        ctx->graph_steps = MPMG_GRAPH_CHUNK;
+    }
+    drop_graphs(ctx);
+    best->g2p_blocks_per_sm = best_ps;
+    best->graph_steps = best_ch;
+    best->ms_per_step = best_ms < 1e30 ? best_ms : 0.0;
+    best->default_ms_per_step = default_ms;
+    best->candidates = tried;
+    best->steps_advanced = advanced;
+    return rc;
+}
 
 int mpmg_step(mpmg_ctx *ctx, int nsteps)
 {

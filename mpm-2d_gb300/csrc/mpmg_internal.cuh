@@ -67,6 +67,8 @@ struct MixedState {
     float4 *node4;         // per node: ax, ay, vx, vy (FP32) for the gathers
     float2 *node_mass;     // per node: mass as float-float (hi, lo)
     int g2p_blocks;        // persistent G2P grid size
+    int g2p_per_sm_max;    // G2P blocks that fit on one SM
+    int sms;
     double *export_buf;    // one FP64 particle field in caller order, for read-back
     float4 *nl_E, *nl_F;   // g_nonlocal_mu2: strain rate and bulk fluidity per stored particle
 };
@@ -159,7 +161,8 @@ struct mpmg_ctx {
     MixedState *mixed;
 
     // CUDA graphs of whole steps (index: buffer parity of the mixed form):
-    // a chunk of MPMG_GRAPH_CHUNK steps and a single step, captured on first use.
+    // a chunk of graph_steps steps and a single step, captured on first use.
+    int graph_steps;       // MPMG_GRAPH_CHUNK unless tuned (mpmg_autotune)
     cudaGraphExec_t graph_chunk[2];
     cudaGraphExec_t graph_single[2];
     long graph_chunk_launches[2];
@@ -226,6 +229,7 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
                     const double *vx, const double *vy, const double *sxx, const double *sxy,
                     const double *syy);
 void mpmg_mixed_free(mpmg_ctx *ctx);
+int mpmg_mixed_set_g2p_per_sm(mpmg_ctx *ctx, int per_sm);   // returns the value set
 int mpmg_mixed_step(mpmg_ctx *ctx);
 // Host read-back / write of a mixed particle or node field; returns
 // MPMG_ERR_UNKNOWN_FIELD for names the mixed state does not hold.

@@ -1159,12 +1159,26 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     G2PKernel g2p = g2p_variant(ctx->cfg.material, bt != nullptr);
     MPMG_CHECK(cudaFuncSetAttribute(g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG2PSmem));
     MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g2p, kG2PTile, kG2PSmem));
-    const size_t tiles = (n + kG2PTile - 1) / kG2PTile;
-    size_t blocks = (size_t)(sms > 0 ? sms : 1) * (size_t)(per_sm > 0 ? per_sm : 1);
-    if (blocks > tiles) blocks = tiles;
-    s->g2p_blocks = (int)(blocks > 0 ? blocks : 1);
+    s->sms = sms > 0 ? sms : 1;
+    s->g2p_per_sm_max = per_sm > 0 ? per_sm : 1;
+    mpmg_mixed_set_g2p_per_sm(ctx, s->g2p_per_sm_max);
     // the first step's element counts; every G2P counts the next step's
     return mpmg_bin_count(ctx, (const uint32_t *)ctx->in_element);
+}
+
+// Persistent G2P grid of per_sm blocks per SM (clamped to what fits), at
+// most one block per tile.  Which block takes which tile does not change any
+// particle's result.
+int mpmg_mixed_set_g2p_per_sm(mpmg_ctx *ctx, int per_sm)
+{
+    MixedState *s = ctx->mixed;
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > s->g2p_per_sm_max) per_sm = s->g2p_per_sm_max;
+    const size_t tiles = (ctx->np + kG2PTile - 1) / kG2PTile;
+    size_t blocks = (size_t)s->sms * (size_t)per_sm;
+    if (blocks > tiles) blocks = tiles;
+    s->g2p_blocks = (int)(blocks > 0 ? blocks : 1);
+    return per_sm;
 }
 
 void mpmg_mixed_free(mpmg_ctx *ctx)

@@ -54,6 +54,11 @@ class Config(C.Structure):
 _lib = None
 
 
+class Tuning(C.Structure):
+    _fields_ = [("g2p_blocks_per_sm", C.c_int), ("graph_steps", C.c_int), ("ms_per_step", C.c_double),
+                ("default_ms_per_step", C.c_double), ("candidates", C.c_int), ("steps_advanced", C.c_int)]
+
+
 def library_path():
     return _build.LIB
 
@@ -88,6 +93,7 @@ def lib(build_if_missing=True):
         L.mpmg_read_state.argtypes = [vp, C.POINTER(Config), C.POINTER(vp)]
         L.mpmg_adj_forward_tape.argtypes = [vp, C.c_int, C.c_int]
         L.mpmg_adj_backward.argtypes = [vp, dp, dp, dp]
+        L.mpmg_autotune.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
         L.mpmg_adj_state.argtypes = [vp, C.c_char_p, dp]
         L.mpmg_get_map.argtypes = [vp, ip, ip]
         L.mpmg_set_map.argtypes = [vp, ip, ip]
@@ -225,6 +231,13 @@ class Simulation:
 
     def step(self, n=1):
         _check(lib().mpmg_step(self._h, n))
+
+    def autotune(self, steps_per_trial=16):
+        """Online tuning of the mixed step's launch shape (mpmg_autotune):
+        advances the simulation by the returned steps_advanced."""
+        t = Tuning()
+        _check(lib().mpmg_autotune(self._h, steps_per_trial, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
 
     def synchronize(self):
         _check(lib().mpmg_synchronize(self._h))

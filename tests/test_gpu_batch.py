@@ -78,3 +78,22 @@ def test_batch_deterministic():
         b.close()
     for u, v in zip(*runs):
         np.testing.assert_array_equal(u, v)
+
+
+def test_autotune_keeps_the_trajectory():
+    """mpmg_autotune times launch shapes on the simulation itself; neither
+    knob changes a result, so a tuned batch continues bit for bit like an
+    untuned one advanced by the same steps."""
+    ens = small_ensemble(count=3, seed=9)
+    tuned = mpm2d.Batch(ens, precision="mixed")
+    plain = mpm2d.Batch(ens, precision="mixed")
+    t = tuned.autotune(steps_per_trial=8)
+    assert t["candidates"] >= 3 and t["graph_steps"] in (4, 8, 16) and t["g2p_blocks_per_sm"] >= 1
+    assert t["ms_per_step"] > 0 and t["ms_per_step"] <= t["default_ms_per_step"]
+    plain.step(t["steps_advanced"])
+    tuned.step(37)
+    plain.step(37)
+    for k in range(3):
+        for f in FIELDS:
+            np.testing.assert_array_equal(tuned.member_get(k, f), plain.member_get(k, f), err_msg="%d %s" % (k, f))
+
