@@ -159,6 +159,50 @@ __device__ __forceinline__ double grid_total(const double *partials, int slot, i
     return out;
 }
 
+// Slots a, b, c of the per-block partials summed in one pass, each in the
+// same fixed order as grid_total; every block gets the same three values.
+__device__ __forceinline__ void grid_total3(const double *partials, int a, int b, int c, int nblocks, double &ta,
+                                            double &tb, double &tc)
+{
+    __shared__ double sh[3][kSolveThreads / 32];
+    __shared__ double res[3];
+    double x = 0, y = 0, z = 0;
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
+        x += __ldcg(partials + (size_t)a * nblocks + k);
+        y += __ldcg(partials + (size_t)b * nblocks + k);
+        z += __ldcg(partials + (size_t)c * nblocks + k);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, off);
+        y += __shfl_down_sync(0xffffffffu, y, off);
+        z += __shfl_down_sync(0xffffffffu, z, off);
+    }
+    if (lane == 0) {
+        sh[0][w] = x;
+        sh[1][w] = y;
+        sh[2][w] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        for (int k = 0; k < kSolveThreads / 32; k++) {
+            s0 += sh[0][k];
+            s1 += sh[1][k];
+            s2 += sh[2][k];
+        }
+        res[0] = s0;
+        res[1] = s1;
+        res[2] = s2;
+    }
+    __syncthreads();
+    ta = res[0];
+    tb = res[1];
+    tc = res[2];
+    __syncthreads();
+}
+
 // Row of node (i, j) as a 9-point stencil and its right-hand side: the four
 // elements around the node (south-west, south-east, north-west, north-east),
 // each element's corners in order.  The node is corner a = TR, TL, BR, BL of
@@ -297,9 +341,7 @@ __global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
         S.partials[3 * nblocks + blockIdx.x] = rr;
     }
     if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
-    gamma = grid_total(S.partials, 0, nblocks);
-    delta = grid_total(S.partials, 1, nblocks);
-    rr = grid_total(S.partials, 3, nblocks);
+    grid_total3(S.partials, 0, 1, 3, nblocks, gamma, delta, rr);
     const double target = S.tol * S.tol * bb;
 
     int it = 0;
@@ -344,9 +386,7 @@ __global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
             S.partials[3 * nblocks + blockIdx.x] = rn;
         }
         if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
-        gn = grid_total(S.partials, 0, nblocks);
-        dl = grid_total(S.partials, 1, nblocks);
-        rr = grid_total(S.partials, 3, nblocks);
+        grid_total3(S.partials, 0, 1, 3, nblocks, gn, dl, rr);
         it++;
         if (!(rr == rr)) break;   // NaN: give up
         converged = (rr <= target);
