@@ -251,7 +251,8 @@ MPMG_API job_t *mpm_init(int N, double h, particle_t *particles, size_t num_part
  * runs the whole step on the GPU (attaching on the first call: the material
  * and boundary conditions are chosen by the plugin file's basename, isolin,
  * g_local_mu2, g_nonlocal_mu2, g_nonlocal, dp_ri_mt, g_local_mu2_plane_strain,
- * g_local_mu2_true_2d, g_local_mu2_ext / box, square_silo) while the rest
+ * g_local_mu2_true_2d, g_local_mu2_ext, g_nonlocal_avg, g_nonlocal_bicgstab,
+ * g_nonlocalxs71 / box, square_silo) while the rest
  * wait; then job->t advances and, when the driver will write a frame after
  * this step (job->t >= job->frame / sample_rate) or the run ends, the host
  * particle array is refreshed from the GPU.  On a GPU error it prints the

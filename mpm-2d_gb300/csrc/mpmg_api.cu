@@ -53,6 +53,7 @@ bool material_uses_state(int material, int k)
     case MPMG_G_NONLOCAL_MU2:   // g_nonlocal_mu2.c:49-57
         return k == 0 || k == 3 || k == 4 || k == 5 || k == 6 || k == 9 || k == 10;
     case MPMG_G_NONLOCAL:       // g_nonlocal.c:51-61
+    case MPMG_G_NONLOCAL_AVG:
         return k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
     case MPMG_DP_RI_MT:         // dp_ri_mt.c:27-29 (szz, gammap, gammadotp)
         return k == 1 || k == 9 || k == 10;
@@ -311,7 +312,8 @@ int mpmg_default_params(int material, double *mp)
         mp[MPMG_MP_GRAINS_D] = 0.01 * 5;
         mp[MPMG_MP_RHO_CRITICAL] = 1485.0f;
         return MPMG_OK;
-    case MPMG_G_NONLOCAL:       // g_nonlocal.c:31-48
+    case MPMG_G_NONLOCAL:       // g_nonlocal.c:31-48 (g_nonlocal_avg.c the same)
+    case MPMG_G_NONLOCAL_AVG:
         mp[MPMG_MP_E] = 1e8;
         mp[MPMG_MP_NU] = 0.3;
         mp[MPMG_MP_MU_S] = 0.3819;
@@ -396,7 +398,7 @@ int validate_config(const mpmg_config *cfg, size_t n)
         mpmg_set_error("grid or particle count exceeds 32-bit indexing");
         return MPMG_ERR_INVALID;
     }
-    if (cfg->material < MPMG_ISOLIN || cfg->material > MPMG_G_LOCAL_MU2_EXT) {
+    if (cfg->material < MPMG_ISOLIN || cfg->material > MPMG_G_NONLOCAL_AVG) {
         mpmg_set_error("unknown material kind %d", cfg->material);
         return MPMG_ERR_UNSUPPORTED;
     }
@@ -415,6 +417,7 @@ int validate_config(const mpmg_config *cfg, size_t n)
     if (cfg->scheme == MPMG_SCHEME_MUSL &&
         (cfg->precision != MPMG_PRECISION_FP64 ||
          cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL ||
+         cfg->material == MPMG_G_NONLOCAL_AVG ||
          cfg->material == MPMG_G_LOCAL_MU2_EXT)) {
         mpmg_set_error("the MUSL step runs in the FP64 form for the particle-local materials");
         return MPMG_ERR_UNSUPPORTED;
@@ -541,10 +544,11 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
     }
     {
         const bool transients = cfg->store_transients != 0;
-        const bool nonlocal = cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL;
+        const bool nonlocal = cfg->material == MPMG_G_NONLOCAL_MU2 || cfg->material == MPMG_G_NONLOCAL ||
+                              cfg->material == MPMG_G_NONLOCAL_AVG;
         const bool mixed =
             cfg->precision == MPMG_PRECISION_MIXED || cfg->precision == MPMG_PRECISION_MIXED_F64NODE;
-        if (mixed && cfg->material == MPMG_G_NONLOCAL) {
+        if (mixed && (cfg->material == MPMG_G_NONLOCAL || cfg->material == MPMG_G_NONLOCAL_AVG)) {
             mpmg_set_error("mixed precision supports isolin, g_local_mu2 and g_nonlocal_mu2");
             rc = MPMG_ERR_UNSUPPORTED;
             goto fail;
@@ -853,7 +857,8 @@ int capture_steps(mpmg_ctx *ctx, int steps, cudaGraphExec_t *out, long *launches
 // phase timing run eagerly instead.
 bool graphs_apply(const mpmg_ctx *ctx)
 {
-    const bool nonlocal = ctx->cfg.material == MPMG_G_NONLOCAL_MU2 || ctx->cfg.material == MPMG_G_NONLOCAL;
+    const bool nonlocal = ctx->cfg.material == MPMG_G_NONLOCAL_MU2 || ctx->cfg.material == MPMG_G_NONLOCAL ||
+                          ctx->cfg.material == MPMG_G_NONLOCAL_AVG;
     return !nonlocal && !ctx->timing;
 }
 
@@ -1181,6 +1186,7 @@ int mpmg_material_only(mpmg_ctx *ctx)
 {
     if (ctx == nullptr) return MPMG_ERR_INVALID;
     if (ctx->cfg.material == MPMG_G_NONLOCAL_MU2 || ctx->cfg.material == MPMG_G_NONLOCAL ||
+        ctx->cfg.material == MPMG_G_NONLOCAL_AVG ||
         ctx->cfg.material == MPMG_G_LOCAL_MU2_EXT || ctx->mixed) {
         mpmg_set_error("material-only update is defined for local materials in FP64");
         return MPMG_ERR_UNSUPPORTED;

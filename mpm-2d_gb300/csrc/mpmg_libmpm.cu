@@ -70,7 +70,8 @@ int material_kind(const char *file)
     if (b == "isolin") return MPMG_ISOLIN;
     if (b == "g_local_mu2") return MPMG_G_LOCAL_MU2;
     if (b == "g_nonlocal_mu2") return MPMG_G_NONLOCAL_MU2;
-    if (b == "g_nonlocal") return MPMG_G_NONLOCAL;
+    if (b == "g_nonlocal" || b == "g_nonlocalxs71") return MPMG_G_NONLOCAL;   // xs71: the same code
+    if (b == "g_nonlocal_avg" || b == "g_nonlocal_bicgstab") return MPMG_G_NONLOCAL_AVG;
     if (b == "dp_ri_mt") return MPMG_DP_RI_MT;
     if (b == "g_local_mu2_plane_strain") return MPMG_G_LOCAL_MU2_PLANE_STRAIN;
     if (b == "g_local_mu2_true_2d") return MPMG_G_LOCAL_MU2_TRUE_2D;
@@ -92,7 +93,8 @@ bool uses_state(int material, int k)
     switch (material) {
     case MPMG_G_LOCAL_MU2: return k == 9 || k == 10;
     case MPMG_G_NONLOCAL_MU2: return k == 0 || k == 3 || k == 4 || k == 5 || k == 6 || k == 9 || k == 10;
-    case MPMG_G_NONLOCAL: return k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
+    case MPMG_G_NONLOCAL:
+    case MPMG_G_NONLOCAL_AVG: return k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
     case MPMG_DP_RI_MT: return k == 1 || k == 9 || k == 10;
     case MPMG_G_LOCAL_MU2_PLANE_STRAIN: return k == 1 || k == 5 || k == 9 || k == 10;
     case MPMG_G_LOCAL_MU2_TRUE_2D: return k == 5 || k == 9 || k == 10;
@@ -313,7 +315,7 @@ int mpm_gpu_attach(job_t *job)
     cfg.dt = job->dt;
     cfg.material = mat;
     mpmg_default_params(mat, cfg.mp);
-    if (mat != MPMG_G_NONLOCAL) {
+    if (mat != MPMG_G_NONLOCAL && mat != MPMG_G_NONLOCAL_AVG) {
         // E and nu from the configuration (isolin.c:46-51, g_local_mu2.c:131-140);
         // g_nonlocal.c fixes them at compile time.
         if (job->material.num_fp64_props < 2) {

@@ -407,7 +407,9 @@ __global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
 
 // Nodal fluidity back to the particles, then the stress update
 // (g_nonlocal_mu2.c:545-564 and :160-218; g_nonlocal.c:559-578, :154-298).
-template <bool MU2>
+// AVG: the element average of the four nodal values instead of the shape
+// functions (g_nonlocal_avg.c:575-578).
+template <bool MU2, bool AVG>
 __global__ void __launch_bounds__(256) fluidity_stress_kernel(
     int n, int Nx, int Ex, mat::Elastic el, mat::NonlocalParams np, const StepParams *__restrict__ sp,
     const int *__restrict__ active, const int *__restrict__ in_element, const double *__restrict__ xl,
@@ -427,10 +429,17 @@ __global__ void __launch_bounds__(256) fluidity_stress_kernel(
         const double a = xl[i], b = yl[i];
         const double ox = 1 - a, oy = 1 - b;
         double g = 0;
-        g += node_gf[n0] * (ox * oy);
-        g += node_gf[n0 + 1] * (a * oy);
-        g += node_gf[n0 + 1 + Nx] * (a * b);
-        g += node_gf[n0 + Nx] * (ox * b);
+        if (AVG) {
+            g += 0.25 * node_gf[n0];
+            g += 0.25 * node_gf[n0 + 1];
+            g += 0.25 * node_gf[n0 + 1 + Nx];
+            g += 0.25 * node_gf[n0 + Nx];
+        } else {
+            g += node_gf[n0] * (ox * oy);
+            g += node_gf[n0 + 1] * (a * oy);
+            g += node_gf[n0 + 1 + Nx] * (a * b);
+            g += node_gf[n0 + Nx] * (ox * b);
+        }
         gf[i] = g;
     }
     if (MU2) {
@@ -583,12 +592,14 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     el.lambda = ctx->lambda;
     el.dt = c.dt;
     if (mu2) {
-        fluidity_stress_kernel<true><<<blocks_for(n, 256), 256, 0, s>>>(
+        fluidity_stress_kernel<true, false><<<blocks_for(n, 256), 256, 0, s>>>(
             n, c.Nx, ctx->Ex, el, np, ctx->d_params, ctx->active, ctx->in_element, ctx->xl, ctx->yl,
             ctx->node_gf, ctx->exx, ctx->exy, ctx->eyy, ctx->wxy, ctx->state[0], ctx->state[3], ctx->sxx,
             ctx->sxy, ctx->syy, ctx->state[9], ctx->state[10]);
     } else {
-        fluidity_stress_kernel<false><<<blocks_for(n, 256), 256, 0, s>>>(
+        auto k = c.material == MPMG_G_NONLOCAL_AVG ? fluidity_stress_kernel<false, true>
+                                                   : fluidity_stress_kernel<false, false>;
+        k<<<blocks_for(n, 256), 256, 0, s>>>(
             n, c.Nx, ctx->Ex, el, np, ctx->d_params, ctx->active, ctx->in_element, ctx->xl, ctx->yl,
             ctx->node_gf, ctx->exx, ctx->exy, ctx->eyy, ctx->wxy, ctx->state[0], ctx->state[3], ctx->sxx,
             ctx->sxy, ctx->syy, ctx->state[9], ctx->state[10]);

@@ -684,7 +684,7 @@ int mpmg_launch_step(mpmg_ctx *ctx)
     mpmg_phase_end(ctx, PH_G2P);
     MPMG_CHECK(cudaGetLastError());
 
-    if (c.material == MPMG_G_NONLOCAL_MU2 || c.material == MPMG_G_NONLOCAL) {
+    if (c.material == MPMG_G_NONLOCAL_MU2 || c.material == MPMG_G_NONLOCAL || c.material == MPMG_G_NONLOCAL_AVG) {
         mpmg_phase_begin(ctx, PH_FLUIDITY);
         rc = mpmg_launch_fluidity(ctx);
         if (rc != MPMG_OK) return rc;

@@ -35,7 +35,7 @@ KAT_MATERIALS = ["isolin", "g_local_mu2", "dp_ri_mt", "g_local_mu2_plane_strain"
 # g_local_mu2_ext needs the team's element lists and barrier, which
 # tests/test_material.c does not set up: plugin only
 LOCAL_MATERIALS = KAT_MATERIALS + ["g_local_mu2_ext"]
-NONLOCAL_MATERIALS = ["g_nonlocal_mu2", "g_nonlocal"]
+NONLOCAL_MATERIALS = ["g_nonlocal_mu2", "g_nonlocal", "g_nonlocal_avg", "g_nonlocal_bicgstab", "g_nonlocalxs71"]
 BCS = ["box", "square_silo"]
 
 

@@ -138,6 +138,7 @@ void orc_default_params(int material, double *mp)
         mp[ORC_MP_RHO_CRITICAL] = 1485.0f;
         break;
     case ORC_G_NONLOCAL:              /* g_nonlocal.c:31-48 */
+    case ORC_G_NONLOCAL_AVG:          /* g_nonlocal_avg.c: the same constants */
         mp[ORC_MP_E] = 1e8;
         mp[ORC_MP_NU] = 0.3;
         mp[ORC_MP_MU_S] = 0.3819;
@@ -312,7 +313,7 @@ orc_sim *orc_create(const orc_config *cfg, size_t n, const double *m, const doub
     s->G = E / (2.0 * (1.0 + nu));
     s->K = E / (3.0 * (1.0 - 2 * nu));
     s->lambda = s->K - 2.0 * s->G / 3.0;
-    if (s->c.material == ORC_G_NONLOCAL) {
+    if (s->c.material == ORC_G_NONLOCAL || s->c.material == ORC_G_NONLOCAL_AVG) {
         /* g_nonlocal.c:34-35: G and K from the compile-time EMOD and NUMOD. */
         s->G = (E / (2.0f * (1.0f + nu)));
         s->K = (E / (3.0f * (1.0f - 2 * nu)));
@@ -1216,7 +1217,11 @@ static int nonlocal_solve(orc_sim *s, int mu2)
         const int *nn = s->enodes + 4 * p;
         double gf = 0;
         for (int ei = 0; ei < 4; ei++) {
-            gf += s->gf_nodes[nn[ei]] * sv[ei];
+            if (s->c.material == ORC_G_NONLOCAL_AVG) {
+                gf += 0.25 * s->gf_nodes[nn[ei]];    /* g_nonlocal_avg.c:575-578 */
+            } else {
+                gf += s->gf_nodes[nn[ei]] * sv[ei];
+            }
         }
         s->state[DEPVAR * i + 3] = gf;
     }
@@ -1647,6 +1652,7 @@ static void step_thread(orc_task *task)
         }
         break;
     case ORC_G_NONLOCAL:
+    case ORC_G_NONLOCAL_AVG:
         pthread_barrier_wait(&s->bar);
         if (task->id == 0) {
             task->status = g_nonlocal_stress(s);

@@ -135,6 +135,18 @@ def plane_cases():
         print(record_steps("%s_silo" % tag, sc, [1, 50, 400], nthreads=4)[1])
 
 
+def nonlocal_avg_cases():
+    # g_nonlocal_avg (the element average of the nodal fluidity at the
+    # particles), the sheared silo of nonlocal_silo
+    sc = scenes.silo(cells=16, material="g_nonlocal_avg", props=(1e8, 0.3), dt=1e-6, hole_radius=0.1,
+                     open_time=0.0, wall_frac=0.5, fill_height=0.6)
+    n = len(sc["particles"]["x"])
+    sc["particles"]["sxx"] = np.full(n, -1000.0)
+    sc["particles"]["syy"] = np.full(n, -2000.0)
+    sc["particles"]["sxy"] = np.full(n, 600.0)
+    print(record_steps("nonlocal_avg_silo", sc, [1, 10, 60], nthreads=1)[1])
+
+
 def ext_cases():
     # g_local_mu2_ext: the nodal Laplacian of the local fluidity (threaded,
     # with the team's element lists and barriers)
@@ -171,6 +183,9 @@ def main():
         return
     if sys.argv[1:] == ["ext"]:
         ext_cases()
+        return
+    if sys.argv[1:] == ["nlavg"]:
+        nonlocal_avg_cases()
         return
     print(kat("isolin"))
     print(kat("g_local_mu2"))
@@ -230,6 +245,7 @@ def main():
     dp_cases()
     plane_cases()
     ext_cases()
+    nonlocal_avg_cases()
 
 
 if __name__ == "__main__":

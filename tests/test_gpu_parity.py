@@ -294,8 +294,11 @@ def test_gpu_nonlocal_mu2_vs_golden():
         assert rel_err(sim.get("state3"), d["s%d_state3" % c]) <= 1e-7, c
 
 
-def test_gpu_nonlocal_variant_vs_golden():
-    scene, d = load_golden("nonlocal_silo")
+@pytest.mark.parametrize("case", ["nonlocal_silo", "nonlocal_avg_silo"])
+def test_gpu_nonlocal_variant_vs_golden(case):
+    """g_nonlocal and g_nonlocal_avg (element-averaged fluidity at the
+    particles) against the reference's runs."""
+    scene, d = load_golden(case)
     sim = mpm2d.Simulation(scene, solver_tol=1e-12, solver_maxit=50000)
     done = 0
     for c in (int(c) for c in d["checkpoints"]):
@@ -303,7 +306,8 @@ def test_gpu_nonlocal_variant_vs_golden():
         done = c
         want = lambda f, c=c: d["s%d_%s" % (c, f)]
         for f in ("sxx", "sxy", "syy", "x", "y"):
-            assert field_err(sim.get(f), want, f) <= 1e-8, (c, f, field_err(sim.get(f), want, f))
+            assert field_err(sim.get(f), want, f) <= 1e-8, (case, c, f, field_err(sim.get(f), want, f))
+        assert rel_err(sim.get("state3"), want("state3")) <= 1e-7, (case, c)
 
 
 def test_gpu_deterministic():

@@ -14,7 +14,7 @@ import scenes
 CASES = ["config1", "mu2_column", "mu2_silo", "nonlocal_mu2_silo", "nonlocal_mu2_prestressed",
          "nonlocal_silo", "musl_config1", "musl_mu2_column", "dp_column", "dp_silo",
          "musl_dp_column", "ps_column", "ps_silo", "t2d_column", "t2d_silo",
-         "ext_column", "ext_silo"]
+         "ext_column", "ext_silo", "nonlocal_avg_silo"]
 COMPARE = ["x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy", "exx", "exy", "eyy", "wxy",
            "ax", "ay"]
 
@@ -221,3 +221,22 @@ def test_nonlocal_round_off_sensitivity():
     e_pre, flips_pre = spread(pre)
     assert e_free > 1e-6 and flips > 0
     assert e_pre < 1e-12 and flips_pre == 0
+
+
+@needs_ref
+def test_nonlocal_plugins_that_share_code():
+    """g_nonlocal_bicgstab.c is g_nonlocal_avg.c and g_nonlocalxs71.c is
+    g_nonlocal.c (the live reference plugins give bit-identical runs), which
+    is why the libmpm layer maps them onto MPMG_G_NONLOCAL_AVG and
+    MPMG_G_NONLOCAL; the averaged variant does differ from g_nonlocal."""
+    scene, _ = load_golden("nonlocal_silo")
+    runs = {}
+    for mat in ("g_nonlocal", "g_nonlocalxs71", "g_nonlocal_avg", "g_nonlocal_bicgstab"):
+        ref = O.RefHarness(dict(scene, material=mat), nthreads=1)
+        ref.step(10)
+        runs[mat] = ref.particles()
+    for a, b in (("g_nonlocal", "g_nonlocalxs71"), ("g_nonlocal_avg", "g_nonlocal_bicgstab")):
+        for f in ("x", "y", "sxx", "state3"):
+            np.testing.assert_array_equal(runs[a][f], runs[b][f])
+    assert not np.array_equal(runs["g_nonlocal"]["state3"], runs["g_nonlocal_avg"]["state3"])
+
