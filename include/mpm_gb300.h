@@ -59,9 +59,10 @@ enum mpmg_material {
     MPMG_G_LOCAL_MU2_PLANE_STRAIN = 5,  /* materialsrc/g_local_mu2_plane_strain.c */
     MPMG_G_LOCAL_MU2_TRUE_2D = 6,       /* materialsrc/g_local_mu2_true_2d.c */
     MPMG_G_LOCAL_MU2_EXT = 7,           /* materialsrc/g_local_mu2_ext.c */
-    MPMG_G_NONLOCAL_AVG = 8             /* materialsrc/g_nonlocal_avg.c (and g_nonlocal_bicgstab.c, the same
+    MPMG_G_NONLOCAL_AVG = 8,            /* materialsrc/g_nonlocal_avg.c (and g_nonlocal_bicgstab.c, the same
                                            code): g_nonlocal with the element average of the nodal
                                            fluidity at the particles */
+    MPMG_G_LOCAL_MU2_REVERSE = 9        /* materialsrc/g_local_mu2_reverse.c */
 };
 
 /* Boundary-condition kinds: the reference plugins with a device implementation. */

@@ -61,6 +61,8 @@ bool material_uses_state(int material, int k)
         return k == 1 || k == 5 || k == 9 || k == 10;
     case MPMG_G_LOCAL_MU2_TRUE_2D:        // g_local_mu2_true_2d.c:43-51 (beta, gammap, gammadotp)
         return k == 5 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_REVERSE:        // g_local_mu2_reverse.c:57-64 (beta, gammap, gammadotp)
+        return k == 5 || k == 9 || k == 10;
     case MPMG_G_LOCAL_MU2_EXT:            // g_local_mu2_ext.c:47-57 (mu_t, gf, gflocal, beta, gammap, gammadotp)
         return k == 0 || k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
     default:
@@ -303,6 +305,14 @@ int mpmg_default_params(int material, double *mp)
         mp[MPMG_MP_GRAINS_D] = material == MPMG_G_LOCAL_MU2_TRUE_2D ? 0.01 * 5 : 0.001 * 5;
         mp[MPMG_MP_RHO_CRITICAL] = 1485.0f;
         return MPMG_OK;
+    case MPMG_G_LOCAL_MU2_REVERSE:        // g_local_mu2_reverse.c:33-53 (compile-time there)
+        mp[MPMG_MP_MU_S] = 0.3819;
+        mp[MPMG_MP_GRAINS_RHO] = 2450;
+        mp[MPMG_MP_MU_2] = 0.6435;
+        mp[MPMG_MP_I0] = 0.278 / 1.0;
+        mp[MPMG_MP_GRAINS_D] = 0.01 * 5;
+        mp[MPMG_MP_RHO_CRITICAL] = 1485.0f;
+        return MPMG_OK;
     case MPMG_G_LOCAL_MU2_EXT:            // g_local_mu2_ext.c:26-45 (compile-time there)
         mp[MPMG_MP_MU_S] = 0.3819;
         mp[MPMG_MP_GRAINS_RHO] = 2450;
@@ -398,7 +408,7 @@ int validate_config(const mpmg_config *cfg, size_t n)
         mpmg_set_error("grid or particle count exceeds 32-bit indexing");
         return MPMG_ERR_INVALID;
     }
-    if (cfg->material < MPMG_ISOLIN || cfg->material > MPMG_G_NONLOCAL_AVG) {
+    if (cfg->material < MPMG_ISOLIN || cfg->material > MPMG_G_LOCAL_MU2_REVERSE) {
         mpmg_set_error("unknown material kind %d", cfg->material);
         return MPMG_ERR_UNSUPPORTED;
     }

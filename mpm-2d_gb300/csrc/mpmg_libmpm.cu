@@ -76,6 +76,7 @@ int material_kind(const char *file)
     if (b == "g_local_mu2_plane_strain") return MPMG_G_LOCAL_MU2_PLANE_STRAIN;
     if (b == "g_local_mu2_true_2d") return MPMG_G_LOCAL_MU2_TRUE_2D;
     if (b == "g_local_mu2_ext") return MPMG_G_LOCAL_MU2_EXT;
+    if (b == "g_local_mu2_reverse") return MPMG_G_LOCAL_MU2_REVERSE;
     return -1;
 }
 
@@ -97,7 +98,8 @@ bool uses_state(int material, int k)
     case MPMG_G_NONLOCAL_AVG: return k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
     case MPMG_DP_RI_MT: return k == 1 || k == 9 || k == 10;
     case MPMG_G_LOCAL_MU2_PLANE_STRAIN: return k == 1 || k == 5 || k == 9 || k == 10;
-    case MPMG_G_LOCAL_MU2_TRUE_2D: return k == 5 || k == 9 || k == 10;
+    case MPMG_G_LOCAL_MU2_TRUE_2D:
+    case MPMG_G_LOCAL_MU2_REVERSE: return k == 5 || k == 9 || k == 10;
     case MPMG_G_LOCAL_MU2_EXT: return k == 0 || k == 3 || k == 4 || k == 5 || k == 9 || k == 10;
     default: return false;
     }

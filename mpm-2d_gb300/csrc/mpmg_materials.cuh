@@ -204,6 +204,75 @@ __device__ __forceinline__ void plane_return(const Elastic &el, const ReturnPara
     gammadotp = nup_tau;
 }
 
+// g_local_mu2_reverse calculate_stress_threaded, g_local_mu2_reverse.c:166-302:
+// a rate-dependent return to mu(I) (p + c), c = 0, with mu from the previous
+// step's gammadotp and the start-of-step pressure, and Jaumann terms of the
+// opposite sign to isolin's.  beta in state[5].
+__device__ __forceinline__ void g_local_mu2_reverse(const Elastic &el, const Mu2Params &mp, double m, double v,
+                                                    double exx, double exy, double eyy, double wxy, double &sxx,
+                                                    double &sxy, double &syy, double &beta, double &gammap,
+                                                    double &gammadotp)
+{
+    const double G = el.G, K = el.K, dt = el.dt, c = 0;
+    const double lambda = sub(K, dvd(mul(2.0, G), 3.0));
+    const double twoG = mul(2.0, G);
+    double p_t = mul(-0.5, add(sxx, syy));
+    double trD = add(exx, eyy);
+    double dsjxx = add(mul(lambda, trD), mul(twoG, exx));
+    double dsjxy = mul(twoG, exy);
+    double dsjyy = add(mul(lambda, trD), mul(twoG, eyy));
+    double w2s = mul(mul(2.0, wxy), sxy);
+    dsjxx = sub(dsjxx, w2s);
+    dsjxy = add(dsjxy, mul(wxy, sub(sxx, syy)));
+    dsjyy = add(dsjyy, w2s);
+    double sxx_tr = add(sxx, mul(dt, dsjxx));
+    double sxy_tr = add(sxy, mul(dt, dsjxy));
+    double syy_tr = add(syy, mul(dt, dsjyy));
+    double p_tr = mul(-0.5, add(sxx_tr, syy_tr));
+    double t0xx = add(sxx_tr, p_tr), t0xy = sxy_tr, t0yy = add(syy_tr, p_tr);
+    double tau_tr = __dsqrt_rn(mul(0.5, add(add(mul(t0xx, t0xx), mul(mul(2.0, t0xy), t0xy)), mul(t0yy, t0yy))));
+    double inum = mul(mul(gammadotp, mp.grains_d), __dsqrt_rn(mp.grains_rho));
+    double mu_t;
+    if (p_t <= 0) {
+        mu_t = mp.mu_2;
+    } else {
+        inum = dvd(inum, __dsqrt_rn(p_t));
+        if (inum <= 0) mu_t = mp.mu_s;
+        else mu_t = add(mp.mu_s, dvd(sub(mp.mu_2, mp.mu_s), add(dvd(mp.I0, inum), 1.0)));
+    }
+    double tau_tau = mul(mu_t, add(p_tr, c));
+    double f = sub(tau_tr, tau_tau);
+    const bool density_flag = dvd(m, v) < mp.rho_critical;
+    const double pmin = dvd(-c, mu_t);
+    double nup_tau;
+    if (density_flag) {
+        nup_tau = dvd(tau_tr, mul(G, dt));
+        beta = dvd(-p_tr, mul(K, dt));
+        sxx = 0; sxy = 0; syy = 0;
+    } else if (f < 0) {
+        nup_tau = 0;
+        beta = 0;
+        sxx = sub(t0xx, p_tr);
+        sxy = t0xy;
+        syy = sub(t0yy, p_tr);
+    } else if (f >= 0 && p_tr > pmin) {
+        nup_tau = dvd(dvd(f, G), dt);
+        beta = 0;
+        double scale_factor = dvd(tau_tau, tau_tr);
+        sxx = sub(mul(scale_factor, t0xx), p_tr);
+        sxy = mul(scale_factor, t0xy);
+        syy = sub(mul(scale_factor, t0yy), p_tr);
+    } else if (p_tr <= pmin) {
+        nup_tau = dvd(tau_tr, mul(G, dt));
+        beta = dvd(sub(dvd(c, mu_t), p_tr), mul(K, dt));
+        sxx = 0; sxy = 0; syy = 0;
+    } else {
+        nup_tau = 0;   // NaN: the reference prints the particle and keeps s
+    }
+    gammap = add(gammap, mul(nup_tau, dt));
+    gammadotp = nup_tau;
+}
+
 // mu_from_gammadot, g_local_mu2_ext.c:75-95.
 __device__ __forceinline__ double mu_from_gammadot(double gammadot, double p, double dsqrtrhos, double mu_s,
                                                    double mu_2, double inum_0)

@@ -238,6 +238,21 @@ __device__ __forceinline__ void plane_return_particle(const G2PArgs &A, int i, d
     A.st10[i] = gdp;
 }
 
+// g_local_mu2_reverse on particle i: beta in state[5], gammap in state[9],
+// gammadotp in state[10] (g_local_mu2_reverse.c:57-64).
+__device__ __forceinline__ void reverse_particle(const G2PArgs &A, int i, double vol, double exx, double exy,
+                                                 double eyy, double wxy)
+{
+    double sxx = A.sxx[i], sxy = A.sxy[i], syy = A.syy[i], b = A.st5[i], gp = A.st9[i], gdp = A.st10[i];
+    mat::g_local_mu2_reverse(A.el, A.mu2, A.m[i], vol, exx, exy, eyy, wxy, sxx, sxy, syy, b, gp, gdp);
+    A.sxx[i] = sxx;
+    A.sxy[i] = sxy;
+    A.syy[i] = syy;
+    A.st5[i] = b;
+    A.st9[i] = gp;
+    A.st10[i] = gdp;
+}
+
 template <int MATERIAL, int PHASE>
 __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
 {
@@ -335,6 +350,8 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
     } else if (MATERIAL == MPMG_DP_RI_MT || MATERIAL == MPMG_G_LOCAL_MU2_PLANE_STRAIN ||
                MATERIAL == MPMG_G_LOCAL_MU2_TRUE_2D) {
         plane_return_particle<MATERIAL>(A, i, vol, exx, exy, eyy, wxy);
+    } else if (MATERIAL == MPMG_G_LOCAL_MU2_REVERSE) {
+        reverse_particle(A, i, vol, exx, exy, eyy, wxy);
     } else if (MATERIAL == MPMG_G_LOCAL_MU2_EXT) {
         // first phase only; the stress waits for the nodal Laplacian
         double mu_t = A.st0[i], gfl;
@@ -523,6 +540,8 @@ __global__ void material_only_kernel(G2PArgs A, int material)
         plane_return_particle<MPMG_G_LOCAL_MU2_PLANE_STRAIN>(A, i, A.v[i], exx, exy, eyy, wxy);
     } else if (material == MPMG_G_LOCAL_MU2_TRUE_2D) {
         plane_return_particle<MPMG_G_LOCAL_MU2_TRUE_2D>(A, i, A.v[i], exx, exy, eyy, wxy);
+    } else if (material == MPMG_G_LOCAL_MU2_REVERSE) {
+        reverse_particle(A, i, A.v[i], exx, exy, eyy, wxy);
     } else {
         double Txx = A.sxx[i], Txy = A.sxy[i], Tyy = A.syy[i], Tzz = A.Tzz[i];
         double gp = A.st9[i], gdp;
@@ -644,6 +663,9 @@ int mpmg_launch_step(mpmg_ctx *ctx)
         case MPMG_G_LOCAL_MU2_TRUE_2D:
             g2p_kernel<MPMG_G_LOCAL_MU2_TRUE_2D, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
             break;
+        case MPMG_G_LOCAL_MU2_REVERSE:
+            g2p_kernel<MPMG_G_LOCAL_MU2_REVERSE, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
         default: g2p_kernel<MPMG_G_LOCAL_MU2, G2P_STRAIN><<<blocks_for(n, 256), 256, 0, s>>>(A); break;
         }
         ctx->launches += 4;
@@ -663,6 +685,9 @@ int mpmg_launch_step(mpmg_ctx *ctx)
             break;
         case MPMG_G_LOCAL_MU2_TRUE_2D:
             g2p_kernel<MPMG_G_LOCAL_MU2_TRUE_2D, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
+            break;
+        case MPMG_G_LOCAL_MU2_REVERSE:
+            g2p_kernel<MPMG_G_LOCAL_MU2_REVERSE, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);
             break;
         case MPMG_G_LOCAL_MU2_EXT:
             g2p_kernel<MPMG_G_LOCAL_MU2_EXT, G2P_FULL><<<blocks_for(n, 256), 256, 0, s>>>(A);

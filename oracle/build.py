@@ -31,7 +31,8 @@ CFLAGS = ["-O2", "-std=gnu99", "-fPIC", "-ffp-contract=off", "-w"]
 
 LIBMPM_SOURCES = ["element.c", "interpolate.c", "loading.c", "map.c", "material.c",
                   "particle.c", "process_usl.c", "rtsafe.c", "tensor.c"]
-KAT_MATERIALS = ["isolin", "g_local_mu2", "dp_ri_mt", "g_local_mu2_plane_strain", "g_local_mu2_true_2d"]
+KAT_MATERIALS = ["isolin", "g_local_mu2", "dp_ri_mt", "g_local_mu2_plane_strain", "g_local_mu2_true_2d",
+                 "g_local_mu2_reverse"]
 # g_local_mu2_ext needs the team's element lists and barrier, which
 # tests/test_material.c does not set up: plugin only
 LOCAL_MATERIALS = KAT_MATERIALS + ["g_local_mu2_ext"]

@@ -128,6 +128,14 @@ void orc_default_params(int material, double *mp)
         mp[ORC_MP_GRAINS_D] = material == ORC_G_LOCAL_MU2_TRUE_2D ? 0.01 * 5 : 0.001 * 5;
         mp[ORC_MP_RHO_CRITICAL] = 1485.0f;
         break;
+    case ORC_G_LOCAL_MU2_REVERSE:      /* g_local_mu2_reverse.c:33-53 */
+        mp[ORC_MP_MU_S] = 0.3819;
+        mp[ORC_MP_GRAINS_RHO] = 2450;
+        mp[ORC_MP_MU_2] = 0.6435;
+        mp[ORC_MP_I0] = 0.278 / 1.0;
+        mp[ORC_MP_GRAINS_D] = 0.01 * 5;
+        mp[ORC_MP_RHO_CRITICAL] = 1485.0f;
+        break;
     case ORC_G_LOCAL_MU2_EXT:          /* g_local_mu2_ext.c:26-45 */
         mp[ORC_MP_MU_S] = 0.3819;
         mp[ORC_MP_GRAINS_RHO] = 2450;
@@ -908,6 +916,86 @@ static void g_local_mu2_ext_thread(orc_task *task)
     }
 }
 
+/* g_local_mu2_reverse calculate_stress_threaded, g_local_mu2_reverse.c:166-302:
+   a rate-dependent return to mu(I) (p + c), c = 0, with mu from the previous
+   step's gammadotp and start-of-step pressure, and the Jaumann terms of the
+   opposite sign to isolin's.  beta in state[5]. */
+static void g_local_mu2_reverse_range(orc_sim *s, size_t p0, size_t p1)
+{
+    const double G = s->G, K = s->K, dt = s->c.dt;
+    const double *mp = s->c.mp;
+    const double lambda = K - 2.0 * G / 3.0;
+    const double c = 0;
+    for (size_t i = p0; i < p1; i++) {
+        if (s->active[i] == 0) {
+            continue;
+        }
+        double *st = s->state + DEPVAR * i;
+        double p_t = -0.5 * (s->sxx[i] + s->syy[i]);
+        double trD = s->exx[i] + s->eyy[i];
+        double dsjxx = lambda * trD + 2.0 * G * s->exx[i];
+        double dsjxy = 2.0 * G * s->exy[i];
+        double dsjyy = lambda * trD + 2.0 * G * s->eyy[i];
+        dsjxx -= 2 * s->wxy[i] * s->sxy[i];
+        dsjxy += s->wxy[i] * (s->sxx[i] - s->syy[i]);
+        dsjyy += 2 * s->wxy[i] * s->sxy[i];
+        double sxx_tr = s->sxx[i] + dt * dsjxx;
+        double sxy_tr = s->sxy[i] + dt * dsjxy;
+        double syy_tr = s->syy[i] + dt * dsjyy;
+        double p_tr = -0.5 * (sxx_tr + syy_tr);
+        double t0xx = sxx_tr + p_tr;
+        double t0xy = sxy_tr;
+        double t0yy = syy_tr + p_tr;
+        double tau_tr = sqrt(0.5 * (t0xx * t0xx + 2 * t0xy * t0xy + t0yy * t0yy));
+        double inertial_num = st[10] * mp[ORC_MP_GRAINS_D] * sqrt(mp[ORC_MP_GRAINS_RHO]);
+        double mu_t;
+        if (p_t <= 0) {
+            mu_t = mp[ORC_MP_MU_2];
+        } else {
+            inertial_num = inertial_num / sqrt(p_t);
+            if (inertial_num <= 0) {
+                mu_t = mp[ORC_MP_MU_S];
+            } else {
+                mu_t = mp[ORC_MP_MU_S] + (mp[ORC_MP_MU_2] - mp[ORC_MP_MU_S]) / ((mp[ORC_MP_I0] / inertial_num) + 1.0);
+            }
+        }
+        double tau_tau = mu_t * (p_tr + c);
+        double f = tau_tr - tau_tau;
+        int density_flag = (s->m[i] / s->v[i]) < mp[ORC_MP_RHO_CRITICAL];
+        double nup_tau;
+        if (density_flag) {
+            nup_tau = (tau_tr) / (G * dt);
+            st[5] = -p_tr / (K * dt);
+            s->sxx[i] = 0;
+            s->sxy[i] = 0;
+            s->syy[i] = 0;
+        } else if (f < 0) {
+            nup_tau = 0;
+            st[5] = 0;
+            s->sxx[i] = t0xx - p_tr;
+            s->sxy[i] = t0xy;
+            s->syy[i] = t0yy - p_tr;
+        } else if (f >= 0 && p_tr > -c / mu_t) {
+            nup_tau = (f / G) / dt;
+            st[5] = 0;
+            double scale_factor = (tau_tau / tau_tr);
+            s->sxx[i] = scale_factor * t0xx - p_tr;
+            s->sxy[i] = scale_factor * t0xy;
+            s->syy[i] = scale_factor * t0yy - p_tr;
+        } else if (p_tr <= -c / mu_t) {
+            nup_tau = tau_tr / (G * dt);
+            st[5] = ((c / mu_t) - p_tr) / (K * dt);
+            s->sxx[i] = 0;
+            s->sxy[i] = 0;
+            s->syy[i] = 0;
+        } else {
+            nup_tau = 0;   /* NaN: the reference prints the particle and keeps s */
+        }
+        st[9] += nup_tau * dt;
+        st[10] = nup_tau;
+    }
+}
+
 /* Trial Jaumann stress shared by g_nonlocal_mu2.c:166-186 and :271-290. */
 static void nonlocal_mu2_trial(const orc_sim *s, size_t i, double *p_tr, double *t0xx,
                                double *t0xy, double *t0yy, double *tau_tr)
@@ -1640,6 +1728,9 @@ static void step_thread(orc_task *task)
     case ORC_G_LOCAL_MU2_EXT:
         g_local_mu2_ext_thread(task);
         break;
+    case ORC_G_LOCAL_MU2_REVERSE:
+        g_local_mu2_reverse_range(s, task->p0, task->p1);
+        break;
     case ORC_G_NONLOCAL_MU2:
         /* g_nonlocal_mu2.c:113-123: thread 0 solves for everyone.  The
            reference has no barrier here, so with more than one thread its
@@ -1710,6 +1801,9 @@ int orc_material_only(orc_sim *s)
     case ORC_G_LOCAL_MU2_PLANE_STRAIN:
     case ORC_G_LOCAL_MU2_TRUE_2D:
         plane_return_material(s->c.material, 0, s->np, s);
+        return 0;
+    case ORC_G_LOCAL_MU2_REVERSE:
+        g_local_mu2_reverse_range(s, 0, s->np);
         return 0;
     default:
         return 1;

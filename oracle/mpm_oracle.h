@@ -25,7 +25,7 @@
 
 enum orc_material { ORC_ISOLIN = 0, ORC_G_LOCAL_MU2 = 1, ORC_G_NONLOCAL_MU2 = 2, ORC_G_NONLOCAL = 3,
                     ORC_DP_RI_MT = 4, ORC_G_LOCAL_MU2_PLANE_STRAIN = 5, ORC_G_LOCAL_MU2_TRUE_2D = 6,
-                    ORC_G_LOCAL_MU2_EXT = 7, ORC_G_NONLOCAL_AVG = 8 };
+                    ORC_G_LOCAL_MU2_EXT = 7, ORC_G_NONLOCAL_AVG = 8, ORC_G_LOCAL_MU2_REVERSE = 9 };
 enum orc_bc { ORC_BOX = 0, ORC_SQUARE_SILO = 1 };
 enum orc_gravity { ORC_GRAVITY_REFERENCE_RAMP = 0, ORC_GRAVITY_CONSTANT = 1 };
 enum orc_solver { ORC_SOLVER_DIRECT = 0, ORC_SOLVER_PCG = 1 };

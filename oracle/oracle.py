@@ -17,7 +17,7 @@ from . import build as _build
 
 MATERIALS = {"isolin": 0, "g_local_mu2": 1, "g_nonlocal_mu2": 2, "g_nonlocal": 3, "dp_ri_mt": 4,
              "g_local_mu2_plane_strain": 5, "g_local_mu2_true_2d": 6,
-             "g_local_mu2_ext": 7, "g_nonlocal_avg": 8,
+             "g_local_mu2_ext": 7, "g_nonlocal_avg": 8, "g_local_mu2_reverse": 9,
              # plugins whose code is one of the above: g_nonlocal_bicgstab.c is g_nonlocal_avg.c,
              # g_nonlocalxs71.c is g_nonlocal.c
              "g_nonlocal_bicgstab": 8, "g_nonlocalxs71": 3}

@@ -135,6 +135,17 @@ def plane_cases():
         print(record_steps("%s_silo" % tag, sc, [1, 50, 400], nthreads=4)[1])
 
 
+def reverse_cases():
+    # g_local_mu2_reverse: known answers, a column and a silo
+    print(kat("g_local_mu2_reverse"))
+    sc = scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2_reverse",
+                       rho=2450.0, props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+    print(record_steps("rev_column", sc, [1, 50, 300], nthreads=4)[1])
+    sc = scenes.silo(cells=32, material="g_local_mu2_reverse", props=(1e6, 0.3), dt=1e-5, hole_radius=0.1,
+                     open_time=0.001, wall_frac=0.5, fill_height=0.6)
+    print(record_steps("rev_silo", sc, [1, 50, 400], nthreads=4)[1])
+
+
 def nonlocal_avg_cases():
     # g_nonlocal_avg (the element average of the nodal fluidity at the
     # particles), the sheared silo of nonlocal_silo
@@ -186,6 +197,9 @@ def main():
         return
     if sys.argv[1:] == ["nlavg"]:
         nonlocal_avg_cases()
+        return
+    if sys.argv[1:] == ["reverse"]:
+        reverse_cases()
         return
     print(kat("isolin"))
     print(kat("g_local_mu2"))
@@ -246,6 +260,7 @@ def main():
     plane_cases()
     ext_cases()
     nonlocal_avg_cases()
+    reverse_cases()
 
 
 if __name__ == "__main__":

@@ -77,7 +77,7 @@ def test_invalid_configuration_is_rejected():
         mpm2d.Simulation(sc)
     assert e.value.status == 16
     cfg = mpm2d.make_config(scenes.config1())
-    cfg.material = 9                       # not an mpmg_material
+    cfg.material = 10                      # not an mpmg_material
     h = mpm2d.C.c_void_p()
     z = mpm2d.np.zeros(1)
     rc = mpm2d.lib().mpmg_create(mpm2d.C.byref(cfg), 1, *([mpm2d._dptr(z)] * 9), mpm2d.C.byref(h))

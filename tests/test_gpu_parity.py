@@ -33,7 +33,8 @@ EXTRA_STATE = {"g_local_mu2": ("Tzz", "state9", "state10"),
                "dp_ri_mt": ("state1", "state9", "state10"),
                "g_local_mu2_plane_strain": ("state1", "state5", "state9", "state10"),
                "g_local_mu2_true_2d": ("state5", "state9", "state10"),
-               "g_local_mu2_ext": ("state0", "state3", "state4", "state5", "state9", "state10")}
+               "g_local_mu2_ext": ("state0", "state3", "state4", "state5", "state9", "state10"),
+               "g_local_mu2_reverse": ("state5", "state9", "state10")}
 
 
 def check_mu_t(got, want, tol, mu_s=0.3819, mu_2=0.6435):
@@ -146,6 +147,37 @@ def test_gpu_trajectory_matches_golden(case):
         assert sim.t == float(d["s%d_t" % c])
 
 
+@pytest.mark.parametrize("case", ["rev_column", "rev_silo"])
+def test_gpu_reverse_law_within_reference_round_off_spread(case):
+    """g_local_mu2_reverse feeds the previous step's plastic rate back into
+    mu, which makes the reference's own trajectories sensitive at round-off
+    level: nudging x by 1e-15 (relative) moves the silo's velocities by ~1e-7,
+    its stresses by ~1e-4 and its plastic rate by ~0.2 after 400 steps.  The
+    GPU run must stay within ten times that spread of the reference's run
+    (the oracle, bit-exact with the reference, nudged), and within the usual
+    tolerances where the spread is smaller."""
+    scene, d = load_golden(case)
+    sim = mpm2d.Simulation(scene, store_transients=True)
+    sc2 = dict(scene)
+    sc2["particles"] = {k: np.array(v, copy=True) for k, v in scene["particles"].items()}
+    sc2["particles"]["x"] = sc2["particles"]["x"] * (1 + 1e-15)
+    nudged = O.Oracle(sc2, nthreads=4)
+    done = 0
+    for c in (int(c) for c in d["checkpoints"]):
+        sim.step(c - done)
+        nudged.step(c - done)
+        done = c
+        tol = ONE_STEP_TOL if c == 1 else TRAJ_TOL
+        want = lambda f, c=c: d["s%d_%s" % (c, f)]
+        for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "state5", "state9", "state10"):
+            spread = field_err(nudged.get(f), want, f)
+            got = field_err(sim.get(f), want, f)
+            floor = tol if not f.startswith("state") else max(tol, 1e-8)
+            assert got <= max(floor, 10 * spread), (case, c, f, got, spread)
+        e, a = sim.get_map()
+        assert np.mean(a == d["s%d_active" % c]) >= 0.999
+
+
 def test_gpu_rectangular_domain_vs_oracle():
     """The 2 x 0.5 m column on 512 x 128 elements (31 212 particles), the
     rectangular workload: FP64 GPU against the oracle (whose element map
@@ -247,7 +279,7 @@ def test_gpu_one_step_vs_oracle_from_checkpoint(case):
 
 
 @pytest.mark.parametrize("kind", ["isolin", "g_local_mu2", "dp_ri_mt", "g_local_mu2_plane_strain",
-                                  "g_local_mu2_true_2d"])
+                                  "g_local_mu2_true_2d", "g_local_mu2_reverse"])
 def test_gpu_material_known_answers_bit_exact(kind):
     """The device material functions reproduce tests/test_material.c's %a
     output exactly."""

@@ -14,7 +14,7 @@ import scenes
 CASES = ["config1", "mu2_column", "mu2_silo", "nonlocal_mu2_silo", "nonlocal_mu2_prestressed",
          "nonlocal_silo", "musl_config1", "musl_mu2_column", "dp_column", "dp_silo",
          "musl_dp_column", "ps_column", "ps_silo", "t2d_column", "t2d_silo",
-         "ext_column", "ext_silo", "nonlocal_avg_silo"]
+         "ext_column", "ext_silo", "nonlocal_avg_silo", "rev_column", "rev_silo"]
 COMPARE = ["x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy", "exx", "exy", "eyy", "wxy",
            "ax", "ay"]
 
@@ -127,7 +127,7 @@ def _velocity_gradient(t):
 
 
 @pytest.mark.parametrize("kind", ["isolin", "g_local_mu2", "dp_ri_mt", "g_local_mu2_plane_strain",
-                                  "g_local_mu2_true_2d"])
+                                  "g_local_mu2_true_2d", "g_local_mu2_reverse"])
 def test_oracle_material_known_answers(kind):
     d = np.load(os.path.join(GOLDEN, "kat_%s.npz" % kind))
     rows = d["rows"]
