@@ -462,20 +462,27 @@ def run_gpu(args):
 
     # --- end to end through the C ABI with host buffers (mixed) ---------------
     # The user's run: create the simulation from host arrays (H2D of the
-    # particle state), step, read each step's result back (mpmg_get_time:
-    # stream sync + D2H of the step record), and write the output frame at
-    # the end (mpmg_get_fields of the driver's write_frame fields into pinned
-    # host buffers).
+    # particle state), step, read each step's result back (the step record:
+    # time, step count, device status, one D2H copy per step, pipelined with
+    # mpmg_record_async / mpmg_record_wait so that step k + 1 is issued before
+    # step k's record is waited for), and write the output frame at the end
+    # (mpmg_get_fields of the driver's write_frame fields into pinned host
+    # buffers).
     e2e_steps = args.e2e_steps
     host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
     barrier()
     t0 = time.perf_counter()
     sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
     t1 = time.perf_counter()
-    for _ in range(e2e_steps):
+    last = None
+    for k in range(e2e_steps):
         sim2.step(1)
-        sim2.t
+        sim2.record_async(k % 2)
+        if k > 0:
+            last = sim2.record_wait((k - 1) % 2)
+    last = sim2.record_wait((e2e_steps - 1) % 2)
     t2 = time.perf_counter()
+    assert last[1] == e2e_steps
     sim2.get_frame(FRAME_FIELDS, out=host)
     t3 = time.perf_counter()
     barrier()
@@ -518,7 +525,8 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
                 "d2h_bytes_per_step": step_record + d2h_frame / e2e_steps, "steps": e2e_steps,
                 "create_s": t1 - t0, "steps_s": t2 - t1, "frame_s": t3 - t2,
-                "path": "mpmg_create from host arrays, per step mpmg_step + mpmg_get_time, "
+                "path": "mpmg_create from host arrays, per step mpmg_step + the step record read back "
+                        "(mpmg_record_async / mpmg_record_wait, one step behind), "
                         "one output frame (mpmg_get_fields of %d fields)" % len(FRAME_FIELDS)},
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -225,6 +225,14 @@ typedef struct mpmg_tuning {
 MPMG_API int mpmg_autotune(mpmg_ctx *ctx, int steps_per_trial, mpmg_tuning *best);
 
 MPMG_API int mpmg_get_time(mpmg_ctx *ctx, double *t, int *step_number);
+/* Asynchronous read-back of the step record (time, step count, device
+   status) for pipelined drivers: mpmg_record_async enqueues the copy of the
+   record as it stands after the work issued so far into ring slot
+   0..3; mpmg_record_wait waits for that copy and returns what it holds
+   (errors as mpmg_get_time).  A driver can issue step k + 1 before waiting
+   for step k's record, so the GPU never idles on the host. */
+MPMG_API int mpmg_record_async(mpmg_ctx *ctx, int slot);
+MPMG_API int mpmg_record_wait(mpmg_ctx *ctx, int slot, double *t, int *step_number);
 MPMG_API int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number);
 MPMG_API int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *num_elements);
 

@@ -98,14 +98,13 @@ int alloc_step_record(mpmg_ctx *ctx, int count)
     return MPMG_OK;
 }
 
-int sync_status(mpmg_ctx *ctx)
+// The step parameters and the status word of a read-back step record: the
+// parameters go to ctx->h_params, device-side errors to their status codes.
+int take_record(mpmg_ctx *ctx, const unsigned char *rec)
 {
-    MPMG_CHECK(cudaMemcpyAsync(ctx->h_record, ctx->d_params, step_record_bytes(ctx), cudaMemcpyDeviceToHost,
-                               ctx->stream));
-    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
     int st = 0;
-    memcpy(&ctx->h_params, ctx->h_record, sizeof(StepParams));
-    memcpy(&st, ctx->h_record + ctx->status_offset, sizeof(int));
+    memcpy(&ctx->h_params, rec, sizeof(StepParams));
+    memcpy(&st, rec + ctx->status_offset, sizeof(int));
     if (st != 0) {
         // Report each device-side error once; the caller decides whether to go on.
         MPMG_CHECK(cudaMemset(ctx->d_status, 0, sizeof(int)));
@@ -125,6 +124,14 @@ int sync_status(mpmg_ctx *ctx)
         return MPMG_ERR_SOLVER;
     }
     return MPMG_OK;
+}
+
+int sync_status(mpmg_ctx *ctx)
+{
+    MPMG_CHECK(cudaMemcpyAsync(ctx->h_record, ctx->d_params, step_record_bytes(ctx), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    return take_record(ctx, ctx->h_record);
 }
 
 struct FieldRef {
@@ -374,6 +381,10 @@ int mpmg_destroy(mpmg_ctx *ctx)
     cudaFree(ctx->cell_start);
     cudaFree(ctx->d_params);      // the step record block (d_status lies inside it)
     if (ctx->h_record) cudaFreeHost(ctx->h_record);
+    for (int k = 0; k < MPMG_RECORD_SLOTS; k++) {
+        if (ctx->h_ring[k]) cudaFreeHost(ctx->h_ring[k]);
+        if (ctx->ring_ev[k]) cudaEventDestroy(ctx->ring_ev[k]);
+    }
     mpmg_bin_free(ctx);
     mpmg_nonlocal_free(ctx);
     mpmg_mixed_free(ctx);
@@ -1158,6 +1169,33 @@ int mpmg_get_time(mpmg_ctx *ctx, double *t, int *step_number)
     if (t) *t = ctx->h_params.t;
     if (step_number) *step_number = (int)ctx->h_params.step_count;
     return MPMG_OK;
+}
+
+int mpmg_record_async(mpmg_ctx *ctx, int slot)
+{
+    if (ctx == nullptr || slot < 0 || slot >= MPMG_RECORD_SLOTS) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    if (ctx->h_ring[slot] == nullptr) {
+        MPMG_CHECK(cudaHostAlloc((void **)&ctx->h_ring[slot], step_record_bytes(ctx), cudaHostAllocDefault));
+        MPMG_CHECK(cudaEventCreateWithFlags(&ctx->ring_ev[slot], cudaEventDisableTiming));
+    }
+    MPMG_CHECK(cudaMemcpyAsync(ctx->h_ring[slot], ctx->d_params, step_record_bytes(ctx), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+    MPMG_CHECK(cudaEventRecord(ctx->ring_ev[slot], ctx->stream));
+    return MPMG_OK;
+}
+
+int mpmg_record_wait(mpmg_ctx *ctx, int slot, double *t, int *step_number)
+{
+    if (ctx == nullptr || slot < 0 || slot >= MPMG_RECORD_SLOTS || ctx->h_ring[slot] == nullptr)
+        return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    MPMG_CHECK(cudaEventSynchronize(ctx->ring_ev[slot]));
+    int rc = take_record(ctx, ctx->h_ring[slot]);
+    if (rc != MPMG_OK && rc != MPMG_ERR_SOLVER) return rc;
+    if (t) *t = ctx->h_params.t;
+    if (step_number) *step_number = (int)ctx->h_params.step_count;
+    return rc;
 }
 
 int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number)

@@ -16,6 +16,7 @@
 #define MPMG_NCOLORS 4
 #define MPMG_DEPVAR 11          // particle.h:13
 #define MPMG_GRAPH_CHUNK 8      // steps per replayed CUDA graph
+#define MPMG_RECORD_SLOTS 4     // asynchronous step-record read-backs in flight
 
 // Device status word bits (ctx->d_status); any nonzero value fails the step.
 #define MPMG_DEV_ERR_SOLVER 0x1
@@ -148,6 +149,10 @@ struct mpmg_ctx {
     StepParams h_params;   // host mirror of the first, refreshed on read-back
     int *d_status;
     unsigned char *h_record;   // pinned host mirror of the step records and status
+    // asynchronous read-backs of the step records (mpmg_record_async): pinned
+    // ring slots, each completed by its event
+    unsigned char *h_ring[MPMG_RECORD_SLOTS];
+    cudaEvent_t ring_ev[MPMG_RECORD_SLOTS];
     size_t status_offset;      // byte offset of the status word in the record block
 
     // Batched ensemble (mpmg_batch_create): several independent simulations

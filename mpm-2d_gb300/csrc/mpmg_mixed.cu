@@ -1032,28 +1032,47 @@ int dalloc(T **p, size_t count)
     return MPMG_OK;
 }
 
-// Element (local to the simulation) and local coordinates of a host
-// position (FP64, as WHICH_ELEMENT4); -1 outside the grid, where xl, yl
-// keep the position.
-void locate(const mpmg_config &c, double x, double y, int *cell, float *xl, float *yl)
+// Geometry of one simulation for placing its particles.
+struct PlaceGeom {
+    double h, xmax, ymax;
+    int Ex, Ey, e0;
+};
+
+// The initial records of particle i from the caller's FP64 arrays (staged on
+// the device, array k at in[k]): the element and local coordinates of
+// WHICH_ELEMENT4 (process_usl.c:43-44; the particle.c:14-30 coordinates,
+// held below 1 in FP32), -1 outside the grid, where xl, yl keep the
+// position.  The FP64 operations are the _rn intrinsics, so the keys are
+// the same whatever the host compiler would have fused.
+__global__ void __launch_bounds__(256) mx_place_kernel(int n, const double *const *in, PlaceGeom single,
+                                                       const PlaceGeom *__restrict__ members,
+                                                       const int *__restrict__ poff, int count, int ne_total,
+                                                       Buf P, int *__restrict__ cell)
 {
-    const int Ex = c.Nx - 1, Ey = c.Ny - 1;
-    if (x < c.xmax && x >= 0.0 && y < c.ymax && y >= 0.0) {
-        double fx = floor(x / c.h), fy = floor(y / c.h);
-        if (fx < (double)Ex && fy < (double)Ey) {
-            *cell = (int)(fx + fy * (double)Ex);
-            double lx = (x - fx * c.h) / c.h, ly = (y - fy * c.h) / c.h;
-            float fxl = (float)lx, fyl = (float)ly;
-            if (fxl >= 1.0f) fxl = nextafterf(1.0f, 0.0f);
-            if (fyl >= 1.0f) fyl = nextafterf(1.0f, 0.0f);
-            *xl = fxl;
-            *yl = fyl;
-            return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const PlaceGeom g = members ? members[find_member(poff, count, i)] : single;
+    const double m = in[0][i], v = in[1][i], x = in[2][i], y = in[3][i], vx = in[4][i], vy = in[5][i];
+    const double sxx = in[6][i], sxy = in[7][i], syy = in[8][i];
+    int local = -1;
+    float xl = (float)x, yl = (float)y;
+    if (x < g.xmax && x >= 0.0 && y < g.ymax && y >= 0.0) {
+        const double fx = floor(__ddiv_rn(x, g.h)), fy = floor(__ddiv_rn(y, g.h));
+        if (fx < (double)g.Ex && fy < (double)g.Ey) {
+            local = (int)__dadd_rn(fx, __dmul_rn(fy, (double)g.Ex));
+            const double lx = __ddiv_rn(__dsub_rn(x, __dmul_rn(fx, g.h)), g.h);
+            const double ly = __ddiv_rn(__dsub_rn(y, __dmul_rn(fy, g.h)), g.h);
+            xl = __double2float_rn(lx);
+            yl = __double2float_rn(ly);
+            if (xl >= 1.0f) xl = __int_as_float(0x3f7fffff);   // the float just below 1
+            if (yl >= 1.0f) yl = __int_as_float(0x3f7fffff);
         }
     }
-    *cell = -1;
-    *xl = (float)x;
-    *yl = (float)y;
+    cell[i] = local < 0 ? ne_total : g.e0 + local;
+    P.A[i] = make_float4(xl, yl, (float)vx, (float)vy);
+    P.B[i] = make_float4((float)m, (float)v, (float)sxx, (float)sxy);
+    P.C[i] = make_float4((float)syy, 0.0f, 0.0f, 0.0f);
+    P.D[i] = make_float4(0.0f, 0.0f, __int_as_float(i), 0.0f);
 }
 
 using G2PKernel = void (*)(MemberM, BatchView, int, int, const uint32_t *, Buf, Buf, const int *, int *,
@@ -1125,32 +1144,53 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
         MPMG_CHECK(cudaMemcpy(bt->d_node_off, no.data(), (count + 1) * sizeof(int), cudaMemcpyHostToDevice));
     }
 
-    // host staging: element, local coordinates, records
-    std::vector<float4> ha(n ? n : 1), hb(n ? n : 1), hc(n ? n : 1), hd(n ? n : 1);
-    std::vector<int> cell(n ? n : 1);
-    int member = 0;
-    for (size_t i = 0; i < n; i++) {
-        while (bt && i >= bt->poff[member + 1]) member++;
-        const mpmg_config &c = bt ? bt->cfg[member] : ctx->cfg;
-        float xl, yl;
-        int local;
-        locate(c, x[i], y[i], &local, &xl, &yl);
-        cell[i] = local < 0 ? (int)ctx->ne : (int)((bt ? bt->eoff[member] : 0) + (size_t)local);
-        ha[i] = make_float4(xl, yl, (float)vx[i], (float)vy[i]);
-        hb[i] = make_float4((float)m[i], (float)v[i], (float)sxx[i], (float)sxy[i]);
-        hc[i] = make_float4((float)syy[i], 0.0f, 0.0f, 0.0f);
-        hd[i] = make_float4(0.0f, 0.0f, mpmg_bits_float((int)i), 0.0f);
-    }
-    cudaError_t e = cudaSuccess;
+    // The caller's FP64 arrays go to the device as they are, into buffer 1's
+    // records and the export buffer (64 + 8 bytes a particle: the nine
+    // arrays), and a kernel places the particles and builds buffer 0's
+    // records and elements.
     if (n > 0) {
-        e = cudaMemcpy(s->A[0], ha.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(s->B[0], hb.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(s->C[0], hc.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(s->D[0], hd.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
-        // element index of the stored particles of buffer 0 (see cell_array)
-        if (e == cudaSuccess) e = cudaMemcpy(ctx->in_element, cell.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+        double *stage[9];
+        float4 *const spare[4] = {s->A[1], s->B[1], s->C[1], s->D[1]};
+        for (int k = 0; k < 8; k++) stage[k] = reinterpret_cast<double *>(spare[k / 2]) + (k % 2) * n;
+        stage[8] = s->export_buf;
+        const double *src[9] = {m, v, x, y, vx, vy, sxx, sxy, syy};
+        for (int k = 0; k < 9; k++)
+            MPMG_CHECK(cudaMemcpyAsync(stage[k], src[k], n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        double **d_stage = nullptr;
+        if ((rc = dalloc(&d_stage, 9)) != MPMG_OK) return rc;
+        MPMG_CHECK(cudaMemcpyAsync(d_stage, stage, sizeof(stage), cudaMemcpyHostToDevice, ctx->stream));
+        PlaceGeom single{};
+        PlaceGeom *d_geo = nullptr;
+        int *d_poff = nullptr;
+        const mpmg_config &c0 = bt ? bt->cfg[0] : ctx->cfg;
+        single = PlaceGeom{c0.h, c0.xmax, c0.ymax, c0.Nx - 1, c0.Ny - 1, 0};
+        std::vector<PlaceGeom> hg;
+        std::vector<int> hp;
+        if (bt) {
+            hg.resize(count);
+            hp.resize(count + 1);
+            for (int k = 0; k < count; k++) {
+                const mpmg_config &ck = bt->cfg[k];
+                hg[k] = PlaceGeom{ck.h, ck.xmax, ck.ymax, ck.Nx - 1, ck.Ny - 1, (int)bt->eoff[k]};
+            }
+            for (int k = 0; k <= count; k++) hp[k] = (int)bt->poff[k];
+            if ((rc = dalloc(&d_geo, count)) != MPMG_OK) return rc;
+            if ((rc = dalloc(&d_poff, count + 1)) != MPMG_OK) return rc;
+            MPMG_CHECK(cudaMemcpyAsync(d_geo, hg.data(), count * sizeof(PlaceGeom), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+            MPMG_CHECK(cudaMemcpyAsync(d_poff, hp.data(), (count + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                                       ctx->stream));
+        }
+        mx_place_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>((int)n, d_stage, single, d_geo, d_poff, count,
+                                                                    (int)ctx->ne, buf(s, 0), ctx->in_element);
+        ctx->launches += 1;
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(d_stage);
+        cudaFree(d_geo);
+        cudaFree(d_poff);
+        if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed state upload");
     }
-    if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed state upload");
     s->cur = 0;
     // persistent G2P grid: as many blocks as fit on the device at once, at
     // most one per tile

@@ -97,6 +97,8 @@ def lib(build_if_missing=True):
         L.mpmg_adj_forward_tape.argtypes = [vp, C.c_int, C.c_int]
         L.mpmg_adj_backward.argtypes = [vp, dp, dp, dp]
         L.mpmg_autotune.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
+        L.mpmg_record_async.argtypes = [vp, C.c_int]
+        L.mpmg_record_wait.argtypes = [vp, C.c_int, dp, ip]
         L.mpmg_adj_state.argtypes = [vp, C.c_char_p, dp]
         L.mpmg_get_map.argtypes = [vp, ip, ip]
         L.mpmg_set_map.argtypes = [vp, ip, ip]
@@ -234,6 +236,17 @@ class Simulation:
 
     def step(self, n=1):
         _check(lib().mpmg_step(self._h, n))
+
+    def record_async(self, slot):
+        """Enqueue the read-back of the step record into ring slot 0-3 (mpmg_record_async)."""
+        _check(lib().mpmg_record_async(self._h, slot))
+
+    def record_wait(self, slot):
+        """(t, step count) of the record enqueued in slot (mpmg_record_wait)."""
+        t = C.c_double()
+        k = C.c_int()
+        _check(lib().mpmg_record_wait(self._h, slot, C.byref(t), C.byref(k)))
+        return t.value, k.value
 
     def autotune(self, steps_per_trial=16):
         """Online tuning of the mixed step's launch shape (mpmg_autotune):

@@ -250,3 +250,24 @@ def test_mixed_full_size_invariants():
     assert abs(m_nodes - m_parts) <= 1e-6 * m_parts
     x = sim.get("x")
     assert np.all((x >= 0) & (x < 1))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_pipelined_record_reads_match_synchronous_ones(precision):
+    """mpmg_record_async / mpmg_record_wait one step behind give every
+    step's time and count as mpmg_get_time after each step does."""
+    sc = scenes.config1(seed=5)
+    a = mpm2d.Simulation(sc, precision=precision)
+    b = mpm2d.Simulation(sc, precision=precision)
+    got, want = [], []
+    for k in range(12):
+        a.step(1)
+        a.record_async(k % 2)
+        if k > 0:
+            got.append(a.record_wait((k - 1) % 2))
+        b.step(1)
+        want.append((b.t, b.step_count))
+    got.append(a.record_wait(11 % 2))
+    assert got == want
+    np.testing.assert_array_equal(a.get("x"), b.get("x"))
+
