@@ -8,7 +8,7 @@
  * serial tail (frame check, time_varying_loads).  No plugin is loaded: the
  * GPU library runs the material and boundary conditions named by the files.
  *
- * usage: driver_test IN OUT
+ * usage: driver_test IN OUT [musl]   (musl: explicit_mpm_step_musl_threaded)
  * IN  (native binary): int32 N, nthreads, nsteps, nmprops, nbprops, nbiprops;
  *     float64 h, dt, sample_rate; char material[64], bc[64];
  *     float64 mprops[nmprops], bprops[nbprops]; int32 biprops[nbiprops];
@@ -26,13 +26,18 @@
 
 static int g_nsteps;
 static long g_frames;
+static int g_musl;
 
 static void *run(void *arg)
 {
     threadtask_t *task = (threadtask_t *)arg;
     job_t *job = task->job;
     for (int k = 0; k < g_nsteps; k++) {
-        explicit_mpm_step_usl_threaded(task);
+        if (g_musl) {
+            explicit_mpm_step_musl_threaded(task);
+        } else {
+            explicit_mpm_step_usl_threaded(task);
+        }
         if (pthread_barrier_wait(job->serialize_barrier) == PTHREAD_BARRIER_SERIAL_THREAD) {
             job->stepcount++;
             if (job->t >= (job->frame / job->output.sample_rate_hz)) {
@@ -53,6 +58,7 @@ int main(int argc, char **argv)
         fprintf(stderr, "usage: %s IN OUT\n", argv[0]);
         return 2;
     }
+    g_musl = argc > 3 && strcmp(argv[3], "musl") == 0;
     FILE *f = fopen(argv[1], "rb");
     if (!f) return 2;
     int32_t hdr[6];

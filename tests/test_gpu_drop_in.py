@@ -30,7 +30,7 @@ def driver(tmp_path_factory):
     return out
 
 
-def run_driver(driver, tmp_path, scene, threads, steps, sample_rate):
+def run_driver(driver, tmp_path, scene, threads, steps, sample_rate, musl=False):
     p = scene["particles"]
     n = len(p["x"])
     mprops = scene.get("props", [1e6, 0.3])
@@ -46,8 +46,8 @@ def run_driver(driver, tmp_path, scene, threads, steps, sample_rate):
         f.write(struct.pack("q", n))
         f.write(np.stack([np.asarray(p[k], dtype=np.float64) for k in
                           ("m", "v", "x", "y", "vx", "vy", "sxx", "sxy", "syy")], axis=1).tobytes())
-    subprocess.run([driver, str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True,
-                   capture_output=True, timeout=600)
+    subprocess.run([driver, str(tmp_path / "in.bin"), str(tmp_path / "out.bin")] + (["musl"] if musl else []),
+                   check=True, capture_output=True, timeout=600)
     raw = open(tmp_path / "out.bin", "rb").read()
     n_out, t, frames = struct.unpack_from("qdq", raw, 0)
     rec = np.dtype([("d", "<f8", 12), ("i", "<i4", 2)])
@@ -86,3 +86,25 @@ def test_drop_in_driver_matches_oracle(driver, tmp_path, case):
     if scene["material"] != "isolin":
         for f in ("state9", "state10"):
             assert field_err(got[f], orc.get, f) <= 1e-8, (case, f)
+
+
+@pytest.mark.parametrize("case", ["isolin_box", "dp_silo"])
+def test_drop_in_musl_entry_point_matches_oracle(driver, tmp_path, case):
+    """explicit_mpm_step_musl_threaded through the libmpm layer, against the
+    oracle's MUSL step with the same number of threads."""
+    if case == "isolin_box":
+        scene, steps = scenes.config1(seed=2), 200
+    else:
+        scene = scenes.silo(cells=32, material="dp_ri_mt", props=(1e6, 0.3, 0.3819), dt=1e-5, hole_radius=0.1,
+                            open_time=0.001, wall_frac=0.5, fill_height=0.6)
+        steps = 300
+    threads = 3
+    t, frames, got = run_driver(driver, tmp_path, scene, threads, steps, sample_rate=5000.0, musl=True)
+    orc = O.Oracle(dict(scene, scheme="musl"), nthreads=threads)
+    orc.step(steps)
+    assert t == orc.t
+    for f in ("x", "y", "vx", "vy", "sxx", "sxy", "syy", "v", "ux", "uy"):
+        assert field_err(got[f], orc.get, f) <= 1e-9, (case, f, field_err(got[f], orc.get, f))
+    e, a = orc.get_map()
+    np.testing.assert_array_equal(got["active"], a)
+
