@@ -193,6 +193,10 @@ MPMG_API int mpmg_get_fields(mpmg_ctx *ctx, int count, const char *const *names,
    particles).  Color, the deformation gradient and the CPDI corners are
    written as mpm_init leaves them (0, identity, 0). */
 MPMG_API int mpmg_write_frame(mpmg_ctx *ctx, FILE *fd, size_t frame, double t);
+/* write_element_frame (src/writer.c:205-263): a header line, then per
+   element its four corners and the volume-weighted mean stress (sxx, sxy,
+   syy) of its active particles, summed in particle order. */
+MPMG_API int mpmg_write_element_frame(mpmg_ctx *ctx, FILE *fd, size_t frame, double t);
 MPMG_API int mpmg_write_state(mpmg_ctx *ctx, FILE *fd, double t_stop);
 MPMG_API int mpmg_read_state(FILE *fd, const mpmg_config *base, mpmg_ctx **out);
 MPMG_API int mpmg_set_field(mpmg_ctx *ctx, const char *name, const double *host_in);

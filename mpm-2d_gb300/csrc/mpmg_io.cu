@@ -118,6 +118,58 @@ int mpmg_write_frame(mpmg_ctx *ctx, FILE *fd, size_t frame, double t)
     return MPMG_OK;
 }
 
+// write_element_frame (src/writer.c:205-263): per element the
+// volume-weighted mean stress of its active particles, summed in particle
+// order as the reference does (from one read-back of v, the stresses and the
+// element map), with the element's corner coordinates (node_number_to_coords,
+// element.c:10-19).
+int mpmg_write_element_frame(mpmg_ctx *ctx, FILE *fd, size_t frame, double t)
+{
+    if (ctx == nullptr || fd == nullptr) return MPMG_ERR_INVALID;
+    if (ctx->batch) {
+        mpmg_set_error("element frames hold one simulation");
+        return MPMG_ERR_UNSUPPORTED;
+    }
+    const size_t n = ctx->np, ne = ctx->ne;
+    static const char *names[] = {"v", "sxx", "sxy", "syy"};
+    std::vector<std::vector<double>> f(4, std::vector<double>(n ? n : 1));
+    std::vector<double *> out(4);
+    for (int k = 0; k < 4; k++) out[k] = f[k].data();
+    int rc = mpmg_get_fields(ctx, 4, names, out.data());
+    if (rc != MPMG_OK) return rc;
+    std::vector<int> elem(n ? n : 1), active(n ? n : 1);
+    if ((rc = mpmg_get_map(ctx, elem.data(), active.data())) != MPMG_OK) return rc;
+    std::vector<double> sxx_acc(ne, 0.0), sxy_acc(ne, 0.0), syy_acc(ne, 0.0), v_acc(ne, 0.0);
+    for (size_t i = 0; i < n; i++) {
+        if (active[i] == 0) continue;
+        const int e = elem[i];
+        if (e < 0 || (size_t)e >= ne) continue;
+        sxx_acc[e] += f[0][i] * f[1][i];
+        sxy_acc[e] += f[0][i] * f[2][i];
+        syy_acc[e] += f[0][i] * f[3][i];
+        v_acc[e] += f[0][i];
+    }
+    const int N = ctx->cfg.Nx, Ex = N - 1;
+    const double h = ctx->cfg.h;
+    fprintf(fd, "%zu %lg %zu\n", frame, t, ne);
+    rc = write_rows(fd, ne, [&](size_t e, char *buf, size_t cap) {
+        const int n0 = (int)(e / (size_t)Ex) * N + (int)(e % (size_t)Ex);
+        const int nodes[4] = {n0, n0 + 1, n0 + 1 + N, n0 + N};
+        double c[8];
+        for (int k = 0; k < 4; k++) {
+            c[2 * k] = (nodes[k] % N) * h;
+            c[2 * k + 1] = (nodes[k] / N) * h;
+        }
+        const double va = v_acc[e];
+        return snprintf(buf, cap, "%lg %lg %lg %lg %lg %lg %lg %lg %lg %lg %lg\n", c[0], c[1], c[2], c[3], c[4],
+                        c[5], c[6], c[7], (va > 0) ? (sxx_acc[e] / va) : 0.0f, (va > 0) ? (sxy_acc[e] / va) : 0.0f,
+                        (va > 0) ? (syy_acc[e] / va) : 0.0f);
+    });
+    if (rc != MPMG_OK) return rc;
+    fflush(fd);
+    return MPMG_OK;
+}
+
 int mpmg_write_state(mpmg_ctx *ctx, FILE *fd, double t_stop)
 {
     if (ctx == nullptr || fd == nullptr) return MPMG_ERR_INVALID;

@@ -93,6 +93,7 @@ def lib(build_if_missing=True):
         L.mpmg_batch_get_time.argtypes = [vp, C.c_int, dp, ip]
         L.mpmg_write_frame.argtypes = [vp, vp, C.c_size_t, C.c_double]
         L.mpmg_write_state.argtypes = [vp, vp, C.c_double]
+        L.mpmg_write_element_frame.argtypes = [vp, vp, C.c_size_t, C.c_double]
         L.mpmg_read_state.argtypes = [vp, C.POINTER(Config), C.POINTER(vp)]
         L.mpmg_adj_forward_tape.argtypes = [vp, C.c_int, C.c_int]
         L.mpmg_adj_backward.argtypes = [vp, dp, dp, dp]
@@ -270,6 +271,11 @@ class Simulation:
             t = self.t
         with _File(path, mode) as fp:
             _check(lib().mpmg_write_frame(self._h, fp, frame, t))
+
+    def write_element_frame(self, path, frame, t, mode="w"):
+        """The driver's element frame (write_element_frame) appended or written to path."""
+        with _File(path, mode) as fp:
+            _check(lib().mpmg_write_element_frame(self._h, fp, frame, t))
 
     def write_state(self, path, t_stop=0.0):
         """The driver's state (restart) file, exact to FP64."""

@@ -16,7 +16,10 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libmpm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code is compiled without contraction of multiply-adds, so host-side
+# arithmetic (file writers, the libmpm layer) rounds the same on x86 and Arm
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", INCLUDE]
 CU_SOURCES = ["mpmg_api.cu", "mpmg_step.cu", "mpmg_sort.cu", "mpmg_nonlocal.cu", "mpmg_sort_noalloc.cu",
               "mpmg_libmpm.cu", "mpmg_mixed.cu", "mpmg_bin.cu", "mpmg_adjoint.cu",
@@ -36,6 +39,7 @@ def nvcc():
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    files.append(os.path.abspath(__file__))   # the flags
     return max(os.path.getmtime(f) for f in files)
 
 

@@ -101,3 +101,41 @@ def test_frame_rows(tmp_path, precision):
     _, act = s.get_map()
     np.testing.assert_array_equal(rows[:, 14], act)
     assert np.all(rows[:, 12] == 0) and np.all(rows[:, 15:] == 0)
+
+
+def _fmt_g(x):
+    """C's %lg."""
+    return "%g" % x
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_element_frame_rows(tmp_path, precision):
+    """write_element_frame (src/writer.c:205-263): the volume-weighted
+    element stresses summed in particle order, restated here from the same
+    read-back fields, match the library's rows text for text."""
+    sc = scenes.column(Nx=33, Ny=33, h=1 / 32, width=0.25, height=0.5, material="g_local_mu2", rho=2450.0,
+                       props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1)
+    sim = mpm2d.Simulation(sc, precision=precision)
+    sim.step(40)
+    path = tmp_path / "elements.txt"
+    sim.write_element_frame(path, 3, 0.25)
+    lines = open(path).read().splitlines()
+    ne = 32 * 32
+    assert lines[0] == "3 0.25 %d" % ne and len(lines) == ne + 1
+    v, sxx, sxy, syy = (sim.get(f) for f in ("v", "sxx", "sxy", "syy"))
+    e, a = sim.get_map()
+    acc = np.zeros((ne, 4))
+    for i in range(len(v)):
+        if a[i]:
+            acc[e[i]] += (v[i] * sxx[i], v[i] * sxy[i], v[i] * syy[i], v[i])
+    h, N = 1 / 32, 33
+    for k in (0, 5, 40, 500, ne - 1):
+        n0 = (k // 32) * N + k % 32
+        corners = []
+        for nd in (n0, n0 + 1, n0 + 1 + N, n0 + N):
+            corners += [(nd % N) * h, (nd // N) * h]
+        va = acc[k, 3]
+        vals = [acc[k, j] / va if va > 0 else 0.0 for j in range(3)]
+        assert lines[k + 1] == " ".join(_fmt_g(x) for x in corners + vals), k
+    assert any(float(l.split()[8]) != 0 for l in lines[1:])
+
