@@ -1156,14 +1156,22 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
         const double *src[9] = {m, v, x, y, vx, vy, sxx, sxy, syy};
         for (int k = 0; k < 9; k++)
             MPMG_CHECK(cudaMemcpyAsync(stage[k], src[k], n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        double **d_stage = nullptr;
-        if ((rc = dalloc(&d_stage, 9)) != MPMG_OK) return rc;
-        MPMG_CHECK(cudaMemcpyAsync(d_stage, stage, sizeof(stage), cudaMemcpyHostToDevice, ctx->stream));
-        PlaceGeom single{};
-        PlaceGeom *d_geo = nullptr;
-        int *d_poff = nullptr;
+        // scratch freed on every way out
+        struct Scratch {
+            double **stage = nullptr;
+            PlaceGeom *geo = nullptr;
+            int *poff = nullptr;
+            ~Scratch()
+            {
+                cudaFree(stage);
+                cudaFree(geo);
+                cudaFree(poff);
+            }
+        } sc;
+        if ((rc = dalloc(&sc.stage, 9)) != MPMG_OK) return rc;
+        MPMG_CHECK(cudaMemcpyAsync(sc.stage, stage, sizeof(stage), cudaMemcpyHostToDevice, ctx->stream));
         const mpmg_config &c0 = bt ? bt->cfg[0] : ctx->cfg;
-        single = PlaceGeom{c0.h, c0.xmax, c0.ymax, c0.Nx - 1, c0.Ny - 1, 0};
+        const PlaceGeom single{c0.h, c0.xmax, c0.ymax, c0.Nx - 1, c0.Ny - 1, 0};
         std::vector<PlaceGeom> hg;
         std::vector<int> hp;
         if (bt) {
@@ -1174,21 +1182,18 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
                 hg[k] = PlaceGeom{ck.h, ck.xmax, ck.ymax, ck.Nx - 1, ck.Ny - 1, (int)bt->eoff[k]};
             }
             for (int k = 0; k <= count; k++) hp[k] = (int)bt->poff[k];
-            if ((rc = dalloc(&d_geo, count)) != MPMG_OK) return rc;
-            if ((rc = dalloc(&d_poff, count + 1)) != MPMG_OK) return rc;
-            MPMG_CHECK(cudaMemcpyAsync(d_geo, hg.data(), count * sizeof(PlaceGeom), cudaMemcpyHostToDevice,
+            if ((rc = dalloc(&sc.geo, count)) != MPMG_OK) return rc;
+            if ((rc = dalloc(&sc.poff, count + 1)) != MPMG_OK) return rc;
+            MPMG_CHECK(cudaMemcpyAsync(sc.geo, hg.data(), count * sizeof(PlaceGeom), cudaMemcpyHostToDevice,
                                        ctx->stream));
-            MPMG_CHECK(cudaMemcpyAsync(d_poff, hp.data(), (count + 1) * sizeof(int), cudaMemcpyHostToDevice,
+            MPMG_CHECK(cudaMemcpyAsync(sc.poff, hp.data(), (count + 1) * sizeof(int), cudaMemcpyHostToDevice,
                                        ctx->stream));
         }
-        mx_place_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>((int)n, d_stage, single, d_geo, d_poff, count,
+        mx_place_kernel<<<blocks_for(n, 256), 256, 0, ctx->stream>>>((int)n, sc.stage, single, sc.geo, sc.poff, count,
                                                                     (int)ctx->ne, buf(s, 0), ctx->in_element);
         ctx->launches += 1;
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        cudaFree(d_stage);
-        cudaFree(d_geo);
-        cudaFree(d_poff);
         if (e != cudaSuccess) return mpmg_cuda_status(e, "mixed state upload");
     }
     s->cur = 0;

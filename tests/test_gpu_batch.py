@@ -97,3 +97,21 @@ def test_autotune_keeps_the_trajectory():
         for f in FIELDS:
             np.testing.assert_array_equal(tuned.member_get(k, f), plain.member_get(k, f), err_msg="%d %s" % (k, f))
 
+
+def test_batch_dp_ri_mt_members_equal_single_runs():
+    """Batches of the rate-independent Drucker-Prager law (szz in the record's
+    Tzz slot, mu_s per member) equal their members run alone."""
+    ens = small_ensemble(count=3, seed=4)
+    for k, sc in enumerate(ens):
+        sc["material"] = "dp_ri_mt"
+        sc["props"] = [1e6, 0.3, 0.30 + 0.05 * k]
+        sc.pop("mp", None)
+    batch = mpm2d.Batch(ens, precision="mixed")
+    batch.step(40)
+    for k, sc in enumerate(ens):
+        one = mpm2d.Simulation(sc, precision="mixed")
+        one.step(40)
+        for f in ("x", "y", "vx", "vy", "sxx", "sxy", "syy", "state1", "state9", "state10"):
+            np.testing.assert_array_equal(batch.member_get(k, f), one.get(f), err_msg="member %d %s" % (k, f))
+        one.close()
+
