@@ -99,6 +99,44 @@ def dist_env():
     return rank, world, local
 
 
+def init_ranks(torch):
+    """One process per GPU under torchrun: NCCL where there are GPUs, gloo on
+    CPU hosts."""
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, local
+
+
+def barrier(torch, dev=None):
+    """Device work done, then every rank here."""
+    if dev is not None and torch.cuda.is_available():
+        torch.cuda.synchronize(dev)
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.barrier()
+
+
+def max_over_ranks(torch, t):
+    """The largest of the ranks' values of t (a time: the job ends with its
+    slowest rank)."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return t
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_value(units_per_rank, world, seconds):
+    """Whole-job throughput: the units all ranks processed over the slowest
+    rank's time."""
+    return units_per_rank * world / seconds
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -203,7 +241,9 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     n = len(scene["particles"]["x"])
     value = n * steps / dt
-    kind = "reference" if os.path.exists(os.path.join(obuild.REF_OUT, "libref_harness.so")) and False else "port"
+    # the reference's own objects are built from its sources, which only the
+    # development host has; here the oracle (the CPU restatement) is timed
+    kind = "port"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
@@ -249,10 +289,7 @@ def phase_profile(sim, steps, table, n, ne, nn):
 def run_gpu(args):
     import torch
 
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    rank, world, local = init_ranks(torch)
     dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
     import mpm2d
@@ -264,19 +301,11 @@ def run_gpu(args):
     ne = (scene["Nx"] - 1) * (scene["Ny"] - 1)
     peak, peak_kind = measured_peaks()
 
-    def barrier():
-        torch.cuda.synchronize(dev)
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    def sync_all():
+        barrier(torch, dev)
 
-    def max_over_ranks(t):
-        if world > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([t], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            return float(tt.item())
-        return t
+    def slowest(t):
+        return max_over_ranks(torch, t)
 
     # --- mixed precision (headline) ---------------------------------------
     sim = mpm2d.Simulation(scene, device=dev, precision="mixed")
@@ -284,14 +313,14 @@ def run_gpu(args):
     sim.step(args.warmup)
     sim.synchronize()
     launches0 = sim.launch_count()
-    barrier()
+    sync_all()
     with ClockSampler(dev) as clocks:
         ms = time_steps(sim, args.steps, stream, torch)
-        barrier()
+        sync_all()
     launches = sim.launch_count() - launches0
     clk = clocks.summary()
-    t = max_over_ranks(ms / 1e3)
-    value = n * args.steps * world / t
+    t = slowest(ms / 1e3)
+    value = job_value(n * args.steps, world, t)
     phases = phase_profile(sim, max(3, min(args.steps, 10)), MIXED_BYTES, n, ne, nn)
     top = max(phases.items(), key=lambda kv: kv[1]["ms"])
     step_bytes = sum(phase_bytes(MIXED_BYTES, k, n, ne, nn) for k in MIXED_BYTES)
@@ -303,10 +332,10 @@ def run_gpu(args):
     sim64.step(args.warmup)
     sim64.synchronize()
     fp64_steps = max(3, min(args.steps, 20))
-    barrier()
+    sync_all()
     ms64 = time_steps(sim64, fp64_steps, stream64, torch)
-    barrier()
-    t64 = max_over_ranks(ms64 / 1e3)
+    sync_all()
+    t64 = slowest(ms64 / 1e3)
     value64 = n * fp64_steps * world / t64
     phases64 = phase_profile(sim64, 3, FP64_BYTES, n, ne, nn)
     sim64.close()
@@ -316,10 +345,10 @@ def run_gpu(args):
     streamf = torch.cuda.ExternalStream(simf.stream(), device=dev)
     simf.step(args.warmup)
     simf.synchronize()
-    barrier()
+    sync_all()
     msf = time_steps(simf, args.steps, streamf, torch)
-    barrier()
-    valuef = n * args.steps * world / max_over_ranks(msf / 1e3)
+    sync_all()
+    valuef = n * args.steps * world / slowest(msf / 1e3)
     simf.close()
 
     # --- batched ensemble: 256 independent silo / heap runs in one context ------
@@ -335,11 +364,11 @@ def run_gpu(args):
         tuning = bsim.autotune(steps_per_trial=16)
         bsim.synchronize()
         bsteps = max(3, min(args.steps, 20))
-        barrier()
+        sync_all()
         msb = time_steps(bsim, bsteps, bstream, torch)
-        barrier()
+        sync_all()
         bsim.close()
-        value_b = nb * bsteps * world / max_over_ranks(msb / 1e3)
+        value_b = nb * bsteps * world / slowest(msb / 1e3)
         # the same members one at a time (each its own context and step graphs)
         seq_ms = 0.0
         for sc in ens:
@@ -369,9 +398,9 @@ def run_gpu(args):
         nsim.step(args.warmup)
         nsim.synchronize()
         nsteps_nl = max(3, min(args.steps, 10))
-        barrier()
+        sync_all()
         msn = time_steps(nsim, nsteps_nl, nstream, torch)
-        barrier()
+        sync_all()
         iters = []
         nsim.enable_phase_timing(True)
         for _ in range(3):
@@ -389,9 +418,9 @@ def run_gpu(args):
         mstream = torch.cuda.ExternalStream(msim.stream(), device=dev)
         msim.step(args.warmup)
         msim.synchronize()
-        barrier()
+        sync_all()
         msm = time_steps(msim, nsteps_nl, mstream, torch)
-        barrier()
+        sync_all()
         msim.close()
         solve_ms = pt["fluidity"][0] / max(pt["fluidity"][1], 1)
         it_mean = float(np.mean(iters))
@@ -470,7 +499,7 @@ def run_gpu(args):
     # buffers).
     e2e_steps = args.e2e_steps
     host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
-    barrier()
+    sync_all()
     t0 = time.perf_counter()
     sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
     t1 = time.perf_counter()
@@ -485,8 +514,8 @@ def run_gpu(args):
     assert last[1] == e2e_steps
     sim2.get_frame(FRAME_FIELDS, out=host)
     t3 = time.perf_counter()
-    barrier()
-    e2e_t = max_over_ranks(t3 - t0)
+    sync_all()
+    e2e_t = slowest(t3 - t0)
     sim2.close()
     e2e_value = n * e2e_steps * world / e2e_t
     h2d_total = 9 * 8 * n                      # m v x y vx vy sxx sxy syy
