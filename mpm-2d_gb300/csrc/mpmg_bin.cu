@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(uint32_t *__restrict
     __syncthreads();
     const int tile = tile_s;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int base = tile * kScanTile + threadIdx.x * kScanItems;   // 12 consecutive bins per thread
+    const int base = tile * kScanTile + threadIdx.x * kScanItems;   // kScanItems consecutive bins per thread
     uint32_t v[kScanItems];
     uint32_t sum = 0;
     if (base + kScanItems <= m) {
