@@ -317,9 +317,22 @@ __device__ __forceinline__ int find_member(const int *__restrict__ off, int coun
 // fx, fy) in FP32 (process_usl.c:491-522 per particle, regrouped per
 // element).  An element with more particles than the stage is summed alone
 // from global memory.
+//
+// The stage is padded: with about four particles an element, the threads of
+// a warp read entries about four apart, which in an unpadded array land on
+// the same few banks (16-byte records 64 bytes apart, 4-byte words 16 bytes
+// apart).  One pad record after every 8 records, one pad word after every 32
+// words and two pad halves after every 64 halves spread them over all banks.
 constexpr int kP2GThreads = 256;
 constexpr int kP2GChunk = 1024;
 constexpr int kP2GPer = kP2GChunk / kP2GThreads;   // stage entries per thread
+
+__device__ __forceinline__ int pad16b(int j) { return j + (j >> 3); }
+__device__ __forceinline__ int pad4b(int j) { return j + (j >> 5); }
+__device__ __forceinline__ int pad2b(int j) { return j + ((j >> 6) << 1); }
+constexpr int kP2GChunk16 = kP2GChunk + kP2GChunk / 8;
+constexpr int kP2GChunk4 = kP2GChunk + kP2GChunk / 32;
+constexpr int kP2GChunk2 = kP2GChunk + kP2GChunk / 32;
 
 __device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, float grav, float4 a4, float4 b4,
                                                float syy)
@@ -350,11 +363,11 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(const __grid_con
                                                                 const StepParams *__restrict__ sp,
                                                                 float *__restrict__ cell_sums)
 {
-    __shared__ float4 sh_a[kP2GChunk];
-    __shared__ float4 sh_b[kP2GChunk];
-    __shared__ float sh_syy[kP2GChunk];
-    __shared__ uint32_t sh_slot[kP2GChunk];
-    __shared__ uint16_t sh_ord[kP2GChunk];
+    __shared__ float4 sh_a[kP2GChunk16];
+    __shared__ float4 sh_b[kP2GChunk16];
+    __shared__ float sh_syy[kP2GChunk4];
+    __shared__ uint32_t sh_slot[kP2GChunk4];
+    __shared__ uint16_t sh_ord[kP2GChunk2];
     __shared__ int sh_cs[kP2GThreads + 1];
     const int e0 = blockIdx.x * kP2GThreads;
     const int ne_blk = min(kP2GThreads, ne_total - e0);
@@ -403,10 +416,10 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(const __grid_con
             for (int u = 0; u < kP2GPer; u++) {
                 const int j = (int)threadIdx.x + u * kP2GThreads;
                 if (base + j < end) {
-                    sh_slot[j] = sl[u];
-                    mpmg_cp_async16(&sh_a[j], P.A + sl[u]);
-                    mpmg_cp_async16(&sh_b[j], P.B + sl[u]);
-                    mpmg_cp_async4(&sh_syy[j], &P.C[sl[u]].x);
+                    sh_slot[pad4b(j)] = sl[u];
+                    mpmg_cp_async16(&sh_a[pad16b(j)], P.A + sl[u]);
+                    mpmg_cp_async16(&sh_b[pad16b(j)], P.B + sl[u]);
+                    mpmg_cp_async4(&sh_syy[pad4b(j)], &P.C[sl[u]].x);
                 }
             }
             mpmg_cp_async_wait_all();
@@ -414,20 +427,20 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(const __grid_con
             if (mine) {
                 const int j0 = k0 - base, j1 = k1 - base;
                 for (int j = j0; j < j1; j++) {
-                    const uint32_t x = sh_slot[j];
+                    const uint32_t x = sh_slot[pad4b(j)];
                     int t = j - 1;
-                    while (t >= j0 && sh_slot[sh_ord[t]] > x) {
-                        sh_ord[t + 1] = sh_ord[t];
+                    while (t >= j0 && sh_slot[pad4b(sh_ord[pad2b(t)])] > x) {
+                        sh_ord[pad2b(t + 1)] = sh_ord[pad2b(t)];
                         t--;
                     }
-                    sh_ord[t + 1] = (uint16_t)j;
+                    sh_ord[pad2b(t + 1)] = (uint16_t)j;
                 }
                 for (int j = j0; j < j1; j++) {
-                    const int q = sh_ord[j];
-                    const uint32_t i = sh_slot[q];
+                    const int q = sh_ord[pad2b(j)];
+                    const uint32_t i = sh_slot[pad4b(q)];
                     perm[base + j] = i;
                     rank[i] = (uint32_t)(base + j);
-                    p2g_accumulate(acc, ih, grav, sh_a[q], sh_b[q], sh_syy[q]);
+                    p2g_accumulate(acc, ih, grav, sh_a[pad16b(q)], sh_b[pad16b(q)], sh_syy[pad4b(q)]);
                 }
             }
             __syncthreads();
