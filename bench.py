@@ -56,17 +56,15 @@ WORKLOAD = "box_fill_1M_g_local_mu2"
 #         writes slot + sorted key (8 B); the P2G's ordering reads the slot and
 #         writes perm (8 B): 20 B per particle; scan: bins read + cursor,
 #         cell_start written, bins zeroed (16 B per element)
-#   p2g   perm 4 + xl yl m vx vy v sxx sxy syy 36 = 40 B per particle; 20
-#         FP32 corner sums written = 80 B per element
-#   grid  80 B of corner sums per element read; FP64 mass + float4 node = 24 B
-#         per node written
+#   p2g   P2G and grid update in one kernel (the corner sums stay in shared
+#         memory): perm 4 + xl yl m vx vy v sxx sxy syy 36 = 40 B per
+#         particle; float-float mass + float4 node = 24 B per node written
 #   g2p   perm 4 + sorted key 4 + 13 floats 52 + pid 4 read, 14 floats 56 +
 #         element 4 + pid 4 written = 128 B per particle; float4 node 16 B per
 #         node read
 MIXED_BYTES = {
     "sort": (20, 16, 0),    # (per particle, per element, per node)
-    "p2g": (40, 80, 0),
-    "grid": (0, 80, 24),
+    "p2g": (40, 0, 24),
     "g2p": (128, 0, 16),
 }
 # FP64 form, g_local_mu2: keys read x y active (20 B) and write element,

@@ -64,7 +64,8 @@ struct SortScratch {
 struct MixedState {
     float4 *A[2], *B[2], *C[2], *D[2];
     int cur;
-    float *cell_sums;      // 20 FP32 corner sums per element, value-major
+    float *cell_sums;      // batches: 20 FP32 corner sums per element, value-major
+    uint32_t *halo_perm;   // single simulations: 3 x np scratch orders of oversized shared tile elements
     float4 *node4;         // per node: ax, ay, vx, vy (FP32) for the gathers
     float2 *node_mass;     // per node: mass as float-float (hi, lo)
     int g2p_blocks;        // persistent G2P grid size

@@ -493,70 +493,43 @@ __device__ __forceinline__ float ff_div(float nh, float nl, float dh, float dl, 
     return __fmaf_rn(res, r, q);
 }
 
-// Grid update, one thread per node: the four elements' corner sums in
-// colour order (process_usl.c:524-540), float-float for mass and momentum;
-// boundary masks; momentum update and nodal velocity / acceleration
-// (process_usl.c:542-566).
-template <bool F64NODE, bool BATCH>
-__global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ MemberM m0, BatchView bv, int ne_total,
-                                                      int nn_total, const int *__restrict__ cell_start,
-                                                      const float *__restrict__ cell_sums,
-                                                      const StepParams *__restrict__ sp, float tol,
-                                                      float2 *__restrict__ node_mass, float4 *__restrict__ node4,
-                                                      double *__restrict__ node_mx,
-                                                      double *__restrict__ node_my, double *__restrict__ node_fx,
-                                                      double *__restrict__ node_fy, double *__restrict__ node_m64)
+// One node of the grid update: the four elements' corner sums in colour
+// order (process_usl.c:524-540), float-float for mass and momentum; boundary
+// masks; momentum update and nodal velocity / acceleration
+// (process_usl.c:542-566).  cs[c] points at the node's corner mass sum in
+// colour element c (null when that element is absent or holds no particle);
+// the corner's other four sums follow at stride fs.
+template <bool F64NODE>
+__device__ __forceinline__ void node_finish(const MemberM &M, double t_next, float tol, int i, int j, int n,
+                                            const float *const (&cs)[4], size_t fs,
+                                            float2 *__restrict__ node_mass, float4 *__restrict__ node4,
+                                            double *__restrict__ node_mx, double *__restrict__ node_my,
+                                            double *__restrict__ node_fx, double *__restrict__ node_fy,
+                                            double *__restrict__ node_m64)
 {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nn_total) return;
-    const int k = BATCH ? find_member(bv.node_off, bv.count, n) : 0;
-    const MemberM &M = BATCH ? bv.m[k] : m0;
-    const GeomM &g = M.g;
-    const BcM &bc = M.bc;
     const double dt = M.dt;
     const float dt_hi = M.dt_hi, dt_lo = M.dt_lo;
-    const int ln = n - M.nd0;
-    const int j = (int)mpmg_div((uint32_t)ln, g.div_Nx), i = ln - j * g.Nx;
-    // the four elements in colour order and whether they hold particles
-    // (cell_start is from the scan, three kernels back)
-    int elem[4];
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-        int ci = ((i & 1) == (c & 1)) ? i : i - 1;
-        int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
-        elem[c] = -1;
-        if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
-        const int e = M.e0 + cj * g.Ex + ci;
-        if (cell_start[e] != cell_start[e + 1]) elem[c] = e;
-    }
-    const double t_next = sp[k].t + dt;
-    mpmg_pdl_wait();        // the corner sums come from the P2G just before
-    mpmg_pdl_trigger();
     float mh = 0, ml = 0, xh = 0, xl = 0, yh = 0, yl = 0;
     float fx = 0, fy = 0;
     double m64 = 0, mx64 = 0, my64 = 0;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-        if (elem[c] < 0) continue;
-        const int e = elem[c];
-        const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
-        const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
-        const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
-        const float *cs = cell_sums + (size_t)(a * 5) * ne_total + e;
+        const float *p = cs[c];
+        if (p == nullptr) continue;
         if (F64NODE) {
-            m64 += (double)cs[0];
-            mx64 += (double)cs[(size_t)ne_total];
-            my64 += (double)cs[(size_t)2 * ne_total];
+            m64 += (double)p[0];
+            mx64 += (double)p[fs];
+            my64 += (double)p[2 * fs];
         } else {
-            ff_add(mh, ml, cs[0]);
-            ff_add(xh, xl, cs[(size_t)ne_total]);
-            ff_add(yh, yl, cs[(size_t)2 * ne_total]);
+            ff_add(mh, ml, p[0]);
+            ff_add(xh, xl, p[fs]);
+            ff_add(yh, yl, p[2 * fs]);
         }
-        fx += cs[(size_t)3 * ne_total];
-        fy += cs[(size_t)4 * ne_total];
+        fx += p[3 * fs];
+        fy += p[4 * fs];
     }
     bool bx, by;
-    bc_mask_m(bc, i, j, t_next, bx, by);
+    bc_mask_m(M.bc, i, j, t_next, bx, by);
     if (F64NODE) {
         if (bx) { mx64 = 0; fx = 0; }
         if (by) { my64 = 0; fy = 0; }
@@ -618,6 +591,232 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ Me
         node_fx[n] = fx;
         node_fy[n] = fy;
     }
+}
+
+// Grid update, one thread per node, from the corner sums mx_p2g_kernel left
+// in global memory.
+template <bool F64NODE, bool BATCH>
+__global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ MemberM m0, BatchView bv, int ne_total,
+                                                      int nn_total, const int *__restrict__ cell_start,
+                                                      const float *__restrict__ cell_sums,
+                                                      const StepParams *__restrict__ sp, float tol,
+                                                      float2 *__restrict__ node_mass, float4 *__restrict__ node4,
+                                                      double *__restrict__ node_mx,
+                                                      double *__restrict__ node_my, double *__restrict__ node_fx,
+                                                      double *__restrict__ node_fy, double *__restrict__ node_m64)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn_total) return;
+    const int k = BATCH ? find_member(bv.node_off, bv.count, n) : 0;
+    const MemberM &M = BATCH ? bv.m[k] : m0;
+    const GeomM &g = M.g;
+    const int ln = n - M.nd0;
+    const int j = (int)mpmg_div((uint32_t)ln, g.div_Nx), i = ln - j * g.Nx;
+    // the four elements in colour order, where they hold particles
+    // (cell_start is from the scan, three kernels back)
+    const float *cs[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+        const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+        cs[c] = nullptr;
+        if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
+        const int e = M.e0 + cj * g.Ex + ci;
+        const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+        if (cell_start[e] != cell_start[e + 1]) cs[c] = cell_sums + (size_t)(a * 5) * ne_total + e;
+    }
+    const double t_next = sp[k].t + M.dt;
+    mpmg_pdl_wait();        // the corner sums come from the P2G just before
+    mpmg_pdl_trigger();
+    node_finish<F64NODE>(M, t_next, tol, i, j, n, cs, (size_t)ne_total, node_mass, node4, node_mx, node_my, node_fx,
+                         node_fy, node_m64);
+}
+
+// P2G and grid update in one kernel, for a single simulation.  A block takes
+// a 16 x 16 tile of elements, one thread each, sums them exactly as
+// mx_p2g_kernel does (the same stage, order and arithmetic), leaves the 20
+// corner sums in shared memory and finishes the 15 x 15 nodes whose four
+// elements all lie in the tile exactly as mx_grid_kernel does.  Neighbouring
+// tiles share one column or row of elements, which both sum to the same
+// values; perm and rank of an element are written by the one tile where it
+// is not in the first column or row.  An element with more particles than
+// the stage is ordered in global memory: by its owner in perm, by the other
+// tiles in a scratch copy of their own (one per kind of overlap).  The corner
+// sums never reach global memory and the grid update needs no launch.
+constexpr int kTileE = 16;                        // elements per tile side
+constexpr int kTileN = kTileE - 1;                // nodes finished per tile side
+constexpr int kSumStride = kTileE * kTileE + 1;   // corner-sum row in shared memory
+constexpr int kStageBytes = (int)(sizeof(float4) * 2 * kP2GChunk16 + sizeof(float) * 2 * kP2GChunk4 +
+                                  sizeof(uint16_t) * kP2GChunk2);
+static_assert(kTileE * kTileE == kP2GThreads, "one thread per tile element");
+static_assert((int)sizeof(float) * 20 * kSumStride <= kStageBytes, "the corner sums overlay the stage");
+
+template <bool F64NODE>
+__global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
+    const __grid_constant__ MemberM M, int np, int tiles_x, const int *__restrict__ cell_start,
+    const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm, uint32_t *__restrict__ rank,
+    uint32_t *__restrict__ halo_perm, Buf P, const StepParams *__restrict__ sp, float tol,
+    float2 *__restrict__ node_mass, float4 *__restrict__ node4, double *__restrict__ node_mx,
+    double *__restrict__ node_my, double *__restrict__ node_fx, double *__restrict__ node_fy,
+    double *__restrict__ node_m64)
+{
+    __shared__ __align__(16) unsigned char smem[kStageBytes];
+    __shared__ int sh_off[kP2GThreads + 1];   // stage offsets of the tile's elements
+    __shared__ int sh_gs[kTileE];             // storage position of each tile row's first particle
+    __shared__ int sh_wsum[kP2GThreads / 32];
+    float4 *sh_a = reinterpret_cast<float4 *>(smem);
+    float4 *sh_b = sh_a + kP2GChunk16;
+    float *sh_syy = reinterpret_cast<float *>(sh_b + kP2GChunk16);
+    uint32_t *sh_slot = reinterpret_cast<uint32_t *>(sh_syy + kP2GChunk4);
+    uint16_t *sh_ord = reinterpret_cast<uint16_t *>(sh_slot + kP2GChunk4);
+    float *sh_sum = reinterpret_cast<float *>(smem);
+
+    const int me = threadIdx.x, lane = me & 31, warp = me >> 5;
+    const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const int lx = me % kTileE, ly = me / kTileE;
+    const int ei = tx * kTileN - 1 + lx, ej = ty * kTileN - 1 + ly;
+    const bool exists = ei >= 0 && ej >= 0 && ei < M.g.Ex && ej < M.g.Ey;
+    const bool owner = lx > 0 && ly > 0;
+    // element offsets come from the scan, two kernels back
+    int k0 = 0, k1 = 0;
+    if (exists) {
+        const int e = ej * M.g.Ex + ei;
+        k0 = cell_start[e];
+        k1 = cell_start[e + 1];
+    }
+    const int cnt = k1 - k0;
+    // stage offsets: exclusive prefix of the counts in tile order
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    if (lane == 31) sh_wsum[warp] = incl;
+    __syncthreads();
+    int wbase = 0;
+    for (int w = 0; w < warp; w++) wbase += sh_wsum[w];
+    sh_off[me] = wbase + incl - cnt;
+    if (me == kP2GThreads - 1) sh_off[kP2GThreads] = wbase + incl;
+    // a row's elements are consecutive, so its particles are one storage run
+    if (exists && (lx == 0 || ei == 0)) sh_gs[ly] = k0;
+    // the slots come from the scatter, the kernel just before
+    mpmg_pdl_wait();
+    __syncthreads();
+    const float grav = (float)sp->gravity, ih = M.g.inv_hf;
+    float acc[4][5];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
+    int ea = 0;
+    while (ea < kP2GThreads) {
+        // elements [ea, eb) of this pass: the most whose particles fit the stage
+        const int limit = sh_off[ea] + kP2GChunk;
+        int lo = ea + 1, hi = kP2GThreads;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sh_off[mid] <= limit) lo = mid;
+            else hi = mid - 1;
+        }
+        const int eb = lo;
+        const int base = sh_off[ea], end = sh_off[eb];
+        const bool mine = me >= ea && me < eb && cnt > 0;
+        if (end - base <= kP2GChunk) {
+            // each warp stages its two tile rows' share of the pass
+            const int r0 = 2 * warp, r1 = r0 + 1;
+            const int s0 = max(sh_off[r0 * kTileE], base), e0 = min(sh_off[r0 * kTileE + kTileE], end);
+            const int s1 = max(sh_off[r1 * kTileE], base), e1 = min(sh_off[r1 * kTileE + kTileE], end);
+            const int n0 = max(e0 - s0, 0), n1 = max(e1 - s1, 0);
+            const int g0 = n0 > 0 ? sh_gs[r0] - sh_off[r0 * kTileE] : 0;
+            const int g1 = n1 > 0 ? sh_gs[r1] - sh_off[r1 * kTileE] : 0;
+            for (int v0 = 0; v0 < n0 + n1; v0 += 32 * kP2GPer) {
+                uint32_t sl[kP2GPer];
+                int q[kP2GPer];
+#pragma unroll
+                for (int u = 0; u < kP2GPer; u++) {
+                    const int v = v0 + lane + 32 * u;
+                    q[u] = -1;
+                    sl[u] = 0u;
+                    if (v < n0) {
+                        q[u] = s0 + v - base;
+                        sl[u] = slots[g0 + s0 + v];
+                    } else if (v < n0 + n1) {
+                        q[u] = s1 + (v - n0) - base;
+                        sl[u] = slots[g1 + s1 + (v - n0)];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kP2GPer; u++) {
+                    if (q[u] < 0) continue;
+                    sh_slot[pad4b(q[u])] = sl[u];
+                    mpmg_cp_async16(&sh_a[pad16b(q[u])], P.A + sl[u]);
+                    mpmg_cp_async16(&sh_b[pad16b(q[u])], P.B + sl[u]);
+                    mpmg_cp_async4(&sh_syy[pad4b(q[u])], &P.C[sl[u]].x);
+                }
+            }
+            mpmg_cp_async_wait_all();
+            __syncthreads();
+            if (mine) {
+                const int j0 = sh_off[me] - base, j1 = j0 + cnt;
+                for (int j = j0; j < j1; j++) {
+                    const uint32_t x = sh_slot[pad4b(j)];
+                    int t = j - 1;
+                    while (t >= j0 && sh_slot[pad4b(sh_ord[pad2b(t)])] > x) {
+                        sh_ord[pad2b(t + 1)] = sh_ord[pad2b(t)];
+                        t--;
+                    }
+                    sh_ord[pad2b(t + 1)] = (uint16_t)j;
+                }
+                for (int j = j0; j < j1; j++) {
+                    const int q = sh_ord[pad2b(j)];
+                    const uint32_t i = sh_slot[pad4b(q)];
+                    if (owner) {
+                        perm[k0 + (j - j0)] = i;
+                        rank[i] = (uint32_t)(k0 + (j - j0));
+                    }
+                    p2g_accumulate(acc, ih, grav, sh_a[pad16b(q)], sh_b[pad16b(q)], sh_syy[pad4b(q)]);
+                }
+            }
+            __syncthreads();
+        } else if (mine) {
+            // a single element larger than the stage
+            uint32_t *order = perm;
+            if (!owner) order = halo_perm + (size_t)(lx == 0 ? (ly == 0 ? 2 : 0) : 1) * (size_t)np;
+            mpmg_order_segment(slots, order, owner ? rank : nullptr, k0, k1);
+            for (int k = k0; k < k1; k++) {
+                const uint32_t i = order[k];
+                p2g_accumulate(acc, ih, grav, P.A[i], P.B[i], P.C[i].x);
+            }
+        }
+        ea = eb;
+    }
+    // the stage is free: the corner sums take its place
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < 5; f++) sh_sum[(a * 5 + f) * kSumStride + me] = acc[a][f];
+    __syncthreads();
+    if (me < kTileN * kTileN) {
+        const int i = tx * kTileN + me % kTileN, j = ty * kTileN + me / kTileN;
+        if (i < M.g.Nx && j < M.g.Ny) {
+            const float *cs[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
+                const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
+                cs[c] = nullptr;
+                if (ci < 0 || cj < 0 || ci >= M.g.Ex || cj >= M.g.Ey) continue;
+                const int le = (cj - ty * kTileN + 1) * kTileE + (ci - tx * kTileN + 1);
+                const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
+                if (sh_off[le + 1] != sh_off[le]) cs[c] = sh_sum + (a * 5) * kSumStride + le;
+            }
+            node_finish<F64NODE>(M, sp->t + M.dt, tol, i, j, j * M.g.Nx + i, cs, (size_t)kSumStride, node_mass,
+                                 node4, node_mx, node_my, node_fx, node_fy, node_m64);
+        }
+    }
+    mpmg_pdl_trigger();
 }
 
 // G2P of one particle read from the stored position i (element e of member
@@ -1120,7 +1319,11 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
         for (float4 **p : f)
             if ((rc = dalloc(p, n)) != MPMG_OK) return rc;
     }
-    if ((rc = dalloc(&s->cell_sums, 20 * ctx->ne)) != MPMG_OK) return rc;
+    if (ctx->batch != nullptr) {
+        if ((rc = dalloc(&s->cell_sums, 20 * ctx->ne)) != MPMG_OK) return rc;
+    } else if ((rc = dalloc(&s->halo_perm, 3 * n)) != MPMG_OK) {
+        return rc;
+    }
     if ((rc = dalloc(&s->node4, ctx->nn)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->node_mass, ctx->nn)) != MPMG_OK) return rc;
     if ((rc = dalloc(&s->export_buf, n)) != MPMG_OK) return rc;
@@ -1250,6 +1453,7 @@ void mpmg_mixed_free(mpmg_ctx *ctx)
         cudaFree(s->D[b]);
     }
     cudaFree(s->cell_sums);
+    cudaFree(s->halo_perm);
     cudaFree(s->node4);
     cudaFree(s->node_mass);
     cudaFree(s->export_buf);
@@ -1297,24 +1501,36 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     mpmg_phase_end(ctx, PH_SORT);
 
     Buf S = buf(s, cur), D = buf(s, nxt);
-    mpmg_phase_begin(ctx, PH_P2G);
-    MPMG_CHECK(mpmg_launch_pdl(true, batch ? mx_p2g_kernel<true> : mx_p2g_kernel<false>,
-                               dim3(blocks_for(ctx->ne, kP2GThreads)), dim3(kP2GThreads), 0, st, m0, bv, ne,
-                               (const int *)ctx->cell_start, (const uint32_t *)ctx->bin.slots, ctx->perm,
-                               ctx->bin.rank, S, (const StepParams *)ctx->d_params, s->cell_sums));
-    mpmg_phase_end(ctx, PH_P2G);
-
-    mpmg_phase_begin(ctx, PH_GRID);
     const bool f64 = c.precision == MPMG_PRECISION_MIXED_F64NODE;
-    auto grid = f64 ? (batch ? mx_grid_kernel<true, true> : mx_grid_kernel<true, false>)
-                    : (batch ? mx_grid_kernel<false, true> : mx_grid_kernel<false, false>);
     const bool nonlocal = c.material == MPMG_G_NONLOCAL_MU2;
-    MPMG_CHECK(mpmg_launch_pdl(true, grid, dim3(blocks_for(ctx->nn, 256)), dim3(256), 0, st, m0, bv, ne, nn,
-                               (const int *)ctx->cell_start, (const float *)s->cell_sums,
-                               (const StepParams *)ctx->d_params, (float)MPMG_TOL, s->node_mass, s->node4,
-                               ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy,
-                               nonlocal ? ctx->node_m : (double *)nullptr));
-    mpmg_phase_end(ctx, PH_GRID);
+    double *node_m64 = nonlocal ? ctx->node_m : (double *)nullptr;
+    if (!batch) {
+        // P2G and grid update fused over 16 x 16 element tiles
+        mpmg_phase_begin(ctx, PH_P2G);
+        const int tiles_x = (m0.g.Nx + kTileN - 1) / kTileN, tiles_y = (m0.g.Ny + kTileN - 1) / kTileN;
+        MPMG_CHECK(mpmg_launch_pdl(true, f64 ? mx_p2g_grid_kernel<true> : mx_p2g_grid_kernel<false>,
+                                   dim3(tiles_x * tiles_y), dim3(kP2GThreads), 0, st, m0, n, tiles_x,
+                                   (const int *)ctx->cell_start, (const uint32_t *)ctx->bin.slots, ctx->perm,
+                                   ctx->bin.rank, s->halo_perm, S, (const StepParams *)ctx->d_params,
+                                   (float)MPMG_TOL, s->node_mass, s->node4, ctx->node_mx, ctx->node_my,
+                                   ctx->node_fx, ctx->node_fy, node_m64));
+        mpmg_phase_end(ctx, PH_P2G);
+    } else {
+        mpmg_phase_begin(ctx, PH_P2G);
+        MPMG_CHECK(mpmg_launch_pdl(true, mx_p2g_kernel<true>, dim3(blocks_for(ctx->ne, kP2GThreads)),
+                                   dim3(kP2GThreads), 0, st, m0, bv, ne, (const int *)ctx->cell_start,
+                                   (const uint32_t *)ctx->bin.slots, ctx->perm, ctx->bin.rank, S,
+                                   (const StepParams *)ctx->d_params, s->cell_sums));
+        mpmg_phase_end(ctx, PH_P2G);
+
+        mpmg_phase_begin(ctx, PH_GRID);
+        MPMG_CHECK(mpmg_launch_pdl(true, f64 ? mx_grid_kernel<true, true> : mx_grid_kernel<false, true>,
+                                   dim3(blocks_for(ctx->nn, 256)), dim3(256), 0, st, m0, bv, ne, nn,
+                                   (const int *)ctx->cell_start, (const float *)s->cell_sums,
+                                   (const StepParams *)ctx->d_params, (float)MPMG_TOL, s->node_mass, s->node4,
+                                   ctx->node_mx, ctx->node_my, ctx->node_fx, ctx->node_fy, node_m64));
+        mpmg_phase_end(ctx, PH_GRID);
+    }
 
     mpmg_phase_begin(ctx, PH_G2P);
     MPMG_CHECK(mpmg_launch_pdl(true, g2p_variant(c.material, batch), dim3(s->g2p_blocks), dim3(kG2PTile),
@@ -1322,7 +1538,7 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
                                (const int *)cell_array(ctx, cur), cell_array(ctx, nxt), (const float4 *)s->node4,
                                ctx->bin.counts, ctx->d_params, ctx->d_status, NLOut{s->nl_E, s->nl_F}));
     mpmg_phase_end(ctx, PH_G2P);
-    ctx->launches += 3;
+    ctx->launches += batch ? 3 : 2;
     if (nonlocal) {
         // the fluidity solve (FP64 Krylov) and the stress update
         mpmg_phase_begin(ctx, PH_FLUIDITY);
