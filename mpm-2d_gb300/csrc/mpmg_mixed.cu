@@ -633,26 +633,33 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ Me
 }
 
 // P2G and grid update in one kernel, for a single simulation.  A block takes
-// a 16 x 16 tile of elements, one thread each, sums them exactly as
-// mx_p2g_kernel does (the same stage, order and arithmetic), leaves the 20
-// corner sums in shared memory and finishes the 15 x 15 nodes whose four
-// elements all lie in the tile exactly as mx_grid_kernel does.  Neighbouring
-// tiles share one column or row of elements, which both sum to the same
-// values; perm and rank of an element are written by the one tile where it
-// is not in the first column or row.  An element with more particles than
-// the stage is ordered in global memory: by its owner in perm, by the other
-// tiles in a scratch copy of their own (one per kind of overlap).  The corner
-// sums never reach global memory and the grid update needs no launch.
-constexpr int kTileE = 16;                        // elements per tile side
-constexpr int kTileN = kTileE - 1;                // nodes finished per tile side
-constexpr int kSumStride = kTileE * kTileE + 1;   // corner-sum row in shared memory
-constexpr int kStageBytes = (int)(sizeof(float4) * 2 * kP2GChunk16 + sizeof(float) * 2 * kP2GChunk4 +
-                                  sizeof(uint16_t) * kP2GChunk2);
-static_assert(kTileE * kTileE == kP2GThreads, "one thread per tile element");
-static_assert((int)sizeof(float) * 20 * kSumStride <= kStageBytes, "the corner sums overlay the stage");
+// a TX x TY tile of elements, one thread each, sums them exactly as
+// mx_p2g_kernel does (the same staging, order and arithmetic), leaves the 20
+// corner sums in shared memory and finishes the (TX - 1) x (TY - 1) nodes
+// whose four elements all lie in the tile exactly as mx_grid_kernel does.
+// Neighbouring tiles share one column or row of elements, which both sum to
+// the same values; perm and rank of an element are written by the one tile
+// where it is not in the first column or row.  An element with more
+// particles than the stage is ordered in global memory: by its owner in
+// perm, by the other tiles in a scratch copy of their own (one per kind of
+// overlap).  The corner sums never reach global memory and the grid update
+// needs no launch.
+template <int TX, int TY>
+struct FusedTile {
+    static constexpr int threads = TX * TY;
+    static constexpr int chunk = 4 * threads;                  // staged particles a pass
+    static constexpr int c16 = chunk + chunk / 8, c4 = chunk + chunk / 32, c2 = chunk + chunk / 32;
+    static constexpr int sum_stride = threads + 1;             // corner-sum row in shared memory
+    static constexpr int rows_per_warp = 32 / TX;
+    static constexpr size_t smem = sizeof(float4) * 2 * c16 + sizeof(float) * 2 * c4 + sizeof(uint16_t) * c2;
+    static_assert(TX * (32 / TX) == 32 && rows_per_warp <= 2 && threads % 32 == 0, "a warp stages one or two whole tile rows");
+    static_assert(sizeof(float) * 20 * sum_stride <= smem, "the corner sums overlay the stage");
+};
+constexpr int kFusedTX = 16, kFusedTY = 16;
+using FusedT = FusedTile<kFusedTX, kFusedTY>;
 
-template <bool F64NODE>
-__global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
+template <bool F64NODE, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) mx_p2g_grid_kernel(
     const __grid_constant__ MemberM M, int np, int tiles_x, const int *__restrict__ cell_start,
     const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm, uint32_t *__restrict__ rank,
     uint32_t *__restrict__ halo_perm, Buf P, const StepParams *__restrict__ sp, float tol,
@@ -660,21 +667,23 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
     double *__restrict__ node_my, double *__restrict__ node_fx, double *__restrict__ node_fy,
     double *__restrict__ node_m64)
 {
-    __shared__ __align__(16) unsigned char smem[kStageBytes];
-    __shared__ int sh_off[kP2GThreads + 1];   // stage offsets of the tile's elements
-    __shared__ int sh_gs[kTileE];             // storage position of each tile row's first particle
-    __shared__ int sh_wsum[kP2GThreads / 32];
+    using T = FusedTile<TX, TY>;
+    constexpr int NT = T::threads, CH = T::chunk, SS = T::sum_stride;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int sh_off[NT + 1];     // stage offsets of the tile's elements
+    __shared__ int sh_gs[TY];          // storage position of each tile row's first particle
+    __shared__ int sh_wsum[NT / 32];
     float4 *sh_a = reinterpret_cast<float4 *>(smem);
-    float4 *sh_b = sh_a + kP2GChunk16;
-    float *sh_syy = reinterpret_cast<float *>(sh_b + kP2GChunk16);
-    uint32_t *sh_slot = reinterpret_cast<uint32_t *>(sh_syy + kP2GChunk4);
-    uint16_t *sh_ord = reinterpret_cast<uint16_t *>(sh_slot + kP2GChunk4);
+    float4 *sh_b = sh_a + T::c16;
+    float *sh_syy = reinterpret_cast<float *>(sh_b + T::c16);
+    uint32_t *sh_slot = reinterpret_cast<uint32_t *>(sh_syy + T::c4);
+    uint16_t *sh_ord = reinterpret_cast<uint16_t *>(sh_slot + T::c4);
     float *sh_sum = reinterpret_cast<float *>(smem);
 
     const int me = threadIdx.x, lane = me & 31, warp = me >> 5;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    const int lx = me % kTileE, ly = me / kTileE;
-    const int ei = tx * kTileN - 1 + lx, ej = ty * kTileN - 1 + ly;
+    const int lx = me % TX, ly = me / TX;
+    const int ei = tx * (TX - 1) - 1 + lx, ej = ty * (TY - 1) - 1 + ly;
     const bool exists = ei >= 0 && ej >= 0 && ei < M.g.Ex && ej < M.g.Ey;
     const bool owner = lx > 0 && ly > 0;
     // element offsets come from the scan, two kernels back
@@ -697,7 +706,7 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
     int wbase = 0;
     for (int w = 0; w < warp; w++) wbase += sh_wsum[w];
     sh_off[me] = wbase + incl - cnt;
-    if (me == kP2GThreads - 1) sh_off[kP2GThreads] = wbase + incl;
+    if (me == NT - 1) sh_off[NT] = wbase + incl;
     // a row's elements are consecutive, so its particles are one storage run
     if (exists && (lx == 0 || ei == 0)) sh_gs[ly] = k0;
     // the slots come from the scatter, the kernel just before
@@ -710,10 +719,10 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
 #pragma unroll
         for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
     int ea = 0;
-    while (ea < kP2GThreads) {
+    while (ea < NT) {
         // elements [ea, eb) of this pass: the most whose particles fit the stage
-        const int limit = sh_off[ea] + kP2GChunk;
-        int lo = ea + 1, hi = kP2GThreads;
+        const int limit = sh_off[ea] + CH;
+        int lo = ea + 1, hi = NT;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (sh_off[mid] <= limit) lo = mid;
@@ -722,14 +731,21 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
         const int eb = lo;
         const int base = sh_off[ea], end = sh_off[eb];
         const bool mine = me >= ea && me < eb && cnt > 0;
-        if (end - base <= kP2GChunk) {
-            // each warp stages its two tile rows' share of the pass
-            const int r0 = 2 * warp, r1 = r0 + 1;
-            const int s0 = max(sh_off[r0 * kTileE], base), e0 = min(sh_off[r0 * kTileE + kTileE], end);
-            const int s1 = max(sh_off[r1 * kTileE], base), e1 = min(sh_off[r1 * kTileE + kTileE], end);
-            const int n0 = max(e0 - s0, 0), n1 = max(e1 - s1, 0);
-            const int g0 = n0 > 0 ? sh_gs[r0] - sh_off[r0 * kTileE] : 0;
-            const int g1 = n1 > 0 ? sh_gs[r1] - sh_off[r1 * kTileE] : 0;
+        if (end - base <= CH) {
+            // each warp stages its tile rows' share of the pass (one or two
+            // storage runs), four loads in flight a lane
+            int s0 = 0, n0 = 0, g0 = 0, s1 = 0, n1 = 0, g1 = 0;
+            {
+                const int r = warp * T::rows_per_warp;
+                s0 = max(sh_off[r * TX], base);
+                n0 = max(min(sh_off[r * TX + TX], end) - s0, 0);
+                if (n0 > 0) g0 = sh_gs[r] - sh_off[r * TX];
+                if (T::rows_per_warp == 2) {
+                    s1 = max(sh_off[(r + 1) * TX], base);
+                    n1 = max(min(sh_off[(r + 1) * TX + TX], end) - s1, 0);
+                    if (n1 > 0) g1 = sh_gs[r + 1] - sh_off[(r + 1) * TX];
+                }
+            }
             for (int v0 = 0; v0 < n0 + n1; v0 += 32 * kP2GPer) {
                 uint32_t sl[kP2GPer];
                 int q[kP2GPer];
@@ -796,10 +812,10 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
 #pragma unroll
     for (int a = 0; a < 4; a++)
 #pragma unroll
-        for (int f = 0; f < 5; f++) sh_sum[(a * 5 + f) * kSumStride + me] = acc[a][f];
+        for (int f = 0; f < 5; f++) sh_sum[(a * 5 + f) * SS + me] = acc[a][f];
     __syncthreads();
-    if (me < kTileN * kTileN) {
-        const int i = tx * kTileN + me % kTileN, j = ty * kTileN + me / kTileN;
+    if (me < (TX - 1) * (TY - 1)) {
+        const int i = tx * (TX - 1) + me % (TX - 1), j = ty * (TY - 1) + me / (TX - 1);
         if (i < M.g.Nx && j < M.g.Ny) {
             const float *cs[4];
 #pragma unroll
@@ -808,12 +824,12 @@ __global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_grid_kernel(
                 const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
                 cs[c] = nullptr;
                 if (ci < 0 || cj < 0 || ci >= M.g.Ex || cj >= M.g.Ey) continue;
-                const int le = (cj - ty * kTileN + 1) * kTileE + (ci - tx * kTileN + 1);
+                const int le = (cj - ty * (TY - 1) + 1) * TX + (ci - tx * (TX - 1) + 1);
                 const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
-                if (sh_off[le + 1] != sh_off[le]) cs[c] = sh_sum + (a * 5) * kSumStride + le;
+                if (sh_off[le + 1] != sh_off[le]) cs[c] = sh_sum + (a * 5) * SS + le;
             }
-            node_finish<F64NODE>(M, sp->t + M.dt, tol, i, j, j * M.g.Nx + i, cs, (size_t)kSumStride, node_mass,
-                                 node4, node_mx, node_my, node_fx, node_fy, node_m64);
+            node_finish<F64NODE>(M, sp->t + M.dt, tol, i, j, j * M.g.Nx + i, cs, (size_t)SS, node_mass, node4,
+                                 node_mx, node_my, node_fx, node_fy, node_m64);
         }
     }
     mpmg_pdl_trigger();
@@ -1419,6 +1435,10 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
     G2PKernel g2p = g2p_variant(ctx->cfg.material, bt != nullptr);
     MPMG_CHECK(cudaFuncSetAttribute(g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG2PSmem));
+    MPMG_CHECK(cudaFuncSetAttribute(mx_p2g_grid_kernel<false, kFusedTX, kFusedTY>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedT::smem));
+    MPMG_CHECK(cudaFuncSetAttribute(mx_p2g_grid_kernel<true, kFusedTX, kFusedTY>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedT::smem));
     MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g2p, kG2PTile, kG2PSmem));
     s->sms = sms > 0 ? sms : 1;
     s->g2p_per_sm_max = per_sm > 0 ? per_sm : 1;
@@ -1505,13 +1525,15 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     const bool nonlocal = c.material == MPMG_G_NONLOCAL_MU2;
     double *node_m64 = nonlocal ? ctx->node_m : (double *)nullptr;
     if (!batch) {
-        // P2G and grid update fused over 16 x 16 element tiles
+        // P2G and grid update fused over element tiles
         mpmg_phase_begin(ctx, PH_P2G);
-        const int tiles_x = (m0.g.Nx + kTileN - 1) / kTileN, tiles_y = (m0.g.Ny + kTileN - 1) / kTileN;
-        MPMG_CHECK(mpmg_launch_pdl(true, f64 ? mx_p2g_grid_kernel<true> : mx_p2g_grid_kernel<false>,
-                                   dim3(tiles_x * tiles_y), dim3(kP2GThreads), 0, st, m0, n, tiles_x,
-                                   (const int *)ctx->cell_start, (const uint32_t *)ctx->bin.slots, ctx->perm,
-                                   ctx->bin.rank, s->halo_perm, S, (const StepParams *)ctx->d_params,
+        const int tiles_x = (m0.g.Nx + kFusedTX - 2) / (kFusedTX - 1);
+        const int tiles_y = (m0.g.Ny + kFusedTY - 2) / (kFusedTY - 1);
+        MPMG_CHECK(mpmg_launch_pdl(true, f64 ? mx_p2g_grid_kernel<true, kFusedTX, kFusedTY>
+                                             : mx_p2g_grid_kernel<false, kFusedTX, kFusedTY>,
+                                   dim3(tiles_x * tiles_y), dim3(FusedT::threads), FusedT::smem, st, m0, n,
+                                   tiles_x, (const int *)ctx->cell_start, (const uint32_t *)ctx->bin.slots,
+                                   ctx->perm, ctx->bin.rank, s->halo_perm, S, (const StepParams *)ctx->d_params,
                                    (float)MPMG_TOL, s->node_mass, s->node4, ctx->node_mx, ctx->node_my,
                                    ctx->node_fx, ctx->node_fy, node_m64));
         mpmg_phase_end(ctx, PH_P2G);
