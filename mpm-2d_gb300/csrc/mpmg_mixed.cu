@@ -496,12 +496,12 @@ __device__ __forceinline__ float ff_div(float nh, float nl, float dh, float dl, 
 // One node of the grid update: the four elements' corner sums in colour
 // order (process_usl.c:524-540), float-float for mass and momentum; boundary
 // masks; momentum update and nodal velocity / acceleration
-// (process_usl.c:542-566).  cs[c] points at the node's corner mass sum in
-// colour element c (null when that element is absent or holds no particle);
-// the corner's other four sums follow at stride fs.
-template <bool F64NODE>
+// (process_usl.c:542-566).  cs + off[c] is the node's corner mass sum in
+// colour element c (off[c] < 0 when that element is absent or holds no
+// particle); the corner's other four sums follow at stride fs.
+template <bool F64NODE, typename Off>
 __device__ __forceinline__ void node_finish(const MemberM &M, double t_next, float tol, int i, int j, int n,
-                                            const float *const (&cs)[4], size_t fs,
+                                            const float *__restrict__ cs, const Off (&off)[4], Off fs,
                                             float2 *__restrict__ node_mass, float4 *__restrict__ node4,
                                             double *__restrict__ node_mx, double *__restrict__ node_my,
                                             double *__restrict__ node_fx, double *__restrict__ node_fy,
@@ -514,8 +514,8 @@ __device__ __forceinline__ void node_finish(const MemberM &M, double t_next, flo
     double m64 = 0, mx64 = 0, my64 = 0;
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-        const float *p = cs[c];
-        if (p == nullptr) continue;
+        if (off[c] < 0) continue;
+        const float *p = cs + off[c];
         if (F64NODE) {
             m64 += (double)p[0];
             mx64 += (double)p[fs];
@@ -614,22 +614,22 @@ __global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ Me
     const int j = (int)mpmg_div((uint32_t)ln, g.div_Nx), i = ln - j * g.Nx;
     // the four elements in colour order, where they hold particles
     // (cell_start is from the scan, three kernels back)
-    const float *cs[4];
+    long long off[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
         const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
-        cs[c] = nullptr;
+        off[c] = -1;
         if (ci < 0 || cj < 0 || ci >= g.Ex || cj >= g.Ey) continue;
         const int e = M.e0 + cj * g.Ex + ci;
         const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
-        if (cell_start[e] != cell_start[e + 1]) cs[c] = cell_sums + (size_t)(a * 5) * ne_total + e;
+        if (cell_start[e] != cell_start[e + 1]) off[c] = (long long)(a * 5) * ne_total + e;
     }
     const double t_next = sp[k].t + M.dt;
     mpmg_pdl_wait();        // the corner sums come from the P2G just before
     mpmg_pdl_trigger();
-    node_finish<F64NODE>(M, t_next, tol, i, j, n, cs, (size_t)ne_total, node_mass, node4, node_mx, node_my, node_fx,
-                         node_fy, node_m64);
+    node_finish<F64NODE>(M, t_next, tol, i, j, n, cell_sums, off, (long long)ne_total, node_mass, node4, node_mx,
+                         node_my, node_fx, node_fy, node_m64);
 }
 
 // P2G and grid update in one kernel, for a single simulation.  A block takes
@@ -720,9 +720,10 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) mx_p2g_grid_kernel(
         for (int f = 0; f < 5; f++) acc[a][f] = 0.0f;
     int ea = 0;
     while (ea < NT) {
-        // elements [ea, eb) of this pass: the most whose particles fit the stage
+        // elements [ea, eb) of this pass: the most whose particles fit the
+        // stage (usually all the rest)
         const int limit = sh_off[ea] + CH;
-        int lo = ea + 1, hi = NT;
+        int lo = sh_off[NT] <= limit ? NT : ea + 1, hi = NT;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (sh_off[mid] <= limit) lo = mid;
@@ -817,18 +818,18 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) mx_p2g_grid_kernel(
     if (me < (TX - 1) * (TY - 1)) {
         const int i = tx * (TX - 1) + me % (TX - 1), j = ty * (TY - 1) + me / (TX - 1);
         if (i < M.g.Nx && j < M.g.Ny) {
-            const float *cs[4];
+            int off[4];
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
                 const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
-                cs[c] = nullptr;
+                off[c] = -1;
                 if (ci < 0 || cj < 0 || ci >= M.g.Ex || cj >= M.g.Ey) continue;
                 const int le = (cj - ty * (TY - 1) + 1) * TX + (ci - tx * (TX - 1) + 1);
                 const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
-                if (sh_off[le + 1] != sh_off[le]) cs[c] = sh_sum + (a * 5) * SS + le;
+                if (sh_off[le + 1] != sh_off[le]) off[c] = (a * 5) * SS + le;
             }
-            node_finish<F64NODE>(M, sp->t + M.dt, tol, i, j, j * M.g.Nx + i, cs, (size_t)SS, node_mass, node4,
+            node_finish<F64NODE>(M, sp->t + M.dt, tol, i, j, j * M.g.Nx + i, sh_sum, off, SS, node_mass, node4,
                                  node_mx, node_my, node_fx, node_fy, node_m64);
         }
     }
