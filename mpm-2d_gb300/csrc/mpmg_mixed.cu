@@ -818,16 +818,18 @@ __global__ void __launch_bounds__(TX * TY, 1024 / (TX * TY)) mx_p2g_grid_kernel(
     if (me < (TX - 1) * (TY - 1)) {
         const int i = tx * (TX - 1) + me % (TX - 1), j = ty * (TY - 1) + me / (TX - 1);
         if (i < M.g.Nx && j < M.g.Ny) {
+            // the node's elements lie in the tile (local column and row
+            // nx or nx + 1, ny or ny + 1); one outside the grid has no
+            // particles, so the count test alone skips it
+            const int nx = me % (TX - 1), ny = me / (TX - 1);
             int off[4];
 #pragma unroll
             for (int c = 0; c < 4; c++) {
-                const int ci = ((i & 1) == (c & 1)) ? i : i - 1;
-                const int cj = ((j & 1) == (c >> 1)) ? j : j - 1;
-                off[c] = -1;
-                if (ci < 0 || cj < 0 || ci >= M.g.Ex || cj >= M.g.Ey) continue;
-                const int le = (cj - ty * (TY - 1) + 1) * TX + (ci - tx * (TX - 1) + 1);
-                const int a = (ci == i) ? ((cj == j) ? 0 : 3) : ((cj == j) ? 1 : 2);
-                if (sh_off[le + 1] != sh_off[le]) off[c] = (a * 5) * SS + le;
+                const int dx = ((i & 1) == (c & 1)) ? 1 : 0;
+                const int dy = ((j & 1) == (c >> 1)) ? 1 : 0;
+                const int le = (ny + dy) * TX + nx + dx;
+                const int a = dx ? (dy ? 0 : 3) : (dy ? 1 : 2);
+                off[c] = sh_off[le + 1] != sh_off[le] ? (a * 5) * SS + le : -1;
             }
             node_finish<F64NODE>(M, sp->t + M.dt, tol, i, j, j * M.g.Nx + i, sh_sum, off, SS, node_mass, node4,
                                  node_mx, node_my, node_fx, node_fy, node_m64);
