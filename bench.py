@@ -80,9 +80,9 @@ FP64_BYTES = {
 
 # DRAM bytes (read + write) of one mx_g2p_kernel launch on this workload from
 # one ncu capture (profiles/ncu_mixed_step_box_fill_1M_g_local_mu2.md):
-# 80.8 MB read + 18.1 MB written; writes still in L2 at the kernel's end are
+# 80.8 MB read + 17.0 MB written; writes still in L2 at the kernel's end are
 # not in the figure.
-G2P_TRAFFIC_BYTES = 98.9e6
+G2P_TRAFFIC_BYTES = 97.8e6
 
 
 def phase_bytes(table, phase, n, ne, nn):
