@@ -73,18 +73,21 @@ struct MatF {
     float inv_A2d2;        // 1 / (A^2 d^2), the nonlocal cooperativity scale (g_nonlocal_mu2)
 };
 
-// isolin (isolin.c:75-116) in FP32.
+// isolin (isolin.c:75-116) in FP32.  Every rounding is spelled out (explicit
+// FMAs), so each instantiation of the G2P (single simulation or batch)
+// evaluates the law to the same bits; left to the compiler, a sum of two
+// products can be contracted either way round.
 __device__ __forceinline__ void isolin_f(const MatF &p, float exx, float exy, float eyy, float wxy,
                                          float &sxx, float &sxy, float &syy)
 {
-    float trD = exx + eyy;
-    float twoG = 2.0f * p.G;
-    float dsjxx = p.lambda * trD + twoG * exx + 2.0f * wxy * sxy;
-    float dsjxy = twoG * exy - wxy * (sxx - syy);
-    float dsjyy = p.lambda * trD + twoG * eyy - 2.0f * wxy * sxy;
-    sxx += p.dt * dsjxx;
-    sxy += p.dt * dsjxy;
-    syy += p.dt * dsjyy;
+    const float trD = __fadd_rn(exx, eyy);
+    const float twoG = 2.0f * p.G, twoW = 2.0f * wxy;
+    const float dsjxx = __fmaf_rn(twoW, sxy, __fmaf_rn(p.lambda, trD, __fmul_rn(twoG, exx)));
+    const float dsjxy = __fmaf_rn(-wxy, __fsub_rn(sxx, syy), __fmul_rn(twoG, exy));
+    const float dsjyy = __fmaf_rn(-twoW, sxy, __fmaf_rn(p.lambda, trD, __fmul_rn(twoG, eyy)));
+    sxx = __fmaf_rn(p.dt, dsjxx, sxx);
+    sxy = __fmaf_rn(p.dt, dsjxy, sxy);
+    syy = __fmaf_rn(p.dt, dsjyy, syy);
 }
 
 // dp_ri_mt (dp_ri_mt.c:99-200) in FP32; szz travels where g_local_mu2 keeps
@@ -93,34 +96,39 @@ __device__ __forceinline__ void dp_ri_mt_f(const MatF &p, float m, float v, floa
                                            float eyy, float wxy, float &sxx, float &sxy, float &syy,
                                            float &szz, float &gp, float &gdp)
 {
-    const float twoG = 2.0f * p.G, dt = p.dt;
-    const float trD = exx + eyy;
-    const float lt = p.lambda * trD;
-    const float sxx_tr = sxx + dt * (lt + twoG * exx + 2.0f * wxy * sxy);
-    const float sxy_tr = sxy + dt * (twoG * exy - wxy * (sxx - syy));
-    const float syy_tr = syy + dt * (lt + twoG * eyy - 2.0f * wxy * sxy);
-    const float szz_tr = szz + dt * lt;
-    const float p_tr = -(sxx_tr + syy_tr + szz_tr) * (1.0f / 3.0f);
-    const float t0xx = sxx_tr + p_tr, t0xy = sxy_tr, t0yy = syy_tr + p_tr, t0zz = szz_tr + p_tr;
-    const float tau_tr = sqrtf(0.5f * (t0xx * t0xx + 2.0f * t0xy * t0xy + t0yy * t0yy + t0zz * t0zz));
+    const float twoG = 2.0f * p.G, dt = p.dt, twoW = 2.0f * wxy;
+    const float trD = __fadd_rn(exx, eyy);
+    const float lt = __fmul_rn(p.lambda, trD);
+    const float sxx_tr = __fmaf_rn(dt, __fmaf_rn(twoW, sxy, __fmaf_rn(twoG, exx, lt)), sxx);
+    const float sxy_tr = __fmaf_rn(dt, __fmaf_rn(-wxy, __fsub_rn(sxx, syy), __fmul_rn(twoG, exy)), sxy);
+    const float syy_tr = __fmaf_rn(dt, __fmaf_rn(-twoW, sxy, __fmaf_rn(twoG, eyy, lt)), syy);
+    const float szz_tr = __fmaf_rn(dt, lt, szz);
+    const float p_tr = __fmul_rn(-__fadd_rn(__fadd_rn(sxx_tr, syy_tr), szz_tr), 1.0f / 3.0f);
+    const float t0xx = __fadd_rn(sxx_tr, p_tr), t0xy = sxy_tr, t0yy = __fadd_rn(syy_tr, p_tr);
+    const float t0zz = __fadd_rn(szz_tr, p_tr);
+    float q = __fmul_rn(t0xx, t0xx);
+    q = __fmaf_rn(2.0f * t0xy, t0xy, q);
+    q = __fmaf_rn(t0yy, t0yy, q);
+    q = __fmaf_rn(t0zz, t0zz, q);
+    const float tau_tr = sqrtf(0.5f * q);
     float nup = 0.0f;
-    if (m < p.rho_critical * v || p_tr <= 0.0f) {
-        nup = tau_tr * p.inv_G_dt;
+    if (m < __fmul_rn(p.rho_critical, v) || p_tr <= 0.0f) {
+        nup = __fmul_rn(tau_tr, p.inv_G_dt);
         sxx = sxy = syy = szz = 0.0f;
     } else if (p_tr > 0.0f) {
-        const float S0 = p.mu_s * p_tr;
+        const float S0 = __fmul_rn(p.mu_s, p_tr);
         float tau_tau = tau_tr, scale = 1.0f;
         if (tau_tr > S0) {
             tau_tau = S0;
             scale = __fdividef(S0, tau_tr);
         }
-        nup = (tau_tr - tau_tau) * p.inv_G_dt;
-        sxx = scale * t0xx - p_tr;
-        sxy = scale * t0xy;
-        syy = scale * t0yy - p_tr;
-        szz = scale * t0zz - p_tr;
+        nup = __fmul_rn(__fsub_rn(tau_tr, tau_tau), p.inv_G_dt);
+        sxx = __fmaf_rn(scale, t0xx, -p_tr);
+        sxy = __fmul_rn(scale, t0xy);
+        syy = __fmaf_rn(scale, t0yy, -p_tr);
+        szz = __fmaf_rn(scale, t0zz, -p_tr);
     }
-    gp += nup * dt;
+    gp = __fmaf_rn(nup, dt, gp);
     gdp = nup;
 }
 
@@ -132,46 +140,51 @@ __device__ __forceinline__ void g_local_mu2_f(const MatF &p, float m, float v, f
 {
     const float G = p.G, dt = p.dt;
     const float twoG = 2.0f * G;
-    const float trD = exx + eyy;
-    const float lt = p.lambda * trD;
+    const float trD = __fadd_rn(exx, eyy);
+    const float lt = __fmul_rn(p.lambda, trD);
     // Jaumann terms W T - T W with W_xy = wxy
-    const float JSxx = 2.0f * wxy * Txy;
-    const float JSxy = wxy * (Tyy - Txx);
-    const float JSyy = -2.0f * wxy * Txy;
-    const float Txx_tr = (exx * twoG + lt + JSxx) * dt + Txx;
-    const float Txy_tr = (exy * twoG + JSxy) * dt + Txy;
-    const float Tyy_tr = (eyy * twoG + lt + JSyy) * dt + Tyy;
-    const float Tzz_tr = lt * dt + Tzz;
-    const float pm = (Txx_tr + Tyy_tr + Tzz_tr) * (1.0f / 3.0f);
-    const float T0xx = Txx_tr - pm, T0yy = Tyy_tr - pm, T0zz = Tzz_tr - pm, T0xy = Txy_tr;
-    const float tau_tr = sqrtf(0.5f * (T0xx * T0xx + 2.0f * T0xy * T0xy + T0yy * T0yy + T0zz * T0zz));
+    const float JSxx = __fmul_rn(2.0f * wxy, Txy);
+    const float JSxy = __fmul_rn(wxy, __fsub_rn(Tyy, Txx));
+    const float JSyy = -JSxx;
+    const float Txx_tr = __fmaf_rn(__fadd_rn(__fmaf_rn(exx, twoG, lt), JSxx), dt, Txx);
+    const float Txy_tr = __fmaf_rn(__fmaf_rn(exy, twoG, JSxy), dt, Txy);
+    const float Tyy_tr = __fmaf_rn(__fadd_rn(__fmaf_rn(eyy, twoG, lt), JSyy), dt, Tyy);
+    const float Tzz_tr = __fmaf_rn(lt, dt, Tzz);
+    const float pm = __fmul_rn(__fadd_rn(__fadd_rn(Txx_tr, Tyy_tr), Tzz_tr), 1.0f / 3.0f);
+    const float T0xx = __fsub_rn(Txx_tr, pm), T0yy = __fsub_rn(Tyy_tr, pm), T0zz = __fsub_rn(Tzz_tr, pm);
+    const float T0xy = Txy_tr;
+    float q = __fmul_rn(T0xx, T0xx);
+    q = __fmaf_rn(2.0f * T0xy, T0xy, q);
+    q = __fmaf_rn(T0yy, T0yy, q);
+    q = __fmaf_rn(T0zz, T0zz, q);
+    const float tau_tr = sqrtf(0.5f * q);
     const float p_tr = -pm;
     float nup = 0.0f;
     // m / v < rho_critical with v > 0; the divisions of the reference become
     // products with the host-formed reciprocals, and the two that remain use
     // the fast FP32 divide (about 2 ulp), all well inside the mixed form's
-    // FP32 rounding budget
-    if (m < p.rho_critical * v || p_tr <= 0.0f) {
+    // FP32 rounding budget.  Every rounding is spelled out, as in isolin_f.
+    if (m < __fmul_rn(p.rho_critical, v) || p_tr <= 0.0f) {
         Txx = Txy = Tyy = Tzz = 0.0f;
     } else if (p_tr > 0.0f) {
-        const float S0 = p.mu_s * p_tr;
+        const float S0 = __fmul_rn(p.mu_s, p_tr);
         float tau_tau = tau_tr, scale = 1.0f;
         if (tau_tr > S0) {
-            const float S2 = p.mu_2 * p_tr;
-            const float alpha = p.alpha_coef * sqrtf(p_tr * p.inv_grains_rho);
-            const float B = -(S2 + tau_tr + alpha);
-            const float H = S2 * tau_tr + S0 * alpha;
-            const float disc = sqrtf(B * B - 4.0f * H);
-            tau_tau = (B > 0.0f) ? (-B - disc) * 0.5f : __fdividef(2.0f * H, -B + disc);
+            const float S2 = __fmul_rn(p.mu_2, p_tr);
+            const float alpha = __fmul_rn(p.alpha_coef, sqrtf(__fmul_rn(p_tr, p.inv_grains_rho)));
+            const float B = -__fadd_rn(__fadd_rn(S2, tau_tr), alpha);
+            const float H = __fmaf_rn(S2, tau_tr, __fmul_rn(S0, alpha));
+            const float disc = sqrtf(__fmaf_rn(B, B, -4.0f * H));
+            tau_tau = (B > 0.0f) ? __fmul_rn(__fsub_rn(-B, disc), 0.5f) : __fdividef(2.0f * H, __fadd_rn(-B, disc));
             scale = __fdividef(tau_tau, tau_tr);
         }
-        nup = (tau_tr - tau_tau) * p.inv_G_dt;
-        Txx = T0xx * scale - p_tr;
-        Txy = T0xy * scale;
-        Tyy = T0yy * scale - p_tr;
-        Tzz = T0zz * scale - p_tr;
+        nup = __fmul_rn(__fsub_rn(tau_tr, tau_tau), p.inv_G_dt);
+        Txx = __fmaf_rn(T0xx, scale, -p_tr);
+        Txy = __fmul_rn(T0xy, scale);
+        Tyy = __fmaf_rn(T0yy, scale, -p_tr);
+        Tzz = __fmaf_rn(T0zz, scale, -p_tr);
     }
-    gp += nup * dt;
+    gp = __fmaf_rn(nup, dt, gp);
     gdp = nup;
 }
 
@@ -344,13 +357,15 @@ __device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, flo
     const float gy[4] = {-ox * ih, -xl * ih, xl * ih, ox * ih};
     const float pmx = a4.z * m, pmy = a4.w * m, pby = grav * m;
     const float s0 = -b4.z * vol, s1 = -b4.w * vol, s2 = -syy * vol;
+    // every rounding spelled out, so that the batched and the fused kernels
+    // (separate inlined copies) sum to the same bits
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-        acc[a][0] += s[a] * m;
-        acc[a][1] += s[a] * pmx;
-        acc[a][2] += s[a] * pmy;
-        acc[a][3] += gx[a] * s0 + gy[a] * s1;
-        acc[a][4] += s[a] * pby + gx[a] * s1 + gy[a] * s2;
+        acc[a][0] = __fmaf_rn(s[a], m, acc[a][0]);
+        acc[a][1] = __fmaf_rn(s[a], pmx, acc[a][1]);
+        acc[a][2] = __fmaf_rn(s[a], pmy, acc[a][2]);
+        acc[a][3] = __fadd_rn(acc[a][3], __fmaf_rn(gy[a], s1, __fmul_rn(gx[a], s0)));
+        acc[a][4] = __fadd_rn(acc[a][4], __fmaf_rn(gy[a], s2, __fmaf_rn(gx[a], s1, __fmul_rn(s[a], pby))));
     }
 }
 

@@ -6,7 +6,9 @@ Each member of a batch must reproduce, bit for bit, the same simulation run on
 its own: the batch concatenates the members' particles, elements and nodes,
 and every per-particle, per-element and per-node operation and its order are
 those of the single run (the members' storage orders differ only by a
-constant offset).
+constant offset).  A single simulation sums P2G and grid update in one
+tiled kernel (mx_p2g_grid_kernel) while a batch runs them as two kernels, so
+the equality also checks the fused kernel against the unfused pair.
 """
 import numpy as np
 import pytest
@@ -114,4 +116,49 @@ def test_batch_dp_ri_mt_members_equal_single_runs():
         for f in ("x", "y", "vx", "vy", "sxx", "sxy", "syy", "state1", "state9", "state10"):
             np.testing.assert_array_equal(batch.member_get(k, f), one.get(f), err_msg="member %d %s" % (k, f))
         one.close()
+
+
+def crowded_scene():
+    """The config-1 block plus two crowded elements.  Element (14, 14) holds
+    1500 particles, more than the fused kernel's 1024-particle stage, and lies
+    in four 16 x 16 element tiles (column and row 14 are each shared by two
+    tiles): its owner orders it into perm, the three others into their own
+    scratch orders.  Element (20, 3) gets 300 more particles inside the
+    block, so its tile is summed in several stage passes."""
+    sc = scenes.config1(gravity=-9.81)
+    h = sc["h"]
+    p = sc["particles"]
+    rng = np.random.default_rng(11)
+    add = {k: [v] for k, v in p.items()}
+    for ei, ej, cnt in ((14, 14, 1500), (20, 3, 300)):
+        x = (ei + rng.uniform(0.05, 0.95, cnt)) * h
+        y = (ej + rng.uniform(0.05, 0.95, cnt)) * h
+        extra = {"m": np.full(cnt, p["m"][0]), "v": np.full(cnt, p["v"][0]), "x": x, "y": y}
+        for k in add:
+            add[k].append(extra.get(k, np.zeros(cnt)))
+    sc["particles"] = {k: np.concatenate(v) for k, v in add.items()}
+    return sc
+
+
+def test_crowded_elements_fused_equals_unfused():
+    sc = crowded_scene()
+    other = scenes.config1(seed=3)
+    batch = mpm2d.Batch([sc, other], precision="mixed")
+    batch.step(20)
+    one = mpm2d.Simulation(sc, precision="mixed")
+    one.step(20)
+    for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy"):
+        np.testing.assert_array_equal(batch.member_get(0, f), one.get(f), err_msg=f)
+    for f in ("node_m", "node_vx", "node_vy", "node_ax", "node_ay"):
+        np.testing.assert_array_equal(batch.member_get(0, f), one.get(f), err_msg=f)
+    # and the crowded run against the FP64 form (a wrong or missing particle
+    # in a sum would show as an O(1) error)
+    ref = mpm2d.Simulation(sc, precision="fp64")
+    ref.step(20)
+    for fs in (("x", "y"), ("vx", "vy")):
+        a = np.concatenate([one.get(f) for f in fs])
+        b = np.concatenate([ref.get(f) for f in fs])
+        assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b), fs
+    ref.close()
+    one.close()
 

@@ -7,7 +7,9 @@ Criteria (the mixed form's contract):
   * relative L2 error per field, ||a - b|| / ||b||, after 100 steps <= 1e-4;
   * silo discharge rate (minus the slope of the active mass over the steady
     window, the reference's examples/silo/write_active_mass.py measure) and
-    column runout (largest x of an active particle) within 1 %;
+    column runout (largest x of an active particle) within 1 %; for the
+    chaotic nonlocal silo, the median rate over eight perturbed fills within
+    5 %;
   * bit-identical repeat runs; permutation and mass invariants at 1 M.
 """
 import numpy as np
@@ -199,13 +201,14 @@ def test_mixed_nonlocal_vs_fp64_after_100_steps():
     assert np.linalg.norm(ga - gb) <= 1e-3 * np.linalg.norm(gb)
 
 
-def test_mixed_nonlocal_silo_discharge_within_fp64_spread():
-    # The nonlocal silo's discharge is chaotic at the FP64 level: 1e-9 m
-    # perturbations of the fill change the FP64 form's rate by several per
-    # cent (the nodal fluidity undershoots below zero near the outlet and
-    # the stress update p / (p + G dt gf) then swings).  The mixed form's
-    # rate must lie within the FP64 form's own spread over perturbed fills,
-    # widened by 1 %.
+def test_mixed_nonlocal_silo_discharge_median_within_5pct():
+    # The nonlocal silo's discharge is chaotic in both forms: fills perturbed
+    # by 1e-9 m give FP64 rates from about 300 to 500 (the nodal fluidity
+    # undershoots below zero near the outlet and the stress update
+    # p / (p + G dt gf) then swings), and a one-ulp change in the mixed
+    # form's sums moves a single run as far.  One run therefore says little;
+    # the medians over eight perturbed fills must agree within 5 %, which a
+    # consistent bias (FP32 material arithmetic once gave +8 %) would break.
     def silo(seed):
         sc = scenes.silo(cells=32, material="g_nonlocal_mu2", props=(1e6, 0.3), dt=1e-4, hole_radius=0.12,
                          open_time=0.05, wall_frac=0.5, fill_height=0.5, mp={"grains_d": 5.3e-4})
@@ -214,13 +217,18 @@ def test_mixed_nonlocal_silo_discharge_within_fp64_spread():
             sc["particles"]["x"] = sc["particles"]["x"] + 1e-9 * rng.uniform(-1, 1, size=sc["particles"]["x"].shape)
         return sc
 
-    sc = silo(None)
-    m = sc["particles"]["m"]
-    qf = [discharge_rate(active_mass_history(mpm2d.Simulation(silo(sd), precision="fp64"), m, 3000, 50))
-          for sd in (None, 0, 2)]
-    qm = discharge_rate(active_mass_history(mpm2d.Simulation(sc, precision="mixed"), m, 3000, 50))
-    assert min(qf) > 0
-    assert 0.99 * min(qf) <= qm <= 1.01 * max(qf), (qm, qf)
+    m = silo(None)["particles"]["m"]
+    seeds = (None, 0, 2, 5, 7, 11, 13, 17)
+    q = {}
+    for precision in ("fp64", "mixed"):
+        q[precision] = []
+        for sd in seeds:
+            sim = mpm2d.Simulation(silo(sd), precision=precision)
+            q[precision].append(discharge_rate(active_mass_history(sim, m, 3000, 50)))
+            sim.close()
+    qf, qm = np.median(q["fp64"]), np.median(q["mixed"])
+    assert min(q["fp64"]) > 0 and min(q["mixed"]) > 0
+    assert abs(qm - qf) <= 0.05 * qf, q
 
 
 def test_mixed_deterministic():
