@@ -107,30 +107,36 @@ struct SolveArgs {
     StepParams *sp;
 };
 
-// Block-wide sum of up to three values, fixed tree; result valid in thread 0.
+// Block-wide sum of up to three values in a fixed order; result valid in
+// thread 0.  One warp adds: lane l sums the values of threads l, l + 32, ...
+// then the lanes combine in a shuffle tree.  (GB300 issues FP64 at 1/64 of
+// the FP32 rate, so the reduction keeps its FP64 adds to one warp rather
+// than a tree in every warp.)
 __device__ __forceinline__ void block_sum3(double &a, double &b, double &c)
 {
-    __shared__ double sh[3][kSolveThreads / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, off);
-        b += __shfl_down_sync(0xffffffffu, b, off);
-        c += __shfl_down_sync(0xffffffffu, c, off);
-    }
-    if (lane == 0) {
-        sh[0][w] = a;
-        sh[1][w] = b;
-        sh[2][w] = c;
-    }
+    __shared__ double sh[3][kSolveThreads];
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    sh[2][threadIdx.x] = c;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        a = 0; b = 0; c = 0;
-        for (int k = 0; k < kSolveThreads / 32; k++) {
-            a += sh[0][k];
-            b += sh[1][k];
-            c += sh[2][k];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double x = sh[0][lane], y = sh[1][lane], z = sh[2][lane];
+#pragma unroll
+        for (int k = 1; k < kSolveThreads / 32; k++) {
+            x += sh[0][lane + 32 * k];
+            y += sh[1][lane + 32 * k];
+            z += sh[2][lane + 32 * k];
         }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, off);
+            y += __shfl_down_sync(0xffffffffu, y, off);
+            z += __shfl_down_sync(0xffffffffu, z, off);
+        }
+        a = x;
+        b = y;
+        c = z;
     }
     __syncthreads();
 }
@@ -159,42 +165,31 @@ __device__ __forceinline__ double grid_total(const double *partials, int slot, i
     return out;
 }
 
-// Slots a, b, c of the per-block partials summed in one pass, each in the
-// same fixed order as grid_total; every block gets the same three values.
+// Slots a, b, c of the per-block partials summed in one pass by one warp
+// (lane l takes partials l, l + 32, ..., then a shuffle tree): the same fixed
+// order in every block, so every block gets the same three values.
 __device__ __forceinline__ void grid_total3(const double *partials, int a, int b, int c, int nblocks, double &ta,
                                             double &tb, double &tc)
 {
-    __shared__ double sh[3][kSolveThreads / 32];
     __shared__ double res[3];
-    double x = 0, y = 0, z = 0;
-    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
-        x += __ldcg(partials + (size_t)a * nblocks + k);
-        y += __ldcg(partials + (size_t)b * nblocks + k);
-        z += __ldcg(partials + (size_t)c * nblocks + k);
-    }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        x += __shfl_down_sync(0xffffffffu, x, off);
-        y += __shfl_down_sync(0xffffffffu, y, off);
-        z += __shfl_down_sync(0xffffffffu, z, off);
-    }
-    if (lane == 0) {
-        sh[0][w] = x;
-        sh[1][w] = y;
-        sh[2][w] = z;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s0 = 0, s1 = 0, s2 = 0;
-        for (int k = 0; k < kSolveThreads / 32; k++) {
-            s0 += sh[0][k];
-            s1 += sh[1][k];
-            s2 += sh[2][k];
+    if (threadIdx.x < 32) {
+        double x = 0, y = 0, z = 0;
+        for (int k = threadIdx.x; k < nblocks; k += 32) {
+            x += __ldcg(partials + (size_t)a * nblocks + k);
+            y += __ldcg(partials + (size_t)b * nblocks + k);
+            z += __ldcg(partials + (size_t)c * nblocks + k);
         }
-        res[0] = s0;
-        res[1] = s1;
-        res[2] = s2;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, off);
+            y += __shfl_down_sync(0xffffffffu, y, off);
+            z += __shfl_down_sync(0xffffffffu, z, off);
+        }
+        if (threadIdx.x == 0) {
+            res[0] = x;
+            res[1] = y;
+            res[2] = z;
+        }
     }
     __syncthreads();
     ta = res[0];
@@ -265,7 +260,7 @@ __device__ __forceinline__ double apply_stencil(const SolveArgs &S, int n, int i
 //   p = u + beta p;  s = w + beta s;  x += alpha p;  r -= alpha s
 //   u = D^-1 r;  w = A u;  gamma' = <r, u>;  delta = <w, u>
 //   beta = gamma' / gamma;  alpha = gamma' / (delta - beta gamma' / alpha)
-__global__ void __launch_bounds__(kSolveThreads) pcg_kernel(SolveArgs S)
+__global__ void __launch_bounds__(kSolveThreads, 2) pcg_kernel(SolveArgs S)
 {
     const int nn = S.Nx * S.Ny;
     const int nblocks = gridDim.x;
