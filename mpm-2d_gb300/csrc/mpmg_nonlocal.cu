@@ -348,6 +348,8 @@ __global__ void __launch_bounds__(kSolveThreads, 2) pcg_kernel(SolveArgs S)
         converged = true;
     }
     double alpha = gamma / delta, beta = 0;
+    __shared__ double sh_scalar[2];
+    __shared__ int sh_next;
     while (!converged && it < S.maxit) {
         // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s (own nodes)
         for (int n = tid; n < nn; n += stride) {
@@ -383,13 +385,36 @@ __global__ void __launch_bounds__(kSolveThreads, 2) pcg_kernel(SolveArgs S)
         if (!mpmg_grid_barrier(S.barrier, nblocks, S.status, kSpinLimit)) return;
         grid_total3(S.partials, 0, 1, 3, nblocks, gn, dl, rr);
         it++;
-        if (!(rr == rr)) break;   // NaN: give up
-        converged = (rr <= target);
-        if (converged) break;
-        beta = gn / gamma;
-        const double eta = dl - beta * gn / alpha;
-        if (!(eta > 0)) break;    // breakdown of the recurrence: report non-convergence
-        alpha = gn / eta;
+        // The recurrence's scalars, formed by one thread and shared through
+        // shared memory (three FP64 divisions, which every warp would
+        // otherwise issue); the next writes come after the next grid barrier.
+        if (threadIdx.x == 0) {
+            int next = 0;                        // 0: go on, 1: give up, 2: converged
+            if (!(rr == rr)) {
+                next = 1;                        // NaN
+            } else if (rr <= target) {
+                next = 2;
+            } else {
+                const double beta_n = gn / gamma;
+                const double eta = dl - beta_n * gn / alpha;
+                if (!(eta > 0)) {
+                    next = 1;                    // breakdown of the recurrence: report non-convergence
+                } else {
+                    sh_scalar[0] = beta_n;
+                    sh_scalar[1] = gn / eta;
+                }
+            }
+            sh_next = next;
+        }
+        __syncthreads();
+        const int next = sh_next;
+        if (next == 1) break;
+        if (next == 2) {
+            converged = true;
+            break;
+        }
+        beta = sh_scalar[0];
+        alpha = sh_scalar[1];
         gamma = gn;
     }
     if (tid == 0) {
