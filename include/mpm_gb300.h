@@ -275,11 +275,16 @@ MPMG_API int mpmg_batch_get_time(mpmg_ctx *ctx, int member, double *t, int *step
    P2G.  The context is left at the taped run's final state.  The element of
    each particle and the branches of the material law are held fixed within
    a step.  mpmg_adj_state then reads the adjoint of a field of the run's
-   initial state: x y vx vy v sxx sxy syy Tzz.  FP64 form, isolin or
-   g_local_mu2, one simulation. */
+   initial state: x y vx vy v sxx sxy syy Tzz.  FP64 form, isolin,
+   g_local_mu2 or g_nonlocal_mu2 (its fluidity solve reversed by a solve of
+   the same symmetric system for the fluidity's adjoint), one simulation. */
 MPMG_API int mpmg_adj_forward_tape(mpmg_ctx *ctx, int nsteps, int checkpoint_every);
 MPMG_API int mpmg_adj_backward(mpmg_ctx *ctx, const double *dl_dx, const double *dl_dy, double *dl_dtheta);
 MPMG_API int mpmg_adj_state(mpmg_ctx *ctx, const char *name, double *host_out);
+/* One parameter's gradient from the last mpmg_adj_backward: index 0 mu_s,
+   1 mu_2, 2 I0, 3 E (the four dl_dtheta holds), 4 the nonlocal amplitude A
+   of g_nonlocal_mu2 (zero for the local materials). */
+MPMG_API int mpmg_adj_gradient(mpmg_ctx *ctx, int index, double *out);
 
 /* Runs only the material update on every active particle from the current
    strain rates (the per-particle path of the reference's tests/test_material.c).

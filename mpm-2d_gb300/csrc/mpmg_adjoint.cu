@@ -49,11 +49,12 @@ constexpr int kStateFields = 9;     // x y vx vy v sxx sxy syy Tzz
 constexpr int kNodeFields = 5;      // m ax ay vx vy
 
 // Parameter adjoint slots (mpmg_adj_backward's dtheta).
-enum { TH_MU_S = 0, TH_MU_2 = 1, TH_I0 = 2, TH_E = 3, TH_COUNT = 4 };
+enum { TH_MU_S = 0, TH_MU_2 = 1, TH_I0 = 2, TH_E = 3, TH_COUNT = 4, TH_A = 4, TH_ALL = 5 };
 
 struct MatParams {
     double G, K, lambda, dt, nu;
     double mu_s, mu_2, I0, grains_rho, grains_d, rho_critical;
+    double A;               // nonlocal amplitude (g_nonlocal_mu2)
 };
 
 // ---------------------------------------------------------------------------
@@ -65,7 +66,7 @@ struct MatParams {
 
 struct MatAdj {
     double exx, exy, eyy, wxy;
-    double G, K, lambda, mu_s, mu_2, I0;
+    double G, K, lambda, mu_s, mu_2, I0, A;
 };
 
 // isolin.c:75-116: s' = s + dt (lambda trD I + 2G D + W s - s W).
@@ -188,6 +189,154 @@ __device__ void g_local_mu2_adj(const MatParams &p, double m, double v, double e
     Tb[3] = bzz;
 }
 
+// Upper-triangle index of (a, b), a <= b, in an element's 10-entry symmetric
+// block (the layout of the fluidity assembly).
+__device__ __forceinline__ int sym10(int a, int b)
+{
+    const int row_start[4] = {0, 4, 7, 9};
+    return row_start[a] + (b - a);
+}
+
+// g_nonlocal_mu2 reversed for one particle: the stress update after the
+// fluidity solve (g_nonlocal_mu2.c:160-218), the bulk fluidity
+// (calculate_bulk_granular_fluidity, :238-321) and the particle's share of
+// the assembled system (:418-507: K_ab += v (xi^-2 N_a N_b + grad N_a .
+// grad N_b), f_a += v gf_local xi^-2 N_a over dense particles).  gf is the
+// fluidity interpolated at the particle; kb and fb are the adjoints of its
+// element's block and right-hand side.  Returns, besides Tb and a as
+// g_local_mu2_adj does, the adjoint of the updated volume (vb) and adds the
+// adjoints of the shape values and gradients to sb, gxb, gyb.  (The
+// adjoint of gf itself is formed by adj_nl_pre_kernel.)
+__device__ void g_nonlocal_mu2_adj(const MatParams &p, double m, double v, double exx, double exy, double eyy,
+                                   double wxy, double Txx, double Txy, double Tyy, const ShapeFns &f, double gf,
+                                   const double kb[10], const double fb[4], double Tb[4], MatAdj &a, double &vb,
+                                   double sb[4], double gxb[4], double gyb[4])
+{
+    const double G = p.G, dt = p.dt, lambda = p.K - 2.0 * G / 3.0;
+    const double trD = exx + eyy;
+    const double sxx_tr = Txx + dt * (lambda * trD + 2.0 * G * exx + 2.0 * wxy * Txy);
+    const double sxy_tr = Txy + dt * (2.0 * G * exy - wxy * (Txx - Tyy));
+    const double syy_tr = Tyy + dt * (lambda * trD + 2.0 * G * eyy - 2.0 * wxy * Txy);
+    const double pr = -0.5 * (sxx_tr + syy_tr);
+    const double t0xx = sxx_tr + pr, t0xy = sxy_tr, t0yy = syy_tr + pr;
+    const double tau = sqrt(0.5 * (t0xx * t0xx + 2.0 * t0xy * t0xy + t0yy * t0yy));
+    const bool dense = !(m / v < p.rho_critical || pr < 0);
+    double t0xxb = 0, t0xyb = 0, t0yyb = 0, prb = 0, taub = 0;
+    vb = 0;
+    if (dense && pr > 0) {
+        // stress update: s = pr / (G dt gf + pr), T' = s t0 - pr I
+        const double den = G * dt * gf + pr;
+        const double sc = pr / den;
+        const double sbar = Tb[0] * t0xx + Tb[1] * t0xy + Tb[2] * t0yy;
+        t0xxb += sc * Tb[0];
+        t0xyb += sc * Tb[1];
+        t0yyb += sc * Tb[2];
+        prb -= Tb[0] + Tb[2];
+        prb += sbar * (G * dt * gf) / (den * den);
+        a.G -= sbar * pr * dt * gf / (den * den);
+
+        // bulk fluidity: tau' from the mu(I) return (tau itself below yield)
+        const double S0 = p.mu_s * pr;
+        const bool plastic = tau > S0;
+        double taup = tau, dB = 0, dH = 0, S2 = 0, alpha = 0, sq = 0, ca = 0;
+        if (plastic) {
+            S2 = p.mu_2 * pr;
+            sq = sqrt(pr / p.grains_rho);
+            ca = G * p.I0 * dt / p.grains_d;
+            alpha = ca * sq;
+            const double B = -(S2 + tau + alpha);
+            const double H = S2 * tau + S0 * alpha;
+            const double disc = sqrt(B * B - 4.0 * H);
+            if (B > 0) {
+                taup = 0.5 * (-B - disc);
+                dB = 0.5 * (-1.0 - B / disc);
+                dH = 1.0 / disc;
+            } else {
+                const double q = -B + disc;
+                taup = 2.0 * H / q;
+                const double dqB = -1.0 + B / disc, dqH = -2.0 / disc;
+                dB = -2.0 * H / (q * q) * dqB;
+                dH = 2.0 / q - 2.0 * H / (q * q) * dqH;
+            }
+        }
+        const double gfl = plastic ? pr / (G * dt) * (tau / taup - 1.0) : 0.0;
+        const double D = p.A * p.A * p.grains_d * p.grains_d;
+        const double r = taup / pr - p.mu_s;
+        const double xisq = fabs(r) / D;
+
+        // the particle's share of the element block and right-hand side
+        double xisqb = 0, gflb = 0;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+#pragma unroll
+            for (int j = i; j < 4; j++) {
+                const double k = kb[sym10(i, j)];
+                vb += k * (xisq * f.s[i] * f.s[j] + f.gx[i] * f.gx[j] + f.gy[i] * f.gy[j]);
+                xisqb += k * v * f.s[i] * f.s[j];
+                sb[i] += k * v * xisq * f.s[j];
+                sb[j] += k * v * xisq * f.s[i];
+                gxb[i] += k * v * f.gx[j];
+                gxb[j] += k * v * f.gx[i];
+                gyb[i] += k * v * f.gy[j];
+                gyb[j] += k * v * f.gy[i];
+            }
+            vb += fb[i] * gfl * xisq * f.s[i];
+            gflb += fb[i] * v * xisq * f.s[i];
+            xisqb += fb[i] * v * gfl * f.s[i];
+            sb[i] += fb[i] * v * gfl * xisq;
+        }
+        // xi^-2 = |tau' / pr - mu_s| / (A^2 d^2)
+        const double rb = xisqb * (r >= 0 ? 1.0 : -1.0) / D;
+        a.A -= xisqb * 2.0 * xisq / p.A;
+        double taupb = rb / pr;
+        prb -= rb * taup / (pr * pr);
+        a.mu_s -= rb;
+        if (plastic) {
+            // gf_local = pr / (G dt) (tau / tau' - 1)
+            const double c = pr / (G * dt);
+            prb += gflb * (tau / taup - 1.0) / (G * dt);
+            a.G -= gflb * gfl / G;
+            taub += gflb * c / taup;
+            taupb -= gflb * c * tau / (taup * taup);
+            // the return's root reversed (as in g_local_mu2_adj)
+            const double Bb = taupb * dB, Hb = taupb * dH;
+            const double S2b = Hb * tau - Bb;
+            taub += Hb * S2 - Bb;
+            const double S0b = Hb * alpha;
+            const double alphab = Hb * S0 - Bb;
+            prb += alphab * ca * 0.5 / (sq * p.grains_rho);
+            const double cab = alphab * sq;
+            a.G += cab * p.I0 * dt / p.grains_d;
+            a.I0 += cab * G * dt / p.grains_d;
+            a.mu_2 += S2b * pr;
+            prb += S2b * p.mu_2;
+            a.mu_s += S0b * pr;
+            prb += S0b * p.mu_s;
+        } else {
+            taub += taupb;
+        }
+    }
+    // tau = sqrt((t0xx^2 + 2 t0xy^2 + t0yy^2) / 2)
+    if (tau > 0) {
+        t0xxb += taub * t0xx / (2.0 * tau);
+        t0xyb += taub * t0xy / tau;
+        t0yyb += taub * t0yy / (2.0 * tau);
+    }
+    // t0 = T_trial + pr I (xx, yy), pr = -(T_trial,xx + T_trial,yy) / 2
+    const double P = prb + t0xxb + t0yyb;
+    const double bxx = t0xxb - 0.5 * P, byy = t0yyb - 0.5 * P, bxy = t0xyb;
+    // the trial Jaumann stress reversed, lambda = K - 2G/3
+    a.exx += dt * (lambda * (bxx + byy) + 2.0 * G * bxx);
+    a.eyy += dt * (lambda * (bxx + byy) + 2.0 * G * byy);
+    a.exy += dt * 2.0 * G * bxy;
+    a.wxy += dt * (2.0 * Txy * bxx - (Txx - Tyy) * bxy - 2.0 * Txy * byy);
+    a.lambda += dt * trD * (bxx + byy);
+    a.G += dt * 2.0 * (exx * bxx + exy * bxy + eyy * byy);
+    Tb[0] = bxx - dt * wxy * bxy;
+    Tb[2] = byy + dt * wxy * bxy;
+    Tb[1] = bxy + dt * 2.0 * wxy * (bxx - byy);
+}
+
 // Mixed second derivative of the shape functions, d2 N_a / dx dy (tent
 // products): +1, -1, +1, -1 over h^2 for BL, BR, TR, TL.
 __device__ __forceinline__ double shape_xy(int a, double inv_h)
@@ -218,9 +367,14 @@ struct AdjStep {
     double *cell_adj;           // 16 x ne, value-major
     double *node_adj;           // 5 x nn: pb_x, pb_y, fb_x, fb_y, mb
     double *theta_part;         // per adj_g2p block: TH_COUNT + (G, K, lambda) partials
+    // g_nonlocal_mu2
+    const double *gf_nodes;     // nn: the step's nodal fluidity (solution of the solve)
+    double *gfb;                // n: adjoint of the fluidity interpolated at each particle
+    double *rhs;                // 4 x ne: its gather to the nodes, as element corner sums
+    const double *lam;          // nn: adjoint of the nodal fluidity (the adjoint solve)
 };
 
-constexpr int kThetaSlots = 7;   // mu_s mu_2 I0 (direct) G K lambda, E folded later; slot 6 unused
+constexpr int kThetaSlots = 7;   // mu_s mu_2 I0 (direct) G K lambda, E folded later; A (nonlocal)
 
 __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(AdjStep S)
 {
@@ -275,15 +429,42 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(AdjStep S)
             // material
             double Tb[4] = {in[5], in[6], in[7], in[8]};
             MatAdj ma = {};
+            double vnl = 0, snl[4] = {0, 0, 0, 0}, gxnl[4] = {0, 0, 0, 0}, gynl[4] = {0, 0, 0, 0};
             if (S.material == MPMG_ISOLIN) {
                 isolin_adj(S.mp, exx, exy, eyy, wxy, Txx, Txy, Tyy, Tb, ma);
                 Tb[3] = in[8];      // isolin leaves Tzz alone
+            } else if (S.material == MPMG_G_NONLOCAL_MU2) {
+                // the element's nodal fluidity g and its adjoint lam: the block's
+                // adjoint is -(lam g^T) symmetrised, the right-hand side's lam
+                double gn[4], ln[4], gf = 0;
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    gn[a] = S.gf_nodes[nd[a]];
+                    ln[a] = S.lam[nd[a]];
+                    gf += gn[a] * f.s[a];
+                }
+                double kb[10], fb[4];
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    fb[a] = ln[a];
+#pragma unroll
+                    for (int b = a; b < 4; b++)
+                        kb[sym10(a, b)] = a == b ? -ln[a] * gn[a] : -(ln[a] * gn[b] + ln[b] * gn[a]);
+                }
+                g_nonlocal_mu2_adj(S.mp, S.mass[i], Vn, exx, exy, eyy, wxy, Txx, Txy, Tyy, f, gf, kb, fb, Tb, ma,
+                                   vnl, snl, gxnl, gynl);
+                // the fluidity gather gf = sum N_a g_a, shape values reversed
+                const double gfb = S.gfb[i];
+#pragma unroll
+                for (int a = 0; a < 4; a++) snl[a] += gfb * gn[a];
+                Tb[3] = in[8];      // plane stress state: Tzz is carried
             } else {
                 g_local_mu2_adj(S.mp, S.mass[i], Vn, exx, exy, eyy, wxy, Txx, Txy, Tyy, Tzz, Tb, ma);
             }
-            // volume V' = V exp(dt trD)
-            const double Vb = in[4] * ex;
-            const double trb = in[4] * Vn * dt;
+            // volume V' = V exp(dt trD) (the nonlocal assembly also reads V')
+            const double vnb = in[4] + vnl;
+            const double Vb = vnb * ex;
+            const double trb = vnb * Vn * dt;
             const double exxb = ma.exx + trb, eyyb = ma.eyy + trb;
             const double dxdyb = 0.5 * (ma.exy + ma.wxy), dydxb = 0.5 * (ma.exy - ma.wxy);
             // gathers
@@ -298,9 +479,9 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(AdjStep S)
                 S.contrib[(a * 4 + 1) * n + i] = uyb;
                 S.contrib[(a * 4 + 2) * n + i] = axb;
                 S.contrib[(a * 4 + 3) * n + i] = ayb;
-                sb[a] = dt * (ux[a] * in[0] + uy[a] * in[1] + ax[a] * in[2] + ay[a] * in[3]);
-                gxb[a] = exxb * ux[a] + dydxb * uy[a];
-                gyb[a] = eyyb * uy[a] + dxdyb * ux[a];
+                sb[a] = dt * (ux[a] * in[0] + uy[a] * in[1] + ax[a] * in[2] + ay[a] * in[3]) + snl[a];
+                gxb[a] = exxb * ux[a] + dydxb * uy[a] + gxnl[a];
+                gyb[a] = eyyb * uy[a] + dxdyb * ux[a] + gynl[a];
             }
             double xb = in[0], yb = in[1];
 #pragma unroll
@@ -324,6 +505,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(AdjStep S)
             th[3] = ma.G;
             th[4] = ma.K;
             th[5] = ma.lambda;
+            th[6] = ma.A;
         }
     }
     // block partials of the parameter adjoint (fixed tree order)
@@ -341,6 +523,79 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(AdjStep S)
         for (int q = 0; q < kAdjThreads / 32; q++) v += red[q][threadIdx.x];
         S.theta_part[(size_t)blockIdx.x * kThetaSlots + threadIdx.x] = v;
     }
+}
+
+// g_nonlocal_mu2, before adj_g2p: per particle, the adjoint of the fluidity
+// interpolated at it, through the stress update s = pr / (G dt gf + pr),
+// T' = s t0 - pr I (g_nonlocal_mu2.c:160-218).
+__global__ void __launch_bounds__(kAdjThreads) adj_nl_pre_kernel(AdjStep S)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.n) return;
+    const int e = S.elem[i];
+    double gfb = 0;
+    if (S.active[i] && e >= 0) {
+        const GridGeom &g = S.g;
+        const size_t n = (size_t)S.n, nn = (size_t)S.nn;
+        const double x = S.state[0 * n + i], y = S.state[1 * n + i], V = S.state[4 * n + i];
+        const double Txx = S.state[5 * n + i], Txy = S.state[6 * n + i], Tyy = S.state[7 * n + i];
+        const int ci = e % g.Ex, cj = e / g.Ex;
+        const int n0 = cj * g.Nx + ci;
+        const int nd[4] = {n0, n0 + 1, n0 + 1 + g.Nx, n0 + g.Nx};
+        const double xl = (x - ci * g.h) * g.inv_h, yl = (y - cj * g.h) * g.inv_h;
+        const ShapeFns f = fp64::shape(xl, yl, g.inv_h);
+        double exx = 0, eyy = 0, dxdy = 0, dydx = 0, gf = 0;
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const double ux = S.nodes[3 * nn + nd[a]], uy = S.nodes[4 * nn + nd[a]];
+            exx += f.gx[a] * ux;
+            eyy += f.gy[a] * uy;
+            dxdy += f.gy[a] * ux;
+            dydx += f.gx[a] * uy;
+            gf += S.gf_nodes[nd[a]] * f.s[a];
+        }
+        const MatParams &p = S.mp;
+        const double dt = S.dt, G = p.G, lambda = p.K - 2.0 * G / 3.0;
+        const double exy = 0.5 * (dxdy + dydx), wxy = 0.5 * (dxdy - dydx);
+        const double Vn = V * exp(dt * (exx + eyy));
+        const double trD = exx + eyy;
+        const double sxx_tr = Txx + dt * (lambda * trD + 2.0 * G * exx + 2.0 * wxy * Txy);
+        const double sxy_tr = Txy + dt * (2.0 * G * exy - wxy * (Txx - Tyy));
+        const double syy_tr = Tyy + dt * (lambda * trD + 2.0 * G * eyy - 2.0 * wxy * Txy);
+        const double pr = -0.5 * (sxx_tr + syy_tr);
+        const bool dense = !(S.mass[i] / Vn < p.rho_critical || pr < 0);
+        if (dense && pr > 0) {
+            const double den = G * dt * gf + pr;
+            const double sbar = S.adj_in[5 * n + i] * (sxx_tr + pr) + S.adj_in[6 * n + i] * sxy_tr +
+                                S.adj_in[7 * n + i] * (syy_tr + pr);
+            gfb = -sbar * pr * G * dt / (den * den);
+        }
+    }
+    S.gfb[i] = gfb;
+}
+
+// g_nonlocal_mu2: per element, the gather gf_p = sum N_a g_a reversed as
+// corner sums N_a gfb_p over the element's particles in the binned order
+// (the right-hand-side layout of the assembly, so that the solver sums the
+// corners to the nodes).
+__global__ void __launch_bounds__(128) adj_nl_rhs_kernel(AdjStep S)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= S.ne) return;
+    const GridGeom &g = S.g;
+    const size_t n = (size_t)S.n;
+    const int ci = e % g.Ex, cj = e / g.Ex;
+    double F[4] = {0, 0, 0, 0};
+    for (int k = S.cell_start[e]; k < S.cell_start[e + 1]; k++) {
+        const int i = (int)S.perm[k];
+        const double xl = (S.state[0 * n + i] - ci * g.h) * g.inv_h, yl = (S.state[1 * n + i] - cj * g.h) * g.inv_h;
+        const ShapeFns f = fp64::shape(xl, yl, g.inv_h);
+        const double gfb = S.gfb[i];
+#pragma unroll
+        for (int a = 0; a < 4; a++) F[a] += f.s[a] * gfb;
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++) S.rhs[(size_t)a * S.ne + e] = F[a];
 }
 
 // Per element: the corner shares of its particles, in the binned order.
@@ -570,10 +825,15 @@ struct AdjTape {
     int *seg_cs = nullptr;          // K x (ne + 1)
     double *seg_nodes = nullptr;    // K x kNodeFields x nn
     StepParams *seg_params = nullptr;   // K
+    // g_nonlocal_mu2: each recorded step's nodal fluidity and element blocks
+    double *seg_gf = nullptr;       // K x nn
+    double *seg_ek = nullptr;       // K x 10 x ne
     // reverse pass
     double *adj[2] = {nullptr, nullptr};   // kStateFields x n
     double *contrib = nullptr, *cell_adj = nullptr, *node_adj = nullptr;
     double *theta_part = nullptr, *theta_acc = nullptr;
+    double *gfb = nullptr, *rhs = nullptr, *lam = nullptr;   // g_nonlocal_mu2
+    double grad[TH_ALL] = {0, 0, 0, 0, 0};   // the last backward pass's parameter gradient
     int cur = 0;                    // adj[cur] holds the latest adjoint state
 };
 
@@ -584,7 +844,7 @@ void mpmg_adj_free(mpmg_ctx *ctx)
     void *ptrs[] = {t->ck_state, t->ck_active, t->ck_elem, t->ck_params, t->final_state, t->final_active,
                     t->final_elem, t->final_params, t->seg_state, t->seg_elem, t->seg_active, t->seg_perm,
                     t->seg_cs, t->seg_nodes, t->seg_params, t->adj[0], t->adj[1], t->contrib, t->cell_adj,
-                    t->node_adj, t->theta_part, t->theta_acc};
+                    t->node_adj, t->theta_part, t->theta_acc, t->seg_gf, t->seg_ek, t->gfb, t->rhs, t->lam};
     for (void *p : ptrs) cudaFree(p);
     delete t;
     ctx->adj = nullptr;
@@ -648,6 +908,7 @@ MatParams make_params(const mpmg_ctx *ctx)
     p.grains_rho = c.mp[MPMG_MP_GRAINS_RHO];
     p.grains_d = c.mp[MPMG_MP_GRAINS_D];
     p.rho_critical = c.mp[MPMG_MP_RHO_CRITICAL];
+    p.A = c.mp[MPMG_MP_A];
     return p;
 }
 
@@ -657,8 +918,9 @@ int check_adjoint_ctx(const mpmg_ctx *ctx)
         mpmg_set_error("the adjoint runs on the FP64 form of a single simulation");
         return MPMG_ERR_UNSUPPORTED;
     }
-    if (ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2) {
-        mpmg_set_error("the adjoint supports isolin and g_local_mu2");
+    if (ctx->cfg.material != MPMG_ISOLIN && ctx->cfg.material != MPMG_G_LOCAL_MU2 &&
+        ctx->cfg.material != MPMG_G_NONLOCAL_MU2) {
+        mpmg_set_error("the adjoint supports isolin, g_local_mu2 and g_nonlocal_mu2");
         return MPMG_ERR_UNSUPPORTED;
     }
     return MPMG_OK;
@@ -701,6 +963,13 @@ int mpmg_adj_forward_tape(mpmg_ctx *ctx, int nsteps, int checkpoint_every)
         (rc = dalloc(&t->cell_adj, 16 * ne)) != MPMG_OK || (rc = dalloc(&t->node_adj, 5 * nn)) != MPMG_OK ||
         (rc = dalloc(&t->theta_part, (size_t)blocks_for(n, kAdjThreads) * kThetaSlots)) != MPMG_OK ||
         (rc = dalloc(&t->theta_acc, kThetaSlots)) != MPMG_OK) {
+        mpmg_adj_free(ctx);
+        return rc;
+    }
+    if (ctx->cfg.material == MPMG_G_NONLOCAL_MU2 &&
+        ((rc = dalloc(&t->seg_gf, (size_t)K * nn)) != MPMG_OK ||
+         (rc = dalloc(&t->seg_ek, (size_t)K * 10 * ne)) != MPMG_OK || (rc = dalloc(&t->gfb, n)) != MPMG_OK ||
+         (rc = dalloc(&t->rhs, 4 * ne)) != MPMG_OK || (rc = dalloc(&t->lam, nn)) != MPMG_OK)) {
         mpmg_adj_free(ctx);
         return rc;
     }
@@ -752,6 +1021,10 @@ int mpmg_adj_backward(mpmg_ctx *ctx, const double *dl_dx, const double *dl_dy, d
     S.cell_adj = t->cell_adj;
     S.node_adj = t->node_adj;
     S.theta_part = t->theta_part;
+    S.gfb = t->gfb;
+    S.rhs = t->rhs;
+    S.lam = t->lam;
+    const bool nonlocal = ctx->cfg.material == MPMG_G_NONLOCAL_MU2;
     const int pblocks = blocks_for(n, kAdjThreads);
     int rc;
     for (int c = t->nck - 1; c >= 0; c--) {
@@ -770,6 +1043,12 @@ int mpmg_adj_backward(mpmg_ctx *ctx, const double *dl_dx, const double *dl_dy, d
                 t->seg_active + (size_t)k * n, t->seg_perm + (size_t)k * n, t->seg_cs + (size_t)k * (ne + 1),
                 t->seg_nodes + (size_t)k * kNodeFields * nn, t->seg_params + k);
             ctx->launches += 1;
+            if (nonlocal) {
+                MPMG_CHECK(cudaMemcpyAsync(t->seg_gf + (size_t)k * nn, ctx->node_gf, nn * sizeof(double),
+                                           cudaMemcpyDeviceToDevice, s));
+                MPMG_CHECK(cudaMemcpyAsync(t->seg_ek + (size_t)k * 10 * ne, ctx->elem_k, 10 * ne * sizeof(double),
+                                           cudaMemcpyDeviceToDevice, s));
+            }
         }
         // reverse the segment's steps
         for (int k = len - 1; k >= 0; k--) {
@@ -782,6 +1061,18 @@ int mpmg_adj_backward(mpmg_ctx *ctx, const double *dl_dx, const double *dl_dy, d
             S.params = t->seg_params + k;
             S.adj_in = t->adj[t->cur];
             S.adj_out = t->adj[1 - t->cur];
+            if (n > 0 && nonlocal) {
+                // the fluidity's adjoint: gathered to the nodes, then the same
+                // symmetric system solved for it (zero start, same tolerance)
+                S.gf_nodes = t->seg_gf + (size_t)k * nn;
+                adj_nl_pre_kernel<<<pblocks, kAdjThreads, 0, s>>>(S);
+                adj_nl_rhs_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(S);
+                ctx->launches += 2;
+                MPMG_CHECK(cudaGetLastError());
+                rc = mpmg_solve_fluidity_system(ctx, t->seg_ek + (size_t)k * 10 * ne, t->rhs, S.nodes, S.cell_start,
+                                                t->lam, true);
+                if (rc != MPMG_OK) return rc;
+            }
             if (n > 0) {
                 adj_g2p_kernel<<<pblocks, kAdjThreads, 0, s>>>(S);
                 adj_cells_kernel<<<blocks_for(ne, 128), 128, 0, s>>>(S);
@@ -804,11 +1095,23 @@ int mpmg_adj_backward(mpmg_ctx *ctx, const double *dl_dx, const double *dl_dy, d
     // lambda = K - 2 G / 3
     const double nu = ctx->cfg.mp[MPMG_MP_NU];
     const double dG = 1.0 / (2.0 * (1.0 + nu)), dK = 1.0 / (3.0 * (1.0 - 2.0 * nu));
-    dl_dtheta[TH_MU_S] = th[0];
-    dl_dtheta[TH_MU_2] = th[1];
-    dl_dtheta[TH_I0] = th[2];
-    dl_dtheta[TH_E] = th[3] * dG + th[4] * dK + th[5] * (dK - 2.0 / 3.0 * dG);
+    t->grad[TH_MU_S] = th[0];
+    t->grad[TH_MU_2] = th[1];
+    t->grad[TH_I0] = th[2];
+    t->grad[TH_E] = th[3] * dG + th[4] * dK + th[5] * (dK - 2.0 / 3.0 * dG);
+    t->grad[TH_A] = th[6];
+    for (int k = 0; k < TH_COUNT; k++) dl_dtheta[k] = t->grad[k];
     return mpmg_synchronize(ctx);
+}
+
+// One parameter's gradient from the last mpmg_adj_backward: 0 mu_s, 1 mu_2,
+// 2 I0, 3 E, 4 the nonlocal amplitude A (zero for the local materials).
+int mpmg_adj_gradient(mpmg_ctx *ctx, int index, double *out)
+{
+    if (ctx == nullptr || out == nullptr || index < 0 || index >= TH_ALL) return MPMG_ERR_INVALID;
+    if (ctx->adj == nullptr) return MPMG_ERR_INVALID;
+    *out = ctx->adj->grad[index];
+    return MPMG_OK;
 }
 
 // Adjoint of one field of the taped run's initial state (after

@@ -230,6 +230,8 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx);
 void mpmg_nonlocal_free(mpmg_ctx *ctx);
 int mpmg_launch_fluidity(mpmg_ctx *ctx);         // nonlocal: assembly, solve, stress
 int mpmg_launch_solve(mpmg_ctx *ctx);            // nonlocal: the fluidity PCG alone
+int mpmg_solve_fluidity_system(mpmg_ctx *ctx, const double *elem_k, const double *elem_f, const double *node_m,
+                               const int *cell_start, double *x, bool zero_start);
 int mpmg_launch_material_only(mpmg_ctx *ctx);
 int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const double *x, const double *y,
                     const double *vx, const double *vy, const double *sxx, const double *sxy,

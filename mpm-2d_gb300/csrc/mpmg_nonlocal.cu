@@ -530,31 +530,33 @@ void mpmg_nonlocal_free(mpmg_ctx *ctx)
     ctx->cg_barrier = nullptr;
 }
 
-// The fluidity solve on the assembled element blocks (ctx->elem_k,
-// ctx->elem_f): one cooperative launch of the PCG; the nodal fluidity lands
-// in ctx->node_gf, unknowns are the nodes with ctx->node_m above the
-// material's threshold.
-int mpmg_launch_solve(mpmg_ctx *ctx)
+// The fluidity system on element blocks elem_k and right-hand sides elem_f
+// (the layout assemble_kernel writes), unknowns the nodes with node_m above
+// the material's threshold: one cooperative launch of the PCG, the solution
+// in x (its previous contents are the initial guess unless zero_start).  The
+// forward step solves for the nodal fluidity; the adjoint step solves the
+// same symmetric system for the adjoint of the fluidity.
+int mpmg_solve_fluidity_system(mpmg_ctx *ctx, const double *elem_k, const double *elem_f, const double *node_m,
+                               const int *cell_start, double *x, bool zero_start)
 {
     cudaStream_t s = ctx->stream;
     const mpmg_config &c = ctx->cfg;
     const bool mu2 = c.material == MPMG_G_NONLOCAL_MU2;
-    const int ne = (int)ctx->ne;
     SolveArgs S;
     S.Nx = c.Nx;
     S.Ny = c.Ny;
     S.Ex = ctx->Ex;
     S.Ey = ctx->Ey;
-    S.ne = ne;
+    S.ne = (int)ctx->ne;
     S.dof_tol = mu2 ? 0.0 : MPMG_TOL;
     S.shift = mu2 ? 1e-10 : 0.0;
     S.tol = c.solver_tol;
     S.maxit = c.solver_maxit;
-    S.node_m = ctx->node_m;
-    S.cell_start = ctx->cell_start;
-    S.elem_k = ctx->elem_k;
-    S.elem_f = ctx->elem_f;
-    S.x = ctx->node_gf;     // result in place; previous solution when warm-starting
+    S.node_m = node_m;
+    S.cell_start = cell_start;
+    S.elem_k = elem_k;
+    S.elem_f = elem_f;
+    S.x = x;
     S.r = ctx->cg_r;
     S.p = ctx->cg_p;
     S.q = ctx->cg_q;
@@ -567,14 +569,21 @@ int mpmg_launch_solve(mpmg_ctx *ctx)
     S.status = ctx->d_status;
     S.sp = ctx->d_params;
     void *args[] = {&S};
-    if (!c.solver_warm_start) MPMG_CHECK(cudaMemsetAsync(ctx->node_gf, 0, ctx->nn * sizeof(double), s));
+    if (zero_start) MPMG_CHECK(cudaMemsetAsync(x, 0, ctx->nn * sizeof(double), s));
     MPMG_CHECK(cudaMemsetAsync(ctx->cg_barrier, 0, 2 * sizeof(unsigned int), s));
     MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_kernel, dim3(ctx->cg_blocks),
                                            dim3(kSolveThreads), args, 0, s));
     ctx->launches += 1;
-
     MPMG_CHECK(cudaGetLastError());
     return MPMG_OK;
+}
+
+// The fluidity solve on the assembled element blocks (ctx->elem_k,
+// ctx->elem_f): the nodal fluidity lands in ctx->node_gf.
+int mpmg_launch_solve(mpmg_ctx *ctx)
+{
+    return mpmg_solve_fluidity_system(ctx, ctx->elem_k, ctx->elem_f, ctx->node_m, ctx->cell_start, ctx->node_gf,
+                                      !ctx->cfg.solver_warm_start);
 }
 
 int mpmg_launch_fluidity(mpmg_ctx *ctx)

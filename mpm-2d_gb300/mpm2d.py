@@ -101,6 +101,7 @@ def lib(build_if_missing=True):
         L.mpmg_record_async.argtypes = [vp, C.c_int]
         L.mpmg_record_wait.argtypes = [vp, C.c_int, dp, ip]
         L.mpmg_adj_state.argtypes = [vp, C.c_char_p, dp]
+        L.mpmg_adj_gradient.argtypes = [vp, C.c_int, dp]
         L.mpmg_get_map.argtypes = [vp, ip, ip]
         L.mpmg_set_map.argtypes = [vp, ip, ip]
         L.mpmg_get_sort.argtypes = [vp, ip, ip, ip]
@@ -305,11 +306,15 @@ class Simulation:
 
     def adj_backward(self, dl_dx, dl_dy):
         """Gradient of a loss on the taped run's final positions with respect to
-        (mu_s, mu_2, I0, E), given dL/dx and dL/dy per particle."""
+        (mu_s, mu_2, I0, E, A), given dL/dx and dL/dy per particle; A is
+        g_nonlocal_mu2's nonlocal amplitude (zero for the local materials)."""
         gx = np.ascontiguousarray(dl_dx, dtype=np.float64)
         gy = np.ascontiguousarray(dl_dy, dtype=np.float64)
-        out = np.zeros(4)
+        out = np.zeros(5)
         _check(lib().mpmg_adj_backward(self._h, _dptr(gx), _dptr(gy), _dptr(out)))
+        a = C.c_double()
+        _check(lib().mpmg_adj_gradient(self._h, 4, C.byref(a)))
+        out[4] = a.value
         return out
 
     def adj_state(self, name):

@@ -1,5 +1,7 @@
 """Reverse-mode adjoint of the FP64 step (mpmg_adj_forward_tape /
-mpmg_adj_backward) against central finite differences of the forward step.
+mpmg_adj_backward / mpmg_adj_gradient) against central finite differences of
+the forward step, for g_local_mu2, isolin and g_nonlocal_mu2 (whose gradient
+also covers the nonlocal amplitude A).
 
 The loss is the squared distance of the final particle positions to a target
 run with perturbed parameters (the adjoint benchmark's loss, on a small
@@ -142,7 +144,7 @@ def test_torch_autograd_wrapper(target):
         def backward(ctx, gx, gy):
             g = ctx.sim.adj_backward(gx.numpy(), gy.numpy())
             ctx.sim.close()
-            return torch.from_numpy(g)
+            return torch.from_numpy(g[:4])     # (mu_s, mu_2, I0, E); g[4] is A's
 
     theta = torch.tensor(THETA0, dtype=torch.float64, requires_grad=True)
     x, y = Trajectory.apply(theta)
@@ -150,4 +152,47 @@ def test_torch_autograd_wrapper(target):
     L.backward()
     g, sim = adjoint_grad(THETA0, target, K=32)
     sim.close()
-    np.testing.assert_allclose(theta.grad.numpy(), g, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(theta.grad.numpy(), g[:4], rtol=1e-12, atol=0)
+
+
+# g_nonlocal_mu2: the fluidity solve reversed by a solve of the same symmetric
+# system for the fluidity's adjoint, so the gradient also reaches the
+# nonlocal amplitude A.  A 32^2 silo from a lithostatic stress above yield
+# (the fluidity is non-trivial from the first step), outlet open, 40 steps.
+NL_THETA0 = np.array([0.3819, 0.6435, 0.278, 1e6, 0.48])
+NL_STEPS = 40
+
+
+def nl_silo(theta):
+    mp = {"grains_d": 5.3e-4, "mu_s": theta[0], "mu_2": theta[1], "I0": theta[2], "A": theta[4]}
+    return scenes.silo_prestressed(cells=32, dt=1e-4, mp=mp, props=(theta[3], 0.3))
+
+
+def nl_final(theta):
+    sim = mpm2d.Simulation(nl_silo(theta))
+    sim.step(NL_STEPS)
+    x, y = sim.get("x"), sim.get("y")
+    sim.close()
+    return x, y
+
+
+def test_nonlocal_adjoint_matches_central_differences():
+    tx, ty = nl_final(NL_THETA0 * np.array([1.05, 0.95, 1.0, 1.1, 1.2]))
+
+    def nl_loss(theta):
+        x, y = nl_final(theta)
+        return float(np.sum((x - tx) ** 2 + (y - ty) ** 2))
+
+    sim = mpm2d.Simulation(nl_silo(NL_THETA0))
+    sim.adj_forward_tape(NL_STEPS, 10)
+    x, y = sim.get("x"), sim.get("y")
+    g = sim.adj_backward(2 * (x - tx), 2 * (y - ty))
+    sim.close()
+    for k, name in enumerate(PARAMS + ("A",)):
+        h = 1e-4 * NL_THETA0[k]
+        tp, tm = NL_THETA0.copy(), NL_THETA0.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd = (nl_loss(tp) - nl_loss(tm)) / (2 * h)
+        assert abs(g[k] - fd) <= 1e-3 * abs(fd), (name, g[k], fd)
+
