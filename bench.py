@@ -487,6 +487,56 @@ def run_gpu(args):
             "grad": dict(zip(names, map(float, grad))), "fd_central_1e-4": dict(zip(names, map(float, fd))),
             "max_rel_err_vs_fd": float(max(abs(g - f) / abs(f) for g, f in zip(grad, fd) if f != 0))}
 
+        # the nonlocal step (g_nonlocal_mu2: the fluidity solve reversed by an
+        # adjoint solve), whose gradient also reaches the nonlocal amplitude A
+        # 50 steps: over longer horizons the nonlocal silo's loss turns rough
+        # (finite differences stop agreeing across step sizes), see the notes
+        nl_steps, nl_k = 50, 25
+        nl0 = np.array([0.3819, 0.6435, 0.278, 1e6, 0.48])
+
+        def nl_scene(th):
+            mp = {"grains_d": 5.3e-4, "mu_s": th[0], "mu_2": th[1], "I0": th[2], "A": th[4]}
+            return scenes.silo_prestressed(cells=128, dt=2e-5, mp=mp, props=(th[3], 0.3))
+
+        def nl_xy(th):
+            s_ = mpm2d.Simulation(nl_scene(th), device=dev)
+            s_.step(nl_steps)
+            xy = (s_.get("x"), s_.get("y"))
+            s_.close()
+            return xy
+
+        nxt, nyt = nl_xy(nl0 * np.array([1.05, 0.95, 1.0, 1.1, 1.2]))
+        s_ = mpm2d.Simulation(nl_scene(nl0), device=dev)
+        nl_n = s_.n
+        s_.synchronize()
+        t0 = time.perf_counter()
+        s_.step(nl_steps)
+        s_.synchronize()
+        nl_fwd = time.perf_counter() - t0
+        s_.close()
+        s_ = mpm2d.Simulation(nl_scene(nl0), device=dev)
+        t0 = time.perf_counter()
+        s_.adj_forward_tape(nl_steps, nl_k)
+        nl_tape = time.perf_counter() - t0
+        xa, ya = s_.get("x"), s_.get("y")
+        t0 = time.perf_counter()
+        nl_grad = s_.adj_backward(2 * (xa - nxt), 2 * (ya - nyt))
+        nl_bwd = time.perf_counter() - t0
+        s_.close()
+        hA = 1e-4 * nl0[4]
+        tp, tm = nl0.copy(), nl0.copy()
+        tp[4] += hA
+        tm[4] -= hA
+        (xp, yp), (xm, ym) = nl_xy(tp), nl_xy(tm)
+        fdA = (np.sum((xp - nxt) ** 2 + (yp - nyt) ** 2) - np.sum((xm - nxt) ** 2 + (ym - nyt) ** 2)) / (2 * hA)
+        adjoint_line["nonlocal"] = {
+            "workload": "g_nonlocal_mu2 square silo from a lithostatic stress, %d particles, 128^2 elements, "
+                        "dt 2e-5, %d steps, loss against mu_s*1.05, mu_2*0.95, E*1.1, A*1.2" % (nl_n, nl_steps),
+            "checkpoint_every": nl_k, "forward_s": nl_fwd, "tape_forward_s": nl_tape, "backward_s": nl_bwd,
+            "adjoint_over_forward": nl_bwd / nl_fwd,
+            "grad": dict(zip(names + ("A",), map(float, nl_grad))), "fd_central_1e-4_A": float(fdA),
+            "rel_err_A_vs_fd": float(abs(nl_grad[4] - fdA) / abs(fdA)) if fdA != 0 else None}
+
     # --- end to end through the C ABI with host buffers (mixed) ---------------
     # The user's run: create the simulation from host arrays (H2D of the
     # particle state), step, read each step's result back (the step record:
