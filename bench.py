@@ -349,6 +349,44 @@ def run_gpu(args):
     valuef = n * args.steps * world / slowest(msf / 1e3)
     simf.close()
 
+    # --- end to end through the C ABI with host buffers (mixed) ---------------
+    # (measured before the batch, nonlocal and adjoint sections, whose large
+    # allocations and frees would otherwise slow the first cudaMalloc calls
+    # of a user's fresh run)
+    # The user's run: create the simulation from host arrays (H2D of the
+    # particle state), step, read each step's result back (the step record:
+    # time, step count, device status, one D2H copy per step, pipelined with
+    # mpmg_record_async / mpmg_record_wait so that step k + 1 is issued before
+    # step k's record is waited for), and write the output frame at the end
+    # (mpmg_get_fields of the driver's write_frame fields into pinned host
+    # buffers).
+    e2e_steps = args.e2e_steps
+    host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
+    sync_all()
+    t0 = time.perf_counter()
+    sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
+    t1 = time.perf_counter()
+    last = None
+    for k in range(e2e_steps):
+        sim2.step(1)
+        sim2.record_async(k % 2)
+        if k > 0:
+            last = sim2.record_wait((k - 1) % 2)
+    last = sim2.record_wait((e2e_steps - 1) % 2)
+    t2 = time.perf_counter()
+    assert last[1] == e2e_steps
+    sim2.get_frame(FRAME_FIELDS, out=host)
+    t3 = time.perf_counter()
+    sync_all()
+    e2e_t = slowest(t3 - t0)
+    e2e_parts = {"create_s": t1 - t0, "steps_s": t2 - t1, "frame_s": t3 - t2}
+    sim2.close()
+    e2e_value = n * e2e_steps * world / e2e_t
+    h2d_total = 9 * 8 * n                      # m v x y vx vy sxx sxy syy
+    d2h_frame = len(FRAME_FIELDS) * 8 * n      # the frame's FP64 fields in particle order
+    step_record = 64                           # step record + status word, one copy per step
+
+
     # --- batched ensemble: 256 independent silo / heap runs in one context ------
     batch_line = None
     if not args.no_batch:
@@ -537,39 +575,6 @@ def run_gpu(args):
             "grad": dict(zip(names + ("A",), map(float, nl_grad))), "fd_central_1e-4_A": float(fdA),
             "rel_err_A_vs_fd": float(abs(nl_grad[4] - fdA) / abs(fdA)) if fdA != 0 else None}
 
-    # --- end to end through the C ABI with host buffers (mixed) ---------------
-    # The user's run: create the simulation from host arrays (H2D of the
-    # particle state), step, read each step's result back (the step record:
-    # time, step count, device status, one D2H copy per step, pipelined with
-    # mpmg_record_async / mpmg_record_wait so that step k + 1 is issued before
-    # step k's record is waited for), and write the output frame at the end
-    # (mpmg_get_fields of the driver's write_frame fields into pinned host
-    # buffers).
-    e2e_steps = args.e2e_steps
-    host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
-    sync_all()
-    t0 = time.perf_counter()
-    sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
-    t1 = time.perf_counter()
-    last = None
-    for k in range(e2e_steps):
-        sim2.step(1)
-        sim2.record_async(k % 2)
-        if k > 0:
-            last = sim2.record_wait((k - 1) % 2)
-    last = sim2.record_wait((e2e_steps - 1) % 2)
-    t2 = time.perf_counter()
-    assert last[1] == e2e_steps
-    sim2.get_frame(FRAME_FIELDS, out=host)
-    t3 = time.perf_counter()
-    sync_all()
-    e2e_t = slowest(t3 - t0)
-    sim2.close()
-    e2e_value = n * e2e_steps * world / e2e_t
-    h2d_total = 9 * 8 * n                      # m v x y vx vy sxx sxy syy
-    d2h_frame = len(FRAME_FIELDS) * 8 * n      # the frame's FP64 fields in particle order
-    step_record = 64                           # step record + status word, one copy per step
-
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -601,7 +606,7 @@ def run_gpu(args):
                           "note": "same mixed step with FP64 nodal mass/momentum sums and division"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
                 "d2h_bytes_per_step": step_record + d2h_frame / e2e_steps, "steps": e2e_steps,
-                "create_s": t1 - t0, "steps_s": t2 - t1, "frame_s": t3 - t2,
+                **e2e_parts,
                 "path": "mpmg_create from host arrays, per step mpmg_step + the step record read back "
                         "(mpmg_record_async / mpmg_record_wait, one step behind), "
                         "one output frame (mpmg_get_fields of %d fields)" % len(FRAME_FIELDS)},
