@@ -284,6 +284,65 @@ def phase_profile(sim, steps, table, n, ne, nn):
     return out
 
 
+ACC_FIELDS = ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy")
+ACC_GROUPS = {"sxy": ("sxx", "syy"), "vx": ("vx", "vy"), "vy": ("vx", "vy"), "ux": ("ux", "uy"),
+              "uy": ("ux", "uy")}
+
+
+def accuracy_report(mpm2d, scenes, scene, dev):
+    """The mixed form against the FP64 form: relative L2 error per field after
+    100 steps of the benchmark workload (a field of a physical group, such as
+    sxy, scaled by the group's largest norm), and the silo discharge rate and
+    column runout of the mixed-form tests (3000 steps each)."""
+    out = {}
+    sims = {p: mpm2d.Simulation(scene, device=dev, precision=p) for p in ("mixed", "fp64")}
+    for s_ in sims.values():
+        s_.step(100)
+    ref = {f: sims["fp64"].get(f) for f in ACC_FIELDS}
+    err = {}
+    for f in ACC_FIELDS:
+        a, b = sims["mixed"].get(f), ref[f]
+        scale = max(np.linalg.norm(ref[g]) for g in ACC_GROUPS[f]) if f in ACC_GROUPS else np.linalg.norm(b)
+        err[f] = float(np.linalg.norm(a - b) / scale) if scale > 0 else float(np.linalg.norm(a - b))
+    for s_ in sims.values():
+        s_.close()
+    out["rel_l2_after_100_steps"] = err
+
+    def active_mass_rate(sim, m, steps, every):
+        hist = []
+        for _ in range(steps // every):
+            sim.step(every)
+            _, act = sim.get_map()
+            hist.append((sim.t, float(m[act == 1].sum())))
+        h = np.array(hist)
+        t, mass = h[:, 0], h[:, 1]
+        flowing = mass < mass[0] * (1 - 1e-9)
+        t, mass = t[flowing], mass[flowing]
+        return float(-np.polyfit(t, mass, 1)[0]) if t.size >= 2 else 0.0
+
+    silo = scenes.silo(cells=48, material="g_local_mu2", props=(1e6, 0.3), dt=1e-4, hole_radius=0.12,
+                       open_time=0.05, wall_frac=0.5, fill_height=0.5, mp={"grains_d": 5.3e-4})
+    q = {}
+    for p in ("mixed", "fp64"):
+        s_ = mpm2d.Simulation(silo, device=dev, precision=p)
+        q[p] = active_mass_rate(s_, silo["particles"]["m"], 3000, 50)
+        s_.close()
+    out["silo_discharge_rate"] = {"mixed": q["mixed"], "fp64": q["fp64"],
+                                  "rel_diff": abs(q["mixed"] - q["fp64"]) / q["fp64"] if q["fp64"] else None,
+                                  "scene": "g_local_mu2 silo, 48^2 elements, 3000 steps (kg/s per unit depth)"}
+    col = scenes.column(Nx=129, Ny=129, h=1 / 128, width=0.25, height=0.4, material="g_local_mu2", rho=2450.0,
+                        props=(1e6, 0.3), dt=1e-5, mp={"grains_d": 5.3e-4}, jitter=1e-3, seed=4)
+    r = {}
+    for p in ("mixed", "fp64"):
+        s_ = mpm2d.Simulation(col, device=dev, precision=p)
+        s_.step(3000)
+        r[p] = float(s_.get("x")[s_.get_map()[1] == 1].max())
+        s_.close()
+    out["column_runout"] = {"mixed": r["mixed"], "fp64": r["fp64"], "rel_diff": abs(r["mixed"] - r["fp64"]) / r["fp64"],
+                            "scene": "g_local_mu2 column, 128^2 elements, 3000 steps (largest active x, m)"}
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -386,6 +445,9 @@ def run_gpu(args):
     d2h_frame = len(FRAME_FIELDS) * 8 * n      # the frame's FP64 fields in particle order
     step_record = 64                           # step record + status word, one copy per step
 
+
+    # --- accuracy of the mixed form against the FP64 form ------------------------
+    accuracy_line = accuracy_report(mpm2d, scenes, scene, dev) if not args.no_accuracy else None
 
     # --- batched ensemble: 256 independent silo / heap runs in one context ------
     batch_line = None
@@ -600,6 +662,7 @@ def run_gpu(args):
                  "bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s)"},
         "mixed_over_fp64": value / value64,
         "batch": batch_line,
+        "accuracy": accuracy_line,
         "adjoint": adjoint_line,
         "nonlocal_silo": nonlocal_line,
         "mixed_f64node": {"value": valuef, "unit": UNIT, "steps": args.steps, "ms_per_step": msf / args.steps,
@@ -636,6 +699,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-nonlocal", action="store_true", help="skip the nonlocal silo measurement")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 accuracy report")
     ap.add_argument("--e2e-steps", type=int, default=500,
                     help="steps of the end-to-end run (one output frame at its end)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
