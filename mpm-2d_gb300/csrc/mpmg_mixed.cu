@@ -317,7 +317,9 @@ __device__ __forceinline__ int find_member(const int *__restrict__ off, int coun
 
 // ---------------------------------------------------------------------------
 
-// P2G: a block takes 256 consecutive elements, one thread each, and works
+// P2G of a batch (a single simulation runs mx_p2g_grid_kernel, which sums
+// the same way over element tiles and finishes the nodes itself): a block
+// takes 256 consecutive elements, one thread each, and works
 // through them in passes of whole elements whose particles (a contiguous
 // range of the binned order) fit a 1024-particle shared-memory stage.  Each
 // pass loads the range's slots (coalesced) and copies the particle records
@@ -608,8 +610,8 @@ __device__ __forceinline__ void node_finish(const MemberM &M, double t_next, flo
     }
 }
 
-// Grid update, one thread per node, from the corner sums mx_p2g_kernel left
-// in global memory.
+// Grid update of a batch, one thread per node, from the corner sums
+// mx_p2g_kernel left in global memory.
 template <bool F64NODE, bool BATCH>
 __global__ void __launch_bounds__(256) mx_grid_kernel(const __grid_constant__ MemberM m0, BatchView bv, int ne_total,
                                                       int nn_total, const int *__restrict__ cell_start,
