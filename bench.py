@@ -422,25 +422,31 @@ def run_gpu(args):
     # allocations and frees would otherwise slow the first cudaMalloc calls
     # of a user's fresh run)
     # The user's run: create the simulation from host arrays (H2D of the
-    # particle state), step, read each step's result back (the step record:
-    # time, step count, device status, one D2H copy per step, pipelined with
-    # mpmg_record_async / mpmg_record_wait so that step k + 1 is issued before
-    # step k's record is waited for), and write the output frame at the end
-    # (mpmg_get_fields of the driver's write_frame fields into pinned host
-    # buffers).
+    # particle state), step in CUDA graphs of 8 steps with every step writing
+    # its result (the step record: time, step count, device status) into a
+    # ring in mapped pinned host memory (mpmg_record_ring), read each step's
+    # record on the host one chunk behind (mpmg_record_ring_wait), and write
+    # the output frame at the end (mpmg_get_fields of the driver's
+    # write_frame fields into pinned host buffers).
     e2e_steps = args.e2e_steps
     host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
     sync_all()
     t0 = time.perf_counter()
     sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
+    sim2.record_ring(32)
     t1 = time.perf_counter()
     last = None
-    for k in range(e2e_steps):
-        sim2.step(1)
-        sim2.record_async(k % 2)
-        if k > 0:
-            last = sim2.record_wait((k - 1) % 2)
-    last = sim2.record_wait((e2e_steps - 1) % 2)
+    pending = []
+    k = 0
+    while k < e2e_steps:
+        c = min(8, e2e_steps - k)
+        sim2.step(c)
+        for s_ in pending:
+            last = sim2.record_ring_wait(s_)
+        pending = list(range(k + 1, k + c + 1))
+        k += c
+    for s_ in pending:
+        last = sim2.record_ring_wait(s_)
     t2 = time.perf_counter()
     assert last[1] == e2e_steps
     sim2.get_frame(FRAME_FIELDS, out=host)
@@ -452,7 +458,7 @@ def run_gpu(args):
     e2e_value = n * e2e_steps * world / e2e_t
     h2d_total = 9 * 8 * n                      # m v x y vx vy sxx sxy syy
     d2h_frame = len(FRAME_FIELDS) * 8 * n      # the frame's FP64 fields in particle order
-    step_record = 64                           # step record + status word, one copy per step
+    step_record = 80                           # ring slot: step number + step record + status word
 
 
     # --- accuracy of the mixed form against the FP64 form ------------------------
@@ -679,8 +685,9 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
                 "d2h_bytes_per_step": step_record + d2h_frame / e2e_steps, "steps": e2e_steps,
                 **e2e_parts,
-                "path": "mpmg_create from host arrays, per step mpmg_step + the step record read back "
-                        "(mpmg_record_async / mpmg_record_wait, one step behind), "
+                "path": "mpmg_create from host arrays, mpmg_step in CUDA graphs of 8 steps, every step's "
+                        "record written by the step into mapped pinned host memory and read on the host "
+                        "(mpmg_record_ring / mpmg_record_ring_wait, one chunk behind), "
                         "one output frame (mpmg_get_fields of %d fields)" % len(FRAME_FIELDS)},
     }
     if rank == 0 and not args.no_cpu_baseline:

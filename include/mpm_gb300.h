@@ -237,6 +237,18 @@ MPMG_API int mpmg_get_time(mpmg_ctx *ctx, double *t, int *step_number);
    for step k's record, so the GPU never idles on the host. */
 MPMG_API int mpmg_record_async(mpmg_ctx *ctx, int slot);
 MPMG_API int mpmg_record_wait(mpmg_ctx *ctx, int slot, double *t, int *step_number);
+/* Per-step records written by the step itself (no counterpart in the
+   reference): with slots > 0, every step ends with one small kernel that
+   copies the step record (time, step count, solver bookkeeping, device
+   status) into slot (step - 1) % slots of a ring in mapped pinned host
+   memory, so steps can run in CUDA graphs of many steps and the host still
+   reads each step's result.  slots = 0 turns it off.
+   mpmg_record_ring_wait waits (bounded, about 10 s) for the record of step
+   step_number, checks its device status as mpmg_record_wait does, and
+   returns its time and step count; it fails with MPMG_ERR_INVALID when that
+   slot already holds a later step (read within `slots` steps). */
+MPMG_API int mpmg_record_ring(mpmg_ctx *ctx, int slots);
+MPMG_API int mpmg_record_ring_wait(mpmg_ctx *ctx, long long step_number, double *t, int *step_out);
 MPMG_API int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number);
 MPMG_API int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *num_elements);
 

@@ -8,6 +8,9 @@
 #include <new>
 #include <vector>
 
+#include <atomic>
+#include <chrono>
+
 #include "mpmg_internal.cuh"
 
 namespace {
@@ -385,6 +388,7 @@ int mpmg_destroy(mpmg_ctx *ctx)
         if (ctx->h_ring[k]) cudaFreeHost(ctx->h_ring[k]);
         if (ctx->ring_ev[k]) cudaEventDestroy(ctx->ring_ev[k]);
     }
+    if (ctx->rring_h) cudaFreeHost(ctx->rring_h);
     mpmg_bin_free(ctx);
     mpmg_nonlocal_free(ctx);
     mpmg_mixed_free(ctx);
@@ -837,9 +841,40 @@ int mpmg_batch_get_time(mpmg_ctx *ctx, int member, double *t, int *step_number)
 
 namespace {
 
+// The step's own read-back (mpmg_record_ring): one block copies the step
+// record (times, step count, solver bookkeeping, device status) into the ring
+// slot of the step just completed, in mapped pinned host memory, and then the
+// slot's step number, so that a host that sees the number sees the record.
+// It waits for the step's last kernel (programmatic dependent launch) and
+// lets the next step's first kernel start its prologue at once.
+__global__ void record_ring_kernel(const unsigned char *__restrict__ rec, int bytes,
+                                   const StepParams *__restrict__ sp, unsigned char *ring, int slot_bytes,
+                                   int slots)
+{
+    mpmg_pdl_trigger();
+    mpmg_pdl_wait();
+    const long long step = sp->step_count;
+    unsigned char *dst = ring + (size_t)((step - 1 + slots) % slots) * (size_t)slot_bytes;
+    for (int i = threadIdx.x * 4; i < bytes; i += blockDim.x * 4)
+        *reinterpret_cast<volatile uint32_t *>(dst + 16 + i) = *reinterpret_cast<const uint32_t *>(rec + i);
+    __threadfence_system();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *reinterpret_cast<volatile long long *>(dst) = step;
+        __threadfence_system();
+    }
+}
+
 int launch_one_step(mpmg_ctx *ctx)
 {
-    return ctx->mixed ? mpmg_mixed_step(ctx) : mpmg_launch_step(ctx);
+    int rc = ctx->mixed ? mpmg_mixed_step(ctx) : mpmg_launch_step(ctx);
+    if (rc != MPMG_OK || ctx->rring_slots <= 0) return rc;
+    MPMG_CHECK(mpmg_launch_pdl(true, record_ring_kernel, dim3(1), dim3(64), 0, ctx->stream,
+                               (const unsigned char *)ctx->d_params, (int)step_record_bytes(ctx),
+                               (const StepParams *)ctx->d_params, ctx->rring_d, (int)ctx->rring_slot_bytes,
+                               ctx->rring_slots));
+    ctx->launches += 1;
+    return MPMG_OK;
 }
 
 int parity(const mpmg_ctx *ctx)
@@ -998,7 +1033,7 @@ int mpmg_step(mpmg_ctx *ctx, int nsteps)
     if (graphs_apply(ctx)) return step_with_graphs(ctx, nsteps);
     for (int k = 0; k < nsteps; k++) {
         for (int ph = 0; ph < PH_COUNT; ph++) ctx->phase_used[ph] = 0;
-        int rc = ctx->mixed ? mpmg_mixed_step(ctx) : mpmg_launch_step(ctx);
+        int rc = launch_one_step(ctx);
         if (rc != MPMG_OK) return rc;
         if (ctx->timing) {
             MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
@@ -1183,6 +1218,60 @@ int mpmg_record_async(mpmg_ctx *ctx, int slot)
                                ctx->stream));
     MPMG_CHECK(cudaEventRecord(ctx->ring_ev[slot], ctx->stream));
     return MPMG_OK;
+}
+
+int mpmg_record_ring(mpmg_ctx *ctx, int slots)
+{
+    if (ctx == nullptr || slots < 0 || slots > (1 << 20)) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(ctx->dev));
+    MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->rring_h != nullptr) {
+        MPMG_CHECK(cudaFreeHost(ctx->rring_h));
+        ctx->rring_h = nullptr;
+        ctx->rring_d = nullptr;
+    }
+    ctx->rring_slots = 0;
+    drop_graphs(ctx);          // the captured steps gain or lose the record launch
+    if (slots == 0) return MPMG_OK;
+    const size_t slot_bytes = (16 + step_record_bytes(ctx) + 15) / 16 * 16;
+    MPMG_CHECK(cudaHostAlloc((void **)&ctx->rring_h, slots * slot_bytes, cudaHostAllocMapped));
+    memset(ctx->rring_h, 0, slots * slot_bytes);
+    MPMG_CHECK(cudaHostGetDevicePointer((void **)&ctx->rring_d, ctx->rring_h, 0));
+    ctx->rring_slot_bytes = slot_bytes;
+    ctx->rring_slots = slots;
+    return MPMG_OK;
+}
+
+int mpmg_record_ring_wait(mpmg_ctx *ctx, long long step_number, double *t, int *step_out)
+{
+    if (ctx == nullptr || ctx->rring_slots <= 0 || step_number < 1) return MPMG_ERR_INVALID;
+    const unsigned char *slot =
+        ctx->rring_h + (size_t)((step_number - 1) % ctx->rring_slots) * ctx->rring_slot_bytes;
+    const volatile long long *seq = reinterpret_cast<const volatile long long *>(slot);
+    // bounded wait (about 10 s): the step may still be queued behind others
+    const auto t0 = std::chrono::steady_clock::now();
+    long long seen;
+    while ((seen = *seq) < step_number) {
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(10)) {
+            cudaError_t e = cudaStreamQuery(ctx->stream);
+            if (e != cudaSuccess && e != cudaErrorNotReady) return mpmg_cuda_status(e, "record ring");
+            mpmg_set_error("step %lld's record did not arrive", step_number);
+            return MPMG_ERR_DEVICE;
+        }
+    }
+    if (seen != step_number) {
+        mpmg_set_error("step %lld's ring slot was overwritten by step %lld (read the ring within %d steps)",
+                       step_number, seen, ctx->rring_slots);
+        return MPMG_ERR_INVALID;
+    }
+    std::atomic_thread_fence(std::memory_order_acquire);
+    std::vector<unsigned char> rec(step_record_bytes(ctx));
+    memcpy(rec.data(), slot + 16, rec.size());
+    int rc = take_record(ctx, rec.data());
+    if (rc != MPMG_OK && rc != MPMG_ERR_SOLVER) return rc;
+    if (t) *t = ctx->h_params.t;
+    if (step_out) *step_out = (int)ctx->h_params.step_count;
+    return rc;
 }
 
 int mpmg_record_wait(mpmg_ctx *ctx, int slot, double *t, int *step_number)

@@ -154,6 +154,13 @@ struct mpmg_ctx {
     // ring slots, each completed by its event
     unsigned char *h_ring[MPMG_RECORD_SLOTS];
     cudaEvent_t ring_ev[MPMG_RECORD_SLOTS];
+    // per-step records written by the step itself into mapped pinned memory
+    // (mpmg_record_ring): slot k holds a step number (8 bytes, written last)
+    // and then the step record
+    unsigned char *rring_h;
+    unsigned char *rring_d;
+    int rring_slots;
+    size_t rring_slot_bytes;
     size_t status_offset;      // byte offset of the status word in the record block
 
     // Batched ensemble (mpmg_batch_create): several independent simulations

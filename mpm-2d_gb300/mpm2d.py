@@ -102,6 +102,8 @@ def lib(build_if_missing=True):
         L.mpmg_record_wait.argtypes = [vp, C.c_int, dp, ip]
         L.mpmg_adj_state.argtypes = [vp, C.c_char_p, dp]
         L.mpmg_adj_gradient.argtypes = [vp, C.c_int, dp]
+        L.mpmg_record_ring.argtypes = [vp, C.c_int]
+        L.mpmg_record_ring_wait.argtypes = [vp, C.c_longlong, dp, ip]
         L.mpmg_get_map.argtypes = [vp, ip, ip]
         L.mpmg_set_map.argtypes = [vp, ip, ip]
         L.mpmg_get_sort.argtypes = [vp, ip, ip, ip]
@@ -238,6 +240,18 @@ class Simulation:
 
     def step(self, n=1):
         _check(lib().mpmg_step(self._h, n))
+
+    def record_ring(self, slots):
+        """Have every step write its record into a ring of `slots` entries in
+        mapped pinned host memory (0: off); see record_ring_wait."""
+        _check(lib().mpmg_record_ring(self._h, slots))
+
+    def record_ring_wait(self, step_number):
+        """(t, step_count) of step step_number's record from the ring."""
+        t = C.c_double()
+        k = C.c_int()
+        _check(lib().mpmg_record_ring_wait(self._h, step_number, C.byref(t), C.byref(k)))
+        return t.value, k.value
 
     def record_async(self, slot):
         """Enqueue the read-back of the step record into ring slot 0-3 (mpmg_record_async)."""

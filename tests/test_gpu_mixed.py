@@ -279,3 +279,35 @@ def test_pipelined_record_reads_match_synchronous_ones(precision):
     assert got == want
     np.testing.assert_array_equal(a.get("x"), b.get("x"))
 
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_record_ring_reads_every_step(precision):
+    """Steps in CUDA graphs of 8 with every step's record written by the step
+    into the mapped ring (mpmg_record_ring): each step's record arrives, the
+    trajectory equals a run without the ring, and a read that lags more than
+    the ring's length fails instead of returning a later step."""
+    sc = scenes.config1(seed=2)
+    a = mpm2d.Simulation(sc, precision=precision)
+    b = mpm2d.Simulation(sc, precision=precision)
+    a.record_ring(32)
+    recs = []
+    for chunk in range(5):
+        a.step(8)
+        recs += [a.record_ring_wait(k) for k in range(8 * chunk + 1, 8 * chunk + 9)]
+    b.step(40)
+    assert [k for _, k in recs] == list(range(1, 41))
+    assert all(t1 > t0 for (t0, _), (t1, _) in zip(recs, recs[1:]))
+    assert recs[-1][0] == b.t
+    for f in ("x", "y", "vx", "vy", "sxx", "syy"):
+        np.testing.assert_array_equal(a.get(f), b.get(f), err_msg=f)
+    a.record_ring(4)
+    a.step(8)
+    a.synchronize()                     # all eight steps have written their slots
+    with pytest.raises(mpm2d.MpmError):
+        a.record_ring_wait(41)          # slot 0 now holds step 45
+    assert a.record_ring_wait(48)[1] == 48
+    a.record_ring(0)
+    a.step(3)
+    a.close()
+    b.close()
+
