@@ -605,7 +605,7 @@ def run_gpu(args):
         # the nonlocal step (g_nonlocal_mu2: the fluidity solve reversed by an
         # adjoint solve), whose gradient also reaches the nonlocal amplitude A
         # 50 steps: over longer horizons the nonlocal silo's loss turns rough
-        # (finite differences stop agreeing across step sizes), see the notes
+        # (finite differences stop agreeing across step sizes)
         nl_steps, nl_k = 50, 25
         nl0 = np.array([0.3819, 0.6435, 0.278, 1e6, 0.48])
 
