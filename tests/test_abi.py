@@ -117,3 +117,14 @@ def test_frame_read_entry_point_is_exported():
     L = mpm2d.lib()
     assert hasattr(L, "mpmg_get_fields")
     assert mpm2d.PRECISIONS == {"fp64": 0, "mixed": 1, "mixed_f64node": 2}
+
+
+def test_record_ring_and_adjoint_gradient_reject_bad_arguments():
+    """The per-step record ring and the adjoint's parameter gradient check
+    their arguments before touching the device."""
+    L = mpm2d.lib()
+    out = C.c_double()
+    k = C.c_int()
+    assert L.mpmg_record_ring(None, 8) == 16                  # MPMG_ERR_INVALID: no context
+    assert L.mpmg_record_ring_wait(None, 1, C.byref(out), C.byref(k)) == 16
+    assert L.mpmg_adj_gradient(None, 4, C.byref(out)) == 16
