@@ -246,9 +246,21 @@ MPMG_API int mpmg_record_wait(mpmg_ctx *ctx, int slot, double *t, int *step_numb
    mpmg_record_ring_wait waits (bounded, about 10 s) for the record of step
    step_number, checks its device status as mpmg_record_wait does, and
    returns its time and step count; it fails with MPMG_ERR_INVALID when that
-   slot already holds a later step (read within `slots` steps). */
+   slot already holds a later step, or a later step overwrote it while it
+   was being read (read within `slots` steps). */
 MPMG_API int mpmg_record_ring(mpmg_ctx *ctx, int slots);
 MPMG_API int mpmg_record_ring_wait(mpmg_ctx *ctx, long long step_number, double *t, int *step_out);
+/* The ring's read protocol on one slot, host memory only (no CUDA call), as
+   mpmg_record_ring_wait uses it: a slot is a 16-byte header whose first
+   64-bit word is a sequence lock (-1 while the GPU writes the body, then the
+   step number), followed by body_bytes of record.  Waits up to timeout_s
+   seconds for the sequence to reach step_number (MPMG_ERR_DEVICE when it
+   does not), copies the body into out with `copy` (memcpy when NULL) and
+   reads the sequence again: MPMG_ERR_INVALID when it was or became anything
+   but step_number, i.e. a later step overwrote the slot before or during the
+   copy. */
+MPMG_API int mpmg_ring_read_slot(const void *slot, size_t body_bytes, long long step_number, void *out,
+                                 double timeout_s, void (*copy)(void *, const void *, size_t));
 MPMG_API int mpmg_set_time(mpmg_ctx *ctx, double t, int step_number);
 MPMG_API int mpmg_sizes(mpmg_ctx *ctx, size_t *num_particles, size_t *num_nodes, size_t *num_elements);
 
@@ -323,29 +335,45 @@ MPMG_API int mpmg_last_solve(mpmg_ctx *ctx, int *iterations, double *rel_residua
    created (or since the last reset). */
 MPMG_API int mpmg_launch_count(mpmg_ctx *ctx, long *launches, int reset);
 
+/* FP64 FMA throughput of the given device in FLOP/s (an FMA counts two),
+   measured with a short kernel of independent FMA chains (best of three
+   timed launches after one warm-up).  No counterpart in the reference: it
+   is the compute bound of the plain FP64 form's kernels, which the
+   benchmark reports beside their memory bound. */
+MPMG_API int mpmg_measure_fp64_rate(int device, double *flops_per_s);
+
 /*
  * Cell sort without any allocation.  No counterpart in the reference: it
  * gives the same element order as the binning every mpmg_step performs (the
  * GPU form of find_filled_elements, libmpm/process_usl.c:677-723), to callers
- * that cannot call cudaMalloc -- code inside a CUDA stream capture, hosts
- * whose device memory belongs to their own pool allocator, and the
- * reference's dlopen'd plugins, which own no device memory.
+ * that cannot call cudaMalloc -- hosts whose device memory belongs to their
+ * own pool allocator, and the reference's dlopen'd plugins, which own no
+ * device memory.
  *
- * d_keys holds n element keys on the device (num_elements marks a particle
- * outside the grid).  Outputs, also device arrays the caller provides: the
- * keys sorted stably (d_sorted_keys, n), the permutation from sorted
+ * d_keys holds n element keys on the device.  A key in [0, num_elements) is
+ * an element; num_elements marks a particle outside the grid, and so does any
+ * key outside [0, num_elements] (the reference's -1, for instance): those are
+ * clamped to num_elements and sort into the run after the last element.
+ * Outputs, also device arrays the caller provides: the keys sorted stably
+ * (d_sorted_keys, n, with the clamping applied), the permutation from sorted
  * position to particle index (d_perm, n) and the start of every element's
- * run (d_cell_start, num_elements + 1).  Work is queued on `stream` (a
- * cudaStream_t; NULL for the default stream) and is complete when the
- * stream is.
+ * run (d_cell_start, num_elements + 1; entry num_elements is where the
+ * outside run starts).  The three outputs must not overlap one another; any
+ * of them may overlap d_keys, which is read only by the first kernel.  Work
+ * is queued on `stream` (a cudaStream_t; NULL for the default stream) and is
+ * complete when the stream is.  num_elements must lie in [1, 2^30)
+ * (MPMG_ERR_INVALID otherwise).
  *
- * Scratch is a fixed device array inside this library, held by every GPU that
- * loads it until the process exits; n above MPMG_NOALLOC_MAX_PARTICLES is
- * rejected with MPMG_ERR_SCRATCH_LIMIT.  The first call on a device looks up
- * that array's device address, so make the first call on each device before
- * any stream capture.  All calls share the array: calls that overlap on the
- * GPU race, so serialise them.  The entry point calls no cudaMalloc or
- * cudaFree.
+ * Scratch is a fixed device array inside this library (about 19 MB), held by
+ * every GPU that loads it until the process exits; n above
+ * MPMG_NOALLOC_MAX_PARTICLES is rejected with MPMG_ERR_SCRATCH_LIMIT.  The
+ * first call on a device looks up that array's device address and keeps it
+ * for the life of the process, so make the first call on each device before
+ * any stream capture, and do not call this entry point on a device after
+ * resetting it (cudaDeviceReset) in the same process: the kept address would
+ * be stale.  All calls share the array, which keeps the last call's contents:
+ * calls that overlap on the GPU race, so serialise them.  The entry point
+ * calls no cudaMalloc or cudaFree.
  */
 #define MPMG_NOALLOC_MAX_PARTICLES (1u << 20)
 MPMG_API int mpmg_sort_cells_noalloc(const int *d_keys, int n, int num_elements, int *d_sorted_keys,
