@@ -1,3 +1,4 @@
+#include <algorithm>
 // C ABI of the mpm_gb300 library: context lifecycle, host field I/O, stepping,
 // timing and error reporting.  See include/mpm_gb300.h for the contract.
 #include <math.h>
@@ -843,10 +844,14 @@ namespace {
 
 // The step's own read-back (mpmg_record_ring): one block copies the step
 // record (times, step count, solver bookkeeping, device status) into the ring
-// slot of the step just completed, in mapped pinned host memory, and then the
-// slot's step number, so that a host that sees the number sees the record.
-// It waits for the step's last kernel (programmatic dependent launch) and
-// lets the next step's first kernel start its prologue at once.
+// slot of the step just completed, in mapped pinned host memory.  The slot's
+// first word is a sequence lock: it is set to -1 before the body is written
+// and to the step number after it, with system-scope fences between, so that
+// a host that reads the step number, copies the body and then reads the same
+// step number again has read a body that no later step was writing
+// (mpmg_ring_read_slot).  The kernel waits for the step's last kernel
+// (programmatic dependent launch) and lets the next step's first kernel start
+// its prologue at once.
 __global__ void record_ring_kernel(const unsigned char *__restrict__ rec, int bytes,
                                    const StepParams *__restrict__ sp, unsigned char *ring, int slot_bytes,
                                    int slots)
@@ -855,6 +860,12 @@ __global__ void record_ring_kernel(const unsigned char *__restrict__ rec, int by
     mpmg_pdl_wait();
     const long long step = sp->step_count;
     unsigned char *dst = ring + (size_t)((step - 1 + slots) % slots) * (size_t)slot_bytes;
+    if (threadIdx.x == 0) {
+        *reinterpret_cast<volatile long long *>(dst) = -1;
+        __threadfence_system();
+    }
+    __syncthreads();
+    __threadfence_system();
     for (int i = threadIdx.x * 4; i < bytes; i += blockDim.x * 4)
         *reinterpret_cast<volatile uint32_t *>(dst + 16 + i) = *reinterpret_cast<const uint32_t *>(rec + i);
     __threadfence_system();
@@ -1242,32 +1253,58 @@ int mpmg_record_ring(mpmg_ctx *ctx, int slots)
     return MPMG_OK;
 }
 
-int mpmg_record_ring_wait(mpmg_ctx *ctx, long long step_number, double *t, int *step_out)
+int mpmg_ring_read_slot(const void *slot_ptr, size_t body_bytes, long long step_number, void *out,
+                        double timeout_s, void (*copy)(void *, const void *, size_t))
 {
-    if (ctx == nullptr || ctx->rring_slots <= 0 || step_number < 1) return MPMG_ERR_INVALID;
-    const unsigned char *slot =
-        ctx->rring_h + (size_t)((step_number - 1) % ctx->rring_slots) * ctx->rring_slot_bytes;
+    if (slot_ptr == nullptr || out == nullptr || step_number < 1) return MPMG_ERR_INVALID;
+    const unsigned char *slot = static_cast<const unsigned char *>(slot_ptr);
     const volatile long long *seq = reinterpret_cast<const volatile long long *>(slot);
-    // bounded wait (about 10 s): the step may still be queued behind others
+    // bounded wait: the step may still be queued behind others; -1 marks a
+    // slot whose body is being written (this step's or a later one's)
     const auto t0 = std::chrono::steady_clock::now();
     long long seen;
     while ((seen = *seq) < step_number) {
-        if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(10)) {
-            cudaError_t e = cudaStreamQuery(ctx->stream);
-            if (e != cudaSuccess && e != cudaErrorNotReady) return mpmg_cuda_status(e, "record ring");
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > timeout_s) {
             mpmg_set_error("step %lld's record did not arrive", step_number);
             return MPMG_ERR_DEVICE;
         }
     }
     if (seen != step_number) {
-        mpmg_set_error("step %lld's ring slot was overwritten by step %lld (read the ring within %d steps)",
-                       step_number, seen, ctx->rring_slots);
+        mpmg_set_error("step %lld's ring slot was overwritten by step %lld before it was read", step_number,
+                       seen);
         return MPMG_ERR_INVALID;
     }
     std::atomic_thread_fence(std::memory_order_acquire);
+    if (copy != nullptr) copy(out, slot + 16, body_bytes);
+    else memcpy(out, slot + 16, body_bytes);
+    std::atomic_thread_fence(std::memory_order_acquire);
+    seen = *seq;
+    if (seen != step_number) {
+        mpmg_set_error("step %lld's ring slot was overwritten (sequence %lld) while it was read", step_number,
+                       seen);
+        return MPMG_ERR_INVALID;
+    }
+    return MPMG_OK;
+}
+
+int mpmg_record_ring_wait(mpmg_ctx *ctx, long long step_number, double *t, int *step_out)
+{
+    if (ctx == nullptr || ctx->rring_slots <= 0 || step_number < 1) return MPMG_ERR_INVALID;
+    const unsigned char *slot =
+        ctx->rring_h + (size_t)((step_number - 1) % ctx->rring_slots) * ctx->rring_slot_bytes;
     std::vector<unsigned char> rec(step_record_bytes(ctx));
-    memcpy(rec.data(), slot + 16, rec.size());
-    int rc = take_record(ctx, rec.data());
+    int rc = mpmg_ring_read_slot(slot, rec.size(), step_number, rec.data(), 10.0, nullptr);
+    if (rc == MPMG_ERR_DEVICE) {
+        cudaError_t e = cudaStreamQuery(ctx->stream);
+        if (e != cudaSuccess && e != cudaErrorNotReady) return mpmg_cuda_status(e, "record ring");
+        return rc;
+    }
+    if (rc == MPMG_ERR_INVALID) {
+        mpmg_set_error("step %lld's ring slot was overwritten (read the ring within %d steps)", step_number,
+                       ctx->rring_slots);
+        return rc;
+    }
+    rc = take_record(ctx, rec.data());
     if (rc != MPMG_OK && rc != MPMG_ERR_SOLVER) return rc;
     if (t) *t = ctx->h_params.t;
     if (step_out) *step_out = (int)ctx->h_params.step_count;
@@ -1393,3 +1430,59 @@ int mpmg_launch_count(mpmg_ctx *ctx, long *launches, int reset)
 }
 
 }  // extern "C"
+
+namespace {
+
+// Eight independent FMA chains per thread, so that the FP64 pipe, not the
+// chains' latency, sets the rate.
+__global__ void __launch_bounds__(256) fp64_fma_probe_kernel(double *out, int iters, double a, double b)
+{
+    double x[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) x[c] = (threadIdx.x + c) * 1e-9;
+    for (int k = 0; k < iters; k++) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) x[c] = fma(x[c], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) s += x[c];
+    if (s == 12345.0) out[0] = s;   // never true; keeps the chains live
+}
+
+}  // namespace
+
+extern "C" int mpmg_measure_fp64_rate(int device, double *flops_per_s)
+{
+    if (flops_per_s == nullptr) return MPMG_ERR_INVALID;
+    MPMG_CHECK(cudaSetDevice(device));
+    int sms = 0;
+    MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    double *out = nullptr;
+    MPMG_CHECK(cudaMalloc(&out, sizeof(double)));
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = MPMG_OK;
+    cudaError_t err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double best = 0;
+    for (int r = 0; r < 4 && err == cudaSuccess; r++) {
+        cudaEventRecord(e0, s);
+        fp64_fma_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.999999, 1e-7);
+        cudaEventRecord(e1, s);
+        err = cudaEventSynchronize(e1);
+        float ms = 0;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+        if (err == cudaSuccess && r > 0 && ms > 0) best = std::max(best, flops / (ms * 1e-3));
+    }
+    if (err != cudaSuccess) rc = mpmg_cuda_status(err, "FP64 rate probe");
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    cudaFree(out);
+    *flops_per_s = best;
+    return rc;
+}

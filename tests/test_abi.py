@@ -128,3 +128,66 @@ def test_record_ring_and_adjoint_gradient_reject_bad_arguments():
     assert L.mpmg_record_ring(None, 8) == 16                  # MPMG_ERR_INVALID: no context
     assert L.mpmg_record_ring_wait(None, 1, C.byref(out), C.byref(k)) == 16
     assert L.mpmg_adj_gradient(None, 4, C.byref(out)) == 16
+
+
+COPY_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_size_t)
+
+
+def _ring_reader():
+    fn = mpm2d.lib().mpmg_ring_read_slot
+    fn.argtypes = [C.c_void_p, C.c_size_t, C.c_longlong, C.c_void_p, C.c_double, COPY_FN]
+    fn.restype = C.c_int
+    return fn
+
+
+def _fake_slot(seq, body):
+    import numpy as np
+    slot = np.zeros(2 + body.size, dtype=np.int64)      # 16-byte header, then the body
+    slot[0] = seq
+    slot[2:] = body
+    return slot
+
+
+def test_ring_reader_returns_a_consistent_slot():
+    import numpy as np
+    fn = _ring_reader()
+    body = np.arange(10, dtype=np.int64) * 7
+    slot = _fake_slot(5, body)
+    out = np.zeros_like(body)
+    assert fn(slot.ctypes.data, body.nbytes, 5, out.ctypes.data, 1.0, COPY_FN(0)) == 0
+    np.testing.assert_array_equal(out, body)
+
+
+def test_ring_reader_detects_a_lap_during_the_copy():
+    """A later step that starts rewriting the slot while the host copies it
+    (the sequence word turns -1, then the later step number) must not be
+    returned as this step's record."""
+    import numpy as np
+    fn = _ring_reader()
+    body = np.arange(10, dtype=np.int64)
+    out = np.zeros_like(body)
+    for lapped_to in (-1, 5 + 32):
+        slot = _fake_slot(5, body)
+
+        def copy_then_lap(dst, src, n, slot=slot, lapped_to=lapped_to):
+            C.memmove(dst, src, n)
+            slot[0] = lapped_to            # the GPU reached the slot mid-copy
+
+        cb = COPY_FN(copy_then_lap)
+        assert fn(slot.ctypes.data, body.nbytes, 5, out.ctypes.data, 1.0, cb) == 16
+        assert b"while it was read" in mpm2d.lib().mpmg_last_error()
+
+
+def test_ring_reader_detects_an_overwritten_slot_and_times_out():
+    import numpy as np
+    fn = _ring_reader()
+    body = np.arange(4, dtype=np.int64)
+    out = np.zeros_like(body)
+    slot = _fake_slot(9 + 8, body)            # already holds a later step
+    assert fn(slot.ctypes.data, body.nbytes, 9, out.ctypes.data, 1.0, COPY_FN(0)) == 16
+    assert b"before it was read" in mpm2d.lib().mpmg_last_error()
+    slot = _fake_slot(-1, body)               # a body being written that never completes
+    assert fn(slot.ctypes.data, body.nbytes, 9, out.ctypes.data, 0.05, COPY_FN(0)) == 21   # MPMG_ERR_DEVICE
+    slot = _fake_slot(8, body)                # this step has not arrived
+    assert fn(slot.ctypes.data, body.nbytes, 9, out.ctypes.data, 0.05, COPY_FN(0)) == 21
+    assert fn(None, 8, 1, out.ctypes.data, 0.05, COPY_FN(0)) == 16
