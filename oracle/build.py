@@ -6,7 +6,7 @@
   the read-only reference tree, into ``oracle/_ref/``: ``libmpm_ref.so`` (the
   reference's libmpm), one plugin ``.so`` per material and boundary condition,
   ``libref_harness.so`` (the driver set-up of src/main.c:415-835 without
-  libconfuse) and the ``material_<name>`` executables of tests/test_material.c.
+  libconfuse, linked with the reference's src/writer.c) and the ``material_<name>`` executables of tests/test_material.c.
   It needs the reference tree and is skipped where it is absent.
 
 Two deviations are applied while compiling, never by copying source into this
@@ -28,6 +28,10 @@ BUILD_OUT = os.path.join(HERE, "_build")
 DEFAULT_REFERENCE = "/root/reference"
 
 CFLAGS = ["-O2", "-std=gnu99", "-fPIC", "-ffp-contract=off", "-w"]
+# The reference's own release flags (CMakeLists.txt:4), for timing it only:
+# with contraction left on, its results are not the bit-exact golden source.
+PERF_CFLAGS = ["-O3", "-march=native", "-std=gnu99", "-fPIC", "-w"]
+PERF_OUT = os.path.join(REF_OUT, "perf")
 
 LIBMPM_SOURCES = ["element.c", "interpolate.c", "loading.c", "map.c", "material.c",
                   "particle.c", "process_usl.c", "rtsafe.c", "tensor.c"]
@@ -119,14 +123,49 @@ def build_ref(verbose=False):
         sh(["gcc"] + CFLAGS + inc + ["-shared", "-o", os.path.join(REF_OUT, bc + ".so"),
                                      os.path.join(ref, "bcsrc", bc + ".c")] + link_mpm + ["-lm"])
 
-    sh(["gcc"] + CFLAGS + inc + ["-shared", "-o", os.path.join(REF_OUT, "libref_harness.so"),
-                                 os.path.join(HERE, "ref", "ref_harness.c")] + link_mpm + ["-ldl", "-lpthread", "-lm"])
+    # the harness links the reference's own writer (src/writer.c) for golden frame and state text
+    sh(["gcc"] + CFLAGS + inc + ["-I", os.path.join(ref, "src"), "-shared", "-o",
+                                 os.path.join(REF_OUT, "libref_harness.so"),
+                                 os.path.join(HERE, "ref", "ref_harness.c"), os.path.join(ref, "src", "writer.c")]
+       + link_mpm + ["-ldl", "-lpthread", "-lm"])
 
     for mat in KAT_MATERIALS:
         sh(["gcc"] + CFLAGS + inc + ["-o", os.path.join(REF_OUT, "material_" + mat),
                                      os.path.join(ref, "tests", "test_material.c"),
                                      os.path.join(ref, "materialsrc", mat + ".c")] + link_mpm + ["-lm", "-lpthread"])
     return REF_OUT
+
+
+def build_ref_perf(materials=("isolin", "g_local_mu2"), verbose=False):
+    """Compile the reference's libmpm, the given local materials, the box and
+    square_silo plugins and the harness with the reference's own release
+    flags into oracle/_ref/perf/ (the timed CPU baseline).  Returns the
+    directory, or None when the reference tree is absent."""
+    if not have_reference():
+        return None
+    ref = reference_dir()
+    os.makedirs(PERF_OUT, exist_ok=True)
+    inc = ["-I", os.path.join(HERE, "ref", "include"), "-I", os.path.join(ref, "libmpm")]
+    link_mpm = ["-L", PERF_OUT, "-lmpm_ref"] + ["-Wl,-rpath,$ORIGIN"]
+
+    def sh(cmd):
+        if verbose:
+            print(" ".join(cmd))
+        _run(cmd)
+
+    sh(["gcc"] + PERF_CFLAGS + inc + ["-shared", "-o", os.path.join(PERF_OUT, "libmpm_ref.so")]
+       + [os.path.join(ref, "libmpm", f) for f in LIBMPM_SOURCES] + ["-lm", "-lpthread"])
+    for mat in materials:
+        sh(["gcc"] + PERF_CFLAGS + inc + ["-shared", "-o", os.path.join(PERF_OUT, mat + ".so"),
+                                          os.path.join(ref, "materialsrc", mat + ".c")] + link_mpm + ["-lm"])
+    for bc in BCS:
+        sh(["gcc"] + PERF_CFLAGS + inc + ["-shared", "-o", os.path.join(PERF_OUT, bc + ".so"),
+                                          os.path.join(ref, "bcsrc", bc + ".c")] + link_mpm + ["-lm"])
+    sh(["gcc"] + PERF_CFLAGS + inc + ["-I", os.path.join(ref, "src"), "-shared", "-o",
+                                      os.path.join(PERF_OUT, "libref_harness.so"),
+                                      os.path.join(HERE, "ref", "ref_harness.c"), os.path.join(ref, "src", "writer.c")]
+       + link_mpm + ["-ldl", "-lpthread", "-lm"])
+    return PERF_OUT
 
 
 if __name__ == "__main__":

@@ -210,17 +210,20 @@ REFH_FIELDS = ["x", "y", "xl", "yl", "v", "m", "vx", "vy", "ax", "ay", "bx", "by
 REFH_NODE_FIELDS = ["node_m", "node_mx", "node_my", "node_fx", "node_fy", "node_vx",
                     "node_vy", "node_ax", "node_ay"]
 
-_ref = None
+_ref = {}
 
 
 def ref_available():
     return os.path.isfile(os.path.join(_build.REF_OUT, "libref_harness.so")) or _build.have_reference()
 
 
-def ref_lib():
-    global _ref
-    if _ref is None:
-        path = os.path.join(_build.REF_OUT, "libref_harness.so")
+def ref_lib(lib_dir=None):
+    """The harness library of the reference build in lib_dir (default the
+    bit-exact build in oracle/_ref; oracle/_ref/perf holds the build with the
+    reference's release flags, loaded in a process of its own)."""
+    lib_dir = lib_dir or _build.REF_OUT
+    if lib_dir not in _ref:
+        path = os.path.join(lib_dir, "libref_harness.so")
         if not os.path.isfile(path):
             if _build.build_ref() is None:
                 raise RuntimeError("reference build unavailable")
@@ -241,8 +244,10 @@ def ref_lib():
         sp = C.POINTER(C.c_size_t)
         L.refh_get_color_lists.argtypes = [C.c_void_p, sp, sp]
         L.refh_destroy.argtypes = [C.c_void_p]
-        _ref = L
-    return _ref
+        L.refh_write.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_size_t, C.c_double]
+        L.refh_write.restype = C.c_int
+        _ref[lib_dir] = L
+    return _ref[lib_dir]
 
 
 class RefHarness:
@@ -250,8 +255,9 @@ class RefHarness:
     unit-square element map, compile-time material constants, reference
     gravity ramp)."""
 
-    def __init__(self, scene, nthreads=1):
-        L = ref_lib()
+    def __init__(self, scene, nthreads=1, lib_dir=None):
+        self._lib_dir = lib_dir or _build.REF_OUT
+        L = ref_lib(self._lib_dir)
         assert scene["Nx"] == scene["Ny"], "the reference grid is N x N"
         assert scene.get("gravity") is None, "the reference ramps gravity"
         p = scene["particles"]
@@ -262,8 +268,8 @@ class RefHarness:
         mprops = np.ascontiguousarray(scene.get("props", [1e6, 0.3]), dtype=np.float64)
         bprops = np.ascontiguousarray(scene.get("bcf", []), dtype=np.float64)
         biprops = np.ascontiguousarray(scene.get("bci", []), dtype=np.int32)
-        mat_so = os.path.join(_build.REF_OUT, scene["material"] + ".so").encode()
-        bc_so = os.path.join(_build.REF_OUT, scene["bc"] + ".so").encode()
+        mat_so = os.path.join(self._lib_dir, scene["material"] + ".so").encode()
+        bc_so = os.path.join(self._lib_dir, scene["bc"] + ".so").encode()
         self._keep = (pin, mprops, bprops, biprops, mat_so, bc_so)
         self._h = L.refh_create(scene["Nx"], scene["h"], self.n, _dptr(pin), mat_so,
                                 _dptr(mprops), len(mprops), bc_so, _dptr(bprops), len(bprops),
@@ -278,21 +284,28 @@ class RefHarness:
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
-            ref_lib().refh_destroy(h)
+            ref_lib(self._lib_dir).refh_destroy(h)
             self._h = None
 
     def step(self, n=1):
-        ref_lib().refh_step(self._h, n)
+        ref_lib(self._lib_dir).refh_step(self._h, n)
+
+    def write(self, path, what, frame=0, time=0.0):
+        """The reference's writer on the job: what = "frame" (write_frame),
+        "element_frame" (write_element_frame) or "state" (write_state)."""
+        code = {"frame": 0, "element_frame": 1, "state": 2}[what]
+        if ref_lib(self._lib_dir).refh_write(self._h, path.encode(), code, frame, time) != 0:
+            raise RuntimeError("refh_write could not open %s" % path)
 
     @property
     def t(self):
-        return ref_lib().refh_time(self._h)
+        return ref_lib(self._lib_dir).refh_time(self._h)
 
     def particles(self):
         out = np.empty((self.n, len(REFH_FIELDS)))
         e = np.empty(self.n, dtype=np.int32)
         a = np.empty(self.n, dtype=np.int32)
-        ref_lib().refh_get_particles(self._h, _dptr(out), _iptr(e), _iptr(a))
+        ref_lib(self._lib_dir).refh_get_particles(self._h, _dptr(out), _iptr(e), _iptr(a))
         d = {k: out[:, i].copy() for i, k in enumerate(REFH_FIELDS)}
         d["in_element"] = e
         d["active"] = a
@@ -301,7 +314,7 @@ class RefHarness:
     def nodes(self):
         nn = self.N * self.N
         out = np.empty((nn, len(REFH_NODE_FIELDS)))
-        ref_lib().refh_get_nodes(self._h, _dptr(out))
+        ref_lib(self._lib_dir).refh_get_nodes(self._h, _dptr(out))
         return {k: out[:, i].copy() for i, k in enumerate(REFH_NODE_FIELDS)}
 
     def elements(self):
@@ -309,12 +322,12 @@ class RefHarness:
         f = np.empty(ne, dtype=np.int32)
         c = np.empty(ne, dtype=np.int32)
         m = np.empty(ne)
-        ref_lib().refh_get_elements(self._h, _iptr(f), _iptr(c), _dptr(m))
+        ref_lib(self._lib_dir).refh_get_elements(self._h, _iptr(f), _iptr(c), _dptr(m))
         return f, c, m
 
     def color_lists(self):
         out = np.empty(max(self.n, 1), dtype=np.uint64)
         lens = np.empty(self.nthreads * 4, dtype=np.uint64)
-        ref_lib().refh_get_color_lists(self._h, out.ctypes.data_as(C.POINTER(C.c_size_t)),
+        ref_lib(self._lib_dir).refh_get_color_lists(self._h, out.ctypes.data_as(C.POINTER(C.c_size_t)),
                                        lens.ctypes.data_as(C.POINTER(C.c_size_t)))
         return out, lens

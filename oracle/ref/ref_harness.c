@@ -366,3 +366,29 @@ void refh_destroy(refh_t *r)
     /* Plugins keep static state; leave them loaded for the process. */
     free(r);
 }
+
+/* src/writer.c:190-201, :205-263 and :266-380, linked into this harness from
+   the reference's own writer.c. */
+void write_frame(FILE *fd, size_t frame, double time, job_t *job);
+void write_element_frame(FILE *fd, size_t frame, double time, job_t *job);
+void write_state(FILE *fd, job_t *job);
+
+/* Writes the job with the reference's writer: what 0 = write_frame, 1 =
+   write_element_frame (both with the given frame number and time), 2 =
+   write_state.  Returns 0, or 1 when the file cannot be opened. */
+int refh_write(refh_t *r, const char *path, int what, size_t frame, double time)
+{
+    FILE *fd = fopen(path, "w");
+    if (fd == NULL) {
+        return 1;
+    }
+    if (what == 0) {
+        write_frame(fd, frame, time, r->job);
+    } else if (what == 1) {
+        write_element_frame(fd, frame, time, r->job);
+    } else {
+        write_state(fd, r->job);
+    }
+    fclose(fd);
+    return 0;
+}

@@ -17,6 +17,14 @@ compiled from its sources, see oracle/build.py) and records:
   step_musl_<case>.npz   the same for explicit_mpm_step_musl_threaded
                          (python tests/golden/gen_golden.py musl records only
                          these)
+  long_config1.npz       config 1 run to the 1000 steps of its benchmark
+                         configuration: particle state, element map and nodal
+                         mass and momentum at steps 500 and 1000
+                         (python tests/golden/gen_golden.py long)
+  writer_<case>.npz      the reference's own src/writer.c output for a
+                         recorded state: write_frame, write_element_frame and
+                         write_state text (python tests/golden/gen_golden.py
+                         writer)
 
 The nonlocal cases run the reference with one thread: with more, its
 g_nonlocal_mu2 solve reads particles other threads are still updating
@@ -180,6 +188,56 @@ def musl_cases():
     print(record_steps("musl_mu2_column", sc, [1, 50, 300], nthreads=4)[1])
 
 
+LONG_PARTICLE_KEYS = ["x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy"]
+LONG_NODE_KEYS = ["node_m", "node_mx", "node_my"]
+
+
+def long_cases():
+    # config 1 over its full 1000 steps (threaded)
+    sc = scenes.config1(seed=0)
+    ref = O.RefHarness(sc, nthreads=4)
+    data = scene_arrays(sc)
+    checkpoints = [500, 1000]
+    data["checkpoints"] = np.asarray(checkpoints, dtype=np.int64)
+    done = 0
+    for c in checkpoints:
+        ref.step(c - done)
+        done = c
+        p = ref.particles()
+        n = ref.nodes()
+        for k in LONG_PARTICLE_KEYS:
+            data["s%d_%s" % (c, k)] = p[k]
+        data["s%d_in_element" % c] = p["in_element"]
+        data["s%d_active" % c] = p["active"]
+        data["s%d_t" % c] = np.array(ref.t)
+        for k in LONG_NODE_KEYS:
+            data["s%d_%s" % (c, k)] = n[k]
+    path = os.path.join(HERE, "long_config1.npz")
+    np.savez_compressed(path, **data)
+    print(path)
+
+
+def writer_cases():
+    # the reference's writer on recorded states: config 1 after 100 steps
+    # (isolin) and the g_local_mu2 column after 300 (nonzero plastic state)
+    cases = [("config1", scenes.config1(seed=0), 100, 4),
+             ("mu2_column", scenes.column(Nx=65, Ny=65, h=1 / 64, width=0.25, height=0.5, material="g_local_mu2",
+                                          rho=2450.0, props=(1e6, 0.3), dt=1e-5, jitter=5e-4, seed=1), 300, 4)]
+    for name, sc, steps, threads in cases:
+        ref = O.RefHarness(sc, nthreads=threads)
+        ref.step(steps)
+        out = {"step": np.array(steps), "t": np.array(ref.t), "frame_number": np.array(3)}
+        with tempfile.TemporaryDirectory() as d:
+            for what in ("frame", "element_frame", "state"):
+                path = os.path.join(d, what + ".txt")
+                ref.write(path, what, frame=3, time=ref.t)
+                with open(path, "rb") as f:
+                    out[what] = np.frombuffer(f.read(), dtype=np.uint8)
+        path = os.path.join(HERE, "writer_%s.npz" % name)
+        np.savez_compressed(path, **out)
+        print(path)
+
+
 def main():
     if obuild.build_ref(verbose=False) is None:
         raise SystemExit("reference tree not found; fixtures can only be generated where it exists")
@@ -200,6 +258,12 @@ def main():
         return
     if sys.argv[1:] == ["reverse"]:
         reverse_cases()
+        return
+    if sys.argv[1:] == ["long"]:
+        long_cases()
+        return
+    if sys.argv[1:] == ["writer"]:
+        writer_cases()
         return
     print(kat("isolin"))
     print(kat("g_local_mu2"))
@@ -261,6 +325,8 @@ def main():
     ext_cases()
     nonlocal_avg_cases()
     reverse_cases()
+    long_cases()
+    writer_cases()
 
 
 if __name__ == "__main__":

@@ -240,3 +240,22 @@ def test_nonlocal_plugins_that_share_code():
             np.testing.assert_array_equal(runs[a][f], runs[b][f])
     assert not np.array_equal(runs["g_nonlocal"]["state3"], runs["g_nonlocal_avg"]["state3"])
 
+
+
+def test_oracle_matches_reference_over_1000_steps():
+    """Configuration 1 over the 1000 steps of its benchmark configuration:
+    the oracle equals the reference's own threaded run bit for bit
+    (tests/golden/long_config1.npz)."""
+    d = np.load(os.path.join(GOLDEN, "long_config1.npz"))
+    sc = scenes.config1(seed=0)
+    orc = O.Oracle(sc, nthreads=4)
+    done = 0
+    for c in (int(c) for c in d["checkpoints"]):
+        orc.step(c - done)
+        done = c
+        for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy", "node_m", "node_mx", "node_my"):
+            np.testing.assert_array_equal(orc.get(f), d["s%d_%s" % (c, f)], err_msg="%d %s" % (c, f))
+        e, a = orc.get_map()
+        np.testing.assert_array_equal(e, d["s%d_in_element" % c])
+        np.testing.assert_array_equal(a, d["s%d_active" % c])
+        assert orc.t == float(d["s%d_t" % c])
