@@ -1,0 +1,191 @@
+"""Parity at the sizes the benchmark configurations name, through the C ABI.
+
+  * The 1 048 576-particle benchmark workload (512^2 elements filled at 2x2,
+    g_local_mu2, box): the FP64 form against the oracle (the pthreaded CPU
+    restatement of explicit_mpm_step_usl_threaded, run on every host core)
+    after 1, 3 and 25 steps -- element keys and active flags bit-exact, the
+    per-element particle order that of find_filled_elements
+    (process_usl.c:677-723), nodal mass and momentum and particle stress,
+    position and velocity within 1e-10 of the field group's magnitude.
+  * The same workload in both mixed forms against the oracle after 100 steps:
+    relative L2 error per field <= 1e-4.
+  * Configuration 1 (isolin block, 4096 particles, 65^2 nodes) over its full
+    1000 steps against the reference's own run (golden long_config1.npz).
+  * The 835 996-particle g_nonlocal_mu2 silo on 513^2 nodes: one step
+    teacher-forced from the GPU's state after three steps, against the oracle,
+    whose fluidity solve is a banded LDL^T factorisation of the same
+    assembled matrix (the substitute for CXSparse's cs_lusol,
+    g_nonlocal_mu2.c:510-519); the GPU's Jacobi-PCG at the production
+    tolerance (relative residual 1e-10) and at 1e-13.
+
+Set MPMG_PARITY_REPORT to a file path to have the measured errors appended
+there as JSON lines.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, field_err, rel_err
+from oracle import oracle as O
+import mpm2d
+import scenes
+
+pytestmark = pytest.mark.gpu
+
+ONE_STEP_TOL = 1e-10
+THREADS = os.cpu_count() or 1
+
+
+def report(name, values):
+    path = os.environ.get("MPMG_PARITY_REPORT")
+    print(name, json.dumps(values))
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps({"test": name, **values}) + "\n")
+
+
+def bench_scene():
+    return scenes.box_fill(cells=512, ppc_1d=2, material="g_local_mu2", rho=2450.0, props=(1e6, 0.3), dt=2e-6)
+
+
+def test_fp64_bench_workload_vs_oracle():
+    sc = bench_scene()
+    sim = mpm2d.Simulation(sc, store_transients=True)
+    orc = O.Oracle(sc, nthreads=THREADS)
+    done = 0
+    errs = {}
+    for c in (1, 3, 25):
+        sim.step(c - done)
+        orc.step(c - done)
+        done = c
+        e, a = sim.get_map()
+        oe, oa = orc.get_map()
+        np.testing.assert_array_equal(e, oe)
+        np.testing.assert_array_equal(a, oa)
+        # find_filled_elements' order: per element, ascending particle index
+        keys, perm, start = sim.get_sort()
+        act = np.flatnonzero(oa == 1)
+        want_perm = act[np.lexsort((act, oe[act]))]
+        np.testing.assert_array_equal(perm[: act.size], want_perm)
+        np.testing.assert_array_equal(np.diff(start), np.bincount(oe[act], minlength=sim.ne))
+        assert sim.t == orc.t
+        ce = {}
+        for f in ("node_m", "node_mx", "node_my", "node_fx", "node_fy", "x", "y", "vx", "vy", "v",
+                  "sxx", "sxy", "syy", "Tzz", "state9", "state10"):
+            ce[f] = field_err(sim.get(f), orc.get, f)
+            assert ce[f] <= ONE_STEP_TOL, (c, f, ce[f])
+        errs["step%d" % c] = ce
+    report("fp64_bench_workload_vs_oracle", {"particles": sim.n, "max_err": {
+        k: max(v.values()) for k, v in errs.items()}, "errors": errs})
+    sim.close()
+
+
+def rel_l2(a, b, scale):
+    return float(np.linalg.norm(a - b) / scale) if scale > 0 else float(np.linalg.norm(a - b))
+
+
+ACC_GROUPS = {"x": ("x", "y"), "y": ("x", "y"), "vx": ("vx", "vy"), "vy": ("vx", "vy"),
+              "ux": ("ux", "uy"), "uy": ("ux", "uy"), "sxx": ("sxx", "sxy", "syy"),
+              "sxy": ("sxx", "sxy", "syy"), "syy": ("sxx", "sxy", "syy"), "v": ("v",)}
+
+
+def test_mixed_bench_workload_vs_oracle_100_steps():
+    """The mixed forms' relative L2 error per field after 100 steps of the
+    benchmark workload, against the FP64 oracle (a field of a physical
+    group, such as sxy, scaled by the group's largest norm)."""
+    sc = bench_scene()
+    orc = O.Oracle(sc, nthreads=THREADS)
+    orc.step(100)
+    want = {f: orc.get(f) for f in ACC_GROUPS}
+    out = {}
+    for precision in ("mixed_f64node", "mixed"):
+        sim = mpm2d.Simulation(sc, precision=precision)
+        sim.step(100)
+        err = {}
+        for f, grp in ACC_GROUPS.items():
+            scale = max(np.linalg.norm(want[g]) for g in grp)
+            err[f] = rel_l2(sim.get(f), want[f], scale)
+        sim.close()
+        out[precision] = err
+        assert max(err.values()) <= 1e-4, (precision, err)
+    report("mixed_bench_workload_vs_oracle_100_steps", out)
+
+
+def test_config1_1000_steps_vs_reference():
+    """Configuration 1 over the full 1000 steps of its benchmark
+    configuration against the reference's own threaded run."""
+    d = np.load(os.path.join(GOLDEN, "long_config1.npz"))
+    sc = scenes.config1(seed=0)
+    for k in ("m", "v", "x", "y"):
+        np.testing.assert_array_equal(sc["particles"][k], d["in_" + k])
+    sim = mpm2d.Simulation(sc, store_transients=True)
+    done = 0
+    errs = {}
+    for c in (int(c) for c in d["checkpoints"]):
+        sim.step(c - done)
+        done = c
+        e, a = sim.get_map()
+        np.testing.assert_array_equal(e, d["s%d_in_element" % c])
+        np.testing.assert_array_equal(a, d["s%d_active" % c])
+        assert sim.t == float(d["s%d_t" % c])
+        want = lambda f, c=c: d["s%d_%s" % (c, f)]
+        ce = {}
+        for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy", "node_m", "node_mx", "node_my"):
+            ce[f] = field_err(sim.get(f), want, f)
+        errs["step%d" % c] = ce
+        # one-step parity compounds over the run: 1e-9 at 1000 steps
+        assert max(ce.values()) <= 1e-9, (c, ce)
+    report("config1_1000_steps_vs_reference", errs)
+    sim.close()
+
+
+NL_FIELDS = ("sxx", "sxy", "syy", "x", "y", "vx", "vy", "v", "state3", "state9", "state10")
+
+
+def test_c3_silo_teacher_forced_step_vs_direct_solve():
+    sc = scenes.silo_prestressed(cells=512)
+    warm = mpm2d.Simulation(sc, store_transients=True)
+    warm.step(3)
+    warm.synchronize()
+    e, a = warm.get_map()
+    st = {f: warm.get(f) for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy", "ux", "uy")}
+    for k in (0, 3, 4, 5, 6, 9, 10):
+        st["state%d" % k] = warm.get("state%d" % k)
+    t, count = warm.t, warm.step_count
+    warm.close()
+
+    def start_state(sim):
+        for f, v in st.items():
+            sim.set(f, v)
+        sim.set_map(e, a)
+        sim.set_time(t, count)
+
+    orc_sc = dict(sc)
+    orc_sc["particles"] = dict(sc["particles"])
+    orc = O.Oracle(orc_sc, nthreads=THREADS, solver="direct")
+    start_state(orc)
+    orc.step(1)
+    want = {f: orc.get(f) for f in NL_FIELDS + ("node_gf",)}
+    out = {"particles": int(a.sum()), "dofs_with_mass": int(np.count_nonzero(orc.get("node_m") > 0))}
+    for tol in (1e-10, 1e-13):
+        sim = mpm2d.Simulation(sc, store_transients=True, solver_tol=tol, solver_maxit=50000)
+        start_state(sim)
+        sim.step(1)
+        rc, iters, resid = sim.last_solve()
+        assert rc == 0 and resid <= tol
+        np.testing.assert_array_equal(sim.get_map()[1], orc.get_map()[1])
+        gf_err = rel_err(sim.get("node_gf"), want["node_gf"])
+        ferr = {f: field_err(sim.get(f), want.get, f) if f not in ("state3",) else
+                rel_err(sim.get(f), want[f]) for f in NL_FIELDS}
+        out["tol_%g" % tol] = {"iterations": iters, "rel_residual": resid, "node_gf_err": gf_err,
+                               "error_over_residual": gf_err / resid if resid > 0 else None, "fields": ferr}
+        sim.close()
+        # positions and velocities do not depend on this step's solve
+        for f in ("x", "y", "vx", "vy", "v"):
+            assert ferr[f] <= ONE_STEP_TOL, (tol, f, ferr[f])
+        bound = 1e-6 if tol == 1e-10 else 1e-9
+        for f in ("sxx", "sxy", "syy", "state3"):
+            assert ferr[f] <= bound, (tol, f, ferr[f])
+    report("c3_silo_teacher_forced_step_vs_direct_solve", out)

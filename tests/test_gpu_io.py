@@ -139,3 +139,88 @@ def test_element_frame_rows(tmp_path, precision):
         assert lines[k + 1] == " ".join(_fmt_g(x) for x in corners + vals), k
     assert any(float(l.split()[8]) != 0 for l in lines[1:])
 
+
+
+# The reference's own writer (src/writer.c, compiled into the oracle's
+# reference harness) on recorded states: tests/golden/writer_<case>.npz holds
+# its write_frame, write_element_frame and write_state text for config 1
+# after 100 steps and the g_local_mu2 column after 300, the states that
+# step_config1.npz and step_mu2_column.npz record.
+WRITER_CASES = [("config1", 100), ("mu2_column", 300)]
+
+
+def _restarted(case, step):
+    from conftest import load_golden
+    from test_gpu_parity import restart_sim
+    scene, d = load_golden(case)
+    sim = restart_sim(scene, d, step)
+    for f in ("exx", "exy", "eyy", "wxy"):
+        sim.set(f, d["s%d_%s" % (step, f)])
+    return sim, d
+
+
+def _golden_text(case, what):
+    import os
+    from conftest import GOLDEN
+    w = np.load(os.path.join(GOLDEN, "writer_%s.npz" % case))
+    return w[what].tobytes(), float(w["t"]), int(w["frame_number"])
+
+
+@pytest.mark.parametrize("case,step", WRITER_CASES)
+def test_frame_text_equals_reference_writer(tmp_path, case, step):
+    """mpmg_write_frame writes write_frame's text byte for byte."""
+    sim, _ = _restarted(case, step)
+    want, t, frame = _golden_text(case, "frame")
+    path = tmp_path / "frame.txt"
+    sim.write_frame(path, frame, t)
+    got = path.read_bytes()
+    assert len(got) == len(want)
+    assert got == want
+
+
+@pytest.mark.parametrize("case,step", WRITER_CASES)
+def test_element_frame_text_equals_reference_writer(tmp_path, case, step):
+    """mpmg_write_element_frame writes write_element_frame's text byte for
+    byte (volume-weighted element stresses summed in particle order)."""
+    sim, _ = _restarted(case, step)
+    want, t, frame = _golden_text(case, "element_frame")
+    path = tmp_path / "elements.txt"
+    sim.write_element_frame(path, frame, t)
+    assert path.read_bytes() == want
+
+
+def test_state_values_equal_reference_writer(tmp_path):
+    """mpmg_write_state writes write_state's layout with every value exact
+    ("%.17g", for exact restarts) where the reference prints "%lg": each value
+    printed with "%lg" gives the reference's token.  The local coordinates
+    (xl, yl) are exempt: the reference writes the start-of-step coordinates
+    of its last step, this library the coordinates of the current position in
+    the current element."""
+    sim, d = _restarted("config1", 100)
+    want, t, _ = _golden_text("config1", "state")
+    path = tmp_path / "state.txt"
+    sim.write_state(path, t_stop=0.0)
+    ref_tok = want.decode().split()
+    got_tok = path.read_text().split()
+    assert len(got_tok) == len(ref_tok)
+    n = sim.n
+    per_particle = 38          # x y, xl yl, x_t y_t, m, v, v0, s*3, e*4, bx by, F*4, ux uy, color, DEPVAR, 11 state, active
+    head = 8
+    exempt = set()
+    for i in range(n):
+        exempt.update((head + i * per_particle + 2, head + i * per_particle + 3))
+    # the header's t_stop is the caller's
+    exempt.add(2)
+    bad = []
+    for k, (g, r) in enumerate(zip(got_tok, ref_tok)):
+        if k in exempt:
+            continue
+        if g == r:
+            continue
+        try:
+            if "%lg" % float(g) == r:
+                continue
+        except ValueError:
+            pass
+        bad.append((k, g, r))
+    assert not bad, bad[:10]
