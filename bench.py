@@ -5,23 +5,30 @@ element on a 513x513-node grid (512^2 elements), g_local_mu2 granular rheology
 (rho 2450, E 1e6, nu 0.3, reference constants), box walls, synthetic seeded
 inputs in the reference generator's lattice layout.  A step is one
 explicit_mpm_step_usl_threaded + time_varying_loads over all particles.  The
-headline runs the mixed-precision form (FP32 particle state and particle
-arithmetic, float-float nodal mass/momentum sums and division); the plain
-FP64 form is measured beside it ("fp64"), and the mixed form with FP64 nodal
-sums ("mixed_f64node").  Particle state and per-step scratch exceed
-the 129 MB L2 (~170 MB mixed, ~300 MB FP64), so no flush is needed.
+headline runs the plain FP64 form, the reference's own arithmetic, so that it
+compares like for like with the reference's FP64 CPU step; the mixed forms
+(FP32 particle state and arithmetic with FP64 nodal sums, "mixed_f64node",
+the chosen form, and with float-float nodal sums, "mixed") are measured
+beside it.  Particle state and per-step scratch exceed the 129 MB L2 (~300 MB
+FP64, ~170 MB mixed), so no flush is needed between steps.
 
-  value     particle-steps/s of the mixed form with the state resident in HBM
-            (CUDA events on the library's stream, max over ranks)
+  value     particle-steps/s of the FP64 form with the state resident in HBM
+            (CUDA events on the library's stream over CUDA-graph steps, max
+            over ranks)
   e2e       the same metric through the public C ABI with host buffers over
             a 500-step run: the timed region includes creating the context
             from host arrays (H2D of the particle state), a D2H read of each
             step's result (time, step count, status) after every step, and
             one output frame of the driver's particle fields at the end
-  roofline  the dominant kernel's algorithmic bytes per launch over its
-            average CUDA-event duration, against the measured HBM copy peak
+  roofline  the dominant kernel (the FP64 G2P + material update): its
+            algorithmic bytes per launch over its CUDA-event duration against
+            the measured HBM copy peak, and, since it is bound by the FP64
+            pipe, its FP64 operations per launch against the measured FP64
+            FMA rate
   cpu_baseline  the oracle (the CPU restatement of the reference's pthreaded
-            step) on this host's cores over a bounded sample of steps
+            step) on this host's cores over a bounded sample of steps, at all
+            cores and at one; the compiled reference is slower than the port
+            by the factor oracle/time_reference.py measured
 
 --impl reference times the reference's CPU step (the oracle port on hosts
 without the reference build) on all host cores, same metric and config.
@@ -51,24 +58,17 @@ UNIT = "particle-steps/s"
 WORKLOAD = "box_fill_1M_g_local_mu2"
 
 # Algorithmic bytes per unit of work of each phase (each array read or written
-# once per use; node gathers counted once per node).  Mixed form, g_local_mu2:
-#   bin   count fused into the previous G2P; scatter reads the key (4 B) and
-#         writes slot + sorted key (8 B); the P2G's ordering reads the slot and
-#         writes perm (8 B): 20 B per particle; scan: bins read + cursor,
-#         cell_start written, bins zeroed (16 B per element)
-#   p2g   P2G and grid update in one kernel (the corner sums stay in shared
-#         memory): perm 4 + xl yl m vx vy v sxx sxy syy 36 = 40 B per
-#         particle; float-float mass + float4 node = 24 B per node written
-#   g2p   perm 4 + sorted key 4 + 13 floats 52 + pid 4 read, 14 floats 56 +
-#         element 4 + pid 4 written = 128 B per particle; float4 node 16 B per
-#         node read
-MIXED_BYTES = {
-    "sort": (20, 16, 0),    # (per particle, per element, per node)
-    "p2g": (40, 0, 24),
-    "g2p": (128, 0, 16),
-}
+# once per use; node gathers counted once per node), as (per particle, per
+# element, per node).
+#
 # FP64 form, g_local_mu2: keys read x y active (20 B) and write element,
-# active, key (12 B) per particle; the rest as above with 8-byte values.
+# active, key (12 B) per particle; the sort's scatter reads the key and writes
+# slot + sorted key, the P2G's ordering reads the slot and writes perm (20 B
+# per particle; bins read, cursor and offsets written, 16 B per element); the
+# P2G reads perm and 9 particle doubles and writes 4 corners x 5 sums; the
+# grid update reads them back and writes 5 doubles per node; the G2P reads
+# element + 13 doubles and writes 13 doubles per particle and gathers 4
+# doubles per node.
 FP64_BYTES = {
     "keys": (32, 0, 0),
     "sort": (20, 16, 0),
@@ -76,13 +76,54 @@ FP64_BYTES = {
     "grid": (0, 160, 40),
     "g2p": (13 * 8 + 8 + 13 * 8, 0, 32),
 }
+# The survey's compulsory bytes of the FP64 step (each persistent field read
+# and written once, sort scratch and transients excluded): 216 B per
+# particle-step for g_local_mu2 and 80 B per node-step.
+FP64_STEP_SURVEY_BYTES = (216, 0, 80)
 
+# Mixed form, g_local_mu2 (the builder's accounting of what the kernels move):
+#   sort  count fused into the previous G2P; scatter reads the key (4 B) and
+#         writes slot + sorted key (8 B); the P2G's ordering reads the slot and
+#         writes perm (8 B): 20 B per particle; scan: bins read + cursor,
+#         cell_start written, bins zeroed (16 B per element)
+#   p2g   P2G and grid update in one kernel (the corner sums stay in shared
+#         memory): perm 4 + xl yl m vx vy v sxx sxy syy 36 = 40 B per
+#         particle; nodal mass + float4 node = 24 B (float-float) or 32 B
+#         (FP64 nodal sums) per node
+#   g2p   perm 4 + sorted key 4 + 13 floats 52 + pid 4 read, 14 floats 56 +
+#         element 4 + pid 4 written = 128 B per particle; float4 node 16 B per
+#         node read
+MIXED_BYTES = {
+    "sort": (20, 16, 0),
+    "p2g": (40, 0, 24),
+    "g2p": (128, 0, 16),
+}
+# The survey's compulsory bytes of the mixed step, which exclude perm, key and
+# particle index (index and sort scratch): 112 B per particle-step for
+# g_local_mu2, 64 B per node-step; of those the G2P moves the particle state
+# (13 floats read, 13 written = 104 B) and the node gathers (16 B per node).
+MIXED_STEP_SURVEY_BYTES = (112, 0, 64)
+MIXED_G2P_SURVEY_BYTES = (104, 0, 16)
+
+# FP64 operations (DADD + DMUL + 2 x DFMA) per particle of the FP64 G2P +
+# g_local_mu2 on this workload after the warm-up steps, from one ncu capture
+# of g2p_kernel<1,0> (None until measured).
+G2P64_FLOPS_PER_PARTICLE = None
 
 # DRAM bytes (read + write) of one mx_g2p_kernel launch on this workload from
-# one ncu capture (profiles/ncu_mixed_step_box_fill_1M_g_local_mu2.md):
-# 80.8 MB read + 17.0 MB written; writes still in L2 at the kernel's end are
-# not in the figure.
+# one ncu capture: 80.8 MB read + 17.0 MB written; writes still in L2 at the
+# kernel's end are not in the figure.
 G2P_TRAFFIC_BYTES = 97.8e6
+
+# The compiled reference against the oracle port on this workload, same host
+# and thread count (oracle/time_reference.py, 8-core x86-64 development host,
+# the reference built with its release flags -O3 -march=native): the port
+# runs 2.19x the reference's particle-steps/s on 1 thread and 1.64x on 8.  The
+# CPU figures below time the port, so they overstate the reference's speed.
+PORT_OVER_REFERENCE = {"threads_1": 2.19, "threads_8": 1.64,
+                       "how": "oracle/time_reference.py on an 8-core x86-64 host (the GPU host has no "
+                              "reference tree to build): reference with -O3 -march=native vs the port, "
+                              "10 steps of this workload, each leg in its own process"}
 
 
 def phase_bytes(table, phase, n, ne, nn):
@@ -208,12 +249,22 @@ def make_scene():
                            props=(1e6, 0.3), dt=2e-6)
 
 
-def cpu_baseline(scene, steps, threads):
+def bench_config(scene, world):
+    """The workload both arms print (identical keys and values)."""
+    return {"workload": WORKLOAD, "particles": len(scene["particles"]["x"]),
+            "grid_nodes": [scene["Nx"], scene["Ny"]], "material": scene["material"], "bc": scene["bc"],
+            "dt": scene["dt"], "gravity": "reference ramp (loading.c)",
+            "arithmetic": "IEEE FP64 (the reference's)",
+            "l2_policy": "state and step scratch exceed the 129 MB L2 between steps",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+def cpu_baseline(scene, steps, threads, warmup=1):
     """The oracle (CPU restatement of the reference's pthreaded step) on host
     cores over `steps` steps of the full workload."""
     from oracle import oracle as O
     orc = O.Oracle(scene, nthreads=threads)
-    orc.step(1)                                 # warm-up (first-touch of arrays)
+    orc.step(warmup)                            # first-touch of arrays, the gravity ramp's first steps
     t0 = time.perf_counter()
     orc.step(steps)
     dt = time.perf_counter() - t0
@@ -225,31 +276,22 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from oracle import build as obuild
     scene = make_scene()
     threads = os.cpu_count() or 1
     steps = max(1, args.steps)
-    warm = max(0, min(args.warmup, 3))
-    from oracle import oracle as O
-    orc = O.Oracle(scene, nthreads=threads)
-    if warm:
-        orc.step(warm)
-    t0 = time.perf_counter()
-    orc.step(steps)
-    dt = time.perf_counter() - t0
+    value, dt = cpu_baseline(scene, steps, threads, warmup=args.warmup)
     n = len(scene["particles"]["x"])
-    value = n * steps / dt
     # the reference's own objects are built from its sources, which only the
     # development host has; here the oracle (the CPU restatement) is timed
-    kind = "port"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles": n, "grid_nodes": [scene["Nx"], scene["Ny"]],
-                   "material": scene["material"], "bc": scene["bc"], "threads": threads},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": "%d steps of the full %d-particle workload" % (steps, n)},
+        "config": bench_config(scene, world),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d steps of the full %d-particle workload after %d warm-up steps"
+                                   % (steps, n, args.warmup),
+                         "port_over_reference": PORT_OVER_REFERENCE},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -373,54 +415,41 @@ def run_gpu(args):
     def slowest(t):
         return max_over_ranks(torch, t)
 
-    # --- mixed precision (headline) ---------------------------------------
-    sim = mpm2d.Simulation(scene, device=dev, precision="mixed")
-    stream = torch.cuda.ExternalStream(sim.stream(), device=dev)
-    sim.step(args.warmup)
-    sim.synchronize()
-    launches0 = sim.launch_count()
-    sync_all()
-    with ClockSampler(dev) as clocks:
-        ms = time_steps(sim, args.steps, stream, torch)
-        sync_all()
-    launches = sim.launch_count() - launches0
-    clk = clocks.summary()
-    t = slowest(ms / 1e3)
-    value = job_value(n * args.steps, world, t)
-    phases = phase_profile(sim, max(3, min(args.steps, 10)), MIXED_BYTES, n, ne, nn)
-    top = max(phases.items(), key=lambda kv: kv[1]["ms"])
-    step_bytes = sum(phase_bytes(MIXED_BYTES, k, n, ne, nn) for k in MIXED_BYTES)
-    g2p = phases["g2p"]
-
-    # --- plain FP64 form, same workload --------------------------------------
+    # --- plain FP64 form (headline) -------------------------------------------
     sim64 = mpm2d.Simulation(scene, device=dev, precision="fp64")
     stream64 = torch.cuda.ExternalStream(sim64.stream(), device=dev)
     sim64.step(args.warmup)
     sim64.synchronize()
-    fp64_steps = max(3, min(args.steps, 20))
+    launches0 = sim64.launch_count()
     sync_all()
-    ms64 = time_steps(sim64, fp64_steps, stream64, torch)
-    sync_all()
+    with ClockSampler(dev) as clocks:
+        ms64 = time_steps(sim64, args.steps, stream64, torch)
+        sync_all()
+    launches = sim64.launch_count() - launches0
+    clk = clocks.summary()
     t64 = slowest(ms64 / 1e3)
-    value64 = n * fp64_steps * world / t64
-    phases64 = phase_profile(sim64, 3, FP64_BYTES, n, ne, nn)
+    value = job_value(n * args.steps, world, t64)
+    phases64 = phase_profile(sim64, max(3, min(args.steps, 10)), FP64_BYTES, n, ne, nn)
     sim64.close()
+    g2p64 = phases64["g2p"]
+    fp64_peak = mpm2d.fp64_rate(dev)
+    step64_survey = phase_bytes({"s": FP64_STEP_SURVEY_BYTES}, "s", n, ne, nn)
+    roofline = {"bound": "hbm", "kernel": "g2p (FP64 G2P + g_local_mu2, g2p_kernel<1,0>)",
+                "achieved": g2p64["gbs"], "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": g2p64["gbs"] / peak, "traffic": None,
+                "compute_bound": {
+                    "pipe": "fp64", "unit": "FLOP/s", "peak": fp64_peak,
+                    "peak_kind": "measured (mpmg_measure_fp64_rate: independent FMA chains, this GPU)"},
+                "top_phase": max(phases64.items(), key=lambda kv: kv[1]["ms"])[0],
+                "step_survey_bytes": step64_survey,
+                "step_survey_frac": step64_survey / (ms64 / args.steps / 1e3) / 1e9 / peak,
+                "phases": phases64}
+    if G2P64_FLOPS_PER_PARTICLE:
+        fl = G2P64_FLOPS_PER_PARTICLE * n / (g2p64["ms"] / 1e3)
+        roofline["compute_bound"].update({"achieved": fl, "frac": fl / fp64_peak,
+                                          "flops_per_particle": G2P64_FLOPS_PER_PARTICLE})
 
-    # --- mixed form with FP64 nodal sums and division --------------------------
-    simf = mpm2d.Simulation(scene, device=dev, precision="mixed_f64node")
-    streamf = torch.cuda.ExternalStream(simf.stream(), device=dev)
-    simf.step(args.warmup)
-    simf.synchronize()
-    sync_all()
-    msf = time_steps(simf, args.steps, streamf, torch)
-    sync_all()
-    valuef = n * args.steps * world / slowest(msf / 1e3)
-    simf.close()
-
-    # --- end to end through the C ABI with host buffers (mixed) ---------------
-    # (measured before the batch, nonlocal and adjoint sections, whose large
-    # allocations and frees would otherwise slow the first cudaMalloc calls
-    # of a user's fresh run)
+    # --- end to end through the C ABI with host buffers (FP64) ------------------
     # The user's run: create the simulation from host arrays (H2D of the
     # particle state), step in CUDA graphs of 8 steps with every step writing
     # its result (the step record: time, step count, device status) into a
@@ -428,37 +457,85 @@ def run_gpu(args):
     # record on the host one chunk behind (mpmg_record_ring_wait), and write
     # the output frame at the end (mpmg_get_fields of the driver's
     # write_frame fields into pinned host buffers).
-    e2e_steps = args.e2e_steps
-    host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
-    sync_all()
-    t0 = time.perf_counter()
-    sim2 = mpm2d.Simulation(scene, device=dev, precision="mixed")
-    sim2.record_ring(32)
-    t1 = time.perf_counter()
-    last = None
-    pending = []
-    k = 0
-    while k < e2e_steps:
-        c = min(8, e2e_steps - k)
-        sim2.step(c)
+    def e2e_run(precision, e2e_steps):
+        host = {f: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for f in FRAME_FIELDS}
+        sync_all()
+        t0 = time.perf_counter()
+        sim2 = mpm2d.Simulation(scene, device=dev, precision=precision)
+        sim2.record_ring(32)
+        t1 = time.perf_counter()
+        last = None
+        pending = []
+        k = 0
+        while k < e2e_steps:
+            c = min(8, e2e_steps - k)
+            sim2.step(c)
+            for s_ in pending:
+                last = sim2.record_ring_wait(s_)
+            pending = list(range(k + 1, k + c + 1))
+            k += c
         for s_ in pending:
             last = sim2.record_ring_wait(s_)
-        pending = list(range(k + 1, k + c + 1))
-        k += c
-    for s_ in pending:
-        last = sim2.record_ring_wait(s_)
-    t2 = time.perf_counter()
-    assert last[1] == e2e_steps
-    sim2.get_frame(FRAME_FIELDS, out=host)
-    t3 = time.perf_counter()
-    sync_all()
-    e2e_t = slowest(t3 - t0)
-    e2e_parts = {"create_s": t1 - t0, "steps_s": t2 - t1, "frame_s": t3 - t2}
-    sim2.close()
-    e2e_value = n * e2e_steps * world / e2e_t
-    h2d_total = 9 * 8 * n                      # m v x y vx vy sxx sxy syy
-    d2h_frame = len(FRAME_FIELDS) * 8 * n      # the frame's FP64 fields in particle order
-    step_record = 80                           # ring slot: step number + step record + status word
+        t2 = time.perf_counter()
+        assert last[1] == e2e_steps
+        sim2.get_frame(FRAME_FIELDS, out=host)
+        t3 = time.perf_counter()
+        sync_all()
+        e2e_t = slowest(t3 - t0)
+        sim2.close()
+        h2d_total = 9 * 8 * n                      # m v x y vx vy sxx sxy syy
+        d2h_frame = len(FRAME_FIELDS) * 8 * n      # the frame's FP64 fields in particle order
+        step_record = 80                           # ring slot: step number + step record + status word
+        return {"value": n * e2e_steps * world / e2e_t, "unit": UNIT,
+                "h2d_bytes_per_step": h2d_total / e2e_steps,
+                "d2h_bytes_per_step": step_record + d2h_frame / e2e_steps, "steps": e2e_steps,
+                "create_s": t1 - t0, "steps_s": t2 - t1, "frame_s": t3 - t2,
+                "path": "mpmg_create from host arrays, mpmg_step in CUDA graphs of 8 steps, every step's "
+                        "record written by the step into mapped pinned host memory and read on the host "
+                        "(mpmg_record_ring / mpmg_record_ring_wait, one chunk behind), "
+                        "one output frame (mpmg_get_fields of %d fields)" % len(FRAME_FIELDS)}
+
+    e2e = e2e_run("fp64", args.e2e_steps)
+
+    # --- mixed forms (FP32 particles), same workload ------------------------------
+    def mixed_run(precision):
+        sim = mpm2d.Simulation(scene, device=dev, precision=precision)
+        stream = torch.cuda.ExternalStream(sim.stream(), device=dev)
+        sim.step(args.warmup)
+        sim.synchronize()
+        msteps = max(args.steps, 50)
+        sync_all()
+        ms = time_steps(sim, msteps, stream, torch)
+        sync_all()
+        t = slowest(ms / 1e3)
+        phases = phase_profile(sim, max(3, min(args.steps, 10)), MIXED_BYTES, n, ne, nn)
+        sim.close()
+        step_ms = ms / msteps
+        builder = sum(phase_bytes(MIXED_BYTES, k, n, ne, nn) for k in MIXED_BYTES)
+        survey = phase_bytes({"s": MIXED_STEP_SURVEY_BYTES}, "s", n, ne, nn)
+        g2p_survey = phase_bytes({"s": MIXED_G2P_SURVEY_BYTES}, "s", n, ne, nn)
+        g2p_s = phases["g2p"]["ms"] / 1e3
+        return {"value": job_value(n * msteps, world, t), "unit": UNIT, "steps": msteps, "ms_per_step": step_ms,
+                "dtype": "f32 particles",
+                "roofline": {"bound": "hbm", "kernel": "g2p (mx_g2p_kernel)", "unit": "GB/s", "peak": peak,
+                             "g2p_achieved_builder_bytes": phases["g2p"]["gbs"],
+                             "g2p_frac_builder_bytes": phases["g2p"]["gbs"] / peak,
+                             "g2p_achieved_survey_bytes": g2p_survey / g2p_s / 1e9,
+                             "g2p_frac_survey_bytes": g2p_survey / g2p_s / 1e9 / peak,
+                             "traffic": G2P_TRAFFIC_BYTES if n == 1048576 else None,
+                             "step_builder_bytes": builder,
+                             "step_frac_builder_bytes": builder / (step_ms / 1e3) / 1e9 / peak,
+                             "step_survey_bytes": survey,
+                             "step_frac_survey_bytes": survey / (step_ms / 1e3) / 1e9 / peak,
+                             "phases": phases}}
+
+    mixed_f64node = mixed_run("mixed_f64node")
+    mixed_f64node["note"] = ("the chosen form: FP32 particle state, P2G/G2P and material law; FP64 nodal mass "
+                             "and momentum sums and the division by nodal mass")
+    mixed = mixed_run("mixed")
+    mixed["note"] = ("float-float (48-bit) nodal mass and momentum sums and division on the FP32 pipe in place "
+                     "of FP64: a deviation from the chosen form, kept because GB300 runs FP64 at 1/64 of the "
+                     "FP32 rate")
 
 
     # --- accuracy of the mixed form against the FP64 form ------------------------
@@ -654,49 +731,33 @@ def run_gpu(args):
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles": n, "grid_nodes": [scene["Nx"], scene["Ny"]],
-                   "material": scene["material"], "bc": scene["bc"],
-                   "precision": "mixed: FP32 particles, float-float nodal sums",
-                   "l2_policy": "state and step scratch exceed the 129 MB L2 between steps",
-                   "step_launch": "CUDA graphs of 8 steps",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": bench_config(scene, world),
+        "step_launch": "CUDA graphs of 8 steps",
         "gpu_launches": int(launches),
         "clocks": clk,
-        "roofline": {"bound": "hbm", "kernel": "g2p", "achieved": g2p["gbs"], "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": g2p["gbs"] / peak,
-                     "traffic": G2P_TRAFFIC_BYTES if n == 1048576 else None,
-                     "top_phase": top[0],
-                     "step_alg_bytes": step_bytes,
-                     "step_achieved_gbs": step_bytes / (ms / args.steps / 1e3) / 1e9,
-                     "step_frac": step_bytes / (ms / args.steps / 1e3) / 1e9 / peak,
-                     "phases": phases},
-        "fp64": {"value": value64, "unit": UNIT, "steps": fp64_steps, "ms_per_step": ms64 / fp64_steps,
-                 "dtype": "f64", "phases": phases64,
-                 "bound": "fp64 pipe (GB300 FP64 ~1.2 TFLOP/s)"},
-        "mixed_over_fp64": value / value64,
+        "roofline": roofline,
+        "e2e": e2e,
+        "mixed_f64node": mixed_f64node,
+        "mixed": mixed,
+        "mixed_f64node_over_fp64": mixed_f64node["value"] / value,
+        "mixed_over_fp64": mixed["value"] / value,
         "batch": batch_line,
         "accuracy": accuracy_line,
         "adjoint": adjoint_line,
         "nonlocal_silo": nonlocal_line,
-        "mixed_f64node": {"value": valuef, "unit": UNIT, "steps": args.steps, "ms_per_step": msf / args.steps,
-                          "note": "same mixed step with FP64 nodal mass/momentum sums and division"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_total / e2e_steps,
-                "d2h_bytes_per_step": step_record + d2h_frame / e2e_steps, "steps": e2e_steps,
-                **e2e_parts,
-                "path": "mpmg_create from host arrays, mpmg_step in CUDA graphs of 8 steps, every step's "
-                        "record written by the step into mapped pinned host memory and read on the host "
-                        "(mpmg_record_ring / mpmg_record_ring_wait, one chunk behind), "
-                        "one output frame (mpmg_get_fields of %d fields)" % len(FRAME_FIELDS)},
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cb_steps = args.cpu_steps
-        cb, cb_t = cpu_baseline(scene, cb_steps, threads)
-        line["cpu_baseline"] = {"value": cb, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "%d steps of the full %d-particle workload (%.1f s)" % (cb_steps, n, cb_t)}
-    sim.close()
+        cb, cb_t = cpu_baseline(scene, args.cpu_steps, threads)
+        cb1, cb1_t = cpu_baseline(scene, args.cpu_steps_1, 1)
+        line["cpu_baseline"] = {
+            "value": cb, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d steps of the full %d-particle workload (%.1f s)" % (args.cpu_steps, n, cb_t),
+            "threads_all": {"value": cb, "cores": threads, "steps": args.cpu_steps, "seconds": cb_t},
+            "threads_1": {"value": cb1, "cores": 1, "steps": args.cpu_steps_1, "seconds": cb1_t},
+            "port_over_reference": PORT_OVER_REFERENCE}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -711,7 +772,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=60)
+    ap.add_argument("--cpu-steps", type=int, default=60, help="CPU-baseline steps on all host cores")
+    ap.add_argument("--cpu-steps-1", type=int, default=8, help="CPU-baseline steps on one core")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-nonlocal", action="store_true", help="skip the nonlocal silo measurement")
@@ -721,7 +783,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
-        args.warmup = 3
+        args.warmup = 3         # at least three untimed warm-up steps
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -15,9 +15,9 @@
  *
  * Entry points (reference declarations they replace):
  *   mpm_init                          libmpm/process_usl.c:68   (process.h:251)
- *   explicit_mpm_step_usl_threaded    libmpm/process_usl.c:465  (process_usl.h:15)
+ *   explicit_mpm_step_usl_threaded    libmpm/process_usl.c:465  (process_usl.h:14)
  *   explicit_mpm_step_musl_threaded   libmpm/process_usl.c:284  (process_usl.h:13)
- *   find_filled_elements              libmpm/process_usl.c:677  (process_usl.h:18)
+ *   find_filled_elements              libmpm/process_usl.c:677  (process_usl.h:17)
  *   mpm_cleanup                       libmpm/process_usl.c:974  (process.h:253)
  *   initial_loads, time_varying_loads libmpm/loading.c:21,34
  * plus additions that return an int status instead of exiting:

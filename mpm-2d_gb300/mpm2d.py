@@ -171,6 +171,16 @@ def default_params(material):
     return mp
 
 
+def fp64_rate(device=0):
+    """Measured FP64 FMA throughput of the device in FLOP/s
+    (mpmg_measure_fp64_rate)."""
+    L = lib()
+    L.mpmg_measure_fp64_rate.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    out = C.c_double()
+    _check(L.mpmg_measure_fp64_rate(device, C.byref(out)))
+    return out.value
+
+
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_f64node": 2}
 SCHEMES = {"usl": 0, "musl": 1}
 
