@@ -37,6 +37,7 @@
 
 #include "mpmg_fp64_common.cuh"
 #include "mpmg_internal.cuh"
+#include "mpmg_materials.cuh"
 
 namespace {
 
@@ -423,7 +424,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(AdjStep S)
             }
             const double dt = S.dt;
             const double exy = 0.5 * (dxdy + dydx), wxy = 0.5 * (dxdy - dydx);
-            const double ex = exp(dt * (exx + eyy));
+            const double ex = mat::exp_small(dt * (exx + eyy));
             const double Vn = V * ex;
 
             // material
@@ -557,7 +558,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_nl_pre_kernel(AdjStep S)
         const MatParams &p = S.mp;
         const double dt = S.dt, G = p.G, lambda = p.K - 2.0 * G / 3.0;
         const double exy = 0.5 * (dxdy + dydx), wxy = 0.5 * (dxdy - dydx);
-        const double Vn = V * exp(dt * (exx + eyy));
+        const double Vn = V * mat::exp_small(dt * (exx + eyy));
         const double trD = exx + eyy;
         const double sxx_tr = Txx + dt * (lambda * trD + 2.0 * G * exx + 2.0 * wxy * Txy);
         const double sxy_tr = Txy + dt * (2.0 * G * exy - wxy * (Txx - Tyy));

@@ -283,13 +283,58 @@ __device__ __forceinline__ int mpmg_which_element(double xp, double yp, double h
     return (int)(fx + fy * (double)Ex);
 }
 
+// floor(x / h) in integer and FP32 arithmetic, or -1 where that cannot
+// decide it.  x >= 2^-126 (else -1).  The FP32 value of x taken from the top
+// 20 mantissa bits (relative error below 2^-20) times inv_hf = RN32(1 / h)
+// lies within q * 2^-19.8 of x / h; where it is farther than
+// q * 2^-19 + 2^-22 from every integer, x / h, its FP64 product and its FP64
+// quotient all floor to the same integer, which is returned.
+__device__ __forceinline__ int mpmg_floor_quotient_fast(double x, float inv_hf)
+{
+    const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+    if (hi < (897u << 20) || hi >= (1151u << 20)) return -1;
+    const float xf = __uint_as_float((hi - (896u << 20)) << 3);
+    const float q = xf * inv_hf;
+    const float fl = floorf(q);
+    const float fr = q - fl;
+    const float margin = fmaf(q, 0x1p-19f, 0x1p-22f);
+    if (!(fr > margin && fr < 1.0f - margin) || q >= 0x1p22f) return -1;
+    return (int)fl;
+}
+
+// mpmg_which_element with the common case in integer and FP32 arithmetic:
+// the range test on the bit patterns (non-negative doubles order as
+// integers; -0.0 counts as inside, NaN as outside) and each floor from
+// mpmg_floor_quotient_fast; a coordinate that lands near an element edge
+// takes mpmg_which_element.  The result equals mpmg_which_element's for every
+// input.  xmax_bits, ymax_bits are the bit patterns of the (positive) bounds.
+__device__ __forceinline__ int mpmg_which_element_fast(double xp, double yp, double h, double inv_h,
+                                                       float inv_hf, double xmax, double ymax,
+                                                       long long xmax_bits, long long ymax_bits, int Ex, int Ey)
+{
+    const long long bx = __double_as_longlong(xp), by = __double_as_longlong(yp);
+    const long long mag = 0x7fffffffffffffffLL;
+    const bool in_x = (bx >= 0 || bx == (long long)0x8000000000000000ULL) && (bx & mag) < xmax_bits;
+    const bool in_y = (by >= 0 || by == (long long)0x8000000000000000ULL) && (by & mag) < ymax_bits;
+    if (!(in_x && in_y)) return -1;
+    const int fx = mpmg_floor_quotient_fast(xp, inv_hf);
+    const int fy = mpmg_floor_quotient_fast(yp, inv_hf);
+    if (fx < 0 || fy < 0) return mpmg_which_element(xp, yp, h, inv_h, xmax, ymax, Ex, Ey);
+    if (fx >= Ex || fy >= Ey) return -1;
+    return fx + fy * Ex;
+}
+
 // Local coordinates in the element with bottom-left node at (xn, yn), with
 // the reference's snap to +-1 within 1e-10 (particle.c:14-30).
+// |xl| > 1 is tested on the bit pattern (positive doubles order as
+// integers), so that the common case costs no FP64 compare.
 __device__ __forceinline__ double mpmg_local_coord(double xp, double xn, double inv_h)
 {
     double xl = (xp - xn) * inv_h;
-    double sg = copysign(1.0, xl);
-    if ((sg * xl) > 1.0 && ((sg * xl) - 1.0) < MPMG_TOL) xl = sg;
+    if ((__double_as_longlong(xl) & 0x7fffffffffffffffLL) > 0x3ff0000000000000LL) {
+        double sg = copysign(1.0, xl);
+        if (((sg * xl) - 1.0) < MPMG_TOL) xl = sg;
+    }
     return xl;
 }
 

@@ -13,9 +13,47 @@ __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, 
 __device__ __forceinline__ double sub(double a, double b) { return __dadd_rn(a, -b); }
 __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
 
+// a / b where the divisor b is fixed for the run and y = RN(1 / b) was
+// formed once on the host.  Markstein's correction q' = RN(q + r y), with the
+// residual r = a - b q exact through an FMA, is applied twice from q = RN(a y):
+// the first brings q within one ulp of a / b, and from there the second
+// returns the correctly rounded quotient (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990).  Five FP64 operations in place of a full division; the
+// result equals dvd(a, b) for normal operands and quotients (a zero quotient
+// comes out +0, and non-finite operands are not carried through).
+__device__ __forceinline__ double dvd_known(double a, double b, double y)
+{
+    double q = __dmul_rn(a, y);
+    double r = __fma_rn(-b, q, a);
+    q = __fma_rn(r, y, q);
+    r = __fma_rn(-b, q, a);
+    return __fma_rn(r, y, q);
+}
+
+constexpr double kThird = 1.0 / 3.0;   // RN(1/3), the reciprocal of the divisor 3.0
+
 struct Elastic {
     double G, K, lambda, dt;
+    double inv_G, inv_dt;   // RN(1/G), RN(1/dt)
 };
+
+// exp(x) for the volume update v <- v exp(dt tr D), whose argument is tiny at
+// any stable time step: where |x| < 2^-9 the degree-5 Taylor polynomial about
+// 0 in Horner form (truncation below x^6 / 720 < 2^-63, under a tenth of an
+// ulp of the result, so the result lies within about half an ulp of e^x);
+// elsewhere exp().
+__device__ __forceinline__ double exp_small(double x)
+{
+    if ((__double2hiint(x) & 0x7fffffff) < 0x3f600000) {
+        double p = __fma_rn(x, 1.0 / 120.0, 1.0 / 24.0);
+        p = __fma_rn(p, x, 1.0 / 6.0);
+        p = __fma_rn(p, x, 0.5);
+        p = __fma_rn(p, x, 1.0);
+        return __fma_rn(p, x, 1.0);
+    }
+    return exp(x);
+}
 
 // isolin calculate_stress_threaded, materialsrc/isolin.c:75-116.
 __device__ __forceinline__ void isolin(const Elastic &el, double exx, double exy, double eyy,
@@ -45,6 +83,7 @@ __device__ __forceinline__ double negative_root(double a, double b, double c)
 
 struct Mu2Params {
     double mu_s, mu_2, I0, grains_rho, grains_d, rho_critical, A;
+    double inv_grains_rho, inv_grains_d;   // RN(1/grains_rho), RN(1/grains_d)
 };
 
 // g_local_mu2 calculate_stress_threaded, g_local_mu2.c:165-310, written for
@@ -58,7 +97,7 @@ __device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &
                                             double &Tzz, double &gammap, double &gammadotp)
 {
     const double G = el.G, dt = el.dt;
-    const double lambda = sub(el.K, dvd(mul(2.0, G), 3.0));
+    const double lambda = el.lambda;   // K - 2 G / 3, formed on the host with the same roundings
     // L (:191-199), W = skw(L), D = sym(L) (tensor.c:330-384)
     double Lxy = add(exy, wxy), Lyx = sub(exy, wxy);
     double Wxy = mul(0.5, sub(Lxy, Lyx));
@@ -78,7 +117,7 @@ __device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &
     double Tyy_tr = add(mul(add(add(mul(Dyy, twoG), lt), JSyy), dt), Tyy);
     double Tzz_tr = add(mul(add(mul(0.0, twoG), lt), dt), Tzz);
     // decompose and contract (:225-228; tensor.c:205-224, :422-437)
-    double p_tr = dvd(add(add(Txx_tr, Tyy_tr), Tzz_tr), 3.0);
+    double p_tr = dvd_known(add(add(Txx_tr, Tyy_tr), Tzz_tr), 3.0, kThird);
     double T0xx = sub(Txx_tr, p_tr), T0xy = Txy_tr, T0yy = sub(Tyy_tr, p_tr), T0zz = sub(Tzz_tr, p_tr);
     double tt = add(add(add(add(mul(T0xx, T0xx), mul(T0xy, T0xy)), mul(T0xy, T0xy)), mul(T0yy, T0yy)),
                     mul(T0zz, T0zz));
@@ -91,24 +130,36 @@ __device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &
         nup_tau = 0;
         Txx = 0; Txy = 0; Tyy = 0; Tzz = 0;
     } else if (p_tr > 0) {
-        double tau_tau, scale_factor;
         double S0 = mul(mp.mu_s, p_tr);
-        if (tau_tr <= S0) {
-            tau_tau = tau_tr;
-            scale_factor = 1.0;
+        if (tau_tr <= S0 && isfinite(tau_tr)) {
+            // tau_tau = tau_tr, scale factor 1: (tau_tr - tau_tau) / G / dt
+            // is +0 and T0 * 1 is T0 exactly, so neither is formed
+            nup_tau = 0;
+            Txx = sub(T0xx, p_tr);
+            Txy = T0xy;
+            Tyy = sub(T0yy, p_tr);
+            Tzz = sub(T0zz, p_tr);
         } else {
-            double S2 = mul(mp.mu_2, p_tr);
-            double alpha = dvd(mul(mul(mul(G, mp.I0), dt), __dsqrt_rn(dvd(p_tr, mp.grains_rho))), mp.grains_d);
-            double B = -add(add(S2, tau_tr), alpha);
-            double H = add(mul(S2, tau_tr), mul(S0, alpha));
-            tau_tau = negative_root(1.0, B, H);
-            scale_factor = dvd(tau_tau, tau_tr);
+            double tau_tau, scale_factor;
+            if (tau_tr <= S0) {
+                tau_tau = tau_tr;
+                scale_factor = 1.0;
+            } else {
+                double S2 = mul(mp.mu_2, p_tr);
+                double alpha = dvd_known(mul(mul(mul(G, mp.I0), dt),
+                                             __dsqrt_rn(dvd_known(p_tr, mp.grains_rho, mp.inv_grains_rho))),
+                                         mp.grains_d, mp.inv_grains_d);
+                double B = -add(add(S2, tau_tr), alpha);
+                double H = add(mul(S2, tau_tr), mul(S0, alpha));
+                tau_tau = negative_root(1.0, B, H);
+                scale_factor = dvd(tau_tau, tau_tr);
+            }
+            nup_tau = dvd_known(dvd_known(sub(tau_tr, tau_tau), G, el.inv_G), dt, el.inv_dt);
+            Txx = sub(mul(T0xx, scale_factor), p_tr);
+            Txy = mul(T0xy, scale_factor);
+            Tyy = sub(mul(T0yy, scale_factor), p_tr);
+            Tzz = sub(mul(T0zz, scale_factor), p_tr);
         }
-        nup_tau = dvd(dvd(sub(tau_tr, tau_tau), G), dt);
-        Txx = sub(mul(T0xx, scale_factor), p_tr);
-        Txy = mul(T0xy, scale_factor);
-        Tyy = sub(mul(T0yy, scale_factor), p_tr);
-        Tzz = sub(mul(T0zz, scale_factor), p_tr);
     } else {
         nup_tau = 0;   // NaN pressure: the reference prints 'u' and keeps T
     }
@@ -139,7 +190,7 @@ __device__ __forceinline__ void plane_return(const Elastic &el, const ReturnPara
                                              double &gammap, double &gammadotp)
 {
     const double G = el.G, K = el.K, dt = el.dt;
-    const double lambda = sub(K, dvd(mul(2.0, G), 3.0));
+    const double lambda = el.lambda;   // K - 2 G / 3, formed on the host with the same roundings
     const double twoG = mul(2.0, G);
     double trD = add(exx, eyy);
     double dsjxx = add(mul(lambda, trD), mul(twoG, exx));

@@ -37,7 +37,7 @@ using fp64::shape;
 // ---------------------------------------------------------------------------
 // keys
 
-__global__ void __launch_bounds__(256) keys_kernel(GridGeom g, int n, const double *__restrict__ x,
+__global__ void __launch_bounds__(256) keys_kernel(GridGeom g, float inv_hf, int n, const double *__restrict__ x,
                                                    const double *__restrict__ y, int *__restrict__ in_element,
                                                    int *__restrict__ active, uint32_t *__restrict__ keys,
                                                    uint32_t sentinel, uint32_t *__restrict__ bins, StepParams *sp,
@@ -66,7 +66,9 @@ __global__ void __launch_bounds__(256) keys_kernel(GridGeom g, int n, const doub
     uint32_t key = sentinel;
     if (i < n) {
         if (active[i]) {
-            int e = mpmg_which_element(x[i], y[i], g.h, g.inv_h, g.xmax, g.ymax, g.Ex, g.Ey);
+            int e = mpmg_which_element_fast(x[i], y[i], g.h, g.inv_h, inv_hf, g.xmax, g.ymax,
+                                            __double_as_longlong(g.xmax), __double_as_longlong(g.ymax), g.Ex,
+                                            g.Ey);
             in_element[i] = e;
             if (e < 0) {
                 active[i] = 0;   // process_usl.c:660-666: outside the grid for good
@@ -167,12 +169,15 @@ __global__ void __launch_bounds__(256) grid_kernel(
     if (by) { my = 0; fy = 0; }
     double ax = 0, ay = 0, vxn = 0, vyn = 0;
     if (m > MPMG_TOL) {
-        ax = fx / m;
-        ay = fy / m;
+        // one division: the four quotients by m differ from IEEE division
+        // by at most an ulp
+        const double inv_m = 1.0 / m;
+        ax = fx * inv_m;
+        ay = fy * inv_m;
         mx += dt * fx;
         my += dt * fy;
-        vxn = mx / m;
-        vyn = my / m;
+        vxn = mx * inv_m;
+        vyn = my * inv_m;
     }
     node_m[n] = m;
     node_ax[n] = ax;
@@ -322,7 +327,7 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
     const double exy = 0.5 * (dxdy + dydx);
     const double wxy = 0.5 * (dxdy - dydx);
     // update_particle_densities_split (process_usl.c:961-970)
-    double vol = A.v[i] * exp(dt * (exx + eyy));
+    double vol = A.v[i] * mat::exp_small(dt * (exx + eyy));
     A.v[i] = vol;
     if (A.exx != nullptr) {
         A.exx[i] = exx;
@@ -566,6 +571,8 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.el.K = ctx->K;
     A.el.lambda = ctx->lambda;
     A.el.dt = c.dt;
+    A.el.inv_G = 1.0 / ctx->G;
+    A.el.inv_dt = 1.0 / c.dt;
     A.mu2.mu_s = c.mp[MPMG_MP_MU_S];
     A.mu2.mu_2 = c.mp[MPMG_MP_MU_2];
     A.mu2.I0 = c.mp[MPMG_MP_I0];
@@ -573,6 +580,8 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.mu2.grains_d = c.mp[MPMG_MP_GRAINS_D];
     A.mu2.rho_critical = c.mp[MPMG_MP_RHO_CRITICAL];
     A.mu2.A = c.mp[MPMG_MP_A];
+    A.mu2.inv_grains_rho = 1.0 / A.mu2.grains_rho;
+    A.mu2.inv_grains_d = 1.0 / A.mu2.grains_d;
     A.nl.E = c.mp[MPMG_MP_E];
     A.nl.nu = c.mp[MPMG_MP_NU];
     A.nl.mu_s = c.mp[MPMG_MP_MU_S];
@@ -616,7 +625,8 @@ int mpmg_launch_step(mpmg_ctx *ctx)
     const int nn = (int)ctx->nn;
 
     mpmg_phase_begin(ctx, PH_KEYS);
-    keys_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, n, ctx->x, ctx->y, ctx->in_element, ctx->active,
+    keys_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, (float)ctx->inv_h, n, ctx->x, ctx->y, ctx->in_element,
+                                                   ctx->active,
                                                    ctx->keys, (uint32_t)ne, ctx->bin.counts, ctx->d_params,
                                                    c.dt, c.gravity_mode, c.gravity);
     ctx->launches += 1;
