@@ -103,12 +103,22 @@ MIXED_BYTES = {
 # g_local_mu2, 64 B per node-step; of those the G2P moves the particle state
 # (13 floats read, 13 written = 104 B) and the node gathers (16 B per node).
 MIXED_STEP_SURVEY_BYTES = (112, 0, 64)
+# A batch runs P2G and grid update as two kernels, so the element corner sums
+# (5 floats x 4 corners) are written and read back: 80 B per element each.
+BATCH_BYTES = {
+    "sort": (20, 16, 0),
+    "p2g": (40, 80, 0),
+    "grid": (0, 80, 24),
+    "g2p": (128, 0, 16),
+}
 MIXED_G2P_SURVEY_BYTES = (104, 0, 16)
 
-# FP64 operations (DADD + DMUL + 2 x DFMA) per particle of the FP64 G2P +
-# g_local_mu2 on this workload after the warm-up steps, from one ncu capture
-# of g2p_kernel<1,0> (None until measured).
-G2P64_FLOPS_PER_PARTICLE = None
+# FP64 work per particle of the FP64 G2P + g_local_mu2 on this workload after
+# the warm-up steps, from one ncu capture of g2p_kernel<1,0>: operations
+# (DADD + DMUL + 2 DFMA) and FP64 pipe instructions (pipe-active cycles x 2
+# per SM, compares and conversions included).
+G2P64_FLOPS_PER_PARTICLE = 287.1
+G2P64_PIPE_INSTR_PER_PARTICLE = 232.4
 
 # DRAM bytes (read + write) of one mx_g2p_kernel launch on this workload from
 # one ncu capture: 80.8 MB read + 17.0 MB written; writes still in L2 at the
@@ -445,9 +455,14 @@ def run_gpu(args):
                 "step_survey_frac": step64_survey / (ms64 / args.steps / 1e3) / 1e9 / peak,
                 "phases": phases64}
     if G2P64_FLOPS_PER_PARTICLE:
-        fl = G2P64_FLOPS_PER_PARTICLE * n / (g2p64["ms"] / 1e3)
+        g2p_s = g2p64["ms"] / 1e3
+        fl = G2P64_FLOPS_PER_PARTICLE * n / g2p_s
+        # the pipe issues one FP64 instruction (an FMA is two FLOP) per slot
+        inst = G2P64_PIPE_INSTR_PER_PARTICLE * n / g2p_s
         roofline["compute_bound"].update({"achieved": fl, "frac": fl / fp64_peak,
-                                          "flops_per_particle": G2P64_FLOPS_PER_PARTICLE})
+                                          "flops_per_particle": G2P64_FLOPS_PER_PARTICLE,
+                                          "pipe_instr_per_particle": G2P64_PIPE_INSTR_PER_PARTICLE,
+                                          "pipe_instr_per_s": inst, "pipe_frac": inst / (fp64_peak / 2)})
 
     # --- end to end through the C ABI with host buffers (FP64) ------------------
     # The user's run: create the simulation from host arrays (H2D of the
@@ -553,12 +568,20 @@ def run_gpu(args):
         # launch shape tuned on the batch itself (mpmg_autotune; results unchanged)
         tuning = bsim.autotune(steps_per_trial=16)
         bsim.synchronize()
-        bsteps = max(3, min(args.steps, 20))
+        bsteps = args.batch_steps
         sync_all()
         msb = time_steps(bsim, bsteps, bstream, torch)
         sync_all()
         bsim.close()
         value_b = nb * bsteps * world / slowest(msb / 1e3)
+        # algorithmic bytes of a batched step: the builder's accounting of the
+        # unfused kernels a batch runs, and the survey's compulsory bytes
+        bn = nb
+        be = int(sum((sc["Nx"] - 1) * (sc["Ny"] - 1) for sc in ens))
+        bnn = int(sum(sc["Nx"] * sc["Ny"] for sc in ens))
+        b_builder = sum(phase_bytes(BATCH_BYTES, k, bn, be, bnn) for k in BATCH_BYTES)
+        b_survey = phase_bytes({"s": MIXED_STEP_SURVEY_BYTES}, "s", bn, be, bnn)
+        b_step_s = msb / bsteps / 1e3
         # the same members one at a time (each its own context and step graphs)
         seq_ms = 0.0
         for sc in ens:
@@ -574,6 +597,11 @@ def run_gpu(args):
                       "steps": bsteps, "ms_per_step": msb / bsteps,
                       "sequential_value": value_seq, "batch_over_sequential": value_b / value_seq,
                       "autotune": tuning,
+                      "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak,
+                                   "step_builder_bytes": b_builder,
+                                   "step_frac_builder_bytes": b_builder / b_step_s / 1e9 / peak,
+                                   "step_survey_bytes": b_survey,
+                                   "step_frac_survey_bytes": b_survey / b_step_s / 1e9 / peak},
                       "workload": "ensemble of 256 g_local_mu2 runs (silo / heap), grids 64^2-384^2 "
                                   "elements, 5k-200k particles log-uniform, outlet 0.02-0.12, mu_s 0.30-0.45 "
                                   "(seed 1), mixed precision"}
@@ -775,6 +803,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=60, help="CPU-baseline steps on all host cores")
     ap.add_argument("--cpu-steps-1", type=int, default=8, help="CPU-baseline steps on one core")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--batch-steps", type=int, default=2000, help="timed steps of the batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-nonlocal", action="store_true", help="skip the nonlocal silo measurement")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 accuracy report")

@@ -134,11 +134,15 @@ typedef struct mpmg_config {
     int solver_maxit;        /* fluidity PCG iteration cap (default 20000) */
     int device;              /* CUDA device ordinal */
     int solver_warm_start;   /* nonzero: start the fluidity PCG from the previous
-                                step's nodal fluidity instead of zero.  Off by
-                                default: nodes whose rows hold only the 1e-10
-                                diagonal keep a stale warm-start value that the
-                                residual cannot see, where the reference's direct
-                                solve gives zero. */
+                                step's nodal fluidity instead of zero (rows that
+                                no element touches start at zero either way, as
+                                the reference's direct solve gives zero there).
+                                Off by default: with it on, a step's result also
+                                depends on the previous solve's rounding, so a run
+                                restarted from a state file (which carries no
+                                solver state) no longer continues bit for bit;
+                                on the 835 996-particle silo it saves about 5 % of
+                                the iterations. */
     int precision;           /* enum mpmg_precision */
     int scheme;              /* enum mpmg_scheme */
 } mpmg_config;
@@ -211,20 +215,27 @@ MPMG_API int mpmg_set_map(mpmg_ctx *ctx, const int *in_element, const int *activ
    and per-element start offsets (num_elements + 1 entries). */
 MPMG_API int mpmg_get_sort(mpmg_ctx *ctx, int *sorted_keys, int *perm, int *cell_start);
 
-/* Online tuning of a mixed-form context's launch shape (no counterpart in the
-   reference): the persistent G2P grid (1 up to as many blocks per SM as fit)
-   and the steps per replayed CUDA graph (4, 8, 16).  Every candidate runs the simulation itself
-   (a warm-up graph, then steps_per_trial steps rounded up to whole graphs,
-   timed with CUDA events) and the fastest is kept for later steps.  Neither
-   knob changes any result: the trajectory is the untuned one, advanced by
-   steps_advanced steps. */
+/* Online tuning of a mixed-form context's tiles and launch shape (no
+   counterpart in the reference).  First the tiles, at the default launch
+   shape: a batch's P2G tile (256 elements a block staging 1024 particles a
+   pass, 128 staging 512, or 512 staging 1024; a single simulation runs the
+   fused P2G and grid update) with the G2P tile (256 or 128 particles).  Then,
+   with the fastest tiles, the persistent G2P grid (1 up to as many blocks per
+   SM as fit) and the steps per replayed CUDA graph (4, 8, 16).  Every
+   candidate runs the simulation itself (a warm-up graph, then steps_per_trial
+   steps rounded up to whole graphs, timed with CUDA events) and the fastest
+   is kept for later steps.  No knob changes any result: the trajectory is the
+   untuned one, advanced by steps_advanced steps. */
 typedef struct mpmg_tuning {
     int g2p_blocks_per_sm;
     int graph_steps;
     double ms_per_step;          /* of the configuration kept */
-    double default_ms_per_step;  /* of the default (all G2P blocks that fit, 8 steps per graph) */
+    double default_ms_per_step;  /* of the default (default tiles, all G2P blocks that fit, 8 steps per graph) */
     int candidates;
     int steps_advanced;
+    int p2g_elements;            /* batched P2G tile kept: elements a block (0 for a single simulation) */
+    int p2g_stage;               /* batched P2G tile kept: particles staged a pass */
+    int g2p_tile;                /* G2P tile kept: particles a tile */
 } mpmg_tuning;
 MPMG_API int mpmg_autotune(mpmg_ctx *ctx, int steps_per_trial, mpmg_tuning *best);
 

@@ -963,12 +963,15 @@ int step_with_graphs(mpmg_ctx *ctx, int nsteps)
 
 extern "C" {
 
-// Online tuning of the mixed step's launch shape.  Each candidate (G2P
-// blocks per SM x steps per graph) runs the simulation itself for a warm-up
-// graph and then steps_per_trial steps (rounded up to whole graphs) timed
-// with CUDA events; the fastest is kept.  Neither knob changes any result,
-// so the trajectory is the one an untuned run takes; it advances by every
-// trial's steps.
+// Online tuning of the mixed step's tiles and launch shape, on the
+// simulation itself.  First the tiles: every batched-P2G tile (elements a
+// block, particles staged a pass; batches only, a single simulation runs the
+// fused P2G) with every G2P tile, at the default launch shape; then, with
+// the fastest tiles, the launch shape: G2P blocks per SM x steps per graph.
+// Each candidate runs a warm-up graph and then steps_per_trial steps
+// (rounded up to whole graphs) timed with CUDA events.  No knob changes any
+// result, so the trajectory is the one an untuned run takes; it advances by
+// every trial's steps.
 int mpmg_autotune(mpmg_ctx *ctx, int steps_per_trial, mpmg_tuning *best)
 {
     if (ctx == nullptr || best == nullptr || steps_per_trial < 1) return MPMG_ERR_INVALID;
@@ -979,53 +982,84 @@ int mpmg_autotune(mpmg_ctx *ctx, int steps_per_trial, mpmg_tuning *best)
     MPMG_CHECK(cudaSetDevice(ctx->dev));
     memset(best, 0, sizeof(*best));
     const int chunk_opts[3] = {4, 8, 16};
-    const int per_sm_max = ctx->mixed->g2p_per_sm_max;
+    const int g2p_tiles[2] = {256, 128};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     MPMG_CHECK(cudaEventCreate(&e0));
     MPMG_CHECK(cudaEventCreate(&e1));
-    int rc = MPMG_OK;
-    double best_ms = 1e30, default_ms = 0;
-    int best_ps = 0, best_ch = 0, tried = 0, advanced = 0, last_ps = -1;
+    int rc = MPMG_OK, tried = 0, advanced = 0;
+    double default_ms = 0;
+    // one timed trial of the current configuration; ms per step in *per
+    auto trial_of = [&](int ch, double *per) -> int {
+        ctx->graph_steps = ch;
+        drop_graphs(ctx);
+        const int trial = ((steps_per_trial + ch - 1) / ch) * ch;
+        int r = step_with_graphs(ctx, ch);                    // capture and warm up
+        if (r != MPMG_OK) return r;
+        if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) return MPMG_ERR_CUDA;
+        r = step_with_graphs(ctx, trial);
+        if (r != MPMG_OK) return r;
+        if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+            return MPMG_ERR_CUDA;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *per = ms / trial;
+        advanced += ch + trial;
+        tried += 1;
+        return MPMG_OK;
+    };
+    // tiles, at the default launch shape
+    const int p2g_n = ctx->batch ? mpmg_mixed_p2g_variants() : 1;
+    double best_ms = 1e30;
+    int best_pv = 0, best_tile = g2p_tiles[0];
+    for (int pv = 0; pv < p2g_n && rc == MPMG_OK; pv++) {
+        for (int t = 0; t < 2 && rc == MPMG_OK; t++) {
+            rc = mpmg_mixed_set_tiles(ctx, pv, g2p_tiles[t]);
+            if (rc != MPMG_OK) break;
+            double per = 0;
+            rc = trial_of(MPMG_GRAPH_CHUNK, &per);
+            if (rc != MPMG_OK) break;
+            if (pv == 0 && t == 0) default_ms = per;
+            if (per < best_ms) {
+                best_ms = per;
+                best_pv = pv;
+                best_tile = g2p_tiles[t];
+            }
+        }
+    }
+    // launch shape, with those tiles
+    int best_ps = 0, best_ch = MPMG_GRAPH_CHUNK, last_ps = -1;
+    if (rc == MPMG_OK) rc = mpmg_mixed_set_tiles(ctx, best_pv, best_tile);
+    const int per_sm_max = ctx->mixed->g2p_per_sm_max;
+    best_ps = per_sm_max;
     for (int a = 1; a <= per_sm_max && rc == MPMG_OK; a++) {
         const int ps = mpmg_mixed_set_g2p_per_sm(ctx, a);
         if (ps == last_ps) continue;   // clamped to one already tried
         last_ps = ps;
         for (int b = 0; b < 3 && rc == MPMG_OK; b++) {
-            const int ch = chunk_opts[b];
-            ctx->graph_steps = ch;
-            drop_graphs(ctx);
-            const int trial = ((steps_per_trial + ch - 1) / ch) * ch;
-            rc = step_with_graphs(ctx, ch);                    // capture and warm up
+            double per = 0;
+            rc = trial_of(chunk_opts[b], &per);
             if (rc != MPMG_OK) break;
-            if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { rc = MPMG_ERR_CUDA; break; }
-            rc = step_with_graphs(ctx, trial);
-            if (rc != MPMG_OK) break;
-            if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
-                rc = MPMG_ERR_CUDA;
-                break;
-            }
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            const double per = ms / trial;
-            advanced += ch + trial;
-            tried += 1;
-            if (ps == per_sm_max && ch == MPMG_GRAPH_CHUNK) default_ms = per;
             if (per < best_ms) {
                 best_ms = per;
                 best_ps = ps;
-                best_ch = ch;
+                best_ch = chunk_opts[b];
             }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc == MPMG_OK) rc = sync_status(ctx);
-    if (tried > 0) {
+    if (tried > 0 && rc == MPMG_OK) {
+        mpmg_mixed_set_tiles(ctx, best_pv, best_tile);
         mpmg_mixed_set_g2p_per_sm(ctx, best_ps);
         ctx->graph_steps = best_ch;
     } else {
-        mpmg_mixed_set_g2p_per_sm(ctx, ctx->mixed->g2p_per_sm_max);
+        mpmg_mixed_set_tiles(ctx, 0, g2p_tiles[0]);
         ctx->graph_steps = MPMG_GRAPH_CHUNK;
+        best_pv = 0;
+        best_tile = g2p_tiles[0];
+        best_ps = ctx->mixed->g2p_per_sm_max;
+        best_ch = MPMG_GRAPH_CHUNK;
     }
     drop_graphs(ctx);
     best->g2p_blocks_per_sm = best_ps;
@@ -1034,6 +1068,8 @@ int mpmg_autotune(mpmg_ctx *ctx, int steps_per_trial, mpmg_tuning *best)
     best->default_ms_per_step = default_ms;
     best->candidates = tried;
     best->steps_advanced = advanced;
+    if (ctx->batch) mpmg_mixed_p2g_shape(best_pv, &best->p2g_elements, &best->p2g_stage);
+    best->g2p_tile = best_tile;
     return rc;
 }
 

@@ -69,8 +69,10 @@ struct MixedState {
     float4 *node4;         // per node: ax, ay, vx, vy (FP32) for the gathers
     float2 *node_mass;     // per node: mass as float-float (hi, lo)
     int g2p_blocks;        // persistent G2P grid size
-    int g2p_per_sm_max;    // G2P blocks that fit on one SM
+    int g2p_per_sm_max;    // G2P blocks of the current tile that fit on one SM
     int sms;
+    int g2p_tile;          // particles a G2P tile (256 or 128)
+    int p2g_variant;       // batched P2G tile (kP2GElems / kP2GStage index)
     double *export_buf;    // one FP64 particle field in caller order, for read-back
     float4 *nl_E, *nl_F;   // g_nonlocal_mu2: strain rate and bulk fluidity per stored particle
 };
@@ -145,6 +147,9 @@ struct mpmg_ctx {
     double *cg_partials;   // per-block partial sums
     unsigned int *cg_barrier;  // grid barrier counter + generation
     int cg_blocks;
+    int cg_tile_blocks;    // pcg_tile_kernel: blocks (0: the grid does not fit, pcg_kernel runs)
+    int cg_tile_nodes;     // pcg_tile_kernel: nodes per block
+    size_t cg_tile_smem;   // pcg_tile_kernel: dynamic shared memory per block
 
     StepParams *d_params;  // one record per simulation (a batch holds several)
     StepParams h_params;   // host mirror of the first, refreshed on read-back
@@ -245,6 +250,9 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
                     const double *syy);
 void mpmg_mixed_free(mpmg_ctx *ctx);
 int mpmg_mixed_set_g2p_per_sm(mpmg_ctx *ctx, int per_sm);   // returns the value set
+int mpmg_mixed_set_tiles(mpmg_ctx *ctx, int p2g_variant, int g2p_tile);
+int mpmg_mixed_p2g_variants();
+void mpmg_mixed_p2g_shape(int v, int *elements, int *stage);
 int mpmg_mixed_step(mpmg_ctx *ctx);
 // Host read-back / write of a mixed particle or node field; returns
 // MPMG_ERR_UNKNOWN_FIELD for names the mixed state does not hold.

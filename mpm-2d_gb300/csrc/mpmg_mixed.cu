@@ -338,16 +338,21 @@ __device__ __forceinline__ int find_member(const int *__restrict__ off, int coun
 // the same few banks (16-byte records 64 bytes apart, 4-byte words 16 bytes
 // apart).  One pad record after every 8 records, one pad word after every 32
 // words and two pad halves after every 64 halves spread them over all banks.
-constexpr int kP2GThreads = 256;
-constexpr int kP2GChunk = 1024;
-constexpr int kP2GPer = kP2GChunk / kP2GThreads;   // stage entries per thread
+//
+// The batched kernel's tile (elements per block = threads, particles staged
+// per pass) is a template: mpmg_autotune picks one of kP2GVariants at run
+// time.  The fused single-simulation kernel stages 4 entries a thread.
+constexpr int kP2GPer = 4;   // stage entries per thread of the fused kernel
 
 __device__ __forceinline__ int pad16b(int j) { return j + (j >> 3); }
 __device__ __forceinline__ int pad4b(int j) { return j + (j >> 5); }
 __device__ __forceinline__ int pad2b(int j) { return j + ((j >> 6) << 1); }
-constexpr int kP2GChunk16 = kP2GChunk + kP2GChunk / 8;
-constexpr int kP2GChunk4 = kP2GChunk + kP2GChunk / 32;
-constexpr int kP2GChunk2 = kP2GChunk + kP2GChunk / 32;
+
+// (elements a block, staged particles) of the batched P2G; variant 0 is the
+// default
+constexpr int kP2GVariants = 3;
+constexpr int kP2GElems[kP2GVariants] = {256, 128, 512};
+constexpr int kP2GStage[kP2GVariants] = {1024, 512, 1024};
 
 __device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, float grav, float4 a4, float4 b4,
                                                float syy)
@@ -371,15 +376,16 @@ __device__ __forceinline__ void p2g_accumulate(float (&acc)[4][5], float ih, flo
     }
 }
 
-template <bool BATCH>
-__global__ void __launch_bounds__(kP2GThreads, 4) mx_p2g_kernel(const __grid_constant__ MemberM m0, BatchView bv,
-                                                                int ne_total, const int *__restrict__ cell_start,
-                                                                const uint32_t *__restrict__ slots,
-                                                                uint32_t *__restrict__ perm,
-                                                                uint32_t *__restrict__ rank, Buf P,
-                                                                const StepParams *__restrict__ sp,
-                                                                float *__restrict__ cell_sums)
+template <int kP2GThreads, int kP2GChunk, bool BATCH>
+__global__ void __launch_bounds__(kP2GThreads, 1024 / kP2GThreads) mx_p2g_kernel(
+    const __grid_constant__ MemberM m0, BatchView bv, int ne_total, const int *__restrict__ cell_start,
+    const uint32_t *__restrict__ slots, uint32_t *__restrict__ perm, uint32_t *__restrict__ rank, Buf P,
+    const StepParams *__restrict__ sp, float *__restrict__ cell_sums)
 {
+    constexpr int kP2GPer = kP2GChunk / kP2GThreads;   // stage entries per thread
+    constexpr int kP2GChunk16 = kP2GChunk + kP2GChunk / 8;
+    constexpr int kP2GChunk4 = kP2GChunk + kP2GChunk / 32;
+    constexpr int kP2GChunk2 = kP2GChunk + kP2GChunk / 32;
     __shared__ float4 sh_a[kP2GChunk16];
     __shared__ float4 sh_b[kP2GChunk16];
     __shared__ float sh_syy[kP2GChunk4];
@@ -946,28 +952,34 @@ __device__ __forceinline__ uint32_t g2p_particle(const MemberM &M, uint32_t sent
 // element order from step to step).  The last, partial tile is read directly.
 // Every wait is bounded: on a timeout the kernel sets MPMG_DEV_ERR_SPIN,
 // waits (bounded) for its own copies still in flight, and returns.
-constexpr int kG2PTile = 256;
+// The tile (256 by default, or 128: mpmg_autotune's choice) is a template.
 constexpr int kG2PStages = 3;
 constexpr long long kG2PWaitLimit = 1ll << 22;
 
+template <int TILE>
 struct G2PStage {
-    float4 A[kG2PTile], B[kG2PTile], C[kG2PTile], D[kG2PTile];
-    int src[kG2PTile];
-    uint32_t rank[kG2PTile];
+    float4 A[TILE], B[TILE], C[TILE], D[TILE];
+    int src[TILE];
+    uint32_t rank[TILE];
 };
-constexpr uint32_t kG2PStageBytes = (uint32_t)sizeof(G2PStage);
-constexpr size_t kG2PSmem = sizeof(G2PStage) * kG2PStages;
-static_assert(sizeof(G2PStage) % 16 == 0, "stage arrays must stay 16-byte aligned");
-
-template <int MATERIAL, bool BATCH>
-__global__ void __launch_bounds__(kG2PTile, 3) mx_g2p_kernel(const __grid_constant__ MemberM m0, BatchView bv,
-                                                             int ne_total, int n, const uint32_t *__restrict__ rank,
-                                                             Buf S, Buf D, const int *__restrict__ cell_src,
-                                                             int *__restrict__ cell_dst,
-                                                             const float4 *__restrict__ node4,
-                                                             uint32_t *__restrict__ bins, StepParams *sp,
-                                                             int *status, NLOut nl)
+template <int TILE>
+constexpr size_t g2p_smem_bytes()
 {
+    return sizeof(G2PStage<TILE>) * kG2PStages;
+}
+static_assert(sizeof(G2PStage<128>) % 16 == 0 && sizeof(G2PStage<256>) % 16 == 0,
+              "stage arrays must stay 16-byte aligned");
+constexpr int kG2PTiles = 2;
+constexpr int kG2PTileSizes[kG2PTiles] = {256, 128};
+
+template <int MATERIAL, bool BATCH, int kG2PTile>
+__global__ void __launch_bounds__(kG2PTile, 768 / kG2PTile) mx_g2p_kernel(
+    const __grid_constant__ MemberM m0, BatchView bv, int ne_total, int n, const uint32_t *__restrict__ rank,
+    Buf S, Buf D, const int *__restrict__ cell_src, int *__restrict__ cell_dst, const float4 *__restrict__ node4,
+    uint32_t *__restrict__ bins, StepParams *sp, int *status, NLOut nl)
+{
+    using G2PStage = ::G2PStage<kG2PTile>;
+    constexpr uint32_t kG2PStageBytes = (uint32_t)sizeof(G2PStage);
     extern __shared__ __align__(128) unsigned char g2p_smem[];
     G2PStage *stage = reinterpret_cast<G2PStage *>(g2p_smem);
     __shared__ __align__(8) uint64_t full[kG2PStages];
@@ -1326,12 +1338,37 @@ __global__ void __launch_bounds__(256) mx_place_kernel(int n, const double *cons
 using G2PKernel = void (*)(MemberM, BatchView, int, int, const uint32_t *, Buf, Buf, const int *, int *,
                           const float4 *, uint32_t *, StepParams *, int *, NLOut);
 
-G2PKernel g2p_variant(int material, bool batch)
+template <int TILE>
+G2PKernel g2p_variant_t(int material, bool batch)
 {
-    if (material == MPMG_ISOLIN) return batch ? mx_g2p_kernel<MPMG_ISOLIN, true> : mx_g2p_kernel<MPMG_ISOLIN, false>;
-    if (material == MPMG_G_NONLOCAL_MU2) return mx_g2p_kernel<MPMG_G_NONLOCAL_MU2, false>;
-    if (material == MPMG_DP_RI_MT) return batch ? mx_g2p_kernel<MPMG_DP_RI_MT, true> : mx_g2p_kernel<MPMG_DP_RI_MT, false>;
-    return batch ? mx_g2p_kernel<MPMG_G_LOCAL_MU2, true> : mx_g2p_kernel<MPMG_G_LOCAL_MU2, false>;
+    if (material == MPMG_ISOLIN)
+        return batch ? mx_g2p_kernel<MPMG_ISOLIN, true, TILE> : mx_g2p_kernel<MPMG_ISOLIN, false, TILE>;
+    if (material == MPMG_G_NONLOCAL_MU2) return mx_g2p_kernel<MPMG_G_NONLOCAL_MU2, false, TILE>;
+    if (material == MPMG_DP_RI_MT)
+        return batch ? mx_g2p_kernel<MPMG_DP_RI_MT, true, TILE> : mx_g2p_kernel<MPMG_DP_RI_MT, false, TILE>;
+    return batch ? mx_g2p_kernel<MPMG_G_LOCAL_MU2, true, TILE> : mx_g2p_kernel<MPMG_G_LOCAL_MU2, false, TILE>;
+}
+
+// The G2P kernel of a material and tile (one of kG2PTileSizes).
+G2PKernel g2p_variant(int material, bool batch, int tile)
+{
+    return tile == 128 ? g2p_variant_t<128>(material, batch) : g2p_variant_t<256>(material, batch);
+}
+
+size_t g2p_smem_size(int tile)
+{
+    return tile == 128 ? g2p_smem_bytes<128>() : g2p_smem_bytes<256>();
+}
+
+using P2GKernel = void (*)(MemberM, BatchView, int, const int *, const uint32_t *, uint32_t *, uint32_t *, Buf,
+                          const StepParams *, float *);
+
+// The batched P2G of variant v (kP2GElems[v] elements a block).
+P2GKernel p2g_variant(int v)
+{
+    if (v == 1) return mx_p2g_kernel<kP2GElems[1], kP2GStage[1], true>;
+    if (v == 2) return mx_p2g_kernel<kP2GElems[2], kP2GStage[2], true>;
+    return mx_p2g_kernel<kP2GElems[0], kP2GStage[0], true>;
 }
 
 }  // namespace
@@ -1451,18 +1488,21 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     s->cur = 0;
     // persistent G2P grid: as many blocks as fit on the device at once, at
     // most one per tile
-    int sms = 0, per_sm = 0;
+    int sms = 0;
     MPMG_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
-    G2PKernel g2p = g2p_variant(ctx->cfg.material, bt != nullptr);
-    MPMG_CHECK(cudaFuncSetAttribute(g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kG2PSmem));
+    for (int t = 0; t < kG2PTiles; t++) {
+        const int tile = kG2PTileSizes[t];
+        MPMG_CHECK(cudaFuncSetAttribute(g2p_variant(ctx->cfg.material, bt != nullptr, tile),
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g2p_smem_size(tile)));
+    }
     MPMG_CHECK(cudaFuncSetAttribute(mx_p2g_grid_kernel<false, kFusedTX, kFusedTY>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedT::smem));
     MPMG_CHECK(cudaFuncSetAttribute(mx_p2g_grid_kernel<true, kFusedTX, kFusedTY>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FusedT::smem));
-    MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g2p, kG2PTile, kG2PSmem));
     s->sms = sms > 0 ? sms : 1;
-    s->g2p_per_sm_max = per_sm > 0 ? per_sm : 1;
-    mpmg_mixed_set_g2p_per_sm(ctx, s->g2p_per_sm_max);
+    s->p2g_variant = 0;
+    rc = mpmg_mixed_set_tiles(ctx, 0, kG2PTileSizes[0]);
+    if (rc != MPMG_OK) return rc;
     // the first step's element counts; every G2P counts the next step's
     return mpmg_bin_count(ctx, (const uint32_t *)ctx->in_element);
 }
@@ -1475,11 +1515,42 @@ int mpmg_mixed_set_g2p_per_sm(mpmg_ctx *ctx, int per_sm)
     MixedState *s = ctx->mixed;
     if (per_sm < 1) per_sm = 1;
     if (per_sm > s->g2p_per_sm_max) per_sm = s->g2p_per_sm_max;
-    const size_t tiles = (ctx->np + kG2PTile - 1) / kG2PTile;
+    const size_t tiles = (ctx->np + s->g2p_tile - 1) / s->g2p_tile;
     size_t blocks = (size_t)s->sms * (size_t)per_sm;
     if (blocks > tiles) blocks = tiles;
     s->g2p_blocks = (int)(blocks > 0 ? blocks : 1);
     return per_sm;
+}
+
+// The tiles of the mixed step: the batched P2G's variant (elements a block
+// and staged particles, kP2GElems / kP2GStage; single simulations run the
+// fused kernel and ignore it) and the G2P tile (kG2PTileSizes).  The G2P
+// grid goes back to all the blocks of the new tile that fit.  Tiles change
+// which block handles which elements or particles, never a result.
+int mpmg_mixed_set_tiles(mpmg_ctx *ctx, int p2g_variant, int g2p_tile)
+{
+    MixedState *s = ctx->mixed;
+    if (s == nullptr || p2g_variant < 0 || p2g_variant >= kP2GVariants || (g2p_tile != 256 && g2p_tile != 128))
+        return MPMG_ERR_INVALID;
+    int per_sm = 0;
+    MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, g2p_variant(ctx->cfg.material, ctx->batch != nullptr, g2p_tile), g2p_tile, g2p_smem_size(g2p_tile)));
+    s->p2g_variant = p2g_variant;
+    s->g2p_tile = g2p_tile;
+    s->g2p_per_sm_max = per_sm > 0 ? per_sm : 1;
+    mpmg_mixed_set_g2p_per_sm(ctx, s->g2p_per_sm_max);
+    return MPMG_OK;
+}
+
+int mpmg_mixed_p2g_variants()
+{
+    return kP2GVariants;
+}
+
+void mpmg_mixed_p2g_shape(int v, int *elements, int *stage)
+{
+    *elements = kP2GElems[v];
+    *stage = kP2GStage[v];
 }
 
 void mpmg_mixed_free(mpmg_ctx *ctx)
@@ -1559,8 +1630,9 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
         mpmg_phase_end(ctx, PH_P2G);
     } else {
         mpmg_phase_begin(ctx, PH_P2G);
-        MPMG_CHECK(mpmg_launch_pdl(true, mx_p2g_kernel<true>, dim3(blocks_for(ctx->ne, kP2GThreads)),
-                                   dim3(kP2GThreads), 0, st, m0, bv, ne, (const int *)ctx->cell_start,
+        const int pe = kP2GElems[s->p2g_variant];
+        MPMG_CHECK(mpmg_launch_pdl(true, p2g_variant(s->p2g_variant), dim3(blocks_for(ctx->ne, pe)), dim3(pe), 0,
+                                   st, m0, bv, ne, (const int *)ctx->cell_start,
                                    (const uint32_t *)ctx->bin.slots, ctx->perm, ctx->bin.rank, S,
                                    (const StepParams *)ctx->d_params, s->cell_sums));
         mpmg_phase_end(ctx, PH_P2G);
@@ -1575,8 +1647,8 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     }
 
     mpmg_phase_begin(ctx, PH_G2P);
-    MPMG_CHECK(mpmg_launch_pdl(true, g2p_variant(c.material, batch), dim3(s->g2p_blocks), dim3(kG2PTile),
-                               kG2PSmem, st, m0, bv, ne, n, (const uint32_t *)ctx->bin.rank, S, D,
+    MPMG_CHECK(mpmg_launch_pdl(true, g2p_variant(c.material, batch, s->g2p_tile), dim3(s->g2p_blocks),
+                               dim3(s->g2p_tile), g2p_smem_size(s->g2p_tile), st, m0, bv, ne, n, (const uint32_t *)ctx->bin.rank, S, D,
                                (const int *)cell_array(ctx, cur), cell_array(ctx, nxt), (const float4 *)s->node4,
                                ctx->bin.counts, ctx->d_params, ctx->d_status, NLOut{s->nl_E, s->nl_F}));
     mpmg_phase_end(ctx, PH_G2P);

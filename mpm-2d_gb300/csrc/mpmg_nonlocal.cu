@@ -13,8 +13,10 @@
 // per-block partial sums reduced in a fixed order (deterministic), and all
 // grid-wide waits are bounded.  The unknowns are the nodes with mass above
 // the reference's threshold (g_nonlocal_mu2.c:365-381: m > 0; g_nonlocal.c:
-// m > 1e-10); the initial guess is zero, like the reference's direct solve
-// (a warm start from the previous step is available as an option).
+// m > 1e-10).  The initial guess is zero, like the reference's direct solve,
+// or with mpmg_config.solver_warm_start the previous step's nodal fluidity,
+// except on rows that no element touches, whose solution is zero; the
+// stopping test is the same relative residual either way.
 #include "mpmg_internal.cuh"
 #include "mpmg_materials.cuh"
 
@@ -274,13 +276,19 @@ __global__ void __launch_bounds__(kSolveThreads, 2) pcg_kernel(SolveArgs S)
         double cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         double f = 0;
         const bool dof = S.node_m[n] > S.dof_tol;
+        bool coupled = false;
         if (dof) {
             build_row(S, i, j, cf, &f);
+#pragma unroll
+            for (int q = 0; q < 9; q++) coupled |= (__double_as_longlong(cf[q]) << 1) != 0;
             cf[4] += S.shift;
         }
         if (dof && cf[4] > 0) {
             S.dinv[n] = 1.0 / cf[4];
             S.r[n] = f;
+            // a row no element touches holds only the shift and a zero
+            // right-hand side: its solution is zero, whatever the start
+            if (!coupled) S.x[n] = 0;
         } else {
             S.dinv[n] = 0;
             S.r[n] = 0;
@@ -425,6 +433,427 @@ __global__ void __launch_bounds__(kSolveThreads, 2) pcg_kernel(SolveArgs S)
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same Chronopoulos-Gear PCG with each block's rows and vectors resident
+// in shared memory.  Block b owns the contiguous nodes [b C, b C + C) (a few
+// grid rows) for the whole solve: their nine-point rows, D^-1, r, p, s, w
+// and u stay in shared memory, x stays in global memory (read and written
+// once an iteration), and u is also written to global memory so that the
+// neighbouring blocks can read the Nx + 1 halo nodes on either side of their
+// range.  An iteration is then
+//   A  p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^-1 r
+//      (own nodes, shared memory; u also to global)
+//                                  -- wait for the two neighbouring blocks
+//   B  halo of u from global (one batched load); w = A u; block partials of
+//      <r, u>, <w, u>, <r, r>                                -- grid barrier
+//   C  every block sums the partials in one fixed order (one batched load)
+//      and forms the scalars.
+// Compared with pcg_kernel, whose grid-stride loops read every vector and
+// row from L2 with dependent loads in each sweep, the only global reads an
+// iteration waits for are the halo and the partials.  The arithmetic and
+// the order of every sum are fixed, so the result does not depend on
+// timing.  The kernel runs when a block's share of the grid fits in shared
+// memory (pcg_tile_fits); pcg_kernel covers the rest.
+
+constexpr int kTileThreads = 512;
+constexpr int kTileTrips = 4;   // nodes a thread: a block owns at most kTileTrips * kTileThreads
+
+// Sum of (a, b, c) over the block in a fixed order; the result is returned
+// to every thread.  Only warp 0 adds: lane l sums the values of threads l,
+// l + 32, ... from shared memory, then the lanes combine in a shuffle tree.
+// (GB300 issues FP64 at 1/64 of the FP32 rate, and a shuffle tree in every
+// warp would cost as many FP64 adds as the rows of an iteration.)
+// scratch holds 3 * blockDim.x + 3 doubles.
+__device__ __forceinline__ void tile_sum3(double &a, double &b, double &c, double *scratch)
+{
+    const int nt = blockDim.x;
+    scratch[threadIdx.x] = a;
+    scratch[nt + threadIdx.x] = b;
+    scratch[2 * nt + threadIdx.x] = c;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        // four interleaved partial sums a value (a fixed order) to shorten
+        // the chain of dependent FP64 adds
+        double x0 = 0, x1 = 0, x2 = 0, x3 = 0, y0 = 0, y1 = 0, y2 = 0, y3 = 0, z0 = 0, z1 = 0, z2 = 0, z3 = 0;
+        for (int t = lane; t < nt; t += 128) {
+            x0 += scratch[t];
+            y0 += scratch[nt + t];
+            z0 += scratch[2 * nt + t];
+            if (t + 32 < nt) {
+                x1 += scratch[t + 32];
+                y1 += scratch[nt + t + 32];
+                z1 += scratch[2 * nt + t + 32];
+            }
+            if (t + 64 < nt) {
+                x2 += scratch[t + 64];
+                y2 += scratch[nt + t + 64];
+                z2 += scratch[2 * nt + t + 64];
+            }
+            if (t + 96 < nt) {
+                x3 += scratch[t + 96];
+                y3 += scratch[nt + t + 96];
+                z3 += scratch[2 * nt + t + 96];
+            }
+        }
+        double x = (x0 + x1) + (x2 + x3), y = (y0 + y1) + (y2 + y3), z = (z0 + z1) + (z2 + z3);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, off);
+            y += __shfl_down_sync(0xffffffffu, y, off);
+            z += __shfl_down_sync(0xffffffffu, z, off);
+        }
+        if (lane == 0) {
+            scratch[3 * nt] = x;
+            scratch[3 * nt + 1] = y;
+            scratch[3 * nt + 2] = z;
+        }
+    }
+    __syncthreads();
+    a = scratch[3 * nt];
+    b = scratch[3 * nt + 1];
+    c = scratch[3 * nt + 2];
+    __syncthreads();
+}
+
+// Slots (sa, sb, sc) of the per-block partials summed over all blocks in one
+// fixed order by warp 0 (lane l takes blocks l, l + 32, ..., then a shuffle
+// tree); every block computes the same totals.
+__device__ __forceinline__ void tile_totals3(const double *partials, int sa, int sb, int sc, int nblocks,
+                                             double &ta, double &tb, double &tc, double *scratch)
+{
+    const int nt = blockDim.x;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        // all loads first (up to kMaxTotals per lane), then the adds in order
+        constexpr int kMaxTotals = 8;
+        double va[kMaxTotals], vb[kMaxTotals], vc[kMaxTotals];
+#pragma unroll
+        for (int q = 0; q < kMaxTotals; q++) {
+            const int t = lane + 32 * q;
+            const bool in = t < nblocks;
+            va[q] = in ? __ldcg(partials + (size_t)sa * nblocks + t) : 0.0;
+            vb[q] = in ? __ldcg(partials + (size_t)sb * nblocks + t) : 0.0;
+            vc[q] = in ? __ldcg(partials + (size_t)sc * nblocks + t) : 0.0;
+        }
+        double x = 0, y = 0, z = 0;
+#pragma unroll
+        for (int q = 0; q < kMaxTotals; q++) {
+            x += va[q];
+            y += vb[q];
+            z += vc[q];
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, off);
+            y += __shfl_down_sync(0xffffffffu, y, off);
+            z += __shfl_down_sync(0xffffffffu, z, off);
+        }
+        if (lane == 0) {
+            scratch[3 * nt] = x;
+            scratch[3 * nt + 1] = y;
+            scratch[3 * nt + 2] = z;
+        }
+    }
+    __syncthreads();
+    ta = scratch[3 * nt];
+    tb = scratch[3 * nt + 1];
+    tc = scratch[3 * nt + 2];
+    __syncthreads();
+}
+
+// Grid barrier on a counter that only grows: episode k of a launch ends
+// when the counter reaches k * nblocks (the counter starts at zero at each
+// launch).  Thread 0 of each block publishes the block's writes (fence,
+// then a fire-and-forget add) and polls with acquire loads; the poll is
+// bounded, and a timeout or another block's timeout sets the spin error.
+__device__ __forceinline__ bool tile_grid_barrier(unsigned int *counter, unsigned int target, int *status)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(counter, 1u);
+        long long polls = 0;
+        for (;;) {
+            unsigned int v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(counter) : "memory");
+            if ((int)(v - target) >= 0) break;
+            if (++polls > kSpinLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0) {
+                atomicOr(status, MPMG_DEV_ERR_SPIN);
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    return (*(volatile int *)status & MPMG_DEV_ERR_SPIN) == 0;
+}
+
+// Point-to-point wait of phase A -> B: block b publishes that its u of
+// iteration `tag` is written (flags[b] = tag, after a fence) and waits until
+// its neighbours b - 1 and b + 1, whose ranges its halo reads, have
+// published the same tag.  Bounded like the barrier.
+__device__ __forceinline__ bool tile_neighbour_wait(unsigned int *flags, unsigned int tag, int *status)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(flags + blockIdx.x), "r"(tag) : "memory");
+        long long polls = 0;
+        for (int side = -1; side <= 1; side += 2) {
+            const int nb = (int)blockIdx.x + side;
+            if (nb < 0 || nb >= (int)gridDim.x) continue;
+            for (;;) {
+                unsigned int v;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(flags + nb) : "memory");
+                if ((int)(v - tag) >= 0) break;
+                if (++polls > kSpinLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0) {
+                    atomicOr(status, MPMG_DEV_ERR_SPIN);
+                    break;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    return (*(volatile int *)status & MPMG_DEV_ERR_SPIN) == 0;
+}
+
+// (A v) at own node k from the shared-memory rows and the extended vector
+// ve (own nodes at ve[k + H], halo below at ve[0, H), above after the own
+// nodes).  Missing neighbours are skipped by index.
+__device__ __forceinline__ double tile_stencil(const double *coef, int C, int H, int k, int i, int j, int Nx,
+                                               int Ny, const double *ve)
+{
+    double acc = 0;
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++) {
+        if (j + dj < 0 || j + dj >= Ny) continue;
+#pragma unroll
+        for (int di = -1; di <= 1; di++) {
+            if (i + di < 0 || i + di >= Nx) continue;
+            acc = fma(coef[(3 * (dj + 1) + (di + 1)) * C + k], ve[k + H + dj * Nx + di], acc);
+        }
+    }
+    return acc;
+}
+
+// Fills the halo of ve (Nx + 1 nodes on either side of [n0, n1)) from the
+// global vector g; nodes outside the grid read zero.
+__device__ __forceinline__ void tile_halo(const double *g, int n0, int n1, int nn, int H, double *ve)
+{
+    for (int t = threadIdx.x; t < 2 * H; t += blockDim.x) {
+        const int m = t < H ? n0 - H + t : n1 + (t - H);
+        ve[m - n0 + H] = (m >= 0 && m < nn) ? __ldcg(g + m) : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kTileThreads, 1) pcg_tile_kernel(SolveArgs S, int C, int warm, unsigned int *flags)
+{
+    extern __shared__ double sm[];
+    const int Nx = S.Nx, Ny = S.Ny, nn = Nx * Ny, H = Nx + 1;
+    const int nblocks = gridDim.x;
+    const int n0 = blockIdx.x * C;
+    const int n1 = min(n0 + C, nn);
+    const int cnt = n1 - n0;
+    double *coef = sm;                      // 9 C
+    double *dinv = coef + 9 * C;            // C each
+    double *r = dinv + C, *p = r + C, *s = p + C, *w = s + C;
+    double *ve = w + C;                     // C + 2 H: u (or x) with its halo
+    double *scratch = ve + C + 2 * H;       // 3 kTileThreads + 3
+    __shared__ double sh_scalar[2];
+    __shared__ int sh_next;
+    unsigned int episode = 0;      // grid barriers passed (S.barrier[0] counts arrivals)
+
+    // Set-up: rows (with the diagonal shift), D^-1 (zero for nodes that are
+    // not unknowns), right-hand side in r, the start in x.  A row that no
+    // element touches holds only the shift and a zero right-hand side, so
+    // its solution is zero: a warm start there is cleared.
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+        const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+        double cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        double f = 0;
+        const bool dof = S.node_m[n] > S.dof_tol;
+        bool coupled = false;
+        if (dof) {
+            build_row(S, i, j, cf, &f);
+#pragma unroll
+            for (int q = 0; q < 9; q++) coupled |= (__double_as_longlong(cf[q]) << 1) != 0;
+            cf[4] += S.shift;
+        }
+        if (dof && cf[4] > 0) {
+            dinv[k] = 1.0 / cf[4];
+            r[k] = f;
+            if (!warm || !coupled) S.x[n] = 0;
+        } else {
+            dinv[k] = 0;
+            r[k] = 0;
+            S.x[n] = 0;
+#pragma unroll
+            for (int q = 0; q < 9; q++) cf[q] = 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 9; q++) coef[q * C + k] = cf[q];
+    }
+    if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+
+    // r = b - A x, <b, b>
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) ve[k + H] = __ldcg(S.x + n0 + k);
+    tile_halo(S.x, n0, n1, nn, H, ve);
+    __syncthreads();
+    double bb = 0, z0 = 0, z1 = 0;
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+        const double dv = dinv[k];
+        double u = 0;
+        if (!is_zero(dv)) {
+            const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+            const double b = r[k];
+            const double rk = b - tile_stencil(coef, C, H, k, i, j, Nx, Ny, ve);
+            r[k] = rk;
+            bb = fma(b, b, bb);
+            u = dv * rk;
+        }
+        p[k] = 0;      // p, s start at zero: the first update sets p = u, s = w
+        s[k] = 0;
+        S.u[n0 + k] = u;
+    }
+    tile_sum3(bb, z0, z1, scratch);
+    if (threadIdx.x == 0) S.partials[2 * nblocks + blockIdx.x] = bb;
+    if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+    tile_totals3(S.partials, 2, 2, 2, nblocks, bb, z0, z1, scratch);
+
+    // w = A u, gamma = <r, u>, delta = <w, u>, <r, r>
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) ve[k + H] = __ldcg(S.u + n0 + k);
+    tile_halo(S.u, n0, n1, nn, H, ve);
+    __syncthreads();
+    double gamma = 0, delta = 0, rr = 0;
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+        double wk = 0;
+        if (!is_zero(dinv[k])) {
+            const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+            const double rk = r[k], u = ve[k + H];
+            wk = tile_stencil(coef, C, H, k, i, j, Nx, Ny, ve);
+            gamma = fma(rk, u, gamma);
+            delta = fma(wk, u, delta);
+            rr = fma(rk, rk, rr);
+        }
+        w[k] = wk;
+    }
+    tile_sum3(gamma, delta, rr, scratch);
+    if (threadIdx.x == 0) {
+        S.partials[0 * nblocks + blockIdx.x] = gamma;
+        S.partials[1 * nblocks + blockIdx.x] = delta;
+        S.partials[3 * nblocks + blockIdx.x] = rr;
+    }
+    if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+    tile_totals3(S.partials, 0, 1, 3, nblocks, gamma, delta, rr, scratch);
+    const double target = S.tol * S.tol * bb;
+
+    int it = 0;
+    bool converged = (rr <= target);
+    if (bb == 0) {
+        // No load: the solution is zero (the warm start is discarded).
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) S.x[n0 + k] = 0;
+        rr = 0;
+        converged = true;
+    }
+    double alpha = gamma / delta, beta = 0;
+    while (!converged && it < S.maxit) {
+        // A: own nodes only; this thread's x values are loaded first (all
+        // loads in flight at once; a block owns at most kTileTrips *
+        // kTileThreads nodes)
+        double xr[kTileTrips];
+#pragma unroll
+        for (int q = 0; q < kTileTrips; q++) {
+            const int k = threadIdx.x + q * kTileThreads;
+            xr[q] = k < cnt ? __ldcg(S.x + n0 + k) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < kTileTrips; q++) {
+            const int k = threadIdx.x + q * kTileThreads;
+            if (k >= cnt) break;
+            const double dv = dinv[k];
+            if (is_zero(dv)) continue;
+            const int n = n0 + k;
+            const double pk = fma(beta, p[k], ve[k + H]);
+            const double sk = fma(beta, s[k], w[k]);
+            const double rk = fma(-alpha, sk, r[k]);
+            p[k] = pk;
+            s[k] = sk;
+            r[k] = rk;
+            S.x[n] = fma(alpha, pk, xr[q]);
+            const double u = dv * rk;
+            ve[k + H] = u;
+            S.u[n] = u;
+        }
+        // the halo needs only the neighbours' u of this iteration; they read
+        // ours, and nobody rewrites u before the reduction barrier below
+        if (!tile_neighbour_wait(flags, (unsigned)it + 1u, S.status)) return;
+        // B: halo, w = A u, partials
+        tile_halo(S.u, n0, n1, nn, H, ve);
+        __syncthreads();
+        double gn = 0, dl = 0, rn = 0;
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+            if (is_zero(dinv[k])) continue;
+            const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+            const double rk = r[k], u = ve[k + H];
+            const double wk = tile_stencil(coef, C, H, k, i, j, Nx, Ny, ve);
+            w[k] = wk;
+            gn = fma(rk, u, gn);
+            dl = fma(wk, u, dl);
+            rn = fma(rk, rk, rn);
+        }
+        tile_sum3(gn, dl, rn, scratch);
+        if (threadIdx.x == 0) {
+            S.partials[0 * nblocks + blockIdx.x] = gn;
+            S.partials[1 * nblocks + blockIdx.x] = dl;
+            S.partials[3 * nblocks + blockIdx.x] = rn;
+        }
+        if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+        // C: totals and scalars
+        tile_totals3(S.partials, 0, 1, 3, nblocks, gn, dl, rr, scratch);
+        it++;
+        if (threadIdx.x == 0) {
+            int next = 0;                        // 0: go on, 1: give up, 2: converged
+            if (!(rr == rr)) {
+                next = 1;                        // NaN
+            } else if (rr <= target) {
+                next = 2;
+            } else {
+                const double beta_n = gn / gamma;
+                const double eta = dl - beta_n * gn / alpha;
+                if (!(eta > 0)) {
+                    next = 1;                    // breakdown of the recurrence: report non-convergence
+                } else {
+                    sh_scalar[0] = beta_n;
+                    sh_scalar[1] = gn / eta;
+                }
+            }
+            sh_next = next;
+        }
+        __syncthreads();
+        const int next = sh_next;
+        if (next == 1) break;
+        if (next == 2) {
+            converged = true;
+            break;
+        }
+        beta = sh_scalar[0];
+        alpha = sh_scalar[1];
+        gamma = gn;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S.sp->solve_iters = it;
+        S.sp->solve_converged = converged ? 1 : 0;
+        S.sp->solve_rel_resid = (bb > 0) ? sqrt(rr / bb) : 0.0;
+        if (!converged) atomicOr(S.status, MPMG_DEV_ERR_SOLVER);
+    }
+}
+
+// Shared memory of pcg_tile_kernel for C nodes a block on an Nx-wide grid.
+inline size_t pcg_tile_smem(int C, int Nx)
+{
+    return sizeof(double) * ((size_t)15 * C + 2 * (size_t)(Nx + 1) + 3 * kTileThreads + 8);
+}
+
 // Nodal fluidity back to the particles, then the stress update
 // (g_nonlocal_mu2.c:545-564 and :160-218; g_nonlocal.c:559-578, :154-298).
 // AVG: the element average of the four nodal values instead of the shape
@@ -512,8 +941,38 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
     int want = sms * (per_sm < 2 ? per_sm : 2);
     int need = (int)((nn + kSolveThreads - 1) / kSolveThreads);
     ctx->cg_blocks = want < need ? want : (need > 0 ? need : 1);
-    MPMG_CHECK(cudaMalloc(&ctx->cg_partials, 4 * (size_t)ctx->cg_blocks * sizeof(double)));
-    MPMG_CHECK(cudaMalloc(&ctx->cg_barrier, 2 * sizeof(unsigned int)));
+    // The tiled kernel: one block per SM, each block's share of the nodes
+    // resident in shared memory, where it fits.
+    ctx->cg_tile_blocks = 0;
+    {
+        // at least kTileThreads nodes a block, so that small grids take few
+        // blocks (and a short grid barrier)
+        int C = (int)((nn + sms - 1) / sms);
+        if (C < kTileThreads) C = kTileThreads;
+        // a block's halo (Nx + 1 nodes either side) must lie in the two
+        // neighbouring blocks, the only ones its point-to-point wait covers
+        if (C < ctx->cfg.Nx + 1) C = ctx->cfg.Nx + 1;
+        const int blocks = C > 0 ? (int)((nn + C - 1) / C) : 0;
+        const size_t smem = pcg_tile_smem(C, ctx->cfg.Nx);
+        int optin = 0;
+        MPMG_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
+        if (blocks > 0 && smem <= (size_t)optin && C <= kTileTrips * kTileThreads && blocks <= 8 * 32) {
+            MPMG_CHECK(cudaFuncSetAttribute(pcg_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+            int tile_per_sm = 0;
+            MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tile_per_sm, pcg_tile_kernel, kTileThreads,
+                                                                     smem));
+            if (tile_per_sm >= 1) {
+                ctx->cg_tile_blocks = blocks;
+                ctx->cg_tile_nodes = C;
+                ctx->cg_tile_smem = smem;
+            }
+        }
+    }
+    const int part_blocks = ctx->cg_blocks > ctx->cg_tile_blocks ? ctx->cg_blocks : ctx->cg_tile_blocks;
+    MPMG_CHECK(cudaMalloc(&ctx->cg_partials, 4 * (size_t)part_blocks * sizeof(double)));
+    // barrier counter + generation, then one neighbour flag per tiled block
+    MPMG_CHECK(cudaMalloc(&ctx->cg_barrier, (2 + (size_t)ctx->cg_tile_blocks) * sizeof(unsigned int)));
     MPMG_CHECK(cudaMemsetAsync(ctx->cg_barrier, 0, 2 * sizeof(unsigned int), ctx->stream));
     return MPMG_OK;
 }
@@ -568,11 +1027,20 @@ int mpmg_solve_fluidity_system(mpmg_ctx *ctx, const double *elem_k, const double
     S.barrier = ctx->cg_barrier;
     S.status = ctx->d_status;
     S.sp = ctx->d_params;
-    void *args[] = {&S};
     if (zero_start) MPMG_CHECK(cudaMemsetAsync(x, 0, ctx->nn * sizeof(double), s));
     MPMG_CHECK(cudaMemsetAsync(ctx->cg_barrier, 0, 2 * sizeof(unsigned int), s));
-    MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_kernel, dim3(ctx->cg_blocks),
-                                           dim3(kSolveThreads), args, 0, s));
+    if (ctx->cg_tile_blocks > 0) {
+        int C = ctx->cg_tile_nodes, warm = zero_start ? 0 : 1;
+        unsigned int *flags = ctx->cg_barrier + 2;
+        MPMG_CHECK(cudaMemsetAsync(flags, 0, (size_t)ctx->cg_tile_blocks * sizeof(unsigned int), s));
+        void *args[] = {&S, &C, &warm, &flags};
+        MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_tile_kernel, dim3(ctx->cg_tile_blocks),
+                                               dim3(kTileThreads), args, ctx->cg_tile_smem, s));
+    } else {
+        void *args[] = {&S};
+        MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_kernel, dim3(ctx->cg_blocks),
+                                               dim3(kSolveThreads), args, 0, s));
+    }
     ctx->launches += 1;
     MPMG_CHECK(cudaGetLastError());
     return MPMG_OK;
@@ -620,6 +1088,8 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     el.K = ctx->K;
     el.lambda = ctx->lambda;
     el.dt = c.dt;
+    el.inv_G = 1.0 / ctx->G;
+    el.inv_dt = 1.0 / c.dt;
     if (mu2) {
         fluidity_stress_kernel<true, false><<<blocks_for(n, 256), 256, 0, s>>>(
             n, c.Nx, ctx->Ex, el, np, ctx->d_params, ctx->active, ctx->in_element, ctx->xl, ctx->yl,

@@ -59,7 +59,8 @@ _lib = None
 
 class Tuning(C.Structure):
     _fields_ = [("g2p_blocks_per_sm", C.c_int), ("graph_steps", C.c_int), ("ms_per_step", C.c_double),
-                ("default_ms_per_step", C.c_double), ("candidates", C.c_int), ("steps_advanced", C.c_int)]
+                ("default_ms_per_step", C.c_double), ("candidates", C.c_int), ("steps_advanced", C.c_int),
+                ("p2g_elements", C.c_int), ("p2g_stage", C.c_int), ("g2p_tile", C.c_int)]
 
 
 def library_path():

@@ -189,3 +189,23 @@ def test_c3_silo_teacher_forced_step_vs_direct_solve():
         for f in ("sxx", "sxy", "syy", "state3"):
             assert ferr[f] <= bound, (tol, f, ferr[f])
     report("c3_silo_teacher_forced_step_vs_direct_solve", out)
+
+
+def test_large_grid_fluidity_solve_fallback_vs_oracle():
+    """A 601^2-node nonlocal silo (1.15 M particles): a block's share of the
+    nodes no longer fits in shared memory, so the grid-stride PCG runs
+    instead of the tiled one.  One step against the oracle's CG at the same
+    tight tolerance."""
+    sc = scenes.silo_prestressed(cells=600)
+    sim = mpm2d.Simulation(sc, store_transients=True, solver_tol=1e-12, solver_maxit=50000)
+    orc = O.Oracle(sc, nthreads=THREADS, solver="cg", cg_tol=1e-12)
+    sim.step(1)
+    orc.step(1)
+    rc, iters, resid = sim.last_solve()
+    assert rc == 0 and resid <= 1e-12
+    out = {"iterations": iters, "node_gf": rel_err(sim.get("node_gf"), orc.get("node_gf"))}
+    for f in ("sxx", "sxy", "syy", "x", "y", "vx", "vy"):
+        out[f] = field_err(sim.get(f), orc.get, f)
+        assert out[f] <= 1e-8, (f, out[f])
+    assert out["node_gf"] <= 1e-8, out
+    report("large_grid_fluidity_solve_fallback_vs_oracle", out)
