@@ -107,6 +107,21 @@ enum mpmg_scheme {
     MPMG_SCHEME_MUSL = 1
 };
 
+/* Preconditioner of the fluidity solve (g_nonlocal_mu2, g_nonlocal and
+   g_nonlocal_avg).  The reference factorises the assembled matrix
+   (g_nonlocal_mu2.c:510-519); this library solves the same system by
+   conjugate gradients to mpmg_config.solver_tol.
+   MPMG_PRECOND_MULTIGRID: one geometric-multigrid V-cycle on the node lattice
+   per iteration (Galerkin coarse operators, FP32 cycle, FP64 outer
+   iteration).  It takes 5 to 10 iterations where Jacobi takes hundreds.  It
+   is used where a block's share of the grid fits the kernel (up to about
+   280 000 nodes on a GB300); larger grids fall back to Jacobi.
+   MPMG_PRECOND_JACOBI: diagonal scaling. */
+enum mpmg_precond {
+    MPMG_PRECOND_MULTIGRID = 0,
+    MPMG_PRECOND_JACOBI = 1
+};
+
 /* Material parameter slots (mpmg_config.mp).  mpmg_default_params fills the
    reference's compile-time constants for a material kind. */
 enum mpmg_mparam {
@@ -145,6 +160,7 @@ typedef struct mpmg_config {
                                 the iterations. */
     int precision;           /* enum mpmg_precision */
     int scheme;              /* enum mpmg_scheme */
+    int solver_precond;      /* enum mpmg_precond (default multigrid) */
 } mpmg_config;
 
 typedef struct mpmg_ctx mpmg_ctx;

@@ -432,6 +432,10 @@ int validate_config(const mpmg_config *cfg, size_t n)
         mpmg_set_error("unknown boundary-condition kind %d", cfg->bc);
         return MPMG_ERR_UNSUPPORTED;
     }
+    if (cfg->solver_precond != MPMG_PRECOND_MULTIGRID && cfg->solver_precond != MPMG_PRECOND_JACOBI) {
+        mpmg_set_error("unknown fluidity preconditioner %d", cfg->solver_precond);
+        return MPMG_ERR_INVALID;
+    }
     if (cfg->precision < MPMG_PRECISION_FP64 || cfg->precision > MPMG_PRECISION_MIXED_F64NODE) {
         mpmg_set_error("unknown precision %d", cfg->precision);
         return MPMG_ERR_INVALID;

@@ -150,6 +150,13 @@ struct mpmg_ctx {
     int cg_tile_blocks;    // pcg_tile_kernel: blocks (0: the grid does not fit, pcg_kernel runs)
     int cg_tile_nodes;     // pcg_tile_kernel: nodes per block
     size_t cg_tile_smem;   // pcg_tile_kernel: dynamic shared memory per block
+    // multigrid-preconditioned solve (pcg_mg_kernel): level table on the host
+    // and its device copy (NULL when the grid does not fit the kernel), pools
+    struct MgPlan *mg_host, *mg_dev;
+    float *mg_rows;
+    unsigned long long *mg_words;
+    unsigned int *mg_tag;
+    size_t mg_smem;
 
     StepParams *d_params;  // one record per simulation (a batch holds several)
     StepParams h_params;   // host mirror of the first, refreshed on read-back

@@ -20,6 +20,27 @@
 #include "mpmg_internal.cuh"
 #include "mpmg_materials.cuh"
 
+// Level table of the multigrid preconditioner (pcg_mg_kernel), built at
+// set-up: level l has Nx x Ny nodes, C of them per block; its node arrays
+// start at node g of the global pools and its per-block arrays at float sm
+// of a block's shared memory.
+constexpr int kMgMaxLevels = 16;
+
+struct MgLevel {
+    int Nx, Ny, nn, C;
+    int cx, cy;            // coarsened from the finer level along x, y (level 0: 0)
+    int g;                 // first node of the level in the global pools
+    int sm;                // first float of the level's arrays in shared memory
+};
+
+struct MgPlan {
+    int L, nblocks, total; // levels, blocks, nodes over all levels
+    MgLevel lv[kMgMaxLevels];
+    float *rows;           // [5][total]: east, north, north-east, north-west, row sum
+    unsigned long long *z1, *res, *zf;   // [total] tagged words each
+    unsigned int *tag;     // tag counter
+};
+
 namespace {
 
 constexpr int kSolveThreads = 256;
@@ -854,6 +875,816 @@ inline size_t pcg_tile_smem(int C, int Nx)
     return sizeof(double) * ((size_t)15 * C + 2 * (size_t)(Nx + 1) + 3 * kTileThreads + 8);
 }
 
+// ---------------------------------------------------------------------------
+// Multigrid-preconditioned conjugate gradients (pcg_mg_kernel).
+//
+// Jacobi-PCG needs O(l / h) iterations on this operator, where l is the size
+// of the regions near yield: there the cooperativity length grows, xi^-2
+// falls, and the Laplacian part dominates.  On the 513^2 silo it took 30
+// iterations a step after 4 steps, 137 after 18 and 809 after 60.  A
+// geometric multigrid V-cycle on the node lattice makes the count nearly
+// independent of the grid: 6 to 9 iterations on the same systems.
+//
+// Hierarchy.  Level 0 is the node lattice.  Level l + 1 keeps every second
+// node of level l along each direction with more than 3 nodes
+// (n -> n / 2 + 1), down to at most 3 x 3 nodes.  Prolongation P is bilinear
+// interpolation, restriction is P^T, and the coarse operators are the
+// Galerkin products A_{l+1} = P^T A_l P, formed every solve in FP32.
+//
+// Storage of a level.  Each node stores its four upper stencil entries
+// (east, north, north-east, north-west) and its row sum s = A 1.  The lower
+// entries are the neighbours' upper ones, so every level is exactly
+// symmetric.  The diagonal is s minus the off-diagonal sum.  P reproduces
+// constants, so the coarse row sums are P^T s.  The near-null space of a
+// Neumann-like operator (only the 1e-10 shift and the xi^-2-weighted mass
+// keep it from being singular) therefore survives FP32 coarsening.
+//
+// Preconditioner: one V(1,1) cycle in FP32 on r / |r|.
+//   * On each level, one l1-Jacobi step (Baker, Falgout, Kolev and Yang,
+//     2011).  D_l1 is each row's absolute sum, so the smoother converges
+//     without an eigenvalue estimate.  The step size is the Chebyshev step
+//     for the interval [0.3, 1] of D_l1^-1 A.
+//   * Then the residual and its restriction.
+//   * At the coarsest level, an exact solve: an FP64 inverse formed every
+//     solve.
+//   * On the way up, prolongation and one post-smoothing step of the same
+//     size, so the cycle is symmetric.
+//
+// Outer iteration: FP64 CG in the one-reduction form of Chronopoulos and
+// Gear.  It uses the Polak-Ribiere beta, which tolerates the rounding of an
+// FP32 preconditioner:
+//   beta  = -alpha <s, u> / gamma_old
+//   pi    = delta + 2 beta <s, u> + beta^2 pi_old
+//   alpha = gamma / pi
+// where u = M r, w = A u, gamma = <r, u>, delta = <w, u>, and s = A p by
+// recurrence.  Each iteration needs one grid barrier, for the four inner
+// products.
+//
+// Synchronisation inside the V-cycle.  Each phase writes its level vector to
+// global memory as 64-bit words: an FP32 value plus a 32-bit tag that names
+// the V-cycle.  A consumer loads the words it needs and polls again those
+// whose tag is not yet current, so each phase waits for exactly the values
+// it reads.  A word is stored with one single-copy-atomic 64-bit store, so
+// its value and tag arrive together, with no fences or flags.
+//   * Each phase vector is written once per V-cycle, and the outer grid
+//     barrier separates V-cycles, so no value is overwritten while a reader
+//     may still need it.
+//   * Each solve reserves its tags (maxit + 2, from a counter in device
+//     memory), so it never accepts a word written by an earlier solve.
+//   * Polls are bounded, like the barriers.
+
+constexpr int kMgThreads = 512;
+constexpr int kMgTrips = 4;            // nodes of a level a thread owns at most
+constexpr int kMgCoarse = 9;           // nodes of the coarsest level at most (3 x 3)
+// one smoothing step: the Chebyshev step for [0.3, 1], 1 / 0.65
+constexpr float kMgOmega = 1.0f / 0.65f;
+
+__device__ __forceinline__ unsigned long long mg_ld(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ void mg_st(unsigned long long *p, float x, unsigned tag)
+{
+    const unsigned long long v = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(x);
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v));
+}
+
+// A word that needs no wait: value 0 with the current tag.
+__device__ __forceinline__ unsigned long long mg_zero(unsigned tag)
+{
+    return (unsigned long long)tag << 32;
+}
+
+// Polls one word until it carries `tag`.  Bounded: after kSpinLimit polls,
+// or once another block has timed out, the spin error is set and 0 returned.
+__device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag, int *status)
+{
+    for (long long polls = 1;; polls++) {
+        const unsigned long long v = mg_ld(p);
+        if ((unsigned)(v >> 32) == tag) return __uint_as_float((unsigned)v);
+        if ((polls & 31) == 0 &&
+            (polls > kSpinLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0)) {
+            atomicOr(status, MPMG_DEV_ERR_SPIN);
+            return 0.0f;
+        }
+        __nanosleep(20);
+    }
+}
+
+// Value of a loaded word, polling its address again if its tag is stale.
+__device__ __forceinline__ float mg_val(unsigned long long v, const unsigned long long *p, unsigned tag, int *status)
+{
+    return (unsigned)(v >> 32) == tag ? __uint_as_float((unsigned)v) : mg_poll(p, tag, status);
+}
+
+// Block arrays of a level in shared memory (floats): coef[9][C] (the full
+// stencil, q = 3 (dj + 1) + (di + 1)), l1inv[C], b[C], z1[C], res[C].
+struct MgShared {
+    float *coef, *l1inv, *b, *z1, *res;
+};
+
+__device__ __forceinline__ MgShared mg_shared(float *sm, const MgLevel &lv)
+{
+    MgShared s;
+    s.coef = sm + lv.sm;
+    s.l1inv = s.coef + 9 * lv.C;
+    s.b = s.l1inv + lv.C;
+    s.z1 = s.b + lv.C;
+    s.res = s.z1 + lv.C;
+    return s;
+}
+
+// The full stencil of node (i, j) of a level from the stored upper entries
+// and the row sum: a[q], q = 3 (dj + 1) + (di + 1); a[4] = s - sum of the
+// others.  Entries towards nodes outside the grid are zero.
+__device__ __forceinline__ void mg_stencil(const MgPlan &P, const MgLevel &lv, int n, int i, int j, float a[9])
+{
+    const float *E = P.rows + lv.g, *N = E + P.total, *NE = N + P.total, *NW = NE + P.total, *S = NW + P.total;
+    const int Nx = lv.Nx;
+    const bool w = i > 0, e = i + 1 < lv.Nx, s = j > 0, nn = j + 1 < lv.Ny;
+    a[5] = e ? __ldcg(E + n) : 0.0f;
+    a[3] = w ? __ldcg(E + n - 1) : 0.0f;
+    a[7] = nn ? __ldcg(N + n) : 0.0f;
+    a[1] = s ? __ldcg(N + n - Nx) : 0.0f;
+    a[8] = (e && nn) ? __ldcg(NE + n) : 0.0f;
+    a[0] = (w && s) ? __ldcg(NE + n - Nx - 1) : 0.0f;
+    a[6] = (w && nn) ? __ldcg(NW + n) : 0.0f;
+    a[2] = (e && s) ? __ldcg(NW + n - Nx + 1) : 0.0f;
+    const float rs = __ldcg(S + n);
+    a[4] = rs - (((a[0] + a[1]) + (a[2] + a[3])) + ((a[5] + a[6]) + (a[7] + a[8])));
+}
+
+// Coarse parents of fine coordinate g along a direction: g even (or the
+// direction not coarsened) -> one parent with weight 1; g odd -> the two
+// coarse neighbours with weight 1/2.
+__device__ __forceinline__ int mg_parents(int g, int coarsened, int &p0, int &p1)
+{
+    if (!coarsened) {
+        p0 = p1 = g;
+        return 1;
+    }
+    p0 = g >> 1;
+    p1 = (g + 1) >> 1;
+    return (g & 1) ? 2 : 1;
+}
+
+// Fine coordinate of support slot s (0, 1, 2) of coarse coordinate c, or -1.
+__device__ __forceinline__ int mg_fine_of(int c, int s, int coarsened)
+{
+    return coarsened ? 2 * c + s - 1 : (s == 1 ? c : -1);
+}
+
+// Galerkin row of coarse node (ci, cj) of level c from level c - 1: the
+// four upper entries and the row sum, written to the level's rows.
+__device__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
+{
+    const MgLevel &F = P.lv[c - 1], &Cl = P.lv[c];
+    float acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) acc[q] = 0.0f;
+    float srow = 0.0f;
+    const float *Sf = P.rows + 4 * (size_t)P.total + F.g;
+    for (int sy = 0; sy < 3; sy++) {
+        const int fy = mg_fine_of(cj, sy, Cl.cy);
+        if (fy < 0 || fy >= F.Ny) continue;
+        const float wy = (sy == 1) ? 1.0f : 0.5f;
+        for (int sx = 0; sx < 3; sx++) {
+            const int fx = mg_fine_of(ci, sx, Cl.cx);
+            if (fx < 0 || fx >= F.Nx) continue;
+            const float wi = wy * ((sx == 1) ? 1.0f : 0.5f);
+            const int fi = fy * F.Nx + fx;
+            srow = fmaf(wi, __ldcg(Sf + fi), srow);
+            float a[9];
+            mg_stencil(P, F, fi, fx, fy, a);
+#pragma unroll
+            for (int q = 0; q < 9; q++) {
+                const int gx = fx + q % 3 - 1, gy = fy + q / 3 - 1;
+                if (gx < 0 || gx >= F.Nx || gy < 0 || gy >= F.Ny) continue;
+                int px0, px1, py0, py1;
+                const int npx = mg_parents(gx, Cl.cx, px0, px1);
+                const int npy = mg_parents(gy, Cl.cy, py0, py1);
+                const float v = wi * a[q] * ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
+                acc[(py0 - cj + 1) * 3 + (px0 - ci + 1)] += v;
+                if (npx == 2) acc[(py0 - cj + 1) * 3 + (px1 - ci + 1)] += v;
+                if (npy == 2) acc[(py1 - cj + 1) * 3 + (px0 - ci + 1)] += v;
+                if (npx == 2 && npy == 2) acc[(py1 - cj + 1) * 3 + (px1 - ci + 1)] += v;
+            }
+        }
+    }
+    float *R = P.rows + Cl.g + I;
+    R[0] = acc[5];
+    R[P.total] = acc[7];
+    R[2 * (size_t)P.total] = acc[8];
+    R[3 * (size_t)P.total] = acc[6];
+    R[4 * (size_t)P.total] = srow;
+}
+
+// Sum of four values over the block in a fixed order, returned to every
+// thread (warp 0 adds; scratch holds 4 * blockDim.x + 4 doubles).
+__device__ __forceinline__ void mg_sum4(double v[4], double *scratch)
+{
+    const int nt = blockDim.x;
+#pragma unroll
+    for (int c = 0; c < 4; c++) scratch[c * nt + threadIdx.x] = v[c];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double a[4][2];
+#pragma unroll
+        for (int c = 0; c < 4; c++) a[c][0] = a[c][1] = 0;
+        for (int t = lane; t < nt; t += 64) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                a[c][0] += scratch[c * nt + t];
+                if (t + 32 < nt) a[c][1] += scratch[c * nt + t + 32];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            double x = a[c][0] + a[c][1];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+            if (lane == 0) scratch[4 * nt + c] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 4; c++) v[c] = scratch[4 * nt + c];
+    __syncthreads();
+}
+
+// The four per-block partials summed over all blocks in one fixed order by
+// warp 0; every block computes the same totals.
+__device__ __forceinline__ void mg_totals4(const double *partials, int nblocks, double v[4], double *scratch)
+{
+    const int nt = blockDim.x;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        constexpr int kMax = 8;     // blocks <= 32 * kMax
+        double x[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < kMax; q++) {
+            const int t = lane + 32 * q;
+            if (t < nblocks) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) x[c] += __ldcg(partials + (size_t)c * nblocks + t);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) x[c] += __shfl_down_sync(0xffffffffu, x[c], off);
+            if (lane == 0) scratch[4 * nt + c] = x[c];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 4; c++) v[c] = scratch[4 * nt + c];
+    __syncthreads();
+}
+
+// Residual phase of level l: res = b - A z1 (z1 of the neighbours from the
+// tagged words), kept in shared memory and published.
+__device__ __forceinline__ void mg_residual(const MgPlan &P, int l, const MgShared &S, unsigned tag, int *status)
+{
+    const MgLevel &lv = P.lv[l];
+    const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
+    const unsigned long long *z1 = P.z1 + lv.g;
+    unsigned long long v[kMgTrips][9];
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        const int n = n0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int di = q % 3 - 1, dj = q / 3 - 1;
+            const bool in = k < cnt && i + di >= 0 && i + di < lv.Nx && j + dj >= 0 && j + dj < lv.Ny;
+            v[t][q] = in ? mg_ld(z1 + n + dj * lv.Nx + di) : mg_zero(tag);
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        if (k >= cnt) continue;
+        const int n = n0 + k;
+        float acc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            // entries towards nodes outside the grid are zero and their words
+            // carry the current tag (no load, no wait)
+            const int di = q % 3 - 1, dj = q / 3 - 1;
+            acc = fmaf(S.coef[q * lv.C + k], mg_val(v[t][q], z1 + n + dj * lv.Nx + di, tag, status), acc);
+        }
+        const float r = S.b[k] - acc;
+        S.res[k] = r;
+        mg_st(P.res + lv.g + n, r, tag);
+    }
+}
+
+// Restriction to level c (its own nodes): b = P^T res of level c - 1, then
+// the pre-smoothing step z1 = omega D_l1^-1 b (published), or at the
+// coarsest level b itself (published in the res words for the exact solve).
+__device__ __forceinline__ void mg_restrict(const MgPlan &P, int c, const MgShared &S, unsigned tag, int *status)
+{
+    const MgLevel &F = P.lv[c - 1], &lv = P.lv[c];
+    const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
+    const unsigned long long *res = P.res + F.g;
+    unsigned long long v[kMgTrips][9];
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        const int I = n0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
+            const bool in = k < cnt && fx >= 0 && fx < F.Nx && fy >= 0 && fy < F.Ny;
+            v[t][q] = in ? mg_ld(res + fy * F.Nx + fx) : mg_zero(tag);
+        }
+    }
+    const bool coarsest = c == P.L - 1;
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        if (k >= cnt) continue;
+        const int I = n0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
+        float b = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
+            if (fx < 0 || fx >= F.Nx || fy < 0 || fy >= F.Ny) continue;
+            const float w = ((q % 3 == 1) ? 1.0f : 0.5f) * ((q / 3 == 1) ? 1.0f : 0.5f);
+            b = fmaf(w, mg_val(v[t][q], res + fy * F.Nx + fx, tag, status), b);
+        }
+        S.b[k] = b;
+        if (coarsest) {
+            mg_st(P.res + lv.g + I, b, tag);
+        } else {
+            const float z = kMgOmega * S.l1inv[k] * b;
+            S.z1[k] = z;
+            mg_st(P.z1 + lv.g + I, z, tag);
+        }
+    }
+}
+
+// Coarse window [x0, x1] x [y0, y1] holding the parents of fine node (i, j)
+// and of its eight neighbours (at most 3 x 3 coarse nodes).
+__device__ __forceinline__ void mg_window(const MgLevel &lv, const MgLevel &Cl, int i, int j, int &x0, int &x1,
+                                          int &y0, int &y1)
+{
+    int a, b;
+    mg_parents(max(i - 1, 0), Cl.cx, x0, a);
+    mg_parents(min(i + 1, lv.Nx - 1), Cl.cx, a, x1);
+    mg_parents(max(j - 1, 0), Cl.cy, y0, b);
+    mg_parents(min(j + 1, lv.Ny - 1), Cl.cy, b, y1);
+}
+
+// Prolongation and post-smoothing at level l from the coarse solution of
+// level l + 1: with z2 = z1 + P zc and res = b - A z1,
+//   z = z2 + omega D_l1^-1 (res - A P zc)   (published; zero off the unknowns)
+__device__ __forceinline__ void mg_prolong(const MgPlan &P, int l, const MgShared &S, unsigned tag, int *status)
+{
+    const MgLevel &lv = P.lv[l], &Cl = P.lv[l + 1];
+    const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
+    const unsigned long long *zc = P.zf + Cl.g;
+    unsigned long long v[kMgTrips][9];
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        const int n = n0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
+        int x0, x1, y0, y1;
+        mg_window(lv, Cl, i, j, x0, x1, y0, y1);
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int cx = x0 + q % 3, cy = y0 + q / 3;
+            const bool in = k < cnt && cx <= x1 && cy <= y1;
+            v[t][q] = in ? mg_ld(zc + cy * Cl.Nx + cx) : mg_zero(tag);
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        if (k >= cnt) continue;
+        const int n = n0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
+        int x0, x1, y0, y1;
+        mg_window(lv, Cl, i, j, x0, x1, y0, y1);
+        float zv[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int cx = x0 + q % 3, cy = y0 + q / 3;
+            zv[q] = mg_val(v[t][q], zc + cy * Cl.Nx + cx, tag, status);
+        }
+        float acc = 0.0f, own = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int gx = i + q % 3 - 1, gy = j + q / 3 - 1;
+            if (gx < 0 || gx >= lv.Nx || gy < 0 || gy >= lv.Ny) continue;
+            int px0, px1, py0, py1;
+            const int npx = mg_parents(gx, Cl.cx, px0, px1);
+            const int npy = mg_parents(gy, Cl.cy, py0, py1);
+            const int ax = px0 - x0, ay = py0 - y0, bx = px1 - x0, by = py1 - y0;
+            float pz = zv[ay * 3 + ax];
+            if (npx == 2) pz += zv[ay * 3 + bx];
+            if (npy == 2) pz += zv[by * 3 + ax];
+            if (npx == 2 && npy == 2) pz += zv[by * 3 + bx];
+            pz *= ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
+            if (q == 4) own = pz;
+            acc = fmaf(S.coef[q * lv.C + k], pz, acc);
+        }
+        const float li = S.l1inv[k];
+        const float z = (li == 0.0f) ? 0.0f : S.z1[k] + own + kMgOmega * li * (S.res[k] - acc);
+        mg_st(P.zf + lv.g + n, z, tag);
+    }
+}
+
+// The V-cycle on b0 (already in level 0's b): the result lands in level 0's
+// zf words with this tag.
+__device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, double *cb, unsigned tag, int *status)
+{
+    const int L = P.L;
+    {
+        // pre-smoothing at level 0 (or, on a one-level hierarchy, b for the
+        // exact solve)
+        const MgLevel &lv = P.lv[0];
+        const MgShared S = mg_shared(sm, lv);
+        const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
+        for (int k = threadIdx.x; k < cnt; k += kMgThreads) {
+            if (L == 1) {
+                mg_st(P.res + n0 + k, S.b[k], tag);
+            } else {
+                const float z = kMgOmega * S.l1inv[k] * S.b[k];
+                S.z1[k] = z;
+                mg_st(P.z1 + n0 + k, z, tag);
+            }
+        }
+    }
+    for (int l = 0; l + 1 < L; l++) {
+        mg_residual(P, l, mg_shared(sm, P.lv[l]), tag, status);
+        mg_restrict(P, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
+    }
+    // exact solve at the coarsest level (block 0)
+    if (blockIdx.x == 0) {
+        const MgLevel &lv = P.lv[L - 1];
+        const int nc = lv.nn;
+        if (threadIdx.x < nc) cb[threadIdx.x] = mg_poll(P.res + lv.g + threadIdx.x, tag, status);
+        __syncthreads();
+        if (threadIdx.x < nc) {
+            double z = 0;
+            for (int m = 0; m < nc; m++) z = fma(cinv[threadIdx.x * kMgCoarse + m], cb[m], z);
+            mg_st(P.zf + lv.g + threadIdx.x, (float)z, tag);
+        }
+    }
+    for (int l = L - 2; l >= 0; l--) mg_prolong(P, l, mg_shared(sm, P.lv[l]), tag, status);
+}
+
+// Shared memory of pcg_mg_kernel: the level arrays (13 floats a node of
+// each level a block owns), five FP64 outer vectors a level-0 node, the
+// reduction scratch, the coarsest inverse, its right-hand side and the
+// elimination matrix.
+inline size_t pcg_mg_smem(const MgPlan &P)
+{
+    size_t floats = 0;
+    for (int l = 0; l < P.L; l++) floats += 13 * (size_t)P.lv[l].C;
+    floats = (floats + 1) & ~(size_t)1;
+    const size_t doubles = 5 * (size_t)P.lv[0].C + 4 * (size_t)kMgThreads + 4 + kMgCoarse * kMgCoarse + kMgCoarse +
+                           2 * kMgCoarse * kMgCoarse;
+    return floats * sizeof(float) + doubles * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, const MgPlan *__restrict__ plan,
+                                                                int warm)
+{
+    extern __shared__ double smd[];
+    // the level table, indexed by level below, from global memory into
+    // shared memory
+    __shared__ MgPlan P;
+    for (int e = threadIdx.x; e < (int)(sizeof(MgPlan) / sizeof(int)); e += blockDim.x)
+        reinterpret_cast<int *>(&P)[e] = __ldg(reinterpret_cast<const int *>(plan) + e);
+    __syncthreads();
+    float *sm = reinterpret_cast<float *>(smd);
+    const int Nx = S.Nx, Ny = S.Ny, nn = Nx * Ny;
+    const int nblocks = gridDim.x;
+    const MgLevel &L0 = P.lv[0];
+    const int n0 = blockIdx.x * L0.C, cnt = min(L0.C, nn - n0);
+    size_t fl = 0;
+    for (int l = 0; l < P.L; l++) fl += 13 * (size_t)P.lv[l].C;
+    double *dv = smd + ((fl + 1) >> 1);
+    double *r = dv, *p = r + L0.C, *s = p + L0.C, *w = s + L0.C, *u = w + L0.C;
+    double *scratch = u + L0.C;                       // 4 kMgThreads + 4
+    double *cinv = scratch + 4 * kMgThreads + 4;      // kMgCoarse^2
+    double *cb = cinv + kMgCoarse * kMgCoarse;        // kMgCoarse
+    double *gj = cb + kMgCoarse;                      // kMgCoarse x 2 kMgCoarse (coarsest inverse)
+    __shared__ double sh_scalar[3];
+    __shared__ int sh_next;
+    unsigned int episode = 0;
+    unsigned tag0;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(tag0) : "l"(P.tag));
+    double x[kMgTrips];
+
+    // Level 0: FP64 rows (global, for the outer matvec), right-hand side,
+    // start; FP32 upper entries and row sums.  Entries towards nodes that are
+    // not unknowns are left out of the FP32 rows, whose zeroed rows keep them
+    // symmetric.
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        x[t] = 0;
+        if (k >= cnt) continue;
+        const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+        double cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        double f = 0;
+        const bool dof = S.node_m[n] > S.dof_tol;
+        bool coupled = false;
+        if (dof) {
+            build_row(S, i, j, cf, &f);
+#pragma unroll
+            for (int q = 0; q < 9; q++) coupled |= (__double_as_longlong(cf[q]) << 1) != 0;
+            cf[4] += S.shift;
+        }
+        const bool unknown = dof && cf[4] > 0;
+        if (unknown) {
+            r[k] = f;
+            x[t] = (warm && coupled) ? S.x[n] : 0.0;
+        } else {
+            r[k] = 0;
+#pragma unroll
+            for (int q = 0; q < 9; q++) cf[q] = 0;
+        }
+        p[k] = 0;
+        s[k] = 0;
+#pragma unroll
+        for (int q = 0; q < 9; q++) S.coef[(size_t)q * nn + n] = cf[q];
+        S.x[n] = x[t];
+        double rsum = 0;
+        bool nbu[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int di = q % 3 - 1, dj = q / 3 - 1;
+            const bool in = i + di >= 0 && i + di < Nx && j + dj >= 0 && j + dj < Ny;
+            nbu[q] = unknown && (q == 4 || (in && S.node_m[n + dj * Nx + di] > S.dof_tol));
+            if (nbu[q]) rsum += cf[q];
+        }
+        float *R = P.rows + n;
+        R[0] = nbu[5] ? (float)cf[5] : 0.0f;
+        R[P.total] = nbu[7] ? (float)cf[7] : 0.0f;
+        R[2 * (size_t)P.total] = nbu[8] ? (float)cf[8] : 0.0f;
+        R[3 * (size_t)P.total] = nbu[6] ? (float)cf[6] : 0.0f;
+        R[4 * (size_t)P.total] = (float)rsum;
+    }
+    if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+    // every block has read the tag counter: reserve this solve's tags
+    if (blockIdx.x == 0 && threadIdx.x == 0) *P.tag = tag0 + (unsigned)S.maxit + 2u;
+
+    // Coarse levels: Galerkin rows, one level after another.
+    for (int c = 1; c < P.L; c++) {
+        const MgLevel &lv = P.lv[c];
+        const int c0 = blockIdx.x * lv.C, ccnt = min(lv.C, lv.nn - c0);
+        for (int k = threadIdx.x; k < ccnt; k += kMgThreads) {
+            const int I = c0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
+            mg_galerkin_row(P, c, I, ci, cj);
+        }
+        if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+    }
+    // Each block's rows of every level into shared memory, with D_l1^-1.
+    for (int l = 0; l < P.L; l++) {
+        const MgLevel &lv = P.lv[l];
+        const MgShared Sh = mg_shared(sm, lv);
+        const int l0 = blockIdx.x * lv.C, lcnt = min(lv.C, lv.nn - l0);
+        for (int k = threadIdx.x; k < lcnt; k += kMgThreads) {
+            const int n = l0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
+            float a[9];
+            mg_stencil(P, lv, n, i, j, a);
+            float l1 = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 9; q++) l1 += fabsf(a[q]);
+            const float li = l1 > 0.0f ? 1.0f / l1 : 0.0f;
+#pragma unroll
+            for (int q = 0; q < 9; q++) Sh.coef[q * lv.C + k] = li > 0.0f ? a[q] : 0.0f;
+            Sh.l1inv[k] = li;
+        }
+    }
+    // The coarsest level's inverse (block 0): Gauss-Jordan on the symmetric
+    // positive definite matrix of its active nodes, in FP64.  A node whose
+    // pivot is not positive is left out (its correction is zero).
+    if (blockIdx.x == 0) {
+        const MgLevel &lv = P.lv[P.L - 1];
+        const int nc = lv.nn, w2 = 2 * kMgCoarse;
+        for (int e = threadIdx.x; e < kMgCoarse * w2; e += kMgThreads) gj[e] = 0;
+        __syncthreads();
+        if (threadIdx.x < nc) {
+            const int a = threadIdx.x, j = a / lv.Nx, i = a - j * lv.Nx;
+            float st[9];
+            mg_stencil(P, lv, a, i, j, st);
+            double off = 0;
+#pragma unroll
+            for (int q = 0; q < 9; q++) {
+                if (q == 4) continue;
+                const int di = q % 3 - 1, dj = q / 3 - 1;
+                if (i + di < 0 || i + di >= lv.Nx || j + dj < 0 || j + dj >= lv.Ny) continue;
+                gj[a * w2 + (a + dj * lv.Nx + di)] = st[q];
+                off += (double)st[q];
+            }
+            gj[a * w2 + a] = (double)__ldcg(P.rows + 4 * (size_t)P.total + lv.g + a) - off;
+            gj[a * w2 + kMgCoarse + a] = 1.0;
+        }
+        __syncthreads();
+        for (int piv = 0; piv < nc; piv++) {
+            const double d = gj[piv * w2 + piv];
+            const bool keep = d > 0;
+            // this step's factors, read before the rows change
+            const int row = threadIdx.x / w2, col = threadIdx.x % w2;
+            const bool mine = threadIdx.x < nc * w2;
+            const double fac = mine ? gj[row * w2 + piv] : 0.0;
+            const double pv = mine ? gj[piv * w2 + col] : 0.0;
+            __syncthreads();
+            if (mine) {
+                if (!keep) {
+                    if (row == piv || col == piv || col == kMgCoarse + piv) gj[row * w2 + col] = 0;
+                } else if (row == piv) {
+                    gj[row * w2 + col] = pv / d;
+                } else {
+                    gj[row * w2 + col] -= fac * (pv / d);
+                }
+            }
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < kMgCoarse * kMgCoarse; e += kMgThreads) {
+            const int a = e / kMgCoarse, b = e % kMgCoarse;
+            cinv[e] = (a < nc && b < nc) ? gj[a * w2 + kMgCoarse + b] : 0.0;
+        }
+        __syncthreads();
+    }
+
+    // r = b - A x, <b, b>, <r, r> (x of the neighbours is final since the
+    // first barrier)
+    double part[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        if (k >= cnt) continue;
+        const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+        const double b = r[k];
+        double ax = 0;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int di = q % 3 - 1, dj = q / 3 - 1;
+            if (i + di < 0 || i + di >= Nx || j + dj < 0 || j + dj >= Ny) continue;
+            ax = fma(S.coef[(size_t)q * nn + n], __ldcg(S.x + n + dj * Nx + di), ax);
+        }
+        const double rk = b - ax;
+        r[k] = rk;
+        part[0] = fma(b, b, part[0]);
+        part[1] = fma(rk, rk, part[1]);
+    }
+    mg_sum4(part, scratch);
+    if (threadIdx.x == 0) {
+        S.partials[0 * nblocks + blockIdx.x] = part[0];
+        S.partials[1 * nblocks + blockIdx.x] = part[1];
+        S.partials[2 * nblocks + blockIdx.x] = 0;
+        S.partials[3 * nblocks + blockIdx.x] = 0;
+    }
+    if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+    mg_totals4(S.partials, nblocks, part, scratch);
+    const double bb = part[0];
+    double rr = part[1];
+    const double target = S.tol * S.tol * bb;
+
+    int it = 0;
+    bool converged = false, failed = false;
+    double alpha = 0, beta = 0, pi = 0, gamma = 0;
+    if (bb == 0) {
+#pragma unroll
+        for (int t = 0; t < kMgTrips; t++) x[t] = 0;     // no load: the solution is zero
+        rr = 0;
+        converged = true;
+    } else if (rr <= target) {
+        converged = true;                                 // the start already meets the tolerance
+    }
+    for (int v = 0; !converged && !failed; v++) {
+        if (v > 0) {
+            // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s
+#pragma unroll
+            for (int t = 0; t < kMgTrips; t++) {
+                const int k = threadIdx.x + t * kMgThreads;
+                if (k >= cnt) continue;
+                const double pk = fma(beta, p[k], u[k]);
+                const double sk = fma(beta, s[k], w[k]);
+                p[k] = pk;
+                s[k] = sk;
+                x[t] = fma(alpha, pk, x[t]);
+                r[k] = fma(-alpha, sk, r[k]);
+            }
+            it++;
+        }
+        // u = |r| V(r / |r|) (|r| of the last reduction), w = A u, and the
+        // inner products
+        const double sig = sqrt(rr), isig = 1.0 / sig;
+        {
+            const MgShared Sh = mg_shared(sm, L0);
+#pragma unroll
+            for (int t = 0; t < kMgTrips; t++) {
+                const int k = threadIdx.x + t * kMgThreads;
+                if (k < cnt) Sh.b[k] = (float)(r[k] * isig);
+            }
+        }
+        const unsigned tag = tag0 + (unsigned)v;
+        mg_vcycle(P, sm, cinv, cb, tag, S.status);
+        {
+            const unsigned long long *zf = P.zf;
+            unsigned long long wv[kMgTrips][9];
+#pragma unroll
+            for (int t = 0; t < kMgTrips; t++) {
+                const int k = threadIdx.x + t * kMgThreads;
+                const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+#pragma unroll
+                for (int q = 0; q < 9; q++) {
+                    const int di = q % 3 - 1, dj = q / 3 - 1;
+                    const bool in = k < cnt && i + di >= 0 && i + di < Nx && j + dj >= 0 && j + dj < Ny;
+                    wv[t][q] = in ? mg_ld(zf + n + dj * Nx + di) : mg_zero(tag);
+                }
+            }
+            part[0] = part[1] = part[2] = part[3] = 0;
+#pragma unroll
+            for (int t = 0; t < kMgTrips; t++) {
+                const int k = threadIdx.x + t * kMgThreads;
+                if (k >= cnt) continue;
+                const int n = n0 + k;
+                double az = 0, own = 0;
+#pragma unroll
+                for (int q = 0; q < 9; q++) {
+                    // rows are zero towards nodes outside the grid, whose
+                    // words read 0 with the current tag
+                    const int di = q % 3 - 1, dj = q / 3 - 1;
+                    const double zq = (double)mg_val(wv[t][q], zf + n + dj * Nx + di, tag, S.status);
+                    if (q == 4) own = zq;
+                    az = fma(S.coef[(size_t)q * nn + n], zq, az);
+                }
+                const double uk = sig * own, wk = sig * az, rk = r[k];
+                u[k] = uk;
+                w[k] = wk;
+                part[0] = fma(rk, uk, part[0]);
+                part[1] = fma(wk, uk, part[1]);
+                part[2] = fma(s[k], uk, part[2]);
+                part[3] = fma(rk, rk, part[3]);
+            }
+        }
+        mg_sum4(part, scratch);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) S.partials[c * nblocks + blockIdx.x] = part[c];
+        }
+        if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+        mg_totals4(S.partials, nblocks, part, scratch);
+        const double gn = part[0], dl = part[1], sg = part[2];
+        rr = part[3];
+        if (threadIdx.x == 0) {
+            int next = 0;                       // 0: go on, 1: give up, 2: converged
+            if (!(rr == rr)) {
+                next = 1;                       // NaN
+            } else if (rr <= target) {
+                next = 2;
+            } else if (it >= S.maxit) {
+                next = 1;
+            } else {
+                const double bn = (v == 0) ? 0.0 : -alpha * sg / gamma;
+                const double pn = dl + 2.0 * bn * sg + bn * bn * pi;
+                if (!(pn > 0)) {
+                    next = 1;                   // breakdown: report non-convergence
+                } else {
+                    sh_scalar[0] = bn;
+                    sh_scalar[1] = pn;
+                    sh_scalar[2] = gn / pn;
+                }
+            }
+            sh_next = next;
+        }
+        __syncthreads();
+        const int next = sh_next;
+        if (next == 1) failed = true;
+        if (next == 2) converged = true;
+        if (next == 0) {
+            beta = sh_scalar[0];
+            pi = sh_scalar[1];
+            alpha = sh_scalar[2];
+            gamma = gn;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int t = 0; t < kMgTrips; t++) {
+        const int k = threadIdx.x + t * kMgThreads;
+        if (k < cnt) S.x[n0 + k] = x[t];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S.sp->solve_iters = it;
+        S.sp->solve_converged = converged ? 1 : 0;
+        S.sp->solve_rel_resid = (bb > 0) ? sqrt(rr / bb) : 0.0;
+        if (!converged) atomicOr(S.status, MPMG_DEV_ERR_SOLVER);
+    }
+}
+
 // Nodal fluidity back to the particles, then the stress update
 // (g_nonlocal_mu2.c:545-564 and :160-218; g_nonlocal.c:559-578, :154-298).
 // AVG: the element average of the four nodal values instead of the shape
@@ -969,7 +1800,79 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
             }
         }
     }
-    const int part_blocks = ctx->cg_blocks > ctx->cg_tile_blocks ? ctx->cg_blocks : ctx->cg_tile_blocks;
+    // The multigrid-preconditioned kernel: one block per SM at most, each
+    // block's share of every level and its outer vectors in shared memory.
+    ctx->mg_host = nullptr;
+    ctx->mg_dev = nullptr;
+    ctx->mg_rows = nullptr;
+    ctx->mg_words = nullptr;
+    ctx->mg_tag = nullptr;
+    ctx->mg_smem = 0;
+    int mg_blocks = 0;
+    {
+        MgPlan P;
+        memset(&P, 0, sizeof(P));
+        int nb = (int)((nn + kMgThreads - 1) / kMgThreads);
+        if (nb > sms) nb = sms;
+        if (nb < 1) nb = 1;
+        int Nx = ctx->cfg.Nx, Ny = ctx->cfg.Ny, L = 0, total = 0, smf = 0, cxs = 0, cys = 0;
+        bool ok = Nx >= 1 && Ny >= 1;
+        while (ok) {
+            MgLevel &lv = P.lv[L++];
+            lv.Nx = Nx;
+            lv.Ny = Ny;
+            lv.nn = Nx * Ny;
+            lv.C = (lv.nn + nb - 1) / nb;
+            lv.cx = cxs;
+            lv.cy = cys;
+            lv.g = total;
+            lv.sm = smf;
+            total += lv.nn;
+            smf += 13 * lv.C;
+            if (Nx <= 3 && Ny <= 3) break;
+            if (L == kMgMaxLevels) ok = false;
+            cxs = Nx > 3;
+            cys = Ny > 3;
+            if (cxs) Nx = Nx / 2 + 1;
+            if (cys) Ny = Ny / 2 + 1;
+        }
+        P.L = L;
+        P.nblocks = nb;
+        P.total = total;
+        ok = ok && P.lv[0].C <= kMgTrips * kMgThreads && nb <= 8 * 32 && P.lv[L - 1].nn <= kMgCoarse;
+        const size_t smem = ok ? pcg_mg_smem(P) : 0;
+        int optin = 0;
+        MPMG_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
+        if (ok && smem + sizeof(MgPlan) + 256 <= (size_t)optin) {
+            MPMG_CHECK(cudaFuncSetAttribute(pcg_mg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int mg_per_sm = 0;
+            MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mg_per_sm, pcg_mg_kernel, kMgThreads, smem));
+            if (mg_per_sm >= 1) {
+                MPMG_CHECK(cudaMalloc(&ctx->mg_rows, 5 * (size_t)total * sizeof(float)));
+                MPMG_CHECK(cudaMalloc(&ctx->mg_words, 3 * (size_t)total * sizeof(unsigned long long)));
+                MPMG_CHECK(cudaMemsetAsync(ctx->mg_words, 0, 3 * (size_t)total * sizeof(unsigned long long),
+                                           ctx->stream));
+                MPMG_CHECK(cudaMalloc(&ctx->mg_tag, sizeof(unsigned int)));
+                const unsigned int first_tag = 1;   // the pools start with tag 0
+                MPMG_CHECK(cudaMemcpyAsync(ctx->mg_tag, &first_tag, sizeof(first_tag), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+                P.rows = ctx->mg_rows;
+                P.z1 = ctx->mg_words;
+                P.res = ctx->mg_words + total;
+                P.zf = ctx->mg_words + 2 * (size_t)total;
+                P.tag = ctx->mg_tag;
+                ctx->mg_host = new MgPlan(P);
+                MPMG_CHECK(cudaMalloc(&ctx->mg_dev, sizeof(MgPlan)));
+                MPMG_CHECK(cudaMemcpyAsync(ctx->mg_dev, ctx->mg_host, sizeof(MgPlan), cudaMemcpyHostToDevice,
+                                           ctx->stream));
+                MPMG_CHECK(cudaStreamSynchronize(ctx->stream));
+                ctx->mg_smem = smem;
+                mg_blocks = nb;
+            }
+        }
+    }
+    int part_blocks = ctx->cg_blocks > ctx->cg_tile_blocks ? ctx->cg_blocks : ctx->cg_tile_blocks;
+    if (mg_blocks > part_blocks) part_blocks = mg_blocks;
     MPMG_CHECK(cudaMalloc(&ctx->cg_partials, 4 * (size_t)part_blocks * sizeof(double)));
     // barrier counter + generation, then one neighbour flag per tiled block
     MPMG_CHECK(cudaMalloc(&ctx->cg_barrier, (2 + (size_t)ctx->cg_tile_blocks) * sizeof(unsigned int)));
@@ -987,6 +1890,16 @@ void mpmg_nonlocal_free(mpmg_ctx *ctx)
     }
     cudaFree(ctx->cg_barrier);
     ctx->cg_barrier = nullptr;
+    cudaFree(ctx->mg_rows);
+    cudaFree(ctx->mg_words);
+    cudaFree(ctx->mg_tag);
+    cudaFree(ctx->mg_dev);
+    delete ctx->mg_host;
+    ctx->mg_rows = nullptr;
+    ctx->mg_words = nullptr;
+    ctx->mg_tag = nullptr;
+    ctx->mg_dev = nullptr;
+    ctx->mg_host = nullptr;
 }
 
 // The fluidity system on element blocks elem_k and right-hand sides elem_f
@@ -1029,7 +1942,13 @@ int mpmg_solve_fluidity_system(mpmg_ctx *ctx, const double *elem_k, const double
     S.sp = ctx->d_params;
     if (zero_start) MPMG_CHECK(cudaMemsetAsync(x, 0, ctx->nn * sizeof(double), s));
     MPMG_CHECK(cudaMemsetAsync(ctx->cg_barrier, 0, 2 * sizeof(unsigned int), s));
-    if (ctx->cg_tile_blocks > 0) {
+    if (ctx->mg_dev != nullptr && c.solver_precond == MPMG_PRECOND_MULTIGRID) {
+        int warm = zero_start ? 0 : 1;
+        const MgPlan *plan = ctx->mg_dev;
+        void *args[] = {&S, &plan, &warm};
+        MPMG_CHECK(cudaLaunchCooperativeKernel((const void *)pcg_mg_kernel, dim3(ctx->mg_host->nblocks),
+                                               dim3(kMgThreads), args, ctx->mg_smem, s));
+    } else if (ctx->cg_tile_blocks > 0) {
         int C = ctx->cg_tile_nodes, warm = zero_start ? 0 : 1;
         unsigned int *flags = ctx->cg_barrier + 2;
         MPMG_CHECK(cudaMemsetAsync(flags, 0, (size_t)ctx->cg_tile_blocks * sizeof(unsigned int), s));

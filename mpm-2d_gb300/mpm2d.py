@@ -51,7 +51,7 @@ class Config(C.Structure):
                 ("bci", C.c_int * 4), ("gravity_mode", C.c_int), ("gravity", C.c_double),
                 ("store_transients", C.c_int), ("solver_tol", C.c_double),
                 ("solver_maxit", C.c_int), ("device", C.c_int), ("solver_warm_start", C.c_int),
-                ("precision", C.c_int), ("scheme", C.c_int)]
+                ("precision", C.c_int), ("scheme", C.c_int), ("solver_precond", C.c_int)]
 
 
 _lib = None
@@ -184,10 +184,11 @@ def fp64_rate(device=0):
 
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_f64node": 2}
 SCHEMES = {"usl": 0, "musl": 1}
+PRECONDS = {"multigrid": 0, "jacobi": 1}
 
 
 def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0,
-                warm_start=False, precision="fp64"):
+                warm_start=False, precision="fp64", precond="multigrid"):
     cfg = Config()
     _check(lib().mpmg_config_init(C.byref(cfg)))
     cfg.Nx, cfg.Ny, cfg.h = scene["Nx"], scene["Ny"], scene["h"]
@@ -218,6 +219,7 @@ def make_config(scene, store_transients=False, solver_tol=1e-10, solver_maxit=20
     cfg.solver_warm_start = 1 if warm_start else 0
     cfg.precision = PRECISIONS[precision]
     cfg.scheme = SCHEMES[scene.get("scheme", "usl")]
+    cfg.solver_precond = PRECONDS[precond]
     return cfg
 
 
@@ -225,9 +227,10 @@ class Simulation:
     """One simulation resident on the GPU."""
 
     def __init__(self, scene, store_transients=False, solver_tol=1e-10, solver_maxit=20000, device=0,
-                 warm_start=False, precision="fp64"):
+                 warm_start=False, precision="fp64", precond="multigrid"):
         L = lib()
-        cfg = make_config(scene, store_transients, solver_tol, solver_maxit, device, warm_start, precision)
+        cfg = make_config(scene, store_transients, solver_tol, solver_maxit, device, warm_start, precision,
+                          precond)
         self.precision = precision
         p = scene["particles"]
         self.n = len(p["x"])
