@@ -938,6 +938,9 @@ constexpr int kMgTrips = 4;            // nodes of a level a thread owns at most
 constexpr int kMgCoarse = 9;           // nodes of the coarsest level at most (3 x 3)
 // one smoothing step: the Chebyshev step for [0.3, 1], 1 / 0.65
 constexpr float kMgOmega = 1.0f / 0.65f;
+// polls of one wait before it gives up (each poll sleeps and reloads: about
+// a second in all)
+constexpr long long kMgPollLimit = 1ll << 21;
 
 __device__ __forceinline__ unsigned long long mg_ld(const unsigned long long *p)
 {
@@ -958,7 +961,7 @@ __device__ __forceinline__ unsigned long long mg_zero(unsigned tag)
     return (unsigned long long)tag << 32;
 }
 
-// Polls one word until it carries `tag`.  Bounded: after kSpinLimit polls,
+// Polls one word until it carries `tag`.  Bounded: after kMgPollLimit polls,
 // or once another block has timed out, the spin error is set and 0 returned.
 __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag, int *status)
 {
@@ -966,7 +969,7 @@ __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag,
         const unsigned long long v = mg_ld(p);
         if ((unsigned)(v >> 32) == tag) return __uint_as_float((unsigned)v);
         if ((polls & 31) == 0 &&
-            (polls > kSpinLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0)) {
+            (polls > kMgPollLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0)) {
             atomicOr(status, MPMG_DEV_ERR_SPIN);
             return 0.0f;
         }
@@ -974,10 +977,47 @@ __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag,
     }
 }
 
-// Value of a loaded word, polling its address again if its tag is stale.
-__device__ __forceinline__ float mg_val(unsigned long long v, const unsigned long long *p, unsigned tag, int *status)
+// Waits until every word of v carries `tag`: the stale ones are loaded again
+// together (addr(t, q) gives the address of word q of trip t), so a phase
+// waits about one L2 round trip after its last input is written rather than
+// one round trip per late word.  Bounded like mg_poll; on a timeout the
+// words read 0.
+template <class Addr>
+__device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9], unsigned tag, int *status,
+                                           Addr addr)
 {
-    return (unsigned)(v >> 32) == tag ? __uint_as_float((unsigned)v) : mg_poll(p, tag, status);
+    for (long long polls = 1;; polls++) {
+        bool stale = false;
+#pragma unroll
+        for (int t = 0; t < kMgTrips; t++) {
+#pragma unroll
+            for (int q = 0; q < 9; q++) stale |= (unsigned)(v[t][q] >> 32) != tag;
+        }
+        if (!stale) return;
+        if ((polls & 31) == 0 &&
+            (polls > kMgPollLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0)) {
+            atomicOr(status, MPMG_DEV_ERR_SPIN);
+#pragma unroll
+            for (int t = 0; t < kMgTrips; t++) {
+#pragma unroll
+                for (int q = 0; q < 9; q++) v[t][q] = mg_zero(tag);
+            }
+            return;
+        }
+        __nanosleep(32);
+#pragma unroll
+        for (int t = 0; t < kMgTrips; t++) {
+#pragma unroll
+            for (int q = 0; q < 9; q++) {
+                if ((unsigned)(v[t][q] >> 32) != tag) v[t][q] = mg_ld(addr(t, q));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float mg_f(unsigned long long v)
+{
+    return __uint_as_float((unsigned)v);
 }
 
 // Block arrays of a level in shared memory (floats): coef[9][C] (the full
@@ -1165,6 +1205,10 @@ __device__ __forceinline__ void mg_residual(const MgPlan &P, int l, const MgShar
             v[t][q] = in ? mg_ld(z1 + n + dj * lv.Nx + di) : mg_zero(tag);
         }
     }
+    mg_resolve(v, tag, status, [&](int t, int q) {
+        const int n = n0 + threadIdx.x + t * kMgThreads;
+        return z1 + n + (q / 3 - 1) * lv.Nx + (q % 3 - 1);
+    });
 #pragma unroll
     for (int t = 0; t < kMgTrips; t++) {
         const int k = threadIdx.x + t * kMgThreads;
@@ -1174,9 +1218,8 @@ __device__ __forceinline__ void mg_residual(const MgPlan &P, int l, const MgShar
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             // entries towards nodes outside the grid are zero and their words
-            // carry the current tag (no load, no wait)
-            const int di = q % 3 - 1, dj = q / 3 - 1;
-            acc = fmaf(S.coef[q * lv.C + k], mg_val(v[t][q], z1 + n + dj * lv.Nx + di, tag, status), acc);
+            // read 0
+            acc = fmaf(S.coef[q * lv.C + k], mg_f(v[t][q]), acc);
         }
         const float r = S.b[k] - acc;
         S.res[k] = r;
@@ -1204,6 +1247,10 @@ __device__ __forceinline__ void mg_restrict(const MgPlan &P, int c, const MgShar
             v[t][q] = in ? mg_ld(res + fy * F.Nx + fx) : mg_zero(tag);
         }
     }
+    mg_resolve(v, tag, status, [&](int t, int q) {
+        const int I = n0 + threadIdx.x + t * kMgThreads, cj = I / lv.Nx, ci = I - cj * lv.Nx;
+        return res + mg_fine_of(cj, q / 3, lv.cy) * F.Nx + mg_fine_of(ci, q % 3, lv.cx);
+    });
     const bool coarsest = c == P.L - 1;
 #pragma unroll
     for (int t = 0; t < kMgTrips; t++) {
@@ -1216,7 +1263,7 @@ __device__ __forceinline__ void mg_restrict(const MgPlan &P, int c, const MgShar
             const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
             if (fx < 0 || fx >= F.Nx || fy < 0 || fy >= F.Ny) continue;
             const float w = ((q % 3 == 1) ? 1.0f : 0.5f) * ((q / 3 == 1) ? 1.0f : 0.5f);
-            b = fmaf(w, mg_val(v[t][q], res + fy * F.Nx + fx, tag, status), b);
+            b = fmaf(w, mg_f(v[t][q]), b);
         }
         S.b[k] = b;
         if (coarsest) {
@@ -1263,6 +1310,12 @@ __device__ __forceinline__ void mg_prolong(const MgPlan &P, int l, const MgShare
             v[t][q] = in ? mg_ld(zc + cy * Cl.Nx + cx) : mg_zero(tag);
         }
     }
+    mg_resolve(v, tag, status, [&](int t, int q) {
+        const int n = n0 + threadIdx.x + t * kMgThreads, j = n / lv.Nx, i = n - j * lv.Nx;
+        int x0, x1, y0, y1;
+        mg_window(lv, Cl, i, j, x0, x1, y0, y1);
+        return zc + (y0 + q / 3) * Cl.Nx + (x0 + q % 3);
+    });
 #pragma unroll
     for (int t = 0; t < kMgTrips; t++) {
         const int k = threadIdx.x + t * kMgThreads;
@@ -1272,10 +1325,7 @@ __device__ __forceinline__ void mg_prolong(const MgPlan &P, int l, const MgShare
         mg_window(lv, Cl, i, j, x0, x1, y0, y1);
         float zv[9];
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const int cx = x0 + q % 3, cy = y0 + q / 3;
-            zv[q] = mg_val(v[t][q], zc + cy * Cl.Nx + cx, tag, status);
-        }
+        for (int q = 0; q < 9; q++) zv[q] = mg_f(v[t][q]);
         float acc = 0.0f, own = 0.0f;
 #pragma unroll
         for (int q = 0; q < 9; q++) {
@@ -1605,6 +1655,10 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
                     wv[t][q] = in ? mg_ld(zf + n + dj * Nx + di) : mg_zero(tag);
                 }
             }
+            mg_resolve(wv, tag, S.status, [&](int t, int q) {
+                const int n = n0 + threadIdx.x + t * kMgThreads;
+                return zf + n + (q / 3 - 1) * Nx + (q % 3 - 1);
+            });
             part[0] = part[1] = part[2] = part[3] = 0;
 #pragma unroll
             for (int t = 0; t < kMgTrips; t++) {
@@ -1615,9 +1669,8 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
 #pragma unroll
                 for (int q = 0; q < 9; q++) {
                     // rows are zero towards nodes outside the grid, whose
-                    // words read 0 with the current tag
-                    const int di = q % 3 - 1, dj = q / 3 - 1;
-                    const double zq = (double)mg_val(wv[t][q], zf + n + dj * Nx + di, tag, S.status);
+                    // words read 0
+                    const double zq = (double)mg_f(wv[t][q]);
                     if (q == 4) own = zq;
                     az = fma(S.coef[(size_t)q * nn + n], zq, az);
                 }
