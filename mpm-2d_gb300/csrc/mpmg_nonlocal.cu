@@ -29,14 +29,17 @@ constexpr int kMgMaxLevels = 16;
 struct MgLevel {
     int Nx, Ny, nn, C;
     int cx, cy;            // coarsened from the finer level along x, y (level 0: 0)
+    int local;             // 1: block 0 holds the whole level (C = nn)
     int g;                 // first node of the level in the global pools
-    int sm;                // first float of the level's arrays in shared memory
+    int sm;                // first float of the level's block arrays in shared memory
 };
 
 struct MgPlan {
     int L, nblocks, total; // levels, blocks, nodes over all levels
     MgLevel lv[kMgMaxLevels];
-    float *rows;           // [5][total]: east, north, north-east, north-west, row sum
+    float *coef;           // [9][total]: 9-point rows, q = 3 (dj + 1) + (di + 1)
+    float *rsum;           // [total]: row sums
+    float *l1inv;          // [total]: inverse absolute row sums (0: not an unknown)
     unsigned long long *z1, *res, *zf;   // [total] tagged words each
     unsigned int *tag;     // tag counter
 };
@@ -889,15 +892,13 @@ inline size_t pcg_tile_smem(int C, int Nx)
 // node of level l along each direction with more than 3 nodes
 // (n -> n / 2 + 1), down to at most 3 x 3 nodes.  Prolongation P is bilinear
 // interpolation, restriction is P^T, and the coarse operators are the
-// Galerkin products A_{l+1} = P^T A_l P, formed every solve in FP32.
-//
-// Storage of a level.  Each node stores its four upper stencil entries
-// (east, north, north-east, north-west) and its row sum s = A 1.  The lower
-// entries are the neighbours' upper ones, so every level is exactly
-// symmetric.  The diagonal is s minus the off-diagonal sum.  P reproduces
-// constants, so the coarse row sums are P^T s.  The near-null space of a
-// Neumann-like operator (only the 1e-10 shift and the xi^-2-weighted mass
-// keep it from being singular) therefore survives FP32 coarsening.
+// Galerkin products A_{l+1} = P^T A_l P, formed every solve in FP32.  Each
+// node keeps its full 9-point row, its row sum s = A 1 and the inverse of
+// its absolute row sum.  P reproduces constants, so a coarse row sum is
+// P^T s, and a coarse diagonal is set to that row sum minus the row's
+// off-diagonal entries.  The near-null space of a Neumann-like operator
+// (only the 1e-10 shift and the xi^-2-weighted mass keep it from being
+// singular) therefore survives FP32 coarsening.
 //
 // Preconditioner: one V(1,1) cycle in FP32 on r / |r|.
 //   * On each level, one l1-Jacobi step (Baker, Falgout, Kolev and Yang,
@@ -908,11 +909,11 @@ inline size_t pcg_tile_smem(int C, int Nx)
 //   * At the coarsest level, an exact solve: an FP64 inverse formed every
 //     solve.
 //   * On the way up, prolongation and one post-smoothing step of the same
-//     size, so the cycle is symmetric.
+//     size.
 //
 // Outer iteration: FP64 CG in the one-reduction form of Chronopoulos and
 // Gear.  It uses the Polak-Ribiere beta, which tolerates the rounding of an
-// FP32 preconditioner:
+// FP32 preconditioner (whose Galerkin rows are symmetric only to rounding):
 //   beta  = -alpha <s, u> / gamma_old
 //   pi    = delta + 2 beta <s, u> + beta^2 pi_old
 //   alpha = gamma / pi
@@ -920,12 +921,17 @@ inline size_t pcg_tile_smem(int C, int Nx)
 // recurrence.  Each iteration needs one grid barrier, for the four inner
 // products.
 //
-// Synchronisation inside the V-cycle.  Each phase writes its level vector to
+// Where the levels live.  A level of more than 2048 nodes is spread over all
+// blocks in contiguous node ranges; the coarser levels are held whole by
+// block 0, whose threads meet at block barriers between phases.
+//
+// Synchronisation between blocks.  Each phase writes its level vector to
 // global memory as 64-bit words: an FP32 value plus a 32-bit tag that names
-// the V-cycle.  A consumer loads the words it needs and polls again those
-// whose tag is not yet current, so each phase waits for exactly the values
-// it reads.  A word is stored with one single-copy-atomic 64-bit store, so
-// its value and tag arrive together, with no fences or flags.
+// the V-cycle.  A consumer loads the words it needs; if some carry an older
+// tag, it polls one of them with a growing pause and, once that one is
+// current, loads the rest again together.  A word is stored with one
+// single-copy-atomic 64-bit store, so its value and tag arrive together,
+// with no fences or flags.
 //   * Each phase vector is written once per V-cycle, and the outer grid
 //     barrier separates V-cycles, so no value is overwritten while a reader
 //     may still need it.
@@ -935,12 +941,12 @@ inline size_t pcg_tile_smem(int C, int Nx)
 
 constexpr int kMgThreads = 512;
 constexpr int kMgTrips = 4;            // nodes of a level a thread owns at most
+constexpr int kMgLocal = kMgTrips * kMgThreads;   // levels this small are held by block 0
 constexpr int kMgCoarse = 9;           // nodes of the coarsest level at most (3 x 3)
 // one smoothing step: the Chebyshev step for [0.3, 1], 1 / 0.65
 constexpr float kMgOmega = 1.0f / 0.65f;
-// polls of one wait before it gives up (each poll sleeps and reloads: about
-// a second in all)
-constexpr long long kMgPollLimit = 1ll << 21;
+// polls of one wait before it gives up (each poll pauses up to 2 us)
+constexpr long long kMgPollLimit = 1ll << 20;
 
 __device__ __forceinline__ unsigned long long mg_ld(const unsigned long long *p)
 {
@@ -961,42 +967,61 @@ __device__ __forceinline__ unsigned long long mg_zero(unsigned tag)
     return (unsigned long long)tag << 32;
 }
 
-// Polls one word until it carries `tag`.  Bounded: after kMgPollLimit polls,
-// or once another block has timed out, the spin error is set and 0 returned.
+__device__ __forceinline__ float mg_f(unsigned long long v)
+{
+    return __uint_as_float((unsigned)v);
+}
+
+__device__ __forceinline__ bool mg_give_up(long long polls, int *status)
+{
+    if ((polls & 15) != 0) return false;
+    if (polls > kMgPollLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0) {
+        atomicOr(status, MPMG_DEV_ERR_SPIN);
+        return true;
+    }
+    return false;
+}
+
+// Polls one word until it carries `tag`, pausing 64 ns at first and up to
+// 2 us.  Bounded: on a timeout, or once another block has timed out, the
+// spin error is set and 0 returned.
 __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag, int *status)
 {
+    unsigned ns = 64;
     for (long long polls = 1;; polls++) {
         const unsigned long long v = mg_ld(p);
-        if ((unsigned)(v >> 32) == tag) return __uint_as_float((unsigned)v);
-        if ((polls & 31) == 0 &&
-            (polls > kMgPollLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0)) {
-            atomicOr(status, MPMG_DEV_ERR_SPIN);
-            return 0.0f;
-        }
-        __nanosleep(20);
+        if ((unsigned)(v >> 32) == tag) return mg_f(v);
+        if (mg_give_up(polls, status)) return 0.0f;
+        __nanosleep(ns);
+        if (ns < 2048) ns *= 2;
     }
 }
 
-// Waits until every word of v carries `tag`: the stale ones are loaded again
-// together (addr(t, q) gives the address of word q of trip t), so a phase
-// waits about one L2 round trip after its last input is written rather than
-// one round trip per late word.  Bounded like mg_poll; on a timeout the
-// words read 0.
+// Waits until every word of v carries `tag` (addr(t, q) is the address of
+// word q of trip t).  While some are stale, one of them is polled alone
+// with a growing pause, and once it is current the other stale words are
+// loaded again together: a phase waits about one round trip after its last
+// input is written, and waiting threads load little.  Bounded like mg_poll;
+// on a timeout the words read 0.
 template <class Addr>
 __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9], unsigned tag, int *status,
                                            Addr addr)
 {
+    unsigned ns = 64;
     for (long long polls = 1;; polls++) {
-        bool stale = false;
+        int ft = -1, fq = 0;
 #pragma unroll
-        for (int t = 0; t < kMgTrips; t++) {
+        for (int t = kMgTrips - 1; t >= 0; t--) {
 #pragma unroll
-            for (int q = 0; q < 9; q++) stale |= (unsigned)(v[t][q] >> 32) != tag;
+            for (int q = 8; q >= 0; q--) {
+                if ((unsigned)(v[t][q] >> 32) != tag) {
+                    ft = t;
+                    fq = q;
+                }
+            }
         }
-        if (!stale) return;
-        if ((polls & 31) == 0 &&
-            (polls > kMgPollLimit || (*(volatile int *)status & MPMG_DEV_ERR_SPIN) != 0)) {
-            atomicOr(status, MPMG_DEV_ERR_SPIN);
+        if (ft < 0) return;
+        if (mg_give_up(polls, status)) {
 #pragma unroll
             for (int t = 0; t < kMgTrips; t++) {
 #pragma unroll
@@ -1004,7 +1029,10 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
             }
             return;
         }
-        __nanosleep(32);
+        __nanosleep(ns);
+        if (ns < 2048) ns *= 2;
+        if ((unsigned)(mg_ld(addr(ft, fq)) >> 32) != tag) continue;
+        ns = 64;
 #pragma unroll
         for (int t = 0; t < kMgTrips; t++) {
 #pragma unroll
@@ -1015,46 +1043,37 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
     }
 }
 
-__device__ __forceinline__ float mg_f(unsigned long long v)
+// Block barrier of the levels held by block 0 (other blocks own none of
+// their nodes and pass).
+__device__ __forceinline__ void mg_local_sync(const MgLevel &lv)
 {
-    return __uint_as_float((unsigned)v);
+    if (lv.local && blockIdx.x == 0) __syncthreads();
 }
 
-// Block arrays of a level in shared memory (floats): coef[9][C] (the full
-// stencil, q = 3 (dj + 1) + (di + 1)), l1inv[C], b[C], z1[C], res[C].
+// Per-level block arrays in shared memory (floats): b, z1, res (C each);
+// level 0 also keeps its rows there (coef0[9][C0], l1inv0[C0] at float 0).
 struct MgShared {
-    float *coef, *l1inv, *b, *z1, *res;
+    float *b, *z1, *res;
 };
 
 __device__ __forceinline__ MgShared mg_shared(float *sm, const MgLevel &lv)
 {
     MgShared s;
-    s.coef = sm + lv.sm;
-    s.l1inv = s.coef + 9 * lv.C;
-    s.b = s.l1inv + lv.C;
+    s.b = sm + lv.sm;
     s.z1 = s.b + lv.C;
     s.res = s.z1 + lv.C;
     return s;
 }
 
-// The full stencil of node (i, j) of a level from the stored upper entries
-// and the row sum: a[q], q = 3 (dj + 1) + (di + 1); a[4] = s - sum of the
-// others.  Entries towards nodes outside the grid are zero.
-__device__ __forceinline__ void mg_stencil(const MgPlan &P, const MgLevel &lv, int n, int i, int j, float a[9])
+// Row entry q of own node k (global node n) of level l, and D_l1^-1.
+__device__ __forceinline__ float mg_coef(const MgPlan &P, const float *sm, int l, int q, int k, int n)
 {
-    const float *E = P.rows + lv.g, *N = E + P.total, *NE = N + P.total, *NW = NE + P.total, *S = NW + P.total;
-    const int Nx = lv.Nx;
-    const bool w = i > 0, e = i + 1 < lv.Nx, s = j > 0, nn = j + 1 < lv.Ny;
-    a[5] = e ? __ldcg(E + n) : 0.0f;
-    a[3] = w ? __ldcg(E + n - 1) : 0.0f;
-    a[7] = nn ? __ldcg(N + n) : 0.0f;
-    a[1] = s ? __ldcg(N + n - Nx) : 0.0f;
-    a[8] = (e && nn) ? __ldcg(NE + n) : 0.0f;
-    a[0] = (w && s) ? __ldcg(NE + n - Nx - 1) : 0.0f;
-    a[6] = (w && nn) ? __ldcg(NW + n) : 0.0f;
-    a[2] = (e && s) ? __ldcg(NW + n - Nx + 1) : 0.0f;
-    const float rs = __ldcg(S + n);
-    a[4] = rs - (((a[0] + a[1]) + (a[2] + a[3])) + ((a[5] + a[6]) + (a[7] + a[8])));
+    return l == 0 ? sm[q * P.lv[0].C + k] : __ldcg(P.coef + (size_t)q * P.total + P.lv[l].g + n);
+}
+
+__device__ __forceinline__ float mg_l1inv(const MgPlan &P, const float *sm, int l, int k, int n)
+{
+    return l == 0 ? sm[9 * P.lv[0].C + k] : __ldcg(P.l1inv + P.lv[l].g + n);
 }
 
 // Coarse parents of fine coordinate g along a direction: g even (or the
@@ -1077,8 +1096,23 @@ __device__ __forceinline__ int mg_fine_of(int c, int s, int coarsened)
     return coarsened ? 2 * c + s - 1 : (s == 1 ? c : -1);
 }
 
-// Galerkin row of coarse node (ci, cj) of level c from level c - 1: the
-// four upper entries and the row sum, written to the level's rows.
+// Writes a level's row of node (level offset g + n): entries, row sum,
+// D_l1^-1 (a row with no entries is not an unknown: all zero).
+__device__ __forceinline__ void mg_put_row(const MgPlan &P, int at, float a[9], float rs)
+{
+    float l1 = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 9; q++) l1 += fabsf(a[q]);
+    const float li = l1 > 0.0f ? 1.0f / l1 : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 9; q++) P.coef[(size_t)q * P.total + at] = li > 0.0f ? a[q] : 0.0f;
+    P.rsum[at] = rs;
+    P.l1inv[at] = li;
+}
+
+// Galerkin row of coarse node (ci, cj) of level c from the rows of level
+// c - 1: the nine entries of P^T A P, the row sum P^T s, and the diagonal
+// set to the row sum minus the off-diagonal entries.
 __device__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
 {
     const MgLevel &F = P.lv[c - 1], &Cl = P.lv[c];
@@ -1086,19 +1120,28 @@ __device__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
 #pragma unroll
     for (int q = 0; q < 9; q++) acc[q] = 0.0f;
     float srow = 0.0f;
-    const float *Sf = P.rows + 4 * (size_t)P.total + F.g;
+#pragma unroll
     for (int sy = 0; sy < 3; sy++) {
+        // one row of the fine support at a time: its rows loaded together
+        float a[3][9], sf[3];
+        int fxs[3];
         const int fy = mg_fine_of(cj, sy, Cl.cy);
-        if (fy < 0 || fy >= F.Ny) continue;
-        const float wy = (sy == 1) ? 1.0f : 0.5f;
+#pragma unroll
         for (int sx = 0; sx < 3; sx++) {
             const int fx = mg_fine_of(ci, sx, Cl.cx);
-            if (fx < 0 || fx >= F.Nx) continue;
-            const float wi = wy * ((sx == 1) ? 1.0f : 0.5f);
-            const int fi = fy * F.Nx + fx;
-            srow = fmaf(wi, __ldcg(Sf + fi), srow);
-            float a[9];
-            mg_stencil(P, F, fi, fx, fy, a);
+            const bool in = fx >= 0 && fx < F.Nx && fy >= 0 && fy < F.Ny;
+            fxs[sx] = in ? fx : -1;
+            const int fi = in ? fy * F.Nx + fx : 0;
+#pragma unroll
+            for (int q = 0; q < 9; q++) a[sx][q] = in ? __ldcg(P.coef + (size_t)q * P.total + F.g + fi) : 0.0f;
+            sf[sx] = in ? __ldcg(P.rsum + F.g + fi) : 0.0f;
+        }
+#pragma unroll
+        for (int sx = 0; sx < 3; sx++) {
+            const int fx = fxs[sx];
+            if (fx < 0) continue;
+            const float wi = ((sy == 1) ? 1.0f : 0.5f) * ((sx == 1) ? 1.0f : 0.5f);
+            srow = fmaf(wi, sf[sx], srow);
 #pragma unroll
             for (int q = 0; q < 9; q++) {
                 const int gx = fx + q % 3 - 1, gy = fy + q / 3 - 1;
@@ -1106,7 +1149,7 @@ __device__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
                 int px0, px1, py0, py1;
                 const int npx = mg_parents(gx, Cl.cx, px0, px1);
                 const int npy = mg_parents(gy, Cl.cy, py0, py1);
-                const float v = wi * a[q] * ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
+                const float v = wi * a[sx][q] * ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
                 acc[(py0 - cj + 1) * 3 + (px0 - ci + 1)] += v;
                 if (npx == 2) acc[(py0 - cj + 1) * 3 + (px1 - ci + 1)] += v;
                 if (npy == 2) acc[(py1 - cj + 1) * 3 + (px0 - ci + 1)] += v;
@@ -1114,12 +1157,8 @@ __device__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
             }
         }
     }
-    float *R = P.rows + Cl.g + I;
-    R[0] = acc[5];
-    R[P.total] = acc[7];
-    R[2 * (size_t)P.total] = acc[8];
-    R[3 * (size_t)P.total] = acc[6];
-    R[4 * (size_t)P.total] = srow;
+    acc[4] = srow - (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[5] + acc[6]) + (acc[7] + acc[8])));
+    mg_put_row(P, Cl.g + I, acc, srow);
 }
 
 // Sum of four values over the block in a fixed order, returned to every
@@ -1188,7 +1227,8 @@ __device__ __forceinline__ void mg_totals4(const double *partials, int nblocks, 
 
 // Residual phase of level l: res = b - A z1 (z1 of the neighbours from the
 // tagged words), kept in shared memory and published.
-__device__ __forceinline__ void mg_residual(const MgPlan &P, int l, const MgShared &S, unsigned tag, int *status)
+__device__ __forceinline__ void mg_residual(const MgPlan &P, const float *sm, int l, const MgShared &S, unsigned tag,
+                                            int *status)
 {
     const MgLevel &lv = P.lv[l];
     const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
@@ -1219,7 +1259,7 @@ __device__ __forceinline__ void mg_residual(const MgPlan &P, int l, const MgShar
         for (int q = 0; q < 9; q++) {
             // entries towards nodes outside the grid are zero and their words
             // read 0
-            acc = fmaf(S.coef[q * lv.C + k], mg_f(v[t][q]), acc);
+            acc = fmaf(mg_coef(P, sm, l, q, k, n), mg_f(v[t][q]), acc);
         }
         const float r = S.b[k] - acc;
         S.res[k] = r;
@@ -1230,7 +1270,8 @@ __device__ __forceinline__ void mg_residual(const MgPlan &P, int l, const MgShar
 // Restriction to level c (its own nodes): b = P^T res of level c - 1, then
 // the pre-smoothing step z1 = omega D_l1^-1 b (published), or at the
 // coarsest level b itself (published in the res words for the exact solve).
-__device__ __forceinline__ void mg_restrict(const MgPlan &P, int c, const MgShared &S, unsigned tag, int *status)
+__device__ __forceinline__ void mg_restrict(const MgPlan &P, const float *sm, int c, const MgShared &S, unsigned tag,
+                                            int *status)
 {
     const MgLevel &F = P.lv[c - 1], &lv = P.lv[c];
     const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
@@ -1256,20 +1297,18 @@ __device__ __forceinline__ void mg_restrict(const MgPlan &P, int c, const MgShar
     for (int t = 0; t < kMgTrips; t++) {
         const int k = threadIdx.x + t * kMgThreads;
         if (k >= cnt) continue;
-        const int I = n0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
+        const int I = n0 + k;
         float b = 0.0f;
 #pragma unroll
         for (int q = 0; q < 9; q++) {
-            const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
-            if (fx < 0 || fx >= F.Nx || fy < 0 || fy >= F.Ny) continue;
             const float w = ((q % 3 == 1) ? 1.0f : 0.5f) * ((q / 3 == 1) ? 1.0f : 0.5f);
-            b = fmaf(w, mg_f(v[t][q]), b);
+            b = fmaf(w, mg_f(v[t][q]), b);      // words outside the support read 0
         }
         S.b[k] = b;
         if (coarsest) {
             mg_st(P.res + lv.g + I, b, tag);
         } else {
-            const float z = kMgOmega * S.l1inv[k] * b;
+            const float z = kMgOmega * mg_l1inv(P, sm, c, k, I) * b;
             S.z1[k] = z;
             mg_st(P.z1 + lv.g + I, z, tag);
         }
@@ -1291,7 +1330,8 @@ __device__ __forceinline__ void mg_window(const MgLevel &lv, const MgLevel &Cl, 
 // Prolongation and post-smoothing at level l from the coarse solution of
 // level l + 1: with z2 = z1 + P zc and res = b - A z1,
 //   z = z2 + omega D_l1^-1 (res - A P zc)   (published; zero off the unknowns)
-__device__ __forceinline__ void mg_prolong(const MgPlan &P, int l, const MgShared &S, unsigned tag, int *status)
+__device__ __forceinline__ void mg_prolong(const MgPlan &P, const float *sm, int l, const MgShared &S, unsigned tag,
+                                           int *status)
 {
     const MgLevel &lv = P.lv[l], &Cl = P.lv[l + 1];
     const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
@@ -1323,6 +1363,8 @@ __device__ __forceinline__ void mg_prolong(const MgPlan &P, int l, const MgShare
         const int n = n0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
         int x0, x1, y0, y1;
         mg_window(lv, Cl, i, j, x0, x1, y0, y1);
+        // the window's values (indexed by the parents' offsets, which depend
+        // on the node's parity)
         float zv[9];
 #pragma unroll
         for (int q = 0; q < 9; q++) zv[q] = mg_f(v[t][q]);
@@ -1341,9 +1383,9 @@ __device__ __forceinline__ void mg_prolong(const MgPlan &P, int l, const MgShare
             if (npx == 2 && npy == 2) pz += zv[by * 3 + bx];
             pz *= ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
             if (q == 4) own = pz;
-            acc = fmaf(S.coef[q * lv.C + k], pz, acc);
+            acc = fmaf(mg_coef(P, sm, l, q, k, n), pz, acc);
         }
-        const float li = S.l1inv[k];
+        const float li = mg_l1inv(P, sm, l, k, n);
         const float z = (li == 0.0f) ? 0.0f : S.z1[k] + own + kMgOmega * li * (S.res[k] - acc);
         mg_st(P.zf + lv.g + n, z, tag);
     }
@@ -1364,15 +1406,18 @@ __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, double
             if (L == 1) {
                 mg_st(P.res + n0 + k, S.b[k], tag);
             } else {
-                const float z = kMgOmega * S.l1inv[k] * S.b[k];
+                const float z = kMgOmega * sm[9 * lv.C + k] * S.b[k];
                 S.z1[k] = z;
                 mg_st(P.z1 + n0 + k, z, tag);
             }
         }
+        mg_local_sync(lv);
     }
     for (int l = 0; l + 1 < L; l++) {
-        mg_residual(P, l, mg_shared(sm, P.lv[l]), tag, status);
-        mg_restrict(P, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
+        mg_residual(P, sm, l, mg_shared(sm, P.lv[l]), tag, status);
+        mg_local_sync(P.lv[l]);
+        mg_restrict(P, sm, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
+        mg_local_sync(P.lv[l + 1]);
     }
     // exact solve at the coarsest level (block 0)
     if (blockIdx.x == 0) {
@@ -1385,18 +1430,22 @@ __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, double
             for (int m = 0; m < nc; m++) z = fma(cinv[threadIdx.x * kMgCoarse + m], cb[m], z);
             mg_st(P.zf + lv.g + threadIdx.x, (float)z, tag);
         }
+        __syncthreads();
     }
-    for (int l = L - 2; l >= 0; l--) mg_prolong(P, l, mg_shared(sm, P.lv[l]), tag, status);
+    for (int l = L - 2; l >= 0; l--) {
+        mg_prolong(P, sm, l, mg_shared(sm, P.lv[l]), tag, status);
+        mg_local_sync(P.lv[l]);
+    }
 }
 
-// Shared memory of pcg_mg_kernel: the level arrays (13 floats a node of
-// each level a block owns), five FP64 outer vectors a level-0 node, the
-// reduction scratch, the coarsest inverse, its right-hand side and the
-// elimination matrix.
+// Shared memory of pcg_mg_kernel: level 0's rows (10 floats a node), three
+// floats a node of each level a block holds, five FP64 outer vectors a
+// level-0 node, the reduction scratch, the coarsest inverse, its right-hand
+// side and the elimination matrix.
 inline size_t pcg_mg_smem(const MgPlan &P)
 {
-    size_t floats = 0;
-    for (int l = 0; l < P.L; l++) floats += 13 * (size_t)P.lv[l].C;
+    size_t floats = 10 * (size_t)P.lv[0].C;
+    for (int l = 0; l < P.L; l++) floats += 3 * (size_t)P.lv[l].C;
     floats = (floats + 1) & ~(size_t)1;
     const size_t doubles = 5 * (size_t)P.lv[0].C + 4 * (size_t)kMgThreads + 4 + kMgCoarse * kMgCoarse + kMgCoarse +
                            2 * kMgCoarse * kMgCoarse;
@@ -1418,15 +1467,15 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     const int nblocks = gridDim.x;
     const MgLevel &L0 = P.lv[0];
     const int n0 = blockIdx.x * L0.C, cnt = min(L0.C, nn - n0);
-    size_t fl = 0;
-    for (int l = 0; l < P.L; l++) fl += 13 * (size_t)P.lv[l].C;
+    size_t fl = 10 * (size_t)L0.C;
+    for (int l = 0; l < P.L; l++) fl += 3 * (size_t)P.lv[l].C;
     double *dv = smd + ((fl + 1) >> 1);
     double *r = dv, *p = r + L0.C, *s = p + L0.C, *w = s + L0.C, *u = w + L0.C;
     double *scratch = u + L0.C;                       // 4 kMgThreads + 4
     double *cinv = scratch + 4 * kMgThreads + 4;      // kMgCoarse^2
     double *cb = cinv + kMgCoarse * kMgCoarse;        // kMgCoarse
     double *gj = cb + kMgCoarse;                      // kMgCoarse x 2 kMgCoarse (coarsest inverse)
-    __shared__ double sh_scalar[3];
+    __shared__ double sh_scalar[5];
     __shared__ int sh_next;
     unsigned int episode = 0;
     unsigned tag0;
@@ -1434,9 +1483,9 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     double x[kMgTrips];
 
     // Level 0: FP64 rows (global, for the outer matvec), right-hand side,
-    // start; FP32 upper entries and row sums.  Entries towards nodes that are
-    // not unknowns are left out of the FP32 rows, whose zeroed rows keep them
-    // symmetric.
+    // start; FP32 rows (global for the Galerkin products, and this block's in
+    // shared memory).  Entries towards nodes that are not unknowns are left
+    // out of the FP32 rows, whose own rows are zero.
 #pragma unroll
     for (int t = 0; t < kMgTrips; t++) {
         const int k = threadIdx.x + t * kMgThreads;
@@ -1468,26 +1517,27 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         for (int q = 0; q < 9; q++) S.coef[(size_t)q * nn + n] = cf[q];
         S.x[n] = x[t];
         double rsum = 0;
-        bool nbu[9];
+        float a[9];
 #pragma unroll
         for (int q = 0; q < 9; q++) {
             const int di = q % 3 - 1, dj = q / 3 - 1;
             const bool in = i + di >= 0 && i + di < Nx && j + dj >= 0 && j + dj < Ny;
-            nbu[q] = unknown && (q == 4 || (in && S.node_m[n + dj * Nx + di] > S.dof_tol));
-            if (nbu[q]) rsum += cf[q];
+            const bool nbu = unknown && (q == 4 || (in && S.node_m[n + dj * Nx + di] > S.dof_tol));
+            a[q] = nbu ? (float)cf[q] : 0.0f;
+            if (nbu) rsum += cf[q];
         }
-        float *R = P.rows + n;
-        R[0] = nbu[5] ? (float)cf[5] : 0.0f;
-        R[P.total] = nbu[7] ? (float)cf[7] : 0.0f;
-        R[2 * (size_t)P.total] = nbu[8] ? (float)cf[8] : 0.0f;
-        R[3 * (size_t)P.total] = nbu[6] ? (float)cf[6] : 0.0f;
-        R[4 * (size_t)P.total] = (float)rsum;
+        mg_put_row(P, n, a, (float)rsum);
+#pragma unroll
+        for (int q = 0; q < 9; q++) sm[q * L0.C + k] = P.coef[(size_t)q * P.total + n];
+        sm[9 * L0.C + k] = P.l1inv[n];
     }
     if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
     // every block has read the tag counter: reserve this solve's tags
     if (blockIdx.x == 0 && threadIdx.x == 0) *P.tag = tag0 + (unsigned)S.maxit + 2u;
 
-    // Coarse levels: Galerkin rows, one level after another.
+    // Coarse levels: Galerkin rows, one level after another (a grid barrier
+    // after each level spread over the blocks, a block barrier after each
+    // level held by block 0).
     for (int c = 1; c < P.L; c++) {
         const MgLevel &lv = P.lv[c];
         const int c0 = blockIdx.x * lv.C, ccnt = min(lv.C, lv.nn - c0);
@@ -1495,29 +1545,15 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
             const int I = c0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
             mg_galerkin_row(P, c, I, ci, cj);
         }
-        if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
-    }
-    // Each block's rows of every level into shared memory, with D_l1^-1.
-    for (int l = 0; l < P.L; l++) {
-        const MgLevel &lv = P.lv[l];
-        const MgShared Sh = mg_shared(sm, lv);
-        const int l0 = blockIdx.x * lv.C, lcnt = min(lv.C, lv.nn - l0);
-        for (int k = threadIdx.x; k < lcnt; k += kMgThreads) {
-            const int n = l0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
-            float a[9];
-            mg_stencil(P, lv, n, i, j, a);
-            float l1 = 0.0f;
-#pragma unroll
-            for (int q = 0; q < 9; q++) l1 += fabsf(a[q]);
-            const float li = l1 > 0.0f ? 1.0f / l1 : 0.0f;
-#pragma unroll
-            for (int q = 0; q < 9; q++) Sh.coef[q * lv.C + k] = li > 0.0f ? a[q] : 0.0f;
-            Sh.l1inv[k] = li;
+        if (!lv.local) {
+            if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+        } else {
+            mg_local_sync(lv);
         }
     }
-    // The coarsest level's inverse (block 0): Gauss-Jordan on the symmetric
-    // positive definite matrix of its active nodes, in FP64.  A node whose
-    // pivot is not positive is left out (its correction is zero).
+    // The coarsest level's inverse (block 0): Gauss-Jordan on the matrix of
+    // its active nodes, in FP64, with the diagonal from the row sum.  A node
+    // whose pivot is not positive is left out (its correction is zero).
     if (blockIdx.x == 0) {
         const MgLevel &lv = P.lv[P.L - 1];
         const int nc = lv.nn, w2 = 2 * kMgCoarse;
@@ -1525,24 +1561,28 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         __syncthreads();
         if (threadIdx.x < nc) {
             const int a = threadIdx.x, j = a / lv.Nx, i = a - j * lv.Nx;
-            float st[9];
-            mg_stencil(P, lv, a, i, j, st);
             double off = 0;
 #pragma unroll
             for (int q = 0; q < 9; q++) {
                 if (q == 4) continue;
                 const int di = q % 3 - 1, dj = q / 3 - 1;
                 if (i + di < 0 || i + di >= lv.Nx || j + dj < 0 || j + dj >= lv.Ny) continue;
-                gj[a * w2 + (a + dj * lv.Nx + di)] = st[q];
-                off += (double)st[q];
+                const double e = (double)__ldcg(P.coef + (size_t)q * P.total + lv.g + a);
+                gj[a * w2 + (a + dj * lv.Nx + di)] = e;
+                off += e;
             }
-            gj[a * w2 + a] = (double)__ldcg(P.rows + 4 * (size_t)P.total + lv.g + a) - off;
+            const bool active = __ldcg(P.l1inv + lv.g + a) > 0.0f;
+            gj[a * w2 + a] = active ? (double)__ldcg(P.rsum + lv.g + a) - off : 0.0;
             gj[a * w2 + kMgCoarse + a] = 1.0;
         }
         __syncthreads();
         for (int piv = 0; piv < nc; piv++) {
-            const double d = gj[piv * w2 + piv];
-            const bool keep = d > 0;
+            if (threadIdx.x == 0) {
+                const double d = gj[piv * w2 + piv];
+                sh_scalar[0] = d > 0 ? 1.0 / d : 0.0;     // one reciprocal a pivot
+            }
+            __syncthreads();
+            const double id = sh_scalar[0];
             // this step's factors, read before the rows change
             const int row = threadIdx.x / w2, col = threadIdx.x % w2;
             const bool mine = threadIdx.x < nc * w2;
@@ -1550,12 +1590,12 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
             const double pv = mine ? gj[piv * w2 + col] : 0.0;
             __syncthreads();
             if (mine) {
-                if (!keep) {
+                if (id == 0.0) {
                     if (row == piv || col == piv || col == kMgCoarse + piv) gj[row * w2 + col] = 0;
                 } else if (row == piv) {
-                    gj[row * w2 + col] = pv / d;
+                    gj[row * w2 + col] = pv * id;
                 } else {
-                    gj[row * w2 + col] -= fac * (pv / d);
+                    gj[row * w2 + col] -= fac * (pv * id);
                 }
             }
             __syncthreads();
@@ -1612,6 +1652,13 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     } else if (rr <= target) {
         converged = true;                                 // the start already meets the tolerance
     }
+    // |r| and its reciprocal, formed once by thread 0 (GB300 runs FP64 at
+    // 1/64 of the FP32 rate)
+    if (threadIdx.x == 0 && !converged) {
+        sh_scalar[3] = sqrt(rr);
+        sh_scalar[4] = 1.0 / sh_scalar[3];
+    }
+    __syncthreads();
     for (int v = 0; !converged && !failed; v++) {
         if (v > 0) {
             // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s
@@ -1630,7 +1677,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         }
         // u = |r| V(r / |r|) (|r| of the last reduction), w = A u, and the
         // inner products
-        const double sig = sqrt(rr), isig = 1.0 / sig;
+        const double sig = sh_scalar[3], isig = sh_scalar[4];
         {
             const MgShared Sh = mg_shared(sm, L0);
 #pragma unroll
@@ -1665,16 +1712,14 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
                 const int k = threadIdx.x + t * kMgThreads;
                 if (k >= cnt) continue;
                 const int n = n0 + k;
-                double az = 0, own = 0;
+                double az = 0;
 #pragma unroll
                 for (int q = 0; q < 9; q++) {
                     // rows are zero towards nodes outside the grid, whose
                     // words read 0
-                    const double zq = (double)mg_f(wv[t][q]);
-                    if (q == 4) own = zq;
-                    az = fma(S.coef[(size_t)q * nn + n], zq, az);
+                    az = fma(S.coef[(size_t)q * nn + n], (double)mg_f(wv[t][q]), az);
                 }
-                const double uk = sig * own, wk = sig * az, rk = r[k];
+                const double uk = sig * (double)mg_f(wv[t][4]), wk = sig * az, rk = r[k];
                 u[k] = uk;
                 w[k] = wk;
                 part[0] = fma(rk, uk, part[0]);
@@ -1709,6 +1754,8 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
                     sh_scalar[0] = bn;
                     sh_scalar[1] = pn;
                     sh_scalar[2] = gn / pn;
+                    sh_scalar[3] = sqrt(rr);
+                    sh_scalar[4] = 1.0 / sh_scalar[3];
                 }
             }
             sh_next = next;
@@ -1865,23 +1912,27 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
     {
         MgPlan P;
         memset(&P, 0, sizeof(P));
-        int nb = (int)((nn + kMgThreads - 1) / kMgThreads);
+        // a grid that block 0 holds whole runs on one block
+        int nb = nn <= (size_t)kMgLocal ? 1 : (int)((nn + kMgThreads - 1) / kMgThreads);
         if (nb > sms) nb = sms;
         if (nb < 1) nb = 1;
-        int Nx = ctx->cfg.Nx, Ny = ctx->cfg.Ny, L = 0, total = 0, smf = 0, cxs = 0, cys = 0;
+        int Nx = ctx->cfg.Nx, Ny = ctx->cfg.Ny, L = 0, total = 0, cxs = 0, cys = 0;
         bool ok = Nx >= 1 && Ny >= 1;
+        int smf = 0;
         while (ok) {
             MgLevel &lv = P.lv[L++];
             lv.Nx = Nx;
             lv.Ny = Ny;
             lv.nn = Nx * Ny;
-            lv.C = (lv.nn + nb - 1) / nb;
+            lv.local = (nb == 1 || lv.nn <= kMgLocal) ? 1 : 0;
+            lv.C = lv.local ? lv.nn : (lv.nn + nb - 1) / nb;
             lv.cx = cxs;
             lv.cy = cys;
             lv.g = total;
+            if (L == 1) smf = 10 * lv.C;      // level 0's rows come first
             lv.sm = smf;
             total += lv.nn;
-            smf += 13 * lv.C;
+            smf += 3 * lv.C;
             if (Nx <= 3 && Ny <= 3) break;
             if (L == kMgMaxLevels) ok = false;
             cxs = Nx > 3;
@@ -1901,7 +1952,7 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
             int mg_per_sm = 0;
             MPMG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mg_per_sm, pcg_mg_kernel, kMgThreads, smem));
             if (mg_per_sm >= 1) {
-                MPMG_CHECK(cudaMalloc(&ctx->mg_rows, 5 * (size_t)total * sizeof(float)));
+                MPMG_CHECK(cudaMalloc(&ctx->mg_rows, 11 * (size_t)total * sizeof(float)));
                 MPMG_CHECK(cudaMalloc(&ctx->mg_words, 3 * (size_t)total * sizeof(unsigned long long)));
                 MPMG_CHECK(cudaMemsetAsync(ctx->mg_words, 0, 3 * (size_t)total * sizeof(unsigned long long),
                                            ctx->stream));
@@ -1909,7 +1960,9 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
                 const unsigned int first_tag = 1;   // the pools start with tag 0
                 MPMG_CHECK(cudaMemcpyAsync(ctx->mg_tag, &first_tag, sizeof(first_tag), cudaMemcpyHostToDevice,
                                            ctx->stream));
-                P.rows = ctx->mg_rows;
+                P.coef = ctx->mg_rows;
+                P.rsum = ctx->mg_rows + 9 * (size_t)total;
+                P.l1inv = ctx->mg_rows + 10 * (size_t)total;
                 P.z1 = ctx->mg_words;
                 P.res = ctx->mg_words + total;
                 P.zf = ctx->mg_words + 2 * (size_t)total;
