@@ -945,8 +945,9 @@ constexpr int kMgLocal = kMgTrips * kMgThreads;   // levels this small are held 
 constexpr int kMgCoarse = 9;           // nodes of the coarsest level at most (3 x 3)
 // one smoothing step: the Chebyshev step for [0.3, 1], 1 / 0.65
 constexpr float kMgOmega = 1.0f / 0.65f;
-// polls of one wait before it gives up (each poll pauses up to 2 us)
-constexpr long long kMgPollLimit = 1ll << 20;
+// polls of one wait before it gives up (a poll is one L2 round trip, about
+// a microsecond: a few seconds in all)
+constexpr long long kMgPollLimit = 1ll << 22;
 
 __device__ __forceinline__ unsigned long long mg_ld(const unsigned long long *p)
 {
@@ -982,32 +983,29 @@ __device__ __forceinline__ bool mg_give_up(long long polls, int *status)
     return false;
 }
 
-// Polls one word until it carries `tag`, pausing 64 ns at first and up to
-// 2 us.  Bounded: on a timeout, or once another block has timed out, the
-// spin error is set and 0 returned.
+// Polls one word until it carries `tag` (each poll waits for its load: no
+// pause is added).  Bounded: on a timeout, or once another block has timed
+// out, the spin error is set and 0 returned.
 __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag, int *status)
 {
-    unsigned ns = 64;
     for (long long polls = 1;; polls++) {
         const unsigned long long v = mg_ld(p);
         if ((unsigned)(v >> 32) == tag) return mg_f(v);
         if (mg_give_up(polls, status)) return 0.0f;
-        __nanosleep(ns);
-        if (ns < 2048) ns *= 2;
     }
 }
 
 // Waits until every word of v carries `tag` (addr(t, q) is the address of
-// word q of trip t).  While some are stale, one of them is polled alone
-// with a growing pause, and once it is current the other stale words are
-// loaded again together: a phase waits about one round trip after its last
-// input is written, and waiting threads load little.  Bounded like mg_poll;
-// on a timeout the words read 0.
+// word q of trip t).  Called by whole warps.  While some lane holds stale
+// words, one lane polls one of them; once that word is current, every lane
+// loads its stale words again together.  A phase so waits about one round
+// trip after its last input is written, and a waiting warp keeps one load
+// in flight.  Bounded like mg_poll; on a timeout the words read 0.
 template <class Addr>
 __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9], unsigned tag, int *status,
                                            Addr addr)
 {
-    unsigned ns = 64;
+    const unsigned lane = threadIdx.x & 31u;
     for (long long polls = 1;; polls++) {
         int ft = -1, fq = 0;
 #pragma unroll
@@ -1020,7 +1018,8 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
                 }
             }
         }
-        if (ft < 0) return;
+        const unsigned stale = __ballot_sync(0xffffffffu, ft >= 0);
+        if (stale == 0) return;
         if (mg_give_up(polls, status)) {
 #pragma unroll
             for (int t = 0; t < kMgTrips; t++) {
@@ -1029,10 +1028,10 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
             }
             return;
         }
-        __nanosleep(ns);
-        if (ns < 2048) ns *= 2;
-        if ((unsigned)(mg_ld(addr(ft, fq)) >> 32) != tag) continue;
-        ns = 64;
+        const unsigned leader = __ffs(stale) - 1;
+        int fresh = 0;
+        if (lane == leader) fresh = (unsigned)(mg_ld(addr(ft, fq)) >> 32) == tag;
+        if (!__shfl_sync(0xffffffffu, fresh, leader)) continue;
 #pragma unroll
         for (int t = 0; t < kMgTrips; t++) {
 #pragma unroll
@@ -1110,10 +1109,26 @@ __device__ __forceinline__ void mg_put_row(const MgPlan &P, int at, float a[9], 
     P.l1inv[at] = li;
 }
 
+// Offset of fine coordinate 2c + o (coarsened) or c + o (not) from its first
+// coarse parent relative to c, and whether it has a second one at +1.
+template <int CO>
+__device__ __forceinline__ constexpr int mg_par0(int o)
+{
+    return CO ? (o >= 0 ? o / 2 : -((1 - o) / 2)) : o;
+}
+
+template <int CO>
+__device__ __forceinline__ constexpr bool mg_par2(int o)
+{
+    return CO ? (o & 1) != 0 : false;
+}
+
 // Galerkin row of coarse node (ci, cj) of level c from the rows of level
 // c - 1: the nine entries of P^T A P, the row sum P^T s, and the diagonal
-// set to the row sum minus the off-diagonal entries.
-__device__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
+// set to the row sum minus the off-diagonal entries.  CX, CY: the level is
+// coarsened along x, y (every index into the row is then a constant).
+template <int CX, int CY>
+__device__ void mg_galerkin_row_t(const MgPlan &P, int c, int I, int ci, int cj)
 {
     const MgLevel &F = P.lv[c - 1], &Cl = P.lv[c];
     float acc[9];
@@ -1122,43 +1137,51 @@ __device__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
     float srow = 0.0f;
 #pragma unroll
     for (int sy = 0; sy < 3; sy++) {
+        if (!CY && sy != 1) continue;
+        const int fy = CY ? 2 * cj + sy - 1 : cj;
         // one row of the fine support at a time: its rows loaded together
         float a[3][9], sf[3];
-        int fxs[3];
-        const int fy = mg_fine_of(cj, sy, Cl.cy);
+        bool in[3];
 #pragma unroll
         for (int sx = 0; sx < 3; sx++) {
-            const int fx = mg_fine_of(ci, sx, Cl.cx);
-            const bool in = fx >= 0 && fx < F.Nx && fy >= 0 && fy < F.Ny;
-            fxs[sx] = in ? fx : -1;
-            const int fi = in ? fy * F.Nx + fx : 0;
+            const int fx = CX ? 2 * ci + sx - 1 : ci;
+            in[sx] = (CX || sx == 1) && fx >= 0 && fx < F.Nx && fy >= 0 && fy < F.Ny;
+            const int fi = in[sx] ? fy * F.Nx + fx : 0;
 #pragma unroll
-            for (int q = 0; q < 9; q++) a[sx][q] = in ? __ldcg(P.coef + (size_t)q * P.total + F.g + fi) : 0.0f;
-            sf[sx] = in ? __ldcg(P.rsum + F.g + fi) : 0.0f;
+            for (int q = 0; q < 9; q++) a[sx][q] = in[sx] ? __ldcg(P.coef + (size_t)q * P.total + F.g + fi) : 0.0f;
+            sf[sx] = in[sx] ? __ldcg(P.rsum + F.g + fi) : 0.0f;
         }
 #pragma unroll
         for (int sx = 0; sx < 3; sx++) {
-            const int fx = fxs[sx];
-            if (fx < 0) continue;
-            const float wi = ((sy == 1) ? 1.0f : 0.5f) * ((sx == 1) ? 1.0f : 0.5f);
+            if (!in[sx]) continue;
+            const float wi = (CY ? ((sy == 1) ? 1.0f : 0.5f) : 1.0f) * (CX ? ((sx == 1) ? 1.0f : 0.5f) : 1.0f);
             srow = fmaf(wi, sf[sx], srow);
 #pragma unroll
             for (int q = 0; q < 9; q++) {
-                const int gx = fx + q % 3 - 1, gy = fy + q / 3 - 1;
-                if (gx < 0 || gx >= F.Nx || gy < 0 || gy >= F.Ny) continue;
-                int px0, px1, py0, py1;
-                const int npx = mg_parents(gx, Cl.cx, px0, px1);
-                const int npy = mg_parents(gy, Cl.cy, py0, py1);
-                const float v = wi * a[sx][q] * ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
-                acc[(py0 - cj + 1) * 3 + (px0 - ci + 1)] += v;
-                if (npx == 2) acc[(py0 - cj + 1) * 3 + (px1 - ci + 1)] += v;
-                if (npy == 2) acc[(py1 - cj + 1) * 3 + (px0 - ci + 1)] += v;
-                if (npx == 2 && npy == 2) acc[(py1 - cj + 1) * 3 + (px1 - ci + 1)] += v;
+                // fine neighbour at offset ox, oy from (2 ci, 2 cj) (or (ci, cj));
+                // entries towards nodes outside the grid are zero
+                const int ox = (CX ? sx - 1 : 0) + q % 3 - 1, oy = (CY ? sy - 1 : 0) + q / 3 - 1;
+                const int x0 = mg_par0<CX>(ox) + 1, y0 = mg_par0<CY>(oy) + 1;
+                const bool x2 = mg_par2<CX>(ox), y2 = mg_par2<CY>(oy);
+                const float v = wi * a[sx][q] * (x2 ? 0.5f : 1.0f) * (y2 ? 0.5f : 1.0f);
+                acc[y0 * 3 + x0] += v;
+                if (x2) acc[y0 * 3 + x0 + 1] += v;
+                if (y2) acc[(y0 + 1) * 3 + x0] += v;
+                if (x2 && y2) acc[(y0 + 1) * 3 + x0 + 1] += v;
             }
         }
     }
     acc[4] = srow - (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[5] + acc[6]) + (acc[7] + acc[8])));
     mg_put_row(P, Cl.g + I, acc, srow);
+}
+
+__device__ __forceinline__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
+{
+    const MgLevel &Cl = P.lv[c];
+    if (Cl.cx && Cl.cy) mg_galerkin_row_t<1, 1>(P, c, I, ci, cj);
+    else if (Cl.cx) mg_galerkin_row_t<1, 0>(P, c, I, ci, cj);
+    else if (Cl.cy) mg_galerkin_row_t<0, 1>(P, c, I, ci, cj);
+    else mg_galerkin_row_t<0, 0>(P, c, I, ci, cj);
 }
 
 // Sum of four values over the block in a fixed order, returned to every
