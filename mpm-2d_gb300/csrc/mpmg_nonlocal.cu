@@ -29,13 +29,19 @@ constexpr int kMgMaxLevels = 16;
 struct MgLevel {
     int Nx, Ny, nn, C;
     int cx, cy;            // coarsened from the finer level along x, y (level 0: 0)
-    int local;             // 1: block 0 holds the whole level (C = nn)
+    int local;             // 1: block 0 holds the whole level (C = nn) in shared memory
     int g;                 // first node of the level in the global pools
-    int sm;                // first float of the level's block arrays in shared memory
+    int sm;                // shared memory (floats): spread level: its b, z1, res; held
+                           // level: its rows (coef[9][nn], l1inv[nn])
+    int smv;               // held level: its b, z1, res, zf (shared memory, floats)
 };
 
 struct MgPlan {
     int L, nblocks, total; // levels, blocks, nodes over all levels
+    int Lg;                // first level held by block 0 (levels Lg .. L - 1)
+    int sm_zf0, sm_vec, sm_fp64;   // shared memory (floats): level 0's own V-cycle
+                                   // results; the held levels' vectors (also the
+                                   // reduction scratch); the FP64 region
     MgLevel lv[kMgMaxLevels];
     float *coef;           // [9][total]: 9-point rows, q = 3 (dj + 1) + (di + 1)
     float *rsum;           // [total]: row sums
@@ -1042,15 +1048,10 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
     }
 }
 
-// Block barrier of the levels held by block 0 (other blocks own none of
-// their nodes and pass).
-__device__ __forceinline__ void mg_local_sync(const MgLevel &lv)
-{
-    if (lv.local && blockIdx.x == 0) __syncthreads();
-}
-
-// Per-level block arrays in shared memory (floats): b, z1, res (C each);
-// level 0 also keeps its rows there (coef0[9][C0], l1inv0[C0] at float 0).
+// Per-level arrays in shared memory (floats).  A level spread over the
+// blocks keeps its b, z1, res (C each) at lv.sm; level 0 also keeps its rows
+// at float 0 (coef0[9][C0], l1inv0[C0]).  A level held by block 0 keeps its
+// rows at lv.sm and b, z1, res, zf (nn each) at lv.smv.
 struct MgShared {
     float *b, *z1, *res;
 };
@@ -1058,7 +1059,7 @@ struct MgShared {
 __device__ __forceinline__ MgShared mg_shared(float *sm, const MgLevel &lv)
 {
     MgShared s;
-    s.b = sm + lv.sm;
+    s.b = sm + (lv.local ? lv.smv : lv.sm);
     s.z1 = s.b + lv.C;
     s.res = s.z1 + lv.C;
     return s;
@@ -1067,12 +1068,16 @@ __device__ __forceinline__ MgShared mg_shared(float *sm, const MgLevel &lv)
 // Row entry q of own node k (global node n) of level l, and D_l1^-1.
 __device__ __forceinline__ float mg_coef(const MgPlan &P, const float *sm, int l, int q, int k, int n)
 {
-    return l == 0 ? sm[q * P.lv[0].C + k] : __ldcg(P.coef + (size_t)q * P.total + P.lv[l].g + n);
+    if (l == 0) return sm[q * P.lv[0].C + k];
+    if (P.lv[l].local) return sm[P.lv[l].sm + q * P.lv[l].nn + n];
+    return __ldcg(P.coef + (size_t)q * P.total + P.lv[l].g + n);
 }
 
 __device__ __forceinline__ float mg_l1inv(const MgPlan &P, const float *sm, int l, int k, int n)
 {
-    return l == 0 ? sm[9 * P.lv[0].C + k] : __ldcg(P.l1inv + P.lv[l].g + n);
+    if (l == 0) return sm[9 * P.lv[0].C + k];
+    if (P.lv[l].local) return sm[P.lv[l].sm + 9 * P.lv[l].nn + n];
+    return __ldcg(P.l1inv + P.lv[l].g + n);
 }
 
 // Coarse parents of fine coordinate g along a direction: g even (or the
@@ -1290,9 +1295,11 @@ __device__ __forceinline__ void mg_residual(const MgPlan &P, const float *sm, in
     }
 }
 
-// Restriction to level c (its own nodes): b = P^T res of level c - 1, then
-// the pre-smoothing step z1 = omega D_l1^-1 b (published), or at the
-// coarsest level b itself (published in the res words for the exact solve).
+// Restriction to level c (its own nodes) from a level c - 1 spread over the
+// blocks: b = P^T res (tagged words of level c - 1), then the pre-smoothing
+// step z1 = omega D_l1^-1 b.  A spread level publishes z1; a held level (block
+// 0) keeps b and z1 in shared memory only, and at the coarsest level z1 is
+// not formed.
 __device__ __forceinline__ void mg_restrict(const MgPlan &P, const float *sm, int c, const MgShared &S, unsigned tag,
                                             int *status)
 {
@@ -1328,12 +1335,10 @@ __device__ __forceinline__ void mg_restrict(const MgPlan &P, const float *sm, in
             b = fmaf(w, mg_f(v[t][q]), b);      // words outside the support read 0
         }
         S.b[k] = b;
-        if (coarsest) {
-            mg_st(P.res + lv.g + I, b, tag);
-        } else {
+        if (!coarsest) {
             const float z = kMgOmega * mg_l1inv(P, sm, c, k, I) * b;
             S.z1[k] = z;
-            mg_st(P.z1 + lv.g + I, z, tag);
+            if (!lv.local) mg_st(P.z1 + lv.g + I, z, tag);
         }
     }
 }
@@ -1414,65 +1419,150 @@ __device__ __forceinline__ void mg_prolong(const MgPlan &P, const float *sm, int
     }
 }
 
-// The V-cycle on b0 (already in level 0's b): the result lands in level 0's
-// zf words with this tag.
-__device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, double *cb, unsigned tag, int *status)
+// Phases of the levels held by block 0: shared memory only, a block barrier
+// after each.
+struct MgHeld {
+    const float *coef, *l1inv;
+    float *b, *z1, *res, *zf;
+    int Nx, Ny, nn;
+};
+
+__device__ __forceinline__ MgHeld mg_held(float *sm, const MgLevel &lv)
 {
-    const int L = P.L;
+    MgHeld h;
+    h.coef = sm + lv.sm;
+    h.l1inv = h.coef + 9 * lv.nn;
+    h.b = sm + lv.smv;
+    h.z1 = h.b + lv.nn;
+    h.res = h.z1 + lv.nn;
+    h.zf = h.res + lv.nn;
+    h.Nx = lv.Nx;
+    h.Ny = lv.Ny;
+    h.nn = lv.nn;
+    return h;
+}
+
+// res = b - A z1 on a held level.
+__device__ __forceinline__ void mgh_residual(const MgHeld &H)
+{
+    for (int n = threadIdx.x; n < H.nn; n += blockDim.x) {
+        const int j = n / H.Nx, i = n - j * H.Nx;
+        float acc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int di = q % 3 - 1, dj = q / 3 - 1;
+            if (i + di < 0 || i + di >= H.Nx || j + dj < 0 || j + dj >= H.Ny) continue;
+            acc = fmaf(H.coef[q * H.nn + n], H.z1[n + dj * H.Nx + di], acc);
+        }
+        H.res[n] = H.b[n] - acc;
+    }
+    __syncthreads();
+}
+
+// b = P^T res of the finer held level F, then z1 = omega D_l1^-1 b (not at
+// the coarsest level).
+__device__ __forceinline__ void mgh_restrict(const MgHeld &F, const MgHeld &H, const MgLevel &lv, bool coarsest)
+{
+    for (int I = threadIdx.x; I < H.nn; I += blockDim.x) {
+        const int cj = I / H.Nx, ci = I - cj * H.Nx;
+        float b = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
+            if (fx < 0 || fx >= F.Nx || fy < 0 || fy >= F.Ny) continue;
+            const float w = ((q % 3 == 1) ? 1.0f : 0.5f) * ((q / 3 == 1) ? 1.0f : 0.5f);
+            b = fmaf(w, F.res[fy * F.Nx + fx], b);
+        }
+        H.b[I] = b;
+        if (!coarsest) H.z1[I] = kMgOmega * H.l1inv[I] * b;
+    }
+    __syncthreads();
+}
+
+// Prolongation and post-smoothing on a held level from the coarser held
+// level C (its zf): z = z1 + P zc + omega D_l1^-1 (res - A P zc).
+__device__ __forceinline__ void mgh_prolong(const MgHeld &H, const MgHeld &Cz, const MgLevel &Cl)
+{
+    for (int n = threadIdx.x; n < H.nn; n += blockDim.x) {
+        const int j = n / H.Nx, i = n - j * H.Nx;
+        float acc = 0.0f, own = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int gx = i + q % 3 - 1, gy = j + q / 3 - 1;
+            if (gx < 0 || gx >= H.Nx || gy < 0 || gy >= H.Ny) continue;
+            int px0, px1, py0, py1;
+            const int npx = mg_parents(gx, Cl.cx, px0, px1);
+            const int npy = mg_parents(gy, Cl.cy, py0, py1);
+            float pz = Cz.zf[py0 * Cz.Nx + px0];
+            if (npx == 2) pz += Cz.zf[py0 * Cz.Nx + px1];
+            if (npy == 2) pz += Cz.zf[py1 * Cz.Nx + px0];
+            if (npx == 2 && npy == 2) pz += Cz.zf[py1 * Cz.Nx + px1];
+            pz *= ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
+            if (q == 4) own = pz;
+            acc = fmaf(H.coef[q * H.nn + n], pz, acc);
+        }
+        const float li = H.l1inv[n];
+        H.zf[n] = (li == 0.0f) ? 0.0f : H.z1[n] + own + kMgOmega * li * (H.res[n] - acc);
+    }
+    __syncthreads();
+}
+
+// The V-cycle on b0 (already in level 0's b): the result lands in level 0's
+// zf words with this tag.  Levels 0 .. Lg - 1 are spread over the blocks;
+// block 0 runs levels Lg .. L - 1 in its shared memory and publishes level
+// Lg's result for the way up.
+__device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsigned tag, int *status)
+{
+    const int L = P.L, Lg = P.Lg;
     {
-        // pre-smoothing at level 0 (or, on a one-level hierarchy, b for the
-        // exact solve)
+        // pre-smoothing at level 0
         const MgLevel &lv = P.lv[0];
         const MgShared S = mg_shared(sm, lv);
         const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
         for (int k = threadIdx.x; k < cnt; k += kMgThreads) {
-            if (L == 1) {
-                mg_st(P.res + n0 + k, S.b[k], tag);
-            } else {
-                const float z = kMgOmega * sm[9 * lv.C + k] * S.b[k];
-                S.z1[k] = z;
-                mg_st(P.z1 + n0 + k, z, tag);
-            }
+            const float z = kMgOmega * sm[9 * lv.C + k] * S.b[k];
+            S.z1[k] = z;
+            mg_st(P.z1 + n0 + k, z, tag);
         }
-        mg_local_sync(lv);
     }
-    for (int l = 0; l + 1 < L; l++) {
+    for (int l = 0; l < Lg; l++) {
         mg_residual(P, sm, l, mg_shared(sm, P.lv[l]), tag, status);
-        mg_local_sync(P.lv[l]);
-        mg_restrict(P, sm, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
-        mg_local_sync(P.lv[l + 1]);
+        if (l + 1 < Lg) mg_restrict(P, sm, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
     }
-    // exact solve at the coarsest level (block 0)
     if (blockIdx.x == 0) {
-        const MgLevel &lv = P.lv[L - 1];
-        const int nc = lv.nn;
-        if (threadIdx.x < nc) cb[threadIdx.x] = mg_poll(P.res + lv.g + threadIdx.x, tag, status);
+        mg_restrict(P, sm, Lg, mg_shared(sm, P.lv[Lg]), tag, status);
         __syncthreads();
-        if (threadIdx.x < nc) {
-            double z = 0;
-            for (int m = 0; m < nc; m++) z = fma(cinv[threadIdx.x * kMgCoarse + m], cb[m], z);
-            mg_st(P.zf + lv.g + threadIdx.x, (float)z, tag);
+        for (int l = Lg; l + 1 < L; l++) {
+            const MgHeld H = mg_held(sm, P.lv[l]);
+            mgh_residual(H);
+            mgh_restrict(H, mg_held(sm, P.lv[l + 1]), P.lv[l + 1], l + 1 == L - 1);
         }
-        __syncthreads();
+        {
+            // exact solve at the coarsest level
+            const MgHeld H = mg_held(sm, P.lv[L - 1]);
+            if (threadIdx.x < H.nn) {
+                double z = 0;
+                for (int m = 0; m < H.nn; m++) z = fma(cinv[threadIdx.x * kMgCoarse + m], (double)H.b[m], z);
+                H.zf[threadIdx.x] = (float)z;
+            }
+            __syncthreads();
+        }
+        for (int l = L - 2; l >= Lg; l--) mgh_prolong(mg_held(sm, P.lv[l]), mg_held(sm, P.lv[l + 1]), P.lv[l + 1]);
+        const MgHeld H = mg_held(sm, P.lv[Lg]);
+        for (int n = threadIdx.x; n < H.nn; n += blockDim.x) mg_st(P.zf + P.lv[Lg].g + n, H.zf[n], tag);
     }
-    for (int l = L - 2; l >= 0; l--) {
-        mg_prolong(P, sm, l, mg_shared(sm, P.lv[l]), tag, status);
-        mg_local_sync(P.lv[l]);
-    }
+    for (int l = Lg - 1; l >= 0; l--) mg_prolong(P, sm, l, mg_shared(sm, P.lv[l]), tag, status);
 }
 
-// Shared memory of pcg_mg_kernel: level 0's rows (10 floats a node), three
-// floats a node of each level a block holds, five FP64 outer vectors a
-// level-0 node, the reduction scratch, the coarsest inverse, its right-hand
-// side and the elimination matrix.
+// Shared memory of pcg_mg_kernel (the offsets are in the plan): level 0's
+// rows, the spread levels' vectors, the held levels' rows, level 0's own
+// V-cycle results, the held levels' vectors (at least the reduction
+// scratch), then doubles: the outer vectors r and w, the coarsest inverse
+// and the elimination matrix.
 inline size_t pcg_mg_smem(const MgPlan &P)
 {
-    size_t floats = 10 * (size_t)P.lv[0].C;
-    for (int l = 0; l < P.L; l++) floats += 3 * (size_t)P.lv[l].C;
-    floats = (floats + 1) & ~(size_t)1;
-    const size_t doubles = 5 * (size_t)P.lv[0].C + 4 * (size_t)kMgThreads + 4 + kMgCoarse * kMgCoarse + kMgCoarse +
-                           2 * kMgCoarse * kMgCoarse;
-    return floats * sizeof(float) + doubles * sizeof(double);
+    const size_t doubles = 2 * (size_t)P.lv[0].C + kMgCoarse * kMgCoarse + 2 * kMgCoarse * kMgCoarse;
+    return (size_t)P.sm_fp64 * sizeof(float) + doubles * sizeof(double);
 }
 
 __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, const MgPlan *__restrict__ plan,
@@ -1490,20 +1580,18 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     const int nblocks = gridDim.x;
     const MgLevel &L0 = P.lv[0];
     const int n0 = blockIdx.x * L0.C, cnt = min(L0.C, nn - n0);
-    size_t fl = 10 * (size_t)L0.C;
-    for (int l = 0; l < P.L; l++) fl += 3 * (size_t)P.lv[l].C;
-    double *dv = smd + ((fl + 1) >> 1);
-    double *r = dv, *p = r + L0.C, *s = p + L0.C, *w = s + L0.C, *u = w + L0.C;
-    double *scratch = u + L0.C;                       // 4 kMgThreads + 4
-    double *cinv = scratch + 4 * kMgThreads + 4;      // kMgCoarse^2
-    double *cb = cinv + kMgCoarse * kMgCoarse;        // kMgCoarse
-    double *gj = cb + kMgCoarse;                      // kMgCoarse x 2 kMgCoarse (coarsest inverse)
+    float *zf0 = sm + P.sm_zf0;                       // level 0's own V-cycle results
+    double *scratch = reinterpret_cast<double *>(sm + P.sm_vec);   // 4 kMgThreads + 4 (between V-cycles)
+    double *dv = reinterpret_cast<double *>(sm + P.sm_fp64);
+    double *r = dv, *w = r + L0.C;                    // outer residual and A u
+    double *cinv = w + L0.C;                          // kMgCoarse^2
+    double *gj = cinv + kMgCoarse * kMgCoarse;        // kMgCoarse x 2 kMgCoarse (coarsest inverse)
     __shared__ double sh_scalar[5];
     __shared__ int sh_next;
     unsigned int episode = 0;
     unsigned tag0;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(tag0) : "l"(P.tag));
-    double x[kMgTrips];
+    double x[kMgTrips], sv[kMgTrips];   // the outer x and s of this thread's nodes (p is in S.p)
 
     // Level 0: FP64 rows (global, for the outer matvec), right-hand side,
     // start; FP32 rows (global for the Galerkin products, and this block's in
@@ -1513,6 +1601,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     for (int t = 0; t < kMgTrips; t++) {
         const int k = threadIdx.x + t * kMgThreads;
         x[t] = 0;
+        sv[t] = 0;
         if (k >= cnt) continue;
         const int n = n0 + k, j = n / Nx, i = n - j * Nx;
         double cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -1534,8 +1623,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
 #pragma unroll
             for (int q = 0; q < 9; q++) cf[q] = 0;
         }
-        p[k] = 0;
-        s[k] = 0;
+        S.p[n] = 0;
 #pragma unroll
         for (int q = 0; q < 9; q++) S.coef[(size_t)q * nn + n] = cf[q];
         S.x[n] = x[t];
@@ -1570,9 +1658,21 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         }
         if (!lv.local) {
             if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
-        } else {
-            mg_local_sync(lv);
+        } else if (blockIdx.x == 0) {
+            __syncthreads();
         }
+    }
+    // the held levels' rows into block 0's shared memory
+    if (blockIdx.x == 0) {
+        for (int l = P.Lg; l < P.L; l++) {
+            const MgLevel &lv = P.lv[l];
+            float *hc = sm + lv.sm;
+            for (int e = threadIdx.x; e < 10 * lv.nn; e += kMgThreads) {
+                const int q = e / lv.nn, n = e - q * lv.nn;
+                hc[e] = __ldcg(q < 9 ? P.coef + (size_t)q * P.total + lv.g + n : P.l1inv + lv.g + n);
+            }
+        }
+        __syncthreads();
     }
     // The coarsest level's inverse (block 0): Gauss-Jordan on the matrix of
     // its active nodes, in FP64, with the diagonal from the row sum.  A node
@@ -1682,6 +1782,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         sh_scalar[4] = 1.0 / sh_scalar[3];
     }
     __syncthreads();
+    double sig_u = 0;       // u = sig_u zf0 (the last V-cycle's result)
     for (int v = 0; !converged && !failed; v++) {
         if (v > 0) {
             // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s
@@ -1689,10 +1790,11 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
             for (int t = 0; t < kMgTrips; t++) {
                 const int k = threadIdx.x + t * kMgThreads;
                 if (k >= cnt) continue;
-                const double pk = fma(beta, p[k], u[k]);
-                const double sk = fma(beta, s[k], w[k]);
-                p[k] = pk;
-                s[k] = sk;
+                const int n = n0 + k;
+                const double pk = fma(beta, S.p[n], sig_u * (double)zf0[k]);
+                const double sk = fma(beta, sv[t], w[k]);
+                S.p[n] = pk;
+                sv[t] = sk;
                 x[t] = fma(alpha, pk, x[t]);
                 r[k] = fma(-alpha, sk, r[k]);
             }
@@ -1701,6 +1803,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         // u = |r| V(r / |r|) (|r| of the last reduction), w = A u, and the
         // inner products
         const double sig = sh_scalar[3], isig = sh_scalar[4];
+        sig_u = sig;
         {
             const MgShared Sh = mg_shared(sm, L0);
 #pragma unroll
@@ -1710,7 +1813,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
             }
         }
         const unsigned tag = tag0 + (unsigned)v;
-        mg_vcycle(P, sm, cinv, cb, tag, S.status);
+        mg_vcycle(P, sm, cinv, tag, S.status);
         {
             const unsigned long long *zf = P.zf;
             unsigned long long wv[kMgTrips][9];
@@ -1742,12 +1845,13 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
                     // words read 0
                     az = fma(S.coef[(size_t)q * nn + n], (double)mg_f(wv[t][q]), az);
                 }
-                const double uk = sig * (double)mg_f(wv[t][4]), wk = sig * az, rk = r[k];
-                u[k] = uk;
+                const float zo = mg_f(wv[t][4]);
+                const double uk = sig * (double)zo, wk = sig * az, rk = r[k];
+                zf0[k] = zo;
                 w[k] = wk;
                 part[0] = fma(rk, uk, part[0]);
                 part[1] = fma(wk, uk, part[1]);
-                part[2] = fma(s[k], uk, part[2]);
+                part[2] = fma(sv[t], uk, part[2]);
                 part[3] = fma(rk, rk, part[3]);
             }
         }
@@ -1935,27 +2039,26 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
     {
         MgPlan P;
         memset(&P, 0, sizeof(P));
-        // a grid that block 0 holds whole runs on one block
+        // a grid whose level 0 fits one block runs on one block
         int nb = nn <= (size_t)kMgLocal ? 1 : (int)((nn + kMgThreads - 1) / kMgThreads);
         if (nb > sms) nb = sms;
         if (nb < 1) nb = 1;
         int Nx = ctx->cfg.Nx, Ny = ctx->cfg.Ny, L = 0, total = 0, cxs = 0, cys = 0;
         bool ok = Nx >= 1 && Ny >= 1;
-        int smf = 0;
         while (ok) {
-            MgLevel &lv = P.lv[L++];
+            MgLevel &lv = P.lv[L];
             lv.Nx = Nx;
             lv.Ny = Ny;
             lv.nn = Nx * Ny;
-            lv.local = (nb == 1 || lv.nn <= kMgLocal) ? 1 : 0;
+            // level 0 is always spread (one block when nb is 1); coarser
+            // levels of at most kMgLocal nodes are held by block 0
+            lv.local = (L > 0 && (nb == 1 || lv.nn <= kMgLocal)) ? 1 : 0;
             lv.C = lv.local ? lv.nn : (lv.nn + nb - 1) / nb;
             lv.cx = cxs;
             lv.cy = cys;
             lv.g = total;
-            if (L == 1) smf = 10 * lv.C;      // level 0's rows come first
-            lv.sm = smf;
             total += lv.nn;
-            smf += 3 * lv.C;
+            L++;
             if (Nx <= 3 && Ny <= 3) break;
             if (L == kMgMaxLevels) ok = false;
             cxs = Nx > 3;
@@ -1966,7 +2069,35 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
         P.L = L;
         P.nblocks = nb;
         P.total = total;
-        ok = ok && P.lv[0].C <= kMgTrips * kMgThreads && nb <= 8 * 32 && P.lv[L - 1].nn <= kMgCoarse;
+        P.Lg = L;
+        for (int l = L - 1; l >= 1 && P.lv[l].local; l--) P.Lg = l;
+        // a hierarchy of one level (at most 3 x 3 nodes) is left to Jacobi
+        ok = ok && L >= 2 && P.Lg < L && P.lv[0].C <= kMgTrips * kMgThreads && nb <= 8 * 32 &&
+             P.lv[L - 1].nn <= kMgCoarse;
+        if (ok) {
+            // shared memory offsets (floats)
+            int off = 10 * P.lv[0].C;                    // level 0's rows
+            for (int l = 0; l < P.Lg; l++) {
+                P.lv[l].sm = off;                        // spread levels: b, z1, res
+                off += 3 * P.lv[l].C;
+            }
+            for (int l = P.Lg; l < L; l++) {
+                P.lv[l].sm = off;                        // held levels' rows
+                off += 10 * P.lv[l].nn;
+            }
+            P.sm_zf0 = off;
+            off += P.lv[0].C;
+            off = (off + 1) & ~1;
+            P.sm_vec = off;                              // held levels' vectors
+            int vec = 0;
+            for (int l = P.Lg; l < L; l++) {
+                P.lv[l].smv = off + vec;
+                vec += 4 * P.lv[l].nn;
+            }
+            const int scratch = 2 * (4 * kMgThreads + 4);   // the reduction scratch (doubles) aliases them
+            off += vec > scratch ? vec : scratch;
+            P.sm_fp64 = (off + 1) & ~1;
+        }
         const size_t smem = ok ? pcg_mg_smem(P) : 0;
         int optin = 0;
         MPMG_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
