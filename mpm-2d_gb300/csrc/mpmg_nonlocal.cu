@@ -954,6 +954,8 @@ constexpr float kMgOmega = 1.0f / 0.65f;
 // polls of one wait before it gives up (a poll is one L2 round trip, about
 // a microsecond: a few seconds in all)
 constexpr long long kMgPollLimit = 1ll << 22;
+// pause of a polling lane after a stale answer (cycles)
+constexpr long long kMgPause = 512;
 
 __device__ __forceinline__ unsigned long long mg_ld(const unsigned long long *p)
 {
@@ -1003,10 +1005,12 @@ __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag,
 
 // Waits until every word of v carries `tag` (addr(t, q) is the address of
 // word q of trip t).  Called by whole warps.  While some lane holds stale
-// words, one lane polls one of them; once that word is current, every lane
-// loads its stale words again together.  A phase so waits about one round
-// trip after its last input is written, and a waiting warp keeps one load
-// in flight.  Bounded like mg_poll; on a timeout the words read 0.
+// words, one lane polls one of them, pausing kMgPause cycles after a stale
+// answer; once that word is current, every lane loads its stale words again
+// together.  A phase so waits a round trip or two after its last input is
+// written, and a waiting warp keeps at most one load in flight (polling
+// traffic slows the phases it waits for).  Bounded like mg_poll; on a
+// timeout the words read 0.
 template <class Addr>
 __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9], unsigned tag, int *status,
                                            Addr addr)
@@ -1036,7 +1040,14 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
         }
         const unsigned leader = __ffs(stale) - 1;
         int fresh = 0;
-        if (lane == leader) fresh = (unsigned)(mg_ld(addr(ft, fq)) >> 32) == tag;
+        if (lane == leader) {
+            fresh = (unsigned)(mg_ld(addr(ft, fq)) >> 32) == tag;
+            if (!fresh) {
+                const long long t0 = clock64();
+                while (clock64() - t0 < kMgPause) {
+                }
+            }
+        }
         if (!__shfl_sync(0xffffffffu, fresh, leader)) continue;
 #pragma unroll
         for (int t = 0; t < kMgTrips; t++) {
@@ -1514,6 +1525,26 @@ __device__ __forceinline__ void mgh_prolong(const MgHeld &H, const MgHeld &Cz, c
 __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsigned tag, int *status)
 {
     const int L = P.L, Lg = P.Lg;
+    if (Lg == 0) {
+        // one block holds every level
+        const MgHeld H = mg_held(sm, P.lv[0]);
+        for (int n = threadIdx.x; n < H.nn; n += blockDim.x) H.z1[n] = kMgOmega * H.l1inv[n] * H.b[n];
+        __syncthreads();
+        for (int l = 0; l + 1 < L; l++) {
+            const MgHeld Hl = mg_held(sm, P.lv[l]);
+            mgh_residual(Hl);
+            mgh_restrict(Hl, mg_held(sm, P.lv[l + 1]), P.lv[l + 1], l + 1 == L - 1);
+        }
+        const MgHeld Hc = mg_held(sm, P.lv[L - 1]);
+        if (threadIdx.x < Hc.nn) {
+            double z = 0;
+            for (int m = 0; m < Hc.nn; m++) z = fma(cinv[threadIdx.x * kMgCoarse + m], (double)Hc.b[m], z);
+            Hc.zf[threadIdx.x] = (float)z;
+        }
+        __syncthreads();
+        for (int l = L - 2; l >= 0; l--) mgh_prolong(mg_held(sm, P.lv[l]), mg_held(sm, P.lv[l + 1]), P.lv[l + 1]);
+        return;
+    }
     {
         // pre-smoothing at level 0
         const MgLevel &lv = P.lv[0];
@@ -1664,7 +1695,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     }
     // the held levels' rows into block 0's shared memory
     if (blockIdx.x == 0) {
-        for (int l = P.Lg; l < P.L; l++) {
+        for (int l = P.Lg > 0 ? P.Lg : 1; l < P.L; l++) {
             const MgLevel &lv = P.lv[l];
             float *hc = sm + lv.sm;
             for (int e = threadIdx.x; e < 10 * lv.nn; e += kMgThreads) {
@@ -1816,6 +1847,8 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         mg_vcycle(P, sm, cinv, tag, S.status);
         {
             const unsigned long long *zf = P.zf;
+            const float *zh = sm + P.lv[0].smv + 3 * P.lv[0].C;   // a held level 0's zf
+            const bool held0 = P.Lg == 0;
             unsigned long long wv[kMgTrips][9];
 #pragma unroll
             for (int t = 0; t < kMgTrips; t++) {
@@ -1825,7 +1858,10 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
                 for (int q = 0; q < 9; q++) {
                     const int di = q % 3 - 1, dj = q / 3 - 1;
                     const bool in = k < cnt && i + di >= 0 && i + di < Nx && j + dj >= 0 && j + dj < Ny;
-                    wv[t][q] = in ? mg_ld(zf + n + dj * Nx + di) : mg_zero(tag);
+                    const int m = n + dj * Nx + di;
+                    wv[t][q] = !in ? mg_zero(tag)
+                                   : held0 ? (((unsigned long long)tag << 32) | __float_as_uint(zh[m]))
+                                           : mg_ld(zf + m);
                 }
             }
             mg_resolve(wv, tag, S.status, [&](int t, int q) {
@@ -1855,6 +1891,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
                 part[3] = fma(rk, rk, part[3]);
             }
         }
+        __syncthreads();      // the scratch aliases the held levels' vectors (a held level 0's zf)
         mg_sum4(part, scratch);
         if (threadIdx.x == 0) {
 #pragma unroll
@@ -2050,9 +2087,9 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
             lv.Nx = Nx;
             lv.Ny = Ny;
             lv.nn = Nx * Ny;
-            // level 0 is always spread (one block when nb is 1); coarser
-            // levels of at most kMgLocal nodes are held by block 0
-            lv.local = (L > 0 && (nb == 1 || lv.nn <= kMgLocal)) ? 1 : 0;
+            // on one block every level is held; otherwise level 0 is spread
+            // and the coarser levels of at most kMgLocal nodes are held
+            lv.local = (nb == 1 || (L > 0 && lv.nn <= kMgLocal)) ? 1 : 0;
             lv.C = lv.local ? lv.nn : (lv.nn + nb - 1) / nb;
             lv.cx = cxs;
             lv.cy = cys;
@@ -2070,7 +2107,7 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
         P.nblocks = nb;
         P.total = total;
         P.Lg = L;
-        for (int l = L - 1; l >= 1 && P.lv[l].local; l--) P.Lg = l;
+        for (int l = L - 1; l >= 0 && P.lv[l].local; l--) P.Lg = l;
         // a hierarchy of one level (at most 3 x 3 nodes) is left to Jacobi
         ok = ok && L >= 2 && P.Lg < L && P.lv[0].C <= kMgTrips * kMgThreads && nb <= 8 * 32 &&
              P.lv[L - 1].nn <= kMgCoarse;
@@ -2082,6 +2119,7 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
                 off += 3 * P.lv[l].C;
             }
             for (int l = P.Lg; l < L; l++) {
+                if (l == 0) continue;                    // a held level 0 keeps its rows at 0
                 P.lv[l].sm = off;                        // held levels' rows
                 off += 10 * P.lv[l].nn;
             }

@@ -15,8 +15,8 @@
     teacher-forced from the GPU's state after three steps, against the oracle,
     whose fluidity solve is a banded LDL^T factorisation of the same
     assembled matrix (the substitute for CXSparse's cs_lusol,
-    g_nonlocal_mu2.c:510-519); the GPU's Jacobi-PCG at the production
-    tolerance (relative residual 1e-10) and at 1e-13.
+    g_nonlocal_mu2.c:510-519); the GPU's multigrid-preconditioned CG at the
+    production tolerance (relative residual 1e-10) and at 1e-13.
 
 Set MPMG_PARITY_REPORT to a file path to have the measured errors appended
 there as JSON lines.

@@ -203,12 +203,15 @@ def test_mixed_nonlocal_vs_fp64_after_100_steps():
 
 def test_mixed_nonlocal_silo_discharge_median_within_5pct():
     # The nonlocal silo's discharge is chaotic in both forms: fills perturbed
-    # by 1e-9 m give FP64 rates from about 300 to 500 (the nodal fluidity
+    # by 1e-9 m give FP64 rates from about 260 to 470 (the nodal fluidity
     # undershoots below zero near the outlet and the stress update
     # p / (p + G dt gf) then swings), and a one-ulp change in the mixed
     # form's sums moves a single run as far.  One run therefore says little;
-    # the medians over eight perturbed fills must agree within 5 %, which a
+    # the medians over sixteen perturbed fills must agree within 5 %, which a
     # consistent bias (FP32 material arithmetic once gave +8 %) would break.
+    # (Over eight fills the median itself scatters by more than 5 %: with
+    # the multigrid solve, FP64 rates spread with a standard deviation of
+    # about 55 around 380.)
     def silo(seed):
         sc = scenes.silo(cells=32, material="g_nonlocal_mu2", props=(1e6, 0.3), dt=1e-4, hole_radius=0.12,
                          open_time=0.05, wall_frac=0.5, fill_height=0.5, mp={"grains_d": 5.3e-4})
@@ -218,7 +221,7 @@ def test_mixed_nonlocal_silo_discharge_median_within_5pct():
         return sc
 
     m = silo(None)["particles"]["m"]
-    seeds = (None, 0, 2, 5, 7, 11, 13, 17)
+    seeds = (None,) + tuple(range(1, 16))
     q = {}
     for precision in ("fp64", "mixed"):
         q[precision] = []
