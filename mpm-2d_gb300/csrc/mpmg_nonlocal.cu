@@ -954,8 +954,8 @@ constexpr float kMgOmega = 1.0f / 0.65f;
 // polls of one wait before it gives up (a poll is one L2 round trip, about
 // a microsecond: a few seconds in all)
 constexpr long long kMgPollLimit = 1ll << 22;
-// pause of a polling lane after a stale answer (cycles)
-constexpr long long kMgPause = 512;
+// sleep of a waiting warp after a stale answer (ns)
+constexpr unsigned kMgNap = 128;
 
 __device__ __forceinline__ unsigned long long mg_ld(const unsigned long long *p)
 {
@@ -1005,12 +1005,12 @@ __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag,
 
 // Waits until every word of v carries `tag` (addr(t, q) is the address of
 // word q of trip t).  Called by whole warps.  While some lane holds stale
-// words, one lane polls one of them, pausing kMgPause cycles after a stale
-// answer; once that word is current, every lane loads its stale words again
-// together.  A phase so waits a round trip or two after its last input is
-// written, and a waiting warp keeps at most one load in flight (polling
-// traffic slows the phases it waits for).  Bounded like mg_poll; on a
-// timeout the words read 0.
+// words, one lane polls one of them and the warp sleeps kMgNap ns after a
+// stale answer; once that word is current, every lane loads its stale words
+// again together.  A phase so waits a round trip or two after its last
+// input is written, while a waiting warp neither floods L2 with polls (which
+// slows the stores it waits for) nor takes many issue slots from the warps
+// that compute.  Bounded like mg_poll; on a timeout the words read 0.
 template <class Addr>
 __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9], unsigned tag, int *status,
                                            Addr addr)
@@ -1040,15 +1040,11 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
         }
         const unsigned leader = __ffs(stale) - 1;
         int fresh = 0;
-        if (lane == leader) {
-            fresh = (unsigned)(mg_ld(addr(ft, fq)) >> 32) == tag;
-            if (!fresh) {
-                const long long t0 = clock64();
-                while (clock64() - t0 < kMgPause) {
-                }
-            }
+        if (lane == leader) fresh = (unsigned)(mg_ld(addr(ft, fq)) >> 32) == tag;
+        if (!__shfl_sync(0xffffffffu, fresh, leader)) {
+            __nanosleep(kMgNap);
+            continue;
         }
-        if (!__shfl_sync(0xffffffffu, fresh, leader)) continue;
 #pragma unroll
         for (int t = 0; t < kMgTrips; t++) {
 #pragma unroll
