@@ -20,6 +20,7 @@
  *   find_filled_elements              libmpm/process_usl.c:677  (process_usl.h:17)
  *   mpm_cleanup                       libmpm/process_usl.c:974  (process.h:253)
  *   initial_loads, time_varying_loads libmpm/loading.c:21,34
+ *   the *_split phase functions       libmpm/process_usl.h:15-22 (below)
  * plus additions that return an int status instead of exiting:
  *   mpm_gpu_attach, mpm_gpu_step, mpm_gpu_sync_host, mpm_gpu_detach, and the
  *   adjoint pair mpm_adj_forward_tape, mpm_adj_backward.
@@ -268,6 +269,37 @@ MPMG_API void explicit_mpm_step_musl_threaded(void *task);
 /* The reference's per-(thread, colour) particle lists (host; the driver calls
    it once before the time loop). */
 MPMG_API void find_filled_elements(job_t *job);
+
+/*
+ * The phases of the threaded USL step (libmpm/process_usl.h:15-22), with the
+ * reference's names, signatures and ranges, on the job's host arrays: each
+ * call gathers its range, runs one FP64 kernel on the GPU (the attached
+ * context's device, device 0 without one) and writes the results back, in
+ * the reference's operation order.  They do not touch an attached GPU
+ * context's device state.  Threads may call them concurrently on disjoint
+ * ranges; a CUDA failure ends the process (the reference's phases return
+ * nothing).
+ *   move_grid_split                      process_usl.c:596-625  (process_usl.h:15)
+ *   create_particle_to_element_map_threaded  process_usl.c:631-674  (:16)
+ *   calculate_shapefunctions_split       process_usl.c:727-760  (:18)
+ *   calculate_strainrate_split           process_usl.c:764-808  (:19; the CPDI
+ *                                        branch, dead in the reference, ends the
+ *                                        process)
+ *   map_to_grid_explicit_split           process_usl.c:812-910  (:20; called by
+ *                                        every thread of the team like the
+ *                                        reference's: the thread with id 0 maps
+ *                                        all lists, and all meet at the job's
+ *                                        barrier once per colour)
+ *   move_particles_explicit_usl_split    process_usl.c:914-957  (:21)
+ *   update_particle_densities_split      process_usl.c:961-970  (:22)
+ */
+MPMG_API void move_grid_split(job_t *job, size_t n_start, size_t n_stop);
+MPMG_API void create_particle_to_element_map_threaded(threadtask_t *task);
+MPMG_API void calculate_shapefunctions_split(job_t *job, size_t p_start, size_t p_stop);
+MPMG_API void calculate_strainrate_split(job_t *job, size_t p_start, size_t p_stop);
+MPMG_API void map_to_grid_explicit_split(job_t *job, size_t thread_id);
+MPMG_API void move_particles_explicit_usl_split(job_t *job, size_t p_start, size_t p_stop);
+MPMG_API void update_particle_densities_split(job_t *job, size_t p_start, size_t p_stop);
 
 MPMG_API void mpm_cleanup(job_t *job);
 

@@ -40,6 +40,7 @@ const double kEmodDefault = 1e6;   // libmpm/material.h:12 (the default dt only)
 struct GpuJob {
     mpmg_ctx *ctx = nullptr;
     int material = -1;
+    int device = 0;                // the context's CUDA device
     double gravity_next = 0.0;     // what time_varying_loads last computed
 };
 
@@ -122,6 +123,14 @@ int report(int rc)
 }
 
 }  // namespace
+
+// CUDA device of the job's attached context, 0 when none is attached (the
+// phase functions of csrc/mpmg_split.cu run there).
+int mpmg_libmpm_job_device(job_t *job)
+{
+    GpuJob *gj = find_job(job);
+    return gj != nullptr ? gj->device : 0;
+}
 
 extern "C" {
 
@@ -384,6 +393,7 @@ int mpm_gpu_attach(job_t *job)
     GpuJob &gj = g_jobs[job];
     gj.ctx = ctx;
     gj.material = mat;
+    gj.device = cfg.device;
     gj.gravity_next = ramp_gravity(job);
     return MPMG_OK;
 }

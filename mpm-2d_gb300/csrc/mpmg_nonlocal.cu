@@ -991,18 +991,6 @@ __device__ __forceinline__ bool mg_give_up(long long polls, int *status)
     return false;
 }
 
-// Polls one word until it carries `tag` (each poll waits for its load: no
-// pause is added).  Bounded: on a timeout, or once another block has timed
-// out, the spin error is set and 0 returned.
-__device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag, int *status)
-{
-    for (long long polls = 1;; polls++) {
-        const unsigned long long v = mg_ld(p);
-        if ((unsigned)(v >> 32) == tag) return mg_f(v);
-        if (mg_give_up(polls, status)) return 0.0f;
-    }
-}
-
 // Waits until every word of v carries `tag` (addr(t, q) is the address of
 // word q of trip t).  Called by whole warps.  While some lane holds stale
 // words, one lane polls one of them and the warp sleeps kMgNap ns after a
@@ -1010,7 +998,8 @@ __device__ __noinline__ float mg_poll(const unsigned long long *p, unsigned tag,
 // again together.  A phase so waits a round trip or two after its last
 // input is written, while a waiting warp neither floods L2 with polls (which
 // slows the stores it waits for) nor takes many issue slots from the warps
-// that compute.  Bounded like mg_poll; on a timeout the words read 0.
+// that compute.  Bounded (kMgPollLimit polls, or another block's timeout):
+// then the spin error is set and the words read 0.
 template <class Addr>
 __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9], unsigned tag, int *status,
                                            Addr addr)

@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", INCLUDE]
 CU_SOURCES = ["mpmg_api.cu", "mpmg_step.cu", "mpmg_sort.cu", "mpmg_nonlocal.cu", "mpmg_sort_noalloc.cu",
               "mpmg_libmpm.cu", "mpmg_mixed.cu", "mpmg_bin.cu", "mpmg_adjoint.cu",
-              "mpmg_io.cu"]
+              "mpmg_io.cu", "mpmg_split.cu"]
 CPP_SOURCES = []
 
 
