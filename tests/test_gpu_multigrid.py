@@ -87,3 +87,44 @@ def test_rectangular_multiblock_solve_vs_oracle(precond):
     if precond == "multigrid":
         assert iters <= 20, iters
     sim.close()
+
+
+@pytest.mark.parametrize("precond", ["multigrid", "jacobi"])
+def test_iteration_cap_reports_non_convergence(precond):
+    """A solve stopped by solver_maxit before the tolerance reports
+    MPMG_ERR_SOLVER (the reference's EXIT_ERROR_CS_SOL) at the next
+    read-back, and last_solve gives the iterations it ran.  (The silo starts
+    above yield everywhere, so the first step's system has a load.)"""
+    scene = scenes.silo_prestressed(cells=32, dt=1e-5)
+    sim = mpm2d.Simulation(scene, solver_tol=1e-14, solver_maxit=2, precond=precond)
+    with pytest.raises(mpm2d.MpmError) as e:
+        sim.step(1)
+        sim.synchronize()
+    assert e.value.status == 2, e.value
+    rc, iters, resid = sim.last_solve()
+    assert iters == 2 and resid > 1e-14, (rc, iters, resid)
+    sim.close()
+
+
+def test_multigrid_warm_start_agrees_with_cold():
+    """With the previous step's fluidity as the start, the solve meets the
+    same tolerance in no more iterations, and the trajectory agrees with the
+    cold-started one to the solve's tolerance."""
+    scene = scenes.silo_prestressed(cells=64, dt=1e-5)
+    cold = mpm2d.Simulation(scene, solver_tol=1e-12, solver_maxit=50000)
+    warm = mpm2d.Simulation(scene, solver_tol=1e-12, solver_maxit=50000, warm_start=True)
+    it_cold, it_warm = [], []
+    for _ in range(5):
+        cold.step(1)
+        warm.step(1)
+        rc_c, ic, _ = cold.last_solve()
+        rc_w, iw, rw = warm.last_solve()
+        assert rc_c == 0 and rc_w == 0 and rw <= 1e-12
+        it_cold.append(ic)
+        it_warm.append(iw)
+    assert sum(it_warm) <= sum(it_cold), (it_warm, it_cold)
+    assert rel_err(warm.get("node_gf"), cold.get("node_gf")) <= 1e-9
+    for f in ("sxx", "sxy", "syy", "x", "y"):
+        assert rel_err(warm.get(f), cold.get(f)) <= 1e-9, f
+    cold.close()
+    warm.close()
