@@ -124,6 +124,10 @@ G2P64_PIPE_INSTR_PER_PARTICLE = 232.4
 # one ncu capture: 80.8 MB read + 17.0 MB written; writes still in L2 at the
 # kernel's end are not in the figure.
 G2P_TRAFFIC_BYTES = 97.8e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one g2p_kernel<1,0> launch
+# on the 1 048 576-particle workload (126.1 + 49.1 MB, the FP64 step's ncu
+# capture)
+G2P64_TRAFFIC_BYTES = 175.2e6
 
 # The compiled reference against the oracle port on this workload, same host
 # and thread count (oracle/time_reference.py, 8-core x86-64 development host,
@@ -280,6 +284,21 @@ def cpu_baseline(scene, steps, threads, warmup=1):
     dt = time.perf_counter() - t0
     n = len(scene["particles"]["x"])
     return n * steps / dt, dt
+
+
+def cpu_nonlocal_baseline(scene, steps, threads):
+    """The nonlocal silo on host cores through the oracle, whose fluidity solve
+    here is Jacobi-preconditioned CG to the same 1e-10 (its banded direct
+    solve, the stand-in for the reference's CXSparse LU, takes about 40 s a
+    step on this silo and is recorded in the baseline notes instead)."""
+    from oracle import oracle as O
+    orc = O.Oracle(scene, nthreads=threads, solver="cg", cg_tol=1e-10)
+    orc.step(1)
+    t0 = time.perf_counter()
+    orc.step(steps)
+    dt = time.perf_counter() - t0
+    st, iters, res = orc.last_solve()
+    return dt / steps, iters
 
 
 def run_reference(args):
@@ -446,7 +465,8 @@ def run_gpu(args):
     step64_survey = phase_bytes({"s": FP64_STEP_SURVEY_BYTES}, "s", n, ne, nn)
     roofline = {"bound": "hbm", "kernel": "g2p (FP64 G2P + g_local_mu2, g2p_kernel<1,0>)",
                 "achieved": g2p64["gbs"], "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": g2p64["gbs"] / peak, "traffic": None,
+                "frac": g2p64["gbs"] / peak,
+                "traffic": G2P64_TRAFFIC_BYTES if n == 1048576 else None,
                 "compute_bound": {
                     "pipe": "fp64", "unit": "FLOP/s", "peak": fp64_peak,
                     "peak_kind": "measured (mpmg_measure_fp64_rate: independent FMA chains, this GPU)"},
@@ -676,9 +696,17 @@ def run_gpu(args):
             "step_60": {"multigrid": {"ms_per_step": late_mg_ms, "iterations_per_step": late_mg_it},
                         "jacobi": {"ms_per_step": late_jac_ms, "iterations_per_step": late_jac_it}},
             "dofs": dofs, "filled_elements": filled,
+            "cpu_baseline": None,
             "note": "steps %d-%d of the run; fluidity phase = bulk fluidity, element assembly, "
                     "multigrid-preconditioned CG (one cooperative kernel), stress update"
                     % (args.warmup + 1, args.warmup + nsteps_nl)}
+        if rank == 0 and not args.no_cpu_baseline:
+            cpu_threads = os.cpu_count() or 1
+            cpu_s, cpu_it = cpu_nonlocal_baseline(nsc, 2, cpu_threads)
+            nonlocal_line["cpu_baseline"] = {
+                "value": nnl / cpu_s, "unit": UNIT, "cores": cpu_threads, "kind": "port",
+                "ms_per_step": 1e3 * cpu_s, "iterations_per_step": cpu_it,
+                "sample": "steps 2-3 of the same silo through the oracle with Jacobi-CG to 1e-10"}
 
     # --- adjoint: gradient of a trajectory loss w.r.t. (mu_s, mu_2, I0, E) -----
     adjoint_line = None
