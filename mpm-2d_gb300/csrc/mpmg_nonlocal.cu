@@ -1098,16 +1098,24 @@ __device__ __forceinline__ int mg_fine_of(int c, int s, int coarsened)
 
 // Writes a level's row of node (level offset g + n): entries, row sum,
 // D_l1^-1 (a row with no entries is not an unknown: all zero).
-__device__ __forceinline__ void mg_put_row(const MgPlan &P, int at, float a[9], float rs)
+// Also into `held` (a held level's shared-memory rows, coef[9][nn] then
+// l1inv[nn], at node k of nn) when given.
+__device__ __forceinline__ void mg_put_row(const MgPlan &P, int at, float a[9], float rs, float *held = nullptr,
+                                           int k = 0, int nn = 0)
 {
     float l1 = 0.0f;
 #pragma unroll
     for (int q = 0; q < 9; q++) l1 += fabsf(a[q]);
     const float li = l1 > 0.0f ? 1.0f / l1 : 0.0f;
 #pragma unroll
-    for (int q = 0; q < 9; q++) P.coef[(size_t)q * P.total + at] = li > 0.0f ? a[q] : 0.0f;
+    for (int q = 0; q < 9; q++) {
+        const float v = li > 0.0f ? a[q] : 0.0f;
+        P.coef[(size_t)q * P.total + at] = v;
+        if (held != nullptr) held[q * nn + k] = v;
+    }
     P.rsum[at] = rs;
     P.l1inv[at] = li;
+    if (held != nullptr) held[9 * nn + k] = li;
 }
 
 // Offset of fine coordinate 2c + o (coarsened) or c + o (not) from its first
@@ -1129,7 +1137,7 @@ __device__ __forceinline__ constexpr bool mg_par2(int o)
 // set to the row sum minus the off-diagonal entries.  CX, CY: the level is
 // coarsened along x, y (every index into the row is then a constant).
 template <int CX, int CY>
-__device__ void mg_galerkin_row_t(const MgPlan &P, int c, int I, int ci, int cj)
+__device__ void mg_galerkin_row_t(const MgPlan &P, int c, int I, int ci, int cj, float *held)
 {
     const MgLevel &F = P.lv[c - 1], &Cl = P.lv[c];
     float acc[9];
@@ -1173,16 +1181,16 @@ __device__ void mg_galerkin_row_t(const MgPlan &P, int c, int I, int ci, int cj)
         }
     }
     acc[4] = srow - (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[5] + acc[6]) + (acc[7] + acc[8])));
-    mg_put_row(P, Cl.g + I, acc, srow);
+    mg_put_row(P, Cl.g + I, acc, srow, held, I, Cl.nn);
 }
 
-__device__ __forceinline__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj)
+__device__ __noinline__ void mg_galerkin_row(const MgPlan &P, int c, int I, int ci, int cj, float *held)
 {
     const MgLevel &Cl = P.lv[c];
-    if (Cl.cx && Cl.cy) mg_galerkin_row_t<1, 1>(P, c, I, ci, cj);
-    else if (Cl.cx) mg_galerkin_row_t<1, 0>(P, c, I, ci, cj);
-    else if (Cl.cy) mg_galerkin_row_t<0, 1>(P, c, I, ci, cj);
-    else mg_galerkin_row_t<0, 0>(P, c, I, ci, cj);
+    if (Cl.cx && Cl.cy) mg_galerkin_row_t<1, 1>(P, c, I, ci, cj, held);
+    else if (Cl.cx) mg_galerkin_row_t<1, 0>(P, c, I, ci, cj, held);
+    else if (Cl.cy) mg_galerkin_row_t<0, 1>(P, c, I, ci, cj, held);
+    else mg_galerkin_row_t<0, 0>(P, c, I, ci, cj, held);
 }
 
 // Sum of four values over the block in a fixed order, returned to every
@@ -1221,7 +1229,8 @@ __device__ __forceinline__ void mg_sum4(double v[4], double *scratch)
 
 // The four per-block partials summed over all blocks in one fixed order by
 // warp 0; every block computes the same totals.
-__device__ __forceinline__ void mg_totals4(const double *partials, int nblocks, double v[4], double *scratch)
+__device__ __forceinline__ void mg_totals4(const double *partials, int nblocks, double v[4], double *scratch,
+                                           int slots = 4)
 {
     const int nt = blockDim.x;
     if (threadIdx.x < 32) {
@@ -1233,7 +1242,8 @@ __device__ __forceinline__ void mg_totals4(const double *partials, int nblocks, 
             const int t = lane + 32 * q;
             if (t < nblocks) {
 #pragma unroll
-                for (int c = 0; c < 4; c++) x[c] += __ldcg(partials + (size_t)c * nblocks + t);
+                for (int c = 0; c < 4; c++)
+                    if (c < slots) x[c] += __ldcg(partials + (size_t)c * nblocks + t);
             }
         }
 #pragma unroll
@@ -1608,6 +1618,7 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     unsigned tag0;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(tag0) : "l"(P.tag));
     double x[kMgTrips], sv[kMgTrips];   // the outer x and s of this thread's nodes (p is in S.p)
+    double bbp = 0;                     // this thread's share of <b, b>
 
     // Level 0: FP64 rows (global, for the outer matvec), right-hand side,
     // start; FP32 rows (global for the Galerkin products, and this block's in
@@ -1653,12 +1664,23 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
             a[q] = nbu ? (float)cf[q] : 0.0f;
             if (nbu) rsum += cf[q];
         }
-        mg_put_row(P, n, a, (float)rsum);
-#pragma unroll
-        for (int q = 0; q < 9; q++) sm[q * L0.C + k] = P.coef[(size_t)q * P.total + n];
-        sm[9 * L0.C + k] = P.l1inv[n];
+        mg_put_row(P, n, a, (float)rsum, sm, k, L0.C);
+        if (unknown) bbp = fma(f, f, bbp);
+    }
+    // From a zero start r = b: <b, b> rides on the first grid barrier (a warm
+    // start forms r = b - A x and its sums after the set-up instead).
+    if (!warm) {
+        double part0[4] = {bbp, 0, 0, 0};
+        mg_sum4(part0, scratch);
+        if (threadIdx.x == 0) S.partials[blockIdx.x] = part0[0];
     }
     if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+    double bb0 = 0;
+    if (!warm) {
+        double tot[4];
+        mg_totals4(S.partials, nblocks, tot, scratch, 1);
+        bb0 = tot[0];
+    }
     // every block has read the tag counter: reserve this solve's tags
     if (blockIdx.x == 0 && threadIdx.x == 0) *P.tag = tag0 + (unsigned)S.maxit + 2u;
 
@@ -1670,25 +1692,13 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         const int c0 = blockIdx.x * lv.C, ccnt = min(lv.C, lv.nn - c0);
         for (int k = threadIdx.x; k < ccnt; k += kMgThreads) {
             const int I = c0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
-            mg_galerkin_row(P, c, I, ci, cj);
+            mg_galerkin_row(P, c, I, ci, cj, lv.local ? sm + lv.sm : nullptr);
         }
         if (!lv.local) {
             if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
         } else if (blockIdx.x == 0) {
             __syncthreads();
         }
-    }
-    // the held levels' rows into block 0's shared memory
-    if (blockIdx.x == 0) {
-        for (int l = P.Lg > 0 ? P.Lg : 1; l < P.L; l++) {
-            const MgLevel &lv = P.lv[l];
-            float *hc = sm + lv.sm;
-            for (int e = threadIdx.x; e < 10 * lv.nn; e += kMgThreads) {
-                const int q = e / lv.nn, n = e - q * lv.nn;
-                hc[e] = __ldcg(q < 9 ? P.coef + (size_t)q * P.total + lv.g + n : P.l1inv + lv.g + n);
-            }
-        }
-        __syncthreads();
     }
     // The coarsest level's inverse (block 0): Gauss-Jordan on the matrix of
     // its active nodes, in FP64, with the diagonal from the row sum.  A node
@@ -1746,38 +1756,44 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         __syncthreads();
     }
 
-    // r = b - A x, <b, b>, <r, r> (x of the neighbours is final since the
-    // first barrier)
+    // warm start: r = b - A x, <b, b>, <r, r> (x of the neighbours is final
+    // since the first barrier)
     double part[4] = {0, 0, 0, 0};
+    double bb, rr;
+    if (!warm) {
+        bb = bb0;
+        rr = bb0;
+    } else {
 #pragma unroll
-    for (int t = 0; t < kMgTrips; t++) {
-        const int k = threadIdx.x + t * kMgThreads;
-        if (k >= cnt) continue;
-        const int n = n0 + k, j = n / Nx, i = n - j * Nx;
-        const double b = r[k];
-        double ax = 0;
+        for (int t = 0; t < kMgTrips; t++) {
+            const int k = threadIdx.x + t * kMgThreads;
+            if (k >= cnt) continue;
+            const int n = n0 + k, j = n / Nx, i = n - j * Nx;
+            const double b = r[k];
+            double ax = 0;
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const int di = q % 3 - 1, dj = q / 3 - 1;
-            if (i + di < 0 || i + di >= Nx || j + dj < 0 || j + dj >= Ny) continue;
-            ax = fma(S.coef[(size_t)q * nn + n], __ldcg(S.x + n + dj * Nx + di), ax);
+            for (int q = 0; q < 9; q++) {
+                const int di = q % 3 - 1, dj = q / 3 - 1;
+                if (i + di < 0 || i + di >= Nx || j + dj < 0 || j + dj >= Ny) continue;
+                ax = fma(S.coef[(size_t)q * nn + n], __ldcg(S.x + n + dj * Nx + di), ax);
+            }
+            const double rk = b - ax;
+            r[k] = rk;
+            part[0] = fma(b, b, part[0]);
+            part[1] = fma(rk, rk, part[1]);
         }
-        const double rk = b - ax;
-        r[k] = rk;
-        part[0] = fma(b, b, part[0]);
-        part[1] = fma(rk, rk, part[1]);
+        mg_sum4(part, scratch);
+        if (threadIdx.x == 0) {
+            S.partials[0 * nblocks + blockIdx.x] = part[0];
+            S.partials[1 * nblocks + blockIdx.x] = part[1];
+            S.partials[2 * nblocks + blockIdx.x] = 0;
+            S.partials[3 * nblocks + blockIdx.x] = 0;
+        }
+        if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
+        mg_totals4(S.partials, nblocks, part, scratch);
+        bb = part[0];
+        rr = part[1];
     }
-    mg_sum4(part, scratch);
-    if (threadIdx.x == 0) {
-        S.partials[0 * nblocks + blockIdx.x] = part[0];
-        S.partials[1 * nblocks + blockIdx.x] = part[1];
-        S.partials[2 * nblocks + blockIdx.x] = 0;
-        S.partials[3 * nblocks + blockIdx.x] = 0;
-    }
-    if (!tile_grid_barrier(S.barrier, ++episode * (unsigned)nblocks, S.status)) return;
-    mg_totals4(S.partials, nblocks, part, scratch);
-    const double bb = part[0];
-    double rr = part[1];
     const double target = S.tol * S.tol * bb;
 
     int it = 0;
