@@ -36,6 +36,7 @@ constexpr double kThird = 1.0 / 3.0;   // RN(1/3), the reciprocal of the divisor
 struct Elastic {
     double G, K, lambda, dt;
     double inv_G, inv_dt;   // RN(1/G), RN(1/dt)
+    double Gdt, inv_Gdt;    // RN(G dt), RN(1 / RN(G dt))
 };
 
 // exp(x) for the volume update v <- v exp(dt tr D), whose argument is tiny at
@@ -84,7 +85,27 @@ __device__ __forceinline__ double negative_root(double a, double b, double c)
 struct Mu2Params {
     double mu_s, mu_2, I0, grains_rho, grains_d, rho_critical, A;
     double inv_grains_rho, inv_grains_d;   // RN(1/grains_rho), RN(1/grains_d)
+    double rho_lo, rho_hi;                 // RN(rho_critical (1 - 2^-47)), RN(rho_critical (1 + 2^-47))
+    double AAdd, inv_AAdd;                 // RN(RN(RN(A A) d) d) and its reciprocal
 };
+
+// RN(m / v) < rho_critical, decided as the reference's division and compare
+// decide it, without the division for most particles.  For normal v > 0 and
+// rho_lo, rho_hi as above: m < RN(v rho_lo) implies
+// m / v < rho_critical (1 - 2^-48), hence RN(m / v) < rho_critical; and
+// m > RN(v rho_hi) implies m / v > rho_critical (1 + 2^-48), hence
+// RN(m / v) > rho_critical (the roundings add at most 3 2^-53 relative, and
+// the doubles within 2^-48 of rho_critical are further than an ulp from it).
+// Only m inside the bracket, and any v that is not a normal positive number
+// above 2^-959 (or a NaN), takes the division.
+__device__ __forceinline__ bool below_density(double m, double v, const Mu2Params &mp)
+{
+    if (__double_as_longlong(v) > 0x0400000000000000LL && __double_as_longlong(v) < 0x7ff0000000000000LL) {
+        if (m < __dmul_rn(v, mp.rho_lo)) return true;
+        if (m > __dmul_rn(v, mp.rho_hi)) return false;
+    }
+    return __ddiv_rn(m, v) < mp.rho_critical;
+}
 
 // g_local_mu2 calculate_stress_threaded, g_local_mu2.c:165-310, written for
 // the plane-strain stress it keeps: T = [[Txx, Txy, 0], [Txy, Tyy, 0],
@@ -99,32 +120,37 @@ __device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &
     const double G = el.G, dt = el.dt;
     const double lambda = el.lambda;   // K - 2 G / 3, formed on the host with the same roundings
     // L (:191-199), W = skw(L), D = sym(L) (tensor.c:330-384)
+    // Exact shortcuts, bit for bit the reference's values for finite
+    // operands below DBL_MAX / 2: 0.5 (x + x) is x; W T - T W has xx entry
+    // RN(W Txy) + RN(W Txy), an exact doubling, and yy entry its negative;
+    // 0 * 2G is +0.
     double Lxy = add(exy, wxy), Lyx = sub(exy, wxy);
     double Wxy = mul(0.5, sub(Lxy, Lyx));
-    double Dxx = mul(0.5, add(exx, exx));
+    double Dxx = exx;
     double Dxy = mul(0.5, add(Lxy, Lyx));
-    double Dyy = mul(0.5, add(eyy, eyy));
+    double Dyy = eyy;
     double trD = add(Dxx, Dyy);
     // Jaumann term JS = W T - T W (:209-212)
-    double JSxx = add(mul(Wxy, Txy), -mul(Txy, -Wxy));
+    const double wt = mul(Wxy, Txy);
+    double JSxx = add(wt, wt);
     double JSxy = add(mul(Wxy, Tyy), -mul(Txx, Wxy));
-    double JSyy = add(mul(-Wxy, Txy), -mul(Txy, Wxy));
+    double JSyy = -JSxx;
     // trial stress (:215-222)
     const double twoG = mul(2.0, G);
     double lt = mul(lambda, trD);
     double Txx_tr = add(mul(add(add(mul(Dxx, twoG), lt), JSxx), dt), Txx);
     double Txy_tr = add(mul(add(mul(Dxy, twoG), JSxy), dt), Txy);
     double Tyy_tr = add(mul(add(add(mul(Dyy, twoG), lt), JSyy), dt), Tyy);
-    double Tzz_tr = add(mul(add(mul(0.0, twoG), lt), dt), Tzz);
+    double Tzz_tr = add(mul(add(0.0, lt), dt), Tzz);
     // decompose and contract (:225-228; tensor.c:205-224, :422-437)
     double p_tr = dvd_known(add(add(Txx_tr, Tyy_tr), Tzz_tr), 3.0, kThird);
     double T0xx = sub(Txx_tr, p_tr), T0xy = Txy_tr, T0yy = sub(Tyy_tr, p_tr), T0zz = sub(Tzz_tr, p_tr);
     double tt = add(add(add(add(mul(T0xx, T0xx), mul(T0xy, T0xy)), mul(T0xy, T0xy)), mul(T0yy, T0yy)),
                     mul(T0zz, T0zz));
     double tau_tr = __dsqrt_rn(mul(0.5, tt));
-    p_tr = mul(p_tr, -1.0);
+    p_tr = -p_tr;
 
-    const bool density_flag = dvd(m, v) < mp.rho_critical;
+    const bool density_flag = below_density(m, v, mp);
     double nup_tau;
     if (density_flag || p_tr <= 0) {
         nup_tau = 0;
@@ -415,7 +441,7 @@ __device__ __forceinline__ void nonlocal_mu2_trial(const Elastic &el, double exx
                                                    double &t0xy, double &t0yy, double &tau_tr)
 {
     const double G = el.G, dt = el.dt;
-    const double lambda = sub(el.K, dvd(mul(2.0, G), 3.0));
+    const double lambda = el.lambda;   // sub(K, dvd(mul(2, G), 3)), formed on the host with the same roundings
     const double twoG = mul(2.0, G);
     double trD = add(exx, eyy);
     double dsjxx = add(mul(lambda, trD), mul(twoG, exx));
@@ -446,7 +472,7 @@ __device__ __forceinline__ void nonlocal_mu2_bulk(const Elastic &el, const Mu2Pa
     const double G = el.G, dt = el.dt;
     double p_tr, t0xx, t0xy, t0yy, tau_tr;
     nonlocal_mu2_trial(el, exx, exy, eyy, wxy, sxx, sxy, syy, p_tr, t0xx, t0xy, t0yy, tau_tr);
-    dense = (dvd(m, v) < mp.rho_critical || p_tr < 0) ? 0.0 : 1.0;
+    dense = (below_density(m, v, mp) || p_tr < 0) ? 0.0 : 1.0;
     if (dense == 0 || p_tr <= 0) {
         gf_local = 0;
         xisq_inv = 0;
@@ -458,15 +484,16 @@ __device__ __forceinline__ void nonlocal_mu2_bulk(const Elastic &el, const Mu2Pa
             scale_factor = 1.0;
         } else {
             double S2 = mul(mp.mu_2, p_tr);
-            double alpha = dvd(mul(mul(mul(G, mp.I0), dt), __dsqrt_rn(dvd(p_tr, mp.grains_rho))), mp.grains_d);
+            double alpha = dvd_known(mul(mul(mul(G, mp.I0), dt),
+                                         __dsqrt_rn(dvd_known(p_tr, mp.grains_rho, mp.inv_grains_rho))),
+                                     mp.grains_d, mp.inv_grains_d);
             double B = -add(add(S2, tau_tr), alpha);
             double H = add(mul(S2, tau_tr), mul(S0, alpha));
             tau_tau = negative_root(1.0, B, H);
             scale_factor = dvd(tau_tau, tau_tr);
         }
-        gf_local = mul(dvd(p_tr, mul(G, dt)), sub(dvd(1.0, scale_factor), 1.0));
-        xisq_inv = dvd(fabs(sub(dvd(tau_tau, p_tr), mp.mu_s)),
-                       mul(mul(mul(mp.A, mp.A), mp.grains_d), mp.grains_d));
+        gf_local = mul(dvd_known(p_tr, el.Gdt, el.inv_Gdt), sub(dvd(1.0, scale_factor), 1.0));
+        xisq_inv = dvd_known(fabs(sub(dvd(tau_tau, p_tr), mp.mu_s)), mp.AAdd, mp.inv_AAdd);
     } else {
         gf_local = 0;
         xisq_inv = 0;
@@ -486,9 +513,9 @@ __device__ __forceinline__ void nonlocal_mu2_stress(const Elastic &el, double de
         nup_tau = 0;
         sxx = 0; sxy = 0; syy = 0;
     } else if (p_tr > 0) {
-        double scale_factor = dvd(p_tr, add(mul(mul(G, dt), gf), p_tr));
+        double scale_factor = dvd(p_tr, add(mul(el.Gdt, gf), p_tr));
         double tau_tau = mul(tau_tr, scale_factor);
-        nup_tau = dvd(dvd(sub(tau_tr, tau_tau), G), dt);
+        nup_tau = dvd_known(dvd_known(sub(tau_tr, tau_tau), G, el.inv_G), dt, el.inv_dt);
         sxx = sub(mul(scale_factor, t0xx), p_tr);
         sxy = mul(scale_factor, t0xy);
         syy = sub(mul(scale_factor, t0yy), p_tr);

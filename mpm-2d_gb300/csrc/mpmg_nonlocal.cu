@@ -2308,6 +2308,8 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     el.dt = c.dt;
     el.inv_G = 1.0 / ctx->G;
     el.inv_dt = 1.0 / c.dt;
+    el.Gdt = ctx->G * c.dt;
+    el.inv_Gdt = 1.0 / el.Gdt;
     if (mu2) {
         fluidity_stress_kernel<true, false><<<blocks_for(n, 256), 256, 0, s>>>(
             n, c.Nx, ctx->Ex, el, np, ctx->d_params, ctx->active, ctx->in_element, ctx->xl, ctx->yl,

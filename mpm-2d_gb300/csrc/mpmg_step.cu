@@ -619,6 +619,8 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.el.dt = c.dt;
     A.el.inv_G = 1.0 / ctx->G;
     A.el.inv_dt = 1.0 / c.dt;
+    A.el.Gdt = ctx->G * c.dt;
+    A.el.inv_Gdt = 1.0 / A.el.Gdt;
     A.mu2.mu_s = c.mp[MPMG_MP_MU_S];
     A.mu2.mu_2 = c.mp[MPMG_MP_MU_2];
     A.mu2.I0 = c.mp[MPMG_MP_I0];
@@ -628,6 +630,10 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.mu2.A = c.mp[MPMG_MP_A];
     A.mu2.inv_grains_rho = 1.0 / A.mu2.grains_rho;
     A.mu2.inv_grains_d = 1.0 / A.mu2.grains_d;
+    A.mu2.rho_lo = A.mu2.rho_critical * (1.0 - 0x1p-47);
+    A.mu2.rho_hi = A.mu2.rho_critical * (1.0 + 0x1p-47);
+    A.mu2.AAdd = ((A.mu2.A * A.mu2.A) * A.mu2.grains_d) * A.mu2.grains_d;
+    A.mu2.inv_AAdd = 1.0 / A.mu2.AAdd;
     A.nl.E = c.mp[MPMG_MP_E];
     A.nl.nu = c.mp[MPMG_MP_NU];
     A.nl.mu_s = c.mp[MPMG_MP_MU_S];
