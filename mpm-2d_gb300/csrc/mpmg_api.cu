@@ -371,7 +371,8 @@ int mpmg_destroy(mpmg_ctx *ctx)
                      &ctx->sxy, &ctx->syy, &ctx->ux, &ctx->uy, &ctx->Tzz, &ctx->ax, &ctx->ay,
                      &ctx->exx, &ctx->exy, &ctx->eyy, &ctx->wxy, &ctx->xl, &ctx->yl, &ctx->cell_sums,
                      &ctx->node_m, &ctx->node_ax, &ctx->node_ay, &ctx->node_vx, &ctx->node_vy,
-                     &ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy, &ctx->node_gf};
+                     &ctx->node_mx, &ctx->node_my, &ctx->node_fx, &ctx->node_fy, &ctx->node_gf,
+                     &ctx->nl_trial};
     for (double **p : dp) {
         cudaFree(*p);
         *p = nullptr;
@@ -626,6 +627,7 @@ int mpmg_create(const mpmg_config *cfg, size_t n, const double *m, const double 
         TRY(alloc_step_record(ctx, 1));
         TRY(mpmg_bin_init(ctx));
         if (nonlocal) TRY(mpmg_nonlocal_init(ctx));
+        if (cfg->material == MPMG_G_NONLOCAL_MU2) TRY(dalloc(&ctx->nl_trial, 5 * n));
 
         // mpm_init copies (process_usl.c:88-126) and material_init.
         TRY(upload(ctx, ctx->m, m, n));

@@ -74,7 +74,7 @@ struct MixedState {
     int g2p_tile;          // particles a G2P tile (256 or 128)
     int p2g_variant;       // batched P2G tile (kP2GElems / kP2GStage index)
     double *export_buf;    // one FP64 particle field in caller order, for read-back
-    float4 *nl_E, *nl_F;   // g_nonlocal_mu2: strain rate and bulk fluidity per stored particle
+    float4 *nl_T, *nl_F;   // g_nonlocal_mu2: trial stress and bulk fluidity per stored particle
 };
 
 // A batch of independent simulations sharing one context: their particles,
@@ -142,6 +142,7 @@ struct mpmg_ctx {
     // Nonlocal fluidity solve.
     double *elem_k;        // 10 matrix entries per element, value-major
     double *elem_f;        // 4 RHS entries per element, value-major
+    double *nl_trial;      // g_nonlocal_mu2: trial stress from the G2P, 5 per particle, value-major
     double *cg_x, *cg_r, *cg_p, *cg_q, *cg_dinv, *cg_w;   // per node
     double *cg_coef;       // 9-point rows of the assembled matrix, 9 per node
     double *cg_partials;   // per-block partial sums

@@ -462,16 +462,13 @@ __device__ __forceinline__ void nonlocal_mu2_trial(const Elastic &el, double exx
 }
 
 // calculate_bulk_granular_fluidity, g_nonlocal_mu2.c:238-321, for one
-// particle: dense flag, local fluidity and the inverse squared cooperativity
-// length.
+// particle, from its trial pressure and shear stress (nonlocal_mu2_trial):
+// dense flag, local fluidity and the inverse squared cooperativity length.
 __device__ __forceinline__ void nonlocal_mu2_bulk(const Elastic &el, const Mu2Params &mp, double m,
-                                                  double v, double exx, double exy, double eyy,
-                                                  double wxy, double sxx, double sxy, double syy,
-                                                  double &dense, double &gf_local, double &xisq_inv)
+                                                  double v, double p_tr, double tau_tr, double &dense,
+                                                  double &gf_local, double &xisq_inv)
 {
     const double G = el.G, dt = el.dt;
-    double p_tr, t0xx, t0xy, t0yy, tau_tr;
-    nonlocal_mu2_trial(el, exx, exy, eyy, wxy, sxx, sxy, syy, p_tr, t0xx, t0xy, t0yy, tau_tr);
     dense = (below_density(m, v, mp) || p_tr < 0) ? 0.0 : 1.0;
     if (dense == 0 || p_tr <= 0) {
         gf_local = 0;
@@ -500,16 +497,22 @@ __device__ __forceinline__ void nonlocal_mu2_bulk(const Elastic &el, const Mu2Pa
     }
 }
 
-// Stress update after the fluidity solve, g_nonlocal_mu2.c:160-218.
-__device__ __forceinline__ void nonlocal_mu2_stress(const Elastic &el, double dense, double gf,
-                                                    double exx, double exy, double eyy, double wxy,
-                                                    double &sxx, double &sxy, double &syy,
-                                                    double &gammap, double &gammadotp)
+// Stress update after the fluidity solve, g_nonlocal_mu2.c:160-218. The
+// reference forms the trial stress again at :166-186 from the same strain
+// rates and start-of-step stress as the bulk pass; the G2P keeps that trial
+// instead, with the dense flag folded into the pressure (p_d = p_tr where the
+// particle is dense, 0 where it is not), so `dense == 0 || p_tr <= 0` reads
+// `p_d <= 0`. sxx, sxy, syy hold the start-of-step stress, which a NaN trial
+// pressure keeps (neither branch of the reference is taken).
+__device__ __forceinline__ void nonlocal_mu2_stress(const Elastic &el, double gf, double p_d,
+                                                    double t0xx, double t0xy, double t0yy,
+                                                    double tau_tr, double &sxx, double &sxy,
+                                                    double &syy, double &gammap, double &gammadotp)
 {
     const double G = el.G, dt = el.dt;
-    double p_tr, t0xx, t0xy, t0yy, tau_tr, nup_tau;
-    nonlocal_mu2_trial(el, exx, exy, eyy, wxy, sxx, sxy, syy, p_tr, t0xx, t0xy, t0yy, tau_tr);
-    if (dense == 0 || p_tr <= 0) {
+    const double p_tr = p_d;
+    double nup_tau;
+    if (p_tr <= 0) {
         nup_tau = 0;
         sxx = 0; sxy = 0; syy = 0;
     } else if (p_tr > 0) {

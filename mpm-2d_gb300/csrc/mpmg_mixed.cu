@@ -236,12 +236,14 @@ __device__ __forceinline__ void nonlocal_mu2_bulk_f(const MatF &p, float m, floa
     }
 }
 
-__device__ __forceinline__ void nonlocal_mu2_stress_f(const MatF &p, float dense, float gf, float p_tr, float t0xx,
-                                                      float t0xy, float t0yy, float tau_tr, float &sxx, float &sxy,
-                                                      float &syy, float &gp, float &gdp)
+// p_d: the trial pressure where the particle is dense, 0 where it is not.
+__device__ __forceinline__ void nonlocal_mu2_stress_f(const MatF &p, float gf, float p_d, float t0xx, float t0xy,
+                                                      float t0yy, float tau_tr, float &sxx, float &sxy, float &syy,
+                                                      float &gp, float &gdp)
 {
+    const float p_tr = p_d;
     float nup = 0.0f;
-    if (dense == 0.0f || !(p_tr > 0.0f)) {
+    if (!(p_tr > 0.0f)) {
         sxx = sxy = syy = 0.0f;
     } else {
         const double scale = (double)p_tr / ((double)p.G * p.dt * gf + p_tr);
@@ -254,11 +256,14 @@ __device__ __forceinline__ void nonlocal_mu2_stress_f(const MatF &p, float dense
     gdp = nup;
 }
 
-// Per-particle values the nonlocal step keeps from the G2P to the stress
-// update after the fluidity solve, indexed by stored position:
-// E = {exx, exy, eyy, wxy}, F = {dense, gf_local, xisq_inv, updated volume}.
+// Per-particle values the nonlocal step keeps from the G2P to the assembly
+// and the stress update after the fluidity solve, indexed by stored position:
+// T = {p_d, t0xx, t0xy, t0yy}, the trial stress of g_nonlocal_mu2.c:166-186
+// with the dense flag folded into the pressure (p_d = p_tr where dense, 0
+// where not); F = {tau_tr, gf_local, xisq_inv, v_d}, v_d the updated volume
+// where dense and 0 where not.
 struct NLOut {
-    float4 *E, *F;
+    float4 *T, *F;
 };
 
 __device__ __forceinline__ void bc_mask_m(const BcM &bc, int i, int j, double t_now, bool &mx, bool &my)
@@ -915,8 +920,9 @@ __device__ __forceinline__ uint32_t g2p_particle(const MemberM &M, uint32_t sent
         float p_tr, t0xx, t0xy, t0yy, tau_tr, dense, gfl, xisq;
         nonlocal_mu2_trial_f(mp, exx, exy, eyy, wxy, sxx, sxy, syy, p_tr, t0xx, t0xy, t0yy, tau_tr);
         nonlocal_mu2_bulk_f(mp, m, vol, p_tr, tau_tr, dense, gfl, xisq);
-        nl.E[src] = make_float4(exx, exy, eyy, wxy);
-        nl.F[src] = make_float4(dense, gfl, xisq, vol);
+        const bool d = dense != 0.0f;
+        nl.T[src] = make_float4(d ? p_tr : 0.0f, t0xx, t0xy, t0yy);
+        nl.F[src] = make_float4(tau_tr, gfl, xisq, d ? vol : 0.0f);
     }
 
     // New element from the local coordinates (WHICH_ELEMENT4, process_usl.c:43-44).
@@ -1136,7 +1142,7 @@ __global__ void __launch_bounds__(128) mx_assemble_kernel(int ne, float inv_h, c
     for (int k = k0; k < k1; k++) {
         const uint32_t i = perm[k];
         const float4 f4 = nl.F[i];
-        if (f4.x == 0.0f) continue;      // not dense
+        if (f4.w == 0.0f) continue;      // not dense
         const float4 a4 = SA[i];
         const float a = a4.x, b = a4.y, ox = 1.0f - a, oy = 1.0f - b;
         const float sf[4] = {ox * oy, a * oy, a * b, ox * b};
@@ -1171,16 +1177,15 @@ __global__ void __launch_bounds__(256) mx_fluidity_stress_kernel(GeomM g, MatF m
     const uint32_t dst = rank[i];
     const int cj = (int)mpmg_div((uint32_t)e, g.div_Ex), ci = e - cj * g.Ex;
     const int n0 = cj * g.Nx + ci;
-    const float4 a4 = S.A[i], b4 = S.B[i];
-    const float syy0 = S.C[i].x, gp0 = S.D[i].x;
+    const float4 a4 = S.A[i];
+    const float gp0 = S.D[i].x;
     const float a = a4.x, b = a4.y, ox = 1.0f - a, oy = 1.0f - b;
     const float gf = (float)node_gf[n0] * (ox * oy) + (float)node_gf[n0 + 1] * (a * oy) +
                      (float)node_gf[n0 + 1 + g.Nx] * (a * b) + (float)node_gf[n0 + g.Nx] * (ox * b);
-    const float4 e4 = nl.E[i], f4 = nl.F[i];
-    float p_tr, t0xx, t0xy, t0yy, tau_tr;
-    nonlocal_mu2_trial_f(mp, e4.x, e4.y, e4.z, e4.w, b4.z, b4.w, syy0, p_tr, t0xx, t0xy, t0yy, tau_tr);
+    const float4 t4 = nl.T[i];
+    const float tau_tr = nl.F[i].x;
     float sxx, sxy, syy, gp = gp0, gdp;
-    nonlocal_mu2_stress_f(mp, f4.x, gf, p_tr, t0xx, t0xy, t0yy, tau_tr, sxx, sxy, syy, gp, gdp);
+    nonlocal_mu2_stress_f(mp, gf, t4.x, t4.y, t4.z, t4.w, tau_tr, sxx, sxy, syy, gp, gdp);
     float *Bd = reinterpret_cast<float *>(D.B + dst);
     float *Cd = reinterpret_cast<float *>(D.C + dst);
     float *Dd = reinterpret_cast<float *>(D.D + dst);
@@ -1403,7 +1408,7 @@ int mpmg_mixed_init(mpmg_ctx *ctx, const double *m, const double *v, const doubl
     if (mat == MPMG_G_NONLOCAL_MU2) {
         // the fluidity solve: FP64 nodal mass (unknown mask), nodal fluidity,
         // element blocks and Krylov vectors, and the per-particle G2P values
-        if ((rc = dalloc(&s->nl_E, n)) != MPMG_OK) return rc;
+        if ((rc = dalloc(&s->nl_T, n)) != MPMG_OK) return rc;
         if ((rc = dalloc(&s->nl_F, n)) != MPMG_OK) return rc;
         if ((rc = dalloc(&ctx->node_m, ctx->nn)) != MPMG_OK) return rc;
         if ((rc = dalloc(&ctx->node_gf, ctx->nn)) != MPMG_OK) return rc;
@@ -1568,7 +1573,7 @@ void mpmg_mixed_free(mpmg_ctx *ctx)
     cudaFree(s->node4);
     cudaFree(s->node_mass);
     cudaFree(s->export_buf);
-    cudaFree(s->nl_E);
+    cudaFree(s->nl_T);
     cudaFree(s->nl_F);
     delete s;
     ctx->mixed = nullptr;
@@ -1650,19 +1655,19 @@ int mpmg_mixed_step(mpmg_ctx *ctx)
     MPMG_CHECK(mpmg_launch_pdl(true, g2p_variant(c.material, batch, s->g2p_tile), dim3(s->g2p_blocks),
                                dim3(s->g2p_tile), g2p_smem_size(s->g2p_tile), st, m0, bv, ne, n, (const uint32_t *)ctx->bin.rank, S, D,
                                (const int *)cell_array(ctx, cur), cell_array(ctx, nxt), (const float4 *)s->node4,
-                               ctx->bin.counts, ctx->d_params, ctx->d_status, NLOut{s->nl_E, s->nl_F}));
+                               ctx->bin.counts, ctx->d_params, ctx->d_status, NLOut{s->nl_T, s->nl_F}));
     mpmg_phase_end(ctx, PH_G2P);
     ctx->launches += batch ? 3 : 2;
     if (nonlocal) {
         // the fluidity solve (FP64 Krylov) and the stress update
         mpmg_phase_begin(ctx, PH_FLUIDITY);
         mx_assemble_kernel<<<blocks_for(ctx->ne, 128), 128, 0, st>>>(
-            ne, m0.g.inv_hf, ctx->cell_start, ctx->perm, S.A, NLOut{s->nl_E, s->nl_F}, ctx->elem_k, ctx->elem_f);
+            ne, m0.g.inv_hf, ctx->cell_start, ctx->perm, S.A, NLOut{s->nl_T, s->nl_F}, ctx->elem_k, ctx->elem_f);
         rc = mpmg_launch_solve(ctx);
         if (rc != MPMG_OK) return rc;
         mx_fluidity_stress_kernel<<<blocks_for(n, 256), 256, 0, st>>>(m0.g, m0.mat, n, S, D, ctx->bin.rank,
                                                                       cell_array(ctx, cur), ctx->node_gf,
-                                                                      NLOut{s->nl_E, s->nl_F});
+                                                                      NLOut{s->nl_T, s->nl_F});
         mpmg_phase_end(ctx, PH_FLUIDITY);
         ctx->launches += 2;
     }

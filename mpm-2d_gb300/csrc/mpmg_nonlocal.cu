@@ -1953,27 +1953,29 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
 // Nodal fluidity back to the particles, then the stress update
 // (g_nonlocal_mu2.c:545-564 and :160-218; g_nonlocal.c:559-578, :154-298).
 // AVG: the element average of the four nodal values instead of the shape
-// functions (g_nonlocal_avg.c:575-578).
+// functions (g_nonlocal_avg.c:575-578). MU2 reads the trial stress the G2P
+// kept (trial: p_d, t0xx, t0xy, t0yy, tau, value-major) in place of the
+// strain rates.
 template <bool MU2, bool AVG>
 __global__ void __launch_bounds__(256) fluidity_stress_kernel(
     int n, int Nx, int Ex, mat::Elastic el, mat::NonlocalParams np, const StepParams *__restrict__ sp,
     const int *__restrict__ active, const int *__restrict__ in_element, const double *__restrict__ xl,
     const double *__restrict__ yl, const double *__restrict__ node_gf, const double *__restrict__ exx,
     const double *__restrict__ exy, const double *__restrict__ eyy, const double *__restrict__ wxy,
-    const double *__restrict__ dense, double *__restrict__ gf, double *__restrict__ sxx,
+    const double *__restrict__ trial, double *__restrict__ gf, double *__restrict__ sxx,
     double *__restrict__ sxy, double *__restrict__ syy, double *__restrict__ gammap,
     double *__restrict__ gammadotp)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const bool act = active[i] != 0;
+    double g = 0;
     if (act) {
         const int e = in_element[i];
         const int ci = e % Ex, cj = e / Ex;
         const int n0 = cj * Nx + ci;
         const double a = xl[i], b = yl[i];
         const double ox = 1 - a, oy = 1 - b;
-        double g = 0;
         if (AVG) {
             g += 0.25 * node_gf[n0];
             g += 0.25 * node_gf[n0 + 1];
@@ -1989,8 +1991,16 @@ __global__ void __launch_bounds__(256) fluidity_stress_kernel(
     }
     if (MU2) {
         if (!act) return;
-        double s0 = sxx[i], s1 = sxy[i], s2 = syy[i], gp = gammap[i], gdp;
-        mat::nonlocal_mu2_stress(el, dense[i], gf[i], exx[i], exy[i], eyy[i], wxy[i], s0, s1, s2, gp, gdp);
+        const size_t N = (size_t)n;
+        const double p_d = trial[i];
+        double s0 = 0, s1 = 0, s2 = 0, gp = gammap[i], gdp;
+        if (p_d != p_d) {   // NaN trial pressure: the start-of-step stress stays
+            s0 = sxx[i];
+            s1 = sxy[i];
+            s2 = syy[i];
+        }
+        mat::nonlocal_mu2_stress(el, g, p_d, trial[N + i], trial[2 * N + i], trial[3 * N + i],
+                                 trial[4 * N + i], s0, s1, s2, gp, gdp);
         sxx[i] = s0;
         sxy[i] = s1;
         syy[i] = s2;
@@ -2313,7 +2323,7 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
     if (mu2) {
         fluidity_stress_kernel<true, false><<<blocks_for(n, 256), 256, 0, s>>>(
             n, c.Nx, ctx->Ex, el, np, ctx->d_params, ctx->active, ctx->in_element, ctx->xl, ctx->yl,
-            ctx->node_gf, ctx->exx, ctx->exy, ctx->eyy, ctx->wxy, ctx->state[0], ctx->state[3], ctx->sxx,
+            ctx->node_gf, ctx->exx, ctx->exy, ctx->eyy, ctx->wxy, ctx->nl_trial, ctx->state[3], ctx->sxx,
             ctx->sxy, ctx->syy, ctx->state[9], ctx->state[10]);
     } else {
         auto k = c.material == MPMG_G_NONLOCAL_AVG ? fluidity_stress_kernel<false, true>

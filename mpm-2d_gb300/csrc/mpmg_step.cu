@@ -255,6 +255,9 @@ struct G2PArgs {
     double *sxx, *sxy, *syy, *Tzz;
     double *st0, *st1, *st3, *st4, *st5, *st6, *st9, *st10;
     double *ax, *ay, *exx, *exy, *eyy, *wxy, *xl_out, *yl_out;
+    // g_nonlocal_mu2: the trial stress the stress update reads after the
+    // fluidity solve, 5 per particle, value-major (p_d, t0xx, t0xy, t0yy, tau)
+    double *trial;
 };
 
 // G2P phases.  USL (process_usl.c:465-592) runs them all in one pass; MUSL
@@ -410,12 +413,19 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
         A.st0[i] = mu_t;
         A.st4[i] = gfl;
     } else if (MATERIAL == MPMG_G_NONLOCAL_MU2) {
-        double dense, gfl, xisq;
-        mat::nonlocal_mu2_bulk(A.el, A.mu2, A.m[i], vol, exx, exy, eyy, wxy, A.sxx[i], A.sxy[i],
-                               A.syy[i], dense, gfl, xisq);
+        double p_tr, t0xx, t0xy, t0yy, tau_tr, dense, gfl, xisq;
+        mat::nonlocal_mu2_trial(A.el, exx, exy, eyy, wxy, A.sxx[i], A.sxy[i], A.syy[i], p_tr, t0xx, t0xy,
+                                t0yy, tau_tr);
+        mat::nonlocal_mu2_bulk(A.el, A.mu2, A.m[i], vol, p_tr, tau_tr, dense, gfl, xisq);
         A.st0[i] = dense;
         A.st5[i] = gfl;
         A.st6[i] = xisq;
+        const size_t n = (size_t)A.n;
+        A.trial[i] = dense != 0 ? p_tr : 0.0;
+        A.trial[n + i] = t0xx;
+        A.trial[2 * n + i] = t0xy;
+        A.trial[3 * n + i] = t0yy;
+        A.trial[4 * n + i] = tau_tr;
     }
     // MPMG_G_NONLOCAL computes its bulk fluidity over every particle in the
     // fluidity phase (g_nonlocal.c:306-352).
@@ -656,6 +666,7 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.ax = ctx->ax; A.ay = ctx->ay;
     A.exx = ctx->exx; A.exy = ctx->exy; A.eyy = ctx->eyy; A.wxy = ctx->wxy;
     A.xl_out = ctx->xl; A.yl_out = ctx->yl;
+    A.trial = ctx->nl_trial;
     return A;
 }
 
