@@ -41,7 +41,8 @@ struct MgPlan {
     int Lg;                // first level held by block 0 (levels Lg .. L - 1)
     int sm_zf0, sm_vec, sm_fp64;   // shared memory (floats): level 0's own V-cycle
                                    // results; the held levels' vectors (also the
-                                   // reduction scratch); the FP64 region
+                                   // reduction scratch and the staging area of the
+                                   // spread phases); the FP64 region
     MgLevel lv[kMgMaxLevels];
     float *coef;           // [9][total]: 9-point rows, q = 3 (dj + 1) + (di + 1)
     float *rsum;           // [total]: row sums
@@ -992,7 +993,7 @@ __device__ __forceinline__ bool mg_give_up(long long polls, int *status)
 }
 
 // Waits until every word of v carries `tag` (addr(t, q) is the address of
-// word q of trip t).  Called by whole warps.  While some lane holds stale
+// word q of trip t, for T trips of Q words).  Called by whole warps.  While some lane holds stale
 // words, one lane polls one of them and the warp sleeps kMgNap ns after a
 // stale answer; once that word is current, every lane loads its stale words
 // again together.  A phase so waits a round trip or two after its last
@@ -1000,17 +1001,16 @@ __device__ __forceinline__ bool mg_give_up(long long polls, int *status)
 // slows the stores it waits for) nor takes many issue slots from the warps
 // that compute.  Bounded (kMgPollLimit polls, or another block's timeout):
 // then the spin error is set and the words read 0.
-template <class Addr>
-__device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9], unsigned tag, int *status,
-                                           Addr addr)
+template <int T, int Q, class Addr>
+__device__ __forceinline__ void mg_resolve(unsigned long long (&v)[T][Q], unsigned tag, int *status, Addr addr)
 {
     const unsigned lane = threadIdx.x & 31u;
     for (long long polls = 1;; polls++) {
         int ft = -1, fq = 0;
 #pragma unroll
-        for (int t = kMgTrips - 1; t >= 0; t--) {
+        for (int t = T - 1; t >= 0; t--) {
 #pragma unroll
-            for (int q = 8; q >= 0; q--) {
+            for (int q = Q - 1; q >= 0; q--) {
                 if ((unsigned)(v[t][q] >> 32) != tag) {
                     ft = t;
                     fq = q;
@@ -1021,9 +1021,9 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
         if (stale == 0) return;
         if (mg_give_up(polls, status)) {
 #pragma unroll
-            for (int t = 0; t < kMgTrips; t++) {
+            for (int t = 0; t < T; t++) {
 #pragma unroll
-                for (int q = 0; q < 9; q++) v[t][q] = mg_zero(tag);
+                for (int q = 0; q < Q; q++) v[t][q] = mg_zero(tag);
             }
             return;
         }
@@ -1035,13 +1035,43 @@ __device__ __forceinline__ void mg_resolve(unsigned long long (&v)[kMgTrips][9],
             continue;
         }
 #pragma unroll
-        for (int t = 0; t < kMgTrips; t++) {
+        for (int t = 0; t < T; t++) {
 #pragma unroll
-            for (int q = 0; q < 9; q++) {
+            for (int q = 0; q < Q; q++) {
                 if ((unsigned)(v[t][q] >> 32) != tag) v[t][q] = mg_ld(addr(t, q));
             }
         }
     }
+}
+
+// Copies the words of two node ranges of a level vector (nn nodes), [a0, a1)
+// to d0 and [b0, b1) to d1, as floats once they carry `tag`; nodes outside
+// the level read 0.  Called by the whole block; ends with a block barrier.
+__device__ __forceinline__ void mg_stage(const unsigned long long *w, int nn, int a0, int a1, float *d0, int b0,
+                                         int b1, float *d1, unsigned tag, int *status)
+{
+    constexpr int T = 4;
+    const int na = max(a1 - a0, 0), nt = na + max(b1 - b0, 0);
+    for (int base = 0; base < nt; base += T * kMgThreads) {
+        unsigned long long v[T][1];
+#pragma unroll
+        for (int t = 0; t < T; t++) {
+            const int u = base + threadIdx.x + t * kMgThreads;
+            const int m = u < na ? a0 + u : b0 + (u - na);
+            v[t][0] = (u < nt && m >= 0 && m < nn) ? mg_ld(w + m) : mg_zero(tag);
+        }
+        mg_resolve(v, tag, status, [&](int t, int) {
+            const int u = base + threadIdx.x + t * kMgThreads;
+            return w + (u < na ? a0 + u : b0 + (u - na));
+        });
+#pragma unroll
+        for (int t = 0; t < T; t++) {
+            const int u = base + threadIdx.x + t * kMgThreads;
+            if (u < na) d0[u] = mg_f(v[t][0]);
+            else if (u < nt) d1[u - na] = mg_f(v[t][0]);
+        }
+    }
+    __syncthreads();
 }
 
 // Per-level arrays in shared memory (floats).  A level spread over the
@@ -1088,6 +1118,27 @@ __device__ __forceinline__ int mg_parents(int g, int coarsened, int &p0, int &p1
     p0 = g >> 1;
     p1 = (g + 1) >> 1;
     return (g & 1) ? 2 : 1;
+}
+
+// Rows fa .. fb of the finer level F under the coarse nodes [c0, c0 + cnt)
+// of level lv (their restriction support).
+__host__ __device__ inline void mg_fine_rows(const MgLevel &lv, const MgLevel &F, int c0, int cnt, int &fa, int &fb)
+{
+    const int cja = c0 / lv.Nx, cjb = (c0 + cnt - 1) / lv.Nx;
+    fa = lv.cy ? (2 * cja - 1 > 0 ? 2 * cja - 1 : 0) : cja;
+    fb = lv.cy ? (2 * cjb + 1 < F.Ny - 1 ? 2 * cjb + 1 : F.Ny - 1) : cjb;
+}
+
+// Rows ya .. yb of the coarser level Cl holding the parents of the nodes
+// n0 - H .. n0 + cnt + H of level lv (H = lv.Nx + 1, clipped to the level).
+__host__ __device__ inline void mg_parent_rows(const MgLevel &lv, const MgLevel &Cl, int n0, int cnt, int &ya,
+                                               int &yb)
+{
+    const int H = lv.Nx + 1;
+    const int lo = n0 - H > 0 ? n0 - H : 0, hi = n0 + cnt + H < lv.nn ? n0 + cnt + H : lv.nn;
+    const int ja = lo / lv.Nx, jb = (hi - 1) / lv.Nx;
+    ya = Cl.cy ? ja >> 1 : ja;
+    yb = Cl.cy ? (jb + 1) >> 1 : jb;
 }
 
 // Fine coordinate of support slot s (0, 1, 2) of coarse coordinate c, or -1.
@@ -1259,54 +1310,76 @@ __device__ __forceinline__ void mg_totals4(const double *partials, int nblocks, 
     __syncthreads();
 }
 
-// Residual phase of level l: res = b - A z1 (z1 of the neighbours from the
-// tagged words), kept in shared memory and published.
-__device__ __forceinline__ void mg_residual(const MgPlan &P, const float *sm, int l, const MgShared &S, unsigned tag,
+// The phases of a level spread over the blocks.  Block b owns the nodes
+// [b C, b C + C) of the level, whose b, z1 and res stay in its shared memory.
+// A phase copies the words it needs from other blocks (the halo of Nx + 1
+// nodes on either side of the range, or the band of rows a restriction or
+// prolongation reads) into the staging area once, then runs its stencil from
+// shared memory.  Entries of the rows towards nodes outside the grid are
+// zero, so a stencil that wraps around a row end reads a finite value it
+// multiplies by zero.
+
+// Residual phase of level l: res = b - A z1, kept in shared memory and
+// published.
+__device__ __forceinline__ void mg_residual(const MgPlan &P, float *sm, int l, const MgShared &S, unsigned tag,
                                             int *status)
 {
     const MgLevel &lv = P.lv[l];
     const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
-    const unsigned long long *z1 = P.z1 + lv.g;
-    unsigned long long v[kMgTrips][9];
-#pragma unroll
-    for (int t = 0; t < kMgTrips; t++) {
-        const int k = threadIdx.x + t * kMgThreads;
-        const int n = n0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const int di = q % 3 - 1, dj = q / 3 - 1;
-            const bool in = k < cnt && i + di >= 0 && i + di < lv.Nx && j + dj >= 0 && j + dj < lv.Ny;
-            v[t][q] = in ? mg_ld(z1 + n + dj * lv.Nx + di) : mg_zero(tag);
-        }
-    }
-    mg_resolve(v, tag, status, [&](int t, int q) {
-        const int n = n0 + threadIdx.x + t * kMgThreads;
-        return z1 + n + (q / 3 - 1) * lv.Nx + (q % 3 - 1);
-    });
-#pragma unroll
-    for (int t = 0; t < kMgTrips; t++) {
-        const int k = threadIdx.x + t * kMgThreads;
-        if (k >= cnt) continue;
+    if (cnt <= 0) return;
+    const int H = lv.Nx + 1;
+    float *ze = sm + P.sm_vec;          // z1 at nodes n0 - H .. n0 + cnt + H
+    for (int k = threadIdx.x; k < cnt; k += kMgThreads) ze[H + k] = S.z1[k];
+    mg_stage(P.z1 + lv.g, lv.nn, n0 - H, n0, ze, n0 + cnt, n0 + cnt + H, ze + H + cnt, tag, status);
+    for (int k = threadIdx.x; k < cnt; k += kMgThreads) {
         const int n = n0 + k;
+        const float *z = ze + H + k;
         float acc = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-            // entries towards nodes outside the grid are zero and their words
-            // read 0
-            acc = fmaf(mg_coef(P, sm, l, q, k, n), mg_f(v[t][q]), acc);
-        }
+        for (int q = 0; q < 9; q++) acc = fmaf(mg_coef(P, sm, l, q, k, n), z[(q / 3 - 1) * lv.Nx + (q % 3 - 1)], acc);
         const float r = S.b[k] - acc;
         S.res[k] = r;
         mg_st(P.res + lv.g + n, r, tag);
     }
+    __syncthreads();
 }
 
-// Restriction to level c (its own nodes) from a level c - 1 spread over the
-// blocks: b = P^T res (tagged words of level c - 1), then the pre-smoothing
-// step z1 = omega D_l1^-1 b.  A spread level publishes z1; a held level (block
-// 0) keeps b and z1 in shared memory only, and at the coarsest level z1 is
-// not formed.
-__device__ __forceinline__ void mg_restrict(const MgPlan &P, const float *sm, int c, const MgShared &S, unsigned tag,
+// Restriction to the spread level c from the spread level c - 1: the fine
+// residual rows under this block's coarse nodes are staged, then
+// b = P^T res and the pre-smoothing step z1 = omega D_l1^-1 b (published).
+__device__ __forceinline__ void mg_restrict(const MgPlan &P, float *sm, int c, const MgShared &S, unsigned tag,
+                                            int *status)
+{
+    const MgLevel &F = P.lv[c - 1], &lv = P.lv[c];
+    const int c0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - c0);
+    if (cnt <= 0) return;
+    int fa, fb;
+    mg_fine_rows(lv, F, c0, cnt, fa, fb);
+    float *rf = sm + P.sm_vec;          // fine residual rows fa .. fb
+    mg_stage(P.res + F.g, F.nn, fa * F.Nx, (fb + 1) * F.Nx, rf, 0, 0, rf, tag, status);
+    for (int k = threadIdx.x; k < cnt; k += kMgThreads) {
+        const int I = c0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
+        float b = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+            const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
+            if (fx < 0 || fx >= F.Nx || fy < 0 || fy >= F.Ny) continue;
+            const float w = ((q % 3 == 1) ? 1.0f : 0.5f) * ((q / 3 == 1) ? 1.0f : 0.5f);
+            b = fmaf(w, rf[(fy - fa) * F.Nx + fx], b);
+        }
+        S.b[k] = b;
+        const float z = kMgOmega * mg_l1inv(P, sm, c, k, I) * b;
+        S.z1[k] = z;
+        mg_st(P.z1 + lv.g + I, z, tag);
+    }
+    __syncthreads();
+}
+
+// Restriction to the first level held by block 0 (c = Lg) from the spread
+// level c - 1: b = P^T res, each coarse node loading its nine fine words,
+// then the pre-smoothing step z1 = omega D_l1^-1 b, in shared memory only (at
+// the coarsest level z1 is not formed).
+__device__ __forceinline__ void mg_restrict_held(const MgPlan &P, const float *sm, int c, const MgShared &S, unsigned tag,
                                             int *status)
 {
     const MgLevel &F = P.lv[c - 1], &lv = P.lv[c];
@@ -1349,80 +1422,54 @@ __device__ __forceinline__ void mg_restrict(const MgPlan &P, const float *sm, in
     }
 }
 
-// Coarse window [x0, x1] x [y0, y1] holding the parents of fine node (i, j)
-// and of its eight neighbours (at most 3 x 3 coarse nodes).
-__device__ __forceinline__ void mg_window(const MgLevel &lv, const MgLevel &Cl, int i, int j, int &x0, int &x1,
-                                          int &y0, int &y1)
-{
-    int a, b;
-    mg_parents(max(i - 1, 0), Cl.cx, x0, a);
-    mg_parents(min(i + 1, lv.Nx - 1), Cl.cx, a, x1);
-    mg_parents(max(j - 1, 0), Cl.cy, y0, b);
-    mg_parents(min(j + 1, lv.Ny - 1), Cl.cy, b, y1);
-}
-
-// Prolongation and post-smoothing at level l from the coarse solution of
-// level l + 1: with z2 = z1 + P zc and res = b - A z1,
+// Prolongation and post-smoothing at the spread level l from the coarse
+// solution of level l + 1: with z2 = z1 + P zc and res = b - A z1,
 //   z = z2 + omega D_l1^-1 (res - A P zc)   (published; zero off the unknowns)
-__device__ __forceinline__ void mg_prolong(const MgPlan &P, const float *sm, int l, const MgShared &S, unsigned tag,
-                                           int *status)
+// The coarse rows holding the parents of the nodes n0 - H .. n0 + cnt + H
+// are staged, P zc is formed at those nodes, then the stencil runs.  zown:
+// this block's results also into shared memory (level 0), or null.
+__device__ __forceinline__ void mg_prolong(const MgPlan &P, float *sm, int l, const MgShared &S, unsigned tag,
+                                           int *status, float *zown)
 {
     const MgLevel &lv = P.lv[l], &Cl = P.lv[l + 1];
     const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
-    const unsigned long long *zc = P.zf + Cl.g;
-    unsigned long long v[kMgTrips][9];
-#pragma unroll
-    for (int t = 0; t < kMgTrips; t++) {
-        const int k = threadIdx.x + t * kMgThreads;
-        const int n = n0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
-        int x0, x1, y0, y1;
-        mg_window(lv, Cl, i, j, x0, x1, y0, y1);
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const int cx = x0 + q % 3, cy = y0 + q / 3;
-            const bool in = k < cnt && cx <= x1 && cy <= y1;
-            v[t][q] = in ? mg_ld(zc + cy * Cl.Nx + cx) : mg_zero(tag);
-        }
-    }
-    mg_resolve(v, tag, status, [&](int t, int q) {
-        const int n = n0 + threadIdx.x + t * kMgThreads, j = n / lv.Nx, i = n - j * lv.Nx;
-        int x0, x1, y0, y1;
-        mg_window(lv, Cl, i, j, x0, x1, y0, y1);
-        return zc + (y0 + q / 3) * Cl.Nx + (x0 + q % 3);
-    });
-#pragma unroll
-    for (int t = 0; t < kMgTrips; t++) {
-        const int k = threadIdx.x + t * kMgThreads;
-        if (k >= cnt) continue;
-        const int n = n0 + k, j = n / lv.Nx, i = n - j * lv.Nx;
-        int x0, x1, y0, y1;
-        mg_window(lv, Cl, i, j, x0, x1, y0, y1);
-        // the window's values (indexed by the parents' offsets, which depend
-        // on the node's parity)
-        float zv[9];
-#pragma unroll
-        for (int q = 0; q < 9; q++) zv[q] = mg_f(v[t][q]);
-        float acc = 0.0f, own = 0.0f;
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const int gx = i + q % 3 - 1, gy = j + q / 3 - 1;
-            if (gx < 0 || gx >= lv.Nx || gy < 0 || gy >= lv.Ny) continue;
+    if (cnt <= 0) return;
+    const int H = lv.Nx + 1, E = cnt + 2 * H;
+    int ya, yb;
+    mg_parent_rows(lv, Cl, n0, cnt, ya, yb);
+    float *pz = sm + P.sm_vec;          // P zc at nodes n0 - H .. n0 + cnt + H
+    float *cz = pz + E;                 // coarse rows ya .. yb
+    mg_stage(P.zf + Cl.g, Cl.nn, ya * Cl.Nx, (yb + 1) * Cl.Nx, cz, 0, 0, cz, tag, status);
+    for (int u = threadIdx.x; u < E; u += kMgThreads) {
+        const int m = n0 - H + u;
+        float v = 0.0f;
+        if (m >= 0 && m < lv.nn) {
+            const int j = m / lv.Nx, i = m - j * lv.Nx;
             int px0, px1, py0, py1;
-            const int npx = mg_parents(gx, Cl.cx, px0, px1);
-            const int npy = mg_parents(gy, Cl.cy, py0, py1);
-            const int ax = px0 - x0, ay = py0 - y0, bx = px1 - x0, by = py1 - y0;
-            float pz = zv[ay * 3 + ax];
-            if (npx == 2) pz += zv[ay * 3 + bx];
-            if (npy == 2) pz += zv[by * 3 + ax];
-            if (npx == 2 && npy == 2) pz += zv[by * 3 + bx];
-            pz *= ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
-            if (q == 4) own = pz;
-            acc = fmaf(mg_coef(P, sm, l, q, k, n), pz, acc);
+            const int npx = mg_parents(i, Cl.cx, px0, px1);
+            const int npy = mg_parents(j, Cl.cy, py0, py1);
+            const float *r0 = cz + (py0 - ya) * Cl.Nx, *r1 = cz + (py1 - ya) * Cl.Nx;
+            v = r0[px0];
+            if (npx == 2) v += r0[px1];
+            if (npy == 2) v += r1[px0];
+            if (npx == 2 && npy == 2) v += r1[px1];
+            v *= ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
         }
-        const float li = mg_l1inv(P, sm, l, k, n);
-        const float z = (li == 0.0f) ? 0.0f : S.z1[k] + own + kMgOmega * li * (S.res[k] - acc);
-        mg_st(P.zf + lv.g + n, z, tag);
+        pz[u] = v;
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += kMgThreads) {
+        const int n = n0 + k;
+        const float *p = pz + H + k;
+        float acc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc = fmaf(mg_coef(P, sm, l, q, k, n), p[(q / 3 - 1) * lv.Nx + (q % 3 - 1)], acc);
+        const float li = mg_l1inv(P, sm, l, k, n);
+        const float z = (li == 0.0f) ? 0.0f : S.z1[k] + p[0] + kMgOmega * li * (S.res[k] - acc);
+        mg_st(P.zf + lv.g + n, z, tag);
+        if (zown != nullptr) zown[k] = z;
+    }
+    __syncthreads();
 }
 
 // Phases of the levels held by block 0: shared memory only, a block barrier
@@ -1556,7 +1603,7 @@ __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsign
         if (l + 1 < Lg) mg_restrict(P, sm, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
     }
     if (blockIdx.x == 0) {
-        mg_restrict(P, sm, Lg, mg_shared(sm, P.lv[Lg]), tag, status);
+        mg_restrict_held(P, sm, Lg, mg_shared(sm, P.lv[Lg]), tag, status);
         __syncthreads();
         for (int l = Lg; l + 1 < L; l++) {
             const MgHeld H = mg_held(sm, P.lv[l]);
@@ -1576,8 +1623,10 @@ __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsign
         for (int l = L - 2; l >= Lg; l--) mgh_prolong(mg_held(sm, P.lv[l]), mg_held(sm, P.lv[l + 1]), P.lv[l + 1]);
         const MgHeld H = mg_held(sm, P.lv[Lg]);
         for (int n = threadIdx.x; n < H.nn; n += blockDim.x) mg_st(P.zf + P.lv[Lg].g + n, H.zf[n], tag);
+        __syncthreads();      // the staging area of the spread phases aliases the held vectors
     }
-    for (int l = Lg - 1; l >= 0; l--) mg_prolong(P, sm, l, mg_shared(sm, P.lv[l]), tag, status);
+    for (int l = Lg - 1; l >= 0; l--)
+        mg_prolong(P, sm, l, mg_shared(sm, P.lv[l]), tag, status, l == 0 ? sm + P.sm_zf0 : nullptr);
 }
 
 // Shared memory of pcg_mg_kernel (the offsets are in the plan): level 0's
@@ -1847,28 +1896,17 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
         const unsigned tag = tag0 + (unsigned)v;
         mg_vcycle(P, sm, cinv, tag, S.status);
         {
-            const unsigned long long *zf = P.zf;
-            const float *zh = sm + P.lv[0].smv + 3 * P.lv[0].C;   // a held level 0's zf
+            // the V-cycle's result at this block's nodes and their halo of
+            // Nx + 1 nodes on either side: a held level 0's zf, or this
+            // block's own results (zf0) and the neighbours' staged words
             const bool held0 = P.Lg == 0;
-            unsigned long long wv[kMgTrips][9];
-#pragma unroll
-            for (int t = 0; t < kMgTrips; t++) {
-                const int k = threadIdx.x + t * kMgThreads;
-                const int n = n0 + k, j = n / Nx, i = n - j * Nx;
-#pragma unroll
-                for (int q = 0; q < 9; q++) {
-                    const int di = q % 3 - 1, dj = q / 3 - 1;
-                    const bool in = k < cnt && i + di >= 0 && i + di < Nx && j + dj >= 0 && j + dj < Ny;
-                    const int m = n + dj * Nx + di;
-                    wv[t][q] = !in ? mg_zero(tag)
-                                   : held0 ? (((unsigned long long)tag << 32) | __float_as_uint(zh[m]))
-                                           : mg_ld(zf + m);
-                }
+            const int H = Nx + 1;
+            const float *zh = sm + P.lv[0].smv + 3 * P.lv[0].C;
+            float *st = sm + P.sm_vec;      // zf at nodes n0 - H .. n0 + cnt + H
+            if (!held0 && cnt > 0) {
+                for (int k = threadIdx.x; k < cnt; k += kMgThreads) st[H + k] = zf0[k];
+                mg_stage(P.zf, nn, n0 - H, n0, st, n0 + cnt, n0 + cnt + H, st + H + cnt, tag, S.status);
             }
-            mg_resolve(wv, tag, S.status, [&](int t, int q) {
-                const int n = n0 + threadIdx.x + t * kMgThreads;
-                return zf + n + (q / 3 - 1) * Nx + (q % 3 - 1);
-            });
             part[0] = part[1] = part[2] = part[3] = 0;
 #pragma unroll
             for (int t = 0; t < kMgTrips; t++) {
@@ -1878,11 +1916,13 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
                 double az = 0;
 #pragma unroll
                 for (int q = 0; q < 9; q++) {
-                    // rows are zero towards nodes outside the grid, whose
-                    // words read 0
-                    az = fma(S.coef[(size_t)q * nn + n], (double)mg_f(wv[t][q]), az);
+                    // rows are zero towards nodes outside the grid (a held
+                    // level 0 reads no node outside the level)
+                    const int d = (q / 3 - 1) * Nx + (q % 3 - 1), m = n + d;
+                    const float zq = !held0 ? st[H + k + d] : (m < 0 || m >= nn) ? 0.0f : zh[m];
+                    az = fma(S.coef[(size_t)q * nn + n], (double)zq, az);
                 }
-                const float zo = mg_f(wv[t][4]);
+                const float zo = held0 ? zh[n] : st[H + k];
                 const double uk = sig * (double)zo, wk = sig * az, rk = r[k];
                 zf0[k] = zo;
                 w[k] = wk;
@@ -2144,7 +2184,29 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
                 vec += 4 * P.lv[l].nn;
             }
             const int scratch = 2 * (4 * kMgThreads + 4);   // the reduction scratch (doubles) aliases them
-            off += vec > scratch ? vec : scratch;
+            // so does the staging area of the spread phases: a level's range
+            // and its halo, with the coarse rows of a prolongation, or the
+            // fine rows of a restriction
+            int ext = 0;
+            for (int b = 0; b < nb; b++) {
+                for (int l = 0; l < P.Lg; l++) {
+                    const MgLevel &lv = P.lv[l];
+                    const int n0 = b * lv.C, cnt = lv.nn - n0 < lv.C ? lv.nn - n0 : lv.C;
+                    if (cnt <= 0) continue;
+                    int ya, yb, fa, fb;
+                    mg_parent_rows(lv, P.lv[l + 1], n0, cnt, ya, yb);
+                    const int pro = cnt + 2 * (lv.Nx + 1) + (yb - ya + 1) * P.lv[l + 1].Nx;
+                    if (pro > ext) ext = pro;
+                    if (l >= 1) {
+                        mg_fine_rows(lv, P.lv[l - 1], n0, cnt, fa, fb);
+                        const int res = (fb - fa + 1) * P.lv[l - 1].Nx;
+                        if (res > ext) ext = res;
+                    }
+                }
+            }
+            int region = vec > scratch ? vec : scratch;
+            if (ext > region) region = ext;
+            off += region;
             P.sm_fp64 = (off + 1) & ~1;
         }
         const size_t smem = ok ? pcg_mg_smem(P) : 0;
