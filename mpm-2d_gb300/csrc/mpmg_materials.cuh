@@ -87,6 +87,7 @@ struct Mu2Params {
     double inv_grains_rho, inv_grains_d;   // RN(1/grains_rho), RN(1/grains_d)
     double rho_lo, rho_hi;                 // RN(rho_critical (1 - 2^-47)), RN(rho_critical (1 + 2^-47))
     double AAdd, inv_AAdd;                 // RN(RN(RN(A A) d) d) and its reciprocal
+    double alpha_c;                        // G I0 dt / (grains_d sqrt(grains_rho))
 };
 
 // RN(m / v) < rho_critical, decided as the reference's division and compare
@@ -464,32 +465,36 @@ __device__ __forceinline__ void nonlocal_mu2_trial(const Elastic &el, double exx
 // calculate_bulk_granular_fluidity, g_nonlocal_mu2.c:238-321, for one
 // particle, from its trial pressure and shear stress (nonlocal_mu2_trial):
 // dense flag, local fluidity and the inverse squared cooperativity length.
+// The dense flag and the branches are the reference's decisions on the same
+// values.  The flowing branch is the same algebra in fewer FP64 operations
+// (these values feed the iterative fluidity solve, not a bit-exact output):
+//   alpha    = G I0 dt sqrt(p / rho) / d  = alpha_c sqrt(p)
+//   tau_tau  = the negative root of t^2 - B t + H, B = S2 + tau + alpha > 0,
+//              as 2 H / (B + sqrt(B^2 - 4 H)) (negative_root's b < 0 branch)
+//   gf_local = (p / (G dt)) (tau / tau_tau - 1) = p (tau - tau_tau) / (G dt tau_tau)
+// and below yield (scale factor 1) gf_local is +0.
 __device__ __forceinline__ void nonlocal_mu2_bulk(const Elastic &el, const Mu2Params &mp, double m,
                                                   double v, double p_tr, double tau_tr, double &dense,
                                                   double &gf_local, double &xisq_inv)
 {
-    const double G = el.G, dt = el.dt;
     dense = (below_density(m, v, mp) || p_tr < 0) ? 0.0 : 1.0;
     if (dense == 0 || p_tr <= 0) {
         gf_local = 0;
         xisq_inv = 0;
     } else if (p_tr > 0) {
-        double tau_tau, scale_factor;
+        double tau_tau;
         double S0 = mul(mp.mu_s, p_tr);
         if (tau_tr <= S0) {
             tau_tau = tau_tr;
-            scale_factor = 1.0;
+            gf_local = 0;
         } else {
             double S2 = mul(mp.mu_2, p_tr);
-            double alpha = dvd_known(mul(mul(mul(G, mp.I0), dt),
-                                         __dsqrt_rn(dvd_known(p_tr, mp.grains_rho, mp.inv_grains_rho))),
-                                     mp.grains_d, mp.inv_grains_d);
-            double B = -add(add(S2, tau_tr), alpha);
+            double alpha = mul(mp.alpha_c, __dsqrt_rn(p_tr));
+            double B = add(add(S2, tau_tr), alpha);
             double H = add(mul(S2, tau_tr), mul(S0, alpha));
-            tau_tau = negative_root(1.0, B, H);
-            scale_factor = dvd(tau_tau, tau_tr);
+            tau_tau = dvd(add(H, H), add(B, __dsqrt_rn(sub(mul(B, B), mul(4.0, H)))));
+            gf_local = dvd(mul(p_tr, sub(tau_tr, tau_tau)), mul(el.Gdt, tau_tau));
         }
-        gf_local = mul(dvd_known(p_tr, el.Gdt, el.inv_Gdt), sub(dvd(1.0, scale_factor), 1.0));
         xisq_inv = dvd_known(fabs(sub(dvd(tau_tau, p_tr), mp.mu_s)), mp.AAdd, mp.inv_AAdd);
     } else {
         gf_local = 0;

@@ -644,6 +644,7 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.mu2.rho_hi = A.mu2.rho_critical * (1.0 + 0x1p-47);
     A.mu2.AAdd = ((A.mu2.A * A.mu2.A) * A.mu2.grains_d) * A.mu2.grains_d;
     A.mu2.inv_AAdd = 1.0 / A.mu2.AAdd;
+    A.mu2.alpha_c = (((ctx->G * A.mu2.I0) * c.dt) / A.mu2.grains_d) / sqrt(A.mu2.grains_rho);
     A.nl.E = c.mp[MPMG_MP_E];
     A.nl.nu = c.mp[MPMG_MP_NU];
     A.nl.mu_s = c.mp[MPMG_MP_MU_S];
