@@ -1376,50 +1376,33 @@ __device__ __forceinline__ void mg_restrict(const MgPlan &P, float *sm, int c, c
 }
 
 // Restriction to the first level held by block 0 (c = Lg) from the spread
-// level c - 1: b = P^T res, each coarse node loading its nine fine words,
-// then the pre-smoothing step z1 = omega D_l1^-1 b, in shared memory only (at
-// the coarsest level z1 is not formed).
-__device__ __forceinline__ void mg_restrict_held(const MgPlan &P, const float *sm, int c, const MgShared &S, unsigned tag,
-                                            int *status)
+// level c - 1, by all blocks: block b forms b = P^T res at the coarse nodes
+// [b Ch, b Ch + Ch) (Ch = ceil(nn / blocks)) from the staged fine residual
+// rows under them, and publishes it in the held level's z1 words (which a
+// held level does not otherwise use).  Block 0 then stages the whole level.
+__device__ __forceinline__ void mg_restrict_to_held(const MgPlan &P, float *sm, int c, unsigned tag, int *status)
 {
     const MgLevel &F = P.lv[c - 1], &lv = P.lv[c];
-    const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
-    const unsigned long long *res = P.res + F.g;
-    unsigned long long v[kMgTrips][9];
-#pragma unroll
-    for (int t = 0; t < kMgTrips; t++) {
-        const int k = threadIdx.x + t * kMgThreads;
-        const int I = n0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-            const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
-            const bool in = k < cnt && fx >= 0 && fx < F.Nx && fy >= 0 && fy < F.Ny;
-            v[t][q] = in ? mg_ld(res + fy * F.Nx + fx) : mg_zero(tag);
-        }
-    }
-    mg_resolve(v, tag, status, [&](int t, int q) {
-        const int I = n0 + threadIdx.x + t * kMgThreads, cj = I / lv.Nx, ci = I - cj * lv.Nx;
-        return res + mg_fine_of(cj, q / 3, lv.cy) * F.Nx + mg_fine_of(ci, q % 3, lv.cx);
-    });
-    const bool coarsest = c == P.L - 1;
-#pragma unroll
-    for (int t = 0; t < kMgTrips; t++) {
-        const int k = threadIdx.x + t * kMgThreads;
-        if (k >= cnt) continue;
-        const int I = n0 + k;
+    const int Ch = (lv.nn + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int c0 = blockIdx.x * Ch, cnt = min(Ch, lv.nn - c0);
+    if (cnt <= 0) return;
+    int fa, fb;
+    mg_fine_rows(lv, F, c0, cnt, fa, fb);
+    float *rf = sm + P.sm_vec;          // fine residual rows fa .. fb
+    mg_stage(P.res + F.g, F.nn, fa * F.Nx, (fb + 1) * F.Nx, rf, 0, 0, rf, tag, status);
+    for (int k = threadIdx.x; k < cnt; k += kMgThreads) {
+        const int I = c0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
         float b = 0.0f;
 #pragma unroll
         for (int q = 0; q < 9; q++) {
+            const int fx = mg_fine_of(ci, q % 3, lv.cx), fy = mg_fine_of(cj, q / 3, lv.cy);
+            if (fx < 0 || fx >= F.Nx || fy < 0 || fy >= F.Ny) continue;
             const float w = ((q % 3 == 1) ? 1.0f : 0.5f) * ((q / 3 == 1) ? 1.0f : 0.5f);
-            b = fmaf(w, mg_f(v[t][q]), b);      // words outside the support read 0
+            b = fmaf(w, rf[(fy - fa) * F.Nx + fx], b);
         }
-        S.b[k] = b;
-        if (!coarsest) {
-            const float z = kMgOmega * mg_l1inv(P, sm, c, k, I) * b;
-            S.z1[k] = z;
-            if (!lv.local) mg_st(P.z1 + lv.g + I, z, tag);
-        }
+        mg_st(P.z1 + lv.g + I, b, tag);
     }
+    __syncthreads();
 }
 
 // Prolongation and post-smoothing at the spread level l from the coarse
@@ -1533,29 +1516,35 @@ __device__ __forceinline__ void mgh_restrict(const MgHeld &F, const MgHeld &H, c
 }
 
 // Prolongation and post-smoothing on a held level from the coarser held
-// level C (its zf): z = z1 + P zc + omega D_l1^-1 (res - A P zc).
+// level C (its zf): z = z1 + P zc + omega D_l1^-1 (res - A P zc).  P zc is
+// formed once a node, into b (not needed after the level's residual), then
+// the stencil reads it.
 __device__ __forceinline__ void mgh_prolong(const MgHeld &H, const MgHeld &Cz, const MgLevel &Cl)
 {
     for (int n = threadIdx.x; n < H.nn; n += blockDim.x) {
         const int j = n / H.Nx, i = n - j * H.Nx;
-        float acc = 0.0f, own = 0.0f;
+        int px0, px1, py0, py1;
+        const int npx = mg_parents(i, Cl.cx, px0, px1);
+        const int npy = mg_parents(j, Cl.cy, py0, py1);
+        const float *r0 = Cz.zf + py0 * Cz.Nx, *r1 = Cz.zf + py1 * Cz.Nx;
+        float pz = r0[px0];
+        if (npx == 2) pz += r0[px1];
+        if (npy == 2) pz += r1[px0];
+        if (npx == 2 && npy == 2) pz += r1[px1];
+        H.b[n] = pz * (((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f));
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < H.nn; n += blockDim.x) {
+        const int j = n / H.Nx, i = n - j * H.Nx;
+        float acc = 0.0f;
 #pragma unroll
         for (int q = 0; q < 9; q++) {
-            const int gx = i + q % 3 - 1, gy = j + q / 3 - 1;
-            if (gx < 0 || gx >= H.Nx || gy < 0 || gy >= H.Ny) continue;
-            int px0, px1, py0, py1;
-            const int npx = mg_parents(gx, Cl.cx, px0, px1);
-            const int npy = mg_parents(gy, Cl.cy, py0, py1);
-            float pz = Cz.zf[py0 * Cz.Nx + px0];
-            if (npx == 2) pz += Cz.zf[py0 * Cz.Nx + px1];
-            if (npy == 2) pz += Cz.zf[py1 * Cz.Nx + px0];
-            if (npx == 2 && npy == 2) pz += Cz.zf[py1 * Cz.Nx + px1];
-            pz *= ((npx == 2) ? 0.5f : 1.0f) * ((npy == 2) ? 0.5f : 1.0f);
-            if (q == 4) own = pz;
-            acc = fmaf(H.coef[q * H.nn + n], pz, acc);
+            const int di = q % 3 - 1, dj = q / 3 - 1;
+            if (i + di < 0 || i + di >= H.Nx || j + dj < 0 || j + dj >= H.Ny) continue;
+            acc = fmaf(H.coef[q * H.nn + n], H.b[n + dj * H.Nx + di], acc);
         }
         const float li = H.l1inv[n];
-        H.zf[n] = (li == 0.0f) ? 0.0f : H.z1[n] + own + kMgOmega * li * (H.res[n] - acc);
+        H.zf[n] = (li == 0.0f) ? 0.0f : H.z1[n] + H.b[n] + kMgOmega * li * (H.res[n] - acc);
     }
     __syncthreads();
 }
@@ -1602,9 +1591,18 @@ __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsign
         mg_residual(P, sm, l, mg_shared(sm, P.lv[l]), tag, status);
         if (l + 1 < Lg) mg_restrict(P, sm, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
     }
+    mg_restrict_to_held(P, sm, Lg, tag, status);
     if (blockIdx.x == 0) {
-        mg_restrict_held(P, sm, Lg, mg_shared(sm, P.lv[Lg]), tag, status);
-        __syncthreads();
+        {
+            // the first held level's b from every block, then its
+            // pre-smoothing step (not at the coarsest level)
+            const MgHeld H = mg_held(sm, P.lv[Lg]);
+            mg_stage(P.z1 + P.lv[Lg].g, H.nn, 0, H.nn, H.b, 0, 0, H.b, tag, status);
+            if (Lg + 1 < L) {
+                for (int n = threadIdx.x; n < H.nn; n += blockDim.x) H.z1[n] = kMgOmega * H.l1inv[n] * H.b[n];
+            }
+            __syncthreads();
+        }
         for (int l = Lg; l + 1 < L; l++) {
             const MgHeld H = mg_held(sm, P.lv[l]);
             mgh_residual(H);
@@ -2200,6 +2198,18 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
                     if (l >= 1) {
                         mg_fine_rows(lv, P.lv[l - 1], n0, cnt, fa, fb);
                         const int res = (fb - fa + 1) * P.lv[l - 1].Nx;
+                        if (res > ext) ext = res;
+                    }
+                }
+                if (P.Lg > 0 && P.Lg < L) {
+                    // the restriction to the first held level, by all blocks
+                    const MgLevel &lv = P.lv[P.Lg];
+                    const int Ch = (lv.nn + nb - 1) / nb, c0 = b * Ch;
+                    const int cnt = lv.nn - c0 < Ch ? lv.nn - c0 : Ch;
+                    if (cnt > 0) {
+                        int fa, fb;
+                        mg_fine_rows(lv, P.lv[P.Lg - 1], c0, cnt, fa, fb);
+                        const int res = (fb - fa + 1) * P.lv[P.Lg - 1].Nx;
                         if (res > ext) ext = res;
                     }
                 }
