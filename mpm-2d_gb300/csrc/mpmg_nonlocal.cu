@@ -28,6 +28,8 @@ constexpr int kMgMaxLevels = 16;
 
 struct MgLevel {
     int Nx, Ny, nn, C;
+    int b0;                // first block that owns nodes of the level (blocks b0, b0 + 1, ...
+                           // own C nodes each)
     int cx, cy;            // coarsened from the finer level along x, y (level 0: 0)
     int local;             // 1: block 0 holds the whole level (C = nn) in shared memory
     int g;                 // first node of the level in the global pools
@@ -50,6 +52,13 @@ struct MgPlan {
     unsigned long long *z1, *res, *zf;   // [total] tagged words each
     unsigned int *tag;     // tag counter
 };
+
+// Nodes [n0, n0 + cnt) of level lv owned by block b (cnt <= 0: none).
+__host__ __device__ inline void mg_own_range(const MgLevel &lv, int b, int &n0, int &cnt)
+{
+    n0 = (b - lv.b0) * lv.C;
+    cnt = b < lv.b0 ? 0 : (lv.nn - n0 < lv.C ? lv.nn - n0 : lv.C);
+}
 
 namespace {
 
@@ -79,7 +88,14 @@ __global__ void nonlocal_bulk_kernel(int n, mat::NonlocalParams np, const double
     xisq[i] = xi;
 }
 
-// Element blocks and right-hand sides (g_nonlocal_mu2.c:418-507).
+// Element blocks and right-hand sides (g_nonlocal_mu2.c:418-507): per
+// particle, v (xi^-2 s_r s_c + grad s_r . grad s_c) and v gf_local xi^-2 s_r.
+// With s = (ox oy, a oy, a b, ox b) (ox = 1 - a, oy = 1 - b), h grad s is
+// ((-oy, -ox), (oy, -a), (b, a), (-b, ox)), so every grad s_r . grad s_c h^2
+// is a combination of 1, a, a^2, b, b^2: the element sums five moments of v
+// (sum v, v a, v a^2, v b, v b^2) and forms the ten gradient entries from
+// them once, instead of per particle.  The kernel is bound by the FP64 pipe
+// (1/64 of the FP32 rate on GB300); the mass part stays per particle.
 __global__ void __launch_bounds__(128) assemble_kernel(
     int ne, int Ex, double inv_h, int dense_only, const int *__restrict__ cell_start,
     const uint32_t *__restrict__ perm, const double *__restrict__ xl, const double *__restrict__ yl,
@@ -95,27 +111,50 @@ __global__ void __launch_bounds__(128) assemble_kernel(
     for (int k = 0; k < 10; k++) K[k] = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) F[k] = 0;
+    double m0 = 0, ma = 0, maa = 0, mb = 0, mbb = 0;
     for (int k = k0; k < k1; k++) {
         const int i = (int)perm[k];
         if (dense_only && dense[i] == 0) continue;
         const double a = xl[i], b = yl[i];
         const double ox = 1 - a, oy = 1 - b;
         const double s[4] = {ox * oy, a * oy, a * b, ox * b};
-        const double gx[4] = {-oy * inv_h, oy * inv_h, b * inv_h, -b * inv_h};
-        const double gy[4] = {-ox * inv_h, -a * inv_h, a * inv_h, ox * inv_h};
-        const double vol = v[i], xi = xisq[i];
-        const double fv = vol * gfl[i] * xi;
+        const double vol = v[i], w = vol * xisq[i];
+        const double fv = w * gfl[i];
+        double ws[4];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-            F[r] += fv * s[r];
-#pragma unroll
-            for (int c = r; c < 4; c++) {
-                K[sym_index(r, c)] += vol * (xi * s[r] * s[c] + (gx[r] * gx[c] + gy[r] * gy[c]));
-            }
+            F[r] = fma(fv, s[r], F[r]);
+            ws[r] = w * s[r];
         }
-    }
 #pragma unroll
-    for (int k = 0; k < 10; k++) elem_k[(size_t)k * ne + e] = K[k];
+        for (int r = 0; r < 4; r++) {
+#pragma unroll
+            for (int c = r; c < 4; c++) K[sym_index(r, c)] = fma(ws[r], s[c], K[sym_index(r, c)]);
+        }
+        const double va = vol * a, vb = vol * b;
+        m0 += vol;
+        ma += va;
+        mb += vb;
+        maa = fma(va, a, maa);
+        mbb = fma(vb, b, mbb);
+    }
+    // sum v grad s_r . grad s_c h^2 from the moments, rows (0,0..3),
+    // (1,1..3), (2,2..3), (3,3)
+    const double g02 = (maa - ma) + (mbb - mb);
+    const double gg[10] = {
+        (2 * m0 - 2 * ma + maa) + (mbb - 2 * mb),       // oy^2 + ox^2
+        (ma - maa) - (m0 - 2 * mb + mbb),               // ox a - oy^2
+        g02,                                            // -oy b - ox a
+        (mb - mbb) - (m0 - 2 * ma + maa),               // oy b - ox^2
+        (m0 - 2 * mb + mbb) + maa,                      // oy^2 + a^2
+        (mb - mbb) - maa,                               // oy b - a^2
+        g02,                                            // -oy b - a ox
+        mbb + maa,                                      // b^2 + a^2
+        (ma - maa) - mbb,                               // ox a - b^2
+        mbb + (m0 - 2 * ma + maa)};                     // b^2 + ox^2
+    const double ih2 = inv_h * inv_h;
+#pragma unroll
+    for (int k = 0; k < 10; k++) elem_k[(size_t)k * ne + e] = fma(gg[k], ih2, K[k]);
 #pragma unroll
     for (int k = 0; k < 4; k++) elem_f[(size_t)k * ne + e] = F[k];
     (void)Ex;
@@ -1325,7 +1364,8 @@ __device__ __forceinline__ void mg_residual(const MgPlan &P, float *sm, int l, c
                                             int *status)
 {
     const MgLevel &lv = P.lv[l];
-    const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
+    int n0, cnt;
+    mg_own_range(lv, blockIdx.x, n0, cnt);
     if (cnt <= 0) return;
     const int H = lv.Nx + 1;
     float *ze = sm + P.sm_vec;          // z1 at nodes n0 - H .. n0 + cnt + H
@@ -1351,7 +1391,8 @@ __device__ __forceinline__ void mg_restrict(const MgPlan &P, float *sm, int c, c
                                             int *status)
 {
     const MgLevel &F = P.lv[c - 1], &lv = P.lv[c];
-    const int c0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - c0);
+    int c0, cnt;
+    mg_own_range(lv, blockIdx.x, c0, cnt);
     if (cnt <= 0) return;
     int fa, fb;
     mg_fine_rows(lv, F, c0, cnt, fa, fb);
@@ -1415,7 +1456,8 @@ __device__ __forceinline__ void mg_prolong(const MgPlan &P, float *sm, int l, co
                                            int *status, float *zown)
 {
     const MgLevel &lv = P.lv[l], &Cl = P.lv[l + 1];
-    const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
+    int n0, cnt;
+    mg_own_range(lv, blockIdx.x, n0, cnt);
     if (cnt <= 0) return;
     const int H = lv.Nx + 1, E = cnt + 2 * H;
     int ya, yb;
@@ -1553,10 +1595,12 @@ __device__ __forceinline__ void mgh_prolong(const MgHeld &H, const MgHeld &Cz, c
 // zf words with this tag.  Levels 0 .. Lg - 1 are spread over the blocks;
 // block 0 runs levels Lg .. L - 1 in its shared memory and publishes level
 // Lg's result for the way up.
-__device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsigned tag, int *status)
+template <class Defer>
+__device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsigned tag, int *status, Defer defer)
 {
     const int L = P.L, Lg = P.Lg;
     if (Lg == 0) {
+        defer();
         // one block holds every level
         const MgHeld H = mg_held(sm, P.lv[0]);
         for (int n = threadIdx.x; n < H.nn; n += blockDim.x) H.z1[n] = kMgOmega * H.l1inv[n] * H.b[n];
@@ -1580,7 +1624,8 @@ __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsign
         // pre-smoothing at level 0
         const MgLevel &lv = P.lv[0];
         const MgShared S = mg_shared(sm, lv);
-        const int n0 = blockIdx.x * lv.C, cnt = min(lv.C, lv.nn - n0);
+        int n0, cnt;
+        mg_own_range(lv, blockIdx.x, n0, cnt);
         for (int k = threadIdx.x; k < cnt; k += kMgThreads) {
             const float z = kMgOmega * sm[9 * lv.C + k] * S.b[k];
             S.z1[k] = z;
@@ -1592,6 +1637,9 @@ __device__ void mg_vcycle(const MgPlan &P, float *sm, const double *cinv, unsign
         if (l + 1 < Lg) mg_restrict(P, sm, l + 1, mg_shared(sm, P.lv[l + 1]), tag, status);
     }
     mg_restrict_to_held(P, sm, Lg, tag, status);
+    // work that is not on the V-cycle's path, while block 0 runs the held
+    // levels (block 0 owns no level-0 nodes, so it has none)
+    defer();
     if (blockIdx.x == 0) {
         {
             // the first held level's b from every block, then its
@@ -1652,7 +1700,8 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     const int Nx = S.Nx, Ny = S.Ny, nn = Nx * Ny;
     const int nblocks = gridDim.x;
     const MgLevel &L0 = P.lv[0];
-    const int n0 = blockIdx.x * L0.C, cnt = min(L0.C, nn - n0);
+    int n0, cnt;
+    mg_own_range(L0, blockIdx.x, n0, cnt);
     float *zf0 = sm + P.sm_zf0;                       // level 0's own V-cycle results
     double *scratch = reinterpret_cast<double *>(sm + P.sm_vec);   // 4 kMgThreads + 4 (between V-cycles)
     double *dv = reinterpret_cast<double *>(sm + P.sm_fp64);
@@ -1736,7 +1785,8 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     // level held by block 0).
     for (int c = 1; c < P.L; c++) {
         const MgLevel &lv = P.lv[c];
-        const int c0 = blockIdx.x * lv.C, ccnt = min(lv.C, lv.nn - c0);
+        int c0, ccnt;
+        mg_own_range(lv, blockIdx.x, c0, ccnt);
         for (int k = threadIdx.x; k < ccnt; k += kMgThreads) {
             const int I = c0 + k, cj = I / lv.Nx, ci = I - cj * lv.Nx;
             mg_galerkin_row(P, c, I, ci, cj, lv.local ? sm + lv.sm : nullptr);
@@ -1863,18 +1913,16 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
     __syncthreads();
     double sig_u = 0;       // u = sig_u zf0 (the last V-cycle's result)
     for (int v = 0; !converged && !failed; v++) {
+        const double sig_prev = sig_u;
         if (v > 0) {
-            // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s
+            // s = w + beta s, r -= alpha s (the V-cycle's input); p and x
+            // follow inside the V-cycle (defer below)
 #pragma unroll
             for (int t = 0; t < kMgTrips; t++) {
                 const int k = threadIdx.x + t * kMgThreads;
                 if (k >= cnt) continue;
-                const int n = n0 + k;
-                const double pk = fma(beta, S.p[n], sig_u * (double)zf0[k]);
                 const double sk = fma(beta, sv[t], w[k]);
-                S.p[n] = pk;
                 sv[t] = sk;
-                x[t] = fma(alpha, pk, x[t]);
                 r[k] = fma(-alpha, sk, r[k]);
             }
             it++;
@@ -1892,7 +1940,21 @@ __global__ void __launch_bounds__(kMgThreads, 1) pcg_mg_kernel(SolveArgs S, cons
             }
         }
         const unsigned tag = tag0 + (unsigned)v;
-        mg_vcycle(P, sm, cinv, tag, S.status);
+        // p = u + beta p, x += alpha p, with u = sig_prev zf0 (the last
+        // V-cycle's result, in zf0 until level 0's prolongation)
+        auto defer = [&]() {
+            if (v == 0) return;
+#pragma unroll
+            for (int t = 0; t < kMgTrips; t++) {
+                const int k = threadIdx.x + t * kMgThreads;
+                if (k >= cnt) continue;
+                const int n = n0 + k;
+                const double pk = fma(beta, S.p[n], sig_prev * (double)zf0[k]);
+                S.p[n] = pk;
+                x[t] = fma(alpha, pk, x[t]);
+            }
+        };
+        mg_vcycle(P, sm, cinv, tag, S.status, defer);
         {
             // the V-cycle's result at this block's nodes and their halo of
             // Nx + 1 nodes on either side: a held level 0's zf, or this
@@ -2139,7 +2201,12 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
             // on one block every level is held; otherwise level 0 is spread
             // and the coarser levels of at most kMgLocal nodes are held
             lv.local = (nb == 1 || (L > 0 && lv.nn <= kMgLocal)) ? 1 : 0;
-            lv.C = lv.local ? lv.nn : (lv.nn + nb - 1) / nb;
+            // a spread level 0 is shared by blocks 1 .. nb - 1: block 0, which
+            // runs the held levels, then has no level-0 work (the outer
+            // iteration's p and x updates of the other blocks run while it
+            // holds the V-cycle)
+            lv.b0 = (L == 0 && !lv.local) ? 1 : 0;
+            lv.C = lv.local ? lv.nn : (lv.nn + (nb - lv.b0) - 1) / (nb - lv.b0);
             lv.cx = cxs;
             lv.cy = cys;
             lv.g = total;
@@ -2189,7 +2256,8 @@ int mpmg_nonlocal_init(mpmg_ctx *ctx)
             for (int b = 0; b < nb; b++) {
                 for (int l = 0; l < P.Lg; l++) {
                     const MgLevel &lv = P.lv[l];
-                    const int n0 = b * lv.C, cnt = lv.nn - n0 < lv.C ? lv.nn - n0 : lv.C;
+                    int n0, cnt;
+                    mg_own_range(lv, b, n0, cnt);
                     if (cnt <= 0) continue;
                     int ya, yb, fa, fb;
                     mg_parent_rows(lv, P.lv[l + 1], n0, cnt, ya, yb);
