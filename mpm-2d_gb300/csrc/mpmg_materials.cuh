@@ -514,7 +514,7 @@ __device__ __forceinline__ void nonlocal_mu2_stress(const Elastic &el, double gf
                                                     double tau_tr, double &sxx, double &sxy,
                                                     double &syy, double &gammap, double &gammadotp)
 {
-    const double G = el.G, dt = el.dt;
+    const double dt = el.dt;
     const double p_tr = p_d;
     double nup_tau;
     if (p_tr <= 0) {
@@ -523,7 +523,10 @@ __device__ __forceinline__ void nonlocal_mu2_stress(const Elastic &el, double gf
     } else if (p_tr > 0) {
         double scale_factor = dvd(p_tr, add(mul(el.Gdt, gf), p_tr));
         double tau_tau = mul(tau_tr, scale_factor);
-        nup_tau = dvd_known(dvd_known(sub(tau_tr, tau_tau), G, el.inv_G), dt, el.inv_dt);
+        // ((tau - tau_tau) / G) / dt as one quotient by G dt (the fluidity
+        // comes from an iterative solve, so this value is not bit-exact
+        // with the reference's anyway)
+        nup_tau = dvd_known(sub(tau_tr, tau_tau), el.Gdt, el.inv_Gdt);
         sxx = sub(mul(scale_factor, t0xx), p_tr);
         sxy = mul(scale_factor, t0xy);
         syy = sub(mul(scale_factor, t0yy), p_tr);
