@@ -354,6 +354,19 @@ __device__ __forceinline__ double mpmg_local_coord(double xp, double xn, double 
     return xl;
 }
 
+// The same with xl = x / h - c in one FMA from the element's column (or row)
+// c (one FP64 operation in place of three; xl differs from (x - c h) / h by
+// a few ulps of x / h, about 1e-14 on a 512-element grid).
+__device__ __forceinline__ double mpmg_local_coord_fma(double xp, double c, double inv_h)
+{
+    double xl = fma(xp, inv_h, -c);
+    if ((__double_as_longlong(xl) & 0x7fffffffffffffffLL) > 0x3ff0000000000000LL) {
+        double sg = copysign(1.0, xl);
+        if (((sg * xl) - 1.0) < MPMG_TOL) xl = sg;
+    }
+    return xl;
+}
+
 // Counts one key into the bins (see BinScratch): bins[key] for keys inside
 // the grid, bins[sentinel + group] for keys outside it, where group is the
 // key's destination position / 32.  Runs of equal bins in consecutive lanes

@@ -35,6 +35,7 @@ constexpr double kThird = 1.0 / 3.0;   // RN(1/3), the reciprocal of the divisor
 
 struct Elastic {
     double G, K, lambda, dt;
+    double twoG;            // 2 G, exact
     double inv_G, inv_dt;   // RN(1/G), RN(1/dt)
     double Gdt, inv_Gdt;    // RN(G dt), RN(1 / RN(G dt))
 };
@@ -60,7 +61,7 @@ __device__ __forceinline__ double exp_small(double x)
 __device__ __forceinline__ void isolin(const Elastic &el, double exx, double exy, double eyy,
                                        double wxy, double &sxx, double &sxy, double &syy)
 {
-    const double twoG = mul(2.0, el.G);
+    const double twoG = el.twoG;
     double trD = add(exx, eyy);
     double dsjxx = add(mul(el.lambda, trD), mul(twoG, exx));
     double dsjxy = mul(twoG, exy);
@@ -88,6 +89,7 @@ struct Mu2Params {
     double rho_lo, rho_hi;                 // RN(rho_critical (1 - 2^-47)), RN(rho_critical (1 + 2^-47))
     double AAdd, inv_AAdd;                 // RN(RN(RN(A A) d) d) and its reciprocal
     double alpha_c;                        // G I0 dt / (grains_d sqrt(grains_rho))
+    double GI0dt;                          // RN(RN(G I0) dt), formed on the host
 };
 
 // RN(m / v) < rho_critical, decided as the reference's division and compare
@@ -137,7 +139,7 @@ __device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &
     double JSxy = add(mul(Wxy, Tyy), -mul(Txx, Wxy));
     double JSyy = -JSxx;
     // trial stress (:215-222)
-    const double twoG = mul(2.0, G);
+    const double twoG = el.twoG;
     double lt = mul(lambda, trD);
     double Txx_tr = add(mul(add(add(mul(Dxx, twoG), lt), JSxx), dt), Txx);
     double Txy_tr = add(mul(add(mul(Dxy, twoG), JSxy), dt), Txy);
@@ -173,7 +175,7 @@ __device__ __forceinline__ void g_local_mu2(const Elastic &el, const Mu2Params &
                 scale_factor = 1.0;
             } else {
                 double S2 = mul(mp.mu_2, p_tr);
-                double alpha = dvd_known(mul(mul(mul(G, mp.I0), dt),
+                double alpha = dvd_known(mul(mp.GI0dt,
                                              __dsqrt_rn(dvd_known(p_tr, mp.grains_rho, mp.inv_grains_rho))),
                                          mp.grains_d, mp.inv_grains_d);
                 double B = -add(add(S2, tau_tr), alpha);
@@ -218,7 +220,7 @@ __device__ __forceinline__ void plane_return(const Elastic &el, const ReturnPara
 {
     const double G = el.G, K = el.K, dt = el.dt;
     const double lambda = el.lambda;   // K - 2 G / 3, formed on the host with the same roundings
-    const double twoG = mul(2.0, G);
+    const double twoG = el.twoG;
     double trD = add(exx, eyy);
     double dsjxx = add(mul(lambda, trD), mul(twoG, exx));
     double dsjxy = mul(twoG, exy);
@@ -293,7 +295,7 @@ __device__ __forceinline__ void g_local_mu2_reverse(const Elastic &el, const Mu2
 {
     const double G = el.G, K = el.K, dt = el.dt, c = 0;
     const double lambda = sub(K, dvd(mul(2.0, G), 3.0));
-    const double twoG = mul(2.0, G);
+    const double twoG = el.twoG;
     double p_t = mul(-0.5, add(sxx, syy));
     double trD = add(exx, eyy);
     double dsjxx = add(mul(lambda, trD), mul(twoG, exx));
@@ -443,7 +445,7 @@ __device__ __forceinline__ void nonlocal_mu2_trial(const Elastic &el, double exx
 {
     const double G = el.G, dt = el.dt;
     const double lambda = el.lambda;   // sub(K, dvd(mul(2, G), 3)), formed on the host with the same roundings
-    const double twoG = mul(2.0, G);
+    const double twoG = el.twoG;
     double trD = add(exx, eyy);
     double dsjxx = add(mul(lambda, trD), mul(twoG, exx));
     double dsjxy = mul(twoG, exy);

@@ -2453,6 +2453,7 @@ int mpmg_launch_fluidity(mpmg_ctx *ctx)
 
     mat::Elastic el;
     el.G = ctx->G;
+    el.twoG = 2.0 * ctx->G;
     el.K = ctx->K;
     el.lambda = ctx->lambda;
     el.dt = c.dt;

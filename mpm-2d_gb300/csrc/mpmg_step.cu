@@ -110,14 +110,14 @@ __global__ void __launch_bounds__(128) p2g_cells_kernel(
     if (k0 == k1) return;
     mpmg_order_segment(slots, perm, nullptr, k0, k1);   // ascending particle index, as the reference's lists
     const int ci = e % g.Ex, cj = e / g.Ex;
-    const double xn = ci * g.h, yn = cj * g.h;   // node_number_to_coords (element.c:10-19)
+    const double cx = ci, cy = cj;   // the element's column and row (element.c:10-19)
     // moments [A, X, Y, Z] of m, m vx, m vy; stress-term moments
     double mm[4] = {0, 0, 0, 0}, mx[4] = {0, 0, 0, 0}, my[4] = {0, 0, 0, 0};
     double P0 = 0, Py0 = 0, P1 = 0, Px1 = 0, Py1 = 0, P2 = 0, Px2 = 0;
     for (int k = k0; k < k1; k++) {
         const int i = (int)perm[k];
-        const double xl = mpmg_local_coord(x[i], xn, g.inv_h);
-        const double yl = mpmg_local_coord(y[i], yn, g.inv_h);
+        const double xl = mpmg_local_coord_fma(x[i], cx, g.inv_h);
+        const double yl = mpmg_local_coord_fma(y[i], cy, g.inv_h);
         const double xy = xl * yl;
         const double pm = m[i];
         const double pmx = vx[i] * pm, pmy = vy[i] * pm;
@@ -323,8 +323,8 @@ __global__ void __launch_bounds__(256) g2p_kernel(G2PArgs A)
         xl = A.xl_out[i];
         yl = A.yl_out[i];
     } else {
-        xl = mpmg_local_coord(A.x[i], ci * g.h, g.inv_h);
-        yl = mpmg_local_coord(A.y[i], cj * g.h, g.inv_h);
+        xl = mpmg_local_coord_fma(A.x[i], (double)ci, g.inv_h);
+        yl = mpmg_local_coord_fma(A.y[i], (double)cj, g.inv_h);
     }
     const ShapeFns f = shape(xl, yl, g.inv_h);
     const double dt = A.dt;
@@ -627,6 +627,7 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.n = (int)ctx->np;
     A.dt = c.dt;
     A.el.G = ctx->G;
+    A.el.twoG = 2.0 * ctx->G;
     A.el.K = ctx->K;
     A.el.lambda = ctx->lambda;
     A.el.dt = c.dt;
@@ -648,6 +649,7 @@ G2PArgs make_g2p_args(mpmg_ctx *ctx)
     A.mu2.AAdd = ((A.mu2.A * A.mu2.A) * A.mu2.grains_d) * A.mu2.grains_d;
     A.mu2.inv_AAdd = 1.0 / A.mu2.AAdd;
     A.mu2.alpha_c = (((ctx->G * A.mu2.I0) * c.dt) / A.mu2.grains_d) / sqrt(A.mu2.grains_rho);
+    A.mu2.GI0dt = (ctx->G * A.mu2.I0) * c.dt;
     A.nl.E = c.mp[MPMG_MP_E];
     A.nl.nu = c.mp[MPMG_MP_NU];
     A.nl.mu_s = c.mp[MPMG_MP_MU_S];
