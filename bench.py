@@ -116,11 +116,11 @@ MIXED_G2P_SURVEY_BYTES = (104, 0, 16)
 # FP64 work per particle of the FP64 G2P + g_local_mu2 after the warm-up
 # steps, from one ncu capture of g2p_kernel<1,0> (the same fill at 256^2
 # elements, 262 144 particles, step 27; per-particle counts do not depend on
-# the size): operations (DADD + DMUL + 2 DFMA: 41.6 + 58.5 + 2 x 75.0) and
+# the size): operations (DADD + DMUL + 2 DFMA: 48.4 + 48.4 + 2 x 54.6) and
 # FP64 pipe instructions (pipe-active cycles x 2 per SM, compares and
 # conversions included).
-G2P64_FLOPS_PER_PARTICLE = 250.1
-G2P64_PIPE_INSTR_PER_PARTICLE = 224.4
+G2P64_FLOPS_PER_PARTICLE = 206.0
+G2P64_PIPE_INSTR_PER_PARTICLE = 210.8
 
 # DRAM bytes (read + write) of one mx_g2p_kernel launch on this workload from
 # one ncu capture: 80.8 MB read + 17.0 MB written; writes still in L2 at the
