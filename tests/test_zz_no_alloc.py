@@ -129,6 +129,41 @@ def test_noalloc_sort_in_place_keys():
     np.testing.assert_array_equal(start.cpu().numpy(), want[2])
 
 
+def test_noalloc_sort_captured_in_a_cuda_graph():
+    """A call captured into a CUDA graph, after one warm-up call outside
+    capture (which looks the scratch address up), and replayed twice over
+    new keys in the same input buffer: each replay equals numpy's stable
+    argsort.  Only kernel launches go into the graph."""
+    torch = pytest.importorskip("torch")
+    fn = _entry()
+    rng = np.random.default_rng(5)
+    ne, n = 5000, 60000
+    d_keys = torch.empty(n, dtype=torch.int32, device="cuda")
+    out_keys = torch.empty(n, dtype=torch.int32, device="cuda")
+    out_perm = torch.empty(n, dtype=torch.int32, device="cuda")
+    out_start = torch.empty(ne + 1, dtype=torch.int32, device="cuda")
+    args = lambda s: (d_keys.data_ptr(), n, ne, out_keys.data_ptr(), out_perm.data_ptr(),
+                      out_start.data_ptr(), s)
+    d_keys.copy_(torch.from_numpy(rng.integers(0, ne, size=n).astype(np.int32)))
+    assert fn(*args(torch.cuda.current_stream().cuda_stream)) == 0, mpm2d.lib().mpmg_last_error().decode()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rc = fn(*args(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, mpm2d.lib().mpmg_last_error().decode()
+    for replay in range(2):
+        keys = rng.integers(-2, ne + 3, size=n).astype(np.int32)
+        keys[: n // 3] = np.sort(keys[: n // 3])
+        d_keys.copy_(torch.from_numpy(keys))
+        for t in (out_keys, out_perm, out_start):
+            t.fill_(-7)
+        graph.replay()
+        torch.cuda.synchronize()
+        want = _expected(keys, ne)
+        for g, w, name in zip((out_keys, out_perm, out_start), want, ("sorted keys", "perm", "cell start")):
+            np.testing.assert_array_equal(g.cpu().numpy(), w, err_msg="%s, replay %d" % (name, replay))
+
+
 def test_noalloc_sort_rejects_bad_sizes():
     torch = pytest.importorskip("torch")
     fn = _entry()
