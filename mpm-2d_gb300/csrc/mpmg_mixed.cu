@@ -221,7 +221,7 @@ __device__ __forceinline__ void nonlocal_mu2_bulk_f(const MatF &p, float m, floa
     if (dense != 0.0f && p_tr > 0.0f) {
         const double pr = p_tr, tau = tau_tr;
         const double S0 = (double)p.mu_s * pr;
-        double tau_tau = tau, scale = 1.0;
+        double tau_tau = tau;
         if (tau > S0) {
             const double S2 = (double)p.mu_2 * pr;
             const double alpha = (double)p.alpha_coef * sqrt(pr * (double)p.inv_grains_rho);
@@ -229,9 +229,9 @@ __device__ __forceinline__ void nonlocal_mu2_bulk_f(const MatF &p, float m, floa
             const double H = S2 * tau + S0 * alpha;
             const double disc = sqrt(B * B - 4.0 * H);
             tau_tau = (B > 0.0) ? (-B - disc) * 0.5 : (2.0 * H) / (-B + disc);
-            scale = tau_tau / tau;
+            // (1 / scale - 1) with scale = tau_tau / tau, as one quotient
+            gf_local = (float)(pr * (double)p.inv_G_dt * ((tau - tau_tau) / tau_tau));
         }
-        gf_local = (float)(pr * (double)p.inv_G_dt * (1.0 / scale - 1.0));
         xisq_inv = (float)(fabs(tau_tau / pr - (double)p.mu_s) * (double)p.inv_A2d2);
     }
 }

@@ -967,15 +967,18 @@ inline size_t pcg_tile_smem(int C, int Nx)
 // recurrence.  Each iteration needs one grid barrier, for the four inner
 // products.
 //
-// Where the levels live.  A level of more than 2048 nodes is spread over all
-// blocks in contiguous node ranges; the coarser levels are held whole by
-// block 0, whose threads meet at block barriers between phases.
+// Where the levels live.  A level of more than 2048 nodes is spread over the
+// blocks in contiguous node ranges (level 0 over blocks 1 .. n - 1, so that
+// block 0 has no level-0 work); the coarser levels are held whole by block
+// 0, whose threads meet at block barriers between phases.  All blocks
+// restrict into the first held level and block 0 stages it.
 //
 // Synchronisation between blocks.  Each phase writes its level vector to
 // global memory as 64-bit words: an FP32 value plus a 32-bit tag that names
-// the V-cycle.  A consumer loads the words it needs; if some carry an older
-// tag, it polls one of them with a growing pause and, once that one is
-// current, loads the rest again together.  A word is stored with one
+// the V-cycle.  A phase stages the words it needs from other blocks (a halo
+// or a band of rows) into shared memory once; if some carry an older tag, a
+// lane polls one of them with a pause after each stale answer and, once that
+// one is current, the warp loads its stale words again together.  A word is stored with one
 // single-copy-atomic 64-bit store, so its value and tag arrive together,
 // with no fences or flags.
 //   * Each phase vector is written once per V-cycle, and the outer grid
