@@ -443,7 +443,7 @@ __device__ __forceinline__ void nonlocal_mu2_trial(const Elastic &el, double exx
                                                    double syy, double &p_tr, double &t0xx,
                                                    double &t0xy, double &t0yy, double &tau_tr)
 {
-    const double G = el.G, dt = el.dt;
+    const double dt = el.dt;
     const double lambda = el.lambda;   // sub(K, dvd(mul(2, G), 3)), formed on the host with the same roundings
     const double twoG = el.twoG;
     double trD = add(exx, eyy);

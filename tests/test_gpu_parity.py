@@ -11,7 +11,9 @@ Tolerances (FP64 everywhere):
   * multi-step trajectories: <= 1e-9 relative after up to 400 steps (rounding
     differences of the summation order compound slowly);
   * nonlocal fluidity: the GPU solves to a 1e-12 relative residual (PCG) where
-    the reference factorises directly; <= 1e-8 relative in stress.
+    the reference factorises directly; <= 1e-10 relative in stress and in the
+    nodal fluidity carried in state[3] over the recorded trajectories, and
+    <= 1e-9 for one step from the unstressed silo's recorded states.
 """
 import os
 
@@ -269,7 +271,9 @@ def test_gpu_one_step_vs_oracle_from_checkpoint(case):
         orc.set("by", np.full(len(st["x"]), -9.8 * (t / 0.1) if t < 0.1 else -9.8))
         sim.step(1)
         orc.step(1)
-        tol = ONE_STEP_TOL if "nonlocal" not in case else 1e-8
+        # the nonlocal silo from the unstressed fill, whose dense flags switch on
+        # the sign of p ~ 0: 4.1e-10 in stress, the same with the solve to 1e-12
+        tol = ONE_STEP_TOL if "nonlocal" not in case else 1e-9
         for f in ("x", "y", "vx", "vy", "v", "sxx", "sxy", "syy"):
             e = field_err(sim.get(f), orc.get, f)
             assert e <= tol, (case, step, f, e)
@@ -322,8 +326,8 @@ def test_gpu_nonlocal_mu2_vs_golden():
         assert rc == 0 and resid <= 1e-12
         want = lambda f, c=c: d["s%d_%s" % (c, f)]
         for f in ("sxx", "sxy", "syy", "x", "y", "vx", "vy"):
-            assert field_err(sim.get(f), want, f) <= 1e-8, (c, f, field_err(sim.get(f), want, f))
-        assert rel_err(sim.get("state3"), d["s%d_state3" % c]) <= 1e-7, c
+            assert field_err(sim.get(f), want, f) <= ONE_STEP_TOL, (c, f, field_err(sim.get(f), want, f))
+        assert rel_err(sim.get("state3"), d["s%d_state3" % c]) <= ONE_STEP_TOL, c
 
 
 @pytest.mark.parametrize("case", ["nonlocal_silo", "nonlocal_avg_silo"])
@@ -338,8 +342,8 @@ def test_gpu_nonlocal_variant_vs_golden(case):
         done = c
         want = lambda f, c=c: d["s%d_%s" % (c, f)]
         for f in ("sxx", "sxy", "syy", "x", "y"):
-            assert field_err(sim.get(f), want, f) <= 1e-8, (case, c, f, field_err(sim.get(f), want, f))
-        assert rel_err(sim.get("state3"), want("state3")) <= 1e-7, (case, c)
+            assert field_err(sim.get(f), want, f) <= ONE_STEP_TOL, (case, c, f, field_err(sim.get(f), want, f))
+        assert rel_err(sim.get("state3"), want("state3")) <= ONE_STEP_TOL, (case, c)
 
 
 def test_gpu_deterministic():
