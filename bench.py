@@ -76,7 +76,7 @@ FP64_BYTES = {
     "grid": (0, 160, 40),
     "g2p": (13 * 8 + 8 + 13 * 8, 0, 32),
 }
-# The survey's compulsory bytes of the FP64 step (each persistent field read
+# The compulsory bytes of the FP64 step (each persistent field read
 # and written once, sort scratch and transients excluded): 216 B per
 # particle-step for g_local_mu2 and 80 B per node-step.
 FP64_STEP_SURVEY_BYTES = (216, 0, 80)
@@ -98,7 +98,7 @@ MIXED_BYTES = {
     "p2g": (40, 0, 24),
     "g2p": (128, 0, 16),
 }
-# The survey's compulsory bytes of the mixed step, which exclude perm, key and
+# The compulsory bytes of the mixed step, which exclude perm, key and
 # particle index (index and sort scratch): 112 B per particle-step for
 # g_local_mu2, 64 B per node-step; of those the G2P moves the particle state
 # (13 floats read, 13 written = 104 B) and the node gathers (16 B per node).
@@ -597,7 +597,7 @@ def run_gpu(args):
         bsim.close()
         value_b = nb * bsteps * world / slowest(msb / 1e3)
         # algorithmic bytes of a batched step: the builder's accounting of the
-        # unfused kernels a batch runs, and the survey's compulsory bytes
+        # unfused kernels a batch runs, and the compulsory bytes
         bn = nb
         be = int(sum((sc["Nx"] - 1) * (sc["Ny"] - 1) for sc in ens))
         bnn = int(sum(sc["Nx"] * sc["Ny"] for sc in ens))
